@@ -1,0 +1,1604 @@
+// Oracle (test infrastructure only): lattice state, FourBody potential, moves.
+//
+// CPU restatement of the reference's staple-move path, used by tests/, by
+// smoke() and by bench.py's CPU-baseline leg to check and time the CUDA
+// engine.  It is never linked into the engine.  Each member cites the
+// reference function it restates.  The traversal order of the FourBody terms
+// and of every energy accumulation follows the reference so that energies
+// agree bit for bit and every random draw happens at the same point.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "oracle_philox.hpp"
+#include "oracle_thermo.hpp"
+
+namespace oracle {
+
+enum Occ : int { UNASSIGNED = 0, UNBOUND = 1, BOUND = 2, MISBOUND = 3 };
+
+struct V3 {
+    int x {0}, y {0}, z {0};
+    V3() = default;
+    V3(int a, int b, int c): x(a), y(b), z(c) {}
+    V3 operator+(const V3& o) const { return {x + o.x, y + o.y, z + o.z}; }
+    V3 operator-(const V3& o) const { return {x - o.x, y - o.y, z - o.z}; }
+    V3 operator-() const { return {-x, -y, -z}; }
+    bool operator==(const V3& o) const { return x == o.x && y == o.y && z == o.z; }
+    bool operator!=(const V3& o) const { return !(*this == o); }
+    V3 absv() const { return {std::abs(x), std::abs(y), std::abs(z)}; }
+    int abssum() const { return std::abs(x) + std::abs(y) + std::abs(z); }
+};
+
+// Order matters: random index -> direction (include/.../utility.hpp:156-162).
+static const V3 kUnit[6] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+
+// VectorThree::rotate_half (src/utility.cpp:68)
+inline V3 rotate_half(V3 v, V3 axis) {
+    axis = axis.absv();
+    if (axis == V3(1, 0, 0)) { v.y = -v.y; v.z = -v.z; }
+    else if (axis == V3(0, 1, 0)) { v.x = -v.x; v.z = -v.z; }
+    else if (axis == V3(0, 0, 1)) { v.x = -v.x; v.y = -v.y; }
+    return v;
+}
+
+// VectorThree::rotate(axis, turns) (src/utility.cpp:102)
+inline V3 rotate_quarter(V3 v, V3 axis, int turns) {
+    if (turns % 2 == 0) return rotate_half(v, axis);
+    bool odd_even = (turns - 1) / 2 % 2 == 0;
+    int dir = (turns >= 0 && odd_even) ? 1 : -1;
+    V3 a = axis.absv();
+    if (axis != a) dir *= -1;
+    if (a == V3(1, 0, 0)) { std::swap(v.y, v.z); v.y *= -dir; v.z *= dir; }
+    else if (a == V3(0, 1, 0)) { std::swap(v.x, v.z); v.x *= -dir; v.z *= dir; }
+    else if (a == V3(0, 0, 1)) { std::swap(v.x, v.y); v.x *= -dir; v.y *= dir; }
+    return v;
+}
+
+inline uint64_t pos_key(const V3& p) {
+    return ((uint64_t)(uint32_t)(p.x + (1 << 20)) << 42) | ((uint64_t)(uint32_t)(p.y + (1 << 20)) << 21) |
+           (uint64_t)(uint32_t)(p.z + (1 << 20));
+}
+
+struct Dom {
+    int c, cident, d, dident, clen;
+    int fwd {-1}, bwd {-1};
+    V3 pos, ore;
+    int state {UNASSIGNED};
+    int bound {-1};
+};
+
+struct Delta {
+    double e {0};
+    int stacked {0};
+};
+
+struct SiteRec {
+    int occ;
+    int unbound_dom;   // valid when occ == UNBOUND
+};
+
+// ------------------------------------------------------- order params ----
+enum OpKind { OP_NUMSTAPLES, OP_NUMSTAPLESTYPE, OP_STAPLETYPEFULLYBOUND, OP_NUMBOUND, OP_NUMMISBOUND,
+              OP_NUMSTACKED, OP_NUMLINEARHELICES, OP_NUMSTACKEDJUNCTS, OP_SUM };
+
+struct OpRec {
+    OpKind kind;
+    std::string tag;
+    int arg {0};
+    std::vector<int> parts;   // Sum
+    int param {0};
+    bool defined {true};
+};
+
+enum BiasKind { B_LINEARSTEPWELL, B_SQUAREWELL, B_GRID, B_HARMONIC };
+
+struct BiasRec {
+    BiasKind kind;
+    std::string tag;
+    std::vector<int> ops;
+    int min_op {0}, max_op {0};
+    double well_bias {0}, min_bias {0}, slope {0}, outside_bias {0};
+    double k {0}, centre {0};
+    std::vector<double> grid;   // 1-D grid over op value 0..grid.size()-1
+    bool grid_set {false};
+    double off_grid {0};
+    double bias {0};
+};
+
+enum MoveKind { MV_ORIENTATION = 0, MV_MET_EXCHANGE = 1, MV_MET_REGROWTH = 2, MV_CB_REGROWTH = 3 };
+
+struct Config {
+    // chain-type identities, index 0 is the scaffold
+    std::vector<std::vector<int>> identities;
+    bool cyclic {false};
+    bool three_quarter {false};
+    bool misbinding_disallowed {false};
+    bool mean_field {false};
+    double staple_M {1};
+    int max_total_staples {999};
+    int max_type_staples {999};
+    std::vector<int> move_kinds;
+    std::vector<double> move_cum;
+    std::vector<double> exchange_mults;
+    bool adaptive_exchange {false};
+    bool allow_nonsensical_ps {false};
+    double bias_mult {1};
+    int centering_freq {0};
+    int centering_domain {0};
+    int constraint_check_freq {0};
+};
+
+struct ChainInit {
+    int index, identity;
+    std::vector<V3> pos, ore;
+};
+
+class System {
+  public:
+    Config cfg;
+    EnergyTables tab;
+    Stream rng;
+
+    // Bookkeeping (OrigamiSystem members, include/.../origami_system.hpp:175-205)
+    std::vector<Dom> doms;
+    std::vector<int> free_doms;
+    std::vector<std::vector<int>> chains;   // domain ids, m_domains order
+    std::vector<int> chain_index;           // unique chain index per chain
+    std::vector<int> chain_ident;
+    std::vector<std::vector<int>> ident_to_index;
+    std::unordered_map<uint64_t, SiteRec> sites;
+    int num_domains {0}, num_staples {0}, num_bound {0}, num_fully {0}, num_self {0}, num_unassigned {0},
+        num_stacked {0};
+    int current_c_i {0};
+    double energy {0};
+    bool violated {false};
+
+    std::vector<OpRec> ops;
+    std::vector<BiasRec> biases;
+    double move_bias {0};
+
+    // move-loop statistics
+    std::vector<long long> attempts, accepts;
+
+    // ---------------------------------------------------- construction ---
+    void init(const Config& c, const EnergyTables& t, const std::vector<ChainInit>& config) {
+        cfg = c;
+        tab = t;
+        ident_to_index.assign(cfg.identities.size(), {});
+        attempts.assign(cfg.move_kinds.size(), 0);
+        accepts.assign(cfg.move_kinds.size(), 0);
+        // initialize_scaffold (src/origami_system.cpp:680)
+        add_chain_with_index(config[0].identity, config[0].index);
+        num_staples--;
+        if (cfg.cyclic) {
+            auto& sc = chains[0];
+            doms[sc.back()].fwd = sc.front();
+            doms[sc.front()].bwd = sc.back();
+        }
+        // initialize_staples (src/origami_system.cpp:659)
+        for (size_t i = 1; i < config.size(); ++i) add_chain_with_index(config[i].identity, config[i].index);
+        if (cfg.mean_field) energy += (config.size() - 1) * std::log(6);
+        energy += (chains.size() - 1) * tab.init_e;
+        current_c_i = chain_index[0];
+        for (int ci : chain_index) current_c_i = std::max(current_c_i, ci);
+        // set_all_domains(config) (src/origami_system.cpp:588)
+        for (size_t i = 0; i < config.size(); ++i)
+            for (size_t d = 0; d < chains[i].size(); ++d) {
+                doms[chains[i][d]].pos = config[i].pos[d];
+                doms[chains[i][d]].ore = config[i].ore[d];
+            }
+        set_all_current();
+    }
+
+    void set_all_current() {
+        for (size_t i = 0; i < chains.size(); ++i)
+            for (int id : chains[i]) {
+                set_domain_config(id, doms[id].pos, doms[id].ore);
+                if (violated) throw std::runtime_error("Constaints in violation after move complete");
+            }
+        for (auto& ch : chains)
+            for (int id : ch) {
+                int nx = next(id, 1);
+                if (nx >= 0 && (doms[nx].pos - doms[id].pos).abssum() != 1)
+                    throw std::runtime_error("Contiguous domains not on adjacent sites");
+            }
+    }
+
+    // ------------------------------------------------------ accessors ---
+    int next(int id, int incr) const {   // Domain::operator+ (src/domain.cpp:9)
+        while (id >= 0 && incr > 0) { id = doms[id].fwd; --incr; }
+        while (id >= 0 && incr < 0) { id = doms[id].bwd; ++incr; }
+        return id;
+    }
+    int chain_pos(int c_i) const {
+        for (size_t i = 0; i < chain_index.size(); ++i)
+            if (chain_index[i] == c_i) return (int)i;
+        throw std::runtime_error("no chain with index " + std::to_string(c_i));
+    }
+    const std::vector<int>& get_chain(int c_i) const { return chains[chain_pos(c_i)]; }
+    int occupancy(const V3& p) const {
+        auto it = sites.find(pos_key(p));
+        return it == sites.end() ? UNASSIGNED : it->second.occ;
+    }
+    int unbound_at(const V3& p) const { return sites.at(pos_key(p)).unbound_dom; }
+    int num_staples_of_ident(int t) const { return (int)ident_to_index[t].size(); }
+    double hyb(int i, int j) const { return tab.hyb_e[tab.at(doms[i].dident, doms[j].dident)]; }
+    double hyb_h(int i, int j) const { return tab.hyb_h[tab.at(doms[i].dident, doms[j].dident)]; }
+    double hyb_s(int i, int j) const { return tab.hyb_s[tab.at(doms[i].dident, doms[j].dident)]; }
+    double stack(int i, int j) const { return tab.stack_e[tab.at(doms[i].dident, doms[j].dident)]; }
+
+    // --------------------------------------------------- chain add/del ---
+    int add_chain_with_index(int ident, int c_i) {   // src/origami_system.cpp:402
+        if (ident < 0 || ident >= (int)cfg.identities.size()) throw std::runtime_error("bad chain identity");
+        ident_to_index[ident].push_back(c_i);
+        chain_index.push_back(c_i);
+        chain_ident.push_back(ident);
+        const auto& ids = cfg.identities[ident];
+        int len = (int)ids.size();
+        chains.push_back({});
+        num_staples++;
+        int prev = -1;
+        for (int d = 0; d < len; ++d) {
+            int id;
+            if (!free_doms.empty()) {
+                id = free_doms.back();
+                free_doms.pop_back();
+            }
+            else {
+                id = (int)doms.size();
+                doms.push_back({});
+            }
+            Dom dm {c_i, ident, d, ids[d], len};
+            dm.bwd = prev;
+            dm.fwd = -1;
+            doms[id] = dm;
+            if (prev >= 0) doms[prev].fwd = id;
+            chains.back().push_back(id);
+            prev = id;
+            num_domains++;
+            num_unassigned++;
+        }
+        return c_i;
+    }
+    int add_chain(int ident) {   // src/origami_system.cpp:387
+        current_c_i += 1;
+        if (cfg.mean_field) energy += std::log(6);
+        energy += tab.init_e;
+        return add_chain_with_index(ident, current_c_i);
+    }
+    void delete_chain(int c_i) {   // src/origami_system.cpp:445
+        int k = chain_pos(c_i);
+        int ident = chain_ident[k];
+        auto& lst = ident_to_index[ident];
+        lst.erase(std::find(lst.begin(), lst.end(), c_i));
+        chain_index.erase(chain_index.begin() + k);
+        chain_ident.erase(chain_ident.begin() + k);
+        num_domains -= (int)chains[k].size();
+        num_staples--;
+        for (int id : chains[k]) {
+            free_doms.push_back(id);
+            num_unassigned--;
+        }
+        chains.erase(chains.begin() + k);
+        if (cfg.mean_field) energy -= std::log(6);
+        energy -= tab.init_e;
+    }
+
+    // ------------------------------------------------ state transitions ---
+    // update_occupancies (src/origami_system.cpp:770)
+    void update_occupancies(int i, const V3& p) {
+        uint64_t key = pos_key(p);
+        auto it = sites.find(key);
+        int occ = it == sites.end() ? UNASSIGNED : it->second.occ;
+        if (occ == UNBOUND) {
+            int j = it->second.unbound_dom;
+            num_bound += 1;
+            int ns;
+            if (doms[i].dident == -doms[j].dident) {
+                ns = BOUND;
+                num_fully += 1;
+            }
+            else {
+                if (doms[i].c == doms[j].c) num_self += 1;
+                ns = MISBOUND;
+            }
+            doms[i].state = ns;
+            doms[j].state = ns;
+            it->second = {ns, -1};
+            doms[j].bound = i;
+            doms[i].bound = j;
+        }
+        else if (occ == UNASSIGNED) {
+            doms[i].state = UNBOUND;
+            sites[key] = {UNBOUND, i};
+        }
+        else {
+            throw std::runtime_error("Trying to bind to an already bound domain");
+        }
+    }
+
+    // unassign_bound_domain (src/origami_system.cpp:741)
+    double unassign_bound(int i) {
+        int j = doms[i].bound;
+        double de = -hyb(i, j);
+        doms[i].bound = -1;
+        doms[j].bound = -1;
+        doms[i].state = UNASSIGNED;
+        sites[pos_key(doms[i].pos)] = {UNBOUND, j};
+        doms[j].state = UNBOUND;
+        return de;
+    }
+
+    // internal_unassign_domain (src/origami_system.cpp:695)
+    Delta internal_unassign(int i) {
+        int occ = doms[i].state;
+        int j = doms[i].bound;
+        Delta dc;
+        switch (occ) {
+        case BOUND:
+            num_fully -= 1;
+            num_bound -= 1;
+            dc = check_stacking(i, j);
+            dc.e *= -1;
+            dc.stacked *= -1;
+            dc.e += unassign_bound(i);
+            break;
+        case MISBOUND:
+            num_bound -= 1;
+            if (doms[j].c == doms[i].c) num_self -= 1;
+            dc.e += unassign_bound(i);
+            break;
+        case UNBOUND:
+            sites.erase(pos_key(doms[i].pos));
+            doms[i].state = UNASSIGNED;
+            break;
+        case UNASSIGNED:
+            num_unassigned--;
+            break;
+        }
+        if (cfg.mean_field && occ == BOUND) {
+            if (num_fully == 0) dc.e -= 2 * std::log(6);
+            else if (num_fully == 1) dc.e -= std::log(3);
+        }
+        return dc;
+    }
+
+    // internal_check_domain_constraints (src/origami_system.cpp:828)
+    Delta internal_check(int i, const V3& p, const V3& o) {
+        int occ = occupancy(p);
+        Delta dc;
+        switch (occ) {
+        case BOUND:
+        case MISBOUND:
+            violated = true;
+            num_unassigned++;
+            break;
+        case UNBOUND:
+            doms[i].pos = p;
+            doms[i].ore = o;
+            update_occupancies(i, p);
+            dc = bind_domain(i);
+            violated = pot_violated;
+            break;
+        case UNASSIGNED:
+            doms[i].pos = p;
+            doms[i].ore = o;
+            update_occupancies(i, p);
+            break;
+        }
+        if (cfg.mean_field && !violated && doms[i].state == BOUND) {
+            if (num_fully == 1) dc.e += 2 * std::log(6);
+            else if (num_fully == 2) dc.e += std::log(3);
+        }
+        return dc;
+    }
+
+    // set_domain_config (src/origami_system.cpp:517)
+    double set_domain_config(int i, V3 p, V3 o) {
+        if (doms[i].state != UNASSIGNED) throw std::runtime_error("Trying to set an already assigned domain");
+        Delta dc = internal_check(i, p, o);
+        if (violated) {
+            internal_unassign(i);
+        }
+        else {
+            energy += dc.e;
+            num_stacked += dc.stacked;
+            num_unassigned--;
+        }
+        return dc.e;
+    }
+
+    // set_checked_domain_config (src/origami_system.cpp:478)
+    double set_checked(int i, V3 p, V3 o) {
+        doms[i].pos = p;
+        doms[i].ore = o;
+        update_occupancies(i, p);
+        double de = 0;
+        if (doms[i].state == MISBOUND) {
+            de += hyb(i, doms[i].bound);
+        }
+        else if (doms[i].state == BOUND) {
+            de += hyb(i, doms[i].bound);
+            Delta dc = check_stacking(i, doms[i].bound);
+            de += dc.e;
+            num_stacked += dc.stacked;
+        }
+        if (cfg.mean_field && doms[i].state == BOUND) {
+            if (num_fully == 1) de += 2 * std::log(6);
+            else if (num_fully == 2) de += std::log(3);
+        }
+        energy += de;
+        num_unassigned--;
+        return de;
+    }
+
+    // unassign_domain (src/origami_system.cpp:375)
+    double unassign_domain(int i) {
+        Delta dc = internal_unassign(i);
+        energy += dc.e;
+        num_stacked += dc.stacked;
+        num_unassigned++;
+        return dc.e;
+    }
+
+    // check_domain_constraints (src/origami_system.cpp:343)
+    double check_domain_constraints(int i, V3 p, V3 o) {
+        Delta dc = internal_check(i, p, o);
+        internal_unassign(i);
+        return dc.e;
+    }
+
+    // set_domain_orientation (src/origami_system.cpp:543)
+    void set_domain_orientation(int i, V3 o) {
+        if (doms[i].state == BOUND) violated = true;
+        else doms[i].ore = o;
+    }
+
+    // center (src/origami_system.cpp:553)
+    void center(int cd) {
+        V3 ref = doms[chains[0][cd]].pos;
+        std::unordered_map<uint64_t, SiteRec> ns;
+        for (auto& ch : chains)
+            for (int id : ch) {
+                V3 np = doms[id].pos - ref;
+                auto it = sites.find(pos_key(doms[id].pos));
+                if (it != sites.end()) ns[pos_key(np)] = it->second;
+                else ns[pos_key(np)] = {UNASSIGNED, -1};
+                doms[id].pos = np;
+            }
+        sites.clear();
+        for (auto& kv : ns)
+            if (kv.second.occ != UNASSIGNED) sites.insert(kv);
+    }
+
+    // check_all_constraints (src/origami_system.cpp:267)
+    void check_all_constraints() {
+        if (num_unassigned != 0) throw std::runtime_error("Number of unassigned domains is no zero on constraint check");
+        for (size_t c = 0; c < chains.size(); ++c)
+            for (int id : chains[c]) {
+                if (doms[id].state == UNASSIGNED) throw std::runtime_error("Domain unassigned after move complete");
+                unassign_domain(id);
+            }
+        if (cfg.mean_field) energy -= (chains.size() - 1) * std::log(6);
+        energy -= (chains.size() - 1) * tab.init_e;
+        if (num_stacked != 0) {
+            int sp = num_stacked;
+            set_all_current();
+            throw std::runtime_error("Stack count inconsistency: " + std::to_string(sp));
+        }
+        double eps = 0.000001;
+        if (energy < -eps || energy > eps) {
+            double e = energy;
+            set_all_current();
+            throw std::runtime_error("System energy inconsistency: " + std::to_string(e));
+        }
+        energy = 0;
+        set_all_current();
+        if (cfg.mean_field) energy += (chains.size() - 1) * std::log(6);
+        energy += (chains.size() - 1) * tab.init_e;
+    }
+
+    // update_energy (src/origami_system.cpp:808), after a table change
+    void recompute_energy() {
+        for (size_t c = 0; c < chains.size(); ++c)
+            for (int id : chains[c]) unassign_domain(id);
+        energy = 0;
+        if (cfg.mean_field) energy += (chains.size() - 1) * std::log(6);
+        energy += (chains.size() - 1) * tab.init_e;
+        set_all_current();
+    }
+
+    // update_enthalpy_and_entropy (src/origami_system.cpp:204)
+    void enthalpy_entropy(double& H, double& S, double& stacking) const {
+        H = 0;
+        S = 0;
+        std::set<int> acc;
+        for (auto& ch : chains)
+            for (int id : ch) {
+                int st = doms[id].state;
+                if (st == BOUND || st == MISBOUND) {
+                    if (acc.find(id) == acc.end()) {
+                        int b = doms[id].bound;
+                        H += hyb_h(id, b);
+                        S += hyb_s(id, b);
+                        acc.insert(b);
+                    }
+                }
+            }
+        if (cfg.mean_field) {
+            S -= (chains.size() - 1) * std::log(6);
+            if (num_fully >= 1) S -= 2 * std::log(6);
+            if (num_fully >= 2) S -= std::log(3);
+        }
+        H += (chains.size() - 1) * tab.init_h;
+        S += (chains.size() - 1) * tab.init_s;
+        stacking = energy - (H - S);
+    }
+
+    // ================================================== FourBody potential ===
+    // JunctionBindingPotential, src/origami_potential.cpp:51-934.
+    bool pot_violated {false};
+    Delta pd;   // m_delta_config
+
+    bool exists_bound(int id) const { return id >= 0 && doms[id].state == BOUND; }
+
+    bool twist_ok(int i1, V3 ndr, int i2) const {   // src/domain.cpp:33,69
+        V3 r = cfg.three_quarter ? rotate_quarter(doms[i1].ore, ndr, -1) : rotate_half(doms[i1].ore, ndr);
+        return r == doms[i2].ore;
+    }
+    bool kink_ok(int i1, V3 ndr, int i2) const {   // src/domain.cpp:42,80
+        const V3& o1 = doms[i1].ore;
+        const V3& o2 = doms[i2].ore;
+        if (ndr == -o1) return false;
+        if (ndr == o1) {
+            if (cfg.three_quarter) return !(o1 == o2 || o1 == -o2);
+            return !(o2 == -o1);
+        }
+        if (ndr == o2 || ndr == -o2) return false;
+        return true;
+    }
+    bool junction_ok(int j1, int j2, int j3, int j4, int k1, int k2) const {   // src/domain.cpp:59,99
+        (void)j3;
+        (void)j4;
+        if (!cfg.three_quarter) return true;
+        V3 ndr_k = doms[k2].pos - doms[k1].pos;
+        if (ndr_k == doms[k1].ore) {
+            V3 ndr1 = doms[j2].pos - doms[j1].pos;
+            if (doms[j1].d > doms[j2].d) ndr1 = -ndr1;
+            if (!twist_ok(k1, ndr1, k2)) return false;
+        }
+        return true;
+    }
+    bool doubly_contig(int a, int b) const {   // :51
+        if (doms[a].c != doms[b].c || doms[b].d != doms[a].d + 1) return false;
+        int ba = doms[a].bound, bb = doms[b].bound;
+        if (doms[ba].c != doms[bb].c) return false;
+        return std::abs(doms[bb].d - doms[ba].d) == 1;
+    }
+    bool pair_stacked(int a, int b) const {   // :70
+        if (doms[a].d > doms[b].d) std::swap(a, b);
+        V3 ndr = doms[b].pos - doms[a].pos;
+        if (ndr != doms[a].ore && ndr != -doms[a].ore) return twist_ok(a, ndr, b);
+        return false;
+    }
+    int junction_penalty(int j1, int j2, int j3, int j4, int k1, int k2) const {   // :85
+        V3 ndr_k = doms[k2].pos - doms[k1].pos;
+        if (!(ndr_k == doms[k1].ore)) return 0;
+        V3 n1 = doms[j2].pos - doms[j1].pos;
+        if (doms[j1].d > doms[j2].d) n1 = -n1;
+        V3 n3 = doms[j4].pos - doms[j3].pos;
+        if (doms[j3].d > doms[j4].d) n3 = -n3;
+        if (n1 == n3) return 2;
+        if (n1 == -n3) return 0;
+        return 1;
+    }
+    void triplet_single(int h1, int h2, int h3) {   // :158
+        V3 n1 = doms[h2].pos - doms[h1].pos;
+        if (n1 == doms[h1].ore) return;
+        V3 n2 = doms[h3].pos - doms[h2].pos;
+        if (n1 != n2) {
+            pd.e -= stack(h2, h3);
+            pd.stacked -= 1;
+        }
+    }
+    void triplet_double(int h1, int h2, int h3) {   // :181
+        V3 n1 = doms[h2].pos - doms[h1].pos;
+        V3 n2 = doms[h3].pos - doms[h2].pos;
+        if (n1 != n2) {
+            pd.e -= stack(h1, h2) / 2;
+            pd.e -= stack(h2, h3) / 2;
+            pd.stacked -= 1;
+        }
+    }
+    void triply_contig_helix(int h1, int h2, int h3) {   // :200
+        V3 n1 = doms[h2].pos - doms[h1].pos;
+        V3 n2 = doms[h3].pos - doms[h2].pos;
+        if (n1 != n2) pot_violated = true;
+    }
+
+    void stacking_and_steric(int i, int j) {   // :212
+        int jj = 0;
+        for (int cd : {i, j}) {
+            constraints_around(cd, jj);
+            if (pot_violated) return;
+            jj++;
+        }
+        central_triplets(i, j);
+    }
+
+    void constraints_around(int cd, int jj) {   // :231
+        for (int k : {-1, 0}) {
+            int c1 = next(cd, k);
+            int c2 = next(cd, k + 1);
+            if (!(exists_bound(c1) && exists_bound(c2))) continue;
+            int b1 = doms[c1].bound, b2 = doms[c2].bound;
+            if (doms[b1].c == doms[b2].c) {
+                if (doms[b1].d == doms[b2].d - 1) doubly_contig_helix_pair(c1, c2, k, jj);
+                else if (doms[b1].d == doms[b2].d + 1) doubly_contig_junction_pair(c1, c2, jj);
+                else regular_pair(c1, c2, k);
+            }
+            else {
+                regular_pair(c1, c2, k);
+            }
+            if (pot_violated) return;
+        }
+        int prev = next(cd, -1);
+        int forw = next(cd, 1);
+        if (exists_bound(prev) && exists_bound(forw)) {
+            if (pair_stacked(cd, forw)) {
+                if (pair_stacked(prev, cd)) {
+                    if (doubly_contig(prev, cd) && doubly_contig(cd, forw)) {
+                        triply_contig_helix(prev, cd, forw);
+                        if (pot_violated) return;
+                    }
+                    triplet_double(prev, cd, forw);
+                }
+                else {
+                    triplet_single(prev, cd, forw);
+                }
+            }
+        }
+    }
+
+    void regular_pair(int c1, int c2, int k) {   // :288
+        V3 ndr = doms[c2].pos - doms[c1].pos;
+        if (!kink_ok(c1, ndr, c2)) {
+            pot_violated = true;
+            return;
+        }
+        if (pair_stacked(c1, c2)) {
+            pd.e += stack(c1, c2);
+            pd.stacked += 1;
+            if (k == -1) backward_single_junction(c1, c2);
+            else forward_single_junction(c1, c2);
+        }
+        else {
+            central_single_junction(c1, c2);
+        }
+        if (k == -1) backward_triplets(c1, c2);
+        else forward_triplets(c1, c2);
+    }
+
+    void doubly_contig_helix_pair(int c1, int c2, int k, int jj) {   // :322
+        if (jj == 1) return;
+        V3 ndr = doms[c2].pos - doms[c1].pos;
+        if (ndr == doms[c1].ore || ndr == -doms[c1].ore) {
+            pot_violated = true;
+            return;
+        }
+        if (twist_ok(c1, ndr, c2)) {
+            pd.e += stack(c1, c2);
+            pd.stacked += 1;
+        }
+        else {
+            pot_violated = true;
+            return;
+        }
+        if (k == -1) {
+            backward_triplets(c1, c2);
+            backward_single_junction(c1, c2);
+        }
+        else {
+            forward_triplets(c1, c2);
+            forward_single_junction(c1, c2);
+        }
+    }
+
+    void doubly_contig_junction_pair(int c1, int c2, int jj) {   // :359
+        int k1 = c1, k2 = c2;
+        V3 ndr = doms[k2].pos - doms[k1].pos;
+        if (doms[k1].ore != ndr) {
+            pot_violated = true;
+            return;
+        }
+        if (jj == 1) return;
+        int sel[2][2] = {{next(c1, -1), c1}, {next(doms[c1].bound, 1), doms[c1].bound}};
+        for (auto& s : sel) {
+            int j1 = s[0], j2 = s[1];
+            int j3 = k2, j4 = next(k2, 1);
+            if (exists_bound(j4) && exists_bound(j1)) junction(j1, j2, j3, j4, k1, k2);
+            j3 = doms[k2].bound;
+            j4 = next(j3, -1);
+            if (exists_bound(j4) && exists_bound(j1)) junction(j1, j2, j3, j4, k1, k2);
+        }
+    }
+
+    void junction(int j1, int j2, int j3, int j4, int k1, int k2) {   // :419
+        if (doms[k1].d > doms[k2].d) {
+            std::swap(k1, k2);
+            std::swap(j1, j4);
+            std::swap(j2, j3);
+        }
+        if (!(pair_stacked(j1, j2) && pair_stacked(j3, j4))) return;
+        if (!junction_ok(j1, j2, j3, j4, k1, k2)) {
+            pot_violated = true;
+            return;
+        }
+        int pen = junction_penalty(j1, j2, j3, j4, k1, k2);
+        if (pen == 1) {
+            pd.e -= stack(j1, j2) / 2;
+            pd.e -= stack(j3, j4) / 2;
+            pd.stacked -= 1;
+        }
+        else if (pen == 2) {
+            pd.e -= stack(j1, j2);
+            pd.e -= stack(j3, j4);
+            pd.stacked -= 2;
+        }
+    }
+
+    void backward_triplets(int c1, int c2) {   // :464
+        int h2 = c1, h3 = c2;
+        if (!pair_stacked(h2, h3)) return;
+        int h1 = next(c1, -1);
+        bool h23_dc = doubly_contig(h2, h3);
+        if (exists_bound(h1)) {
+            bool h12_dc = doubly_contig(h1, h2);
+            if (pair_stacked(h1, h2)) {
+                if (h12_dc && h23_dc) {
+                    triply_contig_helix(h1, h2, h3);
+                    if (pot_violated) return;
+                }
+                triplet_double(h1, h2, h3);
+            }
+            else {
+                triplet_single(h1, h2, h3);
+            }
+        }
+        int h2_prev = h1;
+        int b1 = doms[c1].bound;
+        h1 = next(b1, 1);
+        if (exists_bound(h1) && doms[h1].bound != h2_prev && doms[h1].bound != h3) {
+            if (pair_stacked(b1, h1)) triplet_double(h1, h2, h3);
+        }
+        h1 = next(b1, -1);
+        if (exists_bound(h1) && doms[h1].bound != h2_prev && doms[h1].bound != h3) {
+            if (pair_stacked(h1, b1)) triplet_double(h1, h2, h3);
+            else triplet_single(h1, b1, h3);
+        }
+    }
+
+    void forward_triplets(int c1, int c2) {   // :521
+        int h2 = c2, h1 = c1;
+        bool first = pair_stacked(h1, h2);
+        int h3 = next(c2, 1);
+        bool h12_dc = doubly_contig(h1, h2);
+        if (exists_bound(h3)) {
+            bool second = pair_stacked(h2, h3);
+            if (first && second) {
+                bool h23_dc = doubly_contig(h2, h3);
+                if (h12_dc && h23_dc) {
+                    triply_contig_helix(h1, h2, h3);
+                    if (pot_violated) return;
+                }
+                triplet_double(h1, h2, h3);
+            }
+            else if (second) {
+                triplet_single(h1, h2, h3);
+            }
+        }
+        int h2_next = h3;
+        int b2 = doms[c2].bound;
+        h3 = next(b2, 1);
+        if (exists_bound(h3) && doms[h3].bound != h2_next && doms[h3].bound != h1) {
+            if (pair_stacked(b2, h3)) {
+                if (first) triplet_double(h1, h2, h3);
+                else triplet_single(h1, h2, h3);
+            }
+        }
+        h3 = next(b2, -1);
+        if (exists_bound(h3) && doms[h3].bound != h2_next && doms[h3].bound != h1) {
+            if (pair_stacked(h3, b2)) {
+                if (first) triplet_double(h1, h2, h3);
+                else triplet_single(h1, h2, h3);
+            }
+            else if (first) {
+                triplet_single(h3, b2, h1);
+            }
+        }
+    }
+
+    void central_triplets(int i, int j) {   // :587
+        int h1 = next(i, -1);
+        int h2 = i;
+        int h3 = next(j, 1);
+        int h2_next = next(i, 1);
+        if (exists_bound(h1) && exists_bound(h3) && doms[h3].bound != h2_next && !doubly_contig(h1, h2)) {
+            if (pair_stacked(j, h3)) {
+                if (pair_stacked(h1, h2)) triplet_double(h1, h2, h3);
+                else triplet_single(h1, h2, h3);
+            }
+        }
+        h3 = next(j, -1);
+        if (exists_bound(h1) && exists_bound(h3) && doms[h3].bound != h1 && !doubly_contig(h1, h2)) {
+            if (pair_stacked(h1, h2)) {
+                if (pair_stacked(h3, j)) triplet_double(h1, h2, h3);
+                else triplet_single(h3, j, h1);
+            }
+            else if (pair_stacked(h3, j)) {
+                triplet_single(h1, h2, h3);
+            }
+        }
+        h2 = i;
+        h3 = next(i, 1);
+        h1 = next(j, 1);
+        int h2_prev = next(i, -1);
+        if (exists_bound(h1) && exists_bound(h3) && doms[h1].bound != h3 && !doubly_contig(h2, h3)) {
+            if (pair_stacked(j, h1) && pair_stacked(h2, h3)) triplet_double(h1, h2, h3);
+        }
+        h1 = next(j, -1);
+        if (exists_bound(h1) && exists_bound(h3) && doms[h1].bound != h2_prev && !doubly_contig(h2, h3)) {
+            if (pair_stacked(h2, h3)) {
+                if (pair_stacked(h1, j)) triplet_double(h1, h2, h3);
+                else triplet_single(h1, j, h3);
+            }
+        }
+    }
+
+    void backward_single_junction(int c1, int c2) {   // :654
+        int j3 = c1, j4 = c2;
+        int first[3][2];
+        int nf = 0;
+        int j3_bac = doms[j3].bwd;
+        first[nf][0] = j3;
+        first[nf][1] = j3_bac;
+        nf++;
+        int j3_b = doms[j3].bound;
+        int j3_b_for = doms[j3_b].fwd;
+        int j3_b_bac = doms[j3_b].bwd;
+        if (j3_b_for == doms[j4].bound) {
+            first[nf][0] = j3_b; first[nf][1] = j3_b_bac; nf++;
+        }
+        else if (exists_bound(j3_bac) && exists_bound(j3_b_bac) && doms[j3_bac].bound == j3_b_bac) {
+            first[nf][0] = j3_b; first[nf][1] = j3_b_for; nf++;
+        }
+        else if (exists_bound(j3_bac) && exists_bound(j3_b_for) && doms[j3_bac].bound == j3_b_for) {
+            first[nf][0] = j3_b; first[nf][1] = j3_b_bac; nf++;
+        }
+        else {
+            first[nf][0] = j3_b; first[nf][1] = j3_b_for; nf++;
+            first[nf][0] = j3_b; first[nf][1] = j3_b_bac; nf++;
+        }
+        for (int a = 0; a < nf; ++a) {
+            int k2 = first[a][0], k1 = first[a][1];
+            if (!exists_bound(k1)) continue;
+            if (pair_stacked(k1, k2)) continue;
+            int second[3][2];
+            int ns = 0;
+            int dir = doms[k1].d - doms[k2].d;
+            int k1_next = next(k1, dir);
+            second[ns][0] = k1; second[ns][1] = k1_next; ns++;
+            int k1_b = doms[k1].bound;
+            int k1_b_for = doms[k1_b].fwd, k1_b_bac = doms[k1_b].bwd;
+            if (exists_bound(k1_next)) {
+                int kn_b = doms[k1_next].bound;
+                if (k1_b_for != kn_b) { second[ns][0] = k1_b; second[ns][1] = k1_b_for; ns++; }
+                if (k1_b_bac != kn_b) { second[ns][0] = k1_b; second[ns][1] = k1_b_bac; ns++; }
+            }
+            else {
+                second[ns][0] = k1_b; second[ns][1] = k1_b_for; ns++;
+                second[ns][0] = k1_b; second[ns][1] = k1_b_bac; ns++;
+            }
+            for (int b = 0; b < ns; ++b) {
+                int j2 = second[b][0], j1 = second[b][1];
+                if (!exists_bound(j1)) continue;
+                junction(j1, j2, j3, j4, k1, k2);
+            }
+        }
+    }
+
+    void forward_single_junction(int c1, int c2) {   // :750
+        int j1 = c1, j2 = c2;
+        int first[3][2];
+        int nf = 0;
+        int j2_for = doms[j2].fwd;
+        first[nf][0] = j2; first[nf][1] = j2_for; nf++;
+        int j1_b = doms[j1].bound;
+        int j2_b = doms[j2].bound;
+        int j2_b_for = doms[j2_b].fwd, j2_b_bac = doms[j2_b].bwd;
+        if (next(j1_b, 1) == j2_b) {
+            first[nf][0] = j2_b; first[nf][1] = j2_b_for; nf++;
+        }
+        else if (exists_bound(j2_for) && exists_bound(j2_b_bac) && doms[j2_for].bound == j2_b_bac) {
+            first[nf][0] = j2_b; first[nf][1] = j2_b_for; nf++;
+        }
+        else if (exists_bound(j2_for) && exists_bound(j2_b_for) && doms[j2_for].bound == j2_b_for) {
+            first[nf][0] = j2_b; first[nf][1] = j2_b_bac; nf++;
+        }
+        else {
+            first[nf][0] = j2_b; first[nf][1] = j2_b_for; nf++;
+            first[nf][0] = j2_b; first[nf][1] = j2_b_bac; nf++;
+        }
+        for (int a = 0; a < nf; ++a) {
+            int k1 = first[a][0], k2 = first[a][1];
+            if (!exists_bound(k2)) continue;
+            if (pair_stacked(k1, k2)) continue;
+            int second[3][2];
+            int ns = 0;
+            int dir = doms[k2].d - doms[k1].d;
+            int k2_next = next(k2, dir);
+            second[ns][0] = k2; second[ns][1] = k2_next; ns++;
+            int k2_b = doms[k2].bound;
+            int k2_b_for = doms[k2_b].fwd, k2_b_bac = doms[k2_b].bwd;
+            if (exists_bound(k2_next)) {
+                int kn_b = doms[k2_next].bound;
+                if (k2_b_for != kn_b) { second[ns][0] = k2_b; second[ns][1] = k2_b_for; ns++; }
+                if (k2_b_bac != kn_b) { second[ns][0] = k2_b; second[ns][1] = k2_b_bac; ns++; }
+            }
+            else {
+                second[ns][0] = k2_b; second[ns][1] = k2_b_for; ns++;
+                second[ns][0] = k2_b; second[ns][1] = k2_b_bac; ns++;
+            }
+            for (int b = 0; b < ns; ++b) {
+                int j3 = second[b][0], j4 = second[b][1];
+                if (!exists_bound(j4)) continue;
+                junction(j1, j2, j3, j4, k1, k2);
+            }
+        }
+    }
+
+    void central_single_junction(int c1, int c2) {   // :846
+        int k1 = c1, k2 = c2;
+        int kb1 = doms[k1].bound, kb2 = doms[k2].bound;
+        if (doms[kb1].c == doms[kb2].c && std::abs(doms[kb1].d - doms[kb2].d) == 1) return;
+        int first[3][2];
+        int nf = 0;
+        int k1_bac = doms[k1].bwd;
+        first[nf][0] = k1; first[nf][1] = k1_bac; nf++;
+        int k1_b = kb1;
+        int k1_b_for = doms[k1_b].fwd, k1_b_bac = doms[k1_b].bwd;
+        if (exists_bound(k1_bac)) {
+            int kbb = doms[k1_bac].bound;
+            if (k1_b_for != kbb) { first[nf][0] = k1_b; first[nf][1] = k1_b_for; nf++; }
+            if (k1_b_bac != kbb) { first[nf][0] = k1_b; first[nf][1] = k1_b_bac; nf++; }
+        }
+        else {
+            first[nf][0] = k1_b; first[nf][1] = k1_b_for; nf++;
+            first[nf][0] = k1_b; first[nf][1] = k1_b_bac; nf++;
+        }
+        for (int a = 0; a < nf; ++a) {
+            int j2 = first[a][0], j1 = first[a][1];
+            if (!exists_bound(j1)) continue;
+            int second[3][2];
+            int ns = 0;
+            int k2_for = doms[k2].fwd;
+            second[ns][0] = k2; second[ns][1] = k2_for; ns++;
+            int k2_b = kb2;
+            int k2_b_for = doms[k2_b].fwd, k2_b_bac = doms[k2_b].bwd;
+            if (exists_bound(k2_for)) {
+                int kfb = doms[k2_for].bound;
+                if (k2_b_for != kfb) { second[ns][0] = k2_b; second[ns][1] = k2_b_for; ns++; }
+                if (k2_b_bac != kfb) { second[ns][0] = k2_b; second[ns][1] = k2_b_bac; ns++; }
+            }
+            else {
+                second[ns][0] = k2_b; second[ns][1] = k2_b_for; ns++;
+                second[ns][0] = k2_b; second[ns][1] = k2_b_bac; ns++;
+            }
+            for (int b = 0; b < ns; ++b) {
+                int j3 = second[b][0], j4 = second[b][1];
+                if (!exists_bound(j4)) continue;
+                junction(j1, j2, j3, j4, k1, k2);
+            }
+        }
+    }
+
+    // BindingPotential::bind_domains (:131) / check_stacking (:149),
+    // OrigamiPotential::bind_domain (:1282), misbinding (:938, :947)
+    Delta bind_domain(int i) {
+        pot_violated = false;
+        int j = doms[i].bound;
+        Delta dc;
+        if (doms[i].dident == -doms[j].dident) {
+            pd = {};
+            if (doms[i].ore != -doms[j].ore) {
+                pot_violated = true;
+                return {};
+            }
+            stacking_and_steric(i, j);
+            if (pot_violated) return {};
+            pd.e += hyb(i, j);
+            dc = pd;
+        }
+        else {
+            if (cfg.misbinding_disallowed) {
+                pot_violated = true;
+                return dc;
+            }
+            pot_violated = true;
+            if (doms[i].ore != -doms[j].ore) return dc;
+            pot_violated = false;
+            dc.e += hyb(i, j);
+        }
+        return dc;
+    }
+    Delta check_stacking(int i, int j) {
+        pd = {};
+        pot_violated = false;
+        stacking_and_steric(i, j);
+        return pd;
+    }
+
+    // =========================================== order params / biases ===
+    // SystemOrderParams::update_move_params (src/order_params.cpp:595)
+    void update_move_params() {
+        for (auto& op : ops) {
+            switch (op.kind) {
+            case OP_NUMSTAPLES: op.param = num_staples; break;
+            case OP_NUMSTAPLESTYPE: op.param = num_staples_of_ident(op.arg); break;
+            case OP_STAPLETYPEFULLYBOUND: {
+                op.param = 0;
+                for (int c_i : ident_to_index[op.arg]) {
+                    bool full = true;
+                    for (int id : get_chain(c_i))
+                        if (doms[id].state != BOUND) { full = false; break; }
+                    if (full) { op.param = 1; break; }
+                }
+                break;
+            }
+            case OP_NUMBOUND: op.param = num_fully; break;
+            case OP_NUMMISBOUND: op.param = num_bound - num_fully; break;
+            case OP_NUMSTACKED: op.param = num_stacked; break;
+            case OP_NUMLINEARHELICES: op.param = 0; break;
+            case OP_NUMSTACKEDJUNCTS: op.param = 0; break;
+            case OP_SUM: {
+                int s = 0;
+                op.defined = true;
+                for (int p : op.parts) {
+                    if (ops[p].defined) s += ops[p].param;
+                    else { op.defined = false; s = op.param; break; }
+                }
+                op.param = s;
+                break;
+            }
+            }
+        }
+    }
+
+    double bias_value(BiasRec& b) {
+        for (int o : b.ops)
+            if (!ops[o].defined) return 0;
+        int x = ops[b.ops[0]].param;
+        switch (b.kind) {
+        case B_LINEARSTEPWELL:   // src/bias_functions.cpp:139
+            if (x < b.min_op) return b.slope * (b.min_op - x - 1) + b.min_bias;
+            if (x > b.max_op) return b.slope * (x - b.max_op - 1) + b.min_bias;
+            return b.well_bias;
+        case B_SQUAREWELL:   // :194
+            if (x < b.min_op || x > b.max_op) return b.outside_bias;
+            return b.well_bias;
+        case B_GRID:   // :242
+            if (x >= 0 && x < (int)b.grid.size() && b.grid_set) return b.grid[x];
+            return b.off_grid;
+        case B_HARMONIC: {
+            double dx = x - b.centre;
+            return 0.5 * b.k * dx * dx;
+        }
+        }
+        return 0;
+    }
+
+    // SystemBiases::calc_move (src/bias_functions.cpp:475)
+    double calc_move() {
+        double diff = 0;
+        for (auto& b : biases) {
+            double prev = b.bias;
+            double nb = bias_value(b);
+            b.bias = nb;
+            diff += nb - prev;
+        }
+        move_bias += diff;
+        return diff * cfg.bias_mult;
+    }
+    double total_bias() const { return move_bias * cfg.bias_mult; }
+
+    void init_biases() {
+        update_move_params();
+        move_bias = 0;
+        for (auto& b : biases) {
+            b.bias = bias_value(b);
+            move_bias += b.bias;
+        }
+    }
+
+    // ================================================================ moves ===
+    // MCMovetype bookkeeping (include/.../movetypes.hpp:141-169)
+    struct Key { int c, d; };
+    std::vector<Key> modified, assigned;
+    std::vector<V3> prev_pos, prev_ore;   // parallel to `modified`
+    std::vector<int> added;
+    bool rejected {false};
+    double modifier {1};
+    double delta_e {0};
+    // CB state (include/.../cb_movetypes.hpp:126-130)
+    double w_bias {1}, w_new_bias {1}, new_modifier {1};
+    bool regrow_old {false};
+    std::vector<Key> old_keys;
+    std::vector<V3> old_pos, old_ore;
+
+    int dom_of(Key k) const { return get_chain(k.c)[k.d]; }
+    Key key_of(int id) const { return {doms[id].c, doms[id].d}; }
+
+    void reset_internal() {   // src/movetypes.cpp:242
+        modified.clear();
+        assigned.clear();
+        prev_pos.clear();
+        prev_ore.clear();
+        added.clear();
+        rejected = false;
+        modifier = 1;
+        delta_e = 0;
+        w_bias = 1;
+        w_new_bias = 1;
+        new_modifier = 1;
+        regrow_old = false;
+    }
+
+    void reset_origami() {   // src/movetypes.cpp:53
+        for (auto& k : assigned) unassign_domain(dom_of(k));
+        for (int c_i : added) {
+            delete_chain(c_i);
+            current_c_i -= 1;
+        }
+        for (size_t n = 0; n < modified.size(); ++n) set_checked(dom_of(modified[n]), prev_pos[n], prev_ore[n]);
+        violated = false;
+    }
+
+    bool test_acceptance(double p) {   // src/movetypes.cpp:142
+        double pa = std::fmin(1.0, p) * modifier;
+        if (pa == 1) return true;
+        return pa > rng.uniform_real();
+    }
+
+    int select_random_domain() {   // src/movetypes.cpp:98
+        int idx = rng.uniform_int(0, num_domains - 1);
+        int cnt = 0;
+        for (auto& ch : chains)
+            for (int id : ch) {
+                if (cnt == idx) return id;
+                cnt++;
+            }
+        return -1;
+    }
+
+    bool staple_is_connector(const std::vector<int>& st) {   // src/movetypes.cpp:160
+        for (int id : st) {
+            if (doms[id].state != UNBOUND) {
+                int b = doms[id].bound;
+                if (doms[b].c == scaffold_c()) continue;
+                std::set<int> part {doms[id].c};
+                if (!scan_for_scaffold(b, part)) return true;
+            }
+        }
+        return false;
+    }
+    bool scan_for_scaffold(int dom, std::set<int>& part) {   // src/movetypes.cpp:191
+        int c_i = doms[dom].c;
+        part.insert(c_i);
+        std::vector<int> st = get_chain(c_i);
+        for (int cur : st) {
+            if (cur == dom) continue;
+            int b = doms[cur].bound;
+            if (b >= 0) {
+                if (doms[b].c == doms[dom].c) continue;
+                if (doms[b].c == scaffold_c()) return true;
+                if (part.count(doms[b].c) > 0) continue;
+                if (scan_for_scaffold(b, part)) return true;
+            }
+        }
+        return false;
+    }
+    int scaffold_c() const { return 0; }
+
+    int num_bound_staple_domains(const std::vector<int>& st) const {   // src/movetypes.cpp:395
+        int n = 0;
+        for (int id : st)
+            if (doms[id].state == BOUND || doms[id].state == MISBOUND) n++;
+        return n;
+    }
+
+    std::vector<std::pair<int, int>> find_bound_domains(const std::vector<int>& st) const {   // :258
+        std::vector<std::pair<int, int>> out;
+        int c = doms[st[0]].c;
+        for (int id : st)
+            if (doms[id].bound >= 0 && doms[doms[id].bound].c != c) out.push_back({id, doms[id].bound});
+        if (out.empty()) throw std::runtime_error("System has unbound staple");
+        return out;
+    }
+
+    void unassign_domains(const std::vector<int>& st) {   // src/met_movetypes.cpp:77, src/cb_movetypes.cpp:200
+        for (int id : st) {
+            modified.push_back(key_of(id));
+            prev_pos.push_back(doms[id].pos);
+            prev_ore.push_back(doms[id].ore);
+            double de = unassign_domain(id);
+            delta_e += de;
+        }
+    }
+
+    // RegrowthMCMovetype::set_growth_point (src/movetypes.cpp:322)
+    double set_growth_point(int gnew, int gold) {
+        V3 o = -doms[gold].ore;
+        double de = set_domain_config(gnew, doms[gold].pos, o);
+        if (violated) rejected = true;
+        else assigned.push_back(key_of(gnew));
+        return de;
+    }
+
+    // MetMCMovetype::grow_chain (src/met_movetypes.cpp:50)
+    void met_grow_chain(const std::vector<int>& ds) {
+        for (size_t i = 1; i < ds.size(); ++i) {
+            int id = ds[i], prev = ds[i - 1];
+            V3 p = doms[prev].pos + kUnit[rng.uniform_int(0, 5)];
+            V3 o = kUnit[rng.uniform_int(0, 5)];
+            delta_e += set_domain_config(id, p, o);
+            if (violated) {
+                rejected = true;
+                break;
+            }
+            assigned.push_back(key_of(id));
+        }
+    }
+
+    // RegrowthMCMovetype::grow_staple (src/movetypes.cpp:343)
+    void grow_staple(int d_i, const std::vector<int>& ch, bool cb) {
+        std::vector<int> three(ch.begin() + d_i, ch.end());
+        if (three.size() > 1) {
+            if (cb) cb_grow_chain(three);
+            else met_grow_chain(three);
+        }
+        if (rejected) return;
+        std::vector<int> five(ch.begin(), ch.begin() + d_i + 1);
+        std::reverse(five.begin(), five.end());
+        if (five.size() > 1) {
+            if (cb) cb_grow_chain(five);
+            else met_grow_chain(five);
+        }
+    }
+
+    double add_external_bias_met() {   // src/met_movetypes.cpp:69
+        update_move_params();
+        double b = calc_move();
+        delta_e += b;
+        return b;
+    }
+
+    // MetStapleExchangeMCMovetype (src/met_movetypes.cpp:192-403)
+    int insertion_sites {0};
+    bool staple_bound {false};
+
+    bool exchange_accept_common(int ident, double pratio) {
+        if (staple_bound) {
+            modifier *= cfg.exchange_mults[ident - 1];
+            if (modifier * std::fmin(1.0, pratio) > 1) {
+                if (cfg.adaptive_exchange) {
+                    cfg.exchange_mults[ident - 1] /= 10;
+                    return false;
+                }
+                if (cfg.allow_nonsensical_ps) return true;
+                throw std::runtime_error("Nonsensical exchange probability detected");
+            }
+            return test_acceptance(pratio);
+        }
+        return test_acceptance(pratio);
+    }
+
+    bool insert_staple() {
+        int S = (int)cfg.identities.size() - 1;
+        int ident = rng.uniform_int(1, S);
+        if (num_staples == cfg.max_total_staples) return false;
+        if (num_staples_of_ident(ident) == cfg.max_type_staples) return false;
+        int c_i = add_chain(ident);
+        if (cfg.mean_field) delta_e += std::log(6);
+        delta_e += tab.init_e;
+        added.push_back(c_i);
+        std::vector<int> ch = chains.back();
+        int gi = rng.uniform_int(0, (int)ch.size() - 1);
+        int gnew = ch[gi];
+        int gold = select_random_domain();
+        long guard = 0;
+        while (doms[gold].c == doms[gnew].c) {
+            gold = select_random_domain();
+            if (++guard > 100000000L) throw std::runtime_error("growth point selection did not terminate");
+        }
+        delta_e += set_growth_point(gnew, gold);
+        if (rejected) return false;
+        grow_staple(doms[gnew].d, ch, false);
+        if (rejected) return false;
+        std::vector<int> st = get_chain(c_i);
+        for (int id : st)
+            if (doms[id].state == BOUND) { staple_bound = true; break; }
+        int nbd = num_bound_staple_domains(st);
+        add_external_bias_met();
+        double boltz = std::exp(-delta_e);
+        int ni = num_staples_of_ident(ident);
+        size_t L = cfg.identities[ident].size();
+        double pratio = static_cast<double>(L) / 6.0 / ni * boltz;
+        pratio *= insertion_sites * cfg.staple_M;
+        pratio /= nbd;
+        return exchange_accept_common(ident, pratio);
+    }
+
+    bool delete_staple() {
+        int S = (int)cfg.identities.size() - 1;
+        int ident = rng.uniform_int(1, S);
+        int n = num_staples_of_ident(ident);
+        if (n == 0) {
+            rejected = true;
+            return false;
+        }
+        int c_i = ident_to_index[ident][rng.uniform_int(0, n - 1)];
+        std::vector<int> st = get_chain(c_i);
+        if (staple_is_connector(st)) return false;
+        for (int id : st)
+            if (doms[id].state == BOUND) { staple_bound = true; break; }
+        int nbd = num_bound_staple_domains(st);
+        unassign_domains(st);
+        if (cfg.mean_field) delta_e -= std::log(6);
+        delta_e -= tab.init_e;
+        num_staples--;
+        add_external_bias_met();
+        num_staples++;
+        double boltz = std::exp(-delta_e);
+        int ni = num_staples_of_ident(ident);
+        size_t L = cfg.identities[ident].size();
+        double pratio = ni * 6.0 / static_cast<double>(L) * boltz;
+        pratio /= cfg.staple_M * (double)(size_t)(insertion_sites - L);
+        pratio *= nbd;
+        bool acc = exchange_accept_common(ident, pratio);
+        if (acc) delete_chain(c_i);
+        return acc;
+    }
+
+    bool met_exchange() {
+        insertion_sites = num_domains;
+        staple_bound = false;
+        if (rng.uniform_real() < 0.5) return insert_staple();
+        return delete_staple();
+    }
+
+    // MetStapleRegrowthMCMovetype (src/met_movetypes.cpp:470)
+    bool met_regrowth() {
+        if (num_staples == 0) return false;
+        int ci = rng.uniform_int(1, num_staples);
+        std::vector<int> sel = chains[ci];
+        if (staple_is_connector(sel)) return false;
+        auto bds = find_bound_domains(sel);
+        auto gp = bds[rng.uniform_int(0, (int)bds.size() - 1)];
+        unassign_domains(sel);
+        delta_e += set_growth_point(gp.first, gp.second);
+        if (rejected) return false;
+        grow_staple(doms[gp.first].d, sel, false);
+        if (rejected) return false;
+        add_external_bias_met();
+        int nbd = num_bound_staple_domains(sel);
+        double boltz = std::exp(-(delta_e));
+        double pratio = boltz * bds.size() / nbd;
+        return test_acceptance(pratio);
+    }
+
+    // CBMCMovetype helpers (src/cb_movetypes.cpp:58-225)
+    void calc_biases(V3 p_prev, int dom, std::vector<V3>& cpos, std::vector<V3>& core,
+                     std::vector<double>& bf) {
+        for (int v = 0; v < 6; ++v) {
+            V3 p = p_prev + kUnit[v];
+            int occ = occupancy(p);
+            if (occ == BOUND || occ == MISBOUND) continue;
+            if (occ == UNBOUND) {
+                int ud = unbound_at(p);
+                V3 o = -doms[ud].ore;
+                double de = check_domain_constraints(dom, p, o);
+                if (!violated) {
+                    cpos.push_back(p);
+                    core.push_back(o);
+                    double b = 1;
+                    b *= std::exp(-de);
+                    bf.push_back(b);
+                }
+                else {
+                    violated = false;
+                }
+            }
+            else {
+                cpos.push_back(p);
+                core.push_back(V3(0, 0, 0));
+                double de = check_domain_constraints(dom, p, V3(1, 0, 0));
+                bf.push_back(6 * std::exp(-de));
+            }
+        }
+    }
+
+    void cb_select_and_set(int i, const std::vector<int>& ds) {
+        int dom = ds[i];
+        int prev = ds[i - 1];
+        V3 p_prev = doms[prev].pos;
+        std::vector<V3> cpos, core;
+        std::vector<double> bf;
+        calc_biases(p_prev, dom, cpos, core, bf);
+        double ros = 0;
+        for (double b : bf) ros += b;
+        std::vector<double> w;
+        if (ros == 0) {
+            rejected = true;
+            return;
+        }
+        w_bias *= ros;
+        for (double b : bf) w.push_back(b / ros);
+        if (!regrow_old) {
+            V3 p(0, 0, 0), o(0, 0, 0);
+            double cum = 0;
+            double r = rng.uniform_real();
+            for (size_t n = 0; n < w.size(); ++n) {
+                cum += w[n];
+                if (r < cum) {
+                    p = cpos[n];
+                    o = core[n];
+                    break;
+                }
+            }
+            if (o == V3(0, 0, 0)) o = kUnit[rng.uniform_int(0, 5)];
+            set_checked(dom, p, o);
+        }
+        else {
+            Key k = key_of(dom);
+            size_t n = 0;
+            while (!(old_keys[n].c == k.c && old_keys[n].d == k.d)) ++n;
+            set_checked(dom, old_pos[n], old_ore[n]);
+        }
+        assigned.push_back(key_of(dom));
+    }
+
+    void cb_grow_chain(const std::vector<int>& ds) {   // src/cb_movetypes.cpp:354
+        for (size_t i = 1; i < ds.size(); ++i) {
+            cb_select_and_set((int)i, ds);
+            if (rejected) break;
+        }
+    }
+
+    void cb_set_gp_and_grow(std::pair<int, int> gp, const std::vector<int>& sel) {   // :389
+        if (regrow_old) {
+            Key k = key_of(gp.first);
+            size_t n = 0;
+            while (!(old_keys[n].c == k.c && old_keys[n].d == k.d)) ++n;
+            double de = 0;
+            de += set_checked(gp.first, doms[gp.second].pos, old_ore[n]);
+            w_bias *= std::exp(-de);
+            assigned.push_back(k);
+        }
+        else {
+            double de = set_growth_point(gp.first, gp.second);
+            w_bias *= std::exp(-de);
+        }
+        if (!rejected) grow_staple(doms[gp.first].d, sel, true);
+    }
+
+    // CBStapleRegrowthMCMovetype::internal_attempt_move (src/cb_movetypes.cpp:292)
+    bool cb_regrowth() {
+        if (num_staples == 0) return false;
+        int ci = rng.uniform_int(1, num_staples);
+        std::vector<int> sel = chains[ci];
+        if (staple_is_connector(sel)) return false;
+        auto bds = find_bound_domains(sel);
+        w_bias *= bds.size();
+        auto gp = bds[rng.uniform_int(0, (int)bds.size() - 1)];
+        unassign_domains(sel);
+        cb_set_gp_and_grow(gp, sel);
+        if (rejected) return false;
+        w_bias /= num_bound_staple_domains(sel);
+        update_move_params();
+        double tb = calc_move();
+        w_bias *= std::exp(-tb);
+        // setup_for_regrow_old (:215)
+        regrow_old = true;
+        w_new_bias = w_bias;
+        new_modifier = modifier;
+        w_bias = 1;
+        old_keys = modified;
+        old_pos = prev_pos;
+        old_ore = prev_ore;
+        modified.clear();
+        assigned.clear();
+        prev_pos.clear();
+        prev_ore.clear();
+        gp = bds[rng.uniform_int(0, (int)bds.size() - 1)];
+        unassign_domains(sel);
+        cb_set_gp_and_grow(gp, sel);
+        modifier = new_modifier;
+        // test_cb_acceptance (:182)
+        double ratio = w_new_bias / w_bias;
+        if (test_acceptance(ratio)) {
+            reset_origami();
+            update_move_params();
+            calc_move();
+            return true;
+        }
+        modified.clear();
+        assigned.clear();
+        prev_pos.clear();
+        prev_ore.clear();
+        return false;
+    }
+
+    // OrientationRotationMCMovetype::internal_attempt_move (src/orientation_movetype.cpp:30)
+    bool orientation_rotation() {
+        int dom = select_random_domain();
+        V3 o_new = kUnit[rng.uniform_int(0, 5)];
+        bool acc = false;
+        if (doms[dom].state == BOUND || doms[dom].state == MISBOUND) {
+            double de = 0;
+            V3 o_old = doms[dom].ore;
+            int bd = doms[dom].bound;
+            de += unassign_domain(bd);
+            set_domain_orientation(dom, o_new);
+            V3 p = doms[dom].pos;
+            de += set_domain_config(bd, p, -o_new);
+            if (!violated) acc = test_acceptance(std::exp(-de));
+            if (!acc) {
+                unassign_domain(bd);
+                set_domain_orientation(dom, o_old);
+                set_checked(bd, p, -o_old);
+            }
+        }
+        else {
+            set_domain_orientation(dom, o_new);
+            acc = true;
+        }
+        return acc;
+    }
+
+    // GCMCSimulation::simulate step body (src/simulation.cpp:575-619)
+    bool step(long long s) {
+        double r = rng.uniform_real();
+        size_t m = 0;
+        for (m = 0; m < cfg.move_cum.size(); ++m)
+            if (r < cfg.move_cum[m]) break;
+        if (m == cfg.move_cum.size()) throw std::runtime_error("movetype selection fell off the end");
+        reset_internal();
+        bool acc = false;
+        switch (cfg.move_kinds[m]) {
+        case MV_ORIENTATION: acc = orientation_rotation(); break;
+        case MV_MET_EXCHANGE: acc = met_exchange(); break;
+        case MV_MET_REGROWTH: acc = met_regrowth(); break;
+        case MV_CB_REGROWTH: acc = cb_regrowth(); break;
+        }
+        attempts[m]++;
+        if (acc) accepts[m]++;
+        if (!acc) {
+            reset_origami();
+            update_move_params();
+            calc_move();
+        }
+        if (cfg.centering_freq != 0 && s % cfg.centering_freq == 0) center(cfg.centering_domain);
+        if (cfg.constraint_check_freq != 0 && s % cfg.constraint_check_freq == 0) check_all_constraints();
+        return acc;
+    }
+};
+
+} // namespace oracle

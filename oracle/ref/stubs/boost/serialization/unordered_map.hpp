@@ -1,0 +1,2 @@
+#pragma once
+#include "../archive/archive_stub.hpp"
