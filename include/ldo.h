@@ -1,0 +1,154 @@
+/* ldo.h - C ABI of the GB300 lattice DNA-origami Monte Carlo engine.
+ *
+ * The reference (cumberworth/LatticeDNAOrigami) is one C++ program with no
+ * plugin or FFI layer; its hot path is reached through C++ classes.  Each
+ * entry point below replaces one of those calls for a batch of replicas that
+ * live on one GPU:
+ *
+ *   ldo_create_from_inp   origami::setup_origami + GCMCSimulation ctor
+ *                         (src/origami_system.cpp:991, src/simulation.cpp:182)
+ *   ldo_set_controls      OrigamiSystem::update_temp / update_staple_us
+ *                         (src/origami_system.cpp:618-628)
+ *   ldo_run               GCMCSimulation::simulate (src/simulation.cpp:568)
+ *   ldo_get_observables   OrigamiSystem counters + energy + SystemBiases
+ *                         (include/.../origami_system.hpp:99-130)
+ *   ldo_get_config        OrigamiSystem::chains (src/origami_system.cpp:175)
+ *   ldo_pt_run            PTGCMCSimulation::run (src/ptmc_simulation.cpp:106)
+ *
+ * Conventions: every call is synchronous at return; input buffers are
+ * copied; output buffers are caller-allocated; no C++ exception crosses the
+ * ABI; the engine is not thread-safe (one host thread per engine).  Random
+ * numbers follow one Philox4x32-10 stream per replica, key (seed, replica).
+ */
+#ifndef LDO_H
+#define LDO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ldo_engine ldo_engine;
+
+typedef enum {
+    LDO_OK = 0,
+    LDO_EINVAL = 1,      /* bad argument or input file (reference: FileError, OrigamiMisuse at load) */
+    LDO_ENOMEM = 2,      /* device or host allocation failed */
+    LDO_ECUDA = 3,       /* CUDA runtime error */
+    LDO_EINVARIANT = 4,  /* a replica hit a state the reference throws on (OrigamiMisuse, SimulationMisuse) */
+    LDO_EITERCAP = 5,    /* a data-dependent loop reached its iteration cap */
+    LDO_ECAPACITY = 6    /* a replica needed more staple or lattice slots than allocated */
+} ldo_status;
+
+/* Per-replica observables, as the reference's log block reports them
+ * (src/simulation.cpp:667-704). */
+typedef struct {
+    double energy;            /* OrigamiSystem::energy(), kT units            */
+    double total_bias;        /* SystemBiases::get_total_bias()               */
+    double temp;              /* current temperature (K)                      */
+    double enthalpy;          /* update_enthalpy_and_entropy: H / T           */
+    double entropy;           /*                              S               */
+    double stacking;          /*                              stacking energy */
+    int64_t draws;            /* random numbers consumed                      */
+    int32_t num_staples;
+    int32_t num_fully_bound;  /* NumBoundDomainPairs order parameter          */
+    int32_t num_bound;        /* bound + misbound pairs                       */
+    int32_t num_self_bound;
+    int32_t num_stacked;
+    int32_t num_unassigned;
+    int32_t current_c_i;      /* next unique chain index - 1                  */
+    int32_t status;           /* ldo_status of this replica                   */
+} ldo_observables;
+
+/* Creates n_replicas copies of the system described by a reference .inp file
+ * (key=value, src/parser.cpp option names).  `overrides` holds extra
+ * key=value lines applied after the file (may be NULL).  Replica r draws from
+ * Philox key (seed, r). */
+ldo_status ldo_create_from_inp(const char* inp_path, const char* overrides, int n_replicas, uint32_t seed,
+                               ldo_engine** out);
+
+/* Like ldo_create_from_inp, but replica r is a copy of system
+ * sys_of_replica[r] taken from inp_paths[] (uneven sizes in one batch). */
+ldo_status ldo_create_multi(const char* const* inp_paths, int n_systems, const char* overrides,
+                            const int* sys_of_replica, int n_replicas, uint32_t seed, ldo_engine** out);
+
+void ldo_destroy(ldo_engine* e);
+
+/* Last error message of this engine (or of the last failed create if e is NULL). */
+const char* ldo_last_error(const ldo_engine* e);
+
+int ldo_num_replicas(const ldo_engine* e);
+
+/* Per-replica temperature, stacking multiplier and staple chemical-potential
+ * multiplier.  Rebuilds the energy tables and recomputes every replica's
+ * energy by unassigning and reassigning all domains, like
+ * OrigamiSystem::update_temp (src/origami_system.cpp:618).  NULL arrays keep
+ * the current values. */
+ldo_status ldo_set_controls(ldo_engine* e, const double* temps, const double* stacking_mults,
+                            const double* staple_u_mults, int n);
+
+/* Each replica performs n_steps move attempts (GCMCSimulation::simulate).
+ * If device_ms is non-NULL it receives the kernel time measured with CUDA
+ * events on the engine's stream. */
+ldo_status ldo_run(ldo_engine* e, int64_t n_steps, double* device_ms);
+
+/* Each replica performs n_sweeps sweeps of n_scaffold move attempts (its own
+ * scaffold length); sampling intervals then count sweeps. */
+ldo_status ldo_run_sweeps(ldo_engine* e, int64_t n_sweeps, double* device_ms);
+
+/* Bytes of device state per replica (the shared-memory footprint of one warp). */
+int ldo_state_bytes(const ldo_engine* e);
+
+ldo_status ldo_get_observables(ldo_engine* e, ldo_observables* out, int n);
+
+/* Configuration of one replica: n_chains, then per chain (index, identity,
+ * length, length x (x, y, z, ox, oy, oz, state)).  *written receives the
+ * number of ints; LDO_EINVAL if cap is too small. */
+ldo_status ldo_get_config(ldo_engine* e, int replica, int32_t* buf, int cap, int* written);
+
+/* Order-parameter sampling: every `interval` steps each replica appends
+ * (num_fully_bound, num_staples) to a ring of `capacity` samples. */
+ldo_status ldo_set_sampling(ldo_engine* e, int interval, int capacity);
+/* Copies samples[replica][k][2] (int16) for the first min(count, capacity). */
+ldo_status ldo_get_samples(ldo_engine* e, int16_t* out, int capacity, int* count);
+
+/* Step trace for replicas [0, n_trace): per step 8 doubles (step, energy,
+ * staples, fully bound, bound, stacked, total bias, draws). */
+ldo_status ldo_set_trace(ldo_engine* e, int n_trace, int max_steps);
+ldo_status ldo_get_trace(ldo_engine* e, double* out, int n_trace, int max_steps);
+
+/* Per-move attempts/accepts summed over replicas: out[2*m], out[2*m+1]. */
+ldo_status ldo_get_move_stats(ldo_engine* e, int64_t* out, int n_moves);
+
+/* Grid-bias values for bias function `tag` (1-D over the order parameter
+ * value 0..n-1) of one replica, or of all replicas if replica < 0
+ * (GridBiasFunction::replace_biases, src/bias_functions.cpp:237). */
+ldo_status ldo_set_grid_bias(ldo_engine* e, const char* tag, int replica, const double* values, int n);
+
+/* Window restraint of one replica for a SquareWell bias `tag`
+ * (SquareWellBiasFunction::set_min_op/set_max_op, src/bias_functions.cpp:218-220). */
+ldo_status ldo_set_window(ldo_engine* e, const char* tag, int replica, int min_op, int max_op);
+
+/* Parallel tempering: `swaps` rounds of (update controls, exchange_interval
+ * steps, exchange attempt between neighbouring control slots), the 1-D
+ * even/odd schedule of PTGCMCSimulation::run / OneDPTGCMCSimulation::
+ * attempt_exchange (src/ptmc_simulation.cpp:106-412).  Replicas are split
+ * into n_ladders independent ladders of n_rungs consecutive replicas.
+ * `exchange_q` selects the exchanged controls as a bit set:
+ * 1 = temperature, 2 = staple chemical potential, 4 = bias multiplier,
+ * 8 = stacking multiplier (T: 1, uT: 3, HuT: 7, ST: 9). */
+ldo_status ldo_pt_run(ldo_engine* e, int n_rungs, int64_t swaps, int exchange_interval, int exchange_q,
+                      double* device_ms);
+
+/* Current control-slot to replica permutation (the .swp file row) for all
+ * ladders: out[ladder * n_rungs + slot] = replica. */
+ldo_status ldo_pt_get_permutation(ldo_engine* e, int32_t* out, int n);
+/* Swap attempts and acceptances per neighbouring slot pair, summed over ladders. */
+ldo_status ldo_pt_get_stats(ldo_engine* e, int64_t* attempts, int64_t* accepts, int n_pairs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LDO_H */

@@ -1,0 +1,1755 @@
+// Device-side Monte Carlo engine: one replica's lattice state lives in shared
+// memory for the whole launch and one thread of the replica's warp applies
+// moves to it.  The member functions restate, in this layout, the reference's
+//   OrigamiSystem state transitions    (src/origami_system.cpp:343-871)
+//   JunctionBindingPotential (FourBody) (src/origami_potential.cpp:51-934)
+//   staple movetypes                   (src/movetypes.cpp, src/met_movetypes.cpp,
+//                                       src/cb_movetypes.cpp, src/orientation_movetype.cpp)
+//   the step body of GCMCSimulation::simulate (src/simulation.cpp:575-619).
+// Terms are visited and summed in the reference's order so that energies and
+// every random draw agree with it exactly.
+//
+// Layout in shared memory (one region per replica, see LdoLayout):
+//   per domain slot   pos x/y/z (int16), orientation index (uint8, unit vector
+//                     k of {+x,-x,+y,-y,+z,-z}), occupancy state, bound partner
+//                     slot, identity, owning chain slot, index in chain
+//   per chain slot    unique chain index, chain type; chain order list
+//   occupancy hash    open addressing, linear probing, backward-shift delete;
+//                     entry = packed position | site state | unbound slot
+// Slot s < ns is scaffold domain s; staple chain slot k >= 1 owns slots
+// ns + (k-1)*lmax + d.
+#pragma once
+#include <stdint.h>
+#include "ldo_types.h"
+
+#ifndef LDO_DEV
+#define LDO_DEV __device__ __forceinline__
+#endif
+
+namespace ldo {
+
+enum { UNASSIGNED = 0, UNBOUND = 1, BOUND = 2, MISBOUND = 3 };
+
+struct V3 {
+    int x, y, z;
+};
+LDO_DEV V3 mk(int x, int y, int z) { V3 r; r.x = x; r.y = y; r.z = z; return r; }
+LDO_DEV V3 add(V3 a, V3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+LDO_DEV V3 sub(V3 a, V3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+LDO_DEV V3 neg(V3 a) { return mk(-a.x, -a.y, -a.z); }
+LDO_DEV bool eq(V3 a, V3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+LDO_DEV V3 absv(V3 a) { return mk(a.x < 0 ? -a.x : a.x, a.y < 0 ? -a.y : a.y, a.z < 0 ? -a.z : a.z); }
+
+// Unit vector k in the order of include/.../utility.hpp:156-162.
+LDO_DEV V3 unit(int k) {
+    int s = (k & 1) ? -1 : 1;
+    int a = k >> 1;
+    return mk(a == 0 ? s : 0, a == 1 ? s : 0, a == 2 ? s : 0);
+}
+LDO_DEV int unit_index(V3 v) {
+    if (v.x != 0) return v.x > 0 ? 0 : 1;
+    if (v.y != 0) return v.y > 0 ? 2 : 3;
+    return v.z > 0 ? 4 : 5;
+}
+
+// VectorThree::rotate_half (src/utility.cpp:68)
+LDO_DEV V3 rotate_half(V3 v, V3 axis) {
+    V3 a = absv(axis);
+    if (a.x == 1 && a.y == 0 && a.z == 0) { v.y = -v.y; v.z = -v.z; }
+    else if (a.x == 0 && a.y == 1 && a.z == 0) { v.x = -v.x; v.z = -v.z; }
+    else if (a.x == 0 && a.y == 0 && a.z == 1) { v.x = -v.x; v.y = -v.y; }
+    return v;
+}
+
+// VectorThree::rotate(axis, -1) (src/utility.cpp:102), the quarter turn used
+// by ThreeQuarterTurnDomain::check_twist_constraint.
+LDO_DEV V3 rotate_quarter_neg(V3 v, V3 axis) {
+    int dir = -1;
+    V3 a = absv(axis);
+    if (!eq(axis, a)) dir = 1;
+    int t;
+    if (a.x == 1 && a.y == 0 && a.z == 0) { t = v.y; v.y = v.z; v.z = t; v.y *= -dir; v.z *= dir; }
+    else if (a.x == 0 && a.y == 1 && a.z == 0) { t = v.x; v.x = v.z; v.z = t; v.x *= -dir; v.z *= dir; }
+    else if (a.x == 0 && a.y == 0 && a.z == 1) { t = v.x; v.x = v.y; v.y = t; v.x *= -dir; v.y *= dir; }
+    return v;
+}
+
+// ------------------------------------------------------------- Philox ---
+// Philox4x32-10 (Salmon et al., SC'11).  Stream contract: key (seed, replica),
+// counter (draw >> 1, 0, stream, 0); draw n is the 64-bit word pair
+// (2*(n&1), 2*(n&1)+1) of its block.
+LDO_DEV void philox10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
+                      uint32_t* out) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        unsigned long long p0 = (unsigned long long)0xD2511F53u * c0;
+        unsigned long long p1 = (unsigned long long)0xCD9E8D57u * c2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        uint32_t n1 = (uint32_t)p1;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        uint32_t n3 = (uint32_t)p0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+struct Rng {
+    uint32_t k0, k1, stream;
+    unsigned long long draws;
+    unsigned long long cblock;
+    uint32_t w[4];
+
+    __device__ void init(uint32_t seed, uint32_t rep, uint32_t s, unsigned long long d) {
+        k0 = seed;
+        k1 = rep;
+        stream = s;
+        draws = d;
+        cblock = ~0ull;
+    }
+    __device__ unsigned long long next64() {
+        unsigned long long b = draws >> 1;
+        if (b != cblock) {
+            philox10((uint32_t)b, (uint32_t)(b >> 32), stream, 0u, k0, k1, w);
+            cblock = b;
+        }
+        int j = (int)(draws & 1ull) * 2;
+        ++draws;
+        return ((unsigned long long)w[j] << 32) | w[j + 1];
+    }
+    __device__ double uniform_real() { return (double)(next64() >> 11) * 0x1.0p-53; }
+    __device__ int uniform_int(int lo, int hi) {
+        unsigned long long range = (unsigned long long)((long long)hi - (long long)lo) + 1ull;
+        return lo + (int)__umul64hi(next64(), range);
+    }
+};
+
+// ------------------------------------------------------------ hashing ---
+#define LDO_KEYMASK ((1ull << 48) - 1ull)
+#define LDO_VALID (1ull << 63)
+
+LDO_DEV unsigned long long pkey(V3 p) {
+    return (unsigned long long)(uint16_t)p.x | ((unsigned long long)(uint16_t)p.y << 16) |
+           ((unsigned long long)(uint16_t)p.z << 32);
+}
+LDO_DEV int ent_occ(unsigned long long e) { return (int)((e >> 48) & 3ull); }
+LDO_DEV int ent_slot(unsigned long long e) { return (int)((e >> 50) & 0xfffull); }
+LDO_DEV unsigned long long mkent(unsigned long long key, int occ, int slot) {
+    return key | ((unsigned long long)occ << 48) | ((unsigned long long)slot << 50) | LDO_VALID;
+}
+
+// Caps for the reference's data-dependent loops (rejection sampling of a
+// growth point, src/movetypes.cpp:378-380).
+#define LDO_GROWTHPOINT_CAP 1000000
+
+struct Delta {
+    double e;
+    int stacked;
+};
+
+struct Scratch {
+    // MCMovetype reversal lists (include/.../movetypes.hpp:156-163)
+    int n_mod, n_asg, added_cs;
+    int mod[LDO_MAX_LEN];
+    V3 mod_pos[LDO_MAX_LEN];
+    int mod_ore[LDO_MAX_LEN];
+    int asg[LDO_MAX_LEN];
+    // CB old configuration (include/.../movetypes.hpp:241-242)
+    int n_old;
+    int old_slot[LDO_MAX_LEN];
+    V3 old_pos[LDO_MAX_LEN];
+    int old_ore[LDO_MAX_LEN];
+    // bound domains of the selected staple (new, old)
+    int n_bd;
+    int bd_new[LDO_MAX_LEN], bd_old[LDO_MAX_LEN];
+};
+
+struct Rep {
+    const LdoSys* sys;
+    const LdoTab* tab;
+    const double* bank;
+    const LdoRepCtl* ctl;
+    const double* grid;
+    LdoHdr* h;
+    int16_t *px, *py, *pz, *bnd, *did;
+    uint8_t *ore, *st, *scs, *sd;
+    int32_t* chain_c;
+    uint8_t *chain_type, *chain_order;
+    int16_t* type_count;
+    unsigned long long* hash;
+    double* bias;
+    int32_t* op;
+    long long* mstat;
+    int hmask, hshift, ns, lmax, nmv;
+    int cyclic, tqt, mean_field;
+    Rng rng;
+    bool pot_violated;
+    Delta pd;
+    Scratch m;
+    bool rejected;
+    double modifier, delta_e;
+    double w_bias, w_new_bias, new_modifier;
+    bool regrow_old;
+    int insertion_sites;
+    bool staple_bound;
+    double log6, log3;
+
+    // ---------------------------------------------------------- errors ---
+    __device__ void fail(int code) {
+        if (h->status == 0) h->status = code;
+    }
+    __device__ bool bad() const { return h->status != 0; }
+
+    // -------------------------------------------------------- accessors ---
+    __device__ V3 pos(int i) const { return mk(px[i], py[i], pz[i]); }
+    __device__ void set_pos(int i, V3 p) {
+        if (p.x < -32000 || p.x > 32000 || p.y < -32000 || p.y > 32000 || p.z < -32000 || p.z > 32000) {
+            fail(LDO_RS_CAPACITY);
+            return;
+        }
+        px[i] = (int16_t)p.x;
+        py[i] = (int16_t)p.y;
+        pz[i] = (int16_t)p.z;
+    }
+    __device__ V3 orev(int i) const { return unit(ore[i]); }
+    __device__ int chain_len(int cs) const { return cs == 0 ? ns : sys->type_len[chain_type[cs]]; }
+    __device__ int slot_of(int cs, int d) const { return cs == 0 ? d : ns + (cs - 1) * lmax + d; }
+    __device__ int cidx(int i) const { return chain_c[scs[i]]; }
+    __device__ int fwd(int i) const {
+        int cs = scs[i], d = sd[i], len = chain_len(cs);
+        if (d + 1 < len) return i + 1;
+        return (cs == 0 && cyclic) ? i - (len - 1) : -1;
+    }
+    __device__ int bwd(int i) const {
+        int cs = scs[i], d = sd[i];
+        if (d > 0) return i - 1;
+        return (cs == 0 && cyclic) ? i + chain_len(cs) - 1 : -1;
+    }
+    __device__ int next(int i, int incr) const {   // Domain::operator+ (src/domain.cpp:9)
+        while (i >= 0 && incr > 0) { i = fwd(i); --incr; }
+        while (i >= 0 && incr < 0) { i = bwd(i); ++incr; }
+        return i;
+    }
+    __device__ double tval(long long off, int a, int b) const {
+        const LdoSys* s = sys;
+        if (tab->dense) return bank[off + (long long)(a + s->imax) * s->dim + (b + s->imax)];
+        return (a == -b) ? bank[off + (a < 0 ? -a : a)] : bank[off + s->imax + 1];
+    }
+    __device__ double hyb(int i, int j) const { return tval(tab->off_e, did[i], did[j]); }
+    __device__ double hyb_h(int i, int j) const { return tval(tab->off_h, did[i], did[j]); }
+    __device__ double hyb_s(int i, int j) const { return tval(tab->off_s, did[i], did[j]); }
+    __device__ double stack(int i, int j) const {
+        if (tab->stack_dense) {
+            const LdoSys* s = sys;
+            return bank[tab->off_stack + (long long)(did[i] + s->imax) * s->dim + (did[j] + s->imax)];
+        }
+        return tab->stack_const;
+    }
+
+    // ------------------------------------------------------------ hash ---
+    __device__ int home(unsigned long long key) const {
+        return (int)((key * 0x9E3779B97F4A7C15ull) >> hshift) & hmask;
+    }
+    // Index of the entry for key, or -1 (then *empty_at is the first free slot).
+    __device__ __noinline__ int hfind(unsigned long long key, int* empty_at) const {
+        int k = home(key);
+        for (int n = 0; n <= hmask; ++n) {
+            unsigned long long e = hash[k];
+            if (!(e & LDO_VALID)) {
+                if (empty_at) *empty_at = k;
+                return -1;
+            }
+            if ((e & LDO_KEYMASK) == key) return k;
+            k = (k + 1) & hmask;
+        }
+        if (empty_at) *empty_at = -1;
+        return -1;
+    }
+    __device__ __noinline__ void herase(int i) {
+        int j = i;
+        for (int n = 0; n <= hmask; ++n) {
+            j = (j + 1) & hmask;
+            unsigned long long e = hash[j];
+            if (!(e & LDO_VALID)) break;
+            int k = home(e & LDO_KEYMASK);
+            bool move = (i <= j) ? (k <= i || k > j) : (k <= i && k > j);
+            if (move) {
+                hash[i] = e;
+                i = j;
+            }
+        }
+        hash[i] = 0ull;
+    }
+    __device__ __noinline__ void hset(V3 p, int occ, int slot) {
+        unsigned long long key = pkey(p);
+        int emp;
+        int k = hfind(key, &emp);
+        if (k < 0) k = emp;
+        if (k < 0) {
+            fail(LDO_RS_CAPACITY);
+            return;
+        }
+        hash[k] = mkent(key, occ, slot);
+    }
+    __device__ int occupancy(V3 p) const {
+        int k = hfind(pkey(p), nullptr);
+        return k < 0 ? UNASSIGNED : ent_occ(hash[k]);
+    }
+    __device__ int unbound_at(V3 p) const {
+        int k = hfind(pkey(p), nullptr);
+        return k < 0 ? -1 : ent_slot(hash[k]);
+    }
+
+    // ----------------------------------------------------- chain add/del ---
+    // OrigamiSystem::add_chain(c_i_ident, c_i) (src/origami_system.cpp:402)
+    __device__ __noinline__ int add_chain_with_index(int type, int c_i) {
+        int cs = -1;
+        int kmax = sys->kmax;
+        for (int k = 1; k <= kmax; ++k)
+            if (chain_type[k] == 0xff) { cs = k; break; }
+        if (cs < 0) {
+            fail(LDO_RS_CAPACITY);
+            return -1;
+        }
+        chain_c[cs] = c_i;
+        chain_type[cs] = (uint8_t)type;
+        chain_order[h->n_chains++] = (uint8_t)cs;
+        type_count[type]++;
+        int len = sys->type_len[type];
+        int off = sys->type_off[type];
+        for (int d = 0; d < len; ++d) {
+            int s = slot_of(cs, d);
+            st[s] = UNASSIGNED;
+            bnd[s] = -1;
+            did[s] = sys->idents[off + d];
+        }
+        h->num_domains += len;
+        h->num_unassigned += len;
+        h->num_staples++;
+        return cs;
+    }
+    // OrigamiSystem::add_chain(c_i_ident) (src/origami_system.cpp:387)
+    __device__ __noinline__ int add_chain(int type) {
+        h->current_c_i += 1;
+        if (mean_field) h->energy += log6;
+        h->energy += tab->init_e;
+        return add_chain_with_index(type, h->current_c_i);
+    }
+    // OrigamiSystem::delete_chain (src/origami_system.cpp:445)
+    __device__ __noinline__ void delete_chain(int cs) {
+        int n = h->n_chains;
+        int k = 0;
+        while (k < n && chain_order[k] != cs) ++k;
+        for (int q = k; q + 1 < n; ++q) chain_order[q] = chain_order[q + 1];
+        h->n_chains = n - 1;
+        int type = chain_type[cs];
+        type_count[type]--;
+        int len = sys->type_len[type];
+        h->num_domains -= len;
+        h->num_staples--;
+        h->num_unassigned -= len;
+        chain_type[cs] = 0xff;
+        if (mean_field) h->energy -= log6;
+        h->energy -= tab->init_e;
+    }
+
+    // ------------------------------------------------- state transitions ---
+    // OrigamiSystem::update_occupancies (src/origami_system.cpp:770)
+    __device__ __noinline__ void update_occupancies(int i, V3 p) {
+        unsigned long long key = pkey(p);
+        int emp;
+        int k = hfind(key, &emp);
+        int occ = k < 0 ? UNASSIGNED : ent_occ(hash[k]);
+        if (occ == UNBOUND) {
+            int j = ent_slot(hash[k]);
+            h->num_bound += 1;
+            int ns_;
+            if (did[i] == -did[j]) {
+                ns_ = BOUND;
+                h->num_fully += 1;
+            }
+            else {
+                if (cidx(i) == cidx(j)) h->num_self += 1;
+                ns_ = MISBOUND;
+            }
+            st[i] = (uint8_t)ns_;
+            st[j] = (uint8_t)ns_;
+            hash[k] = mkent(key, ns_, 0);
+            bnd[j] = (int16_t)i;
+            bnd[i] = (int16_t)j;
+        }
+        else if (occ == UNASSIGNED) {
+            st[i] = UNBOUND;
+            if (emp < 0) {
+                fail(LDO_RS_CAPACITY);
+                return;
+            }
+            hash[emp] = mkent(key, UNBOUND, i);
+        }
+        else {
+            fail(LDO_RS_INVARIANT);   // "Trying to bind to an already bound domain"
+        }
+    }
+
+    // unassign_bound_domain (src/origami_system.cpp:741)
+    __device__ __noinline__ double unassign_bound(int i) {
+        int j = bnd[i];
+        double de = -hyb(i, j);
+        bnd[i] = -1;
+        bnd[j] = -1;
+        st[i] = UNASSIGNED;
+        hset(pos(i), UNBOUND, j);
+        st[j] = UNBOUND;
+        return de;
+    }
+
+    // internal_unassign_domain (src/origami_system.cpp:695)
+    __device__ __noinline__ Delta internal_unassign(int i) {
+        int occ = st[i];
+        int j = bnd[i];
+        Delta dc;
+        dc.e = 0;
+        dc.stacked = 0;
+        if ((occ == BOUND || occ == MISBOUND) && j < 0) {
+            fail(LDO_RS_INVARIANT);
+            return dc;
+        }
+        switch (occ) {
+        case BOUND:
+            h->num_fully -= 1;
+            h->num_bound -= 1;
+            dc = check_stacking(i, j);
+            dc.e *= -1;
+            dc.stacked *= -1;
+            dc.e += unassign_bound(i);
+            break;
+        case MISBOUND:
+            h->num_bound -= 1;
+            if (cidx(j) == cidx(i)) h->num_self -= 1;
+            dc.e += unassign_bound(i);
+            break;
+        case UNBOUND: {
+            int k = hfind(pkey(pos(i)), nullptr);
+            if (k >= 0) herase(k);
+            st[i] = UNASSIGNED;
+            break;
+        }
+        default:
+            h->num_unassigned--;
+            break;
+        }
+        if (mean_field && occ == BOUND) {
+            if (h->num_fully == 0) dc.e -= 2 * log6;
+            else if (h->num_fully == 1) dc.e -= log3;
+        }
+        return dc;
+    }
+
+    // internal_check_domain_constraints (src/origami_system.cpp:828)
+    __device__ __noinline__ Delta internal_check(int i, V3 p, int o) {
+        int occ = occupancy(p);
+        Delta dc;
+        dc.e = 0;
+        dc.stacked = 0;
+        switch (occ) {
+        case BOUND:
+        case MISBOUND:
+            h->violated = 1;
+            h->num_unassigned++;
+            break;
+        case UNBOUND:
+            set_pos(i, p);
+            ore[i] = (uint8_t)o;
+            update_occupancies(i, p);
+            if (bad()) return dc;
+            dc = bind_domain(i);
+            h->violated = pot_violated ? 1 : 0;
+            break;
+        default:
+            set_pos(i, p);
+            ore[i] = (uint8_t)o;
+            update_occupancies(i, p);
+            break;
+        }
+        if (mean_field && !h->violated && st[i] == BOUND) {
+            if (h->num_fully == 1) dc.e += 2 * log6;
+            else if (h->num_fully == 2) dc.e += log3;
+        }
+        return dc;
+    }
+
+    // set_domain_config (src/origami_system.cpp:517)
+    __device__ __noinline__ double set_domain_config(int i, V3 p, int o) {
+        if (st[i] != UNASSIGNED) {
+            fail(LDO_RS_INVARIANT);   // "Trying to set an already assigned domain"
+            return 0;
+        }
+        Delta dc = internal_check(i, p, o);
+        if (h->violated) {
+            internal_unassign(i);
+        }
+        else {
+            h->energy += dc.e;
+            h->num_stacked += dc.stacked;
+            h->num_unassigned--;
+        }
+        return dc.e;
+    }
+
+    // set_checked_domain_config (src/origami_system.cpp:478)
+    __device__ __noinline__ double set_checked(int i, V3 p, int o) {
+        set_pos(i, p);
+        ore[i] = (uint8_t)o;
+        update_occupancies(i, p);
+        double de = 0;
+        if (bad()) return 0;
+        if (st[i] == MISBOUND) {
+            de += hyb(i, bnd[i]);
+        }
+        else if (st[i] == BOUND) {
+            de += hyb(i, bnd[i]);
+            Delta dc = check_stacking(i, bnd[i]);
+            de += dc.e;
+            h->num_stacked += dc.stacked;
+        }
+        if (mean_field && st[i] == BOUND) {
+            if (h->num_fully == 1) de += 2 * log6;
+            else if (h->num_fully == 2) de += log3;
+        }
+        h->energy += de;
+        h->num_unassigned--;
+        return de;
+    }
+
+    // unassign_domain (src/origami_system.cpp:375)
+    __device__ __noinline__ double unassign_domain(int i) {
+        Delta dc = internal_unassign(i);
+        h->energy += dc.e;
+        h->num_stacked += dc.stacked;
+        h->num_unassigned++;
+        return dc.e;
+    }
+
+    // check_domain_constraints (src/origami_system.cpp:343)
+    __device__ __noinline__ double check_domain_constraints(int i, V3 p, int o) {
+        Delta dc = internal_check(i, p, o);
+        internal_unassign(i);
+        return dc.e;
+    }
+
+    // set_domain_orientation (src/origami_system.cpp:543)
+    __device__ void set_domain_orientation(int i, int o) {
+        if (st[i] == BOUND) h->violated = 1;
+        else ore[i] = (uint8_t)o;
+    }
+
+    // center (src/origami_system.cpp:553)
+    __device__ __noinline__ void center(int cd) {
+        V3 ref = pos(cd);
+        for (int k = 0; k <= hmask; ++k) hash[k] = 0ull;
+        for (int c = 0; c < h->n_chains; ++c) {
+            int cs = chain_order[c];
+            int len = chain_len(cs);
+            for (int d = 0; d < len; ++d) {
+                int s = slot_of(cs, d);
+                V3 np = sub(pos(s), ref);
+                set_pos(s, np);
+                int o = st[s];
+                if (o == UNBOUND) hset(np, UNBOUND, s);
+                else if (o == BOUND || o == MISBOUND) hset(np, o, 0);
+            }
+        }
+    }
+
+    // set_all_domains (src/origami_system.cpp:573)
+    __device__ __noinline__ void set_all_current() {
+        for (int c = 0; c < h->n_chains && !bad(); ++c) {
+            int cs = chain_order[c];
+            int len = chain_len(cs);
+            for (int d = 0; d < len; ++d) {
+                int s = slot_of(cs, d);
+                set_domain_config(s, pos(s), ore[s]);
+                if (h->violated) {
+                    fail(LDO_RS_INVARIANT);   // "Constaints in violation after move complete"
+                    return;
+                }
+            }
+        }
+    }
+
+    // check_all_constraints (src/origami_system.cpp:267)
+    __device__ __noinline__ void check_all_constraints() {
+        if (h->num_unassigned != 0) {
+            fail(LDO_RS_INVARIANT);
+            return;
+        }
+        int nc = h->n_chains;
+        for (int c = 0; c < nc; ++c) {
+            int cs = chain_order[c];
+            int len = chain_len(cs);
+            for (int d = 0; d < len; ++d) {
+                int s = slot_of(cs, d);
+                if (st[s] == UNASSIGNED) {
+                    fail(LDO_RS_INVARIANT);
+                    return;
+                }
+                unassign_domain(s);
+            }
+        }
+        unsigned long long nst = (unsigned long long)(nc - 1);
+        if (mean_field) h->energy -= nst * log6;
+        h->energy -= nst * tab->init_e;
+        if (h->num_stacked != 0) {
+            set_all_current();
+            fail(LDO_RS_INVARIANT);
+            return;
+        }
+        double eps = 0.000001;
+        if (h->energy < -eps || h->energy > eps) {
+            set_all_current();
+            fail(LDO_RS_INVARIANT);
+            return;
+        }
+        h->energy = 0;
+        set_all_current();
+        if (mean_field) h->energy += nst * log6;
+        h->energy += nst * tab->init_e;
+    }
+
+    // update_energy (src/origami_system.cpp:808)
+    __device__ __noinline__ void recompute_energy() {
+        int nc = h->n_chains;
+        for (int c = 0; c < nc; ++c) {
+            int cs = chain_order[c];
+            int len = chain_len(cs);
+            for (int d = 0; d < len; ++d) unassign_domain(slot_of(cs, d));
+        }
+        h->energy = 0;
+        unsigned long long nst = (unsigned long long)(nc - 1);
+        if (mean_field) h->energy += nst * log6;
+        h->energy += nst * tab->init_e;
+        set_all_current();
+    }
+
+    // update_enthalpy_and_entropy (src/origami_system.cpp:204)
+    __device__ __noinline__ void dependent_quantities() {
+        double H = 0, S = 0;
+        // "accounted" = partner of an earlier domain in chain order; a pair is
+        // counted at its first domain.
+        int nc = h->n_chains;
+        for (int c = 0; c < nc; ++c) {
+            int cs = chain_order[c];
+            int len = chain_len(cs);
+            for (int d = 0; d < len; ++d) {
+                int s = slot_of(cs, d);
+                int o = st[s];
+                if (o == BOUND || o == MISBOUND) {
+                    int b = bnd[s];
+                    if (!visited_before(s, b, c, d)) {
+                        H += hyb_h(s, b);
+                        S += hyb_s(s, b);
+                    }
+                }
+            }
+        }
+        unsigned long long nst = (unsigned long long)(nc - 1);
+        if (mean_field) {
+            S -= nst * log6;
+            if (h->num_fully >= 1) S -= 2 * log6;
+            if (h->num_fully >= 2) S -= log3;
+        }
+        H += nst * tab->init_h;
+        S += nst * tab->init_s;
+        h->H = H;
+        h->S = S;
+        h->stacking = h->energy - (H - S);
+    }
+    // True if partner b comes before domain s (chain position c, index d) in
+    // chain order, i.e. s was inserted into the reference's accounted set.
+    __device__ __noinline__ bool visited_before(int s, int b, int c, int d) const {
+        int cb = scs[b];
+        for (int q = 0; q < c; ++q)
+            if (chain_order[q] == cb) return true;
+        if (cb == chain_order[c]) return sd[b] < d;
+        return false;
+    }
+
+    // ================================================ FourBody potential ===
+    __device__ bool exists_bound(int i) const { return i >= 0 && st[i] == BOUND; }
+
+    __device__ __noinline__ bool twist_ok(int i1, V3 ndr, int i2) const {   // src/domain.cpp:33,69
+        V3 o1 = orev(i1);
+        V3 r = tqt ? rotate_quarter_neg(o1, ndr) : rotate_half(o1, ndr);
+        return eq(r, orev(i2));
+    }
+    __device__ __noinline__ bool kink_ok(int i1, V3 ndr, int i2) const {   // src/domain.cpp:42,80
+        V3 o1 = orev(i1), o2 = orev(i2);
+        if (eq(ndr, neg(o1))) return false;
+        if (eq(ndr, o1)) {
+            if (tqt) return !(eq(o1, o2) || eq(o1, neg(o2)));
+            return !eq(o2, neg(o1));
+        }
+        if (eq(ndr, o2) || eq(ndr, neg(o2))) return false;
+        return true;
+    }
+    __device__ __noinline__ bool junction_ok(int j1, int j2, int k1, int k2) const {   // src/domain.cpp:59,99
+        if (!tqt) return true;
+        V3 ndr_k = sub(pos(k2), pos(k1));
+        if (eq(ndr_k, orev(k1))) {
+            V3 ndr1 = sub(pos(j2), pos(j1));
+            if (sd[j1] > sd[j2]) ndr1 = neg(ndr1);
+            if (!twist_ok(k1, ndr1, k2)) return false;
+        }
+        return true;
+    }
+    __device__ __noinline__ bool doubly_contig(int a, int b) const {   // src/origami_potential.cpp:51
+        if (scs[a] != scs[b] || sd[b] != sd[a] + 1) return false;
+        int ba = bnd[a], bb = bnd[b];
+        if (scs[ba] != scs[bb]) return false;
+        int dd = sd[bb] - sd[ba];
+        return dd == 1 || dd == -1;
+    }
+    __device__ __noinline__ bool pair_stacked(int a, int b) const {   // :70
+        if (sd[a] > sd[b]) { int t = a; a = b; b = t; }
+        V3 ndr = sub(pos(b), pos(a));
+        V3 oa = orev(a);
+        if (!eq(ndr, oa) && !eq(ndr, neg(oa))) return twist_ok(a, ndr, b);
+        return false;
+    }
+    __device__ __noinline__ int junction_penalty(int j1, int j2, int j3, int j4, int k1, int k2) const {   // :85
+        V3 ndr_k = sub(pos(k2), pos(k1));
+        if (!eq(ndr_k, orev(k1))) return 0;
+        V3 n1 = sub(pos(j2), pos(j1));
+        if (sd[j1] > sd[j2]) n1 = neg(n1);
+        V3 n3 = sub(pos(j4), pos(j3));
+        if (sd[j3] > sd[j4]) n3 = neg(n3);
+        if (eq(n1, n3)) return 2;
+        if (eq(n1, neg(n3))) return 0;
+        return 1;
+    }
+    __device__ __noinline__ void triplet_single(int h1, int h2, int h3) {   // :158
+        V3 n1 = sub(pos(h2), pos(h1));
+        if (eq(n1, orev(h1))) return;
+        V3 n2 = sub(pos(h3), pos(h2));
+        if (!eq(n1, n2)) {
+            pd.e -= stack(h2, h3);
+            pd.stacked -= 1;
+        }
+    }
+    __device__ __noinline__ void triplet_double(int h1, int h2, int h3) {   // :181
+        V3 n1 = sub(pos(h2), pos(h1));
+        V3 n2 = sub(pos(h3), pos(h2));
+        if (!eq(n1, n2)) {
+            pd.e -= stack(h1, h2) / 2;
+            pd.e -= stack(h2, h3) / 2;
+            pd.stacked -= 1;
+        }
+    }
+    __device__ __noinline__ void triply_contig_helix(int h1, int h2, int h3) {   // :200
+        V3 n1 = sub(pos(h2), pos(h1));
+        V3 n2 = sub(pos(h3), pos(h2));
+        if (!eq(n1, n2)) pot_violated = true;
+    }
+
+    __device__ __noinline__ void stacking_and_steric(int i, int j) {   // :212
+        constraints_around(i, 0);
+        if (pot_violated) return;
+        constraints_around(j, 1);
+        if (pot_violated) return;
+        central_triplets(i, j);
+    }
+
+    __device__ __noinline__ void constraints_around(int cd, int jj) {   // :231
+        for (int k = -1; k <= 0; ++k) {
+            int c1 = next(cd, k);
+            int c2 = next(cd, k + 1);
+            if (!(exists_bound(c1) && exists_bound(c2))) continue;
+            int b1 = bnd[c1], b2 = bnd[c2];
+            if (scs[b1] == scs[b2]) {
+                if (sd[b1] == sd[b2] - 1) doubly_contig_helix_pair(c1, c2, k, jj);
+                else if (sd[b1] == sd[b2] + 1) doubly_contig_junction_pair(c1, c2, jj);
+                else regular_pair(c1, c2, k);
+            }
+            else {
+                regular_pair(c1, c2, k);
+            }
+            if (pot_violated) return;
+        }
+        int prev = next(cd, -1);
+        int forw = next(cd, 1);
+        if (exists_bound(prev) && exists_bound(forw)) {
+            if (pair_stacked(cd, forw)) {
+                if (pair_stacked(prev, cd)) {
+                    if (doubly_contig(prev, cd) && doubly_contig(cd, forw)) {
+                        triply_contig_helix(prev, cd, forw);
+                        if (pot_violated) return;
+                    }
+                    triplet_double(prev, cd, forw);
+                }
+                else {
+                    triplet_single(prev, cd, forw);
+                }
+            }
+        }
+    }
+
+    __device__ __noinline__ void regular_pair(int c1, int c2, int k) {   // :288
+        V3 ndr = sub(pos(c2), pos(c1));
+        if (!kink_ok(c1, ndr, c2)) {
+            pot_violated = true;
+            return;
+        }
+        if (pair_stacked(c1, c2)) {
+            pd.e += stack(c1, c2);
+            pd.stacked += 1;
+            if (k == -1) backward_single_junction(c1, c2);
+            else forward_single_junction(c1, c2);
+        }
+        else {
+            central_single_junction(c1, c2);
+        }
+        if (k == -1) backward_triplets(c1, c2);
+        else forward_triplets(c1, c2);
+    }
+
+    __device__ __noinline__ void doubly_contig_helix_pair(int c1, int c2, int k, int jj) {   // :322
+        if (jj == 1) return;
+        V3 ndr = sub(pos(c2), pos(c1));
+        V3 o1 = orev(c1);
+        if (eq(ndr, o1) || eq(ndr, neg(o1))) {
+            pot_violated = true;
+            return;
+        }
+        if (twist_ok(c1, ndr, c2)) {
+            pd.e += stack(c1, c2);
+            pd.stacked += 1;
+        }
+        else {
+            pot_violated = true;
+            return;
+        }
+        if (k == -1) {
+            backward_triplets(c1, c2);
+            backward_single_junction(c1, c2);
+        }
+        else {
+            forward_triplets(c1, c2);
+            forward_single_junction(c1, c2);
+        }
+    }
+
+    __device__ __noinline__ void doubly_contig_junction_pair(int c1, int c2, int jj) {   // :359
+        int k1 = c1, k2 = c2;
+        V3 ndr = sub(pos(k2), pos(k1));
+        if (!eq(orev(k1), ndr)) {
+            pot_violated = true;
+            return;
+        }
+        if (jj == 1) return;
+        for (int a = 0; a < 2; ++a) {
+            int j1 = a == 0 ? next(c1, -1) : next(bnd[c1], 1);
+            int j2 = a == 0 ? c1 : bnd[c1];
+            int j3 = k2, j4 = next(k2, 1);
+            if (exists_bound(j4) && exists_bound(j1)) junction(j1, j2, j3, j4, k1, k2);
+            j3 = bnd[k2];
+            j4 = next(j3, -1);
+            if (exists_bound(j4) && exists_bound(j1)) junction(j1, j2, j3, j4, k1, k2);
+        }
+    }
+
+    __device__ __noinline__ void junction(int j1, int j2, int j3, int j4, int k1, int k2) {   // :419
+        if (sd[k1] > sd[k2]) {
+            int t = k1; k1 = k2; k2 = t;
+            t = j1; j1 = j4; j4 = t;
+            t = j2; j2 = j3; j3 = t;
+        }
+        if (!(pair_stacked(j1, j2) && pair_stacked(j3, j4))) return;
+        if (!junction_ok(j1, j2, k1, k2)) {
+            pot_violated = true;
+            return;
+        }
+        int pen = junction_penalty(j1, j2, j3, j4, k1, k2);
+        if (pen == 1) {
+            pd.e -= stack(j1, j2) / 2;
+            pd.e -= stack(j3, j4) / 2;
+            pd.stacked -= 1;
+        }
+        else if (pen == 2) {
+            pd.e -= stack(j1, j2);
+            pd.e -= stack(j3, j4);
+            pd.stacked -= 2;
+        }
+    }
+
+    __device__ __noinline__ void backward_triplets(int c1, int c2) {   // :464
+        int h2 = c1, h3 = c2;
+        if (!pair_stacked(h2, h3)) return;
+        int h1 = next(c1, -1);
+        bool h23_dc = doubly_contig(h2, h3);
+        if (exists_bound(h1)) {
+            bool h12_dc = doubly_contig(h1, h2);
+            if (pair_stacked(h1, h2)) {
+                if (h12_dc && h23_dc) {
+                    triply_contig_helix(h1, h2, h3);
+                    if (pot_violated) return;
+                }
+                triplet_double(h1, h2, h3);
+            }
+            else {
+                triplet_single(h1, h2, h3);
+            }
+        }
+        int h2_prev = h1;
+        int b1 = bnd[c1];
+        h1 = next(b1, 1);
+        if (exists_bound(h1) && bnd[h1] != h2_prev && bnd[h1] != h3) {
+            if (pair_stacked(b1, h1)) triplet_double(h1, h2, h3);
+        }
+        h1 = next(b1, -1);
+        if (exists_bound(h1) && bnd[h1] != h2_prev && bnd[h1] != h3) {
+            if (pair_stacked(h1, b1)) triplet_double(h1, h2, h3);
+            else triplet_single(h1, b1, h3);
+        }
+    }
+
+    __device__ __noinline__ void forward_triplets(int c1, int c2) {   // :521
+        int h2 = c2, h1 = c1;
+        bool first = pair_stacked(h1, h2);
+        int h3 = next(c2, 1);
+        bool h12_dc = doubly_contig(h1, h2);
+        if (exists_bound(h3)) {
+            bool second = pair_stacked(h2, h3);
+            if (first && second) {
+                bool h23_dc = doubly_contig(h2, h3);
+                if (h12_dc && h23_dc) {
+                    triply_contig_helix(h1, h2, h3);
+                    if (pot_violated) return;
+                }
+                triplet_double(h1, h2, h3);
+            }
+            else if (second) {
+                triplet_single(h1, h2, h3);
+            }
+        }
+        int h2_next = h3;
+        int b2 = bnd[c2];
+        h3 = next(b2, 1);
+        if (exists_bound(h3) && bnd[h3] != h2_next && bnd[h3] != h1) {
+            if (pair_stacked(b2, h3)) {
+                if (first) triplet_double(h1, h2, h3);
+                else triplet_single(h1, h2, h3);
+            }
+        }
+        h3 = next(b2, -1);
+        if (exists_bound(h3) && bnd[h3] != h2_next && bnd[h3] != h1) {
+            if (pair_stacked(h3, b2)) {
+                if (first) triplet_double(h1, h2, h3);
+                else triplet_single(h1, h2, h3);
+            }
+            else if (first) {
+                triplet_single(h3, b2, h1);
+            }
+        }
+    }
+
+    __device__ __noinline__ void central_triplets(int i, int j) {   // :587
+        int h1 = next(i, -1);
+        int h2 = i;
+        int h3 = next(j, 1);
+        int h2_next = next(i, 1);
+        if (exists_bound(h1) && exists_bound(h3) && bnd[h3] != h2_next && !doubly_contig(h1, h2)) {
+            if (pair_stacked(j, h3)) {
+                if (pair_stacked(h1, h2)) triplet_double(h1, h2, h3);
+                else triplet_single(h1, h2, h3);
+            }
+        }
+        h3 = next(j, -1);
+        if (exists_bound(h1) && exists_bound(h3) && bnd[h3] != h1 && !doubly_contig(h1, h2)) {
+            if (pair_stacked(h1, h2)) {
+                if (pair_stacked(h3, j)) triplet_double(h1, h2, h3);
+                else triplet_single(h3, j, h1);
+            }
+            else if (pair_stacked(h3, j)) {
+                triplet_single(h1, h2, h3);
+            }
+        }
+        h2 = i;
+        h3 = next(i, 1);
+        h1 = next(j, 1);
+        int h2_prev = next(i, -1);
+        if (exists_bound(h1) && exists_bound(h3) && bnd[h1] != h3 && !doubly_contig(h2, h3)) {
+            if (pair_stacked(j, h1) && pair_stacked(h2, h3)) triplet_double(h1, h2, h3);
+        }
+        h1 = next(j, -1);
+        if (exists_bound(h1) && exists_bound(h3) && bnd[h1] != h2_prev && !doubly_contig(h2, h3)) {
+            if (pair_stacked(h2, h3)) {
+                if (pair_stacked(h1, j)) triplet_double(h1, h2, h3);
+                else triplet_single(h1, j, h3);
+            }
+        }
+    }
+
+    // The three single-junction searches (:654, :750, :846) share one shape:
+    // up to three kink pairs, then up to three second junction pairs each.
+    __device__ __noinline__ void backward_single_junction(int c1, int c2) {   // :654
+        int j3 = c1, j4 = c2;
+        int fa[3], fb[3];
+        int nf = 0;
+        int j3_bac = bwd(j3);
+        fa[nf] = j3; fb[nf] = j3_bac; nf++;
+        int j3_b = bnd[j3];
+        int j3_b_for = fwd(j3_b), j3_b_bac = bwd(j3_b);
+        if (j3_b_for == bnd[j4]) {
+            fa[nf] = j3_b; fb[nf] = j3_b_bac; nf++;
+        }
+        else if (exists_bound(j3_bac) && exists_bound(j3_b_bac) && bnd[j3_bac] == j3_b_bac) {
+            fa[nf] = j3_b; fb[nf] = j3_b_for; nf++;
+        }
+        else if (exists_bound(j3_bac) && exists_bound(j3_b_for) && bnd[j3_bac] == j3_b_for) {
+            fa[nf] = j3_b; fb[nf] = j3_b_bac; nf++;
+        }
+        else {
+            fa[nf] = j3_b; fb[nf] = j3_b_for; nf++;
+            fa[nf] = j3_b; fb[nf] = j3_b_bac; nf++;
+        }
+        for (int a = 0; a < nf; ++a) {
+            int k2 = fa[a], k1 = fb[a];
+            if (!exists_bound(k1)) continue;
+            if (pair_stacked(k1, k2)) continue;
+            int sa[3], sb[3];
+            int ns_ = 0;
+            int dir = sd[k1] - sd[k2];
+            int k1_next = next(k1, dir);
+            sa[ns_] = k1; sb[ns_] = k1_next; ns_++;
+            int k1_b = bnd[k1];
+            int k1_b_for = fwd(k1_b), k1_b_bac = bwd(k1_b);
+            if (exists_bound(k1_next)) {
+                int kn_b = bnd[k1_next];
+                if (k1_b_for != kn_b) { sa[ns_] = k1_b; sb[ns_] = k1_b_for; ns_++; }
+                if (k1_b_bac != kn_b) { sa[ns_] = k1_b; sb[ns_] = k1_b_bac; ns_++; }
+            }
+            else {
+                sa[ns_] = k1_b; sb[ns_] = k1_b_for; ns_++;
+                sa[ns_] = k1_b; sb[ns_] = k1_b_bac; ns_++;
+            }
+            for (int b = 0; b < ns_; ++b) {
+                int j2 = sa[b], j1 = sb[b];
+                if (!exists_bound(j1)) continue;
+                junction(j1, j2, j3, j4, k1, k2);
+            }
+        }
+    }
+
+    __device__ __noinline__ void forward_single_junction(int c1, int c2) {   // :750
+        int j1 = c1, j2 = c2;
+        int fa[3], fb[3];
+        int nf = 0;
+        int j2_for = fwd(j2);
+        fa[nf] = j2; fb[nf] = j2_for; nf++;
+        int j1_b = bnd[j1];
+        int j2_b = bnd[j2];
+        int j2_b_for = fwd(j2_b), j2_b_bac = bwd(j2_b);
+        if (next(j1_b, 1) == j2_b) {
+            fa[nf] = j2_b; fb[nf] = j2_b_for; nf++;
+        }
+        else if (exists_bound(j2_for) && exists_bound(j2_b_bac) && bnd[j2_for] == j2_b_bac) {
+            fa[nf] = j2_b; fb[nf] = j2_b_for; nf++;
+        }
+        else if (exists_bound(j2_for) && exists_bound(j2_b_for) && bnd[j2_for] == j2_b_for) {
+            fa[nf] = j2_b; fb[nf] = j2_b_bac; nf++;
+        }
+        else {
+            fa[nf] = j2_b; fb[nf] = j2_b_for; nf++;
+            fa[nf] = j2_b; fb[nf] = j2_b_bac; nf++;
+        }
+        for (int a = 0; a < nf; ++a) {
+            int k1 = fa[a], k2 = fb[a];
+            if (!exists_bound(k2)) continue;
+            if (pair_stacked(k1, k2)) continue;
+            int sa[3], sb[3];
+            int ns_ = 0;
+            int dir = sd[k2] - sd[k1];
+            int k2_next = next(k2, dir);
+            sa[ns_] = k2; sb[ns_] = k2_next; ns_++;
+            int k2_b = bnd[k2];
+            int k2_b_for = fwd(k2_b), k2_b_bac = bwd(k2_b);
+            if (exists_bound(k2_next)) {
+                int kn_b = bnd[k2_next];
+                if (k2_b_for != kn_b) { sa[ns_] = k2_b; sb[ns_] = k2_b_for; ns_++; }
+                if (k2_b_bac != kn_b) { sa[ns_] = k2_b; sb[ns_] = k2_b_bac; ns_++; }
+            }
+            else {
+                sa[ns_] = k2_b; sb[ns_] = k2_b_for; ns_++;
+                sa[ns_] = k2_b; sb[ns_] = k2_b_bac; ns_++;
+            }
+            for (int b = 0; b < ns_; ++b) {
+                int j3 = sa[b], j4 = sb[b];
+                if (!exists_bound(j4)) continue;
+                junction(j1, j2, j3, j4, k1, k2);
+            }
+        }
+    }
+
+    __device__ __noinline__ void central_single_junction(int c1, int c2) {   // :846
+        int k1 = c1, k2 = c2;
+        int kb1 = bnd[k1], kb2 = bnd[k2];
+        int dd = sd[kb1] - sd[kb2];
+        if (scs[kb1] == scs[kb2] && (dd == 1 || dd == -1)) return;
+        int fa[3], fb[3];
+        int nf = 0;
+        int k1_bac = bwd(k1);
+        fa[nf] = k1; fb[nf] = k1_bac; nf++;
+        int k1_b_for = fwd(kb1), k1_b_bac = bwd(kb1);
+        if (exists_bound(k1_bac)) {
+            int kbb = bnd[k1_bac];
+            if (k1_b_for != kbb) { fa[nf] = kb1; fb[nf] = k1_b_for; nf++; }
+            if (k1_b_bac != kbb) { fa[nf] = kb1; fb[nf] = k1_b_bac; nf++; }
+        }
+        else {
+            fa[nf] = kb1; fb[nf] = k1_b_for; nf++;
+            fa[nf] = kb1; fb[nf] = k1_b_bac; nf++;
+        }
+        for (int a = 0; a < nf; ++a) {
+            int j2 = fa[a], j1 = fb[a];
+            if (!exists_bound(j1)) continue;
+            int sa[3], sb[3];
+            int ns_ = 0;
+            int k2_for = fwd(k2);
+            sa[ns_] = k2; sb[ns_] = k2_for; ns_++;
+            int k2_b_for = fwd(kb2), k2_b_bac = bwd(kb2);
+            if (exists_bound(k2_for)) {
+                int kfb = bnd[k2_for];
+                if (k2_b_for != kfb) { sa[ns_] = kb2; sb[ns_] = k2_b_for; ns_++; }
+                if (k2_b_bac != kfb) { sa[ns_] = kb2; sb[ns_] = k2_b_bac; ns_++; }
+            }
+            else {
+                sa[ns_] = kb2; sb[ns_] = k2_b_for; ns_++;
+                sa[ns_] = kb2; sb[ns_] = k2_b_bac; ns_++;
+            }
+            for (int b = 0; b < ns_; ++b) {
+                int j3 = sa[b], j4 = sb[b];
+                if (!exists_bound(j4)) continue;
+                junction(j1, j2, j3, j4, k1, k2);
+            }
+        }
+    }
+
+    // OrigamiPotential::bind_domain (:1282) with BindingPotential::bind_domains
+    // (:131) and the misbinding potentials (:938, :947)
+    __device__ __noinline__ Delta bind_domain(int i) {
+        pot_violated = false;
+        int j = bnd[i];
+        Delta dc;
+        dc.e = 0;
+        dc.stacked = 0;
+        if (did[i] == -did[j]) {
+            pd.e = 0;
+            pd.stacked = 0;
+            if (ore[i] != (ore[j] ^ 1)) {
+                pot_violated = true;
+                return dc;
+            }
+            stacking_and_steric(i, j);
+            if (pot_violated) return dc;
+            pd.e += hyb(i, j);
+            dc = pd;
+        }
+        else {
+            pot_violated = true;
+            if (sys->mis_disallowed) return dc;
+            if (ore[i] != (ore[j] ^ 1)) return dc;
+            pot_violated = false;
+            dc.e += hyb(i, j);
+        }
+        return dc;
+    }
+    __device__ __noinline__ Delta check_stacking(int i, int j) {   // :149
+        pd.e = 0;
+        pd.stacked = 0;
+        pot_violated = false;
+        stacking_and_steric(i, j);
+        return pd;
+    }
+
+    // ======================================== order parameters / biases ===
+    __device__ __noinline__ bool staple_type_fully_bound(int type) const {
+        int nc = h->n_chains;
+        for (int c = 1; c < nc; ++c) {
+            int cs = chain_order[c];
+            if (chain_type[cs] != type) continue;
+            int len = chain_len(cs);
+            bool full = true;
+            for (int d = 0; d < len; ++d)
+                if (st[slot_of(cs, d)] != BOUND) { full = false; break; }
+            if (full) return true;
+        }
+        return false;
+    }
+    // SystemOrderParams::update_move_params (src/order_params.cpp:595)
+    __device__ __noinline__ void update_move_params() {
+        const LdoSys* s = sys;
+        for (int q = 0; q < s->n_ops; ++q) {
+            int v = 0;
+            int defined = 1;
+            switch (s->op_kind[q]) {
+            case LDO_OP_NUMSTAPLES: v = h->num_staples; break;
+            case LDO_OP_NUMSTAPLESTYPE: v = type_count[s->op_arg[q]]; break;
+            case LDO_OP_STAPLETYPEFULLYBOUND: v = staple_type_fully_bound(s->op_arg[q]) ? 1 : 0; break;
+            case LDO_OP_NUMBOUND: v = h->num_fully; break;
+            case LDO_OP_NUMMISBOUND: v = h->num_bound - h->num_fully; break;
+            case LDO_OP_NUMSTACKED: v = h->num_stacked; break;
+            case LDO_OP_ZERO: v = 0; break;
+            case LDO_OP_SUM: {
+                for (int p = 0; p < s->op_nparts[q]; ++p) {
+                    int part = s->op_parts[q][p];
+                    if (op[2 * part + 1]) v += op[2 * part];
+                    else { defined = 0; v = op[2 * q]; break; }
+                }
+                break;
+            }
+            }
+            op[2 * q] = v;
+            op[2 * q + 1] = defined;
+        }
+    }
+    __device__ __noinline__ double bias_value(int b) const {
+        const LdoSys* s = sys;
+        int oq = s->bias_op[b];
+        if (!op[2 * oq + 1]) return 0;
+        int x = op[2 * oq];
+        switch (s->bias_kind[b]) {
+        case LDO_B_LINEARSTEPWELL: {   // src/bias_functions.cpp:139
+            int mn = ctl->win_min[b], mx = ctl->win_max[b];
+            if (x < mn) return s->bias_slope[b] * (mn - x - 1) + s->bias_minb[b];
+            if (x > mx) return s->bias_slope[b] * (x - mx - 1) + s->bias_minb[b];
+            return s->bias_well[b];
+        }
+        case LDO_B_SQUAREWELL: {   // :194
+            int mn = ctl->win_min[b], mx = ctl->win_max[b];
+            if (x < mn || x > mx) return s->bias_outside[b];
+            return s->bias_well[b];
+        }
+        case LDO_B_GRID: {   // :242
+            int off = ctl->grid_off[b];
+            if (off >= 0 && x >= 0 && x < s->bias_grid_len[b]) return grid[off + x];
+            return 0.0;
+        }
+        case LDO_B_HARMONIC: {
+            double dx = x - ctl->centre[b];
+            return 0.5 * s->bias_k[b] * dx * dx;
+        }
+        }
+        return 0;
+    }
+    // SystemBiases::calc_move (src/bias_functions.cpp:475)
+    __device__ __noinline__ double calc_move() {
+        double diff = 0;
+        for (int b = 0; b < sys->n_biases; ++b) {
+            double prev = bias[b];
+            double nb = bias_value(b);
+            bias[b] = nb;
+            diff += nb - prev;
+        }
+        h->move_bias += diff;
+        return diff * ctl->bias_mult;
+    }
+    __device__ __noinline__ void init_biases() {
+        update_move_params();
+        h->move_bias = 0;
+        for (int b = 0; b < sys->n_biases; ++b) {
+            bias[b] = bias_value(b);
+            h->move_bias += bias[b];
+        }
+    }
+
+    // ============================================================ moves ===
+    __device__ void reset_internal() {   // src/movetypes.cpp:242
+        m.n_mod = 0;
+        m.n_asg = 0;
+        m.added_cs = -1;
+        rejected = false;
+        modifier = 1;
+        delta_e = 0;
+        w_bias = 1;
+        w_new_bias = 1;
+        new_modifier = 1;
+        regrow_old = false;
+    }
+
+    __device__ __noinline__ void reset_origami() {   // src/movetypes.cpp:53
+        for (int n = 0; n < m.n_asg; ++n) unassign_domain(m.asg[n]);
+        if (m.added_cs >= 0) {
+            delete_chain(m.added_cs);
+            h->current_c_i -= 1;
+        }
+        for (int n = 0; n < m.n_mod; ++n) set_checked(m.mod[n], m.mod_pos[n], m.mod_ore[n]);
+        h->violated = 0;
+    }
+
+    __device__ __noinline__ bool test_acceptance(double p) {   // src/movetypes.cpp:142
+        double pa = fmin(1.0, p) * modifier;
+        if (pa == 1) return true;
+        return pa > rng.uniform_real();
+    }
+
+    __device__ __noinline__ int select_random_domain() {   // src/movetypes.cpp:98
+        int idx = rng.uniform_int(0, h->num_domains - 1);
+        int nc = h->n_chains;
+        for (int c = 0; c < nc; ++c) {
+            int cs = chain_order[c];
+            int len = chain_len(cs);
+            if (idx < len) return slot_of(cs, idx);
+            idx -= len;
+        }
+        return -1;
+    }
+
+    // staple_is_connector / scan_for_scaffold_domain (src/movetypes.cpp:160-232):
+    // reachability of the scaffold from the partner chain, not passing through
+    // the staple, over bound and misbound pairs.
+    __device__ __noinline__ bool staple_is_connector(int cs) {
+        int len = chain_len(cs);
+        for (int d = 0; d < len; ++d) {
+            int i = slot_of(cs, d);
+            if (st[i] == UNBOUND) continue;
+            int b = bnd[i];
+            if (b < 0) {
+                fail(LDO_RS_INVARIANT);
+                return false;
+            }
+            if (chain_c[scs[b]] == 0) continue;
+            if (!reaches_scaffold(scs[b], cs)) return true;
+        }
+        return false;
+    }
+    __device__ __noinline__ bool reaches_scaffold(int start, int excluded) {
+        unsigned long long seen = (1ull << excluded) | (1ull << start);
+        uint8_t stack_[LDO_MAX_KMAX + 1];
+        int sp = 0;
+        stack_[sp++] = (uint8_t)start;
+        while (sp > 0) {
+            int x = stack_[--sp];
+            int len = chain_len(x);
+            for (int d = 0; d < len; ++d) {
+                int b = bnd[slot_of(x, d)];
+                if (b < 0) continue;
+                int cx = scs[b];
+                if (cx == x) continue;
+                if (chain_c[cx] == 0) return true;
+                if (seen & (1ull << cx)) continue;
+                seen |= 1ull << cx;
+                stack_[sp++] = (uint8_t)cx;
+            }
+        }
+        return false;
+    }
+
+    __device__ __noinline__ int num_bound_staple_domains(int cs) const {   // src/movetypes.cpp:395
+        int n = 0, len = chain_len(cs);
+        for (int d = 0; d < len; ++d) {
+            int o = st[slot_of(cs, d)];
+            if (o == BOUND || o == MISBOUND) n++;
+        }
+        return n;
+    }
+
+    __device__ __noinline__ void find_bound_domains(int cs) {   // src/movetypes.cpp:258
+        m.n_bd = 0;
+        int len = chain_len(cs);
+        for (int d = 0; d < len; ++d) {
+            int i = slot_of(cs, d);
+            int b = bnd[i];
+            if (b >= 0 && scs[b] != cs) {
+                m.bd_new[m.n_bd] = i;
+                m.bd_old[m.n_bd] = b;
+                m.n_bd++;
+            }
+        }
+        if (m.n_bd == 0) fail(LDO_RS_INVARIANT);   // "System has unbound staple"
+    }
+
+    __device__ __noinline__ void unassign_domains(int cs) {   // src/met_movetypes.cpp:77
+        int len = chain_len(cs);
+        for (int d = 0; d < len; ++d) {
+            int i = slot_of(cs, d);
+            m.mod[m.n_mod] = i;
+            m.mod_pos[m.n_mod] = pos(i);
+            m.mod_ore[m.n_mod] = ore[i];
+            m.n_mod++;
+            double de = unassign_domain(i);
+            delta_e += de;
+        }
+    }
+
+    // RegrowthMCMovetype::set_growth_point (src/movetypes.cpp:322)
+    __device__ __noinline__ double set_growth_point(int gnew, int gold) {
+        double de = set_domain_config(gnew, pos(gold), ore[gold] ^ 1);
+        if (h->violated) rejected = true;
+        else m.asg[m.n_asg++] = gnew;
+        return de;
+    }
+
+    // MetMCMovetype::grow_chain (src/met_movetypes.cpp:50) over the domains
+    // d0, d0+dir, ... of chain slot cs (count of them, including d0).
+    __device__ __noinline__ void met_grow_chain(int cs, int d0, int dir, int count) {
+        for (int n = 1; n < count; ++n) {
+            int i = slot_of(cs, d0 + dir * n);
+            int prev = slot_of(cs, d0 + dir * (n - 1));
+            V3 p = add(pos(prev), unit(rng.uniform_int(0, 5)));
+            int o = rng.uniform_int(0, 5);
+            delta_e += set_domain_config(i, p, o);
+            if (h->violated) {
+                rejected = true;
+                break;
+            }
+            m.asg[m.n_asg++] = i;
+        }
+    }
+
+    // RegrowthMCMovetype::grow_staple (src/movetypes.cpp:343)
+    __device__ __noinline__ void grow_staple(int d_i, int cs, bool cb) {
+        int len = chain_len(cs);
+        int n3 = len - d_i;
+        if (n3 > 1) {
+            if (cb) cb_grow_chain(cs, d_i, 1, n3);
+            else met_grow_chain(cs, d_i, 1, n3);
+        }
+        if (rejected || bad()) return;
+        int n5 = d_i + 1;
+        if (n5 > 1) {
+            if (cb) cb_grow_chain(cs, d_i, -1, n5);
+            else met_grow_chain(cs, d_i, -1, n5);
+        }
+    }
+
+    __device__ void add_external_bias_met() {   // src/met_movetypes.cpp:69
+        update_move_params();
+        delta_e += calc_move();
+    }
+
+    __device__ __noinline__ bool exchange_accept_common(int type, double pratio) {   // src/met_movetypes.cpp:227-252
+        if (staple_bound) {
+            modifier *= sys->exchange_mults[type - 1];
+            if (modifier * fmin(1.0, pratio) > 1) {
+                if (sys->adaptive_exchange) return false;
+                if (sys->allow_nonsensical) return true;
+                fail(LDO_RS_INVARIANT);   // "Nonsensical exchange probability detected"
+                return false;
+            }
+        }
+        return test_acceptance(pratio);
+    }
+
+    // MetStapleExchangeMCMovetype::insert_staple (src/met_movetypes.cpp:303)
+    __device__ __noinline__ bool insert_staple() {
+        int S = sys->n_types - 1;
+        int type = rng.uniform_int(1, S);
+        if (h->num_staples == sys->max_total_staples) return false;
+        if (type_count[type] == sys->max_type_staples) return false;
+        int cs = add_chain(type);
+        if (cs < 0) return false;
+        if (mean_field) delta_e += log6;
+        delta_e += tab->init_e;
+        m.added_cs = cs;
+        int len = chain_len(cs);
+        int gi = rng.uniform_int(0, len - 1);
+        int gnew = slot_of(cs, gi);
+        int gold = select_random_domain();
+        int guard = 0;
+        while (scs[gold] == cs) {
+            gold = select_random_domain();
+            if (++guard > LDO_GROWTHPOINT_CAP) {
+                fail(LDO_RS_ITERCAP);
+                return false;
+            }
+        }
+        delta_e += set_growth_point(gnew, gold);
+        if (rejected || bad()) return false;
+        grow_staple(gi, cs, false);
+        if (rejected || bad()) return false;
+        for (int d = 0; d < len; ++d)
+            if (st[slot_of(cs, d)] == BOUND) { staple_bound = true; break; }
+        int nbd = num_bound_staple_domains(cs);
+        add_external_bias_met();
+        double boltz = exp(-delta_e);
+        int ni = type_count[type];
+        double pratio = (double)len / 6.0 / ni * boltz;
+        pratio *= insertion_sites * ctl->staple_M;
+        pratio /= nbd;
+        return exchange_accept_common(type, pratio);
+    }
+
+    // MetStapleExchangeMCMovetype::delete_staple (src/met_movetypes.cpp:361)
+    __device__ __noinline__ bool delete_staple() {
+        int S = sys->n_types - 1;
+        int type = rng.uniform_int(1, S);
+        int n = type_count[type];
+        if (n == 0) {
+            rejected = true;
+            return false;
+        }
+        int which = rng.uniform_int(0, n - 1);
+        int cs = -1;
+        for (int c = 1; c < h->n_chains; ++c) {
+            int x = chain_order[c];
+            if (chain_type[x] == type) {
+                if (which == 0) { cs = x; break; }
+                --which;
+            }
+        }
+        if (cs < 0) {
+            fail(LDO_RS_INVARIANT);
+            return false;
+        }
+        if (staple_is_connector(cs)) return false;
+        int len = chain_len(cs);
+        for (int d = 0; d < len; ++d)
+            if (st[slot_of(cs, d)] == BOUND) { staple_bound = true; break; }
+        int nbd = num_bound_staple_domains(cs);
+        unassign_domains(cs);
+        if (mean_field) delta_e -= log6;
+        delta_e -= tab->init_e;
+        h->num_staples--;
+        add_external_bias_met();
+        h->num_staples++;
+        double boltz = exp(-delta_e);
+        int ni = type_count[type];
+        double pratio = ni * 6.0 / (double)len * boltz;
+        pratio /= ctl->staple_M * (double)(unsigned long long)(insertion_sites - len);
+        pratio *= nbd;
+        bool acc = exchange_accept_common(type, pratio);
+        if (acc) delete_chain(cs);
+        return acc;
+    }
+
+    __device__ __noinline__ bool met_exchange() {   // src/met_movetypes.cpp:192
+        insertion_sites = h->num_domains;
+        staple_bound = false;
+        if (rng.uniform_real() < 0.5) return insert_staple();
+        return delete_staple();
+    }
+
+    __device__ __noinline__ int pick_staple_chain() {   // uniform_int(1, num_staples) -> get_chains()[i]
+        int ci = rng.uniform_int(1, h->num_staples);
+        return chain_order[ci];
+    }
+
+    // MetStapleRegrowthMCMovetype::internal_attempt_move (src/met_movetypes.cpp:470)
+    __device__ __noinline__ bool met_regrowth() {
+        if (h->num_staples == 0) return false;
+        int cs = pick_staple_chain();
+        if (staple_is_connector(cs)) return false;
+        find_bound_domains(cs);
+        if (bad()) return false;
+        int g = rng.uniform_int(0, m.n_bd - 1);
+        int gnew = m.bd_new[g], gold = m.bd_old[g];
+        unassign_domains(cs);
+        delta_e += set_growth_point(gnew, gold);
+        if (rejected || bad()) return false;
+        grow_staple(sd[gnew], cs, false);
+        if (rejected || bad()) return false;
+        add_external_bias_met();
+        int nbd = num_bound_staple_domains(cs);
+        double boltz = exp(-(delta_e));
+        double pratio = boltz * (double)(unsigned long long)m.n_bd / nbd;
+        return test_acceptance(pratio);
+    }
+
+    // CBMCMovetype::select_and_set_config (src/cb_movetypes.cpp:104) with
+    // calc_biases (:58) and CBStapleRegrowthMCMovetype::calc_bias (:363)
+    __device__ __noinline__ void cb_select_and_set(int dom, int prev) {
+        V3 p_prev = pos(prev);
+        V3 cpos[6];
+        int core[6];
+        double bf[6];
+        int nc = 0;
+        for (int v = 0; v < 6; ++v) {
+            V3 p = add(p_prev, unit(v));
+            int occ = occupancy(p);
+            if (occ == BOUND || occ == MISBOUND) continue;
+            if (occ == UNBOUND) {
+                int ud = unbound_at(p);
+                int o = ore[ud] ^ 1;
+                double de = check_domain_constraints(dom, p, o);
+                if (!h->violated) {
+                    cpos[nc] = p;
+                    core[nc] = o;
+                    double b = 1;
+                    b *= exp(-de);
+                    bf[nc] = b;
+                    nc++;
+                }
+                else {
+                    h->violated = 0;
+                }
+            }
+            else {
+                cpos[nc] = p;
+                core[nc] = -1;
+                double de = check_domain_constraints(dom, p, 0);
+                bf[nc] = 6 * exp(-de);
+                nc++;
+            }
+            if (bad()) return;
+        }
+        double ros = 0;
+        for (int n = 0; n < nc; ++n) ros += bf[n];
+        if (ros == 0) {
+            rejected = true;
+            return;
+        }
+        w_bias *= ros;
+        if (!regrow_old) {
+            V3 p = mk(0, 0, 0);
+            int o = -1;
+            double cum = 0;
+            double r = rng.uniform_real();
+            for (int n = 0; n < nc; ++n) {
+                cum += bf[n] / ros;
+                if (r < cum) {
+                    p = cpos[n];
+                    o = core[n];
+                    break;
+                }
+            }
+            if (o < 0) o = rng.uniform_int(0, 5);
+            set_checked(dom, p, o);
+        }
+        else {
+            int n = 0;
+            while (n < m.n_old && m.old_slot[n] != dom) ++n;
+            set_checked(dom, m.old_pos[n], m.old_ore[n]);
+        }
+        m.asg[m.n_asg++] = dom;
+    }
+
+    __device__ __noinline__ void cb_grow_chain(int cs, int d0, int dir, int count) {   // src/cb_movetypes.cpp:354
+        for (int n = 1; n < count; ++n) {
+            cb_select_and_set(slot_of(cs, d0 + dir * n), slot_of(cs, d0 + dir * (n - 1)));
+            if (rejected || bad()) break;
+        }
+    }
+
+    __device__ __noinline__ void cb_set_gp_and_grow(int gnew, int gold, int cs) {   // src/cb_movetypes.cpp:389
+        if (regrow_old) {
+            int n = 0;
+            while (n < m.n_old && m.old_slot[n] != gnew) ++n;
+            double de = 0;
+            de += set_checked(gnew, pos(gold), m.old_ore[n]);
+            w_bias *= exp(-de);
+            m.asg[m.n_asg++] = gnew;
+        }
+        else {
+            double de = set_growth_point(gnew, gold);
+            w_bias *= exp(-de);
+        }
+        if (!rejected && !bad()) grow_staple(sd[gnew], cs, true);
+    }
+
+    // CBStapleRegrowthMCMovetype::internal_attempt_move (src/cb_movetypes.cpp:292)
+    __device__ __noinline__ bool cb_regrowth() {
+        if (h->num_staples == 0) return false;
+        int cs = pick_staple_chain();
+        if (staple_is_connector(cs)) return false;
+        find_bound_domains(cs);
+        if (bad()) return false;
+        w_bias *= (double)(unsigned long long)m.n_bd;
+        int g = rng.uniform_int(0, m.n_bd - 1);
+        unassign_domains(cs);
+        cb_set_gp_and_grow(m.bd_new[g], m.bd_old[g], cs);
+        if (rejected || bad()) return false;
+        w_bias /= num_bound_staple_domains(cs);
+        update_move_params();
+        double tb = calc_move();
+        w_bias *= exp(-tb);
+        // setup_for_regrow_old (:215)
+        regrow_old = true;
+        w_new_bias = w_bias;
+        new_modifier = modifier;
+        w_bias = 1;
+        m.n_old = m.n_mod;
+        for (int n = 0; n < m.n_mod; ++n) {
+            m.old_slot[n] = m.mod[n];
+            m.old_pos[n] = m.mod_pos[n];
+            m.old_ore[n] = m.mod_ore[n];
+        }
+        m.n_mod = 0;
+        m.n_asg = 0;
+        g = rng.uniform_int(0, m.n_bd - 1);
+        unassign_domains(cs);
+        cb_set_gp_and_grow(m.bd_new[g], m.bd_old[g], cs);
+        if (bad()) return false;
+        modifier = new_modifier;
+        // test_cb_acceptance (:182)
+        double ratio = w_new_bias / w_bias;
+        if (test_acceptance(ratio)) {
+            reset_origami();
+            update_move_params();
+            calc_move();
+            return true;
+        }
+        m.n_mod = 0;
+        m.n_asg = 0;
+        return false;
+    }
+
+    // OrientationRotationMCMovetype::internal_attempt_move (src/orientation_movetype.cpp:30)
+    __device__ __noinline__ bool orientation_rotation() {
+        int dom = select_random_domain();
+        int o_new = rng.uniform_int(0, 5);
+        bool acc = false;
+        if (st[dom] == BOUND || st[dom] == MISBOUND) {
+            double de = 0;
+            int o_old = ore[dom];
+            int bd = bnd[dom];
+            de += unassign_domain(bd);
+            set_domain_orientation(dom, o_new);
+            V3 p = pos(dom);
+            de += set_domain_config(bd, p, o_new ^ 1);
+            if (!h->violated) acc = test_acceptance(exp(-de));
+            if (!acc) {
+                unassign_domain(bd);
+                set_domain_orientation(dom, o_old);
+                set_checked(bd, p, o_old ^ 1);
+            }
+        }
+        else {
+            set_domain_orientation(dom, o_new);
+            acc = true;
+        }
+        return acc;
+    }
+
+    // GCMCSimulation::simulate, one step (src/simulation.cpp:575-619)
+    __device__ __noinline__ void step(long long s) {
+        double r = rng.uniform_real();
+        int nm = sys->n_moves;
+        int mv = 0;
+        while (mv < nm && !(r < sys->move_cum[mv])) ++mv;
+        if (mv == nm) {
+            fail(LDO_RS_INVARIANT);
+            return;
+        }
+        reset_internal();
+        bool acc = false;
+        switch (sys->move_kind[mv]) {
+        case LDO_MV_ORIENT: acc = orientation_rotation(); break;
+        case LDO_MV_MET_EXCHANGE: acc = met_exchange(); break;
+        case LDO_MV_MET_REGROWTH: acc = met_regrowth(); break;
+        case LDO_MV_CB_REGROWTH: acc = cb_regrowth(); break;
+        }
+        if (bad()) return;
+        mstat[2 * mv] += 1;
+        if (acc) mstat[2 * mv + 1] += 1;
+        else {
+            reset_origami();
+            update_move_params();
+            calc_move();
+        }
+        if (sys->centering_freq != 0 && s % sys->centering_freq == 0) center(sys->centering_domain);
+        if (sys->constraint_check_freq != 0 && s % sys->constraint_check_freq == 0) check_all_constraints();
+    }
+};
+
+} // namespace ldo

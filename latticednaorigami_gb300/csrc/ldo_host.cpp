@@ -1,0 +1,1069 @@
+// Host side of the engine: reads the reference's input files, builds the
+// device descriptors and energy tables, lays out one state region per
+// replica, launches the kernels and implements the C ABI of include/ldo.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/ldo.h"
+#include "ldo_io.hpp"
+#include "ldo_kernels.h"
+#include "ldo_tables.hpp"
+
+namespace {
+
+using std::string;
+using std::vector;
+
+thread_local string g_create_err;
+
+struct LdoError : std::runtime_error {
+    ldo_status code;
+    LdoError(ldo_status c, const string& m): std::runtime_error(m), code(c) {}
+};
+
+#define CU(x)                                                                                   \
+    do {                                                                                        \
+        cudaError_t e_ = (x);                                                                   \
+        if (e_ != cudaSuccess) throw LdoError(LDO_ECUDA, string(#x) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T>
+struct DevBuf {
+    T* p {nullptr};
+    size_t n {0};
+    void alloc(size_t count) {
+        free();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            throw LdoError(LDO_ENOMEM, string("cudaMalloc: ") + cudaGetErrorString(e));
+        }
+        n = count;
+    }
+    void free() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~DevBuf() { free(); }
+};
+
+int move_kind(const string& t) {
+    if (t == "OrientationRotation") return LDO_MV_ORIENT;
+    if (t == "MetStapleExchange") return LDO_MV_MET_EXCHANGE;
+    if (t == "MetStapleRegrowth") return LDO_MV_MET_REGROWTH;
+    if (t == "CBStapleRegrowth") return LDO_MV_CB_REGROWTH;
+    if (t == "CTCBScaffoldRegrowth" || t == "CTCBJumpScaffoldRegrowth" || t == "CTRGScaffoldRegrowth" ||
+        t == "CTRGJumpScaffoldRegrowth" || t == "CTCBLinkerRegrowth" || t == "CTCBClusteredLinkerRegrowth" ||
+        t == "CTRGLinkerRegrowth" || t == "CTRGClusteredLinkerRegrowth")
+        throw LdoError(LDO_EINVAL, t + ": scaffold movetypes are not implemented by this engine");
+    throw LdoError(LDO_EINVAL, t + ": no such movetype");
+}
+
+// One input system (one .inp file) on the host.
+struct HostSystem {
+    ldo_io::Params p;
+    ldo_io::SystemFile sf;
+    vector<ldo_io::MoveSpec> moves;
+    vector<ldo_io::OpSpec> ops;
+    vector<ldo_io::BiasSpec> biases;
+    LdoSys desc {};
+    ldo_host::EnergyInputs energy;
+};
+
+HostSystem load_system(const string& inp, const string& overrides) {
+    HostSystem hs;
+    ldo_io::Params& p = hs.p;
+    try {
+        p = ldo_io::read_inp(inp);
+        if (!overrides.empty()) {
+            std::istringstream is(overrides);
+            string line;
+            while (std::getline(is, line)) {
+                auto h = line.find('#');
+                if (h != string::npos) line = line.substr(0, h);
+                auto eq = line.find('=');
+                if (eq == string::npos) continue;
+                ldo_io::set_param(p, ldo_io::trim(line.substr(0, eq)), ldo_io::trim(line.substr(eq + 1)));
+            }
+        }
+        if (!p.restart_traj_file.empty())
+            throw LdoError(LDO_EINVAL, "restart_traj_file: restart from a trajectory is not implemented by this engine");
+        hs.sf = ldo_io::read_system(ldo_io::resolve(p, p.origami_input_filename));
+        hs.moves = ldo_io::read_movetypes(ldo_io::resolve(p, p.movetype_file));
+        if (!p.order_parameter_file.empty()) hs.ops = ldo_io::read_ops(ldo_io::resolve(p, p.order_parameter_file));
+        if (!p.bias_functions_file.empty())
+            hs.biases = ldo_io::read_biases(ldo_io::resolve(p, p.bias_functions_file));
+    } catch (LdoError&) {
+        throw;
+    } catch (std::exception& e) {
+        throw LdoError(LDO_EINVAL, e.what());
+    }
+    if (p.domain_type != "HalfTurn" && p.domain_type != "ThreeQuarterTurn")
+        throw LdoError(LDO_EINVAL, p.domain_type + ": No such domain type");
+    if (p.binding_pot != "FourBody") throw LdoError(LDO_EINVAL, p.binding_pot + ": No such binding potential");
+    if (p.misbinding_pot != "Opposing" && p.misbinding_pot != "Disallowed")
+        throw LdoError(LDO_EINVAL, p.misbinding_pot + ": No such misbinding potential");
+    if (p.domain_update_biases_present)
+        throw LdoError(LDO_EINVAL, "domain_update_biases_present: per-domain biases are not implemented by this engine");
+
+    const auto& ids = hs.sf.identities;
+    if (ids.size() < 2) throw LdoError(LDO_EINVAL, "system needs a scaffold and at least one staple type");
+    if (ids.size() > LDO_MAX_TYPES) throw LdoError(LDO_EINVAL, "too many staple types");
+    if (hs.sf.chains.empty() || hs.sf.chains[0].identity != 0)
+        throw LdoError(LDO_EINVAL, "first configuration chain must be the scaffold");
+    LdoSys& d = hs.desc;
+    std::memset(&d, 0, sizeof d);
+    d.n_types = (int)ids.size();
+    d.ns = (int)ids[0].size();
+    d.lmax = 1;
+    int noff = 0;
+    for (size_t t = 0; t < ids.size(); ++t) {
+        d.type_len[t] = (int)ids[t].size();
+        d.type_off[t] = noff;
+        if (t > 0) d.lmax = std::max(d.lmax, (int)ids[t].size());
+        for (int x : ids[t]) {
+            if (noff >= LDO_MAX_IDENTS) throw LdoError(LDO_EINVAL, "too many domain identities");
+            d.idents[noff++] = (int16_t)x;
+            d.imax = std::max(d.imax, std::abs(x));
+        }
+    }
+    if (d.lmax > LDO_MAX_LEN) throw LdoError(LDO_EINVAL, "staples longer than 4 domains are not supported");
+    d.dim = 2 * d.imax + 1;
+    int kmax_default = std::min(LDO_MAX_KMAX, d.ns * 2);
+    d.kmax = std::min(p.max_total_staples, LDO_MAX_KMAX);
+    if (p.max_total_staples > LDO_MAX_KMAX) d.kmax = kmax_default;
+    if ((int)hs.sf.chains.size() - 1 > d.kmax)
+        throw LdoError(LDO_ECAPACITY, "initial configuration has more staples than staple slots");
+    d.dcap = d.ns + d.kmax * d.lmax;
+    if (d.dcap > 4000) throw LdoError(LDO_EINVAL, "system too large");
+    d.cyclic = hs.sf.cyclic;
+    d.tqt = p.domain_type == "ThreeQuarterTurn";
+    d.mis_disallowed = p.misbinding_pot == "Disallowed";
+    d.mean_field = p.apply_mean_field_cor;
+    d.max_total_staples = p.max_total_staples;
+    d.max_type_staples = p.max_type_staples;
+    if ((int)hs.moves.size() > LDO_MAX_MOVES) throw LdoError(LDO_EINVAL, "too many movetypes");
+    d.n_moves = (int)hs.moves.size();
+    double cum = 0;
+    for (int t = 0; t < LDO_MAX_TYPES; ++t) d.exchange_mults[t] = 1;
+    for (size_t m = 0; m < hs.moves.size(); ++m) {
+        d.move_kind[m] = move_kind(hs.moves[m].type);
+        cum += hs.moves[m].freq;
+        d.move_cum[m] = cum;
+        if (d.move_kind[m] == LDO_MV_MET_EXCHANGE) {
+            for (size_t t = 0; t < hs.moves[m].exchange_mults.size() && t < LDO_MAX_TYPES; ++t)
+                d.exchange_mults[t] = hs.moves[m].exchange_mults[t];
+            d.adaptive_exchange = hs.moves[m].adaptive_exchange;
+            if (d.adaptive_exchange)
+                for (size_t t = 0; t < hs.moves[m].exchange_mults.size(); ++t)
+                    if (hs.moves[m].exchange_mults[t] != 1)
+                        throw LdoError(LDO_EINVAL, "adaptive_exchange with exchange multipliers is not implemented");
+        }
+    }
+    d.allow_nonsensical = p.allow_nonsensical_ps;
+    if (hs.ops.size() > LDO_MAX_OPS) throw LdoError(LDO_EINVAL, "too many order parameters");
+    d.n_ops = (int)hs.ops.size();
+    d.fully_op = -1;
+    for (size_t q = 0; q < hs.ops.size(); ++q) {
+        const auto& o = hs.ops[q];
+        int k;
+        if (o.type == "NumStaples") k = LDO_OP_NUMSTAPLES;
+        else if (o.type == "NumStaplesType") k = LDO_OP_NUMSTAPLESTYPE;
+        else if (o.type == "StapleTypeFullyBound") k = LDO_OP_STAPLETYPEFULLYBOUND;
+        else if (o.type == "NumBoundDomainPairs") k = LDO_OP_NUMBOUND;
+        else if (o.type == "NumMisboundDomainPairs") k = LDO_OP_NUMMISBOUND;
+        else if (o.type == "NumStackedPairs") k = LDO_OP_NUMSTACKED;
+        else if (o.type == "NumLinearHelices" || o.type == "NumStackedJuncts") k = LDO_OP_ZERO;
+        else if (o.type == "Sum") k = LDO_OP_SUM;
+        else if (o.type == "Dist" || o.type == "AdjacentSite")
+            throw LdoError(LDO_EINVAL, o.type + ": per-domain order parameters are not implemented by this engine");
+        else throw LdoError(LDO_EINVAL, o.type + ": order parameter type does not exist");
+        d.op_kind[q] = k;
+        d.op_arg[q] = o.staple;
+        if (k == LDO_OP_NUMSTAPLESTYPE || k == LDO_OP_STAPLETYPEFULLYBOUND)
+            if (o.staple < 1 || o.staple >= d.n_types) throw LdoError(LDO_EINVAL, "order parameter staple out of range");
+        if (k == LDO_OP_NUMBOUND && d.fully_op < 0) d.fully_op = (int)q;
+        if (k == LDO_OP_SUM) {
+            if (o.ops.size() > LDO_MAX_PARTS) throw LdoError(LDO_EINVAL, "Sum over too many order parameters");
+            d.op_nparts[q] = (int)o.ops.size();
+            for (size_t a = 0; a < o.ops.size(); ++a) {
+                int idx = -1;
+                for (size_t r = 0; r < q; ++r)
+                    if (hs.ops[r].tag == o.ops[a]) idx = (int)r;
+                if (idx < 0) throw LdoError(LDO_EINVAL, "Sum order parameter: unknown tag " + o.ops[a]);
+                d.op_parts[q][a] = idx;
+            }
+        }
+    }
+    if (hs.biases.size() > LDO_MAX_BIASES) throw LdoError(LDO_EINVAL, "too many bias functions");
+    d.n_biases = (int)hs.biases.size();
+    for (size_t b = 0; b < hs.biases.size(); ++b) {
+        const auto& s = hs.biases[b];
+        if (s.type == "LinearStepWell") d.bias_kind[b] = LDO_B_LINEARSTEPWELL;
+        else if (s.type == "SquareWell") d.bias_kind[b] = LDO_B_SQUAREWELL;
+        else if (s.type == "Grid") d.bias_kind[b] = LDO_B_GRID;
+        else if (s.type == "Harmonic") d.bias_kind[b] = LDO_B_HARMONIC;
+        else throw LdoError(LDO_EINVAL, s.type + "; no such bias function type");
+        if (s.ops.size() != 1) throw LdoError(LDO_EINVAL, "bias functions over several order parameters are not implemented");
+        int idx = -1;
+        for (size_t r = 0; r < hs.ops.size(); ++r)
+            if (hs.ops[r].tag == s.ops[0]) idx = (int)r;
+        if (idx < 0) throw LdoError(LDO_EINVAL, "bias function " + s.tag + ": unknown order parameter " + s.ops[0]);
+        d.bias_op[b] = idx;
+        d.bias_nops[b] = 1;
+        d.bias_min[b] = s.min_op;
+        d.bias_max[b] = s.max_op;
+        d.bias_well[b] = s.well_bias;
+        d.bias_minb[b] = s.min_bias;
+        d.bias_slope[b] = s.slope;
+        d.bias_outside[b] = s.outside_bias;
+        d.bias_k[b] = s.k;
+        d.bias_centre[b] = s.centre;
+        d.bias_grid_len[b] = d.bias_kind[b] == LDO_B_GRID ? (d.ns + d.kmax * d.lmax + 1) : 0;
+    }
+    d.bias_mult = p.bias_functions_mult;
+    d.centering_freq = p.centering_freq;
+    d.centering_domain = p.centering_domain;
+    if (p.centering_domain < 0 || p.centering_domain >= d.ns) throw LdoError(LDO_EINVAL, "centering_domain out of range");
+    d.constraint_check_freq = p.constraint_check_freq;
+
+    ldo_host::EnergyInputs& en = hs.energy;
+    en.hybridization_pot = p.hybridization_pot;
+    en.stacking_pot = p.stacking_pot;
+    en.mean_field = p.apply_mean_field_cor;
+    en.temp = p.temp;
+    en.cation_M = p.cation_M;
+    en.stacking_ene = p.stacking_ene;
+    en.binding_h = p.binding_h;
+    en.binding_s = p.binding_s;
+    en.misbinding_h = p.misbinding_h;
+    en.misbinding_s = p.misbinding_s;
+    en.enthalpies = hs.sf.enthalpies;
+    en.entropies = hs.sf.entropies;
+    return hs;
+}
+
+int next_pow2(int x) {
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+LdoLayout make_layout(int dcap, int kmax, int ntypes, int nb, int nop, int nmv) {
+    LdoLayout y {};
+    int off = 0;
+    auto take = [&](int bytes, int align) {
+        off = (off + align - 1) / align * align;
+        int o = off;
+        off += bytes;
+        return o;
+    };
+    y.dcap = dcap;
+    y.kmax = kmax;
+    y.hcap = next_pow2(std::max(16, 2 * dcap));
+    y.ntypes = ntypes;
+    y.nb = nb;
+    y.nop = nop;
+    y.nmv = nmv;
+    y.o_hdr = take(sizeof(LdoHdr), 16);
+    y.o_hash = take(8 * y.hcap, 16);
+    y.o_bias = take(8 * std::max(nb, 1), 8);
+    y.o_mstat = take(8 * 2 * std::max(nmv, 1), 8);
+    y.o_chain_c = take(4 * (kmax + 1), 4);
+    y.o_op = take(4 * 2 * std::max(nop, 1), 4);
+    y.o_px = take(2 * dcap, 2);
+    y.o_py = take(2 * dcap, 2);
+    y.o_pz = take(2 * dcap, 2);
+    y.o_bound = take(2 * dcap, 2);
+    y.o_dident = take(2 * dcap, 2);
+    y.o_type_count = take(2 * ntypes, 2);
+    y.o_ore = take(dcap, 1);
+    y.o_state = take(dcap, 1);
+    y.o_slot_cs = take(dcap, 1);
+    y.o_slot_d = take(dcap, 1);
+    y.o_chain_type = take(kmax + 1, 1);
+    y.o_chain_order = take(kmax + 1, 1);
+    y.bytes = (off + 15) / 16 * 16;
+    return y;
+}
+
+} // namespace
+
+struct ldo_engine {
+    string err;
+    vector<HostSystem> systems;
+    vector<int> sys_of;
+    int n_rep {0};
+    uint32_t seed {0};
+    LdoLayout lay {};
+    int wpb {1};
+    cudaStream_t stream {nullptr};
+    cudaEvent_t ev0 {nullptr}, ev1 {nullptr};
+
+    vector<LdoSys> h_sys;
+    vector<LdoTab> h_tabs;
+    vector<double> h_bank;
+    std::map<std::tuple<int, double, double>, int> tab_index;
+    vector<LdoRepCtl> h_ctl;
+    vector<double> h_grid;
+    vector<double> temps, stack_mults, u_mults;
+
+    DevBuf<LdoSys> d_sys;
+    DevBuf<LdoTab> d_tabs;
+    DevBuf<double> d_bank;
+    DevBuf<LdoRepCtl> d_ctl;
+    DevBuf<double> d_grid;
+    DevBuf<unsigned char> d_arena;
+    DevBuf<int> d_status;
+    DevBuf<int16_t> d_samples;
+    DevBuf<double> d_trace;
+    int sample_interval {0}, sample_cap {0};
+    int n_trace {0}, trace_max {0};
+
+    // parallel tempering
+    int pt_rungs {0}, pt_q {0};
+    long long pt_swap_i {0};
+    DevBuf<double> d_slot_q, d_red_u, d_rep_q;
+    DevBuf<int> d_perm, d_tab_slot;
+    DevBuf<unsigned long long> d_pt_draws;
+    DevBuf<long long> d_pt_att, d_pt_acc;
+    cudaGraphExec_t pt_graph {nullptr};
+    LdoPT pt {};
+
+    ~ldo_engine() {
+        if (pt_graph) cudaGraphExecDestroy(pt_graph);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    int table_for(int s, double temp, double mult) {
+        auto key = std::make_tuple(s, temp, mult);
+        auto it = tab_index.find(key);
+        if (it != tab_index.end()) return it->second;
+        HostSystem& hs = systems[s];
+        ldo_host::EnergyInputs in = hs.energy;
+        in.temp = temp;
+        in.stacking_mult = mult;
+        ldo_host::Tables t;
+        try {
+            t = ldo_host::build_tables(hs.sf.identities, hs.sf.sequences, in);
+        } catch (std::exception& e) {
+            throw LdoError(LDO_EINVAL, e.what());
+        }
+        LdoTab d {};
+        d.dense = t.dense;
+        d.stack_dense = t.stack_dense;
+        d.off_e = (long long)h_bank.size();
+        h_bank.insert(h_bank.end(), t.e.begin(), t.e.end());
+        d.off_h = (long long)h_bank.size();
+        h_bank.insert(h_bank.end(), t.h.begin(), t.h.end());
+        d.off_s = (long long)h_bank.size();
+        h_bank.insert(h_bank.end(), t.s.begin(), t.s.end());
+        d.off_stack = -1;
+        if (t.stack_dense) {
+            d.off_stack = (long long)h_bank.size();
+            h_bank.insert(h_bank.end(), t.stack.begin(), t.stack.end());
+        }
+        d.stack_const = t.stack_const;
+        d.init_e = t.init_e;
+        d.init_h = t.init_h;
+        d.init_s = t.init_s;
+        d.temp = temp;
+        int idx = (int)h_tabs.size();
+        h_tabs.push_back(d);
+        tab_index[key] = idx;
+        return idx;
+    }
+
+    void upload_tables() {
+        d_tabs.alloc(h_tabs.size());
+        CU(cudaMemcpy(d_tabs.p, h_tabs.data(), h_tabs.size() * sizeof(LdoTab), cudaMemcpyHostToDevice));
+        d_bank.alloc(h_bank.size());
+        CU(cudaMemcpy(d_bank.p, h_bank.data(), h_bank.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    void upload_ctl() {
+        CU(cudaMemcpy(d_ctl.p, h_ctl.data(), h_ctl.size() * sizeof(LdoRepCtl), cudaMemcpyHostToDevice));
+    }
+    void upload_grid() {
+        if (h_grid.empty()) return;
+        CU(cudaMemcpy(d_grid.p, h_grid.data(), h_grid.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+
+    LdoLaunch launch_params(int mode, long long steps) {
+        LdoLaunch L {};
+        L.sys = d_sys.p;
+        L.tabs = d_tabs.p;
+        L.bank = d_bank.p;
+        L.ctl = d_ctl.p;
+        L.grid = d_grid.p;
+        L.arena = d_arena.p;
+        L.lay = lay;
+        L.n_rep = n_rep;
+        L.warps_per_block = wpb;
+        L.mode = mode;
+        L.want_dep = 0;
+        L.n_steps = steps;
+        L.sample_interval = sample_interval;
+        L.sample_cap = sample_cap;
+        L.samples = d_samples.p;
+        L.n_trace = n_trace;
+        L.trace_max = trace_max;
+        L.trace = d_trace.p;
+        return L;
+    }
+
+    void check_status() {
+        CU(cudaMemsetAsync(d_status.p, 0, sizeof(int), stream));
+        CU(ldo_launch_status(d_arena.p, lay.bytes, lay.o_hdr, n_rep, d_status.p, stream));
+        int st = 0;
+        CU(cudaMemcpyAsync(&st, d_status.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CU(cudaStreamSynchronize(stream));
+        if (st != 0) {
+            const char* what = st == LDO_EINVARIANT  ? "a replica reached a state the reference rejects (invariant)"
+                               : st == LDO_EITERCAP  ? "a replica hit an iteration cap"
+                               : st == LDO_ECAPACITY ? "a replica ran out of staple or lattice slots"
+                                                     : "replica error";
+            throw LdoError((ldo_status)st, what);
+        }
+    }
+
+    void init_arena() {
+        vector<unsigned char> host((size_t)n_rep * lay.bytes, 0);
+        for (int r = 0; r < n_rep; ++r) {
+            const HostSystem& hs = systems[sys_of[r]];
+            const LdoSys& d = hs.desc;
+            unsigned char* b = host.data() + (size_t)r * lay.bytes;
+            auto* h = reinterpret_cast<LdoHdr*>(b + lay.o_hdr);
+            auto* px = reinterpret_cast<int16_t*>(b + lay.o_px);
+            auto* py = reinterpret_cast<int16_t*>(b + lay.o_py);
+            auto* pz = reinterpret_cast<int16_t*>(b + lay.o_pz);
+            auto* bnd = reinterpret_cast<int16_t*>(b + lay.o_bound);
+            auto* did = reinterpret_cast<int16_t*>(b + lay.o_dident);
+            unsigned char* ore = b + lay.o_ore;
+            unsigned char* st = b + lay.o_state;
+            unsigned char* scs = b + lay.o_slot_cs;
+            unsigned char* sd = b + lay.o_slot_d;
+            auto* chain_c = reinterpret_cast<int32_t*>(b + lay.o_chain_c);
+            unsigned char* chain_type = b + lay.o_chain_type;
+            unsigned char* chain_order = b + lay.o_chain_order;
+            auto* type_count = reinterpret_cast<int16_t*>(b + lay.o_type_count);
+            for (int s = 0; s < lay.dcap; ++s) {
+                bnd[s] = -1;
+                if (s < d.ns) {
+                    scs[s] = 0;
+                    sd[s] = (unsigned char)s;
+                }
+                else if (s < d.dcap) {
+                    scs[s] = (unsigned char)(1 + (s - d.ns) / d.lmax);
+                    sd[s] = (unsigned char)((s - d.ns) % d.lmax);
+                }
+                else {
+                    scs[s] = 0xff;
+                    sd[s] = 0;
+                }
+            }
+            for (int k = 0; k <= lay.kmax; ++k) chain_type[k] = 0xff;
+            const auto& chains = hs.sf.chains;
+            int total = 0;
+            int maxc = 0;
+            for (size_t c = 0; c < chains.size(); ++c) {
+                const auto& ch = chains[c];
+                int cs = (int)c;
+                int type = ch.identity;
+                if (type < 0 || type >= d.n_types) throw LdoError(LDO_EINVAL, "chain identity out of range");
+                if (c == 0 && type != 0) throw LdoError(LDO_EINVAL, "first chain must be the scaffold");
+                if (c > 0 && type == 0) throw LdoError(LDO_EINVAL, "only the first chain may be the scaffold");
+                int len = d.type_len[type];
+                if ((int)ch.positions.size() != len) throw LdoError(LDO_EINVAL, "chain length does not match identity");
+                chain_c[cs] = ch.index;
+                chain_type[cs] = (unsigned char)type;
+                chain_order[c] = (unsigned char)cs;
+                type_count[type]++;
+                maxc = std::max(maxc, ch.index);
+                for (int dd = 0; dd < len; ++dd) {
+                    int s = cs == 0 ? dd : d.ns + (cs - 1) * d.lmax + dd;
+                    px[s] = (int16_t)ch.positions[dd][0];
+                    py[s] = (int16_t)ch.positions[dd][1];
+                    pz[s] = (int16_t)ch.positions[dd][2];
+                    const auto& o = ch.orientations[dd];
+                    int oi;
+                    if (o[0] == 1 && o[1] == 0 && o[2] == 0) oi = 0;
+                    else if (o[0] == -1 && o[1] == 0 && o[2] == 0) oi = 1;
+                    else if (o[0] == 0 && o[1] == 1 && o[2] == 0) oi = 2;
+                    else if (o[0] == 0 && o[1] == -1 && o[2] == 0) oi = 3;
+                    else if (o[0] == 0 && o[1] == 0 && o[2] == 1) oi = 4;
+                    else if (o[0] == 0 && o[1] == 0 && o[2] == -1) oi = 5;
+                    else throw LdoError(LDO_EINVAL, "orientation is not a unit lattice vector");
+                    ore[s] = (unsigned char)oi;
+                    st[s] = 0;
+                    did[s] = d.idents[d.type_off[type] + dd];
+                }
+                total += len;
+            }
+            // OrigamiSystem constructor bookkeeping before set_all_domains
+            // (src/origami_system.cpp:659-678)
+            h->n_chains = (int)chains.size();
+            h->num_domains = total;
+            h->num_unassigned = total;
+            h->num_staples = (int)chains.size() - 1;
+            h->current_c_i = maxc;
+            h->energy = 0;
+            unsigned long long nst = (unsigned long long)(chains.size() - 1);
+            if (d.mean_field) h->energy += nst * std::log(6);
+            h->energy += nst * h_tabs[h_ctl[r].tab].init_e;
+            h->tab = h_ctl[r].tab;
+        }
+        d_arena.alloc(host.size());
+        CU(cudaMemcpy(d_arena.p, host.data(), host.size(), cudaMemcpyHostToDevice));
+    }
+
+    void create(const vector<string>& inps, const string& overrides, const vector<int>& sys_of_replica,
+                uint32_t seed_) {
+        seed = seed_;
+        for (auto& f : inps) systems.push_back(load_system(f, overrides));
+        sys_of = sys_of_replica;
+        n_rep = (int)sys_of.size();
+        if (n_rep <= 0) throw LdoError(LDO_EINVAL, "need at least one replica");
+        int dcap = 0, kmax = 0, ntypes = 0, nb = 0, nop = 0, nmv = 0;
+        for (auto& hs : systems) {
+            dcap = std::max(dcap, hs.desc.dcap);
+            kmax = std::max(kmax, hs.desc.kmax);
+            ntypes = std::max(ntypes, hs.desc.n_types);
+            nb = std::max(nb, hs.desc.n_biases);
+            nop = std::max(nop, hs.desc.n_ops);
+            nmv = std::max(nmv, hs.desc.n_moves);
+        }
+        lay = make_layout(dcap, kmax, ntypes, nb, nop, nmv);
+        CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        CU(cudaEventCreate(&ev0));
+        CU(cudaEventCreate(&ev1));
+        // Warps per block: as many replicas as fit 48 KB, at most 4.
+        wpb = std::max(1, std::min(4, (int)(48 * 1024 / lay.bytes)));
+        for (auto& hs : systems) h_sys.push_back(hs.desc);
+        d_sys.alloc(h_sys.size());
+        CU(cudaMemcpy(d_sys.p, h_sys.data(), h_sys.size() * sizeof(LdoSys), cudaMemcpyHostToDevice));
+        h_ctl.resize(n_rep);
+        temps.resize(n_rep);
+        stack_mults.assign(n_rep, 1.0);
+        u_mults.resize(n_rep);
+        size_t grid_total = 0;
+        for (int r = 0; r < n_rep; ++r) {
+            int s = sys_of[r];
+            if (s < 0 || s >= (int)systems.size()) throw LdoError(LDO_EINVAL, "sys_of_replica out of range");
+            const HostSystem& hs = systems[s];
+            LdoRepCtl& c = h_ctl[r];
+            std::memset(&c, 0, sizeof c);
+            c.sys = s;
+            temps[r] = hs.p.temp;
+            u_mults[r] = hs.p.staple_u_mult;
+            c.tab = table_for(s, hs.p.temp, 1.0);
+            c.staple_M = hs.p.staple_M;
+            c.staple_u_mult = hs.p.staple_u_mult;
+            c.bias_mult = hs.p.bias_functions_mult;
+            for (int b = 0; b < LDO_MAX_BIASES; ++b) {
+                c.win_min[b] = hs.desc.bias_min[b];
+                c.win_max[b] = hs.desc.bias_max[b];
+                c.centre[b] = hs.desc.bias_centre[b];
+                c.grid_off[b] = -1;
+                if (b < hs.desc.n_biases && hs.desc.bias_kind[b] == LDO_B_GRID) {
+                    c.grid_off[b] = (int)grid_total;
+                    grid_total += hs.desc.bias_grid_len[b];
+                }
+            }
+            c.seed = seed;
+            c.rep = (uint32_t)r;
+        }
+        h_grid.assign(std::max<size_t>(grid_total, 1), 0.0);
+        d_grid.alloc(h_grid.size());
+        upload_grid();
+        d_ctl.alloc(n_rep);
+        upload_ctl();
+        upload_tables();
+        d_status.alloc(1);
+        init_arena();
+        LdoLaunch L = launch_params(LDO_MODE_INIT, 0);
+        CU(ldo_launch_mc(L, stream));
+        CU(cudaStreamSynchronize(stream));
+        check_status();
+    }
+
+    void run(long long steps, double* ms, int sweeps = 0) {
+        LdoLaunch L = launch_params(LDO_MODE_RUN, steps);
+        L.sweep_units = sweeps;
+        CU(cudaEventRecord(ev0, stream));
+        CU(ldo_launch_mc(L, stream));
+        CU(cudaEventRecord(ev1, stream));
+        CU(cudaStreamSynchronize(stream));
+        if (ms) {
+            float f = 0;
+            CU(cudaEventElapsedTime(&f, ev0, ev1));
+            *ms = f;
+        }
+        check_status();
+    }
+
+    // PTGCMCSimulation constructor + OneDPTGCMCSimulation::initialize_control_qs
+    // (src/ptmc_simulation.cpp:24-90, 337-358) for n_rep / n_rungs ladders.
+    void pt_setup(int n_rungs, int exchange_q) {
+        if (n_rungs < 2 || n_rep % n_rungs != 0) throw LdoError(LDO_EINVAL, "replicas must form whole ladders of n_rungs");
+        if (!(exchange_q & 1)) throw LdoError(LDO_EINVAL, "every exchange variant exchanges the temperature");
+        int nl = n_rep / n_rungs;
+        for (int r = 0; r < n_rep; ++r)
+            if (sys_of[r] != sys_of[(r / n_rungs) * n_rungs])
+                throw LdoError(LDO_EINVAL, "replicas of one ladder must share a system");
+        const HostSystem& hs = systems[sys_of[0]];
+        for (auto& s : systems)
+            if (&s != &hs && s.desc.n_types != hs.desc.n_types)
+                throw LdoError(LDO_EINVAL, "ladders must have the same staple types");
+        const ldo_io::Params& p = hs.p;
+        if ((int)p.temps.size() != n_rungs) throw LdoError(LDO_EINVAL, "temps must list one temperature per rung");
+        auto fill = [&](const vector<double>& v, const char* what) {
+            if (v.empty()) return vector<double>(n_rungs, 1.0);
+            if ((int)v.size() != n_rungs) throw LdoError(LDO_EINVAL, string(what) + " must list one value per rung");
+            return v;
+        };
+        vector<double> tq = p.temps;
+        vector<double> uq = fill(p.chem_pot_mults, "chem_pot_mults");
+        vector<double> bq = fill(p.bias_mults, "bias_mults");
+        vector<double> sq = fill(p.stacking_mults, "stacking_mults");
+        vector<double> slot(4 * n_rungs);
+        for (int k = 0; k < n_rungs; ++k) {
+            slot[k] = tq[k];
+            slot[n_rungs + k] = uq[k];
+            slot[2 * n_rungs + k] = bq[k];
+            slot[3 * n_rungs + k] = sq[k];
+        }
+        // m_reduced_staple_us from molarity_to_chempots at the input temperature
+        // (src/origami_system.cpp:965-989)
+        int S = hs.desc.n_types - 1;
+        vector<double> red(std::max(S, 1));
+        for (int t = 1; t <= S; ++t) {
+            double n = (double)hs.sf.identities[t].size();
+            double extra = (2 * n - 1) * std::log(6);
+            double u = p.temp * (std::log(p.staple_M) - extra);
+            red[t - 1] = u / p.temp;
+        }
+        vector<int> tab_slot(n_rungs);
+        for (int k = 0; k < n_rungs; ++k) tab_slot[k] = table_for(sys_of[0], tq[k], (exchange_q & 8) ? sq[k] : 1.0);
+        vector<double> rep_q(4 * n_rep);
+        vector<int> perm(n_rep);
+        for (int l = 0; l < nl; ++l)
+            for (int k = 0; k < n_rungs; ++k) {
+                int r = l * n_rungs + k;
+                perm[r] = r;
+                rep_q[4 * r] = tq[k];
+                rep_q[4 * r + 1] = uq[k];
+                rep_q[4 * r + 2] = bq[k];
+                rep_q[4 * r + 3] = sq[k];
+                temps[r] = tq[k];
+                stack_mults[r] = (exchange_q & 8) ? sq[k] : 1.0;
+                h_ctl[r].tab = tab_slot[k];
+                h_ctl[r].staple_u_mult = uq[k];
+            }
+        upload_tables();
+        upload_ctl();
+        d_slot_q.alloc(slot.size());
+        CU(cudaMemcpy(d_slot_q.p, slot.data(), slot.size() * sizeof(double), cudaMemcpyHostToDevice));
+        d_red_u.alloc(red.size());
+        CU(cudaMemcpy(d_red_u.p, red.data(), red.size() * sizeof(double), cudaMemcpyHostToDevice));
+        d_rep_q.alloc(rep_q.size());
+        CU(cudaMemcpy(d_rep_q.p, rep_q.data(), rep_q.size() * sizeof(double), cudaMemcpyHostToDevice));
+        d_perm.alloc(perm.size());
+        CU(cudaMemcpy(d_perm.p, perm.data(), perm.size() * sizeof(int), cudaMemcpyHostToDevice));
+        d_tab_slot.alloc(n_rungs);
+        CU(cudaMemcpy(d_tab_slot.p, tab_slot.data(), n_rungs * sizeof(int), cudaMemcpyHostToDevice));
+        d_pt_draws.alloc(nl);
+        CU(cudaMemset(d_pt_draws.p, 0, nl * sizeof(unsigned long long)));
+        d_pt_att.alloc(n_rungs);
+        d_pt_acc.alloc(n_rungs);
+        CU(cudaMemset(d_pt_att.p, 0, n_rungs * sizeof(long long)));
+        CU(cudaMemset(d_pt_acc.p, 0, n_rungs * sizeof(long long)));
+        pt = LdoPT {};
+        pt.n_ladders = nl;
+        pt.n_rungs = n_rungs;
+        pt.exchange_q = exchange_q;
+        pt.n_types = hs.desc.n_types;
+        pt.slot_temp = d_slot_q.p;
+        pt.slot_u = d_slot_q.p + n_rungs;
+        pt.slot_bias = d_slot_q.p + 2 * n_rungs;
+        pt.slot_stack = d_slot_q.p + 3 * n_rungs;
+        pt.red_u = d_red_u.p;
+        pt.perm = d_perm.p;
+        pt.rep_q = d_rep_q.p;
+        pt.tab_slot = d_tab_slot.p;
+        pt.ctl = d_ctl.p;
+        pt.arena = d_arena.p;
+        pt.lay = lay;
+        pt.draws = d_pt_draws.p;
+        pt.att = d_pt_att.p;
+        pt.acc = d_pt_acc.p;
+        pt.seed = seed;
+        pt_rungs = n_rungs;
+        pt_q = exchange_q;
+        pt_swap_i = 0;
+        if (pt_graph) {
+            cudaGraphExecDestroy(pt_graph);
+            pt_graph = nullptr;
+        }
+    }
+
+    // One PTGCMCSimulation::run iteration (src/ptmc_simulation.cpp:110-141):
+    // update_control_qs (energy recomputed with the slot's tables), simulate,
+    // update_dependent_qs, attempt_exchange.
+    void pt_round(long long swap_i, int exchange_interval) {
+        LdoLaunch L = launch_params(LDO_MODE_RUN, exchange_interval);
+        L.force_recompute = 1;
+        L.want_dep = 1;
+        CU(ldo_launch_mc(L, stream));
+        LdoPT P = pt;
+        P.swap_i = (int)(swap_i % 2);
+        CU(ldo_launch_pt_swap(P, stream));
+    }
+
+    void pt_run(int n_rungs, long long swaps, int exchange_interval, int exchange_q, double* ms) {
+        if (n_rungs != pt_rungs || exchange_q != pt_q) pt_setup(n_rungs, exchange_q);
+        if (swaps < 0 || exchange_interval < 0) throw LdoError(LDO_EINVAL, "negative swaps or interval");
+        CU(cudaEventRecord(ev0, stream));
+        long long done = 0;
+        // Rounds alternate even/odd pair sets; two rounds form one CUDA graph.
+        if (swaps >= 4) {
+            if (!pt_graph) {
+                cudaGraph_t g;
+                CU(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                pt_round(1, exchange_interval);
+                pt_round(2, exchange_interval);
+                CU(cudaStreamEndCapture(stream, &g));
+                CU(cudaGraphInstantiate(&pt_graph, g, 0));
+                cudaGraphDestroy(g);
+                pt_graph_interval = exchange_interval;
+            }
+            if (pt_graph_interval != exchange_interval) throw LdoError(LDO_EINVAL, "exchange interval changed");
+            // the graph starts with an odd round: align with the swap counter
+            if (pt_swap_i % 2 == 1) {
+                pt_round(pt_swap_i + 1, exchange_interval);
+                ++pt_swap_i;
+                ++done;
+            }
+            while (swaps - done >= 2) {
+                CU(cudaGraphLaunch(pt_graph, stream));
+                pt_swap_i += 2;
+                done += 2;
+            }
+        }
+        while (done < swaps) {
+            pt_round(pt_swap_i + 1, exchange_interval);
+            ++pt_swap_i;
+            ++done;
+        }
+        CU(cudaEventRecord(ev1, stream));
+        CU(cudaStreamSynchronize(stream));
+        if (ms) {
+            float f = 0;
+            CU(cudaEventElapsedTime(&f, ev0, ev1));
+            *ms = f;
+        }
+        // host mirror of the replicas' current temperatures
+        vector<double> rq(4 * n_rep);
+        CU(cudaMemcpy(rq.data(), d_rep_q.p, rq.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for (int r = 0; r < n_rep; ++r) temps[r] = rq[4 * r];
+        CU(cudaMemcpy(h_ctl.data(), d_ctl.p, h_ctl.size() * sizeof(LdoRepCtl), cudaMemcpyDeviceToHost));
+        check_status();
+    }
+    int pt_graph_interval {0};
+
+    vector<unsigned char> download_arena() {
+        vector<unsigned char> host((size_t)n_rep * lay.bytes);
+        CU(cudaMemcpy(host.data(), d_arena.p, host.size(), cudaMemcpyDeviceToHost));
+        return host;
+    }
+};
+
+namespace {
+
+ldo_status guard(ldo_engine* e, const std::function<void()>& f) {
+    try {
+        f();
+        if (e) e->err.clear();
+        return LDO_OK;
+    } catch (LdoError& x) {
+        if (e) e->err = x.what();
+        else g_create_err = x.what();
+        return x.code;
+    } catch (std::exception& x) {
+        if (e) e->err = x.what();
+        else g_create_err = x.what();
+        return LDO_EINVAL;
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+ldo_status ldo_create_multi(const char* const* inp_paths, int n_systems, const char* overrides,
+                            const int* sys_of_replica, int n_replicas, uint32_t seed, ldo_engine** out) {
+    if (!out || !inp_paths || n_systems <= 0 || n_replicas <= 0) {
+        g_create_err = "invalid arguments";
+        return LDO_EINVAL;
+    }
+    *out = nullptr;
+    auto* e = new ldo_engine;
+    vector<string> inps;
+    for (int i = 0; i < n_systems; ++i) inps.push_back(inp_paths[i]);
+    vector<int> so(n_replicas, 0);
+    if (sys_of_replica)
+        for (int r = 0; r < n_replicas; ++r) so[r] = sys_of_replica[r];
+    ldo_status st = guard(nullptr, [&]() { e->create(inps, overrides ? overrides : "", so, seed); });
+    if (st != LDO_OK) {
+        delete e;
+        return st;
+    }
+    *out = e;
+    return LDO_OK;
+}
+
+ldo_status ldo_create_from_inp(const char* inp_path, const char* overrides, int n_replicas, uint32_t seed,
+                               ldo_engine** out) {
+    const char* p[1] = {inp_path};
+    return ldo_create_multi(p, 1, overrides, nullptr, n_replicas, seed, out);
+}
+
+void ldo_destroy(ldo_engine* e) { delete e; }
+
+const char* ldo_last_error(const ldo_engine* e) { return e ? e->err.c_str() : g_create_err.c_str(); }
+
+int ldo_num_replicas(const ldo_engine* e) { return e ? e->n_rep : 0; }
+
+ldo_status ldo_run(ldo_engine* e, int64_t n_steps, double* device_ms) {
+    if (!e || n_steps < 0) return LDO_EINVAL;
+    return guard(e, [&]() { e->run(n_steps, device_ms); });
+}
+
+ldo_status ldo_run_sweeps(ldo_engine* e, int64_t n_sweeps, double* device_ms) {
+    if (!e || n_sweeps < 0) return LDO_EINVAL;
+    return guard(e, [&]() { e->run(n_sweeps, device_ms, 1); });
+}
+
+int ldo_state_bytes(const ldo_engine* e) { return e ? e->lay.bytes : 0; }
+
+ldo_status ldo_set_controls(ldo_engine* e, const double* temps, const double* stacking_mults,
+                            const double* staple_u_mults, int n) {
+    if (!e || n != e->n_rep) return LDO_EINVAL;
+    return guard(e, [&]() {
+        for (int r = 0; r < n; ++r) {
+            if (temps) e->temps[r] = temps[r];
+            if (stacking_mults) e->stack_mults[r] = stacking_mults[r];
+            if (staple_u_mults) e->u_mults[r] = staple_u_mults[r];
+            if (!(e->temps[r] > 0)) throw LdoError(LDO_EINVAL, "temperature must be positive");
+            e->h_ctl[r].tab = e->table_for(e->sys_of[r], e->temps[r], e->stack_mults[r]);
+            e->h_ctl[r].staple_u_mult = e->u_mults[r];
+        }
+        e->upload_tables();
+        e->upload_ctl();
+        LdoLaunch L = e->launch_params(LDO_MODE_RECOMPUTE, 0);
+        CU(ldo_launch_mc(L, e->stream));
+        CU(cudaStreamSynchronize(e->stream));
+        e->check_status();
+    });
+}
+
+ldo_status ldo_get_observables(ldo_engine* e, ldo_observables* out, int n) {
+    if (!e || !out || n > e->n_rep) return LDO_EINVAL;
+    return guard(e, [&]() {
+        LdoLaunch L = e->launch_params(LDO_MODE_RUN, 0);
+        L.want_dep = 1;
+        CU(ldo_launch_mc(L, e->stream));
+        CU(cudaStreamSynchronize(e->stream));
+        auto host = e->download_arena();
+        for (int r = 0; r < n; ++r) {
+            const auto* h = reinterpret_cast<const LdoHdr*>(host.data() + (size_t)r * e->lay.bytes + e->lay.o_hdr);
+            ldo_observables& o = out[r];
+            o.energy = h->energy;
+            o.total_bias = h->move_bias * e->h_ctl[r].bias_mult;
+            o.temp = e->temps[r];
+            o.enthalpy = h->H;
+            o.entropy = h->S;
+            o.stacking = h->stacking;
+            o.draws = (int64_t)h->draws;
+            o.num_staples = h->num_staples;
+            o.num_fully_bound = h->num_fully;
+            o.num_bound = h->num_bound;
+            o.num_self_bound = h->num_self;
+            o.num_stacked = h->num_stacked;
+            o.num_unassigned = h->num_unassigned;
+            o.current_c_i = h->current_c_i;
+            o.status = h->status;
+        }
+    });
+}
+
+ldo_status ldo_get_config(ldo_engine* e, int replica, int32_t* buf, int cap, int* written) {
+    if (!e || replica < 0 || replica >= e->n_rep || !buf) return LDO_EINVAL;
+    return guard(e, [&]() {
+        vector<unsigned char> b(e->lay.bytes);
+        CU(cudaMemcpy(b.data(), e->d_arena.p + (size_t)replica * e->lay.bytes, b.size(), cudaMemcpyDeviceToHost));
+        const LdoLayout& y = e->lay;
+        const LdoSys& d = e->systems[e->sys_of[replica]].desc;
+        const auto* h = reinterpret_cast<const LdoHdr*>(b.data() + y.o_hdr);
+        const auto* px = reinterpret_cast<const int16_t*>(b.data() + y.o_px);
+        const auto* py = reinterpret_cast<const int16_t*>(b.data() + y.o_py);
+        const auto* pz = reinterpret_cast<const int16_t*>(b.data() + y.o_pz);
+        const unsigned char* ore = b.data() + y.o_ore;
+        const unsigned char* st = b.data() + y.o_state;
+        const auto* chain_c = reinterpret_cast<const int32_t*>(b.data() + y.o_chain_c);
+        const unsigned char* chain_type = b.data() + y.o_chain_type;
+        const unsigned char* chain_order = b.data() + y.o_chain_order;
+        static const int U[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+        vector<int32_t> out;
+        out.push_back(h->n_chains);
+        for (int c = 0; c < h->n_chains; ++c) {
+            int cs = chain_order[c];
+            int type = cs == 0 ? 0 : chain_type[cs];
+            int len = d.type_len[type];
+            out.push_back(chain_c[cs]);
+            out.push_back(type);
+            out.push_back(len);
+            for (int dd = 0; dd < len; ++dd) {
+                int s = cs == 0 ? dd : d.ns + (cs - 1) * d.lmax + dd;
+                out.push_back(px[s]);
+                out.push_back(py[s]);
+                out.push_back(pz[s]);
+                out.push_back(U[ore[s]][0]);
+                out.push_back(U[ore[s]][1]);
+                out.push_back(U[ore[s]][2]);
+                out.push_back(st[s]);
+            }
+        }
+        if ((int)out.size() > cap) throw LdoError(LDO_EINVAL, "config buffer too small");
+        std::memcpy(buf, out.data(), out.size() * sizeof(int32_t));
+        if (written) *written = (int)out.size();
+    });
+}
+
+ldo_status ldo_set_sampling(ldo_engine* e, int interval, int capacity) {
+    if (!e || interval < 0 || capacity < 0) return LDO_EINVAL;
+    return guard(e, [&]() {
+        e->sample_interval = interval;
+        e->sample_cap = capacity;
+        e->d_samples.alloc((size_t)e->n_rep * std::max(capacity, 1) * 2);
+        CU(cudaMemset(e->d_samples.p, 0, e->d_samples.n * sizeof(int16_t)));
+        // restart the per-replica sample counters
+        auto host = e->download_arena();
+        for (int r = 0; r < e->n_rep; ++r)
+            reinterpret_cast<LdoHdr*>(host.data() + (size_t)r * e->lay.bytes + e->lay.o_hdr)->sample_count = 0;
+        CU(cudaMemcpy(e->d_arena.p, host.data(), host.size(), cudaMemcpyHostToDevice));
+    });
+}
+
+ldo_status ldo_get_samples(ldo_engine* e, int16_t* out, int capacity, int* count) {
+    if (!e || !out || capacity != e->sample_cap) return LDO_EINVAL;
+    return guard(e, [&]() {
+        CU(cudaMemcpy(out, e->d_samples.p, (size_t)e->n_rep * capacity * 2 * sizeof(int16_t), cudaMemcpyDeviceToHost));
+        if (count) {
+            auto host = e->download_arena();
+            for (int r = 0; r < e->n_rep; ++r)
+                count[r] =
+                    reinterpret_cast<const LdoHdr*>(host.data() + (size_t)r * e->lay.bytes + e->lay.o_hdr)->sample_count;
+        }
+    });
+}
+
+ldo_status ldo_set_trace(ldo_engine* e, int n_trace, int max_steps) {
+    if (!e || n_trace < 0 || max_steps < 0) return LDO_EINVAL;
+    return guard(e, [&]() {
+        e->n_trace = std::min(n_trace, e->n_rep);
+        e->trace_max = max_steps;
+        e->d_trace.alloc((size_t)std::max(e->n_trace, 1) * std::max(max_steps, 1) * 8);
+        CU(cudaMemset(e->d_trace.p, 0, e->d_trace.n * sizeof(double)));
+    });
+}
+
+ldo_status ldo_get_trace(ldo_engine* e, double* out, int n_trace, int max_steps) {
+    if (!e || !out || n_trace != e->n_trace || max_steps != e->trace_max) return LDO_EINVAL;
+    return guard(e, [&]() {
+        CU(cudaMemcpy(out, e->d_trace.p, (size_t)n_trace * max_steps * 8 * sizeof(double), cudaMemcpyDeviceToHost));
+    });
+}
+
+ldo_status ldo_get_move_stats(ldo_engine* e, int64_t* out, int n_moves) {
+    if (!e || !out) return LDO_EINVAL;
+    return guard(e, [&]() {
+        auto host = e->download_arena();
+        for (int m = 0; m < 2 * n_moves; ++m) out[m] = 0;
+        for (int r = 0; r < e->n_rep; ++r) {
+            const auto* ms = reinterpret_cast<const long long*>(host.data() + (size_t)r * e->lay.bytes + e->lay.o_mstat);
+            int nm = std::min(n_moves, e->lay.nmv);
+            for (int m = 0; m < 2 * nm; ++m) out[m] += ms[m];
+        }
+    });
+}
+
+ldo_status ldo_set_grid_bias(ldo_engine* e, const char* tag, int replica, const double* values, int n) {
+    if (!e || !tag || !values || replica >= e->n_rep) return LDO_EINVAL;
+    return guard(e, [&]() {
+        int r0 = replica < 0 ? 0 : replica, r1 = replica < 0 ? e->n_rep : replica + 1;
+        bool found = false;
+        for (int r = r0; r < r1; ++r) {
+            const HostSystem& hs = e->systems[e->sys_of[r]];
+            for (int b = 0; b < hs.desc.n_biases; ++b)
+                if (hs.biases[b].tag == tag && hs.desc.bias_kind[b] == LDO_B_GRID) {
+                    found = true;
+                    int len = hs.desc.bias_grid_len[b];
+                    for (int k = 0; k < len; ++k) e->h_grid[e->h_ctl[r].grid_off[b] + k] = k < n ? values[k] : 0.0;
+                }
+        }
+        if (!found) throw LdoError(LDO_EINVAL, string("no Grid bias function tagged ") + tag);
+        e->upload_grid();
+        // Bias state follows the new grid at the next move (SystemBiases::calc_move).
+    });
+}
+
+ldo_status ldo_pt_run(ldo_engine* e, int n_rungs, int64_t swaps, int exchange_interval, int exchange_q,
+                      double* device_ms) {
+    if (!e) return LDO_EINVAL;
+    return guard(e, [&]() { e->pt_run(n_rungs, swaps, exchange_interval, exchange_q, device_ms); });
+}
+
+ldo_status ldo_pt_get_permutation(ldo_engine* e, int32_t* out, int n) {
+    if (!e || !out || e->pt_rungs == 0 || n != e->n_rep) return LDO_EINVAL;
+    return guard(e, [&]() { CU(cudaMemcpy(out, e->d_perm.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost)); });
+}
+
+ldo_status ldo_pt_get_stats(ldo_engine* e, int64_t* attempts, int64_t* accepts, int n_pairs) {
+    if (!e || !attempts || !accepts || e->pt_rungs == 0 || n_pairs != e->pt_rungs - 1) return LDO_EINVAL;
+    return guard(e, [&]() {
+        CU(cudaMemcpy(attempts, e->d_pt_att.p, n_pairs * sizeof(int64_t), cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(accepts, e->d_pt_acc.p, n_pairs * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    });
+}
+
+ldo_status ldo_set_window(ldo_engine* e, const char* tag, int replica, int min_op, int max_op) {
+    if (!e || !tag || replica < 0 || replica >= e->n_rep) return LDO_EINVAL;
+    return guard(e, [&]() {
+        const HostSystem& hs = e->systems[e->sys_of[replica]];
+        bool found = false;
+        for (int b = 0; b < hs.desc.n_biases; ++b)
+            if (hs.biases[b].tag == tag) {
+                found = true;
+                e->h_ctl[replica].win_min[b] = min_op;
+                e->h_ctl[replica].win_max[b] = max_op;
+            }
+        if (!found) throw LdoError(LDO_EINVAL, string("no bias function tagged ") + tag);
+        e->upload_ctl();
+    });
+}
+
+} // extern "C"

@@ -1,0 +1,227 @@
+// CUDA kernels of the engine.
+//
+// ldo_mc_kernel: one warp per replica.  The warp copies the replica's state
+// (LdoLayout bytes) from the global arena into its slice of dynamic shared
+// memory with 16-byte vector loads, one lane runs the move loop on it, and the
+// warp writes it back.  Modes: initialise a replica from its loaded
+// configuration (OrigamiSystem constructor: set_all_domains + order
+// parameters + biases), recompute its energy after a table change
+// (OrigamiSystem::update_temp), and run n_steps move attempts
+// (GCMCSimulation::simulate), optionally recording order-parameter samples,
+// a per-step trace and the PT dependent quantities.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ldo_engine.cuh"
+#include "ldo_kernels.h"
+
+namespace {
+
+__device__ __forceinline__ void warp_copy16(void* dst, const void* src, int bytes, int lane) {
+    uint4* d = reinterpret_cast<uint4*>(dst);
+    const uint4* s = reinterpret_cast<const uint4*>(src);
+    int n = bytes >> 4;
+    for (int k = lane; k < n; k += 32) d[k] = s[k];
+}
+
+__device__ void bind_rep(ldo::Rep& r, const LdoLaunch& L, unsigned char* base, int rep) {
+    const LdoLayout& y = L.lay;
+    r.ctl = L.ctl + rep;
+    r.sys = L.sys + r.ctl->sys;
+    r.bank = L.bank;
+    r.grid = L.grid;
+    r.h = reinterpret_cast<LdoHdr*>(base + y.o_hdr);
+    r.tab = L.tabs + r.ctl->tab;
+    r.px = reinterpret_cast<int16_t*>(base + y.o_px);
+    r.py = reinterpret_cast<int16_t*>(base + y.o_py);
+    r.pz = reinterpret_cast<int16_t*>(base + y.o_pz);
+    r.bnd = reinterpret_cast<int16_t*>(base + y.o_bound);
+    r.did = reinterpret_cast<int16_t*>(base + y.o_dident);
+    r.ore = base + y.o_ore;
+    r.st = base + y.o_state;
+    r.scs = base + y.o_slot_cs;
+    r.sd = base + y.o_slot_d;
+    r.chain_c = reinterpret_cast<int32_t*>(base + y.o_chain_c);
+    r.chain_type = base + y.o_chain_type;
+    r.chain_order = base + y.o_chain_order;
+    r.type_count = reinterpret_cast<int16_t*>(base + y.o_type_count);
+    r.hash = reinterpret_cast<unsigned long long*>(base + y.o_hash);
+    r.bias = reinterpret_cast<double*>(base + y.o_bias);
+    r.op = reinterpret_cast<int32_t*>(base + y.o_op);
+    r.mstat = reinterpret_cast<long long*>(base + y.o_mstat);
+    r.hmask = y.hcap - 1;
+    int lg = 0;
+    while ((1 << lg) < y.hcap) ++lg;
+    r.hshift = 64 - lg;
+    r.ns = r.sys->ns;
+    r.lmax = r.sys->lmax;
+    r.nmv = r.sys->n_moves;
+    r.cyclic = r.sys->cyclic;
+    r.tqt = r.sys->tqt;
+    r.mean_field = r.sys->mean_field;
+    r.log6 = log(6.0);
+    r.log3 = log(3.0);
+    r.rng.init(r.ctl->seed, r.ctl->rep, 0u, r.h->draws);
+}
+
+__global__ void __launch_bounds__(128, 8) ldo_mc_kernel(LdoLaunch L) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    int warp = threadIdx.x >> 5;
+    int lane = threadIdx.x & 31;
+    int rep = blockIdx.x * L.warps_per_block + warp;
+    if (rep >= L.n_rep) return;
+    unsigned char* base = smem + (size_t)warp * L.lay.bytes;
+    unsigned char* gbase = L.arena + (size_t)rep * L.lay.bytes;
+    warp_copy16(base, gbase, L.lay.bytes, lane);
+    __syncwarp();
+    if (lane == 0) {
+        ldo::Rep r;
+        bind_rep(r, L, base, rep);
+        LdoHdr* h = r.h;
+        if (h->status == 0) {
+            if (L.mode == LDO_MODE_INIT) {
+                r.set_all_current();
+                r.init_biases();
+                h->tab = r.ctl->tab;
+            }
+            else if (L.mode == LDO_MODE_RECOMPUTE) {
+                r.recompute_energy();
+                h->tab = r.ctl->tab;
+            }
+            else {
+                if (L.force_recompute || h->tab != r.ctl->tab) {
+                    r.recompute_energy();
+                    h->tab = r.ctl->tab;
+                }
+                double* tr = (rep < L.n_trace) ? L.trace + (size_t)rep * L.trace_max * 8 : nullptr;
+                long long unit = L.sweep_units ? (long long)r.ns : 1ll;
+                long long nsteps = L.n_steps * unit;
+                long long sint = (long long)L.sample_interval * unit;
+                for (long long k = 0; k < nsteps; ++k) {
+                    if (r.bad()) break;
+                    long long s = h->steps_done + 1;
+                    r.step(s);
+                    h->steps_done = s;
+                    h->draws = r.rng.draws;
+                    if (tr && k < L.trace_max) {
+                        double* t = tr + 8 * k;
+                        t[0] = (double)s;
+                        t[1] = h->energy;
+                        t[2] = h->num_staples;
+                        t[3] = h->num_fully;
+                        t[4] = h->num_bound;
+                        t[5] = h->num_stacked;
+                        t[6] = h->move_bias * r.ctl->bias_mult;
+                        t[7] = (double)r.rng.draws;
+                    }
+                    if (sint > 0 && s % sint == 0) {
+                        int c = h->sample_count;
+                        if (c < L.sample_cap) {
+                            int16_t* o = L.samples + ((size_t)rep * L.sample_cap + c) * 2;
+                            o[0] = (int16_t)h->num_fully;
+                            o[1] = (int16_t)h->num_staples;
+                        }
+                        h->sample_count = c + 1;
+                    }
+                }
+            }
+            if (L.want_dep && !r.bad()) r.dependent_quantities();
+            h->draws = r.rng.draws;
+        }
+    }
+    __syncwarp();
+    warp_copy16(gbase, base, L.lay.bytes, lane);
+}
+
+__global__ void ldo_status_kernel(const unsigned char* arena, int bytes, int o_hdr, int n_rep, int* out) {
+    int rep = blockIdx.x * blockDim.x + threadIdx.x;
+    if (rep >= n_rep) return;
+    const LdoHdr* h = reinterpret_cast<const LdoHdr*>(arena + (size_t)rep * bytes + o_hdr);
+    if (h->status != 0) atomicMax(out, h->status);
+}
+
+// One thread per ladder: the exchange attempts of one swap round between
+// neighbouring control slots (OneDPTGCMCSimulation::attempt_exchange,
+// src/ptmc_simulation.cpp:360-412), acceptance from calc_acceptance_p
+// (:275-313) over staple types 1..S, and the master's control broadcast
+// (master_send, :212).
+__global__ void ldo_pt_swap_kernel(LdoPT P) {
+    int lad = blockIdx.x * blockDim.x + threadIdx.x;
+    if (lad >= P.n_ladders) return;
+    int* perm = P.perm + (size_t)lad * P.n_rungs;
+    ldo::Rng rng;
+    rng.init(P.seed, (uint32_t)lad, 1u, P.draws[lad]);
+    int set = P.swap_i % 2;
+    for (int i = set; i < P.n_rungs - 1; i += 2) {
+        atomicAdd((unsigned long long*)&P.att[i], 1ull);
+        double temp1 = P.slot_temp[i], temp2 = P.slot_temp[i + 1];
+        double sm1 = P.slot_stack[i], sm2 = P.slot_stack[i + 1];
+        int r1 = perm[i], r2 = perm[i + 1];
+        const LdoHdr* h1 = reinterpret_cast<const LdoHdr*>(P.arena + (size_t)r1 * P.lay.bytes + P.lay.o_hdr);
+        const LdoHdr* h2 = reinterpret_cast<const LdoHdr*>(P.arena + (size_t)r2 * P.lay.bytes + P.lay.o_hdr);
+        const int16_t* n1 = reinterpret_cast<const int16_t*>(P.arena + (size_t)r1 * P.lay.bytes + P.lay.o_type_count);
+        const int16_t* n2 = reinterpret_cast<const int16_t*>(P.arena + (size_t)r2 * P.lay.bytes + P.lay.o_type_count);
+        double bias1 = h1->move_bias * P.ctl[r1].bias_mult;
+        double bias2 = h2->move_bias * P.ctl[r2].bias_mult;
+        double dbu_dn = 0;
+        for (int t = 1; t < P.n_types; ++t) {
+            double u1 = P.red_u[t - 1] * P.rep_q[4 * r1 + 0] * P.rep_q[4 * r1 + 1];
+            double u2 = P.red_u[t - 1] * P.rep_q[4 * r2 + 0] * P.rep_q[4 * r2 + 1];
+            double N1 = n1[t], N2 = n2[t];
+            dbu_dn += (u2 / temp2 - u1 / temp1) * (N2 - N1);
+        }
+        double DB = 1 / temp2 - 1 / temp1;
+        double DH = h2->H * temp2 - h1->H * temp1;
+        double Dst = h2->stacking * temp2 - h1->stacking * temp1;
+        double DBM = sm2 / temp2 - sm1 / temp1;
+        double DBias = bias2 * temp2 - bias1 * temp1;
+        double p = fmin(1.0, exp(DB * (DH + DBias) + DBM * Dst - dbu_dn));
+        bool accept = (p == 1) ? true : (p > rng.uniform_real());
+        if (accept) {
+            atomicAdd((unsigned long long*)&P.acc[i], 1ull);
+            perm[i] = r2;
+            perm[i + 1] = r1;
+        }
+    }
+    P.draws[lad] = rng.draws;
+    // master_send: each replica takes the exchanged controls of its slot.
+    // Temperature is exchanged by every variant, so the replica at slot k uses
+    // the table set of slot k.
+    for (int k = 0; k < P.n_rungs; ++k) {
+        int r = perm[k];
+        double* q = P.rep_q + 4 * r;
+        if (P.exchange_q & 1) q[0] = P.slot_temp[k];
+        if (P.exchange_q & 2) q[1] = P.slot_u[k];
+        if (P.exchange_q & 4) q[2] = P.slot_bias[k];
+        if (P.exchange_q & 8) q[3] = P.slot_stack[k];
+        P.ctl[r].tab = P.tab_slot[k];
+        P.ctl[r].staple_u_mult = q[1];
+    }
+}
+
+} // namespace
+
+cudaError_t ldo_launch_pt_swap(const LdoPT& P, cudaStream_t stream) {
+    int threads = 128;
+    int blocks = (P.n_ladders + threads - 1) / threads;
+    ldo_pt_swap_kernel<<<blocks, threads, 0, stream>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t ldo_launch_mc(const LdoLaunch& L, cudaStream_t stream) {
+    int wpb = L.warps_per_block;
+    size_t smem = (size_t)wpb * L.lay.bytes;
+    cudaError_t err = cudaFuncSetAttribute(ldo_mc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    int blocks = (L.n_rep + wpb - 1) / wpb;
+    ldo_mc_kernel<<<blocks, wpb * 32, smem, stream>>>(L);
+    return cudaGetLastError();
+}
+
+cudaError_t ldo_launch_status(const unsigned char* arena, int bytes, int o_hdr, int n_rep, int* d_out,
+                              cudaStream_t stream) {
+    int threads = 256;
+    int blocks = (n_rep + threads - 1) / threads;
+    ldo_status_kernel<<<blocks, threads, 0, stream>>>(arena, bytes, o_hdr, n_rep, d_out);
+    return cudaGetLastError();
+}

@@ -1,0 +1,57 @@
+// Launch interface between the host library and the CUDA kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ldo_types.h"
+
+enum { LDO_MODE_RUN = 0, LDO_MODE_INIT = 1, LDO_MODE_RECOMPUTE = 2 };
+
+struct LdoLaunch {
+    const LdoSys* sys;
+    const LdoTab* tabs;
+    const double* bank;
+    const LdoRepCtl* ctl;
+    const double* grid;
+    unsigned char* arena;
+    LdoLayout lay;
+    int n_rep;
+    int warps_per_block;
+    int mode;
+    int want_dep;
+    int force_recompute;
+    int sweep_units;             // n_steps and sample_interval count sweeps of n_scaffold steps
+    long long n_steps;
+    int sample_interval, sample_cap;
+    int16_t* samples;
+    int n_trace, trace_max;
+    double* trace;
+};
+
+cudaError_t ldo_launch_mc(const LdoLaunch& L, cudaStream_t stream);
+cudaError_t ldo_launch_status(const unsigned char* arena, int bytes, int o_hdr, int n_rep, int* d_out,
+                              cudaStream_t stream);
+
+// Parallel-tempering exchange state (PTGCMCSimulation, src/ptmc_simulation.cpp).
+struct LdoPT {
+    int n_ladders, n_rungs;
+    int exchange_q;              // bit set: 1 T, 2 staple u, 4 bias mult, 8 stacking mult
+    int n_types;                 // staple types + 1
+    const double* slot_temp;     // [n_rungs] control quantities by slot
+    const double* slot_u;
+    const double* slot_bias;
+    const double* slot_stack;
+    const double* red_u;         // [n_types-1] reduced staple chemical potentials
+    int* perm;                   // [n_ladders * n_rungs] slot -> replica
+    double* rep_q;               // [n_rep * 4] per-replica temp, u mult, bias mult, stack mult
+    const int* tab_slot;         // [n_rungs] table set used at each slot
+    LdoRepCtl* ctl;
+    const unsigned char* arena;
+    LdoLayout lay;
+    unsigned long long* draws;   // [n_ladders] swap stream counters
+    long long* att;              // [n_rungs - 1]
+    long long* acc;
+    uint32_t seed;
+    int swap_i;
+};
+cudaError_t ldo_launch_pt_swap(const LdoPT& P, cudaStream_t stream);

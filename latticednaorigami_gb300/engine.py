@@ -1,0 +1,203 @@
+"""ctypes binding of the engine's C ABI (include/ldo.h).
+
+The engine itself is CUDA; this module only marshals arguments.  Loading fails
+loudly if the compiled library is missing: there is no CPU fallback."""
+import ctypes
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libldo_gb300.so")
+
+STATUS = {0: "LDO_OK", 1: "LDO_EINVAL", 2: "LDO_ENOMEM", 3: "LDO_ECUDA",
+          4: "LDO_EINVARIANT", 5: "LDO_EITERCAP", 6: "LDO_ECAPACITY"}
+
+# Names and order of every entry point declared in include/ldo.h.
+EXPORTS = [
+    "ldo_create_from_inp", "ldo_create_multi", "ldo_destroy", "ldo_last_error", "ldo_num_replicas",
+    "ldo_set_controls", "ldo_run", "ldo_run_sweeps", "ldo_state_bytes", "ldo_get_observables", "ldo_get_config", "ldo_set_sampling",
+    "ldo_get_samples", "ldo_set_trace", "ldo_get_trace", "ldo_get_move_stats", "ldo_set_grid_bias",
+    "ldo_set_window", "ldo_pt_run", "ldo_pt_get_permutation", "ldo_pt_get_stats",
+]
+
+
+class LdoError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS.get(code, code), msg))
+        self.code = code
+
+
+class Observables(ctypes.Structure):
+    _fields_ = [("energy", ctypes.c_double), ("total_bias", ctypes.c_double), ("temp", ctypes.c_double),
+                ("enthalpy", ctypes.c_double), ("entropy", ctypes.c_double), ("stacking", ctypes.c_double),
+                ("draws", ctypes.c_int64), ("num_staples", ctypes.c_int32),
+                ("num_fully_bound", ctypes.c_int32), ("num_bound", ctypes.c_int32),
+                ("num_self_bound", ctypes.c_int32), ("num_stacked", ctypes.c_int32),
+                ("num_unassigned", ctypes.c_int32), ("current_c_i", ctypes.c_int32),
+                ("status", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def load_library(path=None):
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError("engine library %s is missing: run __graft_entry__.build() "
+                           "(the engine has no CPU fallback)" % p)
+    lib = ctypes.CDLL(p)
+    vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)
+    lib.ldo_create_from_inp.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ip, ctypes.c_uint32,
+                                        ctypes.POINTER(vp)]
+    lib.ldo_create_multi.argtypes = [ctypes.POINTER(ctypes.c_char_p), ip, ctypes.c_char_p,
+                                     ctypes.POINTER(ctypes.c_int), ip, ctypes.c_uint32, ctypes.POINTER(vp)]
+    lib.ldo_destroy.argtypes = [vp]
+    lib.ldo_last_error.argtypes = [vp]
+    lib.ldo_last_error.restype = ctypes.c_char_p
+    lib.ldo_num_replicas.argtypes = [vp]
+    lib.ldo_set_controls.argtypes = [vp, dp, dp, dp, ip]
+    lib.ldo_run.argtypes = [vp, ctypes.c_int64, dp]
+    lib.ldo_run_sweeps.argtypes = [vp, ctypes.c_int64, dp]
+    lib.ldo_state_bytes.argtypes = [vp]
+    lib.ldo_get_observables.argtypes = [vp, ctypes.POINTER(Observables), ip]
+    lib.ldo_get_config.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int32), ip, ctypes.POINTER(ctypes.c_int)]
+    lib.ldo_set_sampling.argtypes = [vp, ip, ip]
+    lib.ldo_get_samples.argtypes = [vp, ctypes.POINTER(ctypes.c_int16), ip, ctypes.POINTER(ctypes.c_int)]
+    lib.ldo_set_trace.argtypes = [vp, ip, ip]
+    lib.ldo_get_trace.argtypes = [vp, dp, ip, ip]
+    lib.ldo_get_move_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ip]
+    lib.ldo_set_grid_bias.argtypes = [vp, ctypes.c_char_p, ip, dp, ip]
+    lib.ldo_set_window.argtypes = [vp, ctypes.c_char_p, ip, ip, ip]
+    lib.ldo_pt_run.argtypes = [vp, ip, ctypes.c_int64, ip, ip, dp]
+    lib.ldo_pt_get_permutation.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ip]
+    lib.ldo_pt_get_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64), ip]
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if a is not None else None
+
+
+class Engine:
+    """A batch of replicas of one or more origami systems on the GPU."""
+
+    def __init__(self, inp, n_replicas, seed=0, overrides="", sys_of_replica=None):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        if isinstance(inp, (list, tuple)):
+            arr = (ctypes.c_char_p * len(inp))(*[os.fsencode(p) for p in inp])
+            so = None
+            if sys_of_replica is not None:
+                so = (ctypes.c_int * n_replicas)(*[int(x) for x in sys_of_replica])
+            rc = self.lib.ldo_create_multi(arr, len(inp), overrides.encode(), so, n_replicas, seed,
+                                           ctypes.byref(h))
+        else:
+            rc = self.lib.ldo_create_from_inp(os.fsencode(inp), overrides.encode(), n_replicas, seed,
+                                              ctypes.byref(h))
+        if rc != 0:
+            raise LdoError(rc, self.lib.ldo_last_error(None).decode())
+        self.h = h
+        self.n = n_replicas
+        self._trace = None
+        self._samples = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ldo_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def _check(self, rc):
+        if rc != 0:
+            raise LdoError(rc, self.lib.ldo_last_error(self.h).decode())
+
+    def run(self, steps):
+        ms = ctypes.c_double(0)
+        self._check(self.lib.ldo_run(self.h, int(steps), ctypes.byref(ms)))
+        return ms.value
+
+    def run_sweeps(self, sweeps):
+        ms = ctypes.c_double(0)
+        self._check(self.lib.ldo_run_sweeps(self.h, int(sweeps), ctypes.byref(ms)))
+        return ms.value
+
+    def state_bytes(self):
+        return self.lib.ldo_state_bytes(self.h)
+
+    def set_controls(self, temps=None, stacking_mults=None, staple_u_mults=None):
+        def arr(x):
+            return None if x is None else np.ascontiguousarray(np.broadcast_to(np.asarray(x, np.float64), (self.n,)))
+        t, s, u = arr(temps), arr(stacking_mults), arr(staple_u_mults)
+        self._check(self.lib.ldo_set_controls(self.h, _dptr(t), _dptr(s), _dptr(u), self.n))
+
+    def observables(self):
+        out = (Observables * self.n)()
+        self._check(self.lib.ldo_get_observables(self.h, out, self.n))
+        return [dict((f, getattr(o, f)) for f, _ in Observables._fields_) for o in out]
+
+    def config(self, replica):
+        cap = 1 << 16
+        buf = (ctypes.c_int32 * cap)()
+        n = ctypes.c_int(0)
+        self._check(self.lib.ldo_get_config(self.h, replica, buf, cap, ctypes.byref(n)))
+        return list(buf[:n.value])
+
+    def set_trace(self, n_trace, max_steps):
+        self._check(self.lib.ldo_set_trace(self.h, n_trace, max_steps))
+        self._trace = (min(n_trace, self.n), max_steps)
+
+    def trace(self):
+        nt, ms = self._trace
+        out = np.zeros((nt, ms, 8))
+        self._check(self.lib.ldo_get_trace(self.h, _dptr(out), nt, ms))
+        return out
+
+    def set_sampling(self, interval, capacity):
+        self._check(self.lib.ldo_set_sampling(self.h, interval, capacity))
+        self._samples = capacity
+
+    def samples(self):
+        cap = self._samples
+        out = np.zeros((self.n, cap, 2), np.int16)
+        cnt = np.zeros(self.n, np.int32)
+        self._check(self.lib.ldo_get_samples(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int16)), cap,
+                                             cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return out, cnt
+
+    def move_stats(self, n_moves):
+        out = np.zeros(2 * n_moves, np.int64)
+        self._check(self.lib.ldo_get_move_stats(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), n_moves))
+        return out.reshape(n_moves, 2)
+
+    def set_grid_bias(self, tag, values, replica=-1):
+        v = np.ascontiguousarray(values, np.float64)
+        self._check(self.lib.ldo_set_grid_bias(self.h, tag.encode(), replica, _dptr(v), len(v)))
+
+    def set_window(self, tag, replica, min_op, max_op):
+        self._check(self.lib.ldo_set_window(self.h, tag.encode(), replica, min_op, max_op))
+
+    def pt_run(self, n_rungs, swaps, exchange_interval, exchange_q=1):
+        ms = ctypes.c_double(0)
+        self._check(self.lib.ldo_pt_run(self.h, n_rungs, int(swaps), exchange_interval, exchange_q,
+                                        ctypes.byref(ms)))
+        return ms.value
+
+    def pt_permutation(self):
+        out = np.zeros(self.n, np.int32)
+        self._check(self.lib.ldo_pt_get_permutation(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                                    self.n))
+        return out
+
+    def pt_stats(self, n_pairs):
+        a = np.zeros(n_pairs, np.int64)
+        b = np.zeros(n_pairs, np.int64)
+        self._check(self.lib.ldo_pt_get_stats(self.h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                              b.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), n_pairs))
+        return a, b

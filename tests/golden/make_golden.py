@@ -1,0 +1,71 @@
+"""Generates the golden fixtures in this directory by running the reference
+itself, compiled from its own sources with the recipe in oracle/ref (Philox
+RNG in place of std::mt19937_64), on the synthetic systems of tests/systems.py.
+
+Needs the reference sources (only present where the fixtures are made):
+    make -C oracle/ref && python tests/golden/make_golden.py
+
+Each fixture <case>_s<seed>.json.gz holds the per-step trace (step, energy,
+staples, fully bound pairs, bound pairs, stacked pairs, total bias, random
+draws) and the final configuration (chains: index, identity, per domain
+x y z ox oy oz state)."""
+import gzip
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+import systems  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref", "ref_trace")
+
+# case, seed, steps
+RUNS = [("c1", 1, 20000), ("c1", 2, 20000), ("g24a", 3, 20000), ("g24b", 4, 20000), ("g24c", 5, 20000),
+        ("g24d", 6, 10000), ("g24e", 7, 20000)]
+
+
+def ref_trace(inp, seed, steps, replica=0):
+    with open(inp) as f:
+        text = f.read()
+    tmp = inp + ".trace.inp"
+    with open(tmp, "w") as f:
+        f.write(text + "trace_steps=%d\ntrace_seed=%d\ntrace_replica=%d\ntrace_every=%d\n"
+                % (steps, seed, replica, steps))
+    out = subprocess.run([REF, tmp], capture_output=True, text=True, cwd=os.path.dirname(inp))
+    os.remove(tmp)
+    d = json.loads(out.stdout)
+    if "error" in d:
+        raise RuntimeError(d["error"])
+    return d
+
+
+def flatten(chains):
+    flat = [len(chains)]
+    for idx, ident, doms in chains:
+        flat += [idx, ident, len(doms)]
+        for d in doms:
+            flat += d
+    return flat
+
+
+def main():
+    if not os.path.exists(REF):
+        sys.exit("build the reference first: make -C oracle/ref")
+    with tempfile.TemporaryDirectory() as tmp:
+        for case, seed, steps in RUNS:
+            inp = systems.write_case(tmp, case)
+            d = ref_trace(inp, seed, steps)
+            fx = {"case": case, "seed": seed, "steps": steps, "initial_energy": d["initial_energy"],
+                  "trace": d["steps"], "final_config": flatten(d["dumps"][-1][1]), "draws": d["draws"]}
+            path = os.path.join(HERE, "%s_s%d.json.gz" % (case, seed))
+            with gzip.open(path, "wt") as f:
+                json.dump(fx, f)
+            print(path, len(d["steps"]), "steps, draws", d["draws"])
+
+
+if __name__ == "__main__":
+    main()

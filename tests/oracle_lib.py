@@ -1,0 +1,113 @@
+"""ctypes wrapper of the CPU oracle (oracle/liboracle.so), the checker the
+GPU engine is compared with.  Test infrastructure only."""
+import ctypes
+import os
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_SO = os.path.join(ROOT, "oracle", "liboracle.so")
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            import subprocess
+            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+        L = ctypes.CDLL(ORACLE_SO)
+        vp = ctypes.c_void_p
+        L.oracle_create.restype = vp
+        L.oracle_create.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_uint32]
+        L.oracle_destroy.argtypes = [vp]
+        L.oracle_run.argtypes = [vp, ctypes.c_longlong, ctypes.c_longlong, vp]
+        L.oracle_get_config.argtypes = [vp, vp, ctypes.c_int]
+        L.oracle_observables.argtypes = [vp, vp]
+        L.oracle_move_stats.argtypes = [vp, vp, ctypes.c_int]
+        L.oracle_tables.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.oracle_update_temp.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+        L.oracle_dependent_qs.argtypes = [vp, vp]
+        L.oracle_set_grid.argtypes = [vp, ctypes.c_char_p, vp, ctypes.c_int]
+        L.oracle_last_error.restype = ctypes.c_char_p
+        L.oracle_run_batch.restype = ctypes.c_double
+        L.oracle_run_batch.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_int,
+                                       ctypes.c_longlong, ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+class OracleReplica:
+    """One replica of the CPU restatement, same Philox stream as the engine's
+    replica `replica` under `seed`."""
+
+    def __init__(self, inp, seed=0, replica=0, overrides=""):
+        self.L = lib()
+        self.h = self.L.oracle_create(os.fsencode(inp), overrides.encode(), seed, replica)
+        if not self.h:
+            raise OracleError(self.L.oracle_last_error().decode())
+        self.step = 0
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.oracle_destroy(self.h)
+            self.h = None
+
+    def run(self, steps, trace=True):
+        tr = np.zeros((steps, 8)) if trace else None
+        rc = self.L.oracle_run(self.h, steps, self.step, tr.ctypes.data if trace else None)
+        if rc != 0:
+            raise OracleError(self.L.oracle_last_error().decode())
+        self.step += steps
+        return tr
+
+    def config(self):
+        buf = np.zeros(1 << 16, np.int32)
+        n = self.L.oracle_get_config(self.h, buf.ctypes.data, len(buf))
+        return buf[:n].tolist()
+
+    def observables(self):
+        o = np.zeros(10)
+        self.L.oracle_observables(self.h, o.ctypes.data)
+        keys = ["energy", "num_staples", "num_fully_bound", "num_bound", "num_self_bound", "num_stacked",
+                "num_unassigned", "total_bias", "draws", "current_c_i"]
+        return dict(zip(keys, o.tolist()))
+
+    def move_stats(self, n):
+        o = np.zeros(2 * n, np.int64)
+        self.L.oracle_move_stats(self.h, o.ctypes.data, 2 * n)
+        return o.reshape(n, 2)
+
+    def tables(self):
+        imax = self.L.oracle_tables(self.h, None, None, None, None, None)
+        d = 2 * imax + 1
+        e, h, s, st = (np.zeros(d * d) for _ in range(4))
+        init = np.zeros(3)
+        self.L.oracle_tables(self.h, e.ctypes.data, h.ctypes.data, s.ctypes.data, st.ctypes.data, init.ctypes.data)
+        return imax, e.reshape(d, d), h.reshape(d, d), s.reshape(d, d), st.reshape(d, d), init
+
+    def update_temp(self, temp, stacking_mult=1.0):
+        if self.L.oracle_update_temp(self.h, temp, stacking_mult) != 0:
+            raise OracleError(self.L.oracle_last_error().decode())
+
+    def dependent_qs(self):
+        o = np.zeros(4)
+        self.L.oracle_dependent_qs(self.h, o.ctypes.data)
+        return o
+
+    def set_grid(self, tag, values):
+        v = np.ascontiguousarray(values, np.float64)
+        if self.L.oracle_set_grid(self.h, tag.encode(), v.ctypes.data, len(v)) != 0:
+            raise OracleError(self.L.oracle_last_error().decode())
+
+
+def run_batch(inp, seed, n_rep, steps, threads, overrides=""):
+    """CPU baseline: wall seconds for n_rep replicas x steps on `threads` threads."""
+    t = lib().oracle_run_batch(os.fsencode(inp), overrides.encode(), seed, n_rep, steps, threads)
+    if t < 0:
+        raise OracleError(lib().oracle_last_error().decode() or "oracle batch failed")
+    return t

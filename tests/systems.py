@@ -1,0 +1,185 @@
+"""Synthetic origami systems in the reference's file formats.
+
+Every system used by the tests and the benchmark is generated here from a
+seed: a scaffold laid out as a serpentine of rows on the z=0 plane, staple
+types that pair either two neighbouring domains of one row (helix staples) or
+the same column of two neighbouring rows (crossover staples), and sequences
+drawn uniformly from ACGT with each staple domain the reverse complement of
+its scaffold partner.  Files are written with the reference's JSON layout
+(system, movetype, order-parameter and bias files) and its key=value .inp
+options."""
+import json
+import os
+import random
+
+COMP = {"A": "T", "T": "A", "G": "C", "C": "G"}
+
+
+def revcomp(s):
+    return "".join(COMP[c] for c in reversed(s))
+
+
+def serpentine(n, row_len):
+    """Positions of n scaffold domains in rows of row_len, alternating x direction."""
+    pos = []
+    for i in range(n):
+        r, c = divmod(i, row_len)
+        x = c if r % 2 == 0 else row_len - 1 - c
+        pos.append([x, r, 0])
+    return pos
+
+
+def staple_pairs(n, row_len=4):
+    """Scaffold index pairs bound by each two-domain staple type (n/2 of them).
+
+    Rows of 4: crossovers join columns 0 and 3 of rows 2k and 2k+1, helix
+    staples take the middle pair of each row; an odd last row gets two helix
+    staples."""
+    assert row_len == 4 and n % 4 == 0
+    rows = n // 4
+    idx = lambda r, x: 4 * r + (x if r % 2 == 0 else 3 - x)
+    pairs = []
+    for r in range(0, rows - (rows % 2), 2):
+        pairs.append((idx(r, 0), idx(r + 1, 0)))
+        pairs.append((idx(r, 3), idx(r + 1, 3)))
+        pairs.append((idx(r, 1), idx(r, 2)))
+        pairs.append((idx(r + 1, 1), idx(r + 1, 2)))
+    if rows % 2:
+        r = rows - 1
+        pairs.append((idx(r, 0), idx(r, 1)))
+        pairs.append((idx(r, 2), idx(r, 3)))
+    return pairs
+
+
+def linear_pairs(n):
+    return [(i, i + 1) for i in range(0, n - 1, 2)]
+
+
+def make_system(n, pairs, seed, positions, seq_len=16, cyclic=False):
+    rng = random.Random(seed)
+    scaf_seq = ["".join(rng.choice("ACGT") for _ in range(seq_len)) for _ in range(n)]
+    idents = [[i + 1 for i in range(n)]]
+    seqs = [scaf_seq]
+    for a, b in pairs:
+        idents.append([-(a + 1), -(b + 1)])
+        seqs.append([revcomp(scaf_seq[a]), revcomp(scaf_seq[b])])
+    return {"origami": {
+        "cyclic": cyclic,
+        "identities": idents,
+        "sequences": seqs,
+        "configurations": [{"step": 0, "chains": [{
+            "index": 0, "identity": 0,
+            "positions": positions,
+            "orientations": [[0, 0, 1]] * n}]}]}}
+
+
+MOVES = {
+    "met3": [("Met staple exchange", "MetStapleExchange", "1/3"),
+             ("Met staple regrowth", "MetStapleRegrowth", "1/3"),
+             ("CB staple regrowth", "CBStapleRegrowth", "1/3")],
+    "all4": [("Orientation rotation", "OrientationRotation", "1/4"),
+             ("Met staple exchange", "MetStapleExchange", "1/4"),
+             ("Met staple regrowth", "MetStapleRegrowth", "1/4"),
+             ("CB staple regrowth", "CBStapleRegrowth", "1/4")],
+}
+
+
+def moves_json(kind):
+    mts = []
+    for label, t, f in MOVES[kind]:
+        m = {"label": label, "type": t, "freq": f}
+        if t == "MetStapleExchange":
+            m["adaptive_exchange"] = False
+        mts.append(m)
+    return {"origami": {"movetypes": mts}}
+
+
+OPS = {"origami": {"order_params": [
+    {"label": "Number of bound staples", "tag": "numstaples", "type": "NumStaples", "level": 0},
+    {"label": "Number of fully bound domain pairs", "tag": "numfulldomains", "type": "NumBoundDomainPairs", "level": 0},
+    {"label": "Number of misbound domain pairs", "tag": "nummisdomains", "type": "NumMisboundDomainPairs", "level": 0},
+    {"label": "Number of stacked domain pairs", "tag": "numstackedpairs", "type": "NumStackedPairs", "level": 0},
+    {"label": "Number of linear helices", "tag": "numlinearhelices", "type": "NumLinearHelices", "level": 0},
+    {"label": "Number of stacked junctions", "tag": "numstackedjuncts", "type": "NumStackedJuncts", "level": 0},
+    {"label": "Bound plus stacked", "tag": "boundplusstacked", "type": "Sum", "ops": ["numfulldomains", "numstackedpairs"], "level": 1},
+    {"label": "Staple 1 fully bound", "tag": "st1full", "type": "StapleTypeFullyBound", "staple": 1, "level": 1},
+]}}
+
+BIASES = {"origami": {"bias_functions": [
+    {"label": "lsw", "tag": "lsw", "type": "LinearStepWell", "min_op": 4, "max_op": 10, "well_bias": 0,
+     "min_bias": 2, "slope": 1.5, "ops": ["numfulldomains"], "level": 0},
+    {"label": "sq", "tag": "sq", "type": "SquareWell", "min_op": 1, "max_op": 6, "well_bias": -0.5,
+     "outside_bias": 1.25, "ops": ["numstaples"], "level": 0},
+    {"label": "grid", "tag": "grid", "type": "Grid", "ops": ["numfulldomains"], "level": 0}]}}
+
+BASE = dict(domain_type="HalfTurn", binding_pot="FourBody", misbinding_pot="Opposing", stacking_pot="Constant",
+            hybridization_pot="NearestNeighbour", temp=330, staple_M=1e-6, cation_M=0.5, max_staple_size=2,
+            order_parameter_file="ops.json")
+
+# name: (system, moveset, overrides)
+CASES = {
+    "c1": ("four", "met3", dict(stacking_ene=1000, max_total_staples=4, max_type_staples=4)),
+    "g24a": ("grid24", "all4", dict(stacking_ene=-1000, staple_M=1e-3, temp=335, max_total_staples=24,
+                                    max_type_staples=4)),
+    "g24b": ("grid24", "all4", dict(domain_type="ThreeQuarterTurn", stacking_ene=-1500, staple_M=1e-3, temp=325,
+                                    max_total_staples=24, max_type_staples=4, centering_freq=97,
+                                    constraint_check_freq=101, apply_mean_field_cor="true")),
+    "g24c": ("grid24", "all4", dict(hybridization_pot="Uniform", binding_h=-60387.1, binding_s=-166.06,
+                                    misbinding_pot="Disallowed", stacking_ene=-1000, temp=340, staple_M=1e-5,
+                                    max_total_staples=24, max_type_staples=4, bias_functions_file="biases.json",
+                                    bias_functions_mult=0.7)),
+    "g24d": ("grid24", "all4", dict(stacking_pot="SequenceSpecific", staple_M=1e-3, max_total_staples=24,
+                                    max_type_staples=4)),
+    "g24e": ("grid24", "met3", dict(stacking_ene=-2000, staple_M=1e-2, temp=315, max_total_staples=24,
+                                    max_type_staples=3)),
+}
+
+
+def system_for(name):
+    if name == "four":
+        pairs = [(1, 0), (3, 2)]
+        return make_system(4, pairs, seed=4, positions=[[i, 0, 0] for i in range(4)])
+    if name.startswith("grid"):
+        n = int(name[4:])
+        return make_system(n, staple_pairs(n), seed=n, positions=serpentine(n, 4))
+    raise KeyError(name)
+
+
+def write_inp(path, opts):
+    with open(path, "w") as f:
+        for k, v in opts.items():
+            f.write("%s=%s\n" % (k, v))
+
+
+def write_case(dirname, name, extra=None):
+    """Writes <name>.inp and its input files into dirname; returns the .inp path."""
+    sysname, moves, over = CASES[name]
+    os.makedirs(dirname, exist_ok=True)
+    with open(os.path.join(dirname, sysname + ".json"), "w") as f:
+        json.dump(system_for(sysname), f)
+    with open(os.path.join(dirname, "moves_%s.json" % moves), "w") as f:
+        json.dump(moves_json(moves), f)
+    with open(os.path.join(dirname, "ops.json"), "w") as f:
+        json.dump(OPS, f)
+    with open(os.path.join(dirname, "biases.json"), "w") as f:
+        json.dump(BIASES, f)
+    opts = dict(BASE)
+    opts["origami_input_filename"] = sysname + ".json"
+    opts["movetype_file"] = "moves_%s.json" % moves
+    opts.update(over)
+    if extra:
+        opts.update(extra)
+    path = os.path.join(dirname, name + ".inp")
+    write_inp(path, opts)
+    return path
+
+
+def write_all(dirname):
+    return {name: write_case(dirname, name) for name in CASES}
+
+
+if __name__ == "__main__":
+    import sys
+    d = sys.argv[1] if len(sys.argv) > 1 else os.path.join(os.path.dirname(__file__), "data")
+    for n, p in write_all(d).items():
+        print(n, p)
