@@ -313,6 +313,27 @@ void oracle_dependent_qs(void* h, double* out) {
     out[3] = s.total_bias();
 }
 
+// Staple counts per chain type (index 0 = scaffold, always 0 here), as
+// OrigamiSystem::get_staple_counts (src/origami_system.cpp:153).
+int oracle_staple_counts(void* h, int* out, int cap) {
+    System& s = static_cast<Replica*>(h)->sys;
+    int n = (int)s.cfg.identities.size();
+    if (n > cap) return -n;
+    for (int t = 0; t < n; ++t) out[t] = t == 0 ? 0 : s.num_staples_of_ident(t);
+    return n;
+}
+
+// Uniform reals of the swap stream: `count` draws of Philox key (seed,
+// ladder), stream 1, starting at draw index `first`.
+void oracle_swap_uniforms(uint32_t seed, uint32_t ladder, unsigned long long first, int count, double* out) {
+    Stream st;
+    st.key[0] = seed;
+    st.key[1] = ladder;
+    st.stream = 1;
+    st.draws = first;
+    for (int i = 0; i < count; ++i) out[i] = st.uniform_real();
+}
+
 // Grid bias values (1-D, index = order-parameter value) for bias `tag`.
 int oracle_set_grid(void* h, const char* tag, const double* vals, int n) {
     System& s = static_cast<Replica*>(h)->sys;

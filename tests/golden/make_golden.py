@@ -52,6 +52,32 @@ def flatten(chains):
     return flat
 
 
+def enumerate_c1(tmp):
+    """Exact staple-only enumeration of the 4-domain system with the
+    reference's enumerator (src/enumerate.cpp:687), weights over
+    (numstaples, numfulldomains)."""
+    base = os.path.join(tmp, "c1enum")
+    inp = systems.write_case(tmp, "c1", extra=dict(
+        simulation_type="enumerate", enumerate_staples_only="true", ops_to_output="numstaples numfulldomains",
+        output_filebase=base))
+    with open(inp, "a") as f:
+        f.write("trace_mode=enumerate\n")
+    subprocess.run([REF, inp], capture_output=True, text=True, cwd=tmp, check=True)
+    weights = {}
+    with open(base + ".weights") as f:
+        tags = f.readline().split()
+        for line in f:
+            line = line.strip()
+            if not line:
+                continue
+            key, w = line.rsplit(" ", 1)
+            weights[" ".join(key.strip("()").split())] = float(w)
+    path = os.path.join(HERE, "c1_enumeration.json")
+    with open(path, "w") as f:
+        json.dump({"case": "c1", "ops": tags, "weights": weights}, f, indent=1, sort_keys=True)
+    print(path, weights)
+
+
 def main():
     if not os.path.exists(REF):
         sys.exit("build the reference first: make -C oracle/ref")
@@ -65,6 +91,7 @@ def main():
             with gzip.open(path, "wt") as f:
                 json.dump(fx, f)
             print(path, len(d["steps"]), "steps, draws", d["draws"])
+        enumerate_c1(tmp)
 
 
 if __name__ == "__main__":

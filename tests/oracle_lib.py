@@ -111,3 +111,20 @@ def run_batch(inp, seed, n_rep, steps, threads, overrides=""):
     if t < 0:
         raise OracleError(lib().oracle_last_error().decode() or "oracle batch failed")
     return t
+
+
+def staple_counts(rep):
+    L = lib()
+    L.oracle_staple_counts.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    out = np.zeros(256, np.int32)
+    n = L.oracle_staple_counts(rep.h, out.ctypes.data, 256)
+    return out[:n]
+
+
+def swap_uniform(seed, ladder, index):
+    L = lib()
+    L.oracle_swap_uniforms.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_ulonglong, ctypes.c_int,
+                                       ctypes.c_void_p]
+    out = np.zeros(1)
+    L.oracle_swap_uniforms(seed, ladder, index, 1, out.ctypes.data)
+    return float(out[0])

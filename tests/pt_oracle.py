@@ -1,0 +1,97 @@
+"""CPU restatement of the 1-D parallel-tempering driver, for checking the
+engine's in-kernel exchange.  Test infrastructure only.
+
+Follows PTGCMCSimulation::run (src/ptmc_simulation.cpp:106-150): every round
+each replica takes its control quantities (update_control_qs: new energy
+tables and a full energy recomputation), runs exchange_interval steps, reports
+its dependent quantities (update_dependent_qs, :152), and neighbouring control
+slots of parity swap_i % 2 attempt an exchange with calc_acceptance_p
+(:275-313) summed over staple types 1..S.  Swap decisions draw from Philox
+stream 1 keyed (seed, ladder)."""
+import math
+
+import numpy as np
+
+from oracle_lib import OracleReplica, staple_counts, swap_uniform
+
+
+class PTOracle:
+    def __init__(self, inp, params, n_ladders, seed, exchange_q=1):
+        self.n_rungs = len(params["temps"])
+        self.n_ladders = n_ladders
+        self.seed = seed
+        self.q = exchange_q
+        R = self.n_rungs
+        self.slot = {"temp": list(params["temps"]), "u": list(params.get("chem_pot_mults", [1.0] * R)),
+                     "bias": list(params.get("bias_mults", [1.0] * R)),
+                     "stack": list(params.get("stacking_mults", [1.0] * R))}
+        self.reps = [OracleReplica(inp, seed=seed, replica=r) for r in range(R * n_ladders)]
+        self.ctrl = []
+        for l in range(n_ladders):
+            for k in range(R):
+                self.ctrl.append({n: self.slot[n][k] for n in self.slot})
+        self.perm = [[l * R + k for k in range(R)] for l in range(n_ladders)]
+        self.draws = [0] * n_ladders
+        self.swap_i = 0
+        temp0 = params.get("temp", 300.0)
+        staple_M = params["staple_M"]
+        self.red_u = []
+        for n in params["staple_lengths"]:
+            extra = (2 * n - 1) * math.log(6)
+            u = temp0 * (math.log(staple_M) - extra)
+            self.red_u.append(u / temp0)
+        self.bias_mult = params.get("bias_functions_mult", 1.0)
+        self.att = [0] * (R - 1)
+        self.acc = [0] * (R - 1)
+
+    def round(self, exchange_interval):
+        self.swap_i += 1
+        R = self.n_rungs
+        deps = []
+        for r, rep in enumerate(self.reps):
+            c = self.ctrl[r]
+            rep.update_temp(c["temp"], c["stack"] if self.q & 8 else 1.0)
+            rep.run(exchange_interval, trace=False)
+            H, S, st, bias = rep.dependent_qs()
+            deps.append((H, st, bias, staple_counts(rep)))
+        for l in range(self.n_ladders):
+            perm = self.perm[l]
+            for i in range(self.swap_i % 2, R - 1, 2):
+                self.att[i] += 1
+                t1, t2 = self.slot["temp"][i], self.slot["temp"][i + 1]
+                sm1, sm2 = self.slot["stack"][i], self.slot["stack"][i + 1]
+                r1, r2 = perm[i], perm[i + 1]
+                H1, st1, b1, n1 = deps[r1]
+                H2, st2, b2, n2 = deps[r2]
+                dbu = 0.0
+                for t in range(1, len(n1)):
+                    u1 = self.red_u[t - 1] * self.ctrl[r1]["temp"] * self.ctrl[r1]["u"]
+                    u2 = self.red_u[t - 1] * self.ctrl[r2]["temp"] * self.ctrl[r2]["u"]
+                    dbu += (u2 / t2 - u1 / t1) * (float(n2[t]) - float(n1[t]))
+                DB = 1 / t2 - 1 / t1
+                DH = H2 * t2 - H1 * t1
+                Dst = st2 * t2 - st1 * t1
+                DBM = sm2 / t2 - sm1 / t1
+                DBias = b2 * t2 - b1 * t1
+                p = min(1.0, math.exp(DB * (DH + DBias) + DBM * Dst - dbu))
+                if p == 1:
+                    accept = True
+                else:
+                    accept = p > swap_uniform(self.seed, l, self.draws[l])
+                    self.draws[l] += 1
+                if accept:
+                    self.acc[i] += 1
+                    perm[i], perm[i + 1] = r2, r1
+            for k in range(R):
+                c = self.ctrl[perm[k]]
+                if self.q & 1:
+                    c["temp"] = self.slot["temp"][k]
+                if self.q & 2:
+                    c["u"] = self.slot["u"][k]
+                if self.q & 4:
+                    c["bias"] = self.slot["bias"][k]
+                if self.q & 8:
+                    c["stack"] = self.slot["stack"][k]
+
+    def permutation(self):
+        return np.array([x for p in self.perm for x in p], np.int32)
