@@ -883,7 +883,7 @@ ldo_status ldo_set_controls(ldo_engine* e, const double* temps, const double* st
 ldo_status ldo_get_observables(ldo_engine* e, ldo_observables* out, int n) {
     if (!e || !out || n > e->n_rep) return LDO_EINVAL;
     return guard(e, [&]() {
-        LdoLaunch L = e->launch_params(LDO_MODE_RUN, 0);
+        LdoLaunch L = e->launch_params(LDO_MODE_OBSERVE, 0);
         L.want_dep = 1;
         CU(ldo_launch_mc(L, e->stream));
         CU(cudaStreamSynchronize(e->stream));

@@ -88,6 +88,12 @@ __global__ void __launch_bounds__(128, 8) ldo_mc_kernel(LdoLaunch L) {
                 r.recompute_energy();
                 h->tab = r.ctl->tab;
             }
+            else if (L.mode == LDO_MODE_OBSERVE) {
+                // Reading observables changes nothing: the energy and the
+                // dependent quantities use the tables the energy was last
+                // computed with, even if the controls have moved since.
+                r.tab = L.tabs + h->tab;
+            }
             else {
                 if (L.force_recompute || h->tab != r.ctl->tab) {
                     r.recompute_energy();

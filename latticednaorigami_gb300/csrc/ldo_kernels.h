@@ -5,7 +5,7 @@
 
 #include "ldo_types.h"
 
-enum { LDO_MODE_RUN = 0, LDO_MODE_INIT = 1, LDO_MODE_RECOMPUTE = 2 };
+enum { LDO_MODE_RUN = 0, LDO_MODE_INIT = 1, LDO_MODE_RECOMPUTE = 2, LDO_MODE_OBSERVE = 3 };
 
 struct LdoLaunch {
     const LdoSys* sys;

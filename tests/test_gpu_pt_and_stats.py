@@ -38,7 +38,7 @@ def test_pt_matches_cpu_restatement(q):
     eng = engine(inp, n_replicas=4 * n_ladders, seed=seed)
     eng.pt_run(4, swaps, interval, q)
     ora = PTOracle(inp, dict(temps=temps, chem_pot_mults=umults, temp=335.0, staple_M=1e-3,
-                             staple_lengths=[2] * 10), n_ladders, seed, exchange_q=q)
+                             staple_lengths=[2] * 12), n_ladders, seed, exchange_q=q)
     for _ in range(swaps):
         ora.round(interval)
     np.testing.assert_array_equal(eng.pt_permutation(), ora.permutation())
