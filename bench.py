@@ -121,7 +121,7 @@ def cpu_baseline(files, sys_of, taus_per_size, budget_s=15.0):
     sweeps_each = 200
     for i, f in enumerate(files):
         n = SIZES[i]
-        t = run_batch(f, "", 0, per, sweeps_each * n, cores)
+        t = run_batch(f, 0, per, sweeps_each * n, cores)
         sweeps = per * sweeps_each
         total_sweeps += sweeps
         total_time += t
@@ -145,11 +145,11 @@ def run_reference_arm(args):
     sweeps_each = 100
     rates = []
     for _ in range(args.warmup):
-        run_batch(files[0], "", 0, cores, 20 * SIZES[0], cores)
+        run_batch(files[0], 0, cores, 20 * SIZES[0], cores)
     for _ in range(args.steps):
         tot_s, tot_t = 0.0, 0.0
         for i, f in enumerate(files):
-            t = run_batch(f, "", 0, per, sweeps_each * SIZES[i], cores)
+            t = run_batch(f, 0, per, sweeps_each * SIZES[i], cores)
             tot_s += per * sweeps_each
             tot_t += t
         rates.append(tot_s / tot_t)

@@ -148,6 +148,22 @@ ldo_status ldo_pt_get_permutation(ldo_engine* e, int32_t* out, int n);
 /* Swap attempts and acceptances per neighbouring slot pair, summed over ladders. */
 ldo_status ldo_pt_get_stats(ldo_engine* e, int64_t* attempts, int64_t* accepts, int n_pairs);
 
+/* Host-only helpers (no GPU needed). */
+
+/* Reduced hybridisation enthalpy H/(RT) and entropy S/R of a fully paired
+ * duplex with top strand `seq` (nearestNeighbour::
+ * calc_unitless_hybridization_thermo, src/nearest_neighbour.cpp:34). */
+ldo_status ldo_nn_duplex_thermo(const char* seq, double temp, double cation_M, double* h, double* s);
+
+/* Energy tables of the system of an .inp file at (temp, stacking_mult), as
+ * OrigamiPotential::calc_energies builds them (src/origami_potential.cpp:1057):
+ * dense (2*imax+1)^2 row-major arrays over identity pairs (i+imax, j+imax) of
+ * hybridisation free energy, enthalpy, entropy and stacking energy (kT units),
+ * and init[3] = initiation enthalpy, entropy, free energy.  *imax receives the
+ * largest |identity|; arrays must hold cap doubles. */
+ldo_status ldo_energy_tables(const char* inp_path, double temp, double stacking_mult, int* imax, double* hyb_e,
+                             double* hyb_h, double* hyb_s, double* stack, double* init, int cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1067,3 +1067,47 @@ ldo_status ldo_set_window(ldo_engine* e, const char* tag, int replica, int min_o
 }
 
 } // extern "C"
+
+extern "C" {
+
+ldo_status ldo_nn_duplex_thermo(const char* seq, double temp, double cation_M, double* h, double* s) {
+    if (!seq || !h || !s || !(temp > 0) || !(cation_M > 0)) return LDO_EINVAL;
+    return guard(nullptr, [&]() {
+        static const ldo_host::NNParams P;
+        ldo_host::HS x = ldo_host::reduce(ldo_host::duplex_hs(P, seq, cation_M), temp);
+        *h = x.h;
+        *s = x.s;
+    });
+}
+
+ldo_status ldo_energy_tables(const char* inp_path, double temp, double stacking_mult, int* imax, double* hyb_e,
+                             double* hyb_h, double* hyb_s, double* stack, double* init, int cap) {
+    if (!inp_path || !imax) return LDO_EINVAL;
+    return guard(nullptr, [&]() {
+        HostSystem hs = load_system(inp_path, "");
+        ldo_host::EnergyInputs in = hs.energy;
+        in.temp = temp;
+        in.stacking_mult = stacking_mult;
+        ldo_host::Tables t = ldo_host::build_tables(hs.sf.identities, hs.sf.sequences, in);
+        *imax = t.imax;
+        int dim = t.dim;
+        if (!hyb_e) return;
+        if (dim * dim > cap) throw LdoError(LDO_EINVAL, "table buffer too small");
+        for (int a = -t.imax; a <= t.imax; ++a)
+            for (int b = -t.imax; b <= t.imax; ++b) {
+                size_t k = (size_t)(a + t.imax) * dim + (size_t)(b + t.imax);
+                size_t src = t.dense ? k : (a == -b ? (size_t)std::abs(a) : (size_t)t.imax + 1);
+                hyb_e[k] = t.e[src];
+                if (hyb_h) hyb_h[k] = t.h[src];
+                if (hyb_s) hyb_s[k] = t.s[src];
+                if (stack) stack[k] = t.stack_dense ? t.stack[k] : t.stack_const;
+            }
+        if (init) {
+            init[0] = t.init_h;
+            init[1] = t.init_s;
+            init[2] = t.init_e;
+        }
+    });
+}
+
+} // extern "C"

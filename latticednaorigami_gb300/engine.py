@@ -18,7 +18,8 @@ EXPORTS = [
     "ldo_create_from_inp", "ldo_create_multi", "ldo_destroy", "ldo_last_error", "ldo_num_replicas",
     "ldo_set_controls", "ldo_run", "ldo_run_sweeps", "ldo_state_bytes", "ldo_get_observables", "ldo_get_config", "ldo_set_sampling",
     "ldo_get_samples", "ldo_set_trace", "ldo_get_trace", "ldo_get_move_stats", "ldo_set_grid_bias",
-    "ldo_set_window", "ldo_pt_run", "ldo_pt_get_permutation", "ldo_pt_get_stats",
+    "ldo_set_window", "ldo_pt_run", "ldo_pt_get_permutation", "ldo_pt_get_stats", "ldo_nn_duplex_thermo",
+    "ldo_energy_tables",
 ]
 
 
@@ -75,6 +76,9 @@ def load_library(path=None):
     lib.ldo_pt_run.argtypes = [vp, ip, ctypes.c_int64, ip, ip, dp]
     lib.ldo_pt_get_permutation.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ip]
     lib.ldo_pt_get_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64), ip]
+    lib.ldo_nn_duplex_thermo.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, dp, dp]
+    lib.ldo_energy_tables.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
+                                      dp, dp, dp, dp, dp, ip]
     if path is None:
         _lib = lib
     return lib
@@ -201,3 +205,31 @@ class Engine:
         self._check(self.lib.ldo_pt_get_stats(self.h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
                                               b.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), n_pairs))
         return a, b
+
+
+def nn_duplex_thermo(seq, temp, cation_M):
+    """Reduced (H/RT, S/R) of a fully paired duplex (host-side helper)."""
+    lib = load_library()
+    h, s = ctypes.c_double(), ctypes.c_double()
+    rc = lib.ldo_nn_duplex_thermo(seq.encode(), temp, cation_M, ctypes.byref(h), ctypes.byref(s))
+    if rc != 0:
+        raise LdoError(rc, lib.ldo_last_error(None).decode())
+    return h.value, s.value
+
+
+def energy_tables(inp, temp, stacking_mult=1.0):
+    """Dense energy tables of an .inp system at one temperature (host-side helper)."""
+    lib = load_library()
+    imax = ctypes.c_int()
+    rc = lib.ldo_energy_tables(os.fsencode(inp), temp, stacking_mult, ctypes.byref(imax), None, None, None, None,
+                               None, 0)
+    if rc != 0:
+        raise LdoError(rc, lib.ldo_last_error(None).decode())
+    d = 2 * imax.value + 1
+    arrs = [np.zeros(d * d) for _ in range(4)]
+    init = np.zeros(3)
+    rc = lib.ldo_energy_tables(os.fsencode(inp), temp, stacking_mult, ctypes.byref(imax), *[_dptr(a) for a in arrs],
+                               _dptr(init), d * d)
+    if rc != 0:
+        raise LdoError(rc, lib.ldo_last_error(None).decode())
+    return imax.value, [a.reshape(d, d) for a in arrs], init
