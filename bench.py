@@ -109,29 +109,41 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(files, sys_of, taus_per_size, budget_s=15.0):
-    """Oracle (CPU restatement) on all host cores, bounded sample of the same
-    workload; returns effective samples/s using the GPU-measured tau_int."""
-    from oracle_lib import run_batch
-    cores = os.cpu_count() or 1
-    per = max(1, 2 * cores // len(files))
-    total_sweeps = 0.0
-    total_time = 0.0
-    ess_rate = 0.0
-    sweeps_each = 200
+CPU_REPS_PER_SIZE = 64
+CPU_BURN_SWEEPS = 300
+CPU_SWEEPS = 1500
+
+
+def cpu_effective_rate(files, cores):
+    """The oracle port on all host cores over a bounded sample of the same
+    workload (64 replicas of each scaffold size, 300 burn-in + 1500 recorded
+    sweeps), with tau_int estimated from its own samples by the same
+    estimator.  Returns (effective samples/s, sweeps/s, median tau)."""
+    from oracle_lib import run_batch_sampled
+    from latticednaorigami_gb300.analysis import effective_samples
+    ess_total, t_total, sweeps_total = 0.0, 0.0, 0.0
+    taus = []
     for i, f in enumerate(files):
         n = SIZES[i]
-        t = run_batch(f, 0, per, sweeps_each * n, cores)
-        sweeps = per * sweeps_each
-        total_sweeps += sweeps
-        total_time += t
-        tau = taus_per_size.get(n) or 0.5
-        ess_rate += (sweeps / t) / (2 * tau) * 0.25   # uniform mix of the four sizes
-    sweeps_per_s = total_sweeps / total_time
-    return {"value": ess_rate, "unit": "effective samples/s", "cores": cores, "kind": "port",
-            "sample": "%d replicas x %d sweeps of each of the 4 scaffold sizes on %d threads; "
-                      "tau_int from the GPU run" % (per, sweeps_each, cores),
-            "sweeps_per_s": sweeps_per_s}
+        t, smp = run_batch_sampled(f, 0, CPU_REPS_PER_SIZE, CPU_BURN_SWEEPS + CPU_SWEEPS, n, cores)
+        rec = smp[:, CPU_BURN_SWEEPS:]
+        ess, tau = effective_samples(list(rec))
+        frac = CPU_SWEEPS / float(CPU_BURN_SWEEPS + CPU_SWEEPS)
+        ess_total += ess
+        t_total += t * frac
+        sweeps_total += CPU_REPS_PER_SIZE * CPU_SWEEPS
+        if tau is not None:
+            taus.append(tau)
+    return ess_total / t_total, sweeps_total / t_total, (float(np.median(taus)) if taus else None)
+
+
+def cpu_baseline(files):
+    cores = os.cpu_count() or 1
+    rate, sweeps_per_s, tau = cpu_effective_rate(files, cores)
+    return {"value": rate, "unit": "effective samples/s", "cores": cores, "kind": "port",
+            "sample": "%d replicas of each scaffold size x %d recorded sweeps (after %d burn-in) on %d threads"
+                      % (CPU_REPS_PER_SIZE, CPU_SWEEPS, CPU_BURN_SWEEPS, cores),
+            "sweeps_per_s": sweeps_per_s, "tau_int_median": tau}
 
 
 def run_reference_arm(args):
@@ -139,37 +151,31 @@ def run_reference_arm(args):
     reference itself cannot be built on the GPU machine) on all host cores."""
     tmp = tempfile.mkdtemp()
     files = write_c2(tmp)
-    from oracle_lib import run_batch
     cores = os.cpu_count() or 1
-    per = max(1, 2 * cores // len(files))
-    sweeps_each = 100
-    rates = []
+    from oracle_lib import run_batch
     for _ in range(args.warmup):
         run_batch(files[0], 0, cores, 20 * SIZES[0], cores)
+    rates, sps, taus, times = [], [], [], []
     for _ in range(args.steps):
-        tot_s, tot_t = 0.0, 0.0
-        for i, f in enumerate(files):
-            t = run_batch(f, 0, per, sweeps_each * SIZES[i], cores)
-            tot_s += per * sweeps_each
-            tot_t += t
-        rates.append(tot_s / tot_t)
-    sweeps_per_s = float(np.mean(rates))
-    tau = 0.5 * 20  # placeholder replaced below when a GPU tau is known
-    tau_path = os.path.join(ROOT, "profiles", "c2_tau.json")
-    if os.path.exists(tau_path):
-        with open(tau_path) as f:
-            tau = json.load(f)["tau_int_median"]
-    value = sweeps_per_s / (2 * tau)
+        t0 = time.perf_counter()
+        r, s_, tau = cpu_effective_rate(files, cores)
+        times.append(time.perf_counter() - t0)
+        rates.append(r)
+        sps.append(s_)
+        taus.append(tau)
+    value = float(np.mean(rates))
     line = {"impl": "reference", "metric": "effective samples/s (tau_int of #bound domains), plain MC",
             "value": value, "unit": "effective samples/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 * per * sweeps_each * 4 / sweeps_per_s,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": "c2: 4096 chains, scaffolds 8/12/16/24, uniform hyb"},
+            "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(times)), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "c2: constant-T chains, scaffolds 8/12/16/24, uniform hyb, T~U[320,350] K; "
+                                   "bounded CPU sample per step"},
             "cpu_baseline": {"value": value, "unit": "effective samples/s", "cores": cores, "kind": "port",
-                             "sample": "%d replicas x %d sweeps per size per step" % (per, sweeps_each)},
+                             "sample": "%d replicas of each scaffold size x %d recorded sweeps per step"
+                                       % (CPU_REPS_PER_SIZE, CPU_SWEEPS)},
             "e2e": {"value": value, "unit": "effective samples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "sweeps_per_s": sweeps_per_s}
+            "sweeps_per_s": float(np.mean(sps)), "tau_int_median": taus[-1]}
     print(json.dumps(line))
 
 
@@ -270,7 +276,7 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind},
             "clocks": clk}
     if not args.no_cpu and rank == 0:
-        line["cpu_baseline"] = cpu_baseline(files, sys_of, taus_per_size)
+        line["cpu_baseline"] = cpu_baseline(files)
     print(json.dumps(line))
 
 

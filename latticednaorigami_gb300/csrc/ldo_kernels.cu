@@ -64,51 +64,64 @@ __device__ void bind_rep(ldo::Rep& r, const LdoLaunch& L, unsigned char* base, i
     r.rng.init(r.ctl->seed, r.ctl->rep, 0u, r.h->draws);
 }
 
-__global__ void __launch_bounds__(128, 8) ldo_mc_kernel(LdoLaunch L) {
+__host__ __device__ constexpr int task_bytes() { return (int)((sizeof(ldo::ProbeTask) + 15) / 16 * 16); }
+__host__ __device__ constexpr int rep_bytes() { return (int)((sizeof(ldo::Rep) + 15) / 16 * 16); }
+
+// Shared memory per warp: replica state | probe task | Rep (the working object).
+__global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
     extern __shared__ __align__(16) unsigned char smem[];
     int warp = threadIdx.x >> 5;
     int lane = threadIdx.x & 31;
     int rep = blockIdx.x * L.warps_per_block + warp;
     if (rep >= L.n_rep) return;
-    unsigned char* base = smem + (size_t)warp * L.lay.bytes;
+    unsigned char* base = smem + (size_t)warp * (L.lay.bytes + task_bytes() + rep_bytes());
+    ldo::ProbeTask* task = reinterpret_cast<ldo::ProbeTask*>(base + L.lay.bytes);
+    ldo::Rep* R = reinterpret_cast<ldo::Rep*>(base + L.lay.bytes + task_bytes());
     unsigned char* gbase = L.arena + (size_t)rep * L.lay.bytes;
     warp_copy16(base, gbase, L.lay.bytes, lane);
     __syncwarp();
     if (lane == 0) {
-        ldo::Rep r;
-        bind_rep(r, L, base, rep);
-        LdoHdr* h = r.h;
+        task->cmd = 0;
+        bind_rep(*R, L, base, rep);
+        R->task = task;
+    }
+    __syncwarp();
+    if (lane > 0 && lane < 6) {
+        // Lanes 1..5 evaluate CB trial positions for lane 0.
+        R->probe_helper_loop();
+    }
+    else if (lane == 0) {
+        LdoHdr* h = R->h;
         if (h->status == 0) {
             if (L.mode == LDO_MODE_INIT) {
-                r.set_all_current();
-                r.init_biases();
-                h->tab = r.ctl->tab;
+                R->set_all_current();
+                R->init_biases();
+                h->tab = R->ctl->tab;
             }
             else if (L.mode == LDO_MODE_RECOMPUTE) {
-                r.recompute_energy();
-                h->tab = r.ctl->tab;
+                R->recompute_energy();
+                h->tab = R->ctl->tab;
             }
             else if (L.mode == LDO_MODE_OBSERVE) {
                 // Reading observables changes nothing: the energy and the
                 // dependent quantities use the tables the energy was last
                 // computed with, even if the controls have moved since.
-                r.tab = L.tabs + h->tab;
+                R->tab = L.tabs + h->tab;
             }
             else {
-                if (L.force_recompute || h->tab != r.ctl->tab) {
-                    r.recompute_energy();
-                    h->tab = r.ctl->tab;
+                if (L.force_recompute || h->tab != R->ctl->tab) {
+                    R->recompute_energy();
+                    h->tab = R->ctl->tab;
                 }
                 double* tr = (rep < L.n_trace) ? L.trace + (size_t)rep * L.trace_max * 8 : nullptr;
-                long long unit = L.sweep_units ? (long long)r.ns : 1ll;
+                long long unit = L.sweep_units ? (long long)R->ns : 1ll;
                 long long nsteps = L.n_steps * unit;
                 long long sint = (long long)L.sample_interval * unit;
                 for (long long k = 0; k < nsteps; ++k) {
-                    if (r.bad()) break;
+                    if (R->bad()) break;
                     long long s = h->steps_done + 1;
-                    r.step(s);
+                    R->step(s);
                     h->steps_done = s;
-                    h->draws = r.rng.draws;
                     if (tr && k < L.trace_max) {
                         double* t = tr + 8 * k;
                         t[0] = (double)s;
@@ -117,8 +130,8 @@ __global__ void __launch_bounds__(128, 8) ldo_mc_kernel(LdoLaunch L) {
                         t[3] = h->num_fully;
                         t[4] = h->num_bound;
                         t[5] = h->num_stacked;
-                        t[6] = h->move_bias * r.ctl->bias_mult;
-                        t[7] = (double)r.rng.draws;
+                        t[6] = h->move_bias * R->ctl->bias_mult;
+                        t[7] = (double)R->rng.draws;
                     }
                     if (sint > 0 && s % sint == 0) {
                         int c = h->sample_count;
@@ -131,9 +144,10 @@ __global__ void __launch_bounds__(128, 8) ldo_mc_kernel(LdoLaunch L) {
                     }
                 }
             }
-            if (L.want_dep && !r.bad()) r.dependent_quantities();
-            h->draws = r.rng.draws;
+            if (L.want_dep && !R->bad()) R->dependent_quantities();
+            h->draws = R->rng.draws;
         }
+        R->post_exit();
     }
     __syncwarp();
     warp_copy16(gbase, base, L.lay.bytes, lane);
@@ -216,7 +230,7 @@ cudaError_t ldo_launch_pt_swap(const LdoPT& P, cudaStream_t stream) {
 
 cudaError_t ldo_launch_mc(const LdoLaunch& L, cudaStream_t stream) {
     int wpb = L.warps_per_block;
-    size_t smem = (size_t)wpb * L.lay.bytes;
+    size_t smem = (size_t)wpb * (L.lay.bytes + task_bytes() + rep_bytes());
     cudaError_t err = cudaFuncSetAttribute(ldo_mc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
     int blocks = (L.n_rep + wpb - 1) / wpb;

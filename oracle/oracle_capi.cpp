@@ -384,4 +384,43 @@ double oracle_run_batch(const char* inp_path, const char* overrides, uint32_t se
     return failed.load() ? -2 : dt;
 }
 
+// CPU baseline with order-parameter samples: n_rep replicas (key (seed0, r)),
+// each `sweeps` sweeps of sweep_len steps; after every sweep the number of
+// fully bound domain pairs goes to out[r * sweeps + k].  Returns wall seconds.
+double oracle_run_batch_sampled(const char* inp_path, const char* overrides, uint32_t seed0, int n_rep,
+                                long long sweeps, int sweep_len, int threads, short* out) {
+    std::vector<Replica*> reps(n_rep, nullptr);
+    for (int i = 0; i < n_rep; ++i) {
+        reps[i] = build(inp_path, overrides, seed0, (uint32_t)i);
+        if (!reps[i]) {
+            for (auto* r : reps) delete r;
+            return -1;
+        }
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<std::thread> pool;
+    std::atomic<int> next {0};
+    std::atomic<int> failed {0};
+    for (int t = 0; t < threads; ++t)
+        pool.emplace_back([&]() {
+            for (;;) {
+                int i = next.fetch_add(1);
+                if (i >= n_rep) break;
+                try {
+                    long long st = 0;
+                    for (long long k = 0; k < sweeps; ++k) {
+                        for (int q = 0; q < sweep_len; ++q) reps[i]->sys.step(++st);
+                        out[(size_t)i * sweeps + k] = (short)reps[i]->sys.num_fully;
+                    }
+                } catch (...) {
+                    failed.store(1);
+                }
+            }
+        });
+    for (auto& th : pool) th.join();
+    double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    for (auto* r : reps) delete r;
+    return failed.load() ? -2 : dt;
+}
+
 } // extern "C"

@@ -128,3 +128,18 @@ def swap_uniform(seed, ladder, index):
     out = np.zeros(1)
     L.oracle_swap_uniforms(seed, ladder, index, 1, out.ctypes.data)
     return float(out[0])
+
+
+def run_batch_sampled(inp, seed, n_rep, sweeps, sweep_len, threads, overrides=""):
+    """CPU baseline with one numfulldomains sample per replica per sweep:
+    returns (wall seconds, samples[n_rep, sweeps])."""
+    L = lib()
+    L.oracle_run_batch_sampled.restype = ctypes.c_double
+    L.oracle_run_batch_sampled.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_int,
+                                           ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    out = np.zeros((n_rep, sweeps), np.int16)
+    t = L.oracle_run_batch_sampled(os.fsencode(inp), overrides.encode(), seed, n_rep, sweeps, sweep_len, threads,
+                                   out.ctypes.data)
+    if t < 0:
+        raise OracleError(L.oracle_last_error().decode() or "oracle batch failed")
+    return t, out
