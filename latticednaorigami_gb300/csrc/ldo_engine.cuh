@@ -108,7 +108,7 @@ struct Rng {
         draws = d;
         cblock = ~0ull;
     }
-    __device__ unsigned long long next64() {
+    __device__ __noinline__ unsigned long long next64() {
         unsigned long long b = draws >> 1;
         if (b != cblock) {
             philox10((uint32_t)b, (uint32_t)(b >> 32), stream, 0u, k0, k1, w);
@@ -118,8 +118,8 @@ struct Rng {
         ++draws;
         return ((unsigned long long)w[j] << 32) | w[j + 1];
     }
-    __device__ double uniform_real() { return (double)(next64() >> 11) * 0x1.0p-53; }
-    __device__ int uniform_int(int lo, int hi) {
+    __device__ __noinline__ double uniform_real() { return (double)(next64() >> 11) * 0x1.0p-53; }
+    __device__ __noinline__ int uniform_int(int lo, int hi) {
         unsigned long long range = (unsigned long long)((long long)hi - (long long)lo) + 1ull;
         return lo + (int)__umul64hi(next64(), range);
     }
@@ -147,6 +147,10 @@ struct Delta {
     double e;
     int stacked;
 };
+
+// One out-of-line copy of exp keeps the hot code small (instruction fetch,
+// not arithmetic, limits this kernel).
+__device__ __noinline__ double dexp(double x) { return exp(x); }
 
 struct Scratch {
     // MCMovetype reversal lists (include/.../movetypes.hpp:156-163)
@@ -198,23 +202,42 @@ __device__ __forceinline__ int lane_id() {
 // One Rep per warp lives in shared memory next to the replica's state; its
 // member data must never sit in a thread's local memory, where a single
 // active lane would touch one 128-byte line per 4-byte access.
-struct Rep {
+template <class C>
+struct Rep : public LdoState<C> {
+    using S_ = LdoState<C>;
+    using S_::hdr;
+    using S_::hash;
+    using S_::bias;
+    using S_::mstat;
+    using S_::chain_c;
+    using S_::op;
+    using S_::px;
+    using S_::py;
+    using S_::pz;
+    using S_::bnd;
+    using S_::did;
+    using S_::type_count;
+    using S_::ore;
+    using S_::st;
+    using S_::scs;
+    using S_::sd;
+    using S_::chain_type;
+    using S_::chain_order;
+    using S_::clen;
+    static constexpr int hmask = C::HCAP - 1;
+    static constexpr int hshift = 64 - (C::HCAP == 256 ? 8 : C::HCAP == 512 ? 9 : C::HCAP == 1024 ? 10 : C::HCAP == 2048 ? 11 : 12);
+
     const LdoSys* sys;
     const LdoTab* tab;
     const double* bank;
     const LdoRepCtl* ctl;
     const double* grid;
-    LdoHdr* h;
-    int16_t *px, *py, *pz, *bnd, *did;
-    uint8_t *ore, *st, *scs, *sd;
-    int32_t* chain_c;
-    uint8_t *chain_type, *chain_order;
-    int16_t* type_count;
-    unsigned long long* hash;
-    double* bias;
-    int32_t* op;
-    long long* mstat;
-    int hmask, hshift, ns, lmax, nmv;
+    // scalars of the current table set and controls, cached in the object
+    int t_dense, t_stack_dense, imax, dim;
+    long long t_off_e, t_off_h, t_off_s, t_off_stack;
+    double t_stack_const, t_init_e, t_init_h, t_init_s;
+    double c_staple_M, c_bias_mult;
+    int ns, lmax, nmv;
     int cyclic, tqt, mean_field;
     Rng rng;
     FBState fbs[6];
@@ -263,9 +286,9 @@ struct Rep {
 
     // ---------------------------------------------------------- errors ---
     __device__ void fail(int code) {
-        if (h->status == 0) h->status = code;
+        if (hdr.status == 0) hdr.status = code;
     }
-    __device__ bool bad() const { return h->status != 0; }
+    __device__ bool bad() const { return hdr.status != 0; }
 
     // -------------------------------------------------------- accessors ---
     __device__ V3 pos(int i) const { return mk(px[i], py[i], pz[i]); }
@@ -279,7 +302,7 @@ struct Rep {
         pz[i] = (int16_t)p.z;
     }
     __device__ V3 orev(int i) const { return unit(ore[i]); }
-    __device__ int chain_len(int cs) const { return cs == 0 ? ns : sys->type_len[chain_type[cs]]; }
+    __device__ int chain_len(int cs) const { return clen[cs]; }
     __device__ int slot_of(int cs, int d) const { return cs == 0 ? d : ns + (cs - 1) * lmax + d; }
     __device__ int cidx(int i) const { return chain_c[scs[i]]; }
     __device__ int fwd(int i) const {
@@ -293,24 +316,35 @@ struct Rep {
         return (cs == 0 && cyclic) ? i + chain_len(cs) - 1 : -1;
     }
     __device__ int next(int i, int incr) const {   // Domain::operator+ (src/domain.cpp:9)
+        #pragma unroll 1
         while (i >= 0 && incr > 0) { i = fwd(i); --incr; }
+        #pragma unroll 1
         while (i >= 0 && incr < 0) { i = bwd(i); ++incr; }
         return i;
     }
-    __device__ double tval(long long off, int a, int b) const {
-        const LdoSys* s = sys;
-        if (tab->dense) return bank[off + (long long)(a + s->imax) * s->dim + (b + s->imax)];
-        return (a == -b) ? bank[off + (a < 0 ? -a : a)] : bank[off + s->imax + 1];
+    __device__ void bind_tables(const LdoTab* t) {
+        tab = t;
+        t_dense = t->dense;
+        t_stack_dense = t->stack_dense;
+        t_off_e = t->off_e;
+        t_off_h = t->off_h;
+        t_off_s = t->off_s;
+        t_off_stack = t->off_stack;
+        t_stack_const = t->stack_const;
+        t_init_e = t->init_e;
+        t_init_h = t->init_h;
+        t_init_s = t->init_s;
     }
-    __device__ double hyb(int i, int j) const { return tval(tab->off_e, did[i], did[j]); }
-    __device__ double hyb_h(int i, int j) const { return tval(tab->off_h, did[i], did[j]); }
-    __device__ double hyb_s(int i, int j) const { return tval(tab->off_s, did[i], did[j]); }
+    __device__ double tval(long long off, int a, int b) const {
+        if (t_dense) return __ldg(bank + off + (long long)(a + imax) * dim + (b + imax));
+        return (a == -b) ? __ldg(bank + off + (a < 0 ? -a : a)) : __ldg(bank + off + imax + 1);
+    }
+    __device__ double hyb(int i, int j) const { return tval(t_off_e, did[i], did[j]); }
+    __device__ double hyb_h(int i, int j) const { return tval(t_off_h, did[i], did[j]); }
+    __device__ double hyb_s(int i, int j) const { return tval(t_off_s, did[i], did[j]); }
     __device__ double stack(int i, int j) const {
-        if (tab->stack_dense) {
-            const LdoSys* s = sys;
-            return bank[tab->off_stack + (long long)(did[i] + s->imax) * s->dim + (did[j] + s->imax)];
-        }
-        return tab->stack_const;
+        if (t_stack_dense) return __ldg(bank + t_off_stack + (long long)(did[i] + imax) * dim + (did[j] + imax));
+        return t_stack_const;
     }
 
     // ------------------------------------------------------------ hash ---
@@ -320,6 +354,7 @@ struct Rep {
     // Index of the entry for key, or -1 (then *empty_at is the first free slot).
     __device__ __noinline__ int hfind(unsigned long long key, int* empty_at) const {
         int k = home(key);
+        #pragma unroll 1
         for (int n = 0; n <= hmask; ++n) {
             unsigned long long e = hash[k];
             if (!(e & LDO_VALID)) {
@@ -334,6 +369,7 @@ struct Rep {
     }
     __device__ __noinline__ void herase(int i) {
         int j = i;
+        #pragma unroll 1
         for (int n = 0; n <= hmask; ++n) {
             j = (j + 1) & hmask;
             unsigned long long e = hash[j];
@@ -372,7 +408,8 @@ struct Rep {
     __device__ __noinline__ int add_chain_with_index(int type, int c_i) {
         int cs = -1;
         int kmax = sys->kmax;
-        for (int k = 1; k <= kmax; ++k)
+        #pragma unroll 1
+        for (int k = 1; k <= kmax && k <= C::KMAX; ++k)
             if (chain_type[k] == 0xff) { cs = k; break; }
         if (cs < 0) {
             fail(LDO_RS_CAPACITY);
@@ -380,44 +417,48 @@ struct Rep {
         }
         chain_c[cs] = c_i;
         chain_type[cs] = (uint8_t)type;
-        chain_order[h->n_chains++] = (uint8_t)cs;
+        clen[cs] = (uint8_t)sys->type_len[type];
+        chain_order[hdr.n_chains++] = (uint8_t)cs;
         type_count[type]++;
         int len = sys->type_len[type];
         int off = sys->type_off[type];
+        #pragma unroll 1
         for (int d = 0; d < len; ++d) {
             int s = slot_of(cs, d);
             st[s] = UNASSIGNED;
             bnd[s] = -1;
             did[s] = sys->idents[off + d];
         }
-        h->num_domains += len;
-        h->num_unassigned += len;
-        h->num_staples++;
+        hdr.num_domains += len;
+        hdr.num_unassigned += len;
+        hdr.num_staples++;
         return cs;
     }
     // OrigamiSystem::add_chain(c_i_ident) (src/origami_system.cpp:387)
     __device__ __noinline__ int add_chain(int type) {
-        h->current_c_i += 1;
-        if (mean_field) h->energy += log6;
-        h->energy += tab->init_e;
-        return add_chain_with_index(type, h->current_c_i);
+        hdr.current_c_i += 1;
+        if (mean_field) hdr.energy += log6;
+        hdr.energy += t_init_e;
+        return add_chain_with_index(type, hdr.current_c_i);
     }
     // OrigamiSystem::delete_chain (src/origami_system.cpp:445)
     __device__ __noinline__ void delete_chain(int cs) {
-        int n = h->n_chains;
+        int n = hdr.n_chains;
         int k = 0;
+        #pragma unroll 1
         while (k < n && chain_order[k] != cs) ++k;
+        #pragma unroll 1
         for (int q = k; q + 1 < n; ++q) chain_order[q] = chain_order[q + 1];
-        h->n_chains = n - 1;
+        hdr.n_chains = n - 1;
         int type = chain_type[cs];
         type_count[type]--;
         int len = sys->type_len[type];
-        h->num_domains -= len;
-        h->num_staples--;
-        h->num_unassigned -= len;
+        hdr.num_domains -= len;
+        hdr.num_staples--;
+        hdr.num_unassigned -= len;
         chain_type[cs] = 0xff;
-        if (mean_field) h->energy -= log6;
-        h->energy -= tab->init_e;
+        if (mean_field) hdr.energy -= log6;
+        hdr.energy -= t_init_e;
     }
 
     // ------------------------------------------------- state transitions ---
@@ -429,14 +470,14 @@ struct Rep {
         int occ = k < 0 ? UNASSIGNED : ent_occ(hash[k]);
         if (occ == UNBOUND) {
             int j = ent_slot(hash[k]);
-            h->num_bound += 1;
+            hdr.num_bound += 1;
             int ns_;
             if (did[i] == -did[j]) {
                 ns_ = BOUND;
-                h->num_fully += 1;
+                hdr.num_fully += 1;
             }
             else {
-                if (cidx(i) == cidx(j)) h->num_self += 1;
+                if (cidx(i) == cidx(j)) hdr.num_self += 1;
                 ns_ = MISBOUND;
             }
             st[i] = (uint8_t)ns_;
@@ -483,16 +524,16 @@ struct Rep {
         }
         switch (occ) {
         case BOUND:
-            h->num_fully -= 1;
-            h->num_bound -= 1;
-            dc = check_stacking<false>(i, j);
+            hdr.num_fully -= 1;
+            hdr.num_bound -= 1;
+            dc = check_stacking<true>(i, j);
             dc.e *= -1;
             dc.stacked *= -1;
             dc.e += unassign_bound(i);
             break;
         case MISBOUND:
-            h->num_bound -= 1;
-            if (cidx(j) == cidx(i)) h->num_self -= 1;
+            hdr.num_bound -= 1;
+            if (cidx(j) == cidx(i)) hdr.num_self -= 1;
             dc.e += unassign_bound(i);
             break;
         case UNBOUND: {
@@ -502,12 +543,12 @@ struct Rep {
             break;
         }
         default:
-            h->num_unassigned--;
+            hdr.num_unassigned--;
             break;
         }
         if (mean_field && occ == BOUND) {
-            if (h->num_fully == 0) dc.e -= 2 * log6;
-            else if (h->num_fully == 1) dc.e -= log3;
+            if (hdr.num_fully == 0) dc.e -= 2 * log6;
+            else if (hdr.num_fully == 1) dc.e -= log3;
         }
         return dc;
     }
@@ -521,16 +562,16 @@ struct Rep {
         switch (occ) {
         case BOUND:
         case MISBOUND:
-            h->violated = 1;
-            h->num_unassigned++;
+            hdr.violated = 1;
+            hdr.num_unassigned++;
             break;
         case UNBOUND:
             set_pos(i, p);
             ore[i] = (uint8_t)o;
             update_occupancies(i, p);
             if (bad()) return dc;
-            dc = bind_domain<false>(i);
-            h->violated = fbst().viol ? 1 : 0;
+            dc = bind_domain<true>(i);
+            hdr.violated = fbst().viol ? 1 : 0;
             break;
         default:
             set_pos(i, p);
@@ -538,9 +579,9 @@ struct Rep {
             update_occupancies(i, p);
             break;
         }
-        if (mean_field && !h->violated && st[i] == BOUND) {
-            if (h->num_fully == 1) dc.e += 2 * log6;
-            else if (h->num_fully == 2) dc.e += log3;
+        if (mean_field && !hdr.violated && st[i] == BOUND) {
+            if (hdr.num_fully == 1) dc.e += 2 * log6;
+            else if (hdr.num_fully == 2) dc.e += log3;
         }
         return dc;
     }
@@ -552,13 +593,13 @@ struct Rep {
             return 0;
         }
         Delta dc = internal_check(i, p, o);
-        if (h->violated) {
+        if (hdr.violated) {
             internal_unassign(i);
         }
         else {
-            h->energy += dc.e;
-            h->num_stacked += dc.stacked;
-            h->num_unassigned--;
+            hdr.energy += dc.e;
+            hdr.num_stacked += dc.stacked;
+            hdr.num_unassigned--;
         }
         return dc.e;
     }
@@ -575,25 +616,25 @@ struct Rep {
         }
         else if (st[i] == BOUND) {
             de += hyb(i, bnd[i]);
-            Delta dc = check_stacking<false>(i, bnd[i]);
+            Delta dc = check_stacking<true>(i, bnd[i]);
             de += dc.e;
-            h->num_stacked += dc.stacked;
+            hdr.num_stacked += dc.stacked;
         }
         if (mean_field && st[i] == BOUND) {
-            if (h->num_fully == 1) de += 2 * log6;
-            else if (h->num_fully == 2) de += log3;
+            if (hdr.num_fully == 1) de += 2 * log6;
+            else if (hdr.num_fully == 2) de += log3;
         }
-        h->energy += de;
-        h->num_unassigned--;
+        hdr.energy += de;
+        hdr.num_unassigned--;
         return de;
     }
 
     // unassign_domain (src/origami_system.cpp:375)
     __device__ __noinline__ double unassign_domain(int i) {
         Delta dc = internal_unassign(i);
-        h->energy += dc.e;
-        h->num_stacked += dc.stacked;
-        h->num_unassigned++;
+        hdr.energy += dc.e;
+        hdr.num_stacked += dc.stacked;
+        hdr.num_unassigned++;
         return dc.e;
     }
 
@@ -619,14 +660,16 @@ struct Rep {
         Delta dc = bind_domain<true>(dom);
         int v = f.viol ? 1 : 0;
         if (mean_field && !v && f.ov_st == BOUND) {
-            int nf = h->num_fully + 1;
+            int nf = hdr.num_fully + 1;
             if (nf == 1) dc.e += 2 * log6;
             else if (nf == 2) dc.e += log3;
         }
+        f.ov_d = -1;
+        f.ov_p = -1;
         *viol = v;
         return dc.e;
     }
-    // Lane k evaluates trial k of the current task (CB weight exp(-dE),
+    // Lane k evaluates trial k of the current task (CB weight dexp(-dE),
     // src/cb_movetypes.cpp:80-85).
     __device__ void probe_lane(int k) {
         volatile ProbeTask* t = task;
@@ -636,7 +679,7 @@ struct Rep {
         double de = overlay_probe(t->dom, t->ud[k], p, t->o[k], &v);
         if (!v) {
             double b = 1;
-            b *= exp(-de);
+            b *= dexp(-de);
             t->bf[k] = b;
         }
         t->viol[k] = v;
@@ -654,6 +697,7 @@ struct Rep {
     // Lanes 1..5: serve probe tasks until lane 0 posts LDO_TASK_EXIT.
     __device__ void probe_helper_loop() {
         volatile ProbeTask* t = task;
+        #pragma unroll 1
         for (;;) {
             __syncwarp(LDO_PROBE_LANES);
             if (t->cmd == LDO_TASK_EXIT) break;
@@ -669,17 +713,20 @@ struct Rep {
 
     // set_domain_orientation (src/origami_system.cpp:543)
     __device__ void set_domain_orientation(int i, int o) {
-        if (st[i] == BOUND) h->violated = 1;
+        if (st[i] == BOUND) hdr.violated = 1;
         else ore[i] = (uint8_t)o;
     }
 
     // center (src/origami_system.cpp:553)
     __device__ __noinline__ void center(int cd) {
         V3 ref = pos(cd);
+        #pragma unroll 1
         for (int k = 0; k <= hmask; ++k) hash[k] = 0ull;
-        for (int c = 0; c < h->n_chains; ++c) {
+        #pragma unroll 1
+        for (int c = 0; c < hdr.n_chains; ++c) {
             int cs = chain_order[c];
             int len = chain_len(cs);
+            #pragma unroll 1
             for (int d = 0; d < len; ++d) {
                 int s = slot_of(cs, d);
                 V3 np = sub(pos(s), ref);
@@ -693,13 +740,15 @@ struct Rep {
 
     // set_all_domains (src/origami_system.cpp:573)
     __device__ __noinline__ void set_all_current() {
-        for (int c = 0; c < h->n_chains && !bad(); ++c) {
+        #pragma unroll 1
+        for (int c = 0; c < hdr.n_chains && !bad(); ++c) {
             int cs = chain_order[c];
             int len = chain_len(cs);
+            #pragma unroll 1
             for (int d = 0; d < len; ++d) {
                 int s = slot_of(cs, d);
                 set_domain_config(s, pos(s), ore[s]);
-                if (h->violated) {
+                if (hdr.violated) {
                     fail(LDO_RS_INVARIANT);   // "Constaints in violation after move complete"
                     return;
                 }
@@ -709,14 +758,16 @@ struct Rep {
 
     // check_all_constraints (src/origami_system.cpp:267)
     __device__ __noinline__ void check_all_constraints() {
-        if (h->num_unassigned != 0) {
+        if (hdr.num_unassigned != 0) {
             fail(LDO_RS_INVARIANT);
             return;
         }
-        int nc = h->n_chains;
+        int nc = hdr.n_chains;
+        #pragma unroll 1
         for (int c = 0; c < nc; ++c) {
             int cs = chain_order[c];
             int len = chain_len(cs);
+            #pragma unroll 1
             for (int d = 0; d < len; ++d) {
                 int s = slot_of(cs, d);
                 if (st[s] == UNASSIGNED) {
@@ -727,37 +778,39 @@ struct Rep {
             }
         }
         unsigned long long nst = (unsigned long long)(nc - 1);
-        if (mean_field) h->energy -= nst * log6;
-        h->energy -= nst * tab->init_e;
-        if (h->num_stacked != 0) {
+        if (mean_field) hdr.energy -= nst * log6;
+        hdr.energy -= nst * t_init_e;
+        if (hdr.num_stacked != 0) {
             set_all_current();
             fail(LDO_RS_INVARIANT);
             return;
         }
         double eps = 0.000001;
-        if (h->energy < -eps || h->energy > eps) {
+        if (hdr.energy < -eps || hdr.energy > eps) {
             set_all_current();
             fail(LDO_RS_INVARIANT);
             return;
         }
-        h->energy = 0;
+        hdr.energy = 0;
         set_all_current();
-        if (mean_field) h->energy += nst * log6;
-        h->energy += nst * tab->init_e;
+        if (mean_field) hdr.energy += nst * log6;
+        hdr.energy += nst * t_init_e;
     }
 
     // update_energy (src/origami_system.cpp:808)
     __device__ __noinline__ void recompute_energy() {
-        int nc = h->n_chains;
+        int nc = hdr.n_chains;
+        #pragma unroll 1
         for (int c = 0; c < nc; ++c) {
             int cs = chain_order[c];
             int len = chain_len(cs);
+            #pragma unroll 1
             for (int d = 0; d < len; ++d) unassign_domain(slot_of(cs, d));
         }
-        h->energy = 0;
+        hdr.energy = 0;
         unsigned long long nst = (unsigned long long)(nc - 1);
-        if (mean_field) h->energy += nst * log6;
-        h->energy += nst * tab->init_e;
+        if (mean_field) hdr.energy += nst * log6;
+        hdr.energy += nst * t_init_e;
         set_all_current();
     }
 
@@ -766,10 +819,12 @@ struct Rep {
         double H = 0, S = 0;
         // "accounted" = partner of an earlier domain in chain order; a pair is
         // counted at its first domain.
-        int nc = h->n_chains;
+        int nc = hdr.n_chains;
+        #pragma unroll 1
         for (int c = 0; c < nc; ++c) {
             int cs = chain_order[c];
             int len = chain_len(cs);
+            #pragma unroll 1
             for (int d = 0; d < len; ++d) {
                 int s = slot_of(cs, d);
                 int o = st[s];
@@ -785,19 +840,20 @@ struct Rep {
         unsigned long long nst = (unsigned long long)(nc - 1);
         if (mean_field) {
             S -= nst * log6;
-            if (h->num_fully >= 1) S -= 2 * log6;
-            if (h->num_fully >= 2) S -= log3;
+            if (hdr.num_fully >= 1) S -= 2 * log6;
+            if (hdr.num_fully >= 2) S -= log3;
         }
-        H += nst * tab->init_h;
-        S += nst * tab->init_s;
-        h->H = H;
-        h->S = S;
-        h->stacking = h->energy - (H - S);
+        H += nst * t_init_h;
+        S += nst * t_init_s;
+        hdr.H = H;
+        hdr.S = S;
+        hdr.stacking = hdr.energy - (H - S);
     }
     // True if partner b comes before domain s (chain position c, index d) in
     // chain order, i.e. s was inserted into the reference's accounted set.
     __device__ __noinline__ bool visited_before(int s, int b, int c, int d) const {
         int cb = scs[b];
+        #pragma unroll 1
         for (int q = 0; q < c; ++q)
             if (chain_order[q] == cb) return true;
         if (cb == chain_order[c]) return sd[b] < d;
@@ -890,6 +946,7 @@ struct Rep {
     }
 
     template <bool OV> __device__ __noinline__ void constraints_around(int cd, int jj) {   // :231
+        #pragma unroll 1
         for (int k = -1; k <= 0; ++k) {
             int c1 = next(cd, k);
             int c2 = next(cd, k + 1);
@@ -976,6 +1033,7 @@ struct Rep {
             return;
         }
         if (jj == 1) return;
+        #pragma unroll 1
         for (int a = 0; a < 2; ++a) {
             int j1 = a == 0 ? next(c1, -1) : next(gbnd<OV>(c1), 1);
             int j2 = a == 0 ? c1 : gbnd<OV>(c1);
@@ -1144,6 +1202,7 @@ struct Rep {
             fa[nf] = j3_b; fb[nf] = j3_b_for; nf++;
             fa[nf] = j3_b; fb[nf] = j3_b_bac; nf++;
         }
+        #pragma unroll 1
         for (int a = 0; a < nf; ++a) {
             int k2 = fa[a], k1 = fb[a];
             if (!exists_bound<OV>(k1)) continue;
@@ -1165,6 +1224,7 @@ struct Rep {
                 sa[ns_] = k1_b; sb[ns_] = k1_b_for; ns_++;
                 sa[ns_] = k1_b; sb[ns_] = k1_b_bac; ns_++;
             }
+            #pragma unroll 1
             for (int b = 0; b < ns_; ++b) {
                 int j2 = sa[b], j1 = sb[b];
                 if (!exists_bound<OV>(j1)) continue;
@@ -1197,6 +1257,7 @@ struct Rep {
             fa[nf] = j2_b; fb[nf] = j2_b_for; nf++;
             fa[nf] = j2_b; fb[nf] = j2_b_bac; nf++;
         }
+        #pragma unroll 1
         for (int a = 0; a < nf; ++a) {
             int k1 = fa[a], k2 = fb[a];
             if (!exists_bound<OV>(k2)) continue;
@@ -1218,6 +1279,7 @@ struct Rep {
                 sa[ns_] = k2_b; sb[ns_] = k2_b_for; ns_++;
                 sa[ns_] = k2_b; sb[ns_] = k2_b_bac; ns_++;
             }
+            #pragma unroll 1
             for (int b = 0; b < ns_; ++b) {
                 int j3 = sa[b], j4 = sb[b];
                 if (!exists_bound<OV>(j4)) continue;
@@ -1247,6 +1309,7 @@ struct Rep {
             fa[nf] = kb1; fb[nf] = k1_b_for; nf++;
             fa[nf] = kb1; fb[nf] = k1_b_bac; nf++;
         }
+        #pragma unroll 1
         for (int a = 0; a < nf; ++a) {
             int j2 = fa[a], j1 = fb[a];
             if (!exists_bound<OV>(j1)) continue;
@@ -1265,6 +1328,7 @@ struct Rep {
                 sa[ns_] = kb2; sb[ns_] = k2_b_for; ns_++;
                 sa[ns_] = kb2; sb[ns_] = k2_b_bac; ns_++;
             }
+            #pragma unroll 1
             for (int b = 0; b < ns_; ++b) {
                 int j3 = sa[b], j4 = sb[b];
                 if (!exists_bound<OV>(j4)) continue;
@@ -1312,12 +1376,14 @@ struct Rep {
 
     // ======================================== order parameters / biases ===
     __device__ __noinline__ bool staple_type_fully_bound(int type) const {
-        int nc = h->n_chains;
+        int nc = hdr.n_chains;
+        #pragma unroll 1
         for (int c = 1; c < nc; ++c) {
             int cs = chain_order[c];
             if (chain_type[cs] != type) continue;
             int len = chain_len(cs);
             bool full = true;
+            #pragma unroll 1
             for (int d = 0; d < len; ++d)
                 if (st[slot_of(cs, d)] != BOUND) { full = false; break; }
             if (full) return true;
@@ -1327,18 +1393,20 @@ struct Rep {
     // SystemOrderParams::update_move_params (src/order_params.cpp:595)
     __device__ __noinline__ void update_move_params() {
         const LdoSys* s = sys;
+        #pragma unroll 1
         for (int q = 0; q < s->n_ops; ++q) {
             int v = 0;
             int defined = 1;
             switch (s->op_kind[q]) {
-            case LDO_OP_NUMSTAPLES: v = h->num_staples; break;
+            case LDO_OP_NUMSTAPLES: v = hdr.num_staples; break;
             case LDO_OP_NUMSTAPLESTYPE: v = type_count[s->op_arg[q]]; break;
             case LDO_OP_STAPLETYPEFULLYBOUND: v = staple_type_fully_bound(s->op_arg[q]) ? 1 : 0; break;
-            case LDO_OP_NUMBOUND: v = h->num_fully; break;
-            case LDO_OP_NUMMISBOUND: v = h->num_bound - h->num_fully; break;
-            case LDO_OP_NUMSTACKED: v = h->num_stacked; break;
+            case LDO_OP_NUMBOUND: v = hdr.num_fully; break;
+            case LDO_OP_NUMMISBOUND: v = hdr.num_bound - hdr.num_fully; break;
+            case LDO_OP_NUMSTACKED: v = hdr.num_stacked; break;
             case LDO_OP_ZERO: v = 0; break;
             case LDO_OP_SUM: {
+                #pragma unroll 1
                 for (int p = 0; p < s->op_nparts[q]; ++p) {
                     int part = s->op_parts[q][p];
                     if (op[2 * part + 1]) v += op[2 * part];
@@ -1383,21 +1451,23 @@ struct Rep {
     // SystemBiases::calc_move (src/bias_functions.cpp:475)
     __device__ __noinline__ double calc_move() {
         double diff = 0;
+        #pragma unroll 1
         for (int b = 0; b < sys->n_biases; ++b) {
             double prev = bias[b];
             double nb = bias_value(b);
             bias[b] = nb;
             diff += nb - prev;
         }
-        h->move_bias += diff;
-        return diff * ctl->bias_mult;
+        hdr.move_bias += diff;
+        return diff * c_bias_mult;
     }
     __device__ __noinline__ void init_biases() {
         update_move_params();
-        h->move_bias = 0;
+        hdr.move_bias = 0;
+        #pragma unroll 1
         for (int b = 0; b < sys->n_biases; ++b) {
             bias[b] = bias_value(b);
-            h->move_bias += bias[b];
+            hdr.move_bias += bias[b];
         }
     }
 
@@ -1416,13 +1486,15 @@ struct Rep {
     }
 
     __device__ __noinline__ void reset_origami() {   // src/movetypes.cpp:53
+        #pragma unroll 1
         for (int n = 0; n < m.n_asg; ++n) unassign_domain(m.asg[n]);
         if (m.added_cs >= 0) {
             delete_chain(m.added_cs);
-            h->current_c_i -= 1;
+            hdr.current_c_i -= 1;
         }
+        #pragma unroll 1
         for (int n = 0; n < m.n_mod; ++n) set_checked(m.mod[n], m.mod_pos[n], m.mod_ore[n]);
-        h->violated = 0;
+        hdr.violated = 0;
     }
 
     __device__ __noinline__ bool test_acceptance(double p) {   // src/movetypes.cpp:142
@@ -1432,8 +1504,9 @@ struct Rep {
     }
 
     __device__ __noinline__ int select_random_domain() {   // src/movetypes.cpp:98
-        int idx = rng.uniform_int(0, h->num_domains - 1);
-        int nc = h->n_chains;
+        int idx = rng.uniform_int(0, hdr.num_domains - 1);
+        int nc = hdr.n_chains;
+        #pragma unroll 1
         for (int c = 0; c < nc; ++c) {
             int cs = chain_order[c];
             int len = chain_len(cs);
@@ -1448,6 +1521,7 @@ struct Rep {
     // the staple, over bound and misbound pairs.
     __device__ __noinline__ bool staple_is_connector(int cs) {
         int len = chain_len(cs);
+        #pragma unroll 1
         for (int d = 0; d < len; ++d) {
             int i = slot_of(cs, d);
             if (st[i] == UNBOUND) continue;
@@ -1466,9 +1540,11 @@ struct Rep {
         uint8_t* stack_ = dfs_stack;
         int sp = 0;
         stack_[sp++] = (uint8_t)start;
+        #pragma unroll 1
         while (sp > 0) {
             int x = stack_[--sp];
             int len = chain_len(x);
+            #pragma unroll 1
             for (int d = 0; d < len; ++d) {
                 int b = bnd[slot_of(x, d)];
                 if (b < 0) continue;
@@ -1485,6 +1561,7 @@ struct Rep {
 
     __device__ __noinline__ int num_bound_staple_domains(int cs) const {   // src/movetypes.cpp:395
         int n = 0, len = chain_len(cs);
+        #pragma unroll 1
         for (int d = 0; d < len; ++d) {
             int o = st[slot_of(cs, d)];
             if (o == BOUND || o == MISBOUND) n++;
@@ -1495,6 +1572,7 @@ struct Rep {
     __device__ __noinline__ void find_bound_domains(int cs) {   // src/movetypes.cpp:258
         m.n_bd = 0;
         int len = chain_len(cs);
+        #pragma unroll 1
         for (int d = 0; d < len; ++d) {
             int i = slot_of(cs, d);
             int b = bnd[i];
@@ -1509,6 +1587,7 @@ struct Rep {
 
     __device__ __noinline__ void unassign_domains(int cs) {   // src/met_movetypes.cpp:77
         int len = chain_len(cs);
+        #pragma unroll 1
         for (int d = 0; d < len; ++d) {
             int i = slot_of(cs, d);
             m.mod[m.n_mod] = i;
@@ -1523,7 +1602,7 @@ struct Rep {
     // RegrowthMCMovetype::set_growth_point (src/movetypes.cpp:322)
     __device__ __noinline__ double set_growth_point(int gnew, int gold) {
         double de = set_domain_config(gnew, pos(gold), ore[gold] ^ 1);
-        if (h->violated) rejected = true;
+        if (hdr.violated) rejected = true;
         else m.asg[m.n_asg++] = gnew;
         return de;
     }
@@ -1531,13 +1610,14 @@ struct Rep {
     // MetMCMovetype::grow_chain (src/met_movetypes.cpp:50) over the domains
     // d0, d0+dir, ... of chain slot cs (count of them, including d0).
     __device__ __noinline__ void met_grow_chain(int cs, int d0, int dir, int count) {
+        #pragma unroll 1
         for (int n = 1; n < count; ++n) {
             int i = slot_of(cs, d0 + dir * n);
             int prev = slot_of(cs, d0 + dir * (n - 1));
             V3 p = add(pos(prev), unit(rng.uniform_int(0, 5)));
             int o = rng.uniform_int(0, 5);
             delta_e += set_domain_config(i, p, o);
-            if (h->violated) {
+            if (hdr.violated) {
                 rejected = true;
                 break;
             }
@@ -1583,18 +1663,19 @@ struct Rep {
     __device__ __noinline__ bool insert_staple() {
         int S = sys->n_types - 1;
         int type = rng.uniform_int(1, S);
-        if (h->num_staples == sys->max_total_staples) return false;
+        if (hdr.num_staples == sys->max_total_staples) return false;
         if (type_count[type] == sys->max_type_staples) return false;
         int cs = add_chain(type);
         if (cs < 0) return false;
         if (mean_field) delta_e += log6;
-        delta_e += tab->init_e;
+        delta_e += t_init_e;
         m.added_cs = cs;
         int len = chain_len(cs);
         int gi = rng.uniform_int(0, len - 1);
         int gnew = slot_of(cs, gi);
         int gold = select_random_domain();
         int guard = 0;
+        #pragma unroll 1
         while (scs[gold] == cs) {
             gold = select_random_domain();
             if (++guard > LDO_GROWTHPOINT_CAP) {
@@ -1606,14 +1687,15 @@ struct Rep {
         if (rejected || bad()) return false;
         grow_staple(gi, cs, false);
         if (rejected || bad()) return false;
+        #pragma unroll 1
         for (int d = 0; d < len; ++d)
             if (st[slot_of(cs, d)] == BOUND) { staple_bound = true; break; }
         int nbd = num_bound_staple_domains(cs);
         add_external_bias_met();
-        double boltz = exp(-delta_e);
+        double boltz = dexp(-delta_e);
         int ni = type_count[type];
         double pratio = (double)len / 6.0 / ni * boltz;
-        pratio *= insertion_sites * ctl->staple_M;
+        pratio *= insertion_sites * c_staple_M;
         pratio /= nbd;
         return exchange_accept_common(type, pratio);
     }
@@ -1629,7 +1711,8 @@ struct Rep {
         }
         int which = rng.uniform_int(0, n - 1);
         int cs = -1;
-        for (int c = 1; c < h->n_chains; ++c) {
+        #pragma unroll 1
+        for (int c = 1; c < hdr.n_chains; ++c) {
             int x = chain_order[c];
             if (chain_type[x] == type) {
                 if (which == 0) { cs = x; break; }
@@ -1642,19 +1725,20 @@ struct Rep {
         }
         if (staple_is_connector(cs)) return false;
         int len = chain_len(cs);
+        #pragma unroll 1
         for (int d = 0; d < len; ++d)
             if (st[slot_of(cs, d)] == BOUND) { staple_bound = true; break; }
         int nbd = num_bound_staple_domains(cs);
         unassign_domains(cs);
         if (mean_field) delta_e -= log6;
-        delta_e -= tab->init_e;
-        h->num_staples--;
+        delta_e -= t_init_e;
+        hdr.num_staples--;
         add_external_bias_met();
-        h->num_staples++;
-        double boltz = exp(-delta_e);
+        hdr.num_staples++;
+        double boltz = dexp(-delta_e);
         int ni = type_count[type];
         double pratio = ni * 6.0 / (double)len * boltz;
-        pratio /= ctl->staple_M * (double)(unsigned long long)(insertion_sites - len);
+        pratio /= c_staple_M * (double)(unsigned long long)(insertion_sites - len);
         pratio *= nbd;
         bool acc = exchange_accept_common(type, pratio);
         if (acc) delete_chain(cs);
@@ -1662,20 +1746,20 @@ struct Rep {
     }
 
     __device__ __noinline__ bool met_exchange() {   // src/met_movetypes.cpp:192
-        insertion_sites = h->num_domains;
+        insertion_sites = hdr.num_domains;
         staple_bound = false;
         if (rng.uniform_real() < 0.5) return insert_staple();
         return delete_staple();
     }
 
     __device__ __noinline__ int pick_staple_chain() {   // uniform_int(1, num_staples) -> get_chains()[i]
-        int ci = rng.uniform_int(1, h->num_staples);
+        int ci = rng.uniform_int(1, hdr.num_staples);
         return chain_order[ci];
     }
 
     // MetStapleRegrowthMCMovetype::internal_attempt_move (src/met_movetypes.cpp:470)
     __device__ __noinline__ bool met_regrowth() {
-        if (h->num_staples == 0) return false;
+        if (hdr.num_staples == 0) return false;
         int cs = pick_staple_chain();
         if (staple_is_connector(cs)) return false;
         find_bound_domains(cs);
@@ -1689,7 +1773,7 @@ struct Rep {
         if (rejected || bad()) return false;
         add_external_bias_met();
         int nbd = num_bound_staple_domains(cs);
-        double boltz = exp(-(delta_e));
+        double boltz = dexp(-(delta_e));
         double pratio = boltz * (double)(unsigned long long)m.n_bd / nbd;
         return test_acceptance(pratio);
     }
@@ -1704,11 +1788,12 @@ struct Rep {
         int nc = 0;
         // Classify the six neighbour sites; unbound ones are probed in
         // parallel, empty ones weigh 6 (no potential is evaluated there:
-        // 6 * exp(-0), src/cb_movetypes.cpp:92-99), occupied ones are skipped.
+        // 6 * dexp(-0), src/cb_movetypes.cpp:92-99), occupied ones are skipped.
         int* kind = cb_kind;
         int* slot_of_v = cb_slot;
         int n_unb = 0;
         volatile ProbeTask* t = task;
+        #pragma unroll 1
         for (int v = 0; v < 6; ++v) {
             V3 p = add(p_prev, unit(v));
             int occ = occupancy(p);
@@ -1730,6 +1815,7 @@ struct Rep {
             }
         }
         if (n_unb > 0) run_probes(dom, n_unb);
+        #pragma unroll 1
         for (int v = 0; v < 6; ++v) {
             if (kind[v] == 0) continue;
             V3 p = add(p_prev, unit(v));
@@ -1750,6 +1836,7 @@ struct Rep {
             }
         }
         double ros = 0;
+        #pragma unroll 1
         for (int n = 0; n < nc; ++n) ros += bf[n];
         if (ros == 0) {
             rejected = true;
@@ -1761,6 +1848,7 @@ struct Rep {
             int o = -1;
             double cum = 0;
             double r = rng.uniform_real();
+            #pragma unroll 1
             for (int n = 0; n < nc; ++n) {
                 cum += bf[n] / ros;
                 if (r < cum) {
@@ -1774,6 +1862,7 @@ struct Rep {
         }
         else {
             int n = 0;
+            #pragma unroll 1
             while (n < m.n_old && m.old_slot[n] != dom) ++n;
             set_checked(dom, m.old_pos[n], m.old_ore[n]);
         }
@@ -1781,6 +1870,7 @@ struct Rep {
     }
 
     __device__ __noinline__ void cb_grow_chain(int cs, int d0, int dir, int count) {   // src/cb_movetypes.cpp:354
+        #pragma unroll 1
         for (int n = 1; n < count; ++n) {
             cb_select_and_set(slot_of(cs, d0 + dir * n), slot_of(cs, d0 + dir * (n - 1)));
             if (rejected || bad()) break;
@@ -1790,22 +1880,23 @@ struct Rep {
     __device__ __noinline__ void cb_set_gp_and_grow(int gnew, int gold, int cs) {   // src/cb_movetypes.cpp:389
         if (regrow_old) {
             int n = 0;
+            #pragma unroll 1
             while (n < m.n_old && m.old_slot[n] != gnew) ++n;
             double de = 0;
             de += set_checked(gnew, pos(gold), m.old_ore[n]);
-            w_bias *= exp(-de);
+            w_bias *= dexp(-de);
             m.asg[m.n_asg++] = gnew;
         }
         else {
             double de = set_growth_point(gnew, gold);
-            w_bias *= exp(-de);
+            w_bias *= dexp(-de);
         }
         if (!rejected && !bad()) grow_staple(sd[gnew], cs, true);
     }
 
     // CBStapleRegrowthMCMovetype::internal_attempt_move (src/cb_movetypes.cpp:292)
     __device__ __noinline__ bool cb_regrowth() {
-        if (h->num_staples == 0) return false;
+        if (hdr.num_staples == 0) return false;
         int cs = pick_staple_chain();
         if (staple_is_connector(cs)) return false;
         find_bound_domains(cs);
@@ -1818,13 +1909,14 @@ struct Rep {
         w_bias /= num_bound_staple_domains(cs);
         update_move_params();
         double tb = calc_move();
-        w_bias *= exp(-tb);
+        w_bias *= dexp(-tb);
         // setup_for_regrow_old (:215)
         regrow_old = true;
         w_new_bias = w_bias;
         new_modifier = modifier;
         w_bias = 1;
         m.n_old = m.n_mod;
+        #pragma unroll 1
         for (int n = 0; n < m.n_mod; ++n) {
             m.old_slot[n] = m.mod[n];
             m.old_pos[n] = m.mod_pos[n];
@@ -1863,7 +1955,7 @@ struct Rep {
             set_domain_orientation(dom, o_new);
             V3 p = pos(dom);
             de += set_domain_config(bd, p, o_new ^ 1);
-            if (!h->violated) acc = test_acceptance(exp(-de));
+            if (!hdr.violated) acc = test_acceptance(dexp(-de));
             if (!acc) {
                 unassign_domain(bd);
                 set_domain_orientation(dom, o_old);
@@ -1882,6 +1974,7 @@ struct Rep {
         double r = rng.uniform_real();
         int nm = sys->n_moves;
         int mv = 0;
+        #pragma unroll 1
         while (mv < nm && !(r < sys->move_cum[mv])) ++mv;
         if (mv == nm) {
             fail(LDO_RS_INVARIANT);

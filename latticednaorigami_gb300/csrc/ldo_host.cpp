@@ -261,42 +261,50 @@ int next_pow2(int x) {
     return p;
 }
 
-LdoLayout make_layout(int dcap, int kmax, int ntypes, int nb, int nop, int nmv) {
+template <class C>
+LdoLayout layout_of(int cls) {
+    using S = LdoState<C>;
     LdoLayout y {};
-    int off = 0;
-    auto take = [&](int bytes, int align) {
-        off = (off + align - 1) / align * align;
-        int o = off;
-        off += bytes;
-        return o;
-    };
-    y.dcap = dcap;
-    y.kmax = kmax;
-    y.hcap = next_pow2(std::max(16, 2 * dcap));
-    y.ntypes = ntypes;
-    y.nb = nb;
-    y.nop = nop;
-    y.nmv = nmv;
-    y.o_hdr = take(sizeof(LdoHdr), 16);
-    y.o_hash = take(8 * y.hcap, 16);
-    y.o_bias = take(8 * std::max(nb, 1), 8);
-    y.o_mstat = take(8 * 2 * std::max(nmv, 1), 8);
-    y.o_chain_c = take(4 * (kmax + 1), 4);
-    y.o_op = take(4 * 2 * std::max(nop, 1), 4);
-    y.o_px = take(2 * dcap, 2);
-    y.o_py = take(2 * dcap, 2);
-    y.o_pz = take(2 * dcap, 2);
-    y.o_bound = take(2 * dcap, 2);
-    y.o_dident = take(2 * dcap, 2);
-    y.o_type_count = take(2 * ntypes, 2);
-    y.o_ore = take(dcap, 1);
-    y.o_state = take(dcap, 1);
-    y.o_slot_cs = take(dcap, 1);
-    y.o_slot_d = take(dcap, 1);
-    y.o_chain_type = take(kmax + 1, 1);
-    y.o_chain_order = take(kmax + 1, 1);
-    y.bytes = (off + 15) / 16 * 16;
+    y.cls = cls;
+    y.bytes = (int)sizeof(S);
+    y.o_hdr = (int)offsetof(S, hdr);
+    y.o_hash = (int)offsetof(S, hash);
+    y.o_bias = (int)offsetof(S, bias);
+    y.o_mstat = (int)offsetof(S, mstat);
+    y.o_chain_c = (int)offsetof(S, chain_c);
+    y.o_op = (int)offsetof(S, op);
+    y.o_px = (int)offsetof(S, px);
+    y.o_py = (int)offsetof(S, py);
+    y.o_pz = (int)offsetof(S, pz);
+    y.o_bound = (int)offsetof(S, bnd);
+    y.o_dident = (int)offsetof(S, did);
+    y.o_type_count = (int)offsetof(S, type_count);
+    y.o_ore = (int)offsetof(S, ore);
+    y.o_state = (int)offsetof(S, st);
+    y.o_slot_cs = (int)offsetof(S, scs);
+    y.o_slot_d = (int)offsetof(S, sd);
+    y.o_chain_type = (int)offsetof(S, chain_type);
+    y.o_chain_order = (int)offsetof(S, chain_order);
+    y.o_clen = (int)offsetof(S, clen);
+    y.dcap = C::DCAP;
+    y.kmax = C::KMAX;
+    y.hcap = C::HCAP;
+    y.ntypes = C::NT;
+    y.nb = C::NB;
+    y.nop = C::NOP;
+    y.nmv = C::NMV;
     return y;
+}
+
+// Smallest capacity class that holds every system of the batch (the occupancy
+// hash gets at least twice as many entries as domain slots).
+LdoLayout make_layout(int dcap, int kmax, int ntypes, int nb, int nop, int nmv) {
+    if (ntypes > LDO_MAX_TYPES || nb > LDO_MAX_BIASES || nop > LDO_MAX_OPS || nmv > LDO_MAX_MOVES)
+        throw LdoError(LDO_EINVAL, "system exceeds the engine's descriptor limits");
+    if (dcap <= LdoCapS::DCAP && kmax <= LdoCapS::KMAX && 2 * dcap <= LdoCapS::HCAP) return layout_of<LdoCapS>(LDO_CLASS_S);
+    if (dcap <= LdoCapM::DCAP && kmax <= LdoCapM::KMAX && 2 * dcap <= LdoCapM::HCAP) return layout_of<LdoCapM>(LDO_CLASS_M);
+    if (dcap <= LdoCapL::DCAP && kmax <= LdoCapL::KMAX && 2 * dcap <= LdoCapL::HCAP) return layout_of<LdoCapL>(LDO_CLASS_L);
+    throw LdoError(LDO_ECAPACITY, "system needs more domain or staple slots than the largest capacity class");
 }
 
 } // namespace
@@ -459,6 +467,7 @@ struct ldo_engine {
             auto* chain_c = reinterpret_cast<int32_t*>(b + lay.o_chain_c);
             unsigned char* chain_type = b + lay.o_chain_type;
             unsigned char* chain_order = b + lay.o_chain_order;
+            unsigned char* clen = b + lay.o_clen;
             auto* type_count = reinterpret_cast<int16_t*>(b + lay.o_type_count);
             for (int s = 0; s < lay.dcap; ++s) {
                 bnd[s] = -1;
@@ -490,6 +499,7 @@ struct ldo_engine {
                 if ((int)ch.positions.size() != len) throw LdoError(LDO_EINVAL, "chain length does not match identity");
                 chain_c[cs] = ch.index;
                 chain_type[cs] = (unsigned char)type;
+                clen[cs] = (unsigned char)len;
                 chain_order[c] = (unsigned char)cs;
                 type_count[type]++;
                 maxc = std::max(maxc, ch.index);
@@ -550,8 +560,9 @@ struct ldo_engine {
         CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         CU(cudaEventCreate(&ev0));
         CU(cudaEventCreate(&ev1));
-        // Warps per block: as many replicas as fit 48 KB, at most 4.
-        wpb = std::max(1, std::min(4, (int)(48 * 1024 / lay.bytes)));
+        // Four replicas (warps) per block; the kernel's launch bounds allow
+        // seven such blocks per SM.
+        wpb = 4;
         for (auto& hs : systems) h_sys.push_back(hs.desc);
         d_sys.alloc(h_sys.size());
         CU(cudaMemcpy(d_sys.p, h_sys.data(), h_sys.size() * sizeof(LdoSys), cudaMemcpyHostToDevice));

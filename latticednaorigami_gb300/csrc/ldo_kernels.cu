@@ -24,35 +24,17 @@ __device__ __forceinline__ void warp_copy16(void* dst, const void* src, int byte
     for (int k = lane; k < n; k += 32) d[k] = s[k];
 }
 
-__device__ void bind_rep(ldo::Rep& r, const LdoLaunch& L, unsigned char* base, int rep) {
-    const LdoLayout& y = L.lay;
+template <class C>
+__device__ void bind_rep(ldo::Rep<C>& r, const LdoLaunch& L, int rep) {
     r.ctl = L.ctl + rep;
     r.sys = L.sys + r.ctl->sys;
     r.bank = L.bank;
     r.grid = L.grid;
-    r.h = reinterpret_cast<LdoHdr*>(base + y.o_hdr);
-    r.tab = L.tabs + r.ctl->tab;
-    r.px = reinterpret_cast<int16_t*>(base + y.o_px);
-    r.py = reinterpret_cast<int16_t*>(base + y.o_py);
-    r.pz = reinterpret_cast<int16_t*>(base + y.o_pz);
-    r.bnd = reinterpret_cast<int16_t*>(base + y.o_bound);
-    r.did = reinterpret_cast<int16_t*>(base + y.o_dident);
-    r.ore = base + y.o_ore;
-    r.st = base + y.o_state;
-    r.scs = base + y.o_slot_cs;
-    r.sd = base + y.o_slot_d;
-    r.chain_c = reinterpret_cast<int32_t*>(base + y.o_chain_c);
-    r.chain_type = base + y.o_chain_type;
-    r.chain_order = base + y.o_chain_order;
-    r.type_count = reinterpret_cast<int16_t*>(base + y.o_type_count);
-    r.hash = reinterpret_cast<unsigned long long*>(base + y.o_hash);
-    r.bias = reinterpret_cast<double*>(base + y.o_bias);
-    r.op = reinterpret_cast<int32_t*>(base + y.o_op);
-    r.mstat = reinterpret_cast<long long*>(base + y.o_mstat);
-    r.hmask = y.hcap - 1;
-    int lg = 0;
-    while ((1 << lg) < y.hcap) ++lg;
-    r.hshift = 64 - lg;
+    r.bind_tables(L.tabs + r.ctl->tab);
+    r.imax = r.sys->imax;
+    r.dim = r.sys->dim;
+    r.c_staple_M = r.ctl->staple_M;
+    r.c_bias_mult = r.ctl->bias_mult;
     r.ns = r.sys->ns;
     r.lmax = r.sys->lmax;
     r.nmv = r.sys->n_moves;
@@ -61,28 +43,37 @@ __device__ void bind_rep(ldo::Rep& r, const LdoLaunch& L, unsigned char* base, i
     r.mean_field = r.sys->mean_field;
     r.log6 = log(6.0);
     r.log3 = log(3.0);
-    r.rng.init(r.ctl->seed, r.ctl->rep, 0u, r.h->draws);
+    r.rng.init(r.ctl->seed, r.ctl->rep, 0u, r.hdr.draws);
+    for (int q = 0; q < 6; ++q) {
+        r.fbs[q].ov_d = -1;
+        r.fbs[q].ov_p = -1;
+    }
 }
 
 __host__ __device__ constexpr int task_bytes() { return (int)((sizeof(ldo::ProbeTask) + 15) / 16 * 16); }
-__host__ __device__ constexpr int rep_bytes() { return (int)((sizeof(ldo::Rep) + 15) / 16 * 16); }
+template <class C>
+__host__ __device__ constexpr int rep_bytes() { return (int)((sizeof(ldo::Rep<C>) + 15) / 16 * 16); }
+template <class C>
+__host__ __device__ constexpr int warp_bytes() { return rep_bytes<C>() + task_bytes(); }
 
-// Shared memory per warp: replica state | probe task | Rep (the working object).
+// Shared memory per warp: Rep (replica state followed by the working fields)
+// then the probe task.
+template <class C>
 __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
     extern __shared__ __align__(16) unsigned char smem[];
     int warp = threadIdx.x >> 5;
     int lane = threadIdx.x & 31;
     int rep = blockIdx.x * L.warps_per_block + warp;
     if (rep >= L.n_rep) return;
-    unsigned char* base = smem + (size_t)warp * (L.lay.bytes + task_bytes() + rep_bytes());
-    ldo::ProbeTask* task = reinterpret_cast<ldo::ProbeTask*>(base + L.lay.bytes);
-    ldo::Rep* R = reinterpret_cast<ldo::Rep*>(base + L.lay.bytes + task_bytes());
-    unsigned char* gbase = L.arena + (size_t)rep * L.lay.bytes;
-    warp_copy16(base, gbase, L.lay.bytes, lane);
+    unsigned char* base = smem + (size_t)warp * warp_bytes<C>();
+    ldo::Rep<C>* R = reinterpret_cast<ldo::Rep<C>*>(base);
+    ldo::ProbeTask* task = reinterpret_cast<ldo::ProbeTask*>(base + rep_bytes<C>());
+    unsigned char* gbase = L.arena + (size_t)rep * sizeof(LdoState<C>);
+    warp_copy16(base, gbase, (int)sizeof(LdoState<C>), lane);
     __syncwarp();
     if (lane == 0) {
         task->cmd = 0;
-        bind_rep(*R, L, base, rep);
+        bind_rep<C>(*R, L, rep);
         R->task = task;
     }
     __syncwarp();
@@ -91,27 +82,27 @@ __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
         R->probe_helper_loop();
     }
     else if (lane == 0) {
-        LdoHdr* h = R->h;
-        if (h->status == 0) {
+        LdoHdr& h = R->hdr;
+        if (h.status == 0) {
             if (L.mode == LDO_MODE_INIT) {
                 R->set_all_current();
                 R->init_biases();
-                h->tab = R->ctl->tab;
+                h.tab = R->ctl->tab;
             }
             else if (L.mode == LDO_MODE_RECOMPUTE) {
                 R->recompute_energy();
-                h->tab = R->ctl->tab;
+                h.tab = R->ctl->tab;
             }
             else if (L.mode == LDO_MODE_OBSERVE) {
                 // Reading observables changes nothing: the energy and the
                 // dependent quantities use the tables the energy was last
                 // computed with, even if the controls have moved since.
-                R->tab = L.tabs + h->tab;
+                R->bind_tables(L.tabs + h.tab);
             }
             else {
-                if (L.force_recompute || h->tab != R->ctl->tab) {
+                if (L.force_recompute || h.tab != R->ctl->tab) {
                     R->recompute_energy();
-                    h->tab = R->ctl->tab;
+                    h.tab = R->ctl->tab;
                 }
                 double* tr = (rep < L.n_trace) ? L.trace + (size_t)rep * L.trace_max * 8 : nullptr;
                 long long unit = L.sweep_units ? (long long)R->ns : 1ll;
@@ -119,38 +110,38 @@ __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
                 long long sint = (long long)L.sample_interval * unit;
                 for (long long k = 0; k < nsteps; ++k) {
                     if (R->bad()) break;
-                    long long s = h->steps_done + 1;
+                    long long s = h.steps_done + 1;
                     R->step(s);
-                    h->steps_done = s;
+                    h.steps_done = s;
                     if (tr && k < L.trace_max) {
                         double* t = tr + 8 * k;
                         t[0] = (double)s;
-                        t[1] = h->energy;
-                        t[2] = h->num_staples;
-                        t[3] = h->num_fully;
-                        t[4] = h->num_bound;
-                        t[5] = h->num_stacked;
-                        t[6] = h->move_bias * R->ctl->bias_mult;
+                        t[1] = h.energy;
+                        t[2] = h.num_staples;
+                        t[3] = h.num_fully;
+                        t[4] = h.num_bound;
+                        t[5] = h.num_stacked;
+                        t[6] = h.move_bias * R->c_bias_mult;
                         t[7] = (double)R->rng.draws;
                     }
                     if (sint > 0 && s % sint == 0) {
-                        int c = h->sample_count;
+                        int c = h.sample_count;
                         if (c < L.sample_cap) {
                             int16_t* o = L.samples + ((size_t)rep * L.sample_cap + c) * 2;
-                            o[0] = (int16_t)h->num_fully;
-                            o[1] = (int16_t)h->num_staples;
+                            o[0] = (int16_t)h.num_fully;
+                            o[1] = (int16_t)h.num_staples;
                         }
-                        h->sample_count = c + 1;
+                        h.sample_count = c + 1;
                     }
                 }
             }
             if (L.want_dep && !R->bad()) R->dependent_quantities();
-            h->draws = R->rng.draws;
+            h.draws = R->rng.draws;
         }
         R->post_exit();
     }
     __syncwarp();
-    warp_copy16(gbase, base, L.lay.bytes, lane);
+    warp_copy16(gbase, base, (int)sizeof(LdoState<C>), lane);
 }
 
 __global__ void ldo_status_kernel(const unsigned char* arena, int bytes, int o_hdr, int n_rep, int* out) {
@@ -228,14 +219,31 @@ cudaError_t ldo_launch_pt_swap(const LdoPT& P, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
-cudaError_t ldo_launch_mc(const LdoLaunch& L, cudaStream_t stream) {
+template <class C>
+static cudaError_t launch_mc_class(const LdoLaunch& L, cudaStream_t stream) {
     int wpb = L.warps_per_block;
-    size_t smem = (size_t)wpb * (L.lay.bytes + task_bytes() + rep_bytes());
-    cudaError_t err = cudaFuncSetAttribute(ldo_mc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    size_t smem = (size_t)wpb * warp_bytes<C>();
+    cudaError_t err = cudaFuncSetAttribute(ldo_mc_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
     int blocks = (L.n_rep + wpb - 1) / wpb;
-    ldo_mc_kernel<<<blocks, wpb * 32, smem, stream>>>(L);
+    ldo_mc_kernel<C><<<blocks, wpb * 32, smem, stream>>>(L);
     return cudaGetLastError();
+}
+
+cudaError_t ldo_launch_mc(const LdoLaunch& L, cudaStream_t stream) {
+    switch (L.lay.cls) {
+    case LDO_CLASS_S: return launch_mc_class<LdoCapS>(L, stream);
+    case LDO_CLASS_M: return launch_mc_class<LdoCapM>(L, stream);
+    default: return launch_mc_class<LdoCapL>(L, stream);
+    }
+}
+
+int ldo_warp_smem_bytes(int cls) {
+    switch (cls) {
+    case LDO_CLASS_S: return warp_bytes<LdoCapS>();
+    case LDO_CLASS_M: return warp_bytes<LdoCapM>();
+    default: return warp_bytes<LdoCapL>();
+    }
 }
 
 cudaError_t ldo_launch_status(const unsigned char* arena, int bytes, int o_hdr, int n_rep, int* d_out,

@@ -29,6 +29,8 @@ struct LdoLaunch {
 };
 
 cudaError_t ldo_launch_mc(const LdoLaunch& L, cudaStream_t stream);
+// Shared memory one replica's warp needs in capacity class cls.
+int ldo_warp_smem_bytes(int cls);
 cudaError_t ldo_launch_status(const unsigned char* arena, int bytes, int o_hdr, int n_rep, int* d_out,
                               cudaStream_t stream);
 

@@ -125,11 +125,47 @@ struct LdoLayout {
     int o_px, o_py, o_pz, o_bound, o_dident;   // int16[dcap]
     int o_ore, o_state, o_slot_cs, o_slot_d;   // uint8[dcap]
     int o_chain_c;                             // int32[kmax+1]
-    int o_chain_type, o_chain_order;           // uint8[kmax+1]
+    int o_chain_type, o_chain_order, o_clen;   // uint8[kmax+1]
     int o_type_count;                          // int16[ntypes]
     int o_hash;                                // uint64[hcap]
     int o_bias;                                // double[nb]
     int o_op;                                  // int32[2*nop]: value, defined
     int o_mstat;                               // int64[2*nmv]
     int dcap, kmax, hcap, ntypes, nb, nop, nmv;
+    int cls;                                   // LDO_CLASS_*
+};
+
+// Capacity classes.  The replica state is a struct whose array sizes are
+// compile-time constants, so that every field is one load at a constant
+// offset (the kernel is instruction-fetch bound; address arithmetic through
+// runtime offsets and pointers tripled its code size).
+template <int DCAP_, int KMAX_, int HCAP_>
+struct LdoCap {
+    static constexpr int DCAP = DCAP_;    // domain slots
+    static constexpr int KMAX = KMAX_;    // staple chain slots
+    static constexpr int HCAP = HCAP_;    // occupancy hash entries (power of two)
+    static constexpr int NT = LDO_MAX_TYPES;
+    static constexpr int NB = LDO_MAX_BIASES;
+    static constexpr int NOP = LDO_MAX_OPS;
+    static constexpr int NMV = LDO_MAX_MOVES;
+};
+using LdoCapS = LdoCap<80, 32, 256>;
+using LdoCapM = LdoCap<160, 56, 512>;
+using LdoCapL = LdoCap<320, 63, 1024>;
+enum { LDO_CLASS_S = 0, LDO_CLASS_M = 1, LDO_CLASS_L = 2 };
+
+// Persistent state of one replica: the same bytes in the global arena between
+// launches and in shared memory during a launch.
+template <class C>
+struct __attribute__((aligned(16))) LdoState {
+    LdoHdr hdr;
+    unsigned long long hash[C::HCAP];
+    double bias[C::NB];
+    long long mstat[2 * C::NMV];
+    int32_t chain_c[C::KMAX + 1];
+    int32_t op[2 * C::NOP];
+    int16_t px[C::DCAP], py[C::DCAP], pz[C::DCAP], bnd[C::DCAP], did[C::DCAP];
+    int16_t type_count[C::NT];
+    uint8_t ore[C::DCAP], st[C::DCAP], scs[C::DCAP], sd[C::DCAP];
+    uint8_t chain_type[C::KMAX + 1], chain_order[C::KMAX + 1], clen[C::KMAX + 1];
 };
