@@ -30,49 +30,65 @@ namespace ldo {
 
 enum { UNASSIGNED = 0, UNBOUND = 1, BOUND = 2, MISBOUND = 3 };
 
-struct V3 {
-    int x, y, z;
-};
-LDO_DEV V3 mk(int x, int y, int z) { V3 r; r.x = x; r.y = y; r.z = z; return r; }
-LDO_DEV V3 add(V3 a, V3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
-LDO_DEV V3 sub(V3 a, V3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
-LDO_DEV V3 neg(V3 a) { return mk(-a.x, -a.y, -a.z); }
-LDO_DEV bool eq(V3 a, V3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
-LDO_DEV V3 absv(V3 a) { return mk(a.x < 0 ? -a.x : a.x, a.y < 0 ? -a.y : a.y, a.z < 0 ? -a.z : a.z); }
+// A lattice vector packed into one 64-bit integer: x + y*2^16 + z*2^32 with
+// |x|, |y|, |z| < 2^15.  Sums, differences, negation and equality of packed
+// values are those of the vectors, so every vector test of the reference is
+// one integer operation here; the occupancy hash key is the packed value too.
+typedef long long V3;
+#define LDO_HD __host__ __device__ __forceinline__
+LDO_HD constexpr V3 mk(int x, int y, int z) { return (long long)x + (long long)y * 65536ll + (long long)z * 4294967296ll; }
+LDO_HD constexpr V3 add(V3 a, V3 b) { return a + b; }
+LDO_HD constexpr V3 sub(V3 a, V3 b) { return a - b; }
+LDO_HD constexpr V3 neg(V3 a) { return -a; }
+LDO_HD constexpr bool eq(V3 a, V3 b) { return a == b; }
+LDO_HD constexpr int vx(V3 p) { return (int)(short)(unsigned short)(p & 0xffff); }
+LDO_HD constexpr int vy(V3 p) { return (int)(short)(unsigned short)(((p - vx(p)) >> 16) & 0xffff); }
+LDO_HD constexpr int vz(V3 p) { return (int)((((p - vx(p)) >> 16) - vy(p)) >> 16); }
 
 // Unit vector k in the order of include/.../utility.hpp:156-162.
-LDO_DEV V3 unit(int k) {
-    int s = (k & 1) ? -1 : 1;
-    int a = k >> 1;
-    return mk(a == 0 ? s : 0, a == 1 ? s : 0, a == 2 ? s : 0);
+LDO_HD constexpr V3 unit(int k) {
+    return k == 0 ? mk(1, 0, 0) : k == 1 ? mk(-1, 0, 0) : k == 2 ? mk(0, 1, 0) : k == 3 ? mk(0, -1, 0)
+                                                          : k == 4 ? mk(0, 0, 1) : mk(0, 0, -1);
 }
-LDO_DEV int unit_index(V3 v) {
-    if (v.x != 0) return v.x > 0 ? 0 : 1;
-    if (v.y != 0) return v.y > 0 ? 2 : 3;
-    return v.z > 0 ? 4 : 5;
-}
-
-// VectorThree::rotate_half (src/utility.cpp:68)
-LDO_DEV V3 rotate_half(V3 v, V3 axis) {
-    V3 a = absv(axis);
-    if (a.x == 1 && a.y == 0 && a.z == 0) { v.y = -v.y; v.z = -v.z; }
-    else if (a.x == 0 && a.y == 1 && a.z == 0) { v.x = -v.x; v.z = -v.z; }
-    else if (a.x == 0 && a.y == 0 && a.z == 1) { v.x = -v.x; v.y = -v.y; }
-    return v;
+// Index of a unit vector, -1 for any other vector.
+LDO_HD constexpr int unit_index(V3 v) {
+    return v == mk(1, 0, 0) ? 0 : v == mk(-1, 0, 0) ? 1 : v == mk(0, 1, 0) ? 2 : v == mk(0, -1, 0) ? 3
+         : v == mk(0, 0, 1) ? 4 : v == mk(0, 0, -1) ? 5 : -1;
 }
 
-// VectorThree::rotate(axis, -1) (src/utility.cpp:102), the quarter turn used
-// by ThreeQuarterTurnDomain::check_twist_constraint.
-LDO_DEV V3 rotate_quarter_neg(V3 v, V3 axis) {
-    int dir = -1;
-    V3 a = absv(axis);
-    if (!eq(axis, a)) dir = 1;
-    int t;
-    if (a.x == 1 && a.y == 0 && a.z == 0) { t = v.y; v.y = v.z; v.z = t; v.y *= -dir; v.z *= dir; }
-    else if (a.x == 0 && a.y == 1 && a.z == 0) { t = v.x; v.x = v.z; v.z = t; v.x *= -dir; v.z *= dir; }
-    else if (a.x == 0 && a.y == 0 && a.z == 1) { t = v.x; v.x = v.y; v.y = t; v.x *= -dir; v.y *= dir; }
-    return v;
+// Rotations used by the twist constraints, tabulated over unit vectors:
+//   half[o][axis]      VectorThree::rotate_half(axis)   (src/utility.cpp:68)
+//   quarter[o][k]      VectorThree::rotate(unit k, -1)  (src/utility.cpp:102)
+// For any vector that is not a unit vector both rotations leave the
+// orientation unchanged (none of the reference's axis tests matches).
+struct RotTab {
+    unsigned char half[6][3];
+    unsigned char quarter[6][6];
+};
+constexpr int rot_comp(int o, int c) { return c == 0 ? vx(unit(o)) : c == 1 ? vy(unit(o)) : vz(unit(o)); }
+constexpr RotTab make_rot() {
+    RotTab t {};
+    for (int o = 0; o < 6; ++o) {
+        for (int a = 0; a < 3; ++a) {
+            int x = rot_comp(o, 0), y = rot_comp(o, 1), z = rot_comp(o, 2);
+            if (a == 0) { y = -y; z = -z; }
+            else if (a == 1) { x = -x; z = -z; }
+            else { x = -x; y = -y; }
+            t.half[o][a] = (unsigned char)unit_index(mk(x, y, z));
+        }
+        for (int k = 0; k < 6; ++k) {
+            int x = rot_comp(o, 0), y = rot_comp(o, 1), z = rot_comp(o, 2);
+            int dir = (k & 1) ? 1 : -1;   // turns = -1: dir -1, flipped for a negative axis
+            int s = 0;
+            if ((k >> 1) == 0) { s = y; y = z; z = s; y *= -dir; z *= dir; }
+            else if ((k >> 1) == 1) { s = x; x = z; z = s; x *= -dir; z *= dir; }
+            else { s = x; x = y; y = s; x *= -dir; y *= dir; }
+            t.quarter[o][k] = (unsigned char)unit_index(mk(x, y, z));
+        }
+    }
+    return t;
 }
+__constant__ const RotTab kRot = make_rot();
 
 // ------------------------------------------------------------- Philox ---
 // Philox4x32-10 (Salmon et al., SC'11).  Stream contract: key (seed, replica),
@@ -129,10 +145,7 @@ struct Rng {
 #define LDO_KEYMASK ((1ull << 48) - 1ull)
 #define LDO_VALID (1ull << 63)
 
-LDO_DEV unsigned long long pkey(V3 p) {
-    return (unsigned long long)(uint16_t)p.x | ((unsigned long long)(uint16_t)p.y << 16) |
-           ((unsigned long long)(uint16_t)p.z << 32);
-}
+LDO_DEV unsigned long long pkey(V3 p) { return (unsigned long long)(p + mk(32768, 32768, 32768)); }
 LDO_DEV int ent_occ(unsigned long long e) { return (int)((e >> 48) & 3ull); }
 LDO_DEV int ent_slot(unsigned long long e) { return (int)((e >> 50) & 0xfffull); }
 LDO_DEV unsigned long long mkent(unsigned long long key, int occ, int slot) {
@@ -211,9 +224,9 @@ struct Rep : public LdoState<C> {
     using S_::mstat;
     using S_::chain_c;
     using S_::op;
-    using S_::px;
-    using S_::py;
-    using S_::pz;
+    using S_::pp;
+    using S_::nxt;
+    using S_::prv;
     using S_::bnd;
     using S_::did;
     using S_::type_count;
@@ -291,15 +304,14 @@ struct Rep : public LdoState<C> {
     __device__ bool bad() const { return hdr.status != 0; }
 
     // -------------------------------------------------------- accessors ---
-    __device__ V3 pos(int i) const { return mk(px[i], py[i], pz[i]); }
+    __device__ V3 pos(int i) const { return pp[i]; }
     __device__ void set_pos(int i, V3 p) {
-        if (p.x < -32000 || p.x > 32000 || p.y < -32000 || p.y > 32000 || p.z < -32000 || p.z > 32000) {
+        int x = vx(p), y = vy(p), z = vz(p);
+        if (x < -32000 || x > 32000 || y < -32000 || y > 32000 || z < -32000 || z > 32000) {
             fail(LDO_RS_CAPACITY);
             return;
         }
-        px[i] = (int16_t)p.x;
-        py[i] = (int16_t)p.y;
-        pz[i] = (int16_t)p.z;
+        pp[i] = p;
     }
     __device__ V3 orev(int i) const { return unit(ore[i]); }
     __device__ int chain_len(int cs) const { return clen[cs]; }
@@ -428,6 +440,8 @@ struct Rep : public LdoState<C> {
             st[s] = UNASSIGNED;
             bnd[s] = -1;
             did[s] = sys->idents[off + d];
+            nxt[s] = (int16_t)(d + 1 < len ? s + 1 : -1);
+            prv[s] = (int16_t)(d > 0 ? s - 1 : -1);
         }
         hdr.num_domains += len;
         hdr.num_unassigned += len;
@@ -674,7 +688,7 @@ struct Rep : public LdoState<C> {
     __device__ void probe_lane(int k) {
         volatile ProbeTask* t = task;
         if (k >= t->n) return;
-        V3 p = mk(t->p[k].x, t->p[k].y, t->p[k].z);
+        V3 p = t->p[k];
         int v;
         double de = overlay_probe(t->dom, t->ud[k], p, t->o[k], &v);
         if (!v) {
@@ -863,10 +877,11 @@ struct Rep : public LdoState<C> {
     // ================================================ FourBody potential ===
     template <bool OV> __device__ bool exists_bound(int i) const { return i >= 0 && gst<OV>(i) == BOUND; }
 
-    template <bool OV> __device__ __noinline__ bool twist_ok(int i1, V3 ndr, int i2) const {   // src/domain.cpp:33,69
-        V3 o1 = gorev<OV>(i1);
-        V3 r = tqt ? rotate_quarter_neg(o1, ndr) : rotate_half(o1, ndr);
-        return eq(r, gorev<OV>(i2));
+    template <bool OV> __device__ __forceinline__ bool twist_ok(int i1, V3 ndr, int i2) const {   // src/domain.cpp:33,69
+        int a = unit_index(ndr);
+        int o1 = gore<OV>(i1);
+        int r = a < 0 ? o1 : (tqt ? kRot.quarter[o1][a] : kRot.half[o1][a >> 1]);
+        return r == gore<OV>(i2);
     }
     template <bool OV> __device__ __noinline__ bool kink_ok(int i1, V3 ndr, int i2) const {   // src/domain.cpp:42,80
         V3 o1 = gorev<OV>(i1), o2 = gorev<OV>(i2);
@@ -1805,9 +1820,7 @@ struct Rep : public LdoState<C> {
                 int ud = unbound_at(p);
                 t->ud[n_unb] = ud;
                 t->o[n_unb] = ore[ud] ^ 1;
-                t->p[n_unb].x = p.x;
-                t->p[n_unb].y = p.y;
-                t->p[n_unb].z = p.z;
+                t->p[n_unb] = p;
                 slot_of_v[v] = n_unb++;
             }
             else {

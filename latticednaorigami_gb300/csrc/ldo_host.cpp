@@ -273,9 +273,9 @@ LdoLayout layout_of(int cls) {
     y.o_mstat = (int)offsetof(S, mstat);
     y.o_chain_c = (int)offsetof(S, chain_c);
     y.o_op = (int)offsetof(S, op);
-    y.o_px = (int)offsetof(S, px);
-    y.o_py = (int)offsetof(S, py);
-    y.o_pz = (int)offsetof(S, pz);
+    y.o_pp = (int)offsetof(S, pp);
+    y.o_nxt = (int)offsetof(S, nxt);
+    y.o_prv = (int)offsetof(S, prv);
     y.o_bound = (int)offsetof(S, bnd);
     y.o_dident = (int)offsetof(S, did);
     y.o_type_count = (int)offsetof(S, type_count);
@@ -317,6 +317,7 @@ struct ldo_engine {
     uint32_t seed {0};
     LdoLayout lay {};
     int wpb {1};
+    int smem_pad {0};
     cudaStream_t stream {nullptr};
     cudaEvent_t ev0 {nullptr}, ev1 {nullptr};
 
@@ -421,6 +422,7 @@ struct ldo_engine {
         L.lay = lay;
         L.n_rep = n_rep;
         L.warps_per_block = wpb;
+        L.smem_pad = smem_pad;
         L.mode = mode;
         L.want_dep = 0;
         L.n_steps = steps;
@@ -455,9 +457,9 @@ struct ldo_engine {
             const LdoSys& d = hs.desc;
             unsigned char* b = host.data() + (size_t)r * lay.bytes;
             auto* h = reinterpret_cast<LdoHdr*>(b + lay.o_hdr);
-            auto* px = reinterpret_cast<int16_t*>(b + lay.o_px);
-            auto* py = reinterpret_cast<int16_t*>(b + lay.o_py);
-            auto* pz = reinterpret_cast<int16_t*>(b + lay.o_pz);
+            auto* pp = reinterpret_cast<long long*>(b + lay.o_pp);
+            auto* nxt = reinterpret_cast<int16_t*>(b + lay.o_nxt);
+            auto* prv = reinterpret_cast<int16_t*>(b + lay.o_prv);
             auto* bnd = reinterpret_cast<int16_t*>(b + lay.o_bound);
             auto* did = reinterpret_cast<int16_t*>(b + lay.o_dident);
             unsigned char* ore = b + lay.o_ore;
@@ -471,6 +473,8 @@ struct ldo_engine {
             auto* type_count = reinterpret_cast<int16_t*>(b + lay.o_type_count);
             for (int s = 0; s < lay.dcap; ++s) {
                 bnd[s] = -1;
+                nxt[s] = -1;
+                prv[s] = -1;
                 if (s < d.ns) {
                     scs[s] = 0;
                     sd[s] = (unsigned char)s;
@@ -505,9 +509,17 @@ struct ldo_engine {
                 maxc = std::max(maxc, ch.index);
                 for (int dd = 0; dd < len; ++dd) {
                     int s = cs == 0 ? dd : d.ns + (cs - 1) * d.lmax + dd;
-                    px[s] = (int16_t)ch.positions[dd][0];
-                    py[s] = (int16_t)ch.positions[dd][1];
-                    pz[s] = (int16_t)ch.positions[dd][2];
+                    for (int q = 0; q < 3; ++q)
+                        if (ch.positions[dd][q] < -32000 || ch.positions[dd][q] > 32000)
+                            throw LdoError(LDO_ECAPACITY, "position coordinate outside +-32000");
+                    pp[s] = (long long)ch.positions[dd][0] + (long long)ch.positions[dd][1] * 65536ll +
+                            (long long)ch.positions[dd][2] * 4294967296ll;
+                    nxt[s] = (int16_t)(dd + 1 < len ? s + 1 : -1);
+                    prv[s] = (int16_t)(dd > 0 ? s - 1 : -1);
+                    if (cs == 0 && d.cyclic) {
+                        if (dd + 1 == len) nxt[s] = 0;
+                        if (dd == 0) prv[s] = (int16_t)(len - 1);
+                    }
                     const auto& o = ch.orientations[dd];
                     int oi;
                     if (o[0] == 1 && o[1] == 0 && o[2] == 0) oi = 0;
@@ -560,9 +572,19 @@ struct ldo_engine {
         CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         CU(cudaEventCreate(&ev0));
         CU(cudaEventCreate(&ev1));
-        // Four replicas (warps) per block; the kernel's launch bounds allow
-        // seven such blocks per SM.
+        // Four replicas (warps) per block by default; the kernel's launch
+        // bounds allow seven such blocks per SM.  Tuning keys (engine-only,
+        // not reference options): gpu_warps_per_block (1..4) and
+        // gpu_smem_pad_bytes (extra shared memory per block, to lower the
+        // number of resident blocks).
         wpb = 4;
+        smem_pad = 0;
+        for (auto& hs : systems) {
+            auto it = hs.p.extra.find("gpu_warps_per_block");
+            if (it != hs.p.extra.end()) wpb = std::max(1, std::min(4, std::atoi(it->second.c_str())));
+            it = hs.p.extra.find("gpu_smem_pad_bytes");
+            if (it != hs.p.extra.end()) smem_pad = std::max(0, std::atoi(it->second.c_str()));
+        }
         for (auto& hs : systems) h_sys.push_back(hs.desc);
         d_sys.alloc(h_sys.size());
         CU(cudaMemcpy(d_sys.p, h_sys.data(), h_sys.size() * sizeof(LdoSys), cudaMemcpyHostToDevice));
@@ -929,9 +951,7 @@ ldo_status ldo_get_config(ldo_engine* e, int replica, int32_t* buf, int cap, int
         const LdoLayout& y = e->lay;
         const LdoSys& d = e->systems[e->sys_of[replica]].desc;
         const auto* h = reinterpret_cast<const LdoHdr*>(b.data() + y.o_hdr);
-        const auto* px = reinterpret_cast<const int16_t*>(b.data() + y.o_px);
-        const auto* py = reinterpret_cast<const int16_t*>(b.data() + y.o_py);
-        const auto* pz = reinterpret_cast<const int16_t*>(b.data() + y.o_pz);
+        const auto* pp = reinterpret_cast<const long long*>(b.data() + y.o_pp);
         const unsigned char* ore = b.data() + y.o_ore;
         const unsigned char* st = b.data() + y.o_state;
         const auto* chain_c = reinterpret_cast<const int32_t*>(b.data() + y.o_chain_c);
@@ -949,9 +969,14 @@ ldo_status ldo_get_config(ldo_engine* e, int replica, int32_t* buf, int cap, int
             out.push_back(len);
             for (int dd = 0; dd < len; ++dd) {
                 int s = cs == 0 ? dd : d.ns + (cs - 1) * d.lmax + dd;
-                out.push_back(px[s]);
-                out.push_back(py[s]);
-                out.push_back(pz[s]);
+                long long p = pp[s];
+                int x = (int)(short)(unsigned short)(p & 0xffff);
+                long long r1 = (p - x) >> 16;
+                int yy = (int)(short)(unsigned short)(r1 & 0xffff);
+                int z = (int)((r1 - yy) >> 16);
+                out.push_back(x);
+                out.push_back(yy);
+                out.push_back(z);
                 out.push_back(U[ore[s]][0]);
                 out.push_back(U[ore[s]][1]);
                 out.push_back(U[ore[s]][2]);

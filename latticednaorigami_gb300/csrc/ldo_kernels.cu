@@ -222,7 +222,7 @@ cudaError_t ldo_launch_pt_swap(const LdoPT& P, cudaStream_t stream) {
 template <class C>
 static cudaError_t launch_mc_class(const LdoLaunch& L, cudaStream_t stream) {
     int wpb = L.warps_per_block;
-    size_t smem = (size_t)wpb * warp_bytes<C>();
+    size_t smem = (size_t)wpb * warp_bytes<C>() + (size_t)L.smem_pad;
     cudaError_t err = cudaFuncSetAttribute(ldo_mc_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
     int blocks = (L.n_rep + wpb - 1) / wpb;

@@ -17,6 +17,7 @@ struct LdoLaunch {
     LdoLayout lay;
     int n_rep;
     int warps_per_block;
+    int smem_pad;                // extra dynamic shared memory per block (occupancy tuning)
     int mode;
     int want_dep;
     int force_recompute;

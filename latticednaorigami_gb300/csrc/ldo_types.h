@@ -122,7 +122,8 @@ struct LdoHdr {
 struct LdoLayout {
     int bytes;
     int o_hdr;
-    int o_px, o_py, o_pz, o_bound, o_dident;   // int16[dcap]
+    int o_pp;                                  // int64[dcap] packed positions
+    int o_bound, o_dident, o_nxt, o_prv;       // int16[dcap]
     int o_ore, o_state, o_slot_cs, o_slot_d;   // uint8[dcap]
     int o_chain_c;                             // int32[kmax+1]
     int o_chain_type, o_chain_order, o_clen;   // uint8[kmax+1]
@@ -164,7 +165,8 @@ struct __attribute__((aligned(16))) LdoState {
     long long mstat[2 * C::NMV];
     int32_t chain_c[C::KMAX + 1];
     int32_t op[2 * C::NOP];
-    int16_t px[C::DCAP], py[C::DCAP], pz[C::DCAP], bnd[C::DCAP], did[C::DCAP];
+    long long pp[C::DCAP];    // packed position x + y*2^16 + z*2^32
+    int16_t bnd[C::DCAP], did[C::DCAP], nxt[C::DCAP], prv[C::DCAP];
     int16_t type_count[C::NT];
     uint8_t ore[C::DCAP], st[C::DCAP], scs[C::DCAP], sd[C::DCAP];
     uint8_t chain_type[C::KMAX + 1], chain_order[C::KMAX + 1], clen[C::KMAX + 1];
