@@ -46,14 +46,14 @@ LDO_HD constexpr int vy(V3 p) { return (int)(short)(unsigned short)(((p - vx(p))
 LDO_HD constexpr int vz(V3 p) { return (int)((((p - vx(p)) >> 16) - vy(p)) >> 16); }
 
 // Unit vector k in the order of include/.../utility.hpp:156-162.
-LDO_HD constexpr V3 unit(int k) {
+LDO_HD constexpr V3 unit_c(int k) {
     return k == 0 ? mk(1, 0, 0) : k == 1 ? mk(-1, 0, 0) : k == 2 ? mk(0, 1, 0) : k == 3 ? mk(0, -1, 0)
                                                           : k == 4 ? mk(0, 0, 1) : mk(0, 0, -1);
 }
 // Index of a unit vector, -1 for any other vector.
 LDO_HD constexpr int unit_index(V3 v) {
-    return v == mk(1, 0, 0) ? 0 : v == mk(-1, 0, 0) ? 1 : v == mk(0, 1, 0) ? 2 : v == mk(0, -1, 0) ? 3
-         : v == mk(0, 0, 1) ? 4 : v == mk(0, 0, -1) ? 5 : -1;
+    return v == 1 ? 0 : v == -1 ? 1 : v == 65536ll ? 2 : v == -65536ll ? 3 : v == 4294967296ll ? 4
+         : v == -4294967296ll ? 5 : -1;
 }
 
 // Rotations used by the twist constraints, tabulated over unit vectors:
@@ -65,7 +65,7 @@ struct RotTab {
     unsigned char half[6][3];
     unsigned char quarter[6][6];
 };
-constexpr int rot_comp(int o, int c) { return c == 0 ? vx(unit(o)) : c == 1 ? vy(unit(o)) : vz(unit(o)); }
+constexpr int rot_comp(int o, int c) { return c == 0 ? vx(unit_c(o)) : c == 1 ? vy(unit_c(o)) : vz(unit_c(o)); }
 constexpr RotTab make_rot() {
     RotTab t {};
     for (int o = 0; o < 6; ++o) {
@@ -89,6 +89,8 @@ constexpr RotTab make_rot() {
     return t;
 }
 __constant__ const RotTab kRot = make_rot();
+__constant__ const long long kUnitP[6] = {unit_c(0), unit_c(1), unit_c(2), unit_c(3), unit_c(4), unit_c(5)};
+__device__ __forceinline__ V3 unit(int k) { return kUnitP[k]; }
 
 // ------------------------------------------------------------- Philox ---
 // Philox4x32-10 (Salmon et al., SC'11).  Stream contract: key (seed, replica),
@@ -182,35 +184,12 @@ struct Scratch {
     int bd_new[LDO_MAX_LEN], bd_old[LDO_MAX_LEN];
 };
 
-// Work item for the lanes that evaluate CB trial positions in parallel.
-struct ProbeTask {
-    int cmd;   // LDO_TASK_*
-    int dom, n;
-    int ud[6], o[6];
-    V3 p[6];
-    double bf[6];
-    int viol[6];
-};
-#define LDO_TASK_PROBE 1
-#define LDO_TASK_EXIT 2
-#define LDO_PROBE_LANES 0x3fu
-
-// Per-lane scratch of the FourBody evaluation: lane 0 uses slot 0 for the
-// moves it applies, lanes 0..5 use their own slot while probing trial
-// positions in parallel.
+// Scratch of the FourBody evaluation.
 struct FBState {
     Delta pd;               // BindingPotential::m_delta_config
     int viol;               // BindingPotential::m_constraints_violated
-    int ov_d, ov_p, ov_st, ov_ore;
-    V3 ov_pos;
     int fa[3], fb[3], sa[3], sb[3];   // single-junction candidate pairs
 };
-
-__device__ __forceinline__ int lane_id() {
-    int l;
-    asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
-    return l;
-}
 
 // One Rep per warp lives in shared memory next to the replica's state; its
 // member data must never sit in a thread's local memory, where a single
@@ -253,14 +232,13 @@ struct Rep : public LdoState<C> {
     int ns, lmax, nmv;
     int cyclic, tqt, mean_field;
     Rng rng;
-    FBState fbs[6];
-    __device__ __forceinline__ FBState& fbst() { return fbs[lane_id()]; }
-    __device__ __forceinline__ const FBState& fbst() const { return fbs[lane_id()]; }
+    FBState fb_;
+    __device__ __forceinline__ FBState& fbst() { return fb_; }
+    __device__ __forceinline__ const FBState& fbst() const { return fb_; }
     // CB trial-position arrays and the connector search stack (lane 0 only)
     V3 cb_pos[6];
     int cb_ore[6];
     double cb_bf[6];
-    int cb_kind[6], cb_slot[6];
     uint8_t dfs_stack[LDO_MAX_KMAX + 1];
     Scratch m;
     bool rejected;
@@ -270,32 +248,13 @@ struct Rep : public LdoState<C> {
     int insertion_sites;
     bool staple_bound;
     double log6, log3;
-    ProbeTask* task;
 
-    // Overlay for read-only trial probes: domain ov_d placed at ov_pos with
-    // orientation ov_ore and paired with ov_p (state ov_st), as
-    // update_occupancies would leave them, without touching shared memory.
-    template <bool OV> __device__ __forceinline__ int gst(int i) const {
-        if (OV) { const FBState& f = fbst(); if (i == f.ov_d || i == f.ov_p) return f.ov_st; }
-        return st[i];
-    }
-    template <bool OV> __device__ __forceinline__ int gbnd(int i) const {
-        if (OV) {
-            const FBState& f = fbst();
-            if (i == f.ov_d) return f.ov_p;
-            if (i == f.ov_p) return f.ov_d;
-        }
-        return bnd[i];
-    }
-    template <bool OV> __device__ __forceinline__ int gore(int i) const {
-        if (OV) { const FBState& f = fbst(); if (i == f.ov_d) return f.ov_ore; }
-        return ore[i];
-    }
-    template <bool OV> __device__ __forceinline__ V3 gorev(int i) const { return unit(gore<OV>(i)); }
-    template <bool OV> __device__ __forceinline__ V3 gpos(int i) const {
-        if (OV) { const FBState& f = fbst(); if (i == f.ov_d) return f.ov_pos; }
-        return pos(i);
-    }
+    // Accessors used by the FourBody traversal.
+    __device__ __forceinline__ int gst(int i) const { return st[i]; }
+    __device__ __forceinline__ int gbnd(int i) const { return bnd[i]; }
+    __device__ __forceinline__ int gore(int i) const { return ore[i]; }
+    __device__ __forceinline__ V3 gorev(int i) const { return unit(gore(i)); }
+    __device__ __forceinline__ V3 gpos(int i) const { return pos(i); }
 
     // ---------------------------------------------------------- errors ---
     __device__ void fail(int code) {
@@ -540,7 +499,7 @@ struct Rep : public LdoState<C> {
         case BOUND:
             hdr.num_fully -= 1;
             hdr.num_bound -= 1;
-            dc = check_stacking<true>(i, j);
+            dc = check_stacking(i, j);
             dc.e *= -1;
             dc.stacked *= -1;
             dc.e += unassign_bound(i);
@@ -584,7 +543,7 @@ struct Rep : public LdoState<C> {
             ore[i] = (uint8_t)o;
             update_occupancies(i, p);
             if (bad()) return dc;
-            dc = bind_domain<true>(i);
+            dc = bind_domain(i);
             hdr.violated = fbst().viol ? 1 : 0;
             break;
         default:
@@ -630,7 +589,7 @@ struct Rep : public LdoState<C> {
         }
         else if (st[i] == BOUND) {
             de += hyb(i, bnd[i]);
-            Delta dc = check_stacking<true>(i, bnd[i]);
+            Delta dc = check_stacking(i, bnd[i]);
             de += dc.e;
             hdr.num_stacked += dc.stacked;
         }
@@ -659,70 +618,36 @@ struct Rep : public LdoState<C> {
         return dc.e;
     }
 
-    // The reference's check_domain_constraints at an unbound site
-    // (src/origami_system.cpp:343 -> internal_check_domain_constraints :846-851)
-    // evaluated read-only: the trial domain and its partner are seen through the
-    // overlay, so several trial positions can be evaluated at once.  Returns the
-    // energy change and sets *viol as the reference sets m_constraints_violated.
-    __device__ double overlay_probe(int dom, int ud, V3 p, int o, int* viol) {
-        FBState& f = fbst();
-        f.ov_d = dom;
-        f.ov_p = ud;
-        f.ov_pos = p;
-        f.ov_ore = o;
-        f.ov_st = (did[dom] == -did[ud]) ? BOUND : MISBOUND;
-        Delta dc = bind_domain<true>(dom);
-        int v = f.viol ? 1 : 0;
-        if (mean_field && !v && f.ov_st == BOUND) {
-            int nf = hdr.num_fully + 1;
-            if (nf == 1) dc.e += 2 * log6;
-            else if (nf == 2) dc.e += log3;
+    // check_domain_constraints for a CB trial position (src/origami_system.cpp:343):
+    // the same state change and energy; the undo skips the stacking traversal
+    // whose result the reference discards (internal_unassign_domain :704).
+    __device__ __noinline__ double probe_domain(int i, V3 p, int o) {
+        Delta dc = internal_check(i, p, o);
+        int occ = st[i];
+        int j = bnd[i];
+        if (occ == BOUND || occ == MISBOUND) {
+            if (j < 0) {
+                fail(LDO_RS_INVARIANT);
+                return 0;
+            }
+            hdr.num_bound -= 1;
+            if (occ == BOUND) hdr.num_fully -= 1;
+            else if (cidx(j) == cidx(i)) hdr.num_self -= 1;
+            bnd[i] = -1;
+            bnd[j] = -1;
+            st[i] = UNASSIGNED;
+            hset(pos(i), UNBOUND, j);
+            st[j] = UNBOUND;
         }
-        f.ov_d = -1;
-        f.ov_p = -1;
-        *viol = v;
+        else if (occ == UNBOUND) {
+            int k = hfind(pkey(pos(i)), nullptr);
+            if (k >= 0) herase(k);
+            st[i] = UNASSIGNED;
+        }
+        else {
+            hdr.num_unassigned--;
+        }
         return dc.e;
-    }
-    // Lane k evaluates trial k of the current task (CB weight dexp(-dE),
-    // src/cb_movetypes.cpp:80-85).
-    __device__ void probe_lane(int k) {
-        volatile ProbeTask* t = task;
-        if (k >= t->n) return;
-        V3 p = t->p[k];
-        int v;
-        double de = overlay_probe(t->dom, t->ud[k], p, t->o[k], &v);
-        if (!v) {
-            double b = 1;
-            b *= dexp(-de);
-            t->bf[k] = b;
-        }
-        t->viol[k] = v;
-    }
-    // Lane 0: hand n trials to lanes 0..n-1 and wait for their results.
-    __device__ void run_probes(int dom, int n) {
-        volatile ProbeTask* t = task;
-        t->dom = dom;
-        t->n = n;
-        t->cmd = LDO_TASK_PROBE;
-        __syncwarp(LDO_PROBE_LANES);
-        probe_lane(0);
-        __syncwarp(LDO_PROBE_LANES);
-    }
-    // Lanes 1..5: serve probe tasks until lane 0 posts LDO_TASK_EXIT.
-    __device__ void probe_helper_loop() {
-        volatile ProbeTask* t = task;
-        #pragma unroll 1
-        for (;;) {
-            __syncwarp(LDO_PROBE_LANES);
-            if (t->cmd == LDO_TASK_EXIT) break;
-            probe_lane(lane_id());
-            __syncwarp(LDO_PROBE_LANES);
-        }
-    }
-    __device__ void post_exit() {
-        volatile ProbeTask* t = task;
-        t->cmd = LDO_TASK_EXIT;
-        __syncwarp(LDO_PROBE_LANES);
     }
 
     // set_domain_orientation (src/origami_system.cpp:543)
@@ -875,16 +800,16 @@ struct Rep : public LdoState<C> {
     }
 
     // ================================================ FourBody potential ===
-    template <bool OV> __device__ bool exists_bound(int i) const { return i >= 0 && gst<OV>(i) == BOUND; }
+    __device__ bool exists_bound(int i) const { return i >= 0 && gst(i) == BOUND; }
 
-    template <bool OV> __device__ __forceinline__ bool twist_ok(int i1, V3 ndr, int i2) const {   // src/domain.cpp:33,69
+    __device__ __forceinline__ bool twist_ok(int i1, V3 ndr, int i2) const {   // src/domain.cpp:33,69
         int a = unit_index(ndr);
-        int o1 = gore<OV>(i1);
+        int o1 = gore(i1);
         int r = a < 0 ? o1 : (tqt ? kRot.quarter[o1][a] : kRot.half[o1][a >> 1]);
-        return r == gore<OV>(i2);
+        return r == gore(i2);
     }
-    template <bool OV> __device__ __noinline__ bool kink_ok(int i1, V3 ndr, int i2) const {   // src/domain.cpp:42,80
-        V3 o1 = gorev<OV>(i1), o2 = gorev<OV>(i2);
+    __device__ __noinline__ bool kink_ok(int i1, V3 ndr, int i2) const {   // src/domain.cpp:42,80
+        V3 o1 = gorev(i1), o2 = gorev(i2);
         if (eq(ndr, neg(o1))) return false;
         if (eq(ndr, o1)) {
             if (tqt) return !(eq(o1, o2) || eq(o1, neg(o2)));
@@ -893,136 +818,136 @@ struct Rep : public LdoState<C> {
         if (eq(ndr, o2) || eq(ndr, neg(o2))) return false;
         return true;
     }
-    template <bool OV> __device__ __noinline__ bool junction_ok(int j1, int j2, int k1, int k2) const {   // src/domain.cpp:59,99
+    __device__ __noinline__ bool junction_ok(int j1, int j2, int k1, int k2) const {   // src/domain.cpp:59,99
         if (!tqt) return true;
-        V3 ndr_k = sub(gpos<OV>(k2), gpos<OV>(k1));
-        if (eq(ndr_k, gorev<OV>(k1))) {
-            V3 ndr1 = sub(gpos<OV>(j2), gpos<OV>(j1));
+        V3 ndr_k = sub(gpos(k2), gpos(k1));
+        if (eq(ndr_k, gorev(k1))) {
+            V3 ndr1 = sub(gpos(j2), gpos(j1));
             if (sd[j1] > sd[j2]) ndr1 = neg(ndr1);
-            if (!twist_ok<OV>(k1, ndr1, k2)) return false;
+            if (!twist_ok(k1, ndr1, k2)) return false;
         }
         return true;
     }
-    template <bool OV> __device__ __noinline__ bool doubly_contig(int a, int b) const {   // src/origami_potential.cpp:51
+    __device__ __noinline__ bool doubly_contig(int a, int b) const {   // src/origami_potential.cpp:51
         if (scs[a] != scs[b] || sd[b] != sd[a] + 1) return false;
-        int ba = gbnd<OV>(a), bb = gbnd<OV>(b);
+        int ba = gbnd(a), bb = gbnd(b);
         if (scs[ba] != scs[bb]) return false;
         int dd = sd[bb] - sd[ba];
         return dd == 1 || dd == -1;
     }
-    template <bool OV> __device__ __noinline__ bool pair_stacked(int a, int b) const {   // :70
+    __device__ __noinline__ bool pair_stacked(int a, int b) const {   // :70
         if (sd[a] > sd[b]) { int t = a; a = b; b = t; }
-        V3 ndr = sub(gpos<OV>(b), gpos<OV>(a));
-        V3 oa = gorev<OV>(a);
-        if (!eq(ndr, oa) && !eq(ndr, neg(oa))) return twist_ok<OV>(a, ndr, b);
+        V3 ndr = sub(gpos(b), gpos(a));
+        V3 oa = gorev(a);
+        if (!eq(ndr, oa) && !eq(ndr, neg(oa))) return twist_ok(a, ndr, b);
         return false;
     }
-    template <bool OV> __device__ __noinline__ int junction_penalty(int j1, int j2, int j3, int j4, int k1, int k2) const {   // :85
-        V3 ndr_k = sub(gpos<OV>(k2), gpos<OV>(k1));
-        if (!eq(ndr_k, gorev<OV>(k1))) return 0;
-        V3 n1 = sub(gpos<OV>(j2), gpos<OV>(j1));
+    __device__ __noinline__ int junction_penalty(int j1, int j2, int j3, int j4, int k1, int k2) const {   // :85
+        V3 ndr_k = sub(gpos(k2), gpos(k1));
+        if (!eq(ndr_k, gorev(k1))) return 0;
+        V3 n1 = sub(gpos(j2), gpos(j1));
         if (sd[j1] > sd[j2]) n1 = neg(n1);
-        V3 n3 = sub(gpos<OV>(j4), gpos<OV>(j3));
+        V3 n3 = sub(gpos(j4), gpos(j3));
         if (sd[j3] > sd[j4]) n3 = neg(n3);
         if (eq(n1, n3)) return 2;
         if (eq(n1, neg(n3))) return 0;
         return 1;
     }
-    template <bool OV> __device__ __noinline__ void triplet_single(int h1, int h2, int h3) {   // :158
-        V3 n1 = sub(gpos<OV>(h2), gpos<OV>(h1));
-        if (eq(n1, gorev<OV>(h1))) return;
-        V3 n2 = sub(gpos<OV>(h3), gpos<OV>(h2));
+    __device__ __noinline__ void triplet_single(int h1, int h2, int h3) {   // :158
+        V3 n1 = sub(gpos(h2), gpos(h1));
+        if (eq(n1, gorev(h1))) return;
+        V3 n2 = sub(gpos(h3), gpos(h2));
         if (!eq(n1, n2)) {
             fbst().pd.e -= stack(h2, h3);
             fbst().pd.stacked -= 1;
         }
     }
-    template <bool OV> __device__ __noinline__ void triplet_double(int h1, int h2, int h3) {   // :181
-        V3 n1 = sub(gpos<OV>(h2), gpos<OV>(h1));
-        V3 n2 = sub(gpos<OV>(h3), gpos<OV>(h2));
+    __device__ __noinline__ void triplet_double(int h1, int h2, int h3) {   // :181
+        V3 n1 = sub(gpos(h2), gpos(h1));
+        V3 n2 = sub(gpos(h3), gpos(h2));
         if (!eq(n1, n2)) {
             fbst().pd.e -= stack(h1, h2) / 2;
             fbst().pd.e -= stack(h2, h3) / 2;
             fbst().pd.stacked -= 1;
         }
     }
-    template <bool OV> __device__ __noinline__ void triply_contig_helix(int h1, int h2, int h3) {   // :200
-        V3 n1 = sub(gpos<OV>(h2), gpos<OV>(h1));
-        V3 n2 = sub(gpos<OV>(h3), gpos<OV>(h2));
+    __device__ __noinline__ void triply_contig_helix(int h1, int h2, int h3) {   // :200
+        V3 n1 = sub(gpos(h2), gpos(h1));
+        V3 n2 = sub(gpos(h3), gpos(h2));
         if (!eq(n1, n2)) fbst().viol = true;
     }
 
-    template <bool OV> __device__ __noinline__ void stacking_and_steric(int i, int j) {   // :212
-        constraints_around<OV>(i, 0);
+    __device__ __noinline__ void stacking_and_steric(int i, int j) {   // :212
+        constraints_around(i, 0);
         if (fbst().viol) return;
-        constraints_around<OV>(j, 1);
+        constraints_around(j, 1);
         if (fbst().viol) return;
-        central_triplets<OV>(i, j);
+        central_triplets(i, j);
     }
 
-    template <bool OV> __device__ __noinline__ void constraints_around(int cd, int jj) {   // :231
+    __device__ __noinline__ void constraints_around(int cd, int jj) {   // :231
         #pragma unroll 1
         for (int k = -1; k <= 0; ++k) {
             int c1 = next(cd, k);
             int c2 = next(cd, k + 1);
-            if (!(exists_bound<OV>(c1) && exists_bound<OV>(c2))) continue;
-            int b1 = gbnd<OV>(c1), b2 = gbnd<OV>(c2);
+            if (!(exists_bound(c1) && exists_bound(c2))) continue;
+            int b1 = gbnd(c1), b2 = gbnd(c2);
             if (scs[b1] == scs[b2]) {
-                if (sd[b1] == sd[b2] - 1) doubly_contig_helix_pair<OV>(c1, c2, k, jj);
-                else if (sd[b1] == sd[b2] + 1) doubly_contig_junction_pair<OV>(c1, c2, jj);
-                else regular_pair<OV>(c1, c2, k);
+                if (sd[b1] == sd[b2] - 1) doubly_contig_helix_pair(c1, c2, k, jj);
+                else if (sd[b1] == sd[b2] + 1) doubly_contig_junction_pair(c1, c2, jj);
+                else regular_pair(c1, c2, k);
             }
             else {
-                regular_pair<OV>(c1, c2, k);
+                regular_pair(c1, c2, k);
             }
             if (fbst().viol) return;
         }
         int prev = next(cd, -1);
         int forw = next(cd, 1);
-        if (exists_bound<OV>(prev) && exists_bound<OV>(forw)) {
-            if (pair_stacked<OV>(cd, forw)) {
-                if (pair_stacked<OV>(prev, cd)) {
-                    if (doubly_contig<OV>(prev, cd) && doubly_contig<OV>(cd, forw)) {
-                        triply_contig_helix<OV>(prev, cd, forw);
+        if (exists_bound(prev) && exists_bound(forw)) {
+            if (pair_stacked(cd, forw)) {
+                if (pair_stacked(prev, cd)) {
+                    if (doubly_contig(prev, cd) && doubly_contig(cd, forw)) {
+                        triply_contig_helix(prev, cd, forw);
                         if (fbst().viol) return;
                     }
-                    triplet_double<OV>(prev, cd, forw);
+                    triplet_double(prev, cd, forw);
                 }
                 else {
-                    triplet_single<OV>(prev, cd, forw);
+                    triplet_single(prev, cd, forw);
                 }
             }
         }
     }
 
-    template <bool OV> __device__ __noinline__ void regular_pair(int c1, int c2, int k) {   // :288
-        V3 ndr = sub(gpos<OV>(c2), gpos<OV>(c1));
-        if (!kink_ok<OV>(c1, ndr, c2)) {
+    __device__ __noinline__ void regular_pair(int c1, int c2, int k) {   // :288
+        V3 ndr = sub(gpos(c2), gpos(c1));
+        if (!kink_ok(c1, ndr, c2)) {
             fbst().viol = true;
             return;
         }
-        if (pair_stacked<OV>(c1, c2)) {
+        if (pair_stacked(c1, c2)) {
             fbst().pd.e += stack(c1, c2);
             fbst().pd.stacked += 1;
-            if (k == -1) backward_single_junction<OV>(c1, c2);
-            else forward_single_junction<OV>(c1, c2);
+            if (k == -1) backward_single_junction(c1, c2);
+            else forward_single_junction(c1, c2);
         }
         else {
-            central_single_junction<OV>(c1, c2);
+            central_single_junction(c1, c2);
         }
-        if (k == -1) backward_triplets<OV>(c1, c2);
-        else forward_triplets<OV>(c1, c2);
+        if (k == -1) backward_triplets(c1, c2);
+        else forward_triplets(c1, c2);
     }
 
-    template <bool OV> __device__ __noinline__ void doubly_contig_helix_pair(int c1, int c2, int k, int jj) {   // :322
+    __device__ __noinline__ void doubly_contig_helix_pair(int c1, int c2, int k, int jj) {   // :322
         if (jj == 1) return;
-        V3 ndr = sub(gpos<OV>(c2), gpos<OV>(c1));
-        V3 o1 = gorev<OV>(c1);
+        V3 ndr = sub(gpos(c2), gpos(c1));
+        V3 o1 = gorev(c1);
         if (eq(ndr, o1) || eq(ndr, neg(o1))) {
             fbst().viol = true;
             return;
         }
-        if (twist_ok<OV>(c1, ndr, c2)) {
+        if (twist_ok(c1, ndr, c2)) {
             fbst().pd.e += stack(c1, c2);
             fbst().pd.stacked += 1;
         }
@@ -1031,47 +956,47 @@ struct Rep : public LdoState<C> {
             return;
         }
         if (k == -1) {
-            backward_triplets<OV>(c1, c2);
-            backward_single_junction<OV>(c1, c2);
+            backward_triplets(c1, c2);
+            backward_single_junction(c1, c2);
         }
         else {
-            forward_triplets<OV>(c1, c2);
-            forward_single_junction<OV>(c1, c2);
+            forward_triplets(c1, c2);
+            forward_single_junction(c1, c2);
         }
     }
 
-    template <bool OV> __device__ __noinline__ void doubly_contig_junction_pair(int c1, int c2, int jj) {   // :359
+    __device__ __noinline__ void doubly_contig_junction_pair(int c1, int c2, int jj) {   // :359
         int k1 = c1, k2 = c2;
-        V3 ndr = sub(gpos<OV>(k2), gpos<OV>(k1));
-        if (!eq(gorev<OV>(k1), ndr)) {
+        V3 ndr = sub(gpos(k2), gpos(k1));
+        if (!eq(gorev(k1), ndr)) {
             fbst().viol = true;
             return;
         }
         if (jj == 1) return;
         #pragma unroll 1
         for (int a = 0; a < 2; ++a) {
-            int j1 = a == 0 ? next(c1, -1) : next(gbnd<OV>(c1), 1);
-            int j2 = a == 0 ? c1 : gbnd<OV>(c1);
+            int j1 = a == 0 ? next(c1, -1) : next(gbnd(c1), 1);
+            int j2 = a == 0 ? c1 : gbnd(c1);
             int j3 = k2, j4 = next(k2, 1);
-            if (exists_bound<OV>(j4) && exists_bound<OV>(j1)) junction<OV>(j1, j2, j3, j4, k1, k2);
-            j3 = gbnd<OV>(k2);
+            if (exists_bound(j4) && exists_bound(j1)) junction(j1, j2, j3, j4, k1, k2);
+            j3 = gbnd(k2);
             j4 = next(j3, -1);
-            if (exists_bound<OV>(j4) && exists_bound<OV>(j1)) junction<OV>(j1, j2, j3, j4, k1, k2);
+            if (exists_bound(j4) && exists_bound(j1)) junction(j1, j2, j3, j4, k1, k2);
         }
     }
 
-    template <bool OV> __device__ __noinline__ void junction(int j1, int j2, int j3, int j4, int k1, int k2) {   // :419
+    __device__ __noinline__ void junction(int j1, int j2, int j3, int j4, int k1, int k2) {   // :419
         if (sd[k1] > sd[k2]) {
             int t = k1; k1 = k2; k2 = t;
             t = j1; j1 = j4; j4 = t;
             t = j2; j2 = j3; j3 = t;
         }
-        if (!(pair_stacked<OV>(j1, j2) && pair_stacked<OV>(j3, j4))) return;
-        if (!junction_ok<OV>(j1, j2, k1, k2)) {
+        if (!(pair_stacked(j1, j2) && pair_stacked(j3, j4))) return;
+        if (!junction_ok(j1, j2, k1, k2)) {
             fbst().viol = true;
             return;
         }
-        int pen = junction_penalty<OV>(j1, j2, j3, j4, k1, k2);
+        int pen = junction_penalty(j1, j2, j3, j4, k1, k2);
         if (pen == 1) {
             fbst().pd.e -= stack(j1, j2) / 2;
             fbst().pd.e -= stack(j3, j4) / 2;
@@ -1084,117 +1009,117 @@ struct Rep : public LdoState<C> {
         }
     }
 
-    template <bool OV> __device__ __noinline__ void backward_triplets(int c1, int c2) {   // :464
+    __device__ __noinline__ void backward_triplets(int c1, int c2) {   // :464
         int h2 = c1, h3 = c2;
-        if (!pair_stacked<OV>(h2, h3)) return;
+        if (!pair_stacked(h2, h3)) return;
         int h1 = next(c1, -1);
-        bool h23_dc = doubly_contig<OV>(h2, h3);
-        if (exists_bound<OV>(h1)) {
-            bool h12_dc = doubly_contig<OV>(h1, h2);
-            if (pair_stacked<OV>(h1, h2)) {
+        bool h23_dc = doubly_contig(h2, h3);
+        if (exists_bound(h1)) {
+            bool h12_dc = doubly_contig(h1, h2);
+            if (pair_stacked(h1, h2)) {
                 if (h12_dc && h23_dc) {
-                    triply_contig_helix<OV>(h1, h2, h3);
+                    triply_contig_helix(h1, h2, h3);
                     if (fbst().viol) return;
                 }
-                triplet_double<OV>(h1, h2, h3);
+                triplet_double(h1, h2, h3);
             }
             else {
-                triplet_single<OV>(h1, h2, h3);
+                triplet_single(h1, h2, h3);
             }
         }
         int h2_prev = h1;
-        int b1 = gbnd<OV>(c1);
+        int b1 = gbnd(c1);
         h1 = next(b1, 1);
-        if (exists_bound<OV>(h1) && gbnd<OV>(h1) != h2_prev && gbnd<OV>(h1) != h3) {
-            if (pair_stacked<OV>(b1, h1)) triplet_double<OV>(h1, h2, h3);
+        if (exists_bound(h1) && gbnd(h1) != h2_prev && gbnd(h1) != h3) {
+            if (pair_stacked(b1, h1)) triplet_double(h1, h2, h3);
         }
         h1 = next(b1, -1);
-        if (exists_bound<OV>(h1) && gbnd<OV>(h1) != h2_prev && gbnd<OV>(h1) != h3) {
-            if (pair_stacked<OV>(h1, b1)) triplet_double<OV>(h1, h2, h3);
-            else triplet_single<OV>(h1, b1, h3);
+        if (exists_bound(h1) && gbnd(h1) != h2_prev && gbnd(h1) != h3) {
+            if (pair_stacked(h1, b1)) triplet_double(h1, h2, h3);
+            else triplet_single(h1, b1, h3);
         }
     }
 
-    template <bool OV> __device__ __noinline__ void forward_triplets(int c1, int c2) {   // :521
+    __device__ __noinline__ void forward_triplets(int c1, int c2) {   // :521
         int h2 = c2, h1 = c1;
-        bool first = pair_stacked<OV>(h1, h2);
+        bool first = pair_stacked(h1, h2);
         int h3 = next(c2, 1);
-        bool h12_dc = doubly_contig<OV>(h1, h2);
-        if (exists_bound<OV>(h3)) {
-            bool second = pair_stacked<OV>(h2, h3);
+        bool h12_dc = doubly_contig(h1, h2);
+        if (exists_bound(h3)) {
+            bool second = pair_stacked(h2, h3);
             if (first && second) {
-                bool h23_dc = doubly_contig<OV>(h2, h3);
+                bool h23_dc = doubly_contig(h2, h3);
                 if (h12_dc && h23_dc) {
-                    triply_contig_helix<OV>(h1, h2, h3);
+                    triply_contig_helix(h1, h2, h3);
                     if (fbst().viol) return;
                 }
-                triplet_double<OV>(h1, h2, h3);
+                triplet_double(h1, h2, h3);
             }
             else if (second) {
-                triplet_single<OV>(h1, h2, h3);
+                triplet_single(h1, h2, h3);
             }
         }
         int h2_next = h3;
-        int b2 = gbnd<OV>(c2);
+        int b2 = gbnd(c2);
         h3 = next(b2, 1);
-        if (exists_bound<OV>(h3) && gbnd<OV>(h3) != h2_next && gbnd<OV>(h3) != h1) {
-            if (pair_stacked<OV>(b2, h3)) {
-                if (first) triplet_double<OV>(h1, h2, h3);
-                else triplet_single<OV>(h1, h2, h3);
+        if (exists_bound(h3) && gbnd(h3) != h2_next && gbnd(h3) != h1) {
+            if (pair_stacked(b2, h3)) {
+                if (first) triplet_double(h1, h2, h3);
+                else triplet_single(h1, h2, h3);
             }
         }
         h3 = next(b2, -1);
-        if (exists_bound<OV>(h3) && gbnd<OV>(h3) != h2_next && gbnd<OV>(h3) != h1) {
-            if (pair_stacked<OV>(h3, b2)) {
-                if (first) triplet_double<OV>(h1, h2, h3);
-                else triplet_single<OV>(h1, h2, h3);
+        if (exists_bound(h3) && gbnd(h3) != h2_next && gbnd(h3) != h1) {
+            if (pair_stacked(h3, b2)) {
+                if (first) triplet_double(h1, h2, h3);
+                else triplet_single(h1, h2, h3);
             }
             else if (first) {
-                triplet_single<OV>(h3, b2, h1);
+                triplet_single(h3, b2, h1);
             }
         }
     }
 
-    template <bool OV> __device__ __noinline__ void central_triplets(int i, int j) {   // :587
+    __device__ __noinline__ void central_triplets(int i, int j) {   // :587
         int h1 = next(i, -1);
         int h2 = i;
         int h3 = next(j, 1);
         int h2_next = next(i, 1);
-        if (exists_bound<OV>(h1) && exists_bound<OV>(h3) && gbnd<OV>(h3) != h2_next && !doubly_contig<OV>(h1, h2)) {
-            if (pair_stacked<OV>(j, h3)) {
-                if (pair_stacked<OV>(h1, h2)) triplet_double<OV>(h1, h2, h3);
-                else triplet_single<OV>(h1, h2, h3);
+        if (exists_bound(h1) && exists_bound(h3) && gbnd(h3) != h2_next && !doubly_contig(h1, h2)) {
+            if (pair_stacked(j, h3)) {
+                if (pair_stacked(h1, h2)) triplet_double(h1, h2, h3);
+                else triplet_single(h1, h2, h3);
             }
         }
         h3 = next(j, -1);
-        if (exists_bound<OV>(h1) && exists_bound<OV>(h3) && gbnd<OV>(h3) != h1 && !doubly_contig<OV>(h1, h2)) {
-            if (pair_stacked<OV>(h1, h2)) {
-                if (pair_stacked<OV>(h3, j)) triplet_double<OV>(h1, h2, h3);
-                else triplet_single<OV>(h3, j, h1);
+        if (exists_bound(h1) && exists_bound(h3) && gbnd(h3) != h1 && !doubly_contig(h1, h2)) {
+            if (pair_stacked(h1, h2)) {
+                if (pair_stacked(h3, j)) triplet_double(h1, h2, h3);
+                else triplet_single(h3, j, h1);
             }
-            else if (pair_stacked<OV>(h3, j)) {
-                triplet_single<OV>(h1, h2, h3);
+            else if (pair_stacked(h3, j)) {
+                triplet_single(h1, h2, h3);
             }
         }
         h2 = i;
         h3 = next(i, 1);
         h1 = next(j, 1);
         int h2_prev = next(i, -1);
-        if (exists_bound<OV>(h1) && exists_bound<OV>(h3) && gbnd<OV>(h1) != h3 && !doubly_contig<OV>(h2, h3)) {
-            if (pair_stacked<OV>(j, h1) && pair_stacked<OV>(h2, h3)) triplet_double<OV>(h1, h2, h3);
+        if (exists_bound(h1) && exists_bound(h3) && gbnd(h1) != h3 && !doubly_contig(h2, h3)) {
+            if (pair_stacked(j, h1) && pair_stacked(h2, h3)) triplet_double(h1, h2, h3);
         }
         h1 = next(j, -1);
-        if (exists_bound<OV>(h1) && exists_bound<OV>(h3) && gbnd<OV>(h1) != h2_prev && !doubly_contig<OV>(h2, h3)) {
-            if (pair_stacked<OV>(h2, h3)) {
-                if (pair_stacked<OV>(h1, j)) triplet_double<OV>(h1, h2, h3);
-                else triplet_single<OV>(h1, j, h3);
+        if (exists_bound(h1) && exists_bound(h3) && gbnd(h1) != h2_prev && !doubly_contig(h2, h3)) {
+            if (pair_stacked(h2, h3)) {
+                if (pair_stacked(h1, j)) triplet_double(h1, h2, h3);
+                else triplet_single(h1, j, h3);
             }
         }
     }
 
     // The three single-junction searches (:654, :750, :846) share one shape:
     // up to three kink pairs, then up to three second junction pairs each.
-    template <bool OV> __device__ __noinline__ void backward_single_junction(int c1, int c2) {   // :654
+    __device__ __noinline__ void backward_single_junction(int c1, int c2) {   // :654
         int j3 = c1, j4 = c2;
         FBState& F = fbst();
         int* fa = F.fa;
@@ -1202,15 +1127,15 @@ struct Rep : public LdoState<C> {
         int nf = 0;
         int j3_bac = bwd(j3);
         fa[nf] = j3; fb[nf] = j3_bac; nf++;
-        int j3_b = gbnd<OV>(j3);
+        int j3_b = gbnd(j3);
         int j3_b_for = fwd(j3_b), j3_b_bac = bwd(j3_b);
-        if (j3_b_for == gbnd<OV>(j4)) {
+        if (j3_b_for == gbnd(j4)) {
             fa[nf] = j3_b; fb[nf] = j3_b_bac; nf++;
         }
-        else if (exists_bound<OV>(j3_bac) && exists_bound<OV>(j3_b_bac) && gbnd<OV>(j3_bac) == j3_b_bac) {
+        else if (exists_bound(j3_bac) && exists_bound(j3_b_bac) && gbnd(j3_bac) == j3_b_bac) {
             fa[nf] = j3_b; fb[nf] = j3_b_for; nf++;
         }
-        else if (exists_bound<OV>(j3_bac) && exists_bound<OV>(j3_b_for) && gbnd<OV>(j3_bac) == j3_b_for) {
+        else if (exists_bound(j3_bac) && exists_bound(j3_b_for) && gbnd(j3_bac) == j3_b_for) {
             fa[nf] = j3_b; fb[nf] = j3_b_bac; nf++;
         }
         else {
@@ -1220,18 +1145,18 @@ struct Rep : public LdoState<C> {
         #pragma unroll 1
         for (int a = 0; a < nf; ++a) {
             int k2 = fa[a], k1 = fb[a];
-            if (!exists_bound<OV>(k1)) continue;
-            if (pair_stacked<OV>(k1, k2)) continue;
+            if (!exists_bound(k1)) continue;
+            if (pair_stacked(k1, k2)) continue;
             int* sa = F.sa;
             int* sb = F.sb;
             int ns_ = 0;
             int dir = sd[k1] - sd[k2];
             int k1_next = next(k1, dir);
             sa[ns_] = k1; sb[ns_] = k1_next; ns_++;
-            int k1_b = gbnd<OV>(k1);
+            int k1_b = gbnd(k1);
             int k1_b_for = fwd(k1_b), k1_b_bac = bwd(k1_b);
-            if (exists_bound<OV>(k1_next)) {
-                int kn_b = gbnd<OV>(k1_next);
+            if (exists_bound(k1_next)) {
+                int kn_b = gbnd(k1_next);
                 if (k1_b_for != kn_b) { sa[ns_] = k1_b; sb[ns_] = k1_b_for; ns_++; }
                 if (k1_b_bac != kn_b) { sa[ns_] = k1_b; sb[ns_] = k1_b_bac; ns_++; }
             }
@@ -1242,13 +1167,13 @@ struct Rep : public LdoState<C> {
             #pragma unroll 1
             for (int b = 0; b < ns_; ++b) {
                 int j2 = sa[b], j1 = sb[b];
-                if (!exists_bound<OV>(j1)) continue;
-                junction<OV>(j1, j2, j3, j4, k1, k2);
+                if (!exists_bound(j1)) continue;
+                junction(j1, j2, j3, j4, k1, k2);
             }
         }
     }
 
-    template <bool OV> __device__ __noinline__ void forward_single_junction(int c1, int c2) {   // :750
+    __device__ __noinline__ void forward_single_junction(int c1, int c2) {   // :750
         int j1 = c1, j2 = c2;
         FBState& F = fbst();
         int* fa = F.fa;
@@ -1256,16 +1181,16 @@ struct Rep : public LdoState<C> {
         int nf = 0;
         int j2_for = fwd(j2);
         fa[nf] = j2; fb[nf] = j2_for; nf++;
-        int j1_b = gbnd<OV>(j1);
-        int j2_b = gbnd<OV>(j2);
+        int j1_b = gbnd(j1);
+        int j2_b = gbnd(j2);
         int j2_b_for = fwd(j2_b), j2_b_bac = bwd(j2_b);
         if (next(j1_b, 1) == j2_b) {
             fa[nf] = j2_b; fb[nf] = j2_b_for; nf++;
         }
-        else if (exists_bound<OV>(j2_for) && exists_bound<OV>(j2_b_bac) && gbnd<OV>(j2_for) == j2_b_bac) {
+        else if (exists_bound(j2_for) && exists_bound(j2_b_bac) && gbnd(j2_for) == j2_b_bac) {
             fa[nf] = j2_b; fb[nf] = j2_b_for; nf++;
         }
-        else if (exists_bound<OV>(j2_for) && exists_bound<OV>(j2_b_for) && gbnd<OV>(j2_for) == j2_b_for) {
+        else if (exists_bound(j2_for) && exists_bound(j2_b_for) && gbnd(j2_for) == j2_b_for) {
             fa[nf] = j2_b; fb[nf] = j2_b_bac; nf++;
         }
         else {
@@ -1275,18 +1200,18 @@ struct Rep : public LdoState<C> {
         #pragma unroll 1
         for (int a = 0; a < nf; ++a) {
             int k1 = fa[a], k2 = fb[a];
-            if (!exists_bound<OV>(k2)) continue;
-            if (pair_stacked<OV>(k1, k2)) continue;
+            if (!exists_bound(k2)) continue;
+            if (pair_stacked(k1, k2)) continue;
             int* sa = F.sa;
             int* sb = F.sb;
             int ns_ = 0;
             int dir = sd[k2] - sd[k1];
             int k2_next = next(k2, dir);
             sa[ns_] = k2; sb[ns_] = k2_next; ns_++;
-            int k2_b = gbnd<OV>(k2);
+            int k2_b = gbnd(k2);
             int k2_b_for = fwd(k2_b), k2_b_bac = bwd(k2_b);
-            if (exists_bound<OV>(k2_next)) {
-                int kn_b = gbnd<OV>(k2_next);
+            if (exists_bound(k2_next)) {
+                int kn_b = gbnd(k2_next);
                 if (k2_b_for != kn_b) { sa[ns_] = k2_b; sb[ns_] = k2_b_for; ns_++; }
                 if (k2_b_bac != kn_b) { sa[ns_] = k2_b; sb[ns_] = k2_b_bac; ns_++; }
             }
@@ -1297,15 +1222,15 @@ struct Rep : public LdoState<C> {
             #pragma unroll 1
             for (int b = 0; b < ns_; ++b) {
                 int j3 = sa[b], j4 = sb[b];
-                if (!exists_bound<OV>(j4)) continue;
-                junction<OV>(j1, j2, j3, j4, k1, k2);
+                if (!exists_bound(j4)) continue;
+                junction(j1, j2, j3, j4, k1, k2);
             }
         }
     }
 
-    template <bool OV> __device__ __noinline__ void central_single_junction(int c1, int c2) {   // :846
+    __device__ __noinline__ void central_single_junction(int c1, int c2) {   // :846
         int k1 = c1, k2 = c2;
-        int kb1 = gbnd<OV>(k1), kb2 = gbnd<OV>(k2);
+        int kb1 = gbnd(k1), kb2 = gbnd(k2);
         int dd = sd[kb1] - sd[kb2];
         if (scs[kb1] == scs[kb2] && (dd == 1 || dd == -1)) return;
         FBState& F = fbst();
@@ -1315,8 +1240,8 @@ struct Rep : public LdoState<C> {
         int k1_bac = bwd(k1);
         fa[nf] = k1; fb[nf] = k1_bac; nf++;
         int k1_b_for = fwd(kb1), k1_b_bac = bwd(kb1);
-        if (exists_bound<OV>(k1_bac)) {
-            int kbb = gbnd<OV>(k1_bac);
+        if (exists_bound(k1_bac)) {
+            int kbb = gbnd(k1_bac);
             if (k1_b_for != kbb) { fa[nf] = kb1; fb[nf] = k1_b_for; nf++; }
             if (k1_b_bac != kbb) { fa[nf] = kb1; fb[nf] = k1_b_bac; nf++; }
         }
@@ -1327,15 +1252,15 @@ struct Rep : public LdoState<C> {
         #pragma unroll 1
         for (int a = 0; a < nf; ++a) {
             int j2 = fa[a], j1 = fb[a];
-            if (!exists_bound<OV>(j1)) continue;
+            if (!exists_bound(j1)) continue;
             int* sa = F.sa;
             int* sb = F.sb;
             int ns_ = 0;
             int k2_for = fwd(k2);
             sa[ns_] = k2; sb[ns_] = k2_for; ns_++;
             int k2_b_for = fwd(kb2), k2_b_bac = bwd(kb2);
-            if (exists_bound<OV>(k2_for)) {
-                int kfb = gbnd<OV>(k2_for);
+            if (exists_bound(k2_for)) {
+                int kfb = gbnd(k2_for);
                 if (k2_b_for != kfb) { sa[ns_] = kb2; sb[ns_] = k2_b_for; ns_++; }
                 if (k2_b_bac != kfb) { sa[ns_] = kb2; sb[ns_] = k2_b_bac; ns_++; }
             }
@@ -1346,28 +1271,28 @@ struct Rep : public LdoState<C> {
             #pragma unroll 1
             for (int b = 0; b < ns_; ++b) {
                 int j3 = sa[b], j4 = sb[b];
-                if (!exists_bound<OV>(j4)) continue;
-                junction<OV>(j1, j2, j3, j4, k1, k2);
+                if (!exists_bound(j4)) continue;
+                junction(j1, j2, j3, j4, k1, k2);
             }
         }
     }
 
     // OrigamiPotential::bind_domain (:1282) with BindingPotential::bind_domains
     // (:131) and the misbinding potentials (:938, :947)
-    template <bool OV> __device__ __noinline__ Delta bind_domain(int i) {
+    __device__ __noinline__ Delta bind_domain(int i) {
         fbst().viol = false;
-        int j = gbnd<OV>(i);
+        int j = gbnd(i);
         Delta dc;
         dc.e = 0;
         dc.stacked = 0;
         if (did[i] == -did[j]) {
             fbst().pd.e = 0;
             fbst().pd.stacked = 0;
-            if (gore<OV>(i) != (gore<OV>(j) ^ 1)) {
+            if (gore(i) != (gore(j) ^ 1)) {
                 fbst().viol = true;
                 return dc;
             }
-            stacking_and_steric<OV>(i, j);
+            stacking_and_steric(i, j);
             if (fbst().viol) return dc;
             fbst().pd.e += hyb(i, j);
             dc = fbst().pd;
@@ -1375,17 +1300,17 @@ struct Rep : public LdoState<C> {
         else {
             fbst().viol = true;
             if (sys->mis_disallowed) return dc;
-            if (gore<OV>(i) != (gore<OV>(j) ^ 1)) return dc;
+            if (gore(i) != (gore(j) ^ 1)) return dc;
             fbst().viol = false;
             dc.e += hyb(i, j);
         }
         return dc;
     }
-    template <bool OV> __device__ __noinline__ Delta check_stacking(int i, int j) {   // :149
+    __device__ __noinline__ Delta check_stacking(int i, int j) {   // :149
         fbst().pd.e = 0;
         fbst().pd.stacked = 0;
         fbst().viol = false;
-        stacking_and_steric<OV>(i, j);
+        stacking_and_steric(i, j);
         return fbst().pd;
     }
 
@@ -1801,44 +1726,29 @@ struct Rep : public LdoState<C> {
         int* core = cb_ore;
         double* bf = cb_bf;
         int nc = 0;
-        // Classify the six neighbour sites; unbound ones are probed in
-        // parallel, empty ones weigh 6 (no potential is evaluated there:
-        // 6 * dexp(-0), src/cb_movetypes.cpp:92-99), occupied ones are skipped.
-        int* kind = cb_kind;
-        int* slot_of_v = cb_slot;
-        int n_unb = 0;
-        volatile ProbeTask* t = task;
-        #pragma unroll 1
+        // The six neighbour sites in the reference's order: unbound ones are
+        // probed, empty ones weigh 6 (no potential is evaluated there:
+        // 6 * exp(-0), src/cb_movetypes.cpp:92-99), occupied ones are skipped.
+#pragma unroll 1
         for (int v = 0; v < 6; ++v) {
             V3 p = add(p_prev, unit(v));
             int occ = occupancy(p);
-            if (occ == BOUND || occ == MISBOUND) {
-                kind[v] = 0;
-            }
-            else if (occ == UNBOUND) {
-                kind[v] = 1;
+            if (occ == BOUND || occ == MISBOUND) continue;
+            if (occ == UNBOUND) {
                 int ud = unbound_at(p);
-                t->ud[n_unb] = ud;
-                t->o[n_unb] = ore[ud] ^ 1;
-                t->p[n_unb] = p;
-                slot_of_v[v] = n_unb++;
-            }
-            else {
-                kind[v] = 2;
-            }
-        }
-        if (n_unb > 0) run_probes(dom, n_unb);
-        #pragma unroll 1
-        for (int v = 0; v < 6; ++v) {
-            if (kind[v] == 0) continue;
-            V3 p = add(p_prev, unit(v));
-            if (kind[v] == 1) {
-                int k = slot_of_v[v];
-                if (!t->viol[k]) {
+                int o = ore[ud] ^ 1;
+                double de = probe_domain(dom, p, o);
+                if (bad()) return;
+                if (!hdr.violated) {
                     cpos[nc] = p;
-                    core[nc] = t->o[k];
-                    bf[nc] = t->bf[k];
+                    core[nc] = o;
+                    double b = 1;
+                    b *= dexp(-de);
+                    bf[nc] = b;
                     nc++;
+                }
+                else {
+                    hdr.violated = 0;
                 }
             }
             else {

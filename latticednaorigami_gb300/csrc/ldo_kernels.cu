@@ -44,20 +44,14 @@ __device__ void bind_rep(ldo::Rep<C>& r, const LdoLaunch& L, int rep) {
     r.log6 = log(6.0);
     r.log3 = log(3.0);
     r.rng.init(r.ctl->seed, r.ctl->rep, 0u, r.hdr.draws);
-    for (int q = 0; q < 6; ++q) {
-        r.fbs[q].ov_d = -1;
-        r.fbs[q].ov_p = -1;
-    }
 }
 
-__host__ __device__ constexpr int task_bytes() { return (int)((sizeof(ldo::ProbeTask) + 15) / 16 * 16); }
 template <class C>
 __host__ __device__ constexpr int rep_bytes() { return (int)((sizeof(ldo::Rep<C>) + 15) / 16 * 16); }
 template <class C>
-__host__ __device__ constexpr int warp_bytes() { return rep_bytes<C>() + task_bytes(); }
+__host__ __device__ constexpr int warp_bytes() { return rep_bytes<C>(); }
 
-// Shared memory per warp: Rep (replica state followed by the working fields)
-// then the probe task.
+// Shared memory per warp: Rep (replica state followed by the working fields).
 template <class C>
 __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -67,21 +61,11 @@ __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
     if (rep >= L.n_rep) return;
     unsigned char* base = smem + (size_t)warp * warp_bytes<C>();
     ldo::Rep<C>* R = reinterpret_cast<ldo::Rep<C>*>(base);
-    ldo::ProbeTask* task = reinterpret_cast<ldo::ProbeTask*>(base + rep_bytes<C>());
     unsigned char* gbase = L.arena + (size_t)rep * sizeof(LdoState<C>);
     warp_copy16(base, gbase, (int)sizeof(LdoState<C>), lane);
     __syncwarp();
     if (lane == 0) {
-        task->cmd = 0;
         bind_rep<C>(*R, L, rep);
-        R->task = task;
-    }
-    __syncwarp();
-    if (lane > 0 && lane < 6) {
-        // Lanes 1..5 evaluate CB trial positions for lane 0.
-        R->probe_helper_loop();
-    }
-    else if (lane == 0) {
         LdoHdr& h = R->hdr;
         if (h.status == 0) {
             if (L.mode == LDO_MODE_INIT) {
@@ -138,7 +122,6 @@ __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
             if (L.want_dep && !R->bad()) R->dependent_quantities();
             h.draws = R->rng.draws;
         }
-        R->post_exit();
     }
     __syncwarp();
     warp_copy16(gbase, base, (int)sizeof(LdoState<C>), lane);
