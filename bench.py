@@ -46,7 +46,10 @@ def write_c2(d):
         with open(os.path.join(d, "moves.json"), "w") as f:
             json.dump(systems.moves_json("met3"), f)
         with open(os.path.join(d, "ops.json"), "w") as f:
-            json.dump(systems.OPS, f)
+            json.dump({"origami": {"order_params": [
+                {"label": "Number of bound staples", "tag": "numstaples", "type": "NumStaples", "level": 0},
+                {"label": "Number of fully bound domain pairs", "tag": "numfulldomains",
+                 "type": "NumBoundDomainPairs", "level": 0}]}}, f)
         opts = dict(systems.BASE)
         opts.update(origami_input_filename="c2_%d.json" % n, movetype_file="moves.json",
                     hybridization_pot="Uniform", binding_h=repr(bh), binding_s=repr(bs), stacking_ene=1000,

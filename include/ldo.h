@@ -148,6 +148,23 @@ ldo_status ldo_pt_get_permutation(ldo_engine* e, int32_t* out, int n);
 /* Swap attempts and acceptances per neighbouring slot pair, summed over ladders. */
 ldo_status ldo_pt_get_stats(ldo_engine* e, int64_t* attempts, int64_t* accepts, int n_pairs);
 
+/* Multi-window umbrella sampling with adaptive grid biases
+ * (MWUSGCMCSimulation::run / PTMWUSGCMCSimulation::run with the updates of
+ * SimpleUSGCMCSimulation, src/us_simulation.cpp:84-434, 454-864).  Window w
+ * starts on replica w; the windows and their square-well bias come from the
+ * system's windows_file (none: one unrestrained window per replica).  After
+ * equil_steps, each of n_iters iterations runs iter_steps steps, counting the
+ * grid point of `grid_tag` after every step, then sets each visited point's
+ * bias to ln of its reweighted probability, changes limited to max_D_bias.
+ * exchange_interval > 0 attempts neighbouring-window exchanges every that
+ * many steps (PTMWUS); window assignments move, configurations stay. */
+ldo_status ldo_us_run(ldo_engine* e, const char* grid_tag, int n_iters, int64_t equil_steps, int64_t iter_steps,
+                      double max_D_bias, int exchange_interval, double* device_ms);
+/* Grid biases per window: out[w * grid_len + point]. */
+ldo_status ldo_us_get_biases(ldo_engine* e, double* out, int n_windows, int grid_len);
+/* Window held by each replica, and the grid length. */
+ldo_status ldo_us_get_windows(ldo_engine* e, int32_t* window_of_replica, int n, int* grid_len);
+
 /* Host-only helpers (no GPU needed). */
 
 /* Reduced hybridisation enthalpy H/(RT) and entropy S/R of a fully paired

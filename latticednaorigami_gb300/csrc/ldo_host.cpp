@@ -351,6 +351,20 @@ struct ldo_engine {
     cudaGraphExec_t pt_graph {nullptr};
     LdoPT pt {};
 
+    // umbrella sampling (one SimpleUS state per window)
+    struct USWindow {
+        int min_op {0}, max_op {0};
+        std::vector<double> E_w;        // bias per grid point (0 off grid)
+        std::vector<char> in_S;         // point visited in an earlier iteration (m_S_n)
+    };
+    std::vector<USWindow> us_win;
+    std::vector<int> us_window_of;      // replica -> window
+    std::vector<int> us_replica_of;     // window -> replica
+    DevBuf<int> d_us_hist, d_us_window;
+    int us_bias {-1}, us_len {0}, us_sq_bias {-1};
+    unsigned long long us_swap_draws {0};
+    std::vector<long long> us_att, us_acc;
+
     ~ldo_engine() {
         if (pt_graph) cudaGraphExecDestroy(pt_graph);
         if (ev0) cudaEventDestroy(ev0);
@@ -432,6 +446,8 @@ struct ldo_engine {
         L.n_trace = n_trace;
         L.trace_max = trace_max;
         L.trace = d_trace.p;
+        L.us_hist = nullptr;
+        L.us_window = nullptr;
         return L;
     }
 
@@ -817,6 +833,222 @@ struct ldo_engine {
     }
     int pt_graph_interval {0};
 
+    // ------------------------------------------------ umbrella sampling ----
+    static uint64_t host_philox_word(uint32_t seed, uint32_t key1, uint32_t stream, unsigned long long draw) {
+        unsigned long long b = draw >> 1;
+        uint32_t c0 = (uint32_t)b, c1 = (uint32_t)(b >> 32), c2 = stream, c3 = 0, k0 = seed, k1 = key1;
+        for (int r = 0; r < 10; ++r) {
+            uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+            uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+            uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n1 = (uint32_t)p1;
+            uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1, n3 = (uint32_t)p0;
+            c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        uint32_t w[4] = {c0, c1, c2, c3};
+        int j = (int)(draw & 1) * 2;
+        return ((uint64_t)w[j] << 32) | w[j + 1];
+    }
+    double us_uniform() {   // window-exchange stream: key (seed, 0), stream 2
+        uint64_t x = host_philox_word(seed, 0u, 2u, us_swap_draws++);
+        return (double)(x >> 11) * 0x1.0p-53;
+    }
+
+    void us_setup(const string& grid_tag) {
+        const HostSystem& hs = systems[sys_of[0]];
+        for (int r = 0; r < n_rep; ++r)
+            if (sys_of[r] != sys_of[0]) throw LdoError(LDO_EINVAL, "umbrella windows must share one system");
+        us_bias = -1;
+        for (int b = 0; b < hs.desc.n_biases; ++b)
+            if (hs.biases[b].tag == grid_tag && hs.desc.bias_kind[b] == LDO_B_GRID) us_bias = b;
+        if (us_bias < 0) throw LdoError(LDO_EINVAL, "us_grid_bias_tag " + grid_tag + " is not a Grid bias function");
+        us_len = hs.desc.bias_grid_len[us_bias];
+        int nw = n_rep;
+        us_win.assign(nw, USWindow {});
+        us_sq_bias = -1;
+        if (!hs.p.windows_file.empty()) {
+            ldo_io::Windows w;
+            try {
+                w = ldo_io::read_windows(ldo_io::resolve(hs.p, hs.p.windows_file));
+            } catch (std::exception& x) {
+                throw LdoError(LDO_EINVAL, x.what());
+            }
+            if ((int)w.bounds.size() != nw)
+                throw LdoError(LDO_EINVAL, "number of windows must equal the number of replicas");
+            for (int b = 0; b < hs.desc.n_biases; ++b)
+                if (hs.biases[b].tag == w.bias_tag) us_sq_bias = b;
+            if (us_sq_bias < 0) throw LdoError(LDO_EINVAL, "window bias function " + w.bias_tag + " not found");
+            for (int i = 0; i < nw; ++i) {
+                us_win[i].min_op = w.bounds[i].first;
+                us_win[i].max_op = w.bounds[i].second;
+            }
+        }
+        else {
+            for (int i = 0; i < nw; ++i) {
+                us_win[i].min_op = 0;
+                us_win[i].max_op = us_len - 1;
+            }
+        }
+        for (auto& w : us_win) {
+            w.E_w.assign(us_len, 0.0);
+            w.in_S.assign(us_len, 0);
+        }
+        us_window_of.resize(n_rep);
+        us_replica_of.resize(nw);
+        for (int r = 0; r < n_rep; ++r) {
+            us_window_of[r] = r;
+            us_replica_of[r] = r;
+        }
+        us_att.assign(std::max(nw - 1, 1), 0);
+        us_acc.assign(std::max(nw - 1, 1), 0);
+        us_swap_draws = 0;
+        d_us_hist.alloc((size_t)nw * us_len);
+        d_us_window.alloc(n_rep);
+        us_apply_windows();
+    }
+
+    // Window restraint and grid values of every replica follow the window it holds
+    // (MWUSGCMCSimulation::setup_window_restraints, src/us_simulation.cpp:503).
+    void us_apply_windows() {
+        for (int r = 0; r < n_rep; ++r) {
+            const USWindow& w = us_win[us_window_of[r]];
+            if (us_sq_bias >= 0) {
+                h_ctl[r].win_min[us_sq_bias] = w.min_op;
+                h_ctl[r].win_max[us_sq_bias] = w.max_op;
+            }
+            int off = h_ctl[r].grid_off[us_bias];
+            for (int x = 0; x < us_len; ++x) h_grid[off + x] = w.E_w[x];
+        }
+        upload_ctl();
+        upload_grid();
+        CU(cudaMemcpy(d_us_window.p, us_window_of.data(), n_rep * sizeof(int), cudaMemcpyHostToDevice));
+    }
+
+    void us_launch(long long steps, bool record) {
+        LdoLaunch L = launch_params(LDO_MODE_RUN, steps);
+        if (record) {
+            L.us_hist = d_us_hist.p;
+            L.us_window = d_us_window.p;
+            L.us_bias = us_bias;
+            L.us_len = us_len;
+        }
+        CU(ldo_launch_mc(L, stream));
+    }
+
+    // PTMWUSGCMCSimulation::attempt_exchange (src/us_simulation.cpp:770-864):
+    // neighbouring windows of parity swap_i % 2 exchange when both grid points
+    // lie in the other window, with probability min(1, exp(bias difference)).
+    void us_exchange(int swap_i) {
+        int nw = (int)us_win.size();
+        vector<int> point(nw, -1);
+        auto host = download_arena();
+        const HostSystem& hs = systems[sys_of[0]];
+        int oq = hs.desc.bias_op[us_bias];
+        for (int w = 0; w < nw; ++w) {
+            int r = us_replica_of[w];
+            const auto* op = reinterpret_cast<const int32_t*>(host.data() + (size_t)r * lay.bytes + lay.o_op);
+            point[w] = op[2 * oq];
+        }
+        for (int i = swap_i % 2; i < nw - 1; i += 2) {
+            us_att[i]++;
+            int w1 = i, w2 = i + 1;
+            int p1 = point[w1], p2 = point[w2];
+            bool inside = !(p2 < us_win[w1].min_op || p2 > us_win[w1].max_op) &&
+                          !(p1 < us_win[w2].min_op || p1 > us_win[w2].max_op);
+            if (!inside) continue;
+            bool accepted = true;
+            if (p1 != p2) {
+                auto bias_at = [&](int w, int p) { return (p >= 0 && p < us_len) ? us_win[w].E_w[p] : 0.0; };
+                double d1 = bias_at(w1, p1) - bias_at(w2, p1);
+                double d2 = bias_at(w2, p2) - bias_at(w1, p2);
+                double pa = std::min(1.0, std::exp(d1 + d2));
+                accepted = (pa == 1) ? true : (pa > us_uniform());
+            }
+            if (accepted) {
+                us_acc[i]++;
+                int r1 = us_replica_of[w1], r2 = us_replica_of[w2];
+                us_replica_of[w1] = r2;
+                us_replica_of[w2] = r1;
+                us_window_of[r1] = w2;
+                us_window_of[r2] = w1;
+            }
+        }
+        us_apply_windows();
+    }
+
+    // SimpleUSGCMCSimulation::process_iteration (src/us_simulation.cpp:154,
+    // 286-416): reweight this iteration's visits by the biases it ran with,
+    // set each visited point's bias to ln p (a point seen before but not now
+    // loses max_D_bias), and limit every change to max_D_bias.
+    void us_process_iteration(const vector<int>& hist, double max_D) {
+        int nw = (int)us_win.size();
+        for (int w = 0; w < nw; ++w) {
+            USWindow& W = us_win[w];
+            const int* f = hist.data() + (size_t)w * us_len;
+            double ave = 0;
+            for (int x = 0; x < us_len; ++x)
+                if (f[x] > 0) ave += f[x] * std::exp(W.E_w[x]);
+            vector<double> p(us_len, 0.0);
+            for (int x = 0; x < us_len; ++x)
+                if (f[x] > 0) p[x] = f[x] * std::exp(W.E_w[x]) / ave;
+            for (int x = 0; x < us_len; ++x)
+                if (f[x] > 0) W.in_S[x] = 1;
+            for (int x = 0; x < us_len; ++x) {
+                if (!W.in_S[x]) continue;
+                double old_bias = W.E_w[x];
+                double D, nb;
+                if (p[x] == 0) {
+                    D = -max_D;
+                    nb = old_bias + D;
+                }
+                else {
+                    nb = std::log(p[x]);
+                    D = nb - old_bias;
+                }
+                double upd = nb;
+                if (std::abs(D) > max_D) upd = D > 0 ? old_bias + max_D : old_bias - max_D;
+                W.E_w[x] = upd;
+            }
+        }
+        us_apply_windows();
+    }
+
+    void us_run(const string& tag, int n_iters, long long equil_steps, long long iter_steps, double max_D,
+                int exchange_interval, double* ms) {
+        us_setup(tag);
+        CU(cudaEventRecord(ev0, stream));
+        // USGCMCSimulation::run_equilibration
+        if (equil_steps > 0) us_launch(equil_steps, false);
+        int nw = (int)us_win.size();
+        vector<int> hist((size_t)nw * us_len);
+        for (int n = 0; n < n_iters; ++n) {
+            CU(cudaMemsetAsync(d_us_hist.p, 0, hist.size() * sizeof(int), stream));
+            if (exchange_interval > 0) {
+                long long swaps = iter_steps / exchange_interval;
+                for (long long s = 1; s <= swaps; ++s) {
+                    us_launch(exchange_interval, true);
+                    us_exchange((int)s);
+                }
+            }
+            else {
+                us_launch(iter_steps, true);
+            }
+            CU(cudaMemcpyAsync(hist.data(), d_us_hist.p, hist.size() * sizeof(int), cudaMemcpyDeviceToHost, stream));
+            CU(cudaStreamSynchronize(stream));
+            check_status();
+            us_process_iteration(hist, max_D);
+        }
+        CU(cudaEventRecord(ev1, stream));
+        CU(cudaStreamSynchronize(stream));
+        if (ms) {
+            float f = 0;
+            CU(cudaEventElapsedTime(&f, ev0, ev1));
+            *ms = f;
+        }
+        check_status();
+    }
+
     vector<unsigned char> download_arena() {
         vector<unsigned char> host((size_t)n_rep * lay.bytes);
         CU(cudaMemcpy(host.data(), d_arena.p, host.size(), cudaMemcpyDeviceToHost));
@@ -1083,6 +1315,31 @@ ldo_status ldo_pt_get_stats(ldo_engine* e, int64_t* attempts, int64_t* accepts, 
     return guard(e, [&]() {
         CU(cudaMemcpy(attempts, e->d_pt_att.p, n_pairs * sizeof(int64_t), cudaMemcpyDeviceToHost));
         CU(cudaMemcpy(accepts, e->d_pt_acc.p, n_pairs * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    });
+}
+
+ldo_status ldo_us_run(ldo_engine* e, const char* grid_tag, int n_iters, int64_t equil_steps, int64_t iter_steps,
+                      double max_D_bias, int exchange_interval, double* device_ms) {
+    if (!e || !grid_tag || n_iters < 0 || equil_steps < 0 || iter_steps < 0 || exchange_interval < 0)
+        return LDO_EINVAL;
+    return guard(e, [&]() {
+        e->us_run(grid_tag, n_iters, equil_steps, iter_steps, max_D_bias, exchange_interval, device_ms);
+    });
+}
+
+ldo_status ldo_us_get_biases(ldo_engine* e, double* out, int n_windows, int grid_len) {
+    if (!e || !out || n_windows != (int)e->us_win.size() || grid_len != e->us_len) return LDO_EINVAL;
+    return guard(e, [&]() {
+        for (int w = 0; w < n_windows; ++w)
+            for (int x = 0; x < grid_len; ++x) out[(size_t)w * grid_len + x] = e->us_win[w].E_w[x];
+    });
+}
+
+ldo_status ldo_us_get_windows(ldo_engine* e, int32_t* window_of_replica, int n, int* grid_len) {
+    if (!e || !window_of_replica || n != e->n_rep || e->us_win.empty()) return LDO_EINVAL;
+    return guard(e, [&]() {
+        for (int r = 0; r < n; ++r) window_of_replica[r] = e->us_window_of[r];
+        if (grid_len) *grid_len = e->us_len;
     });
 }
 

@@ -108,6 +108,13 @@ __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
                         t[6] = h.move_bias * R->c_bias_mult;
                         t[7] = (double)R->rng.draws;
                     }
+                    if (L.us_hist) {
+                        int oq = R->sys->bias_op[L.us_bias];
+                        if (R->op[2 * oq + 1]) {
+                            int x = R->op[2 * oq];
+                            if (x >= 0 && x < L.us_len) L.us_hist[(size_t)L.us_window[rep] * L.us_len + x] += 1;
+                        }
+                    }
                     if (sint > 0 && s % sint == 0) {
                         int c = h.sample_count;
                         if (c < L.sample_cap) {

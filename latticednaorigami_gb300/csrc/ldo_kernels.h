@@ -27,6 +27,12 @@ struct LdoLaunch {
     int16_t* samples;
     int n_trace, trace_max;
     double* trace;
+    // Umbrella-sampling visit histogram (USGCMCSimulation::update_internal,
+    // src/us_simulation.cpp:262): after every step the grid order parameter of
+    // bias function us_bias is counted in us_hist[window * us_len + value].
+    int* us_hist;
+    const int* us_window;        // [n_rep] window held by each replica
+    int us_bias, us_len;
 };
 
 cudaError_t ldo_launch_mc(const LdoLaunch& L, cudaStream_t stream);

@@ -19,7 +19,7 @@ EXPORTS = [
     "ldo_set_controls", "ldo_run", "ldo_run_sweeps", "ldo_state_bytes", "ldo_get_observables", "ldo_get_config", "ldo_set_sampling",
     "ldo_get_samples", "ldo_set_trace", "ldo_get_trace", "ldo_get_move_stats", "ldo_set_grid_bias",
     "ldo_set_window", "ldo_pt_run", "ldo_pt_get_permutation", "ldo_pt_get_stats", "ldo_nn_duplex_thermo",
-    "ldo_energy_tables",
+    "ldo_energy_tables", "ldo_us_run", "ldo_us_get_biases", "ldo_us_get_windows",
 ]
 
 
@@ -76,6 +76,9 @@ def load_library(path=None):
     lib.ldo_pt_run.argtypes = [vp, ip, ctypes.c_int64, ip, ip, dp]
     lib.ldo_pt_get_permutation.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ip]
     lib.ldo_pt_get_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64), ip]
+    lib.ldo_us_run.argtypes = [vp, ctypes.c_char_p, ip, ctypes.c_int64, ctypes.c_int64, ctypes.c_double, ip, dp]
+    lib.ldo_us_get_biases.argtypes = [vp, dp, ip, ip]
+    lib.ldo_us_get_windows.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ip, ctypes.POINTER(ctypes.c_int)]
     lib.ldo_nn_duplex_thermo.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, dp, dp]
     lib.ldo_energy_tables.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
                                       dp, dp, dp, dp, dp, ip]
@@ -192,6 +195,25 @@ class Engine:
         self._check(self.lib.ldo_pt_run(self.h, n_rungs, int(swaps), exchange_interval, exchange_q,
                                         ctypes.byref(ms)))
         return ms.value
+
+    def us_run(self, grid_tag, n_iters, equil_steps, iter_steps, max_D_bias, exchange_interval=0):
+        ms = ctypes.c_double(0)
+        self._check(self.lib.ldo_us_run(self.h, grid_tag.encode(), n_iters, int(equil_steps), int(iter_steps),
+                                        float(max_D_bias), exchange_interval, ctypes.byref(ms)))
+        return ms.value
+
+    def us_windows(self):
+        w = np.zeros(self.n, np.int32)
+        gl = ctypes.c_int(0)
+        self._check(self.lib.ldo_us_get_windows(self.h, w.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), self.n,
+                                                ctypes.byref(gl)))
+        return w, gl.value
+
+    def us_biases(self):
+        w, gl = self.us_windows()
+        out = np.zeros((self.n, gl))
+        self._check(self.lib.ldo_us_get_biases(self.h, _dptr(out), self.n, gl))
+        return out
 
     def pt_permutation(self):
         out = np.zeros(self.n, np.int32)

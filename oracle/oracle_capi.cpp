@@ -313,6 +313,29 @@ void oracle_dependent_qs(void* h, double* out) {
     out[3] = s.total_bias();
 }
 
+// SquareWellBiasFunction::set_min_op / set_max_op (src/bias_functions.cpp:218-220)
+int oracle_set_window(void* h, const char* tag, int min_op, int max_op) {
+    System& s = static_cast<Replica*>(h)->sys;
+    for (auto& b : s.biases)
+        if (b.tag == tag) {
+            b.min_op = min_op;
+            b.max_op = max_op;
+            return 0;
+        }
+    g_err = std::string("no bias ") + tag;
+    return -1;
+}
+
+// `count` uniform reals of Philox key (seed, key1), stream `stream`, from draw `first`.
+void oracle_uniforms(uint32_t seed, uint32_t key1, uint32_t stream, unsigned long long first, int count, double* out) {
+    Stream st;
+    st.key[0] = seed;
+    st.key[1] = key1;
+    st.stream = stream;
+    st.draws = first;
+    for (int i = 0; i < count; ++i) out[i] = st.uniform_real();
+}
+
 // Staple counts per chain type (index 0 = scaffold, always 0 here), as
 // OrigamiSystem::get_staple_counts (src/origami_system.cpp:153).
 int oracle_staple_counts(void* h, int* out, int cap) {
@@ -339,10 +362,10 @@ int oracle_set_grid(void* h, const char* tag, const double* vals, int n) {
     System& s = static_cast<Replica*>(h)->sys;
     for (auto& b : s.biases)
         if (b.tag == tag && b.kind == B_GRID) {
+            // GridBiasFunction::replace_biases (src/bias_functions.cpp:237): the
+            // cached bias value changes only at the next update.
             b.grid.assign(vals, vals + n);
             b.grid_set = true;
-            s.update_move_params();
-            s.calc_move();
             return 0;
         }
     g_err = std::string("no grid bias ") + tag;

@@ -143,3 +143,19 @@ def run_batch_sampled(inp, seed, n_rep, sweeps, sweep_len, threads, overrides=""
     if t < 0:
         raise OracleError(L.oracle_last_error().decode() or "oracle batch failed")
     return t, out
+
+
+def uniform(seed, key1, stream, index):
+    L = lib()
+    L.oracle_uniforms.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_ulonglong,
+                                  ctypes.c_int, ctypes.c_void_p]
+    out = np.zeros(1)
+    L.oracle_uniforms(seed, key1, stream, index, 1, out.ctypes.data)
+    return float(out[0])
+
+
+def set_window(rep, tag, min_op, max_op):
+    L = lib()
+    L.oracle_set_window.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
+    if L.oracle_set_window(rep.h, tag.encode(), min_op, max_op) != 0:
+        raise OracleError(L.oracle_last_error().decode())
