@@ -165,6 +165,20 @@ ldo_status ldo_us_get_biases(ldo_engine* e, double* out, int n_windows, int grid
 /* Window held by each replica, and the grid length. */
 ldo_status ldo_us_get_windows(ldo_engine* e, int32_t* window_of_replica, int n, int* grid_len);
 
+/* No counterpart in the reference.  Status of every replica without
+ * allocating: for a caller that may not allocate device memory at this point
+ * (its own pool allocator owns all device memory, or its step loop must not
+ * stall the device on cudaMalloc/cudaFree).  Writes each replica's status
+ * (an ldo_status code) to status_of_replica[n] (may be NULL), the largest to
+ * *worst and the number of nonzero ones to *n_bad; n must equal the replica
+ * count and be at most 65536 (LDO_EINVAL otherwise).  Its scratch is a fixed
+ * 256 KiB device array of the library, shared by every call: the first call
+ * on a device looks up its address, so make that first call before any stream
+ * capture, and do not let two calls overlap on the GPU (they race on the
+ * array).  Returns after the results are in host memory. */
+ldo_status ldo_replica_status_noalloc(ldo_engine* e, int32_t* status_of_replica, int n, int32_t* worst,
+                                      int32_t* n_bad);
+
 /* Host-only helpers (no GPU needed). */
 
 /* Reduced hybridisation enthalpy H/(RT) and entropy S/R of a fully paired

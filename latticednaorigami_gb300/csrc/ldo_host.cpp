@@ -1343,6 +1343,43 @@ ldo_status ldo_us_get_windows(ldo_engine* e, int32_t* window_of_replica, int n, 
     });
 }
 
+// Status read-out for callers that may not allocate device memory (a program
+// whose pool allocator owns all device memory, a step loop that must not stall
+// the device on cudaMalloc/cudaFree).  The scratch is a fixed device array of
+// the library, found on the first call on a device; nothing is allocated on
+// the success path, on the device or the host.
+ldo_status ldo_replica_status_noalloc(ldo_engine* e, int32_t* status_of_replica, int n, int32_t* worst,
+                                      int32_t* n_bad) {
+    if (!e || !worst || !n_bad) return LDO_EINVAL;
+    if (n != e->n_rep) {
+        e->err = "ldo_replica_status_noalloc: n must equal the engine's replica count";
+        return LDO_EINVAL;
+    }
+    if (n > LDO_NOALLOC_MAX_REPLICAS) {
+        e->err = "ldo_replica_status_noalloc: more replicas than the fixed status scratch holds (limit 65536)";
+        return LDO_EINVAL;
+    }
+    // The scratch address is per device: make the engine's device current.
+    cudaPointerAttributes attr {};
+    cudaError_t err = cudaPointerGetAttributes(&attr, e->d_arena.p);
+    int prev = 0;
+    if (err == cudaSuccess) err = cudaGetDevice(&prev);
+    if (err == cudaSuccess && attr.device != prev) err = cudaSetDevice(attr.device);
+    if (err == cudaSuccess) {
+        err = ldo_status_noalloc(e->d_arena.p, e->lay.bytes, e->lay.o_hdr, n, e->stream, status_of_replica, worst,
+                                 n_bad);
+        if (attr.device != prev) {
+            cudaError_t back = cudaSetDevice(prev);
+            if (err == cudaSuccess) err = back;
+        }
+    }
+    if (err != cudaSuccess) {
+        e->err = std::string("ldo_replica_status_noalloc: ") + cudaGetErrorString(err);
+        return LDO_ECUDA;
+    }
+    return LDO_OK;
+}
+
 ldo_status ldo_set_window(ldo_engine* e, const char* tag, int replica, int min_op, int max_op) {
     if (!e || !tag || replica < 0 || replica >= e->n_rep) return LDO_EINVAL;
     return guard(e, [&]() {

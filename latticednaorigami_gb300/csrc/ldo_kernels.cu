@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "ldo_engine.cuh"
 #include "ldo_kernels.h"
 
@@ -242,4 +244,89 @@ cudaError_t ldo_launch_status(const unsigned char* arena, int bytes, int o_hdr, 
     int blocks = (n_rep + threads - 1) / threads;
     ldo_status_kernel<<<blocks, threads, 0, stream>>>(arena, bytes, o_hdr, n_rep, d_out);
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free status read-out.
+//
+// Some callers may not allocate device memory when they ask for the replicas'
+// status: a host program that hands all device memory to its own pool
+// allocator (a cudaMalloc outside the pool breaks its budget and its
+// accounting), and a step loop that must not stall the device (cudaMalloc and
+// cudaFree can synchronise the whole device and wait on other streams' work).
+// This variant of ldo_status_kernel therefore keeps its scratch in a fixed
+// device array that every GPU loading the library holds until the process
+// exits: [0] largest status code, [1] number of replicas with a nonzero
+// status (both must start at zero and are cleared by every call), then one
+// status word per replica (overwritten by every call).  256 KiB + 8 bytes.
+static __device__ __align__(256) int g_status_scratch[2 + LDO_NOALLOC_MAX_REPLICAS];
+
+namespace {
+
+__global__ void ldo_status_gather_kernel(const unsigned char* arena, int bytes, int o_hdr, int n_rep,
+                                         int* scratch) {
+    int rep = blockIdx.x * blockDim.x + threadIdx.x;
+    if (rep >= n_rep) return;
+    const LdoHdr* h = reinterpret_cast<const LdoHdr*>(arena + (size_t)rep * bytes + o_hdr);
+    int s = h->status;
+    scratch[2 + rep] = s;
+    if (s != 0) {
+        atomicMax(&scratch[0], s);
+        atomicAdd(&scratch[1], 1);
+    }
+}
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_lock;
+int* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_status_scratch on the current device.  In host code the
+// array's name is only a host-side stand-in, so the address must come from
+// cudaGetSymbolAddress, called once per device with that device current.
+cudaError_t scratch_on_current_device(int** out) {
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return err;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> hold(g_scratch_lock);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        err = cudaGetSymbolAddress(&p, g_status_scratch);
+        if (err != cudaSuccess) return err;
+        g_scratch_ptr[dev] = static_cast<int*>(p);
+    }
+    *out = g_scratch_ptr[dev];
+    return cudaSuccess;
+}
+
+} // namespace
+
+cudaError_t ldo_status_noalloc(const unsigned char* arena, int bytes, int o_hdr, int n_rep, cudaStream_t stream,
+                               int* status_of_replica, int* worst, int* n_bad) {
+    if (n_rep < 0 || n_rep > LDO_NOALLOC_MAX_REPLICAS) return cudaErrorInvalidValue;
+    int* scratch = nullptr;
+    cudaError_t err = scratch_on_current_device(&scratch);
+    if (err != cudaSuccess) return err;
+    err = cudaMemsetAsync(scratch, 0, 2 * sizeof(int), stream);
+    if (err != cudaSuccess) return err;
+    if (n_rep > 0) {
+        int threads = 256;
+        int blocks = (n_rep + threads - 1) / threads;
+        ldo_status_gather_kernel<<<blocks, threads, 0, stream>>>(arena, bytes, o_hdr, n_rep, scratch);
+        err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+    }
+    int cells[2] = {0, 0};
+    err = cudaMemcpyAsync(cells, scratch, sizeof(cells), cudaMemcpyDeviceToHost, stream);
+    if (err != cudaSuccess) return err;
+    if (status_of_replica && n_rep > 0) {
+        err = cudaMemcpyAsync(status_of_replica, scratch + 2, (size_t)n_rep * sizeof(int), cudaMemcpyDeviceToHost,
+                              stream);
+        if (err != cudaSuccess) return err;
+    }
+    err = cudaStreamSynchronize(stream);
+    if (err != cudaSuccess) return err;
+    *worst = cells[0];
+    *n_bad = cells[1];
+    return cudaSuccess;
 }

@@ -64,3 +64,14 @@ struct LdoPT {
     int swap_i;
 };
 cudaError_t ldo_launch_pt_swap(const LdoPT& P, cudaStream_t stream);
+
+// Allocation-free status read-out.  The reduction cells and the per-replica
+// copy live in a fixed device array inside the library instead of engine
+// buffers, so the call allocates no memory.  At most LDO_NOALLOC_MAX_REPLICAS
+// replicas.  The first call on a device looks up the array's device address
+// (once per device, under a lock).  Every call uses the same array: calls
+// whose work overlaps on the GPU race.  Copies the results to host memory and
+// synchronises `stream` before returning.
+enum { LDO_NOALLOC_MAX_REPLICAS = 65536 };
+cudaError_t ldo_status_noalloc(const unsigned char* arena, int bytes, int o_hdr, int n_rep, cudaStream_t stream,
+                               int* status_of_replica, int* worst, int* n_bad);

@@ -19,7 +19,7 @@ EXPORTS = [
     "ldo_set_controls", "ldo_run", "ldo_run_sweeps", "ldo_state_bytes", "ldo_get_observables", "ldo_get_config", "ldo_set_sampling",
     "ldo_get_samples", "ldo_set_trace", "ldo_get_trace", "ldo_get_move_stats", "ldo_set_grid_bias",
     "ldo_set_window", "ldo_pt_run", "ldo_pt_get_permutation", "ldo_pt_get_stats", "ldo_nn_duplex_thermo",
-    "ldo_energy_tables", "ldo_us_run", "ldo_us_get_biases", "ldo_us_get_windows",
+    "ldo_energy_tables", "ldo_us_run", "ldo_us_get_biases", "ldo_us_get_windows", "ldo_replica_status_noalloc",
 ]
 
 
@@ -79,6 +79,8 @@ def load_library(path=None):
     lib.ldo_us_run.argtypes = [vp, ctypes.c_char_p, ip, ctypes.c_int64, ctypes.c_int64, ctypes.c_double, ip, dp]
     lib.ldo_us_get_biases.argtypes = [vp, dp, ip, ip]
     lib.ldo_us_get_windows.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ip, ctypes.POINTER(ctypes.c_int)]
+    i32p = ctypes.POINTER(ctypes.c_int32)
+    lib.ldo_replica_status_noalloc.argtypes = [vp, i32p, ip, i32p, i32p]
     lib.ldo_nn_duplex_thermo.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, dp, dp]
     lib.ldo_energy_tables.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
                                       dp, dp, dp, dp, dp, ip]
