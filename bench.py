@@ -112,40 +112,49 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-CPU_REPS_PER_SIZE = 64
-CPU_BURN_SWEEPS = 300
-CPU_SWEEPS = 1500
+CPU_REPS_PER_SIZE = 128
 
 
-def cpu_effective_rate(files, cores):
+def replica_temps():
+    """T ~ U[320, 350] K per replica (seeded); replica r has scaffold size
+    SIZES[r // (N_REP / 4)]."""
+    return np.random.default_rng(0).uniform(320.0, 350.0, N_REP)
+
+
+def cpu_effective_rate(files, cores, burn_sweeps, rec_sweeps):
     """The oracle port on all host cores over a bounded sample of the same
-    workload (64 replicas of each scaffold size, 300 burn-in + 1500 recorded
-    sweeps), with tau_int estimated from its own samples by the same
-    estimator.  Returns (effective samples/s, sweeps/s, median tau)."""
+    workload: CPU_REPS_PER_SIZE replicas of each scaffold size at the
+    temperatures of the first replicas of that size in the GPU run, the same
+    burn-in and recorded sweeps as the GPU run, tau_int estimated from its own
+    samples by the same estimator.  Only the recorded sweeps are timed
+    (pro rata).  Returns (effective samples/s, sweeps/s, median tau)."""
     from oracle_lib import run_batch_sampled
     from latticednaorigami_gb300.analysis import effective_samples
+    temps = replica_temps()
+    per = N_REP // len(SIZES)
     ess_total, t_total, sweeps_total = 0.0, 0.0, 0.0
     taus = []
     for i, f in enumerate(files):
         n = SIZES[i]
-        t, smp = run_batch_sampled(f, 0, CPU_REPS_PER_SIZE, CPU_BURN_SWEEPS + CPU_SWEEPS, n, cores)
-        rec = smp[:, CPU_BURN_SWEEPS:]
+        tt = temps[i * per:i * per + CPU_REPS_PER_SIZE]
+        t, smp = run_batch_sampled(f, 0, CPU_REPS_PER_SIZE, burn_sweeps + rec_sweeps, n, cores, temps=tt)
+        rec = smp[:, burn_sweeps:]
         ess, tau = effective_samples(list(rec))
-        frac = CPU_SWEEPS / float(CPU_BURN_SWEEPS + CPU_SWEEPS)
+        frac = rec_sweeps / float(burn_sweeps + rec_sweeps)
         ess_total += ess
         t_total += t * frac
-        sweeps_total += CPU_REPS_PER_SIZE * CPU_SWEEPS
+        sweeps_total += CPU_REPS_PER_SIZE * rec_sweeps
         if tau is not None:
             taus.append(tau)
     return ess_total / t_total, sweeps_total / t_total, (float(np.median(taus)) if taus else None)
 
 
-def cpu_baseline(files):
+def cpu_baseline(files, burn_sweeps, rec_sweeps):
     cores = os.cpu_count() or 1
-    rate, sweeps_per_s, tau = cpu_effective_rate(files, cores)
+    rate, sweeps_per_s, tau = cpu_effective_rate(files, cores, burn_sweeps, rec_sweeps)
     return {"value": rate, "unit": "effective samples/s", "cores": cores, "kind": "port",
-            "sample": "%d replicas of each scaffold size x %d recorded sweeps (after %d burn-in) on %d threads"
-                      % (CPU_REPS_PER_SIZE, CPU_SWEEPS, CPU_BURN_SWEEPS, cores),
+            "sample": "%d replicas of each scaffold size (GPU-run temperatures) x %d recorded sweeps after %d "
+                      "burn-in, %d threads" % (CPU_REPS_PER_SIZE, rec_sweeps, burn_sweeps, cores),
             "sweeps_per_s": sweeps_per_s, "tau_int_median": tau}
 
 
@@ -158,10 +167,11 @@ def run_reference_arm(args):
     from oracle_lib import run_batch
     for _ in range(args.warmup):
         run_batch(files[0], 0, cores, 20 * SIZES[0], cores)
+    burn, rec = args.warmup * SWEEPS_PER_STEP, args.steps * SWEEPS_PER_STEP
     rates, sps, taus, times = [], [], [], []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        r, s_, tau = cpu_effective_rate(files, cores)
+        r, s_, tau = cpu_effective_rate(files, cores, burn, rec)
         times.append(time.perf_counter() - t0)
         rates.append(r)
         sps.append(s_)
@@ -174,8 +184,8 @@ def run_reference_arm(args):
             "config": {"workload": "c2: constant-T chains, scaffolds 8/12/16/24, uniform hyb, T~U[320,350] K; "
                                    "bounded CPU sample per step"},
             "cpu_baseline": {"value": value, "unit": "effective samples/s", "cores": cores, "kind": "port",
-                             "sample": "%d replicas of each scaffold size x %d recorded sweeps per step"
-                                       % (CPU_REPS_PER_SIZE, CPU_SWEEPS)},
+                             "sample": "%d replicas of each scaffold size (GPU-run temperatures) x %d recorded "
+                                       "sweeps after %d burn-in per step" % (CPU_REPS_PER_SIZE, rec, burn)},
             "e2e": {"value": value, "unit": "effective samples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "sweeps_per_s": float(np.mean(sps)), "tau_int_median": taus[-1]}
@@ -201,8 +211,7 @@ def main():
     files = write_c2(tmp)
     per = N_REP // len(SIZES)
     sys_of = np.repeat(np.arange(len(SIZES)), per)
-    rng = np.random.default_rng(0)
-    temps = rng.uniform(320.0, 350.0, N_REP)
+    temps = replica_temps()
     eng = Engine(files, n_replicas=N_REP, seed=0, sys_of_replica=sys_of.tolist(), overrides="")
     eng.set_controls(temps=temps)
     ns_of = np.array(SIZES)[sys_of]
@@ -279,7 +288,7 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind},
             "clocks": clk}
     if not args.no_cpu and rank == 0:
-        line["cpu_baseline"] = cpu_baseline(files)
+        line["cpu_baseline"] = cpu_baseline(files, args.warmup * SWEEPS_PER_STEP, total_sweeps)
     print(json.dumps(line))
 
 

@@ -411,11 +411,11 @@ double oracle_run_batch(const char* inp_path, const char* overrides, uint32_t se
 // each `sweeps` sweeps of sweep_len steps; after every sweep the number of
 // fully bound domain pairs goes to out[r * sweeps + k].  Returns wall seconds.
 double oracle_run_batch_sampled(const char* inp_path, const char* overrides, uint32_t seed0, int n_rep,
-                                long long sweeps, int sweep_len, int threads, short* out) {
+                                long long sweeps, int sweep_len, int threads, const double* temps, short* out) {
     std::vector<Replica*> reps(n_rep, nullptr);
     for (int i = 0; i < n_rep; ++i) {
         reps[i] = build(inp_path, overrides, seed0, (uint32_t)i);
-        if (!reps[i]) {
+        if (!reps[i] || (temps && oracle_update_temp(reps[i], temps[i], 1.0) != 0)) {
             for (auto* r : reps) delete r;
             return -1;
         }

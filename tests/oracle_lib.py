@@ -130,16 +130,23 @@ def swap_uniform(seed, ladder, index):
     return float(out[0])
 
 
-def run_batch_sampled(inp, seed, n_rep, sweeps, sweep_len, threads, overrides=""):
+def run_batch_sampled(inp, seed, n_rep, sweeps, sweep_len, threads, overrides="", temps=None):
     """CPU baseline with one numfulldomains sample per replica per sweep:
-    returns (wall seconds, samples[n_rep, sweeps])."""
+    returns (wall seconds, samples[n_rep, sweeps]).  temps[n_rep], if given,
+    sets each replica's temperature before the timed run."""
     L = lib()
     L.oracle_run_batch_sampled.restype = ctypes.c_double
     L.oracle_run_batch_sampled.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_int,
-                                           ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+                                           ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.c_void_p]
     out = np.zeros((n_rep, sweeps), np.int16)
+    tp = None
+    if temps is not None:
+        temps = np.ascontiguousarray(temps, np.float64)
+        assert len(temps) == n_rep
+        tp = temps.ctypes.data
     t = L.oracle_run_batch_sampled(os.fsencode(inp), overrides.encode(), seed, n_rep, sweeps, sweep_len, threads,
-                                   out.ctypes.data)
+                                   tp, out.ctypes.data)
     if t < 0:
         raise OracleError(L.oracle_last_error().decode() or "oracle batch failed")
     return t, out
