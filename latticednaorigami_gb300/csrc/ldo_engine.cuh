@@ -182,7 +182,18 @@ struct Scratch {
     // bound domains of the selected staple (new, old)
     int n_bd;
     int bd_new[LDO_MAX_LEN], bd_old[LDO_MAX_LEN];
+    int cb_g;               // growth point index of the CB move's new configuration
 };
+
+// Commands from a replica's move phases to its warp, which copies the state
+// to / from snapshots in global memory between phases (CMD_SNAP(k): state ->
+// snapshot k; CMD_REST(k): snapshot k -> state; the snapshot is taken first
+// unless CMD_REST_FIRST; CMD_MORE: call step_resume afterwards).
+#define CMD_SNAP(k) ((k) + 1)
+#define CMD_REST(k) (((k) + 1) << 4)
+enum : int { CMD_MORE = 1 << 8, CMD_REST_FIRST = 1 << 9, CMD_STOP = 1 << 10 };
+enum : int { PH_POST = 1, PH_CB2 = 2, PH_CB3 = 3 };
+constexpr int N_SNAPSHOTS = 3;
 
 // Scratch of the FourBody evaluation.
 struct FBState {
@@ -248,6 +259,13 @@ struct Rep : public LdoState<C> {
     int insertion_sites;
     bool staple_bound;
     double log6, log3;
+    // step state machine (step_begin / step_resume)
+    bool dirty;             // the move may have changed the state
+    bool recalc;            // update_move_params + calc_move after the restore
+    int phase;              // PH_* of the interrupted move
+    int cur_mv;
+    long long cur_s;
+    int cb_cs;
 
     // Accessors used by the FourBody traversal.
     __device__ __forceinline__ int gst(int i) const { return st[i]; }
@@ -1423,6 +1441,8 @@ struct Rep : public LdoState<C> {
         w_new_bias = 1;
         new_modifier = 1;
         regrow_old = false;
+        dirty = true;
+        phase = 0;
     }
 
     __device__ __noinline__ void reset_origami() {   // src/movetypes.cpp:53
@@ -1603,8 +1623,10 @@ struct Rep : public LdoState<C> {
     __device__ __noinline__ bool insert_staple() {
         int S = sys->n_types - 1;
         int type = rng.uniform_int(1, S);
-        if (hdr.num_staples == sys->max_total_staples) return false;
-        if (type_count[type] == sys->max_type_staples) return false;
+        if (hdr.num_staples == sys->max_total_staples || type_count[type] == sys->max_type_staples) {
+            dirty = false;
+            return false;
+        }
         int cs = add_chain(type);
         if (cs < 0) return false;
         if (mean_field) delta_e += log6;
@@ -1647,6 +1669,7 @@ struct Rep : public LdoState<C> {
         int n = type_count[type];
         if (n == 0) {
             rejected = true;
+            dirty = false;
             return false;
         }
         int which = rng.uniform_int(0, n - 1);
@@ -1663,7 +1686,10 @@ struct Rep : public LdoState<C> {
             fail(LDO_RS_INVARIANT);
             return false;
         }
-        if (staple_is_connector(cs)) return false;
+        if (staple_is_connector(cs)) {
+            dirty = false;
+            return false;
+        }
         int len = chain_len(cs);
         #pragma unroll 1
         for (int d = 0; d < len; ++d)
@@ -1699,9 +1725,11 @@ struct Rep : public LdoState<C> {
 
     // MetStapleRegrowthMCMovetype::internal_attempt_move (src/met_movetypes.cpp:470)
     __device__ __noinline__ bool met_regrowth() {
+        dirty = false;
         if (hdr.num_staples == 0) return false;
         int cs = pick_staple_chain();
         if (staple_is_connector(cs)) return false;
+        dirty = true;
         find_bound_domains(cs);
         if (bad()) return false;
         int g = rng.uniform_int(0, m.n_bd - 1);
@@ -1818,17 +1846,32 @@ struct Rep : public LdoState<C> {
     }
 
     // CBStapleRegrowthMCMovetype::internal_attempt_move (src/cb_movetypes.cpp:292)
-    __device__ __noinline__ bool cb_regrowth() {
-        if (hdr.num_staples == 0) return false;
+    // in three phases around two snapshots: 1 = the staple unassigned, 2 = the
+    // staple in its new configuration.  The reference's second
+    // unassign_domains (before regrowing the old configuration, :215) becomes
+    // a restore of snapshot 1, and its reset_origami on acceptance a restore
+    // of snapshot 2: the same lattice states, reached without re-evaluating
+    // the binding energies.
+    __device__ __noinline__ int cb_begin() {
+        dirty = false;
+        if (hdr.num_staples == 0) return finish_move(false, 0);
         int cs = pick_staple_chain();
-        if (staple_is_connector(cs)) return false;
+        if (staple_is_connector(cs)) return finish_move(false, 0);
+        dirty = true;
         find_bound_domains(cs);
-        if (bad()) return false;
+        if (bad()) return finish_move(false, 0);
         w_bias *= (double)(unsigned long long)m.n_bd;
         int g = rng.uniform_int(0, m.n_bd - 1);
         unassign_domains(cs);
+        cb_cs = cs;
+        m.cb_g = g;
+        phase = PH_CB2;
+        return CMD_SNAP(1) | CMD_MORE;
+    }
+    __device__ __noinline__ int cb_mid() {
+        int cs = cb_cs, g = m.cb_g;
         cb_set_gp_and_grow(m.bd_new[g], m.bd_old[g], cs);
-        if (rejected || bad()) return false;
+        if (rejected || bad()) return finish_move(false, 0);
         w_bias /= num_bound_staple_domains(cs);
         update_move_params();
         double tb = calc_move();
@@ -1847,22 +1890,19 @@ struct Rep : public LdoState<C> {
         }
         m.n_mod = 0;
         m.n_asg = 0;
-        g = rng.uniform_int(0, m.n_bd - 1);
-        unassign_domains(cs);
+        phase = PH_CB3;
+        return CMD_SNAP(2) | CMD_REST(1) | CMD_MORE;
+    }
+    __device__ __noinline__ int cb_end() {
+        int cs = cb_cs;
+        int g = rng.uniform_int(0, m.n_bd - 1);
         cb_set_gp_and_grow(m.bd_new[g], m.bd_old[g], cs);
-        if (bad()) return false;
+        if (bad()) return finish_move(false, 0);
         modifier = new_modifier;
         // test_cb_acceptance (:182)
         double ratio = w_new_bias / w_bias;
-        if (test_acceptance(ratio)) {
-            reset_origami();
-            update_move_params();
-            calc_move();
-            return true;
-        }
-        m.n_mod = 0;
-        m.n_asg = 0;
-        return false;
+        bool acc = test_acceptance(ratio);
+        return finish_move(acc, acc ? 2 : 0);
     }
 
     // OrientationRotationMCMovetype::internal_attempt_move (src/orientation_movetype.cpp:30)
@@ -1879,11 +1919,9 @@ struct Rep : public LdoState<C> {
             V3 p = pos(dom);
             de += set_domain_config(bd, p, o_new ^ 1);
             if (!hdr.violated) acc = test_acceptance(dexp(-de));
-            if (!acc) {
-                unassign_domain(bd);
-                set_domain_orientation(dom, o_old);
-                set_checked(bd, p, o_old ^ 1);
-            }
+            // a rejection (reference: unassign, old orientation, set_checked
+            // of the partner, :55-62) restores the move's snapshot
+            (void)o_old;
         }
         else {
             set_domain_orientation(dom, o_new);
@@ -1892,8 +1930,16 @@ struct Rep : public LdoState<C> {
         return acc;
     }
 
-    // GCMCSimulation::simulate, one step (src/simulation.cpp:575-619)
-    __device__ __noinline__ void step(long long s) {
+    // GCMCSimulation::simulate, one step (src/simulation.cpp:575-619), as a
+    // state machine: step_begin runs the move until it needs the warp to copy
+    // snapshots, step_resume continues it, and each returns the next CMD_*
+    // (0 = step done).  Snapshot 0 always holds the state at the start of the
+    // move.  A rejected move is undone by restoring it instead of the
+    // reference's reset_origami + update_move_params + calc_move: the same
+    // lattice state, order parameters and biases; the energy and bias totals
+    // come back exactly instead of through the reversal's roundings.
+    __device__ __noinline__ int step_begin(long long s) {
+        cur_s = s;
         double r = rng.uniform_real();
         int nm = sys->n_moves;
         int mv = 0;
@@ -1901,26 +1947,72 @@ struct Rep : public LdoState<C> {
         while (mv < nm && !(r < sys->move_cum[mv])) ++mv;
         if (mv == nm) {
             fail(LDO_RS_INVARIANT);
-            return;
+            return 0;
         }
+        cur_mv = mv;
         reset_internal();
         bool acc = false;
         switch (sys->move_kind[mv]) {
         case LDO_MV_ORIENT: acc = orientation_rotation(); break;
         case LDO_MV_MET_EXCHANGE: acc = met_exchange(); break;
         case LDO_MV_MET_REGROWTH: acc = met_regrowth(); break;
-        case LDO_MV_CB_REGROWTH: acc = cb_regrowth(); break;
+        case LDO_MV_CB_REGROWTH: return cb_begin();
         }
-        if (bad()) return;
-        mstat[2 * mv] += 1;
-        if (acc) mstat[2 * mv + 1] += 1;
+        return finish_move(acc, 0);
+    }
+
+    // Move statistics, then the snapshot work: an accepted move refreshes
+    // snapshot 0 (CB: restore snapshot `from` first), a rejected move that
+    // changed anything restores it.
+    __device__ __noinline__ int finish_move(bool acc, int from) {
+        if (bad()) return 0;
+        mstat[2 * cur_mv] += 1;
+        int cmd = 0;
+        recalc = false;
+        if (acc) {
+            mstat[2 * cur_mv + 1] += 1;
+            cmd = from ? (CMD_REST(from) | CMD_SNAP(0) | CMD_REST_FIRST) : CMD_SNAP(0);
+        }
         else {
-            reset_origami();
+            // With bias functions the reference's trailing update_move_params
+            // + calc_move also fold in a grid or window change made since
+            // the last calc_move, so they still run after the restore.
+            if (dirty) cmd = CMD_REST(0);
+            if (sys->n_biases > 0) {
+                if (dirty) recalc = true;
+                else {
+                    update_move_params();
+                    calc_move();
+                }
+            }
+        }
+        long long s = cur_s;
+        if (recalc || (sys->centering_freq != 0 && s % sys->centering_freq == 0) ||
+            (sys->constraint_check_freq != 0 && s % sys->constraint_check_freq == 0)) {
+            phase = PH_POST;
+            cmd |= CMD_MORE;
+        }
+        return cmd;
+    }
+
+    __device__ __noinline__ int step_resume() {
+        if (bad()) return 0;
+        if (phase == PH_CB2) return cb_mid();
+        if (phase == PH_CB3) return cb_end();
+        phase = 0;
+        if (recalc) {
+            recalc = false;
             update_move_params();
             calc_move();
         }
-        if (sys->centering_freq != 0 && s % sys->centering_freq == 0) center(sys->centering_domain);
+        long long s = cur_s;
+        int cmd = 0;
+        if (sys->centering_freq != 0 && s % sys->centering_freq == 0) {
+            center(sys->centering_domain);
+            cmd = CMD_SNAP(0);
+        }
         if (sys->constraint_check_freq != 0 && s % sys->constraint_check_freq == 0) check_all_constraints();
+        return cmd;
     }
 };
 

@@ -335,6 +335,7 @@ struct ldo_engine {
     DevBuf<LdoRepCtl> d_ctl;
     DevBuf<double> d_grid;
     DevBuf<unsigned char> d_arena;
+    DevBuf<unsigned char> d_snap;   // move snapshots (run mode)
     DevBuf<int> d_status;
     DevBuf<int16_t> d_samples;
     DevBuf<double> d_trace;
@@ -433,6 +434,7 @@ struct ldo_engine {
         L.ctl = d_ctl.p;
         L.grid = d_grid.p;
         L.arena = d_arena.p;
+        L.snap = d_snap.p;
         L.lay = lay;
         L.n_rep = n_rep;
         L.warps_per_block = wpb;
@@ -643,6 +645,7 @@ struct ldo_engine {
         upload_tables();
         d_status.alloc(1);
         init_arena();
+        d_snap.alloc((size_t)n_rep * LDO_N_SNAPSHOTS * ldo_snapshot_stride(lay.bytes));
         LdoLaunch L = launch_params(LDO_MODE_INIT, 0);
         CU(ldo_launch_mc(L, stream));
         CU(cudaStreamSynchronize(stream));

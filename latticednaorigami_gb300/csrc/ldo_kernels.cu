@@ -53,7 +53,47 @@ __host__ __device__ constexpr int rep_bytes() { return (int)((sizeof(ldo::Rep<C>
 template <class C>
 __host__ __device__ constexpr int warp_bytes() { return rep_bytes<C>(); }
 
+// Bytes of the replica state that snapshots hold (everything before the move
+// statistics), and the distance between a replica's snapshots.
+template <class C>
+__host__ __device__ constexpr int snap_bytes() { return (int)offsetof(LdoState<C>, mstat); }
+template <class C>
+__host__ __device__ constexpr size_t snap_stride() { return (sizeof(LdoState<C>) + 255) / 256 * 256; }
+static_assert(ldo::N_SNAPSHOTS == LDO_N_SNAPSHOTS, "snapshot count shared with the host");
+
+// The warp's part of a step: the copies a move phase asked for (cmd), with
+// the bookkeeping fields of the header kept across a restore.
+template <class C>
+__device__ __forceinline__ void snapshot_ops(int cmd, ldo::Rep<C>* R, unsigned char* base, unsigned char* snap,
+                                             int lane) {
+    static_assert(snap_bytes<C>() % 16 == 0, "snapshot region must be whole 16-byte vectors");
+    int sn = (cmd & 15) - 1;
+    int rs = ((cmd >> 4) & 15) - 1;
+    LdoHdr& h = R->hdr;
+    long long steps_done = 0;
+    int sample_count = 0, status = 0, tab = 0;
+    if (lane == 0 && rs >= 0) {
+        steps_done = h.steps_done;
+        sample_count = h.sample_count;
+        status = h.status;
+        tab = h.tab;
+    }
+    __syncwarp();
+    if (sn >= 0 && !(cmd & ldo::CMD_REST_FIRST)) warp_copy16(snap + (size_t)sn * snap_stride<C>(), base, snap_bytes<C>(), lane);
+    if (rs >= 0) warp_copy16(base, snap + (size_t)rs * snap_stride<C>(), snap_bytes<C>(), lane);
+    if (sn >= 0 && (cmd & ldo::CMD_REST_FIRST)) warp_copy16(snap + (size_t)sn * snap_stride<C>(), base, snap_bytes<C>(), lane);
+    __syncwarp();
+    if (lane == 0 && rs >= 0) {
+        h.steps_done = steps_done;
+        h.sample_count = sample_count;
+        h.status = status;
+        h.tab = tab;
+    }
+}
+
 // Shared memory per warp: Rep (replica state followed by the working fields).
+// Lane 0 runs the moves; the whole warp loads and stores the state and
+// copies the move snapshots (global memory, L.snap).
 template <class C>
 __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -66,10 +106,14 @@ __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
     unsigned char* gbase = L.arena + (size_t)rep * sizeof(LdoState<C>);
     warp_copy16(base, gbase, (int)sizeof(LdoState<C>), lane);
     __syncwarp();
+    LdoHdr& h = R->hdr;
+    long long nsteps = 0, sint = 0;
+    double* tr = nullptr;
+    bool live = false;
     if (lane == 0) {
         bind_rep<C>(*R, L, rep);
-        LdoHdr& h = R->hdr;
-        if (h.status == 0) {
+        live = h.status == 0;
+        if (live) {
             if (L.mode == LDO_MODE_INIT) {
                 R->set_all_current();
                 R->init_biases();
@@ -90,47 +134,68 @@ __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
                     R->recompute_energy();
                     h.tab = R->ctl->tab;
                 }
-                double* tr = (rep < L.n_trace) ? L.trace + (size_t)rep * L.trace_max * 8 : nullptr;
+                tr = (rep < L.n_trace) ? L.trace + (size_t)rep * L.trace_max * 8 : nullptr;
                 long long unit = L.sweep_units ? (long long)R->ns : 1ll;
-                long long nsteps = L.n_steps * unit;
-                long long sint = (long long)L.sample_interval * unit;
-                for (long long k = 0; k < nsteps; ++k) {
-                    if (R->bad()) break;
-                    long long s = h.steps_done + 1;
-                    R->step(s);
-                    h.steps_done = s;
-                    if (tr && k < L.trace_max) {
-                        double* t = tr + 8 * k;
-                        t[0] = (double)s;
-                        t[1] = h.energy;
-                        t[2] = h.num_staples;
-                        t[3] = h.num_fully;
-                        t[4] = h.num_bound;
-                        t[5] = h.num_stacked;
-                        t[6] = h.move_bias * R->c_bias_mult;
-                        t[7] = (double)R->rng.draws;
-                    }
-                    if (L.us_hist) {
-                        int oq = R->sys->bias_op[L.us_bias];
-                        if (R->op[2 * oq + 1]) {
-                            int x = R->op[2 * oq];
-                            if (x >= 0 && x < L.us_len) L.us_hist[(size_t)L.us_window[rep] * L.us_len + x] += 1;
-                        }
-                    }
-                    if (sint > 0 && s % sint == 0) {
-                        int c = h.sample_count;
-                        if (c < L.sample_cap) {
-                            int16_t* o = L.samples + ((size_t)rep * L.sample_cap + c) * 2;
-                            o[0] = (int16_t)h.num_fully;
-                            o[1] = (int16_t)h.num_staples;
-                        }
-                        h.sample_count = c + 1;
+                nsteps = L.n_steps * unit;
+                sint = (long long)L.sample_interval * unit;
+            }
+        }
+    }
+    nsteps = __shfl_sync(0xffffffffu, nsteps, 0);
+    if (nsteps > 0) {
+        unsigned char* snap = L.snap + (size_t)rep * ldo::N_SNAPSHOTS * snap_stride<C>();
+        __syncwarp();
+        warp_copy16(snap, base, snap_bytes<C>(), lane);   // snapshot 0: state at the start of the move
+        for (long long k = 0; k < nsteps; ++k) {
+            int cmd = 0;
+            if (lane == 0) cmd = R->bad() ? ldo::CMD_STOP : R->step_begin(h.steps_done + 1);
+            cmd = __shfl_sync(0xffffffffu, cmd, 0);
+            if (cmd & ldo::CMD_STOP) break;
+            // a step has at most four phases (CB: three, then the post-move work)
+            #pragma unroll 1
+            for (int guard = 0; guard < 8; ++guard) {
+                if (cmd & 0xff) snapshot_ops<C>(cmd, R, base, snap, lane);
+                if (!(cmd & ldo::CMD_MORE)) break;
+                if (lane == 0) cmd = R->step_resume();
+                cmd = __shfl_sync(0xffffffffu, cmd, 0);
+            }
+            if (lane == 0) {
+                if (cmd & ldo::CMD_MORE) R->fail(LDO_RS_INVARIANT);
+                long long s = h.steps_done + 1;
+                h.steps_done = s;
+                if (tr && k < L.trace_max) {
+                    double* t = tr + 8 * k;
+                    t[0] = (double)s;
+                    t[1] = h.energy;
+                    t[2] = h.num_staples;
+                    t[3] = h.num_fully;
+                    t[4] = h.num_bound;
+                    t[5] = h.num_stacked;
+                    t[6] = h.move_bias * R->c_bias_mult;
+                    t[7] = (double)R->rng.draws;
+                }
+                if (L.us_hist) {
+                    int oq = R->sys->bias_op[L.us_bias];
+                    if (R->op[2 * oq + 1]) {
+                        int x = R->op[2 * oq];
+                        if (x >= 0 && x < L.us_len) L.us_hist[(size_t)L.us_window[rep] * L.us_len + x] += 1;
                     }
                 }
+                if (sint > 0 && s % sint == 0) {
+                    int c = h.sample_count;
+                    if (c < L.sample_cap) {
+                        int16_t* o = L.samples + ((size_t)rep * L.sample_cap + c) * 2;
+                        o[0] = (int16_t)h.num_fully;
+                        o[1] = (int16_t)h.num_staples;
+                    }
+                    h.sample_count = c + 1;
+                }
             }
-            if (L.want_dep && !R->bad()) R->dependent_quantities();
-            h.draws = R->rng.draws;
         }
+    }
+    if (lane == 0 && live) {
+        if (L.want_dep && !R->bad()) R->dependent_quantities();
+        h.draws = R->rng.draws;
     }
     __syncwarp();
     warp_copy16(gbase, base, (int)sizeof(LdoState<C>), lane);

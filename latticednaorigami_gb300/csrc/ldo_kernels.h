@@ -14,6 +14,9 @@ struct LdoLaunch {
     const LdoRepCtl* ctl;
     const double* grid;
     unsigned char* arena;
+    // Move snapshots, LDO_N_SNAPSHOTS per replica, each ldo_snapshot_stride
+    // bytes apart (run mode).
+    unsigned char* snap;
     LdoLayout lay;
     int n_rep;
     int warps_per_block;
@@ -36,6 +39,9 @@ struct LdoLaunch {
 };
 
 cudaError_t ldo_launch_mc(const LdoLaunch& L, cudaStream_t stream);
+enum { LDO_N_SNAPSHOTS = 3 };
+// Bytes between a replica's move snapshots for a state of lay.bytes bytes.
+inline size_t ldo_snapshot_stride(int state_bytes) { return ((size_t)state_bytes + 255) / 256 * 256; }
 // Shared memory one replica's warp needs in capacity class cls.
 int ldo_warp_smem_bytes(int cls);
 cudaError_t ldo_launch_status(const unsigned char* arena, int bytes, int o_hdr, int n_rep, int* d_out,

@@ -156,13 +156,14 @@ using LdoCapL = LdoCap<320, 63, 1024>;
 enum { LDO_CLASS_S = 0, LDO_CLASS_M = 1, LDO_CLASS_L = 2 };
 
 // Persistent state of one replica: the same bytes in the global arena between
-// launches and in shared memory during a launch.
+// launches and in shared memory during a launch.  Everything before `mstat`
+// is the configuration that move snapshots save and restore; the move
+// statistics come last so that a restore leaves them alone.
 template <class C>
 struct __attribute__((aligned(16))) LdoState {
     LdoHdr hdr;
     unsigned long long hash[C::HCAP];
     double bias[C::NB];
-    long long mstat[2 * C::NMV];
     int32_t chain_c[C::KMAX + 1];
     int32_t op[2 * C::NOP];
     long long pp[C::DCAP];    // packed position x + y*2^16 + z*2^32
@@ -170,4 +171,5 @@ struct __attribute__((aligned(16))) LdoState {
     int16_t type_count[C::NT];
     uint8_t ore[C::DCAP], st[C::DCAP], scs[C::DCAP], sd[C::DCAP];
     uint8_t chain_type[C::KMAX + 1], chain_order[C::KMAX + 1], clen[C::KMAX + 1];
+    alignas(16) long long mstat[2 * C::NMV];
 };
