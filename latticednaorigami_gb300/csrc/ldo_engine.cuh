@@ -250,6 +250,8 @@ struct Rep : public LdoState<C> {
     V3 cb_pos[6];
     int cb_ore[6];
     double cb_bf[6];
+    double cb_de[6];        // probed candidates: energy change and stacked-pair change
+    int cb_stk[6];
     uint8_t dfs_stack[LDO_MAX_KMAX + 1];
     Scratch m;
     bool rejected;
@@ -294,16 +296,9 @@ struct Rep : public LdoState<C> {
     __device__ int chain_len(int cs) const { return clen[cs]; }
     __device__ int slot_of(int cs, int d) const { return cs == 0 ? d : ns + (cs - 1) * lmax + d; }
     __device__ int cidx(int i) const { return chain_c[scs[i]]; }
-    __device__ int fwd(int i) const {
-        int cs = scs[i], d = sd[i], len = chain_len(cs);
-        if (d + 1 < len) return i + 1;
-        return (cs == 0 && cyclic) ? i - (len - 1) : -1;
-    }
-    __device__ int bwd(int i) const {
-        int cs = scs[i], d = sd[i];
-        if (d > 0) return i - 1;
-        return (cs == 0 && cyclic) ? i + chain_len(cs) - 1 : -1;
-    }
+    // Chain neighbours (stored links; the scaffold's wrap when it is cyclic).
+    __device__ int fwd(int i) const { return nxt[i]; }
+    __device__ int bwd(int i) const { return prv[i]; }
     __device__ int next(int i, int incr) const {   // Domain::operator+ (src/domain.cpp:9)
         #pragma unroll 1
         while (i >= 0 && incr > 0) { i = fwd(i); --incr; }
@@ -639,14 +634,14 @@ struct Rep : public LdoState<C> {
     // check_domain_constraints for a CB trial position (src/origami_system.cpp:343):
     // the same state change and energy; the undo skips the stacking traversal
     // whose result the reference discards (internal_unassign_domain :704).
-    __device__ __noinline__ double probe_domain(int i, V3 p, int o) {
+    __device__ __noinline__ Delta probe_domain(int i, V3 p, int o) {
         Delta dc = internal_check(i, p, o);
         int occ = st[i];
         int j = bnd[i];
         if (occ == BOUND || occ == MISBOUND) {
             if (j < 0) {
                 fail(LDO_RS_INVARIANT);
-                return 0;
+                return dc;
             }
             hdr.num_bound -= 1;
             if (occ == BOUND) hdr.num_fully -= 1;
@@ -665,7 +660,23 @@ struct Rep : public LdoState<C> {
         else {
             hdr.num_unassigned--;
         }
-        return dc.e;
+        return dc;
+    }
+
+    // set_checked_domain_config for a CB trial position that probe_domain has
+    // evaluated in the same state: the energy change and stacked-pair change
+    // are the probe's (hybridisation + stacking, the same two FP64 operands in
+    // either order, plus the same mean-field term), so the stacking traversal
+    // is not repeated.
+    __device__ __noinline__ double set_checked_probed(int i, V3 p, int o, double de, int stacked) {
+        set_pos(i, p);
+        ore[i] = (uint8_t)o;
+        update_occupancies(i, p);
+        if (bad()) return 0;
+        if (st[i] == BOUND) hdr.num_stacked += stacked;
+        hdr.energy += de;
+        hdr.num_unassigned--;
+        return de;
     }
 
     // set_domain_orientation (src/origami_system.cpp:543)
@@ -1765,13 +1776,15 @@ struct Rep : public LdoState<C> {
             if (occ == UNBOUND) {
                 int ud = unbound_at(p);
                 int o = ore[ud] ^ 1;
-                double de = probe_domain(dom, p, o);
+                Delta dc = probe_domain(dom, p, o);
                 if (bad()) return;
                 if (!hdr.violated) {
                     cpos[nc] = p;
                     core[nc] = o;
+                    cb_de[nc] = dc.e;
+                    cb_stk[nc] = dc.stacked;
                     double b = 1;
-                    b *= dexp(-de);
+                    b *= dexp(-dc.e);
                     bf[nc] = b;
                     nc++;
                 }
@@ -1797,6 +1810,7 @@ struct Rep : public LdoState<C> {
         if (!regrow_old) {
             V3 p = mk(0, 0, 0);
             int o = -1;
+            int chosen = -1;
             double cum = 0;
             double r = rng.uniform_real();
             #pragma unroll 1
@@ -1805,17 +1819,29 @@ struct Rep : public LdoState<C> {
                 if (r < cum) {
                     p = cpos[n];
                     o = core[n];
+                    chosen = n;
                     break;
                 }
             }
-            if (o < 0) o = rng.uniform_int(0, 5);
-            set_checked(dom, p, o);
+            if (o < 0) {
+                o = rng.uniform_int(0, 5);
+                set_checked(dom, p, o);
+            }
+            else {
+                set_checked_probed(dom, p, o, cb_de[chosen], cb_stk[chosen]);
+            }
         }
         else {
             int n = 0;
             #pragma unroll 1
             while (n < m.n_old && m.old_slot[n] != dom) ++n;
-            set_checked(dom, m.old_pos[n], m.old_ore[n]);
+            V3 p = m.old_pos[n];
+            int o = m.old_ore[n];
+            int c = 0;
+            #pragma unroll 1
+            while (c < nc && !(core[c] == o && eq(cpos[c], p))) ++c;
+            if (c < nc) set_checked_probed(dom, p, o, cb_de[c], cb_stk[c]);
+            else set_checked(dom, p, o);
         }
         m.asg[m.n_asg++] = dom;
     }
