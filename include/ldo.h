@@ -179,6 +179,36 @@ ldo_status ldo_us_get_windows(ldo_engine* e, int32_t* window_of_replica, int n, 
 ldo_status ldo_replica_status_noalloc(ldo_engine* e, int32_t* status_of_replica, int n, int32_t* worst,
                                       int32_t* n_bad);
 
+/* Learned insertion proposal (movetype "LearnedStapleExchange"; engine
+ * extension with no counterpart in the reference, which only proposes
+ * uniformly: src/movetypes.cpp:98-120).  A network of three 256-wide GELU
+ * layers scores growth-point targets from their chain neighbourhood and the
+ * temperature; ldo_learn.h describes the input encoding.  Until trained, every
+ * unbound target weighs 1. */
+
+/* Adds every replica's current bound / unbound domains to the training counts
+ * (per network input). */
+ldo_status ldo_learn_collect(ldo_engine* e);
+ldo_status ldo_learn_reset_counts(ldo_engine* e);
+/* Training counts per network input (n = LDO_LEARN_TABLE = 524288). */
+ldo_status ldo_learn_get_counts(ldo_engine* e, float* cnt_bound, float* cnt_total, int n);
+/* Full-batch Adam (lr) on the weighted logistic loss of the counts, starting
+ * from seeded parameters the first time; then the proposal's weight table.
+ * Loss before the first and after the last step (either may be NULL). */
+ldo_status ldo_learn_train(ldo_engine* e, int iters, double lr, uint32_t seed, double* loss_first, double* loss_last);
+/* Network parameters (n = LDO_LEARN_NPARAM = 148481 floats); setting them
+ * recomputes the weight table. */
+ldo_status ldo_learn_set_params(ldo_engine* e, const float* params, int n);
+ldo_status ldo_learn_get_params(ldo_engine* e, float* params, int n);
+/* Proposal weight exp(clamped logit) of every network input (n = 524288). */
+ldo_status ldo_learn_get_table(ldo_engine* e, double* weights, int n);
+ldo_status ldo_learn_set_table(ldo_engine* e, const double* weights, int n);
+/* Loss and gradient of the network for given parameters on a batch of n
+ * network inputs with bound / total counts (no engine; the GPU kernels the
+ * trainer uses). */
+ldo_status ldo_learn_loss_grad(const float* params, const int32_t* idx, const float* cnt_bound, const float* cnt_total,
+                               int n, double* loss, float* grad);
+
 /* Host-only helpers (no GPU needed). */
 
 /* Reduced hybridisation enthalpy H/(RT) and entropy S/R of a fully paired

@@ -37,16 +37,19 @@ def build(verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     nvcc = nvcc_path()
     k_obj = os.path.join(BUILD, "ldo_kernels.o")
+    m_obj = os.path.join(BUILD, "ldo_mlp.o")
     h_obj = os.path.join(BUILD, "ldo_host.o")
     cmds = [
         [nvcc] + ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-c", os.path.join(CSRC, "ldo_kernels.cu"), "-o", k_obj],
+        [nvcc] + ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+                         "-c", os.path.join(CSRC, "ldo_mlp.cu"), "-o", m_obj],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + cuda_include(),
          "-c", os.path.join(CSRC, "ldo_host.cpp"), "-o", h_obj],
     ]
     _run_all(cmds)
     tmp = LIB + ".tmp"
-    _run_all([[nvcc] + ARCH + ["-shared", "-Xcompiler", "-fPIC", k_obj, h_obj, "-o", tmp]])
+    _run_all([[nvcc] + ARCH + ["-shared", "-Xcompiler", "-fPIC", k_obj, m_obj, h_obj, "-o", tmp]])
     os.replace(tmp, LIB)
     if verbose:
         print("built", LIB)

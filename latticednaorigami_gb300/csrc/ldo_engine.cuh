@@ -20,6 +20,7 @@
 // ns + (k-1)*lmax + d.
 #pragma once
 #include <stdint.h>
+#include "ldo_learn.h"
 #include "ldo_types.h"
 
 #ifndef LDO_DEV
@@ -235,6 +236,8 @@ struct Rep : public LdoState<C> {
     const double* bank;
     const LdoRepCtl* ctl;
     const double* grid;
+    const double* learn_w;   // learned insertion proposal weights (LDO_LEARN_TABLE)
+    int learn_tb;            // temperature bin of the current tables
     // scalars of the current table set and controls, cached in the object
     int t_dense, t_stack_dense, imax, dim;
     long long t_off_e, t_off_h, t_off_s, t_off_stack;
@@ -308,6 +311,7 @@ struct Rep : public LdoState<C> {
     }
     __device__ void bind_tables(const LdoTab* t) {
         tab = t;
+        learn_tb = ldo_learn_tbin(t->temp);
         t_dense = t->dense;
         t_stack_dense = t->stack_dense;
         t_off_e = t->off_e;
@@ -1729,6 +1733,263 @@ struct Rep : public LdoState<C> {
         return delete_staple();
     }
 
+
+    // ================================ learned insertion proposal (engine) ===
+    // LearnedStapleExchange: the reference's staple exchange with a proposal
+    // for insertion targets learned from the plain sampler.  An insertion
+    // picks the growth-point target g with probability
+    //   q(g) = eps / N + (1 - eps) * [g unbound] w(g) / Z,   Z = sum of w over unbound domains
+    // (q = 1/N when Z = 0), w(g) = exp(network logit) of g's neighbourhood
+    // (ldo_learn.h), then the staple type and domain complementary to g with
+    // probability 1 - eps_t (uniform type and domain otherwise).  The forward
+    // probability of the new configuration sums q over the staple's bound
+    // domains (each could have been the growth point), so the Metropolis-
+    // Hastings ratio is the reference's (src/met_movetypes.cpp:212-301) with
+    // its uniform proposal factor n_bd / (S L N) replaced by that sum; the
+    // deletion proposal stays the reference's and its ratio uses the same sum
+    // evaluated in the state after the deletion.
+
+    // Neighbour-state code: 0 none, 1 unbound or unassigned, 2 bound,
+    // 3 misbound; a domain bound to chain `fresh` (the staple being inserted)
+    // counts as unbound, its state before the insertion.
+    __device__ __forceinline__ int learn_code(int n, int fresh) const {
+        if (n < 0) return 0;
+        int s = st[n];
+        if (s == BOUND || s == MISBOUND) {
+            if (fresh >= 0 && scs[bnd[n]] == fresh) return 1;
+            return s == BOUND ? 2 : 3;
+        }
+        return 1;
+    }
+    __device__ __noinline__ double learn_weight(int g, int fresh) const {
+        int p1 = bwd(g), n1 = fwd(g);
+        int p2 = p1 >= 0 ? bwd(p1) : -1;
+        int n2 = n1 >= 0 ? fwd(n1) : -1;
+        int combo = learn_code(p2, fresh) | (learn_code(p1, fresh) << 2) | (learn_code(n1, fresh) << 4) |
+                    (learn_code(n2, fresh) << 6);
+        int ts = scs[g] == 0 ? (int)sys->learn_tslot[sd[g]] : 0;
+        return __ldg(learn_w + ldo_learn_index(learn_tb, ts, combo));
+    }
+    // Training data for the network: every bound (label 1) or unbound
+    // (label 0) domain, counted at its network input.
+    __device__ __noinline__ void learn_collect(float* cnt_b, float* cnt_t) const {
+        int nc = hdr.n_chains;
+        #pragma unroll 1
+        for (int c = 0; c < nc; ++c) {
+            int cs = chain_order[c];
+            int len = chain_len(cs);
+            #pragma unroll 1
+            for (int d = 0; d < len; ++d) {
+                int g = slot_of(cs, d);
+                int s = st[g];
+                if (s != BOUND && s != UNBOUND) continue;
+                int p1 = bwd(g), n1 = fwd(g);
+                int p2 = p1 >= 0 ? bwd(p1) : -1;
+                int n2 = n1 >= 0 ? fwd(n1) : -1;
+                int combo = learn_code(p2, -1) | (learn_code(p1, -1) << 2) | (learn_code(n1, -1) << 4) |
+                            (learn_code(n2, -1) << 6);
+                int ts = cs == 0 ? (int)sys->learn_tslot[d] : 0;
+                int k = ldo_learn_index(learn_tb, ts, combo);
+                atomicAdd(cnt_t + k, 1.f);
+                if (s == BOUND) atomicAdd(cnt_b + k, 1.f);
+            }
+        }
+    }
+    // Z over the unbound domains of every chain except `skip`, in chain order.
+    __device__ __noinline__ double learn_z(int skip) const {
+        double z = 0;
+        int nc = hdr.n_chains;
+        #pragma unroll 1
+        for (int c = 0; c < nc; ++c) {
+            int cs = chain_order[c];
+            if (cs == skip) continue;
+            int len = chain_len(cs);
+            #pragma unroll 1
+            for (int d = 0; d < len; ++d) {
+                int g = slot_of(cs, d);
+                if (st[g] == UNBOUND) z += learn_weight(g, -1);
+            }
+        }
+        return z;
+    }
+    // q(g) for a target that was unbound in the state the proposal is made in.
+    __device__ double learn_q_target(int g, double z, int n_sites, int fresh) const {
+        if (z == 0) return 1.0 / n_sites;
+        double q = LDO_LEARN_EPS / n_sites;
+        q += (1.0 - LDO_LEARN_EPS) * (learn_weight(g, fresh) / z);
+        return q;
+    }
+    // q(type, domain d | target g)
+    __device__ double learn_q_type(int g, int type, int d) const {
+        int S = sys->n_types - 1;
+        double u = 1.0 / ((double)S * sys->type_len[type]);
+        int ct = scs[g] == 0 ? (int)sys->comp_type[sd[g]] : 0;
+        if (ct == 0) return u;
+        double q = LDO_LEARN_EPS_T * u;
+        if (ct == type && (int)sys->comp_dom[sd[g]] == d) q += 1.0 - LDO_LEARN_EPS_T;
+        return q;
+    }
+    // Sum over the domains of chain cs bound to another chain of
+    // q(partner) q(type, domain | partner).
+    __device__ __noinline__ double learn_forward(int cs, int type, double z, int n_sites, int fresh) const {
+        double f = 0;
+        int len = chain_len(cs);
+        #pragma unroll 1
+        for (int d = 0; d < len; ++d) {
+            int b = slot_of(cs, d);
+            int p = bnd[b];
+            if (p < 0 || scs[p] == cs) continue;
+            f += learn_q_target(p, z, n_sites, fresh) * learn_q_type(p, type, d);
+        }
+        return f;
+    }
+
+    __device__ __noinline__ bool learned_insert() {
+        int S = sys->n_types - 1;
+        int n_sites = hdr.num_domains;
+        double z = learn_z(-1);
+        int g = -1;
+        double u1 = rng.uniform_real();
+        if (z == 0 || u1 < LDO_LEARN_EPS) {
+            g = select_random_domain();
+        }
+        else {
+            double target = rng.uniform_real() * z;
+            double cum = 0;
+            int last = -1;
+            int nc = hdr.n_chains;
+            #pragma unroll 1
+            for (int c = 0; c < nc && g < 0; ++c) {
+                int cs = chain_order[c];
+                int len = chain_len(cs);
+                #pragma unroll 1
+                for (int d = 0; d < len; ++d) {
+                    int x = slot_of(cs, d);
+                    if (st[x] != UNBOUND) continue;
+                    cum += learn_weight(x, -1);
+                    last = x;
+                    if (target < cum) {
+                        g = x;
+                        break;
+                    }
+                }
+            }
+            if (g < 0) g = last;   // rounding left target >= Z
+        }
+        if (g < 0) {
+            fail(LDO_RS_INVARIANT);
+            return false;
+        }
+        int ct = scs[g] == 0 ? (int)sys->comp_type[sd[g]] : 0;
+        int type, gi;
+        double u3 = rng.uniform_real();
+        if (ct != 0 && u3 < 1.0 - LDO_LEARN_EPS_T) {
+            type = ct;
+            gi = sys->comp_dom[sd[g]];
+        }
+        else {
+            type = rng.uniform_int(1, S);
+            gi = rng.uniform_int(0, sys->type_len[type] - 1);
+        }
+        if (hdr.num_staples == sys->max_total_staples || type_count[type] == sys->max_type_staples) {
+            dirty = false;
+            return false;
+        }
+        int cs = add_chain(type);
+        if (cs < 0) return false;
+        if (mean_field) delta_e += log6;
+        delta_e += t_init_e;
+        m.added_cs = cs;
+        int len = chain_len(cs);
+        int gnew = slot_of(cs, gi);
+        delta_e += set_growth_point(gnew, g);
+        if (rejected || bad()) return false;
+        grow_staple(gi, cs, false);
+        if (rejected || bad()) return false;
+        #pragma unroll 1
+        for (int d = 0; d < len; ++d)
+            if (st[slot_of(cs, d)] == BOUND) { staple_bound = true; break; }
+        double f = learn_forward(cs, type, z, n_sites, cs);
+        add_external_bias_met();
+        double boltz = dexp(-delta_e);
+        int ni = type_count[type];
+        double pratio = boltz * c_staple_M;
+        pratio /= 6.0 * ni;
+        pratio /= (double)S * f;
+        return exchange_accept_common(type, pratio);
+    }
+
+    __device__ __noinline__ bool learned_delete() {
+        int S = sys->n_types - 1;
+        int type = rng.uniform_int(1, S);
+        int n = type_count[type];
+        if (n == 0) {
+            rejected = true;
+            dirty = false;
+            return false;
+        }
+        int which = rng.uniform_int(0, n - 1);
+        int cs = -1;
+        #pragma unroll 1
+        for (int c = 1; c < hdr.n_chains; ++c) {
+            int x = chain_order[c];
+            if (chain_type[x] == type) {
+                if (which == 0) { cs = x; break; }
+                --which;
+            }
+        }
+        if (cs < 0) {
+            fail(LDO_RS_INVARIANT);
+            return false;
+        }
+        if (staple_is_connector(cs)) {
+            dirty = false;
+            return false;
+        }
+        int len = chain_len(cs);
+        #pragma unroll 1
+        for (int d = 0; d < len; ++d)
+            if (st[slot_of(cs, d)] == BOUND) { staple_bound = true; break; }
+        // growth-point alternatives of the reverse insertion: (domain, partner)
+        int na = 0;
+        #pragma unroll 1
+        for (int d = 0; d < len; ++d) {
+            int b = slot_of(cs, d);
+            int p = bnd[b];
+            if (p < 0 || scs[p] == cs) continue;
+            m.bd_new[na] = d;
+            m.bd_old[na] = p;
+            na++;
+        }
+        unassign_domains(cs);
+        if (mean_field) delta_e -= log6;
+        delta_e -= t_init_e;
+        hdr.num_staples--;
+        add_external_bias_met();
+        hdr.num_staples++;
+        double boltz = dexp(-delta_e);
+        int n_sites = insertion_sites - len;
+        double z = learn_z(cs);
+        double f = 0;
+        #pragma unroll 1
+        for (int a = 0; a < na; ++a)
+            f += learn_q_target(m.bd_old[a], z, n_sites, -1) * learn_q_type(m.bd_old[a], type, m.bd_new[a]);
+        int ni = type_count[type];
+        double pratio = (double)ni * 6.0 * boltz;
+        pratio *= (double)S * f;
+        pratio /= c_staple_M;
+        bool acc = exchange_accept_common(type, pratio);
+        if (acc) delete_chain(cs);
+        return acc;
+    }
+
+    __device__ __noinline__ bool learned_exchange() {
+        insertion_sites = hdr.num_domains;
+        staple_bound = false;
+        if (rng.uniform_real() < 0.5) return learned_insert();
+        return learned_delete();
+    }
+
     __device__ __noinline__ int pick_staple_chain() {   // uniform_int(1, num_staples) -> get_chains()[i]
         int ci = rng.uniform_int(1, hdr.num_staples);
         return chain_order[ci];
@@ -1982,6 +2243,7 @@ struct Rep : public LdoState<C> {
         case LDO_MV_ORIENT: acc = orientation_rotation(); break;
         case LDO_MV_MET_EXCHANGE: acc = met_exchange(); break;
         case LDO_MV_MET_REGROWTH: acc = met_regrowth(); break;
+        case LDO_MV_LEARNED_EXCHANGE: acc = learned_exchange(); break;
         case LDO_MV_CB_REGROWTH: return cb_begin();
         }
         return finish_move(acc, 0);

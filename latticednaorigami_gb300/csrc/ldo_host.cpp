@@ -17,6 +17,7 @@
 #include "../../include/ldo.h"
 #include "ldo_io.hpp"
 #include "ldo_kernels.h"
+#include "ldo_mlp.h"
 #include "ldo_tables.hpp"
 
 namespace {
@@ -64,6 +65,7 @@ int move_kind(const string& t) {
     if (t == "MetStapleExchange") return LDO_MV_MET_EXCHANGE;
     if (t == "MetStapleRegrowth") return LDO_MV_MET_REGROWTH;
     if (t == "CBStapleRegrowth") return LDO_MV_CB_REGROWTH;
+    if (t == "LearnedStapleExchange") return LDO_MV_LEARNED_EXCHANGE;
     if (t == "CTCBScaffoldRegrowth" || t == "CTCBJumpScaffoldRegrowth" || t == "CTRGScaffoldRegrowth" ||
         t == "CTRGJumpScaffoldRegrowth" || t == "CTCBLinkerRegrowth" || t == "CTCBClusteredLinkerRegrowth" ||
         t == "CTRGLinkerRegrowth" || t == "CTRGClusteredLinkerRegrowth")
@@ -162,7 +164,9 @@ HostSystem load_system(const string& inp, const string& overrides) {
         d.move_kind[m] = move_kind(hs.moves[m].type);
         cum += hs.moves[m].freq;
         d.move_cum[m] = cum;
-        if (d.move_kind[m] == LDO_MV_MET_EXCHANGE) {
+        if (d.move_kind[m] == LDO_MV_LEARNED_EXCHANGE && d.ns > LDO_MAX_SCAF)
+            throw LdoError(LDO_EINVAL, "LearnedStapleExchange: scaffold longer than 320 domains");
+        if (d.move_kind[m] == LDO_MV_MET_EXCHANGE || d.move_kind[m] == LDO_MV_LEARNED_EXCHANGE) {
             for (size_t t = 0; t < hs.moves[m].exchange_mults.size() && t < LDO_MAX_TYPES; ++t)
                 d.exchange_mults[t] = hs.moves[m].exchange_mults[t];
             d.adaptive_exchange = hs.moves[m].adaptive_exchange;
@@ -173,6 +177,18 @@ HostSystem load_system(const string& inp, const string& overrides) {
         }
     }
     d.allow_nonsensical = p.allow_nonsensical_ps;
+    // complementary staple domain of each scaffold domain (first in type order)
+    for (int k = 0; k < d.ns && k < LDO_MAX_SCAF; ++k) {
+        int id = ids[0][k];
+        for (size_t t = 1; t < ids.size() && !d.comp_type[k]; ++t)
+            for (size_t q = 0; q < ids[t].size(); ++q)
+                if (ids[t][q] == -id) {
+                    d.comp_type[k] = (uint8_t)t;
+                    d.comp_dom[k] = (uint8_t)q;
+                    d.learn_tslot[k] = (uint8_t)ldo_learn_tslot((int)t);
+                    break;
+                }
+    }
     if (hs.ops.size() > LDO_MAX_OPS) throw LdoError(LDO_EINVAL, "too many order parameters");
     d.n_ops = (int)hs.ops.size();
     d.fully_op = -1;
@@ -309,6 +325,30 @@ LdoLayout make_layout(int dcap, int kmax, int ntypes, int nb, int nop, int nmv) 
 
 } // namespace
 
+// Seeded initial network parameters: uniform(-a, a) with a = sqrt(6 / (fan_in
+// + fan_out)) for the weight matrices, zero biases (splitmix64 stream).
+vector<float> ldo_learn_init_params(uint32_t seed) {
+    vector<float> p(LDO_LEARN_NPARAM, 0.f);
+    unsigned long long x = 0x9E3779B97F4A7C15ull * (seed + 1ull);
+    auto next = [&]() {
+        x += 0x9E3779B97F4A7C15ull;
+        unsigned long long z = x;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) * 0x1.0p-53;
+    };
+    auto fill = [&](int off, int fan_in, int fan_out) {
+        double a = std::sqrt(6.0 / (fan_in + fan_out));
+        for (int i = 0; i < fan_in * fan_out; ++i) p[off + i] = (float)((2 * next() - 1) * a);
+    };
+    fill(LDO_LEARN_OFF_W1, LDO_LEARN_DIN, LDO_LEARN_H);
+    fill(LDO_LEARN_OFF_W2, LDO_LEARN_H, LDO_LEARN_H);
+    fill(LDO_LEARN_OFF_W3, LDO_LEARN_H, LDO_LEARN_H);
+    fill(LDO_LEARN_OFF_W4, LDO_LEARN_H, 1);
+    return p;
+}
+
 struct ldo_engine {
     string err;
     vector<HostSystem> systems;
@@ -336,6 +376,11 @@ struct ldo_engine {
     DevBuf<double> d_grid;
     DevBuf<unsigned char> d_arena;
     DevBuf<unsigned char> d_snap;   // move snapshots (run mode)
+    // learned insertion proposal: weight table, training counts, network
+    DevBuf<double> d_learn_w;
+    DevBuf<float> d_cnt_b, d_cnt_t;
+    LdoMlp mlp;
+    bool mlp_init {false};
     DevBuf<int> d_status;
     DevBuf<int16_t> d_samples;
     DevBuf<double> d_trace;
@@ -367,6 +412,7 @@ struct ldo_engine {
     std::vector<long long> us_att, us_acc;
 
     ~ldo_engine() {
+        ldo_mlp_free(mlp);
         if (pt_graph) cudaGraphExecDestroy(pt_graph);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -450,6 +496,9 @@ struct ldo_engine {
         L.trace = d_trace.p;
         L.us_hist = nullptr;
         L.us_window = nullptr;
+        L.learn_w = d_learn_w.p;
+        L.learn_cnt_b = d_cnt_b.p;
+        L.learn_cnt_t = d_cnt_t.p;
         return L;
     }
 
@@ -646,6 +695,16 @@ struct ldo_engine {
         d_status.alloc(1);
         init_arena();
         d_snap.alloc((size_t)n_rep * LDO_N_SNAPSHOTS * ldo_snapshot_stride(lay.bytes));
+        // untrained proposal: every unbound domain weighs 1
+        {
+            vector<double> ones(LDO_LEARN_TABLE, 1.0);
+            d_learn_w.alloc(LDO_LEARN_TABLE);
+            CU(cudaMemcpy(d_learn_w.p, ones.data(), ones.size() * sizeof(double), cudaMemcpyHostToDevice));
+            d_cnt_b.alloc(LDO_LEARN_TABLE);
+            d_cnt_t.alloc(LDO_LEARN_TABLE);
+            CU(cudaMemset(d_cnt_b.p, 0, LDO_LEARN_TABLE * sizeof(float)));
+            CU(cudaMemset(d_cnt_t.p, 0, LDO_LEARN_TABLE * sizeof(float)));
+        }
         LdoLaunch L = launch_params(LDO_MODE_INIT, 0);
         CU(ldo_launch_mc(L, stream));
         CU(cudaStreamSynchronize(stream));
@@ -665,6 +724,60 @@ struct ldo_engine {
             *ms = f;
         }
         check_status();
+    }
+
+    // ---------------------------------------- learned insertion proposal ---
+    static constexpr int kMlpCap = 1 << 17;
+
+    void mlp_ensure(uint32_t seed) {
+        if (!mlp.params) CU(ldo_mlp_alloc(mlp, kMlpCap));
+        if (!mlp_init) {
+            vector<float> p = ldo_learn_init_params(seed);
+            CU(cudaMemcpy(mlp.params, p.data(), p.size() * sizeof(float), cudaMemcpyHostToDevice));
+            CU(ldo_mlp_sync_weights(mlp, stream));
+            mlp_init = true;
+        }
+    }
+
+    void learn_collect() {
+        LdoLaunch L = launch_params(LDO_MODE_COLLECT, 0);
+        CU(ldo_launch_mc(L, stream));
+        CU(cudaStreamSynchronize(stream));
+        check_status();
+    }
+
+    // Adam on the weighted logistic loss over the collected counts (full
+    // batch), then the weight table.
+    void learn_train(int iters, double lr, uint32_t seed, double* loss0, double* loss1) {
+        vector<float> cb(LDO_LEARN_TABLE), ct(LDO_LEARN_TABLE);
+        CU(cudaMemcpy(cb.data(), d_cnt_b.p, cb.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(ct.data(), d_cnt_t.p, ct.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        vector<int32_t> idx;
+        vector<float> bb, tt;
+        double norm = 0;
+        for (int k = 0; k < LDO_LEARN_TABLE; ++k)
+            if (ct[k] > 0) {
+                idx.push_back(k);
+                bb.push_back(cb[k]);
+                tt.push_back(ct[k]);
+                norm += ct[k];
+            }
+        if (idx.empty()) throw LdoError(LDO_EINVAL, "no training data collected");
+        if ((int)idx.size() > kMlpCap) throw LdoError(LDO_EINVAL, "too many distinct network inputs");
+        mlp_ensure(seed);
+        int n = (int)idx.size();
+        CU(cudaMemcpy(mlp.idx, idx.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(mlp.cnt_b, bb.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(mlp.cnt_t, tt.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+        for (int it = 0; it < iters; ++it) {
+            CU(ldo_mlp_loss_grad(mlp, n, norm, stream));
+            if (it == 0 && loss0) CU(cudaMemcpyAsync(loss0, mlp.loss, sizeof(double), cudaMemcpyDeviceToHost, stream));
+            CU(ldo_mlp_adam(mlp, (float)lr, stream));
+        }
+        CU(ldo_mlp_loss_grad(mlp, n, norm, stream));
+        if (loss1) CU(cudaMemcpyAsync(loss1, mlp.loss, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        CU(ldo_mlp_table(mlp, d_learn_w.p, stream));
+        CU(cudaStreamSynchronize(stream));
     }
 
     // PTGCMCSimulation constructor + OneDPTGCMCSimulation::initialize_control_qs
@@ -1440,6 +1553,86 @@ ldo_status ldo_energy_tables(const char* inp_path, double temp, double stacking_
             init[1] = t.init_s;
             init[2] = t.init_e;
         }
+    });
+}
+
+// ------------------------------------------------ learned proposal ABI ---
+
+ldo_status ldo_learn_collect(ldo_engine* e) {
+    if (!e) return LDO_EINVAL;
+    return guard(e, [&]() { e->learn_collect(); });
+}
+
+ldo_status ldo_learn_reset_counts(ldo_engine* e) {
+    if (!e) return LDO_EINVAL;
+    return guard(e, [&]() {
+        CU(cudaMemset(e->d_cnt_b.p, 0, LDO_LEARN_TABLE * sizeof(float)));
+        CU(cudaMemset(e->d_cnt_t.p, 0, LDO_LEARN_TABLE * sizeof(float)));
+    });
+}
+
+ldo_status ldo_learn_get_counts(ldo_engine* e, float* cnt_bound, float* cnt_total, int n) {
+    if (!e || !cnt_bound || !cnt_total || n != LDO_LEARN_TABLE) return LDO_EINVAL;
+    return guard(e, [&]() {
+        CU(cudaMemcpy(cnt_bound, e->d_cnt_b.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(cnt_total, e->d_cnt_t.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+    });
+}
+
+ldo_status ldo_learn_train(ldo_engine* e, int iters, double lr, uint32_t seed, double* loss_first, double* loss_last) {
+    if (!e || iters < 0 || !(lr > 0)) return LDO_EINVAL;
+    return guard(e, [&]() { e->learn_train(iters, lr, seed, loss_first, loss_last); });
+}
+
+ldo_status ldo_learn_set_params(ldo_engine* e, const float* params, int n) {
+    if (!e || !params || n != LDO_LEARN_NPARAM) return LDO_EINVAL;
+    return guard(e, [&]() {
+        e->mlp_ensure(0);
+        CU(cudaMemcpy(e->mlp.params, params, n * sizeof(float), cudaMemcpyHostToDevice));
+        CU(ldo_mlp_sync_weights(e->mlp, e->stream));
+        CU(ldo_mlp_table(e->mlp, e->d_learn_w.p, e->stream));
+        CU(cudaStreamSynchronize(e->stream));
+    });
+}
+
+ldo_status ldo_learn_get_params(ldo_engine* e, float* params, int n) {
+    if (!e || !params || n != LDO_LEARN_NPARAM) return LDO_EINVAL;
+    return guard(e, [&]() {
+        e->mlp_ensure(0);
+        CU(cudaMemcpy(params, e->mlp.params, n * sizeof(float), cudaMemcpyDeviceToHost));
+    });
+}
+
+ldo_status ldo_learn_get_table(ldo_engine* e, double* weights, int n) {
+    if (!e || !weights || n != LDO_LEARN_TABLE) return LDO_EINVAL;
+    return guard(e, [&]() { CU(cudaMemcpy(weights, e->d_learn_w.p, n * sizeof(double), cudaMemcpyDeviceToHost)); });
+}
+
+ldo_status ldo_learn_set_table(ldo_engine* e, const double* weights, int n) {
+    if (!e || !weights || n != LDO_LEARN_TABLE) return LDO_EINVAL;
+    return guard(e, [&]() { CU(cudaMemcpy(e->d_learn_w.p, weights, n * sizeof(double), cudaMemcpyHostToDevice)); });
+}
+
+ldo_status ldo_learn_loss_grad(const float* params, const int32_t* idx, const float* cnt_bound, const float* cnt_total,
+                             int n, double* loss, float* grad) {
+    if (!params || !idx || !cnt_bound || !cnt_total || n <= 0 || !loss || !grad) return LDO_EINVAL;
+    return guard(nullptr, [&]() {
+        LdoMlp m;
+        struct Free {
+            LdoMlp& m;
+            ~Free() { ldo_mlp_free(m); }
+        } hold {m};
+        CU(ldo_mlp_alloc(m, n));
+        double norm = 0;
+        for (int i = 0; i < n; ++i) norm += cnt_total[i];
+        CU(cudaMemcpy(m.params, params, LDO_LEARN_NPARAM * sizeof(float), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(m.idx, idx, n * sizeof(int32_t), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(m.cnt_b, cnt_bound, n * sizeof(float), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(m.cnt_t, cnt_total, n * sizeof(float), cudaMemcpyHostToDevice));
+        CU(ldo_mlp_sync_weights(m, 0));
+        CU(ldo_mlp_loss_grad(m, n, norm, 0));
+        CU(cudaMemcpy(loss, m.loss, sizeof(double), cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(grad, m.grad, LDO_LEARN_NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
     });
 }
 

@@ -32,6 +32,7 @@ __device__ void bind_rep(ldo::Rep<C>& r, const LdoLaunch& L, int rep) {
     r.sys = L.sys + r.ctl->sys;
     r.bank = L.bank;
     r.grid = L.grid;
+    r.learn_w = L.learn_w;
     r.bind_tables(L.tabs + r.ctl->tab);
     r.imax = r.sys->imax;
     r.dim = r.sys->dim;
@@ -128,6 +129,13 @@ __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
                 // dependent quantities use the tables the energy was last
                 // computed with, even if the controls have moved since.
                 R->bind_tables(L.tabs + h.tab);
+            }
+            else if (L.mode == LDO_MODE_COLLECT) {
+                // training data of the learned insertion proposal: for every
+                // bound or unbound domain, its network input and whether it
+                // is bound
+                R->bind_tables(L.tabs + h.tab);
+                R->learn_collect(L.learn_cnt_b, L.learn_cnt_t);
             }
             else {
                 if (L.force_recompute || h.tab != R->ctl->tab) {

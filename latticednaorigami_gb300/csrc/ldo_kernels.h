@@ -5,7 +5,7 @@
 
 #include "ldo_types.h"
 
-enum { LDO_MODE_RUN = 0, LDO_MODE_INIT = 1, LDO_MODE_RECOMPUTE = 2, LDO_MODE_OBSERVE = 3 };
+enum { LDO_MODE_RUN = 0, LDO_MODE_INIT = 1, LDO_MODE_RECOMPUTE = 2, LDO_MODE_OBSERVE = 3, LDO_MODE_COLLECT = 4 };
 
 struct LdoLaunch {
     const LdoSys* sys;
@@ -36,6 +36,11 @@ struct LdoLaunch {
     int* us_hist;
     const int* us_window;        // [n_rep] window held by each replica
     int us_bias, us_len;
+    // Learned insertion proposal: weight exp(logit) of every network input
+    // (LDO_LEARN_TABLE entries), read by LearnedStapleExchange.
+    const double* learn_w;
+    float* learn_cnt_b;          // collect mode: bound / total counts per network input
+    float* learn_cnt_t;
 };
 
 cudaError_t ldo_launch_mc(const LdoLaunch& L, cudaStream_t stream);

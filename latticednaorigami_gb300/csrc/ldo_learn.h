@@ -1,0 +1,72 @@
+// Learned staple-insertion proposal: feature encoding and network shape,
+// shared by the MC kernel, the network kernels, the host library and the
+// oracle.
+//
+// The proposal scores a candidate growth-point domain g from its local
+// neighbourhood along its chain: the states of the domains two and one step
+// before and after g (none / unbound / bound / misbound), the type slot of
+// the staple complementary to g, and the temperature bin.  The network maps
+// that input to a logit; exp(logit) weighs g among the unbound domains.  The
+// input space is finite (LDO_LEARN_TABLE entries), so the network is
+// evaluated once for every input on the tensor cores and the MC kernel reads
+// the weights from that table: the proposal is an exact function of the
+// current state, as the Metropolis-Hastings ratio requires.
+#pragma once
+#include <math.h>
+
+#ifdef __CUDACC__
+#define LDO_LHD __host__ __device__
+#else
+#define LDO_LHD
+#endif
+
+enum {
+    LDO_LEARN_DIN = 64,       // network input width
+    LDO_LEARN_H = 256,        // hidden width (three GELU layers)
+    LDO_LEARN_NTYPE = 32,     // type slots: 0 = no complementary staple
+    LDO_LEARN_NTB = 64,       // temperature bins of 1 K from 300 K
+    LDO_LEARN_NCOMBO = 256,   // 4 neighbour states x 4 positions
+    LDO_LEARN_TABLE = LDO_LEARN_NTB * LDO_LEARN_NTYPE * LDO_LEARN_NCOMBO,
+    // parameter vector: W1[64][256] b1[256] W2[256][256] b2 W3[256][256] b3 w4[256] b4
+    LDO_LEARN_OFF_W1 = 0,
+    LDO_LEARN_OFF_B1 = LDO_LEARN_OFF_W1 + LDO_LEARN_DIN * LDO_LEARN_H,
+    LDO_LEARN_OFF_W2 = LDO_LEARN_OFF_B1 + LDO_LEARN_H,
+    LDO_LEARN_OFF_B2 = LDO_LEARN_OFF_W2 + LDO_LEARN_H * LDO_LEARN_H,
+    LDO_LEARN_OFF_W3 = LDO_LEARN_OFF_B2 + LDO_LEARN_H,
+    LDO_LEARN_OFF_B3 = LDO_LEARN_OFF_W3 + LDO_LEARN_H * LDO_LEARN_H,
+    LDO_LEARN_OFF_W4 = LDO_LEARN_OFF_B3 + LDO_LEARN_H,
+    LDO_LEARN_OFF_B4 = LDO_LEARN_OFF_W4 + LDO_LEARN_H,
+    LDO_LEARN_NPARAM = LDO_LEARN_OFF_B4 + 1
+};
+
+// Proposal mixture weights: with probability LDO_LEARN_EPS the target is
+// uniform over all domains, and with LDO_LEARN_EPS_T the staple type and
+// domain are uniform; both keep every insertion the reference can make
+// possible.
+#define LDO_LEARN_EPS 0.05
+#define LDO_LEARN_EPS_T 0.05
+#define LDO_LEARN_LOGIT_CLAMP 30.0f
+
+LDO_LHD inline int ldo_learn_tbin(double temp) {
+    int b = (int)floor(temp - 300.0 + 0.5);
+    return b < 0 ? 0 : (b >= LDO_LEARN_NTB ? LDO_LEARN_NTB - 1 : b);
+}
+LDO_LHD inline int ldo_learn_index(int tbin, int tslot, int combo) {
+    return (tbin * LDO_LEARN_NTYPE + tslot) * LDO_LEARN_NCOMBO + combo;
+}
+// Type slot of staple type t (1..S) in the one-hot (types above 31 share slots).
+LDO_LHD inline int ldo_learn_tslot(int t) { return t <= 0 ? 0 : 1 + (t - 1) % (LDO_LEARN_NTYPE - 1); }
+// Input vector of table entry k (written as floats; the kernels round to bf16):
+// [0,16) one-hot neighbour states (position-major: two before, one before,
+// one after, two after), [16,48) type-slot one-hot, [48] (T - 335 K) / 15 K,
+// [49] 1, the rest 0.
+LDO_LHD inline void ldo_learn_input(int k, float* x) {
+    for (int i = 0; i < LDO_LEARN_DIN; ++i) x[i] = 0.f;
+    int combo = k % LDO_LEARN_NCOMBO;
+    int tslot = (k / LDO_LEARN_NCOMBO) % LDO_LEARN_NTYPE;
+    int tbin = k / (LDO_LEARN_NCOMBO * LDO_LEARN_NTYPE);
+    for (int o = 0; o < 4; ++o) x[4 * o + ((combo >> (2 * o)) & 3)] = 1.f;
+    x[16 + tslot] = 1.f;
+    x[48] = (float)(tbin - 35) / 15.f;
+    x[49] = 1.f;
+}

@@ -21,8 +21,15 @@
 #define LDO_MAX_PARTS 4
 #define LDO_MAX_LEN 4
 #define LDO_MAX_KMAX 63
+#define LDO_MAX_SCAF 320
 
-enum LdoMove { LDO_MV_ORIENT = 0, LDO_MV_MET_EXCHANGE = 1, LDO_MV_MET_REGROWTH = 2, LDO_MV_CB_REGROWTH = 3 };
+enum LdoMove {
+    LDO_MV_ORIENT = 0,
+    LDO_MV_MET_EXCHANGE = 1,
+    LDO_MV_MET_REGROWTH = 2,
+    LDO_MV_CB_REGROWTH = 3,
+    LDO_MV_LEARNED_EXCHANGE = 4   // engine extension: exchange with the learned insertion proposal
+};
 
 enum LdoOp {
     LDO_OP_NUMSTAPLES = 0,
@@ -78,6 +85,12 @@ struct LdoSys {
     double bias_mult;
     int centering_freq, centering_domain, constraint_check_freq;
     int fully_op;         // index of a NumBoundDomainPairs op, or -1 (sampling)
+    // Learned insertion proposal: for each scaffold domain the staple type
+    // (0: none) and domain index complementary to it, and the network's type
+    // slot for that type.
+    uint8_t comp_type[LDO_MAX_SCAF];
+    uint8_t comp_dom[LDO_MAX_SCAF];
+    uint8_t learn_tslot[LDO_MAX_SCAF];
 };
 
 struct LdoTab {

@@ -20,7 +20,12 @@ EXPORTS = [
     "ldo_get_samples", "ldo_set_trace", "ldo_get_trace", "ldo_get_move_stats", "ldo_set_grid_bias",
     "ldo_set_window", "ldo_pt_run", "ldo_pt_get_permutation", "ldo_pt_get_stats", "ldo_nn_duplex_thermo",
     "ldo_energy_tables", "ldo_us_run", "ldo_us_get_biases", "ldo_us_get_windows", "ldo_replica_status_noalloc",
+    "ldo_learn_collect", "ldo_learn_reset_counts", "ldo_learn_get_counts", "ldo_learn_train", "ldo_learn_set_params",
+    "ldo_learn_get_params", "ldo_learn_get_table", "ldo_learn_set_table", "ldo_learn_loss_grad",
 ]
+
+LEARN_TABLE = 524288      # network inputs (ldo_learn.h)
+LEARN_NPARAM = 148481     # network parameters
 
 
 class LdoError(RuntimeError):
@@ -81,6 +86,16 @@ def load_library(path=None):
     lib.ldo_us_get_windows.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ip, ctypes.POINTER(ctypes.c_int)]
     i32p = ctypes.POINTER(ctypes.c_int32)
     lib.ldo_replica_status_noalloc.argtypes = [vp, i32p, ip, i32p, i32p]
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib.ldo_learn_collect.argtypes = [vp]
+    lib.ldo_learn_reset_counts.argtypes = [vp]
+    lib.ldo_learn_get_counts.argtypes = [vp, fp, fp, ip]
+    lib.ldo_learn_train.argtypes = [vp, ip, ctypes.c_double, ctypes.c_uint32, dp, dp]
+    lib.ldo_learn_set_params.argtypes = [vp, fp, ip]
+    lib.ldo_learn_get_params.argtypes = [vp, fp, ip]
+    lib.ldo_learn_get_table.argtypes = [vp, dp, ip]
+    lib.ldo_learn_set_table.argtypes = [vp, dp, ip]
+    lib.ldo_learn_loss_grad.argtypes = [fp, i32p, fp, fp, ip, dp, fp]
     lib.ldo_nn_duplex_thermo.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, dp, dp]
     lib.ldo_energy_tables.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
                                       dp, dp, dp, dp, dp, ip]
@@ -217,6 +232,42 @@ class Engine:
         self._check(self.lib.ldo_us_get_biases(self.h, _dptr(out), self.n, gl))
         return out
 
+    # learned insertion proposal
+    def learn_collect(self):
+        self._check(self.lib.ldo_learn_collect(self.h))
+
+    def learn_reset_counts(self):
+        self._check(self.lib.ldo_learn_reset_counts(self.h))
+
+    def learn_counts(self):
+        b = np.zeros(LEARN_TABLE, np.float32)
+        t = np.zeros(LEARN_TABLE, np.float32)
+        self._check(self.lib.ldo_learn_get_counts(self.h, _fptr(b), _fptr(t), LEARN_TABLE))
+        return b, t
+
+    def learn_train(self, iters, lr=1e-3, seed=0):
+        l0, l1 = ctypes.c_double(0), ctypes.c_double(0)
+        self._check(self.lib.ldo_learn_train(self.h, int(iters), float(lr), seed, ctypes.byref(l0), ctypes.byref(l1)))
+        return l0.value, l1.value
+
+    def learn_params(self):
+        p = np.zeros(LEARN_NPARAM, np.float32)
+        self._check(self.lib.ldo_learn_get_params(self.h, _fptr(p), LEARN_NPARAM))
+        return p
+
+    def learn_set_params(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        self._check(self.lib.ldo_learn_set_params(self.h, _fptr(p), len(p)))
+
+    def learn_table(self):
+        w = np.zeros(LEARN_TABLE)
+        self._check(self.lib.ldo_learn_get_table(self.h, _dptr(w), LEARN_TABLE))
+        return w
+
+    def learn_set_table(self, w):
+        w = np.ascontiguousarray(w, np.float64)
+        self._check(self.lib.ldo_learn_set_table(self.h, _dptr(w), len(w)))
+
     def pt_permutation(self):
         out = np.zeros(self.n, np.int32)
         self._check(self.lib.ldo_pt_get_permutation(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
@@ -229,6 +280,26 @@ class Engine:
         self._check(self.lib.ldo_pt_get_stats(self.h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
                                               b.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), n_pairs))
         return a, b
+
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def learn_loss_grad(params, idx, cnt_bound, cnt_total):
+    """Loss and gradient of the proposal network on the GPU (ldo_learn_loss_grad)."""
+    lib = load_library()
+    p = np.ascontiguousarray(params, np.float32)
+    i = np.ascontiguousarray(idx, np.int32)
+    b = np.ascontiguousarray(cnt_bound, np.float32)
+    t = np.ascontiguousarray(cnt_total, np.float32)
+    loss = ctypes.c_double(0)
+    grad = np.zeros(LEARN_NPARAM, np.float32)
+    rc = lib.ldo_learn_loss_grad(_fptr(p), i.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _fptr(b), _fptr(t),
+                                 len(i), ctypes.byref(loss), _fptr(grad))
+    if rc != 0:
+        raise LdoError(rc, lib.ldo_last_error(None).decode())
+    return loss.value, grad
 
 
 def nn_duplex_thermo(seq, temp, cation_M):

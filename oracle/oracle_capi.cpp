@@ -22,6 +22,7 @@ struct Replica {
     ldo_io::SystemFile sf;
     EnergyModel model;
     System sys;
+    std::vector<double> learn_w;   // learned-proposal weight table (engine's)
 };
 
 int move_kind(const std::string& t) {
@@ -29,6 +30,7 @@ int move_kind(const std::string& t) {
     if (t == "MetStapleExchange") return MV_MET_EXCHANGE;
     if (t == "MetStapleRegrowth") return MV_MET_REGROWTH;
     if (t == "CBStapleRegrowth") return MV_CB_REGROWTH;
+    if (t == "LearnedStapleExchange") return MV_LEARNED_EXCHANGE;
     throw std::runtime_error(t + ": movetype not supported by the oracle");
 }
 
@@ -91,7 +93,7 @@ Replica* build(const char* inp_path, const char* overrides, uint32_t seed, uint3
             c.move_kinds.push_back(move_kind(mv.type));
             cum += mv.freq;
             c.move_cum.push_back(cum);
-            if (mv.type == "MetStapleExchange") {
+            if (mv.type == "MetStapleExchange" || mv.type == "LearnedStapleExchange") {
                 c.exchange_mults = mv.exchange_mults;
                 while (c.exchange_mults.size() < S) c.exchange_mults.push_back(1);
                 c.adaptive_exchange = mv.adaptive_exchange;
@@ -112,6 +114,7 @@ Replica* build(const char* inp_path, const char* overrides, uint32_t seed, uint3
         s.rng.stream = 0;
         s.rng.draws = 0;
         s.init(c, tab, init);
+        s.learn_tb = ldo_learn_tbin(m.temp);
 
         if (!p.order_parameter_file.empty()) {
             auto ops = ldo_io::read_ops(ldo_io::resolve(p, p.order_parameter_file));
@@ -286,6 +289,19 @@ int oracle_tables(void* h, double* hyb_e, double* hyb_h, double* hyb_s, double* 
 
 // OrigamiSystem::update_temp (src/origami_system.cpp:618): new tables, full
 // energy recomputation.
+// Weight table of the learned insertion proposal (the engine's, LDO_LEARN_TABLE
+// doubles), used by LearnedStapleExchange.
+int oracle_set_learn_table(void* h, const double* w, int n) {
+    auto* r = static_cast<Replica*>(h);
+    if (n != LDO_LEARN_TABLE) {
+        g_err = "learn table size";
+        return -1;
+    }
+    r->learn_w.assign(w, w + n);
+    r->sys.learn_w = r->learn_w.data();
+    return 0;
+}
+
 int oracle_update_temp(void* h, double temp, double stacking_mult) {
     auto* r = static_cast<Replica*>(h);
     try {
@@ -293,6 +309,7 @@ int oracle_update_temp(void* h, double temp, double stacking_mult) {
         m.temp = temp;
         m.stacking_mult = stacking_mult;
         r->sys.tab = build_tables(r->sf.identities, r->sf.sequences, m);
+        r->sys.learn_tb = ldo_learn_tbin(temp);
         r->sys.recompute_energy();
     } catch (std::exception& e) {
         g_err = e.what();
@@ -405,6 +422,47 @@ double oracle_run_batch(const char* inp_path, const char* overrides, uint32_t se
     double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     for (auto* r : reps) delete r;
     return failed.load() ? -2 : dt;
+}
+
+// Independent replicas (key (seed0, r)) with an optional learned-proposal
+// weight table: after `burn` steps, n_snaps snapshots `gap` steps apart of
+// (staples, fully bound pairs) into out[(r * n_snaps + k) * 2].  Returns 0, or
+// -1 if a replica failed.
+int oracle_run_batch_states(const char* inp_path, const char* overrides, uint32_t seed0, int n_rep, long long burn,
+                            long long gap, int n_snaps, int threads, const double* learn_w, int* out) {
+    std::vector<Replica*> reps(n_rep, nullptr);
+    for (int i = 0; i < n_rep; ++i) {
+        reps[i] = build(inp_path, overrides, seed0, (uint32_t)i);
+        if (!reps[i]) {
+            for (auto* r : reps) delete r;
+            return -1;
+        }
+        reps[i]->sys.learn_w = learn_w;   // shared, read-only
+    }
+    std::vector<std::thread> pool;
+    std::atomic<int> next {0};
+    std::atomic<int> failed {0};
+    for (int t = 0; t < threads; ++t)
+        pool.emplace_back([&]() {
+            for (;;) {
+                int i = next.fetch_add(1);
+                if (i >= n_rep) break;
+                try {
+                    long long st = 0;
+                    for (long long k = 0; k < burn; ++k) reps[i]->sys.step(++st);
+                    for (int s = 0; s < n_snaps; ++s) {
+                        for (long long k = 0; k < gap; ++k) reps[i]->sys.step(++st);
+                        out[((size_t)i * n_snaps + s) * 2] = reps[i]->sys.num_staples;
+                        out[((size_t)i * n_snaps + s) * 2 + 1] = reps[i]->sys.num_fully;
+                    }
+                } catch (std::exception& e) {
+                    failed.store(1);
+                }
+            }
+        });
+    for (auto& th : pool) th.join();
+    for (auto* r : reps) delete r;
+    return failed.load() ? -1 : 0;
 }
 
 // CPU baseline with order-parameter samples: n_rep replicas (key (seed0, r)),

@@ -19,6 +19,7 @@
 
 #include "oracle_philox.hpp"
 #include "oracle_thermo.hpp"
+#include "../latticednaorigami_gb300/csrc/ldo_learn.h"
 
 namespace oracle {
 
@@ -113,7 +114,7 @@ struct BiasRec {
     double bias {0};
 };
 
-enum MoveKind { MV_ORIENTATION = 0, MV_MET_EXCHANGE = 1, MV_MET_REGROWTH = 2, MV_CB_REGROWTH = 3 };
+enum MoveKind { MV_ORIENTATION = 0, MV_MET_EXCHANGE = 1, MV_MET_REGROWTH = 2, MV_CB_REGROWTH = 3, MV_LEARNED_EXCHANGE = 4 };
 
 struct Config {
     // chain-type identities, index 0 is the scaffold
@@ -1384,6 +1385,188 @@ class System {
         return delete_staple();
     }
 
+    // ---------------------------- learned insertion proposal (engine only) ---
+    // CPU restatement of the engine's LearnedStapleExchange (no reference
+    // counterpart): the same targets, the same weights (the engine's table),
+    // the same order of every sum, so trajectories agree exactly.
+    const double* learn_w {nullptr};
+    int learn_tb {0};
+
+    int learn_code(int n, int fresh_c) const {
+        if (n < 0) return 0;
+        int s = doms[n].state;
+        if (s == BOUND || s == MISBOUND) {
+            if (fresh_c >= 0 && doms[doms[n].bound].c == fresh_c) return 1;
+            return s == BOUND ? 2 : 3;
+        }
+        return 1;
+    }
+    // complementary staple type / domain of scaffold domain index k (0: none)
+    std::pair<int, int> learn_comp(int k) const {
+        int id = cfg.identities[0][k];
+        for (size_t t = 1; t < cfg.identities.size(); ++t)
+            for (size_t q = 0; q < cfg.identities[t].size(); ++q)
+                if (cfg.identities[t][q] == -id) return {(int)t, (int)q};
+        return {0, 0};
+    }
+    double learn_weight(int g, int fresh_c) const {
+        int p1 = doms[g].bwd, n1 = doms[g].fwd;
+        int p2 = p1 >= 0 ? doms[p1].bwd : -1;
+        int n2 = n1 >= 0 ? doms[n1].fwd : -1;
+        int combo = learn_code(p2, fresh_c) | (learn_code(p1, fresh_c) << 2) | (learn_code(n1, fresh_c) << 4) |
+                    (learn_code(n2, fresh_c) << 6);
+        int ts = doms[g].cident == 0 ? ldo_learn_tslot(learn_comp(doms[g].d).first) : 0;
+        return learn_w[ldo_learn_index(learn_tb, ts, combo)];
+    }
+    double learn_z(int skip_c) const {
+        double z = 0;
+        for (size_t c = 0; c < chains.size(); ++c) {
+            if (chain_index[c] == skip_c) continue;
+            for (int g : chains[c])
+                if (doms[g].state == UNBOUND) z += learn_weight(g, -1);
+        }
+        return z;
+    }
+    double learn_q_target(int g, double z, int n_sites, int fresh_c) const {
+        if (z == 0) return 1.0 / n_sites;
+        double q = LDO_LEARN_EPS / n_sites;
+        q += (1.0 - LDO_LEARN_EPS) * (learn_weight(g, fresh_c) / z);
+        return q;
+    }
+    double learn_q_type(int g, int type, int d) const {
+        int S = (int)cfg.identities.size() - 1;
+        double u = 1.0 / ((double)S * cfg.identities[type].size());
+        int ct = 0, cd = 0;
+        if (doms[g].cident == 0) {
+            auto cc = learn_comp(doms[g].d);
+            ct = cc.first;
+            cd = cc.second;
+        }
+        if (ct == 0) return u;
+        double q = LDO_LEARN_EPS_T * u;
+        if (ct == type && cd == d) q += 1.0 - LDO_LEARN_EPS_T;
+        return q;
+    }
+
+    bool learned_insert() {
+        if (!learn_w) throw std::runtime_error("LearnedStapleExchange needs the weight table");
+        int S = (int)cfg.identities.size() - 1;
+        int n_sites = num_domains;
+        double z = learn_z(-1);
+        int g = -1;
+        double u1 = rng.uniform_real();
+        if (z == 0 || u1 < LDO_LEARN_EPS) {
+            g = select_random_domain();
+        }
+        else {
+            double target = rng.uniform_real() * z;
+            double cum = 0;
+            int last = -1;
+            for (size_t c = 0; c < chains.size() && g < 0; ++c)
+                for (int x : chains[c]) {
+                    if (doms[x].state != UNBOUND) continue;
+                    cum += learn_weight(x, -1);
+                    last = x;
+                    if (target < cum) {
+                        g = x;
+                        break;
+                    }
+                }
+            if (g < 0) g = last;
+        }
+        int ct = 0, cd = 0;
+        if (doms[g].cident == 0) {
+            auto cc = learn_comp(doms[g].d);
+            ct = cc.first;
+            cd = cc.second;
+        }
+        int ident, gi;
+        double u3 = rng.uniform_real();
+        if (ct != 0 && u3 < 1.0 - LDO_LEARN_EPS_T) {
+            ident = ct;
+            gi = cd;
+        }
+        else {
+            ident = rng.uniform_int(1, S);
+            gi = rng.uniform_int(0, (int)cfg.identities[ident].size() - 1);
+        }
+        if (num_staples == cfg.max_total_staples) return false;
+        if (num_staples_of_ident(ident) == cfg.max_type_staples) return false;
+        int c_i = add_chain(ident);
+        if (cfg.mean_field) delta_e += std::log(6);
+        delta_e += tab.init_e;
+        added.push_back(c_i);
+        std::vector<int> ch = chains.back();
+        int gnew = ch[gi];
+        delta_e += set_growth_point(gnew, g);
+        if (rejected) return false;
+        grow_staple(doms[gnew].d, ch, false);
+        if (rejected) return false;
+        std::vector<int> st = get_chain(c_i);
+        for (int id : st)
+            if (doms[id].state == BOUND) { staple_bound = true; break; }
+        double f = 0;
+        for (size_t d = 0; d < st.size(); ++d) {
+            int b = st[d];
+            int p = doms[b].bound;
+            if (p < 0 || doms[p].c == c_i) continue;
+            f += learn_q_target(p, z, n_sites, c_i) * learn_q_type(p, ident, (int)d);
+        }
+        add_external_bias_met();
+        double boltz = std::exp(-delta_e);
+        int ni = num_staples_of_ident(ident);
+        double pratio = boltz * cfg.staple_M;
+        pratio /= 6.0 * ni;
+        pratio /= (double)S * f;
+        return exchange_accept_common(ident, pratio);
+    }
+
+    bool learned_delete() {
+        int S = (int)cfg.identities.size() - 1;
+        int ident = rng.uniform_int(1, S);
+        int n = num_staples_of_ident(ident);
+        if (n == 0) {
+            rejected = true;
+            return false;
+        }
+        int c_i = ident_to_index[ident][rng.uniform_int(0, n - 1)];
+        std::vector<int> st = get_chain(c_i);
+        if (staple_is_connector(st)) return false;
+        for (int id : st)
+            if (doms[id].state == BOUND) { staple_bound = true; break; }
+        std::vector<std::pair<int, int>> alt;   // (domain index, partner)
+        for (size_t d = 0; d < st.size(); ++d) {
+            int p = doms[st[d]].bound;
+            if (p < 0 || doms[p].c == c_i) continue;
+            alt.push_back({(int)d, p});
+        }
+        unassign_domains(st);
+        if (cfg.mean_field) delta_e -= std::log(6);
+        delta_e -= tab.init_e;
+        num_staples--;
+        add_external_bias_met();
+        num_staples++;
+        double boltz = std::exp(-delta_e);
+        int n_sites = insertion_sites - (int)st.size();
+        double z = learn_z(c_i);
+        double f = 0;
+        for (auto& a : alt) f += learn_q_target(a.second, z, n_sites, -1) * learn_q_type(a.second, ident, a.first);
+        int ni = num_staples_of_ident(ident);
+        double pratio = (double)ni * 6.0 * boltz;
+        pratio *= (double)S * f;
+        pratio /= cfg.staple_M;
+        bool acc = exchange_accept_common(ident, pratio);
+        if (acc) delete_chain(c_i);
+        return acc;
+    }
+
+    bool learned_exchange() {
+        insertion_sites = num_domains;
+        staple_bound = false;
+        if (rng.uniform_real() < 0.5) return learned_insert();
+        return learned_delete();
+    }
+
     // MetStapleRegrowthMCMovetype (src/met_movetypes.cpp:470)
     bool met_regrowth() {
         if (num_staples == 0) return false;
@@ -1587,6 +1770,7 @@ class System {
         case MV_MET_EXCHANGE: acc = met_exchange(); break;
         case MV_MET_REGROWTH: acc = met_regrowth(); break;
         case MV_CB_REGROWTH: acc = cb_regrowth(); break;
+        case MV_LEARNED_EXCHANGE: acc = learned_exchange(); break;
         }
         attempts[m]++;
         if (acc) accepts[m]++;

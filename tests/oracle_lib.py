@@ -166,3 +166,31 @@ def set_window(rep, tag, min_op, max_op):
     L.oracle_set_window.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
     if L.oracle_set_window(rep.h, tag.encode(), min_op, max_op) != 0:
         raise OracleError(L.oracle_last_error().decode())
+
+
+def run_batch_states(inp, seed, n_rep, burn, gap, n_snaps, threads, overrides="", learn_w=None):
+    """Independent replicas; (staples, fully bound) at n_snaps snapshots after
+    burn steps, gap steps apart: int32[n_rep, n_snaps, 2]."""
+    L = lib()
+    L.oracle_run_batch_states.restype = ctypes.c_int
+    L.oracle_run_batch_states.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_int,
+                                          ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_void_p, ctypes.c_void_p]
+    out = np.zeros((n_rep, n_snaps, 2), np.int32)
+    w = None
+    if learn_w is not None:
+        w = np.ascontiguousarray(learn_w, np.float64)
+    rc = L.oracle_run_batch_states(os.fsencode(inp), overrides.encode(), seed, n_rep, burn, gap, n_snaps, threads,
+                                   w.ctypes.data if w is not None else None, out.ctypes.data)
+    if rc != 0:
+        raise OracleError(L.oracle_last_error().decode() or "oracle batch failed")
+    return out
+
+
+def set_learn_table(rep, w):
+    L = rep.L
+    L.oracle_set_learn_table.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    w = np.ascontiguousarray(w, np.float64)
+    rep._learn_w = w
+    if L.oracle_set_learn_table(rep.h, w.ctypes.data, len(w)) != 0:
+        raise OracleError(L.oracle_last_error().decode())
