@@ -1,18 +1,22 @@
-"""Benchmark of the batched plain-MC workload (4096 independent constant-T
-chains of uneven size) on one GB300.
+"""Benchmark of the batched MC workload (4096 independent constant-T chains
+of uneven size) on one GB300: learned-proposal MC against plain MC.
 
 Workload: scaffolds of 8/12/16/24 domains (1024 replicas each, serpentine
 layout, n/2 two-domain staple types), uniform hybridisation dH = -120 kcal/mol
 and dS = -0.33 kcal/mol/K per bound domain, T ~ U[320, 350] K (seeded),
-1 uM staples, FourBody, Opposing misbinding, constant stacking 1000 K, the
-Met exchange / Met regrowth / CB regrowth moveset at 1/3 each.  Philox seeds:
-replica r uses key (0, r).  Inputs are synthetic (tests/systems.py).
+1 uM staples, FourBody, Opposing misbinding, constant stacking 1000 K.  Plain
+moveset: Met exchange / Met regrowth / CB regrowth at 1/3 each; learned
+moveset: the exchange replaced by LearnedStapleExchange, whose network is
+trained (on the GPU) on states of the plain run.  Philox seeds: replica r uses
+key (0, r).  Inputs are synthetic (tests/systems.py).
 
 A step is one launch of SWEEPS sweeps of every replica (a sweep = n_scaffold
 move attempts).  `value` is effective samples per second of the number of
 fully bound domains (one sample per replica per sweep, tau_int by Sokal
-windowing), from the device-timed region; `e2e` repeats the timed loop through
-the C ABI with host buffers (temperatures in, samples out every step)."""
+windowing) of the learned moveset, from the device-timed region; `plain`
+holds the same figures for the plain moveset; `e2e` repeats the timed loop
+through the C ABI with host buffers (temperatures in, samples out every step).
+"""
 import argparse
 import json
 import os
@@ -113,6 +117,20 @@ def measured_peaks():
 
 
 CPU_REPS_PER_SIZE = 128
+LEARN_ITERS = 400
+LEARN_LR = 2e-3
+
+
+def write_learned_moves(d):
+    """The c2 moveset with the staple exchange replaced by the learned one."""
+    p = os.path.join(d, "moves_learned.json")
+    with open(p, "w") as f:
+        json.dump({"origami": {"movetypes": [
+            {"label": "Learned staple exchange", "type": "LearnedStapleExchange", "freq": "1/3",
+             "adaptive_exchange": False},
+            {"label": "Met staple regrowth", "type": "MetStapleRegrowth", "freq": "1/3"},
+            {"label": "CB staple regrowth", "type": "CBStapleRegrowth", "freq": "1/3"}]}}, f)
+    return p
 
 
 def replica_temps():
@@ -177,12 +195,13 @@ def run_reference_arm(args):
         sps.append(s_)
         taus.append(tau)
     value = float(np.mean(rates))
-    line = {"impl": "reference", "metric": "effective samples/s (tau_int of #bound domains), plain MC",
+    line = {"impl": "reference", "metric": "effective samples/s (tau_int of #bound domains), learned vs plain MC",
             "value": value, "unit": "effective samples/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(times)), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "c2: constant-T chains, scaffolds 8/12/16/24, uniform hyb, T~U[320,350] K; "
-                                   "bounded CPU sample per step"},
+                                   "bounded CPU sample per step; plain moveset (the reference has no learned "
+                                   "proposal)"},
             "cpu_baseline": {"value": value, "unit": "effective samples/s", "cores": cores, "kind": "port",
                              "sample": "%d replicas of each scaffold size (GPU-run temperatures) x %d recorded "
                                        "sweeps after %d burn-in per step" % (CPU_REPS_PER_SIZE, rec, burn)},
@@ -206,62 +225,100 @@ def main():
             run_reference_arm(args)
         return
     from latticednaorigami_gb300 import Engine
+    from latticednaorigami_gb300.analysis import effective_samples, tau_int
 
     tmp = tempfile.mkdtemp()
     files = write_c2(tmp)
+    learned_over = "movetype_file = %s" % write_learned_moves(tmp)
     per = N_REP // len(SIZES)
     sys_of = np.repeat(np.arange(len(SIZES)), per)
     temps = replica_temps()
-    eng = Engine(files, n_replicas=N_REP, seed=0, sys_of_replica=sys_of.tolist(), overrides="")
-    eng.set_controls(temps=temps)
     ns_of = np.array(SIZES)[sys_of]
     total_sweeps = args.steps * SWEEPS_PER_STEP
-    eng.set_sampling(1, total_sweeps)   # one sample per sweep
-    # warmup: run, then restart the sample ring
-    for _ in range(args.warmup):
-        eng.run_sweeps(SWEEPS_PER_STEP)
-    eng.set_sampling(1, total_sweeps)
-    clocks = ClockSampler()
-    clocks.start()
-    dev_ms = []
-    for _ in range(args.steps):
-        dev_ms.append(eng.run_sweeps(SWEEPS_PER_STEP))
-    clk = clocks.stop()
-    t_dev = sum(dev_ms) / 1000.0
-    smp, cnt = eng.samples()
-    series = [smp[r, :cnt[r], 0] for r in range(N_REP)]
-    from latticednaorigami_gb300.analysis import effective_samples, tau_int
-    ess, tau_med = effective_samples(series)
-    taus_per_size = {}
-    for i, n in enumerate(SIZES):
-        ts = [tau_int(series[r]) for r in range(i * per, (i + 1) * per)]
-        ts = [t for t in ts if t is not None]
-        taus_per_size[n] = float(np.median(ts)) if ts else None
-    value = ess / t_dev
-    sweeps_per_s = N_REP * total_sweeps / t_dev
-    moves_per_s = float(np.sum(ns_of)) * total_sweeps / t_dev
 
-    # e2e through the C ABI with host buffers: temperatures in, samples out
-    eng2 = Engine(files, n_replicas=N_REP, seed=1, sys_of_replica=sys_of.tolist())
-    eng2.set_controls(temps=temps)
-    eng2.set_sampling(1, SWEEPS_PER_STEP)
-    for _ in range(args.warmup):
-        eng2.run_sweeps(SWEEPS_PER_STEP)
-    e2e_series = [[] for _ in range(N_REP)]
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
+    def timed_arm(overrides, table, collect):
+        """W warm-up launches, then K timed launches of SWEEPS_PER_STEP sweeps
+        with one numfulldomains sample per replica per sweep."""
+        eng = Engine(files, n_replicas=N_REP, seed=0, sys_of_replica=sys_of.tolist(), overrides=overrides)
+        eng.set_controls(temps=temps)
+        if table is not None:
+            eng.learn_set_table(table)
+        eng.set_sampling(1, total_sweeps)
+        for _ in range(args.warmup):
+            eng.run_sweeps(SWEEPS_PER_STEP)
+        eng.set_sampling(1, total_sweeps)
+        clocks = ClockSampler()
+        clocks.start()
+        dev_ms = [eng.run_sweeps(SWEEPS_PER_STEP) for _ in range(args.steps)]
+        clk = clocks.stop()
+        t_dev = sum(dev_ms) / 1000.0
+        smp, cnt = eng.samples()
+        series = [smp[r, :cnt[r], 0] for r in range(N_REP)]
+        ess, tau_med = effective_samples(series)
+        taus = {}
+        for i, n in enumerate(SIZES):
+            ts = [tau_int(series[r]) for r in range(i * per, (i + 1) * per)]
+            ts = [t for t in ts if t is not None]
+            taus[n] = float(np.median(ts)) if ts else None
+        hists = [np.bincount(np.concatenate(series[i * per:(i + 1) * per]).astype(np.int64), minlength=2 * n + 1)
+                 for i, n in enumerate(SIZES)]
+        train = None
+        if collect:
+            # training data for the proposal network from the plain sampler (untimed)
+            for _ in range(10):
+                eng.run_sweeps(10)
+                eng.learn_collect()
+            t0 = time.perf_counter()
+            loss0, loss1 = eng.learn_train(LEARN_ITERS, lr=LEARN_LR, seed=0)
+            train = {"loss_first": loss0, "loss_last": loss1, "iters": LEARN_ITERS,
+                     "train_s": time.perf_counter() - t0, "table": eng.learn_table()}
+        return {"eng": eng, "dev_ms": dev_ms, "t_dev": t_dev, "ess": ess, "tau_med": tau_med, "taus": taus,
+                "clk": clk, "hists": hists, "train": train}
+
+    def e2e_arm(overrides, table):
+        """The same loop through the C ABI with host buffers: temperatures in,
+        samples out, every step."""
+        eng2 = Engine(files, n_replicas=N_REP, seed=1, sys_of_replica=sys_of.tolist(), overrides=overrides)
         eng2.set_controls(temps=temps)
+        if table is not None:
+            eng2.learn_set_table(table)
         eng2.set_sampling(1, SWEEPS_PER_STEP)
-        eng2.run_sweeps(SWEEPS_PER_STEP)
-        s2, c2 = eng2.samples()
-        for r in range(N_REP):
-            e2e_series[r].append(s2[r, :c2[r], 0])
-    t_e2e = time.perf_counter() - t0
-    e2e_ess, _ = effective_samples([np.concatenate(x) for x in e2e_series])
+        for _ in range(args.warmup):
+            eng2.run_sweeps(SWEEPS_PER_STEP)
+        e2e_series = [[] for _ in range(N_REP)]
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            eng2.set_controls(temps=temps)
+            eng2.set_sampling(1, SWEEPS_PER_STEP)
+            eng2.run_sweeps(SWEEPS_PER_STEP)
+            s2, c2 = eng2.samples()
+            for r in range(N_REP):
+                e2e_series[r].append(s2[r, :c2[r], 0])
+        t_e2e = time.perf_counter() - t0
+        e2e_ess, _ = effective_samples([np.concatenate(x) for x in e2e_series])
+        return e2e_ess / t_e2e
+
+    plain = timed_arm("", None, collect=True)
+    table = plain["train"]["table"]
+    learned = timed_arm(learned_over, table, collect=False)
+    value = learned["ess"] / learned["t_dev"]
+    plain_value = plain["ess"] / plain["t_dev"]
+    e2e_learned = e2e_arm(learned_over, table)
+    e2e_plain = e2e_arm("", None)
     h2d = N_REP * 8
     d2h = N_REP * SWEEPS_PER_STEP * 2 * 2
 
+    def kl(p, q):
+        p = p / p.sum()
+        q = (q + 0.5) / (q + 0.5).sum()
+        m = p > 0
+        return float(np.sum(p[m] * np.log(p[m] / q[m])))
+
+    kls = {n: kl(plain["hists"][i].astype(float), learned["hists"][i].astype(float)) for i, n in enumerate(SIZES)}
+
     # roofline of the MC kernel: algorithmic DRAM bytes = state in + out + samples
+    eng = learned["eng"]
+    dev_ms = learned["dev_ms"]
     lay_bytes = eng.state_bytes()
     alg_bytes = N_REP * lay_bytes * 2 + N_REP * SWEEPS_PER_STEP * 4
     achieved = alg_bytes / (np.mean(dev_ms) / 1000.0) / 1e9
@@ -271,22 +328,38 @@ def main():
     if os.path.exists(tp):
         with open(tp) as f:
             traffic = json.load(f).get("dram_bytes_per_launch")
-    line = {"metric": "effective samples/s (tau_int of #bound domains), plain MC", "value": value,
+
+    def rates(arm):
+        t = arm["t_dev"]
+        return {"value": arm["ess"] / t, "sweeps_per_s": N_REP * total_sweeps / t,
+                "move_attempts_per_s": float(np.sum(ns_of)) * total_sweeps / t,
+                "ms_per_step": float(np.mean(arm["dev_ms"])), "tau_int_median": arm["tau_med"],
+                "tau_int_by_size": arm["taus"]}
+
+    tr = plain["train"]
+    line = {"metric": "effective samples/s (tau_int of #bound domains), learned vs plain MC", "value": value,
             "unit": "effective samples/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": float(np.mean(dev_ms)), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "c2: 4096 constant-T chains, scaffolds 8/12/16/24 (1024 each), uniform hyb "
-                                   "dH=-120 kcal/mol dS=-0.33 kcal/mol/K, T~U[320,350] K, 1 uM, Met exchange/"
-                                   "regrowth + CB regrowth", "sweeps_per_step": SWEEPS_PER_STEP,
-                       "replicas": N_REP, "l2": "state resident in shared memory; no L2 flush needed"},
-            "sweeps_per_s": sweeps_per_s, "move_attempts_per_s": moves_per_s, "tau_int_median": tau_med,
-            "tau_int_by_size": taus_per_size,
-            "e2e": {"value": e2e_ess / t_e2e, "unit": "effective samples/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                                   "dH=-120 kcal/mol dS=-0.33 kcal/mol/K, T~U[320,350] K, 1 uM; moveset "
+                                   "learned staple exchange + Met regrowth + CB regrowth (value) vs Met "
+                                   "exchange + Met regrowth + CB regrowth (plain)",
+                       "sweeps_per_step": SWEEPS_PER_STEP, "replicas": N_REP,
+                       "l2": "state resident in shared memory; no L2 flush needed"},
+            "learned": rates(learned), "plain": rates(plain),
+            "learned_over_plain": value / plain_value,
+            "kl_plain_learned_by_size": kls,
+            "network": {"layers": "64-256-256-256-1 GELU, bf16 weights/activations, fp32 accumulation",
+                        "train_iters": tr["iters"], "loss_first": tr["loss_first"], "loss_last": tr["loss_last"],
+                        "train_s": tr["train_s"]},
+            "sweeps_per_s": rates(learned)["sweeps_per_s"],
+            "e2e": {"value": e2e_learned, "unit": "effective samples/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "plain_value": e2e_plain},
             "gpu_launches": args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind},
-            "clocks": clk}
+            "clocks": learned["clk"], "clocks_plain": plain["clk"]}
     if not args.no_cpu and rank == 0:
         line["cpu_baseline"] = cpu_baseline(files, args.warmup * SWEEPS_PER_STEP, total_sweeps)
     print(json.dumps(line))
