@@ -126,3 +126,44 @@ def test_trained_network_gains_over_plain_and_untrained():
           % (plain, untrained, trained))
     assert trained > 2 * plain
     assert trained > untrained
+
+
+def test_learned_distribution_matches_plain_on_c2():
+    """KL divergence between the bound-domain distributions of plain and
+    learned-proposal MC on the 12-domain c2 system (both relaxed from the
+    empty start for 4000 sweeps, then 4000 sweeps sampled every 10)."""
+    import bench
+    d = tempfile.mkdtemp()
+    f = bench.write_c2(d)[1]
+    over = "movetype_file = %s" % learned_moves(d)
+    n = 1024
+    temps = np.linspace(320.0, 350.0, n)
+    eng = engine(f, n_replicas=n, seed=5)
+    eng.set_controls(temps=temps)
+    eng.run_sweeps(200)
+    for _ in range(10):
+        eng.run_sweeps(10)
+        eng.learn_collect()
+    eng.learn_train(300, lr=2e-3, seed=0)
+    table = eng.learn_table()
+
+    def hist(overrides, tab, seed):
+        e = engine(f, n_replicas=n, seed=seed, overrides=overrides)
+        e.set_controls(temps=temps)
+        if tab is not None:
+            e.learn_set_table(tab)
+        for _ in range(4):
+            e.run_sweeps(1000)
+        e.set_sampling(10, 400)
+        for _ in range(4):
+            e.run_sweeps(1000)
+        smp, cnt = e.samples()
+        return np.bincount(np.concatenate([smp[r, :cnt[r], 0] for r in range(n)]).astype(np.int64), minlength=25)
+
+    hp = hist("", None, 6).astype(float)
+    hl = hist(over, table, 7).astype(float)
+    p, q = hp / hp.sum(), (hl + 0.5) / (hl + 0.5).sum()
+    m = p > 0
+    kl = float(np.sum(p[m] * np.log(p[m] / q[m])))
+    print("KL(plain || learned) = %.5f" % kl)
+    assert kl < 0.01, kl
