@@ -777,7 +777,13 @@ struct ldo_engine {
         CU(ldo_mlp_loss_grad(mlp, n, norm, stream));
         if (loss1) CU(cudaMemcpyAsync(loss1, mlp.loss, sizeof(double), cudaMemcpyDeviceToHost, stream));
         CU(ldo_mlp_table(mlp, d_learn_w.p, stream));
-        CU(cudaStreamSynchronize(stream));
+        mlp_check();
+    }
+
+    void mlp_check() {
+        bool timed_out = false;
+        CU(ldo_mlp_check(mlp, stream, &timed_out));
+        if (timed_out) throw LdoError(LDO_ECUDA, "network product: a tensor-core completion wait ran out");
     }
 
     // PTGCMCSimulation constructor + OneDPTGCMCSimulation::initialize_control_qs
@@ -1591,7 +1597,7 @@ ldo_status ldo_learn_set_params(ldo_engine* e, const float* params, int n) {
         CU(cudaMemcpy(e->mlp.params, params, n * sizeof(float), cudaMemcpyHostToDevice));
         CU(ldo_mlp_sync_weights(e->mlp, e->stream));
         CU(ldo_mlp_table(e->mlp, e->d_learn_w.p, e->stream));
-        CU(cudaStreamSynchronize(e->stream));
+        e->mlp_check();
     });
 }
 
@@ -1631,6 +1637,9 @@ ldo_status ldo_learn_loss_grad(const float* params, const int32_t* idx, const fl
         CU(cudaMemcpy(m.cnt_t, cnt_total, n * sizeof(float), cudaMemcpyHostToDevice));
         CU(ldo_mlp_sync_weights(m, 0));
         CU(ldo_mlp_loss_grad(m, n, norm, 0));
+        bool timed_out = false;
+        CU(ldo_mlp_check(m, 0, &timed_out));
+        if (timed_out) throw LdoError(LDO_ECUDA, "network product: a tensor-core completion wait ran out");
         CU(cudaMemcpy(loss, m.loss, sizeof(double), cudaMemcpyDeviceToHost));
         CU(cudaMemcpy(grad, m.grad, LDO_LEARN_NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
     });

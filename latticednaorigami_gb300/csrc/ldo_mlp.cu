@@ -1,25 +1,33 @@
 // Kernels of the learned-proposal network (ldo_mlp.h).
 //
-// Matrix products run on the tensor cores as bf16 x bf16 -> fp32 warp MMAs
-// (m16n8k16) over 64x64 output tiles staged through shared memory; every
-// other step (bias, GELU and its derivative, the 256 -> 1 output layer, the
-// loss, column sums, Adam) is an elementwise or reduction kernel in fp32.
+// Matrix products run on the 5th-generation tensor cores (ldo_umma.cuh:
+// tcgen05.mma, operands staged in shared memory, fp32 accumulators in tensor
+// memory) as C = A * B^T with both operands K-major; the weight copies are
+// kept in both orientations and the backward pass transposes activations and
+// gradients for the weight-gradient products.  Every other step (bias, GELU
+// and its derivative, the 256 -> 1 output layer, the loss, column sums, Adam)
+// is an elementwise or reduction kernel in fp32.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "ldo_mlp.h"
+#include "ldo_umma.cuh"
 
 namespace {
 
 constexpr int H = LDO_LEARN_H;
 constexpr int DIN = LDO_LEARN_DIN;
-// bf16 weight copies: W1 [DIN][H], W2 [H][H], W3 [H][H], w4 [H]
+// bf16 weight copies: W1 [DIN][H], W2 [H][H], W3 [H][H], w4 [H], and the
+// transposes W1t [H][DIN], W2t, W3t (K-major operands of the forward products)
 constexpr int BF_W1 = 0;
 constexpr int BF_W2 = BF_W1 + DIN * H;
 constexpr int BF_W3 = BF_W2 + H * H;
 constexpr int BF_W4 = BF_W3 + H * H;
-constexpr int BF_N = BF_W4 + H;
+constexpr int BF_W1T = BF_W4 + H;
+constexpr int BF_W2T = BF_W1T + DIN * H;
+constexpr int BF_W3T = BF_W2T + H * H;
+constexpr int BF_N = BF_W3T + H * H;
 
 __device__ __forceinline__ uint16_t f2bf(float f) {
     __nv_bfloat16 b = __float2bfloat16_rn(f);
@@ -29,102 +37,30 @@ __device__ __forceinline__ float bf2f(uint16_t u) {
     return __uint_as_float(((unsigned)u) << 16);
 }
 
-// ---------------------------------------------------------------- GEMM ---
-// C[M][N] (fp32, row-major) = op(A) * op(B), bf16 operands.
-// TA = 0: A is [M][K] row-major; TA = 1: A is stored [K][M] row-major.
-// TB = 0: B is [K][N] row-major; TB = 1: B is stored [N][K] row-major.
-constexpr int GT_M = 64, GT_N = 64, GT_K = 32, GT_PAD = 8;
-
-template <int TA, int TB>
-__global__ void __launch_bounds__(128) gemm_bf16_kernel(const uint16_t* __restrict__ A, const uint16_t* __restrict__ B,
-                                                        float* __restrict__ C, int M, int N, int K) {
-    __shared__ __align__(16) uint16_t As[GT_M][GT_K + GT_PAD];   // [m][k]
-    __shared__ __align__(16) uint16_t Bs[GT_N][GT_K + GT_PAD];   // [n][k]
-    int tid = threadIdx.x;
-    int warp = tid >> 5, lane = tid & 31;
-    int g = lane >> 2, c = lane & 3;
-    int m0 = blockIdx.y * GT_M, n0 = blockIdx.x * GT_N;
-    int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-    float acc[2][4][4];
-    #pragma unroll
-    for (int i = 0; i < 2; ++i)
-        #pragma unroll
-        for (int j = 0; j < 4; ++j)
-            #pragma unroll
-            for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
-
-    for (int k0 = 0; k0 < K; k0 += GT_K) {
-        // stage the A and B tiles (consecutive threads read consecutive addresses)
-        for (int e = tid; e < GT_M * GT_K; e += 128) {
-            int m, k;
-            if (TA == 0) { m = e / GT_K; k = e % GT_K; }
-            else { k = e / GT_M; m = e % GT_M; }
-            int gm = m0 + m, gk = k0 + k;
-            uint16_t v = 0;
-            if (gm < M && gk < K) v = TA == 0 ? A[(size_t)gm * K + gk] : A[(size_t)gk * M + gm];
-            As[m][k] = v;
-        }
-        for (int e = tid; e < GT_N * GT_K; e += 128) {
-            int n, k;
-            if (TB == 0) { k = e / GT_N; n = e % GT_N; }
-            else { n = e / GT_K; k = e % GT_K; }
-            int gn = n0 + n, gk = k0 + k;
-            uint16_t v = 0;
-            if (gn < N && gk < K) v = TB == 0 ? B[(size_t)gk * N + gn] : B[(size_t)gn * K + gk];
-            Bs[n][k] = v;
-        }
-        __syncthreads();
-        #pragma unroll
-        for (int kk = 0; kk < GT_K; kk += 16) {
-            uint32_t af[2][4], bfr[4][2];
-            #pragma unroll
-            for (int i = 0; i < 2; ++i) {
-                int r = wm + i * 16 + g;
-                af[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][kk + 2 * c]);
-                af[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + 2 * c]);
-                af[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][kk + 8 + 2 * c]);
-                af[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + 8 + 2 * c]);
-            }
-            #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                int n = wn + j * 8 + g;
-                bfr[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[n][kk + 2 * c]);
-                bfr[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[n][kk + 8 + 2 * c]);
-            }
-            #pragma unroll
-            for (int i = 0; i < 2; ++i)
-                #pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    asm volatile(
-                        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-                        "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-                        : "+f"(acc[i][j][0]), "+f"(acc[i][j][1]), "+f"(acc[i][j][2]), "+f"(acc[i][j][3])
-                        : "r"(af[i][0]), "r"(af[i][1]), "r"(af[i][2]), "r"(af[i][3]), "r"(bfr[j][0]),
-                          "r"(bfr[j][1]));
-        }
-        __syncthreads();
-    }
-    #pragma unroll
-    for (int i = 0; i < 2; ++i)
-        #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            int r = m0 + wm + i * 16 + g;
-            int col = n0 + wn + j * 8 + 2 * c;
-            if (r < M) {
-                if (col < N) C[(size_t)r * N + col] = acc[i][j][0];
-                if (col + 1 < N) C[(size_t)r * N + col + 1] = acc[i][j][1];
-            }
-            if (r + 8 < M) {
-                if (col < N) C[(size_t)(r + 8) * N + col] = acc[i][j][2];
-                if (col + 1 < N) C[(size_t)(r + 8) * N + col + 1] = acc[i][j][3];
-            }
-        }
+// ---------------------------------------------------------- products ---
+// C[M][N] = A[M][K] * Bt[N][K]^T on the tensor cores
+cudaError_t tn(const uint16_t* A, const uint16_t* Bt, float* C, int M, int N, int K, int* err, cudaStream_t s) {
+    return ldo_umma::gemm_tn(A, Bt, C, M, N, K, err, s);
 }
 
-template <int TA, int TB>
-cudaError_t gemm(const uint16_t* A, const uint16_t* B, float* C, int M, int N, int K, cudaStream_t s) {
-    dim3 grid((N + GT_N - 1) / GT_N, (M + GT_M - 1) / GT_M);
-    gemm_bf16_kernel<TA, TB><<<grid, 128, 0, s>>>(A, B, C, M, N, K);
+// dst[C][R] = src[R][C] (bf16), 32 x 32 tiles through shared memory
+__global__ void transpose_kernel(const uint16_t* __restrict__ src, uint16_t* __restrict__ dst, int R, int C) {
+    __shared__ uint16_t t[32][33];
+    int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        int r = r0 + i, c = c0 + threadIdx.x;
+        if (r < R && c < C) t[i][threadIdx.x] = src[(size_t)r * C + c];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        int c = c0 + i, r = r0 + threadIdx.x;
+        if (r < R && c < C) dst[(size_t)c * R + r] = t[threadIdx.x][i];
+    }
+}
+
+cudaError_t transpose(const uint16_t* src, uint16_t* dst, int R, int C, cudaStream_t s) {
+    dim3 grid((C + 31) / 32, (R + 31) / 32), block(32, 8);
+    transpose_kernel<<<grid, block, 0, s>>>(src, dst, R, C);
     return cudaGetLastError();
 }
 
@@ -222,17 +158,20 @@ __global__ void colsum_kernel(const float* dz, int n, float* gb) {
     atomicAdd(&gb[j], s);
 }
 
-__global__ void add_kernel(float* dst, const float* src, int n) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < n) dst[e] += src[e];
-}
-
 __global__ void to_bf16_kernel(const float* p, uint16_t* wbf) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < DIN * H) wbf[BF_W1 + e] = f2bf(p[LDO_LEARN_OFF_W1 + e]);
+    if (e < DIN * H) {
+        uint16_t v = f2bf(p[LDO_LEARN_OFF_W1 + e]);
+        wbf[BF_W1 + e] = v;
+        wbf[BF_W1T + (e % H) * DIN + e / H] = v;
+    }
     if (e < H * H) {
-        wbf[BF_W2 + e] = f2bf(p[LDO_LEARN_OFF_W2 + e]);
-        wbf[BF_W3 + e] = f2bf(p[LDO_LEARN_OFF_W3 + e]);
+        uint16_t v2 = f2bf(p[LDO_LEARN_OFF_W2 + e]);
+        uint16_t v3 = f2bf(p[LDO_LEARN_OFF_W3 + e]);
+        wbf[BF_W2 + e] = v2;
+        wbf[BF_W3 + e] = v3;
+        wbf[BF_W2T + (e % H) * H + e / H] = v2;
+        wbf[BF_W3T + (e % H) * H + e / H] = v3;
     }
     if (e < H) wbf[BF_W4 + e] = f2bf(p[LDO_LEARN_OFF_W4 + e]);
 }
@@ -294,6 +233,10 @@ cudaError_t ldo_mlp_alloc(LdoMlp& m, int cap) {
     }
     MLP_CU(dalloc(&m.dz, (size_t)cap * H));
     MLP_CU(dalloc(&m.gbf, (size_t)cap * H));
+    MLP_CU(dalloc(&m.ht, (size_t)cap * H));
+    MLP_CU(dalloc(&m.gt, (size_t)cap * H));
+    MLP_CU(dalloc(&m.err, 1));
+    MLP_CU(cudaMemset(m.err, 0, sizeof(int)));
     MLP_CU(dalloc(&m.out, cap));
     MLP_CU(dalloc(&m.dout, cap));
     MLP_CU(dalloc(&m.loss, 1));
@@ -305,7 +248,7 @@ cudaError_t ldo_mlp_alloc(LdoMlp& m, int cap) {
 
 void ldo_mlp_free(LdoMlp& m) {
     void* ps[] = {m.params, m.grad, m.adam_m, m.adam_v, m.wbf, m.idx, m.cnt_b, m.cnt_t, m.x, m.z[0], m.z[1], m.z[2],
-                  m.h[0], m.h[1], m.h[2], m.dz, m.gbf, m.out, m.dout, m.loss};
+                  m.h[0], m.h[1], m.h[2], m.dz, m.gbf, m.ht, m.gt, m.err, m.out, m.dout, m.loss};
     for (void* p : ps)
         if (p) cudaFree(p);
     m = LdoMlp {};
@@ -321,11 +264,11 @@ cudaError_t ldo_mlp_forward(LdoMlp& m, int n, cudaStream_t s) {
     build_x_kernel<<<blocks_for(n, 128), 128, 0, s>>>(m.idx, n, m.x);
     MLP_CU(cudaGetLastError());
     // layer 1: [n][64] x [64][256]
-    MLP_CU((gemm<0, 0>(m.x, m.wbf + BF_W1, m.z[0], n, H, DIN, s)));
+    MLP_CU(tn(m.x, m.wbf + BF_W1T, m.z[0], n, H, DIN, m.err, s));
     bias_gelu_kernel<<<blocks_for(tot, 256), 256, 0, s>>>(m.z[0], m.params + LDO_LEARN_OFF_B1, m.h[0], tot);
-    MLP_CU((gemm<0, 0>(m.h[0], m.wbf + BF_W2, m.z[1], n, H, H, s)));
+    MLP_CU(tn(m.h[0], m.wbf + BF_W2T, m.z[1], n, H, H, m.err, s));
     bias_gelu_kernel<<<blocks_for(tot, 256), 256, 0, s>>>(m.z[1], m.params + LDO_LEARN_OFF_B2, m.h[1], tot);
-    MLP_CU((gemm<0, 0>(m.h[1], m.wbf + BF_W3, m.z[2], n, H, H, s)));
+    MLP_CU(tn(m.h[1], m.wbf + BF_W3T, m.z[2], n, H, H, m.err, s));
     bias_gelu_kernel<<<blocks_for(tot, 256), 256, 0, s>>>(m.z[2], m.params + LDO_LEARN_OFF_B3, m.h[2], tot);
     out_layer_kernel<<<blocks_for((long long)n * 32, 256), 256, 0, s>>>(m.h[2], m.wbf + BF_W4,
                                                                        m.params + LDO_LEARN_OFF_B4, m.out, n);
@@ -344,17 +287,23 @@ cudaError_t ldo_mlp_loss_grad(LdoMlp& m, int n, double norm, cudaStream_t s) {
     MLP_CU(cudaGetLastError());
     // layer 3: dW3 = h2^T g3 ; db3 = colsum ; dh2 = g3 W3^T
     colsum_kernel<<<rb, H, 0, s>>>(m.dz, n, m.grad + LDO_LEARN_OFF_B3);
-    MLP_CU((gemm<1, 0>(m.h[1], m.gbf, m.grad + LDO_LEARN_OFF_W3, H, H, n, s)));
-    MLP_CU((gemm<0, 1>(m.gbf, m.wbf + BF_W3, m.dz, n, H, H, s)));
+    MLP_CU(transpose(m.h[1], m.ht, n, H, s));
+    MLP_CU(transpose(m.gbf, m.gt, n, H, s));
+    MLP_CU(tn(m.ht, m.gt, m.grad + LDO_LEARN_OFF_W3, H, H, n, m.err, s));
+    MLP_CU(tn(m.gbf, m.wbf + BF_W3, m.dz, n, H, H, m.err, s));
     gelu_back_kernel<<<blocks_for(tot, 256), 256, 0, s>>>(m.dz, m.z[1], m.gbf, tot);
     // layer 2
     colsum_kernel<<<rb, H, 0, s>>>(m.dz, n, m.grad + LDO_LEARN_OFF_B2);
-    MLP_CU((gemm<1, 0>(m.h[0], m.gbf, m.grad + LDO_LEARN_OFF_W2, H, H, n, s)));
-    MLP_CU((gemm<0, 1>(m.gbf, m.wbf + BF_W2, m.dz, n, H, H, s)));
+    MLP_CU(transpose(m.h[0], m.ht, n, H, s));
+    MLP_CU(transpose(m.gbf, m.gt, n, H, s));
+    MLP_CU(tn(m.ht, m.gt, m.grad + LDO_LEARN_OFF_W2, H, H, n, m.err, s));
+    MLP_CU(tn(m.gbf, m.wbf + BF_W2, m.dz, n, H, H, m.err, s));
     gelu_back_kernel<<<blocks_for(tot, 256), 256, 0, s>>>(m.dz, m.z[0], m.gbf, tot);
     // layer 1
     colsum_kernel<<<rb, H, 0, s>>>(m.dz, n, m.grad + LDO_LEARN_OFF_B1);
-    MLP_CU((gemm<1, 0>(m.x, m.gbf, m.grad + LDO_LEARN_OFF_W1, DIN, H, n, s)));
+    MLP_CU(transpose(m.x, m.ht, n, DIN, s));
+    MLP_CU(transpose(m.gbf, m.gt, n, H, s));
+    MLP_CU(tn(m.ht, m.gt, m.grad + LDO_LEARN_OFF_W1, DIN, H, n, m.err, s));
     return cudaGetLastError();
 }
 
@@ -376,5 +325,14 @@ cudaError_t ldo_mlp_table(LdoMlp& m, double* table, cudaStream_t s) {
         table_kernel<<<blocks_for(n, 256), 256, 0, s>>>(m.out, n, table + base);
         MLP_CU(cudaGetLastError());
     }
+    return cudaSuccess;
+}
+
+cudaError_t ldo_mlp_check(LdoMlp& m, cudaStream_t s, bool* timed_out) {
+    int e = 0;
+    MLP_CU(cudaMemcpyAsync(&e, m.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MLP_CU(cudaStreamSynchronize(s));
+    *timed_out = e != 0;
+    if (e) MLP_CU(cudaMemsetAsync(m.err, 0, sizeof(int), s));
     return cudaSuccess;
 }

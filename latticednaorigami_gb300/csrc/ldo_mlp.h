@@ -1,6 +1,6 @@
 // Network of the learned insertion proposal: 64 -> 256 -> 256 -> 256 -> 1,
-// GELU, bf16 weights and activations as tensor-core operands, fp32
-// accumulation and fp32 master weights (Adam).
+// GELU, bf16 weights and activations as tensor-core operands (tcgen05),
+// fp32 accumulation and fp32 master weights (Adam).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -14,7 +14,7 @@ struct LdoMlp {
     float* grad {nullptr};       // [NPARAM]
     float* adam_m {nullptr};
     float* adam_v {nullptr};
-    uint16_t* wbf {nullptr};     // bf16 copies: W1 | W2 | W3 | w4 (same offsets minus biases, see ldo_mlp.cu)
+    uint16_t* wbf {nullptr};     // bf16 weight copies, both orientations (ldo_mlp.cu)
     int32_t* idx {nullptr};      // [cap] table entries of the batch
     float* cnt_b {nullptr};      // [cap] bound counts
     float* cnt_t {nullptr};      // [cap] total counts
@@ -23,6 +23,9 @@ struct LdoMlp {
     uint16_t* h[3] {};           // [cap][256] bf16 activations
     float* dz {nullptr};         // [cap][256] fp32 gradient scratch
     uint16_t* gbf {nullptr};     // [cap][256] bf16 gradient
+    uint16_t* ht {nullptr};      // [256][cap] transposed activation (weight-gradient operand)
+    uint16_t* gt {nullptr};      // [256][cap] transposed gradient
+    int* err {nullptr};          // set if a tensor-core wait ran out (ldo_umma.cuh)
     float* out {nullptr};        // [cap] logits
     float* dout {nullptr};       // [cap]
     double* loss {nullptr};      // [1]
@@ -43,3 +46,6 @@ cudaError_t ldo_mlp_adam(LdoMlp& m, float lr, cudaStream_t s);
 // Weights exp(clamp(logit)) of every table entry (LDO_LEARN_TABLE doubles),
 // evaluated in batches of m.cap.
 cudaError_t ldo_mlp_table(LdoMlp& m, double* table, cudaStream_t s);
+// Synchronises s and reports whether a tensor-core wait ran out since the
+// last check (then the products are incomplete).
+cudaError_t ldo_mlp_check(LdoMlp& m, cudaStream_t s, bool* timed_out);
