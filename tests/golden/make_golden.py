@@ -25,7 +25,7 @@ REF = os.path.join(ROOT, "oracle", "_ref", "ref_trace")
 
 # case, seed, steps
 RUNS = [("c1", 1, 20000), ("c1", 2, 20000), ("g24a", 3, 20000), ("g24b", 4, 20000), ("g24c", 5, 20000),
-        ("g24d", 6, 10000), ("g24e", 7, 20000)]
+        ("g24d", 6, 10000), ("g24e", 7, 20000), ("c3", 8, 10000)]
 
 
 def ref_trace(inp, seed, steps, replica=0):
@@ -78,11 +78,13 @@ def enumerate_c1(tmp):
     print(path, weights)
 
 
-def main():
+def main(only=None):
     if not os.path.exists(REF):
         sys.exit("build the reference first: make -C oracle/ref")
     with tempfile.TemporaryDirectory() as tmp:
         for case, seed, steps in RUNS:
+            if only and case not in only:
+                continue
             inp = systems.write_case(tmp, case)
             d = ref_trace(inp, seed, steps)
             fx = {"case": case, "seed": seed, "steps": steps, "initial_energy": d["initial_energy"],
@@ -91,8 +93,10 @@ def main():
             with gzip.open(path, "wt") as f:
                 json.dump(fx, f)
             print(path, len(d["steps"]), "steps, draws", d["draws"])
-        enumerate_c1(tmp)
+        if not only or "c1" in only:
+            enumerate_c1(tmp)
 
 
 if __name__ == "__main__":
-    main()
+    # python tests/golden/make_golden.py [case ...]   (default: every run)
+    main(sys.argv[1:] or None)

@@ -132,6 +132,9 @@ CASES = {
                                     max_type_staples=4)),
     "g24e": ("grid24", "met3", dict(stacking_ene=-2000, staple_M=1e-2, temp=315, max_total_staples=24,
                                     max_type_staples=3)),
+    # the 48-domain PTMC system's shape: 24 two-domain staple types, NN on random 16-mers, 1 uM
+    "c3": ("grid48", "met3", dict(stacking_ene=1000, staple_M=1e-6, temp=340, max_total_staples=48,
+                                  max_type_staples=2)),
 }
 
 

@@ -15,7 +15,7 @@ from oracle_lib import OracleReplica
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["c1", "g24a", "g24b", "g24c", "g24d", "g24e"]
+CASES = ["c1", "g24a", "g24b", "g24c", "g24d", "g24e", "c3"]
 EXACT = [0, 2, 3, 4, 5, 7]   # step, staples, fully bound, bound, stacked, draws
 
 

@@ -52,6 +52,33 @@ def test_pt_matches_cpu_restatement(q):
         assert abs(obs[r]["energy"] - ob["energy"]) <= 1e-12 * max(1.0, abs(ob["energy"]))
 
 
+def test_pt_48_domain_ladder_matches_cpu_restatement():
+    """The 48-domain PTMC system's shape (nearest-neighbour energies, 24
+    staple types): 8 temperatures geometric over 310-370 K, 2 ladders,
+    temperature exchange every 500 steps."""
+    from pt_oracle import PTOracle
+    temps = [310.0 * (370.0 / 310.0) ** (k / 7.0) for k in range(8)]
+    d = tempfile.mkdtemp()
+    inp = systems.write_case(d, "c3", extra=dict(temps=" ".join(repr(t) for t in temps), num_reps=8,
+                                                   exchange_interval=500))
+    n_ladders, swaps, interval, seed = 2, 8, 500, 41
+    eng = engine(inp, n_replicas=8 * n_ladders, seed=seed)
+    eng.pt_run(8, swaps, interval, 1)
+    ora = PTOracle(inp, dict(temps=temps, chem_pot_mults=[1.0] * 8, temp=340.0, staple_M=1e-6,
+                             staple_lengths=[2] * 24), n_ladders, seed, exchange_q=1)
+    for _ in range(swaps):
+        ora.round(interval)
+    np.testing.assert_array_equal(eng.pt_permutation(), ora.permutation())
+    att, acc = eng.pt_stats(7)
+    assert att.tolist() == ora.att and acc.tolist() == ora.acc
+    obs = eng.observables()
+    for r, rep in enumerate(ora.reps):
+        ob = rep.observables()
+        assert obs[r]["draws"] == ob["draws"]
+        assert obs[r]["num_staples"] == ob["num_staples"]
+        assert abs(obs[r]["energy"] - ob["energy"]) <= 1e-12 * max(1.0, abs(ob["energy"]))
+
+
 def chi2_sf(x, k):
     # survival function of chi-square with k dof (series for the regularised gamma)
     a = k / 2.0
