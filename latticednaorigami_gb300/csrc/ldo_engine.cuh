@@ -1738,8 +1738,9 @@ struct Rep : public LdoState<C> {
     // LearnedStapleExchange: the reference's staple exchange with a proposal
     // for insertion targets learned from the plain sampler.  An insertion
     // picks the growth-point target g with probability
-    //   q(g) = eps / N + (1 - eps) * [g unbound] w(g) / Z,   Z = sum of w over unbound domains
-    // (q = 1/N when Z = 0), w(g) = exp(network logit) of g's neighbourhood
+    //   q(g) = eps / N + (1 - eps) * [g unbound scaffold domain] w(g) / Z,
+    // Z = sum of w over the unbound scaffold domains (q = 1/N when Z = 0),
+    // w(g) = exp(network logit) of g's neighbourhood
     // (ldo_learn.h), then the staple type and domain complementary to g with
     // probability 1 - eps_t (uniform type and domain otherwise).  The forward
     // probability of the new configuration sums q over the staple's bound
@@ -1795,28 +1796,19 @@ struct Rep : public LdoState<C> {
             }
         }
     }
-    // Z over the unbound domains of every chain except `skip`, in chain order.
-    __device__ __noinline__ double learn_z(int skip) const {
+    // Z over the unbound scaffold domains, in scaffold order.
+    __device__ __noinline__ double learn_z() const {
         double z = 0;
-        int nc = hdr.n_chains;
         #pragma unroll 1
-        for (int c = 0; c < nc; ++c) {
-            int cs = chain_order[c];
-            if (cs == skip) continue;
-            int len = chain_len(cs);
-            #pragma unroll 1
-            for (int d = 0; d < len; ++d) {
-                int g = slot_of(cs, d);
-                if (st[g] == UNBOUND) z += learn_weight(g, -1);
-            }
-        }
+        for (int g = 0; g < ns; ++g)
+            if (st[g] == UNBOUND) z += learn_weight(g, -1);
         return z;
     }
     // q(g) for a target that was unbound in the state the proposal is made in.
     __device__ double learn_q_target(int g, double z, int n_sites, int fresh) const {
         if (z == 0) return 1.0 / n_sites;
         double q = LDO_LEARN_EPS / n_sites;
-        q += (1.0 - LDO_LEARN_EPS) * (learn_weight(g, fresh) / z);
+        if (scs[g] == 0) q += (1.0 - LDO_LEARN_EPS) * (learn_weight(g, fresh) / z);
         return q;
     }
     // q(type, domain d | target g)
@@ -1847,7 +1839,7 @@ struct Rep : public LdoState<C> {
     __device__ __noinline__ bool learned_insert() {
         int S = sys->n_types - 1;
         int n_sites = hdr.num_domains;
-        double z = learn_z(-1);
+        double z = learn_z();
         int g = -1;
         double u1 = rng.uniform_real();
         if (z == 0 || u1 < LDO_LEARN_EPS) {
@@ -1857,21 +1849,14 @@ struct Rep : public LdoState<C> {
             double target = rng.uniform_real() * z;
             double cum = 0;
             int last = -1;
-            int nc = hdr.n_chains;
             #pragma unroll 1
-            for (int c = 0; c < nc && g < 0; ++c) {
-                int cs = chain_order[c];
-                int len = chain_len(cs);
-                #pragma unroll 1
-                for (int d = 0; d < len; ++d) {
-                    int x = slot_of(cs, d);
-                    if (st[x] != UNBOUND) continue;
-                    cum += learn_weight(x, -1);
-                    last = x;
-                    if (target < cum) {
-                        g = x;
-                        break;
-                    }
+            for (int x = 0; x < ns; ++x) {
+                if (st[x] != UNBOUND) continue;
+                cum += learn_weight(x, -1);
+                last = x;
+                if (target < cum) {
+                    g = x;
+                    break;
                 }
             }
             if (g < 0) g = last;   // rounding left target >= Z
@@ -1969,7 +1954,7 @@ struct Rep : public LdoState<C> {
         hdr.num_staples++;
         double boltz = dexp(-delta_e);
         int n_sites = insertion_sites - len;
-        double z = learn_z(cs);
+        double z = learn_z();
         double f = 0;
         #pragma unroll 1
         for (int a = 0; a < na; ++a)

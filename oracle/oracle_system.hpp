@@ -1418,19 +1418,16 @@ class System {
         int ts = doms[g].cident == 0 ? ldo_learn_tslot(learn_comp(doms[g].d).first) : 0;
         return learn_w[ldo_learn_index(learn_tb, ts, combo)];
     }
-    double learn_z(int skip_c) const {
+    double learn_z() const {
         double z = 0;
-        for (size_t c = 0; c < chains.size(); ++c) {
-            if (chain_index[c] == skip_c) continue;
-            for (int g : chains[c])
-                if (doms[g].state == UNBOUND) z += learn_weight(g, -1);
-        }
+        for (int g : chains[0])
+            if (doms[g].state == UNBOUND) z += learn_weight(g, -1);
         return z;
     }
     double learn_q_target(int g, double z, int n_sites, int fresh_c) const {
         if (z == 0) return 1.0 / n_sites;
         double q = LDO_LEARN_EPS / n_sites;
-        q += (1.0 - LDO_LEARN_EPS) * (learn_weight(g, fresh_c) / z);
+        if (doms[g].cident == 0) q += (1.0 - LDO_LEARN_EPS) * (learn_weight(g, fresh_c) / z);
         return q;
     }
     double learn_q_type(int g, int type, int d) const {
@@ -1452,7 +1449,7 @@ class System {
         if (!learn_w) throw std::runtime_error("LearnedStapleExchange needs the weight table");
         int S = (int)cfg.identities.size() - 1;
         int n_sites = num_domains;
-        double z = learn_z(-1);
+        double z = learn_z();
         int g = -1;
         double u1 = rng.uniform_real();
         if (z == 0 || u1 < LDO_LEARN_EPS) {
@@ -1462,16 +1459,15 @@ class System {
             double target = rng.uniform_real() * z;
             double cum = 0;
             int last = -1;
-            for (size_t c = 0; c < chains.size() && g < 0; ++c)
-                for (int x : chains[c]) {
-                    if (doms[x].state != UNBOUND) continue;
-                    cum += learn_weight(x, -1);
-                    last = x;
-                    if (target < cum) {
-                        g = x;
-                        break;
-                    }
+            for (int x : chains[0]) {
+                if (doms[x].state != UNBOUND) continue;
+                cum += learn_weight(x, -1);
+                last = x;
+                if (target < cum) {
+                    g = x;
+                    break;
                 }
+            }
             if (g < 0) g = last;
         }
         int ct = 0, cd = 0;
@@ -1548,7 +1544,7 @@ class System {
         num_staples++;
         double boltz = std::exp(-delta_e);
         int n_sites = insertion_sites - (int)st.size();
-        double z = learn_z(c_i);
+        double z = learn_z();
         double f = 0;
         for (auto& a : alt) f += learn_q_target(a.second, z, n_sites, -1) * learn_q_type(a.second, ident, a.first);
         int ni = num_staples_of_ident(ident);
