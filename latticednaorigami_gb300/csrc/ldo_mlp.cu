@@ -42,6 +42,16 @@ __device__ __forceinline__ float bf2f(uint16_t u) {
 cudaError_t tn(const uint16_t* A, const uint16_t* Bt, float* C, int M, int N, int K, int* err, cudaStream_t s) {
     return ldo_umma::gemm_tn(A, Bt, C, M, N, K, err, s);
 }
+// Weight gradients (K = batch rows, M x N = a few 128 x 128 tiles): split K
+// so that ~128 CTAs share the batch; C (the gradient) starts at zero.
+cudaError_t tn_wgrad(const uint16_t* A, const uint16_t* Bt, float* C, int M, int N, int K, int* err,
+                     cudaStream_t s) {
+    int tiles = ((M + 127) / 128) * ((N + 127) / 128);
+    int splits = (K + 511) / 512;
+    int cap = 512 / tiles;
+    if (splits > cap) splits = cap;
+    return ldo_umma::gemm_tn(A, Bt, C, M, N, K, err, s, splits);
+}
 
 // dst[C][R] = src[R][C] (bf16), 32 x 32 tiles through shared memory
 __global__ void transpose_kernel(const uint16_t* __restrict__ src, uint16_t* __restrict__ dst, int R, int C) {
@@ -289,21 +299,21 @@ cudaError_t ldo_mlp_loss_grad(LdoMlp& m, int n, double norm, cudaStream_t s) {
     colsum_kernel<<<rb, H, 0, s>>>(m.dz, n, m.grad + LDO_LEARN_OFF_B3);
     MLP_CU(transpose(m.h[1], m.ht, n, H, s));
     MLP_CU(transpose(m.gbf, m.gt, n, H, s));
-    MLP_CU(tn(m.ht, m.gt, m.grad + LDO_LEARN_OFF_W3, H, H, n, m.err, s));
+    MLP_CU(tn_wgrad(m.ht, m.gt, m.grad + LDO_LEARN_OFF_W3, H, H, n, m.err, s));
     MLP_CU(tn(m.gbf, m.wbf + BF_W3, m.dz, n, H, H, m.err, s));
     gelu_back_kernel<<<blocks_for(tot, 256), 256, 0, s>>>(m.dz, m.z[1], m.gbf, tot);
     // layer 2
     colsum_kernel<<<rb, H, 0, s>>>(m.dz, n, m.grad + LDO_LEARN_OFF_B2);
     MLP_CU(transpose(m.h[0], m.ht, n, H, s));
     MLP_CU(transpose(m.gbf, m.gt, n, H, s));
-    MLP_CU(tn(m.ht, m.gt, m.grad + LDO_LEARN_OFF_W2, H, H, n, m.err, s));
+    MLP_CU(tn_wgrad(m.ht, m.gt, m.grad + LDO_LEARN_OFF_W2, H, H, n, m.err, s));
     MLP_CU(tn(m.gbf, m.wbf + BF_W2, m.dz, n, H, H, m.err, s));
     gelu_back_kernel<<<blocks_for(tot, 256), 256, 0, s>>>(m.dz, m.z[0], m.gbf, tot);
     // layer 1
     colsum_kernel<<<rb, H, 0, s>>>(m.dz, n, m.grad + LDO_LEARN_OFF_B1);
     MLP_CU(transpose(m.x, m.ht, n, DIN, s));
     MLP_CU(transpose(m.gbf, m.gt, n, H, s));
-    MLP_CU(tn(m.ht, m.gt, m.grad + LDO_LEARN_OFF_W1, DIN, H, n, m.err, s));
+    MLP_CU(tn_wgrad(m.ht, m.gt, m.grad + LDO_LEARN_OFF_W1, DIN, H, n, m.err, s));
     return cudaGetLastError();
 }
 

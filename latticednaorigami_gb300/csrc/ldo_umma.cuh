@@ -4,7 +4,9 @@
 //
 //   C[M][N] (fp32, row-major) = A[M][K] * B[N][K]^T     (A, B bf16, K-major)
 //
-// One CTA of 128 threads per 128 x 128 output tile.  Per 64-wide K slice the
+// One CTA of 128 threads per 128 x 128 output tile and K segment (split-K for
+// long K: the segments' partial products are added into C, which then has to
+// start at zero).  Per 64-wide K slice the
 // four warps stage both operand tiles in shared memory, one thread issues
 // four MMAs (K = 16 each) and commits them to an mbarrier; the CTA waits for
 // the commit before the next slice overwrites the tiles.  Each warp then
@@ -63,9 +65,10 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Stage rows [r0, r0+128) x cols [k0, k0+64) of a K-major bf16 matrix
-// (rows x K, row stride K) into a tile; out-of-range elements are zero.
+// (rows x K, row stride K) into a tile; rows >= rows and columns >= klim are
+// zero.
 __device__ __forceinline__ void stage_tile(unsigned char* tile, const uint16_t* __restrict__ src, int rows, int K,
-                                           int r0, int k0) {
+                                           int klim, int r0, int k0) {
     // 128 rows x 8 chunks of 8 elements (16 bytes)
     for (int e = threadIdx.x; e < TM * (TK / 8); e += blockDim.x) {
         int r = e >> 3, c = e & 7;
@@ -73,13 +76,13 @@ __device__ __forceinline__ void stage_tile(unsigned char* tile, const uint16_t* 
         uint4 v = make_uint4(0, 0, 0, 0);
         if (gr < rows) {
             const uint16_t* p = src + (size_t)gr * K + gk;
-            if (gk + 8 <= K && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
+            if (gk + 8 <= klim && ((reinterpret_cast<uintptr_t>(p) & 15) == 0)) {
                 v = *reinterpret_cast<const uint4*>(p);
             }
             else {
                 uint16_t t[8];
                 #pragma unroll
-                for (int q = 0; q < 8; ++q) t[q] = (gk + q < K) ? p[q] : (uint16_t)0;
+                for (int q = 0; q < 8; ++q) t[q] = (gk + q < klim) ? p[q] : (uint16_t)0;
                 v = *reinterpret_cast<uint4*>(t);
             }
         }
@@ -88,7 +91,8 @@ __device__ __forceinline__ void stage_tile(unsigned char* tile, const uint16_t* 
 }
 
 __global__ void __launch_bounds__(128) gemm_tn_kernel(const uint16_t* __restrict__ A, const uint16_t* __restrict__ B,
-                                                      float* __restrict__ C, int M, int N, int K, int* err) {
+                                                      float* __restrict__ C, int M, int N, int K, int k_per,
+                                                      int* err) {
     __shared__ __align__(1024) unsigned char sA[TILE_BYTES];
     __shared__ __align__(1024) unsigned char sB[TILE_BYTES];
     __shared__ __align__(8) unsigned long long mbar;
@@ -114,10 +118,13 @@ __global__ void __launch_bounds__(128) gemm_tn_kernel(const uint16_t* __restrict
 
     bool ok = true;
     uint32_t parity = 0;
-    int nk = (K + TK - 1) / TK;
+    int kb = blockIdx.z * k_per;
+    int ke = min(K, kb + k_per);
+    int nk = ke > kb ? (ke - kb + TK - 1) / TK : 0;
+    bool split = gridDim.z > 1;
     for (int kt = 0; kt < nk && ok; ++kt) {
-        stage_tile(sA, A, M, K, m0, kt * TK);
-        stage_tile(sB, B, N, K, n0, kt * TK);
+        stage_tile(sA, A, M, K, ke, m0, kb + kt * TK);
+        stage_tile(sB, B, N, K, ke, n0, kb + kt * TK);
         // generic-proxy stores -> visible to the tensor core's async proxy
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         __syncthreads();
@@ -147,7 +154,7 @@ __global__ void __launch_bounds__(128) gemm_tn_kernel(const uint16_t* __restrict
         if (!ok && threadIdx.x == 0) atomicExch(err, 1);
     }
 
-    if (ok) {
+    if (ok && nk > 0) {
         int row = m0 + warp * 32 + lane;
         #pragma unroll 1
         for (int c0 = 0; c0 < TN; c0 += 32) {
@@ -168,7 +175,10 @@ __global__ void __launch_bounds__(128) gemm_tn_kernel(const uint16_t* __restrict
                 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
                     int col = n0 + c0 + j;
-                    if (col < N) C[(size_t)row * N + col] = __uint_as_float(v[j]);
+                    if (col < N) {
+                        if (split) atomicAdd(&C[(size_t)row * N + col], __uint_as_float(v[j]));
+                        else C[(size_t)row * N + col] = __uint_as_float(v[j]);
+                    }
                 }
             }
         }
@@ -182,10 +192,18 @@ __global__ void __launch_bounds__(128) gemm_tn_kernel(const uint16_t* __restrict
     }
 }
 
+// splits > 1: K is cut into that many segments of whole 64-wide slices whose
+// products are added into C (C must be zero on entry).
 inline cudaError_t gemm_tn(const uint16_t* A, const uint16_t* B, float* C, int M, int N, int K, int* err,
-                           cudaStream_t s) {
-    dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM);
-    gemm_tn_kernel<<<grid, 128, 0, s>>>(A, B, C, M, N, K, err);
+                           cudaStream_t s, int splits = 1) {
+    int slices = (K + TK - 1) / TK;
+    if (splits < 1) splits = 1;
+    if (splits > slices) splits = slices > 0 ? slices : 1;
+    int k_per = ((slices + splits - 1) / splits) * TK;
+    splits = (K + k_per - 1) / k_per;
+    if (splits < 1) splits = 1;
+    dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM, splits);
+    gemm_tn_kernel<<<grid, 128, 0, s>>>(A, B, C, M, N, K, k_per, err);
     return cudaGetLastError();
 }
 
