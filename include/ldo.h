@@ -209,6 +209,17 @@ ldo_status ldo_learn_set_table(ldo_engine* e, const double* weights, int n);
 ldo_status ldo_learn_loss_grad(const float* params, const int32_t* idx, const float* cnt_bound, const float* cnt_total,
                                int n, double* loss, float* grad);
 
+/* Output files of one replica in the reference's formats and file names
+ * (setup_output_files, src/simulation.cpp:47-147; writers src/files.cpp:
+ * 519-789): <filebase>.vsf at open, then on every ldo_writer_write the
+ * replica's current state, for the kinds set in `kinds`: 1 .trj, 2 .vcf
+ * .states .ores, 4 .counts .staples .staplestates, 8 .ene, 16 .ops (the
+ * .inp's ops_to_output, or every order parameter). */
+typedef struct ldo_writer ldo_writer;
+ldo_status ldo_writer_open(ldo_engine* e, int replica, const char* filebase, uint32_t kinds, ldo_writer** out);
+ldo_status ldo_writer_write(ldo_writer* w, int64_t step);
+void ldo_writer_close(ldo_writer* w);
+
 /* Host-only helpers (no GPU needed). */
 
 /* Reduced hybridisation enthalpy H/(RT) and entropy S/R of a fully paired

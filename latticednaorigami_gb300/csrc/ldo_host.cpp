@@ -18,6 +18,7 @@
 #include "ldo_io.hpp"
 #include "ldo_kernels.h"
 #include "ldo_mlp.h"
+#include "ldo_output.hpp"
 #include "ldo_tables.hpp"
 
 namespace {
@@ -1644,5 +1645,107 @@ ldo_status ldo_learn_loss_grad(const float* params, const int32_t* idx, const fl
         CU(cudaMemcpy(grad, m.grad, LDO_LEARN_NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
     });
 }
+
+} // extern "C"
+
+// ------------------------------------------------------ output writers ---
+
+struct ldo_writer {
+    ldo_engine* e {nullptr};
+    int replica {0};
+    std::unique_ptr<ldo_out::Writer> w;
+    vector<int> op_index;
+};
+
+namespace {
+
+ldo_out::Snapshot replica_snapshot(ldo_engine* e, int replica, const vector<int>& op_index) {
+    LdoLaunch L = e->launch_params(LDO_MODE_OBSERVE, 0);
+    L.want_dep = 1;
+    CU(ldo_launch_mc(L, e->stream));
+    CU(cudaStreamSynchronize(e->stream));
+    vector<unsigned char> b(e->lay.bytes);
+    CU(cudaMemcpy(b.data(), e->d_arena.p + (size_t)replica * e->lay.bytes, b.size(), cudaMemcpyDeviceToHost));
+    const LdoLayout& y = e->lay;
+    const LdoSys& d = e->systems[e->sys_of[replica]].desc;
+    const auto* h = reinterpret_cast<const LdoHdr*>(b.data() + y.o_hdr);
+    const auto* pp = reinterpret_cast<const long long*>(b.data() + y.o_pp);
+    const unsigned char* ore = b.data() + y.o_ore;
+    const unsigned char* st = b.data() + y.o_state;
+    const auto* chain_c = reinterpret_cast<const int32_t*>(b.data() + y.o_chain_c);
+    const unsigned char* chain_type = b.data() + y.o_chain_type;
+    const unsigned char* chain_order = b.data() + y.o_chain_order;
+    const auto* op = reinterpret_cast<const int32_t*>(b.data() + y.o_op);
+    static const int U[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+    ldo_out::Snapshot s;
+    for (int c = 0; c < h->n_chains; ++c) {
+        int cs = chain_order[c];
+        int type = cs == 0 ? 0 : chain_type[cs];
+        ldo_out::Snapshot::Chain ch;
+        ch.index = chain_c[cs];
+        ch.identity = type;
+        for (int dd = 0; dd < d.type_len[type]; ++dd) {
+            int sl = cs == 0 ? dd : d.ns + (cs - 1) * d.lmax + dd;
+            long long p = pp[sl];
+            int x = (int)(short)(unsigned short)(p & 0xffff);
+            long long r1 = (p - x) >> 16;
+            int yy = (int)(short)(unsigned short)(r1 & 0xffff);
+            int z = (int)((r1 - yy) >> 16);
+            ldo_out::Snapshot::Dom dm {{x, yy, z}, {U[ore[sl]][0], U[ore[sl]][1], U[ore[sl]][2]}, st[sl]};
+            ch.doms.push_back(dm);
+        }
+        s.chains.push_back(std::move(ch));
+    }
+    s.n_types = d.n_types - 1;
+    s.num_staples = h->num_staples;
+    s.num_bound = h->num_bound;
+    s.num_fully = h->num_fully;
+    s.energy = h->energy;
+    s.enthalpy = h->H;
+    s.entropy = h->S;
+    s.stacking = h->stacking;
+    s.bias = h->move_bias * e->h_ctl[replica].bias_mult;
+    for (int q : op_index) s.op_values.push_back(op[2 * q]);
+    return s;
+}
+
+} // namespace
+
+extern "C" {
+
+ldo_status ldo_writer_open(ldo_engine* e, int replica, const char* filebase, uint32_t kinds, ldo_writer** out) {
+    if (!e || !filebase || !out || replica < 0 || replica >= e->n_rep) return LDO_EINVAL;
+    *out = nullptr;
+    return guard(e, [&]() {
+        const HostSystem& hs = e->systems[e->sys_of[replica]];
+        auto wr = std::make_unique<ldo_writer>();
+        wr->e = e;
+        wr->replica = replica;
+        vector<string> tags = hs.p.ops_to_output;
+        if (tags.empty())
+            for (auto& o : hs.ops) tags.push_back(o.tag);
+        for (auto& t : tags) {
+            int q = -1;
+            for (size_t k = 0; k < hs.ops.size(); ++k)
+                if (hs.ops[k].tag == t) q = (int)k;
+            if (q < 0) throw LdoError(LDO_EINVAL, t + ": no such order parameter to output");
+            wr->op_index.push_back(q);
+        }
+        try {
+            wr->w = std::make_unique<ldo_out::Writer>(filebase, kinds, hs.desc.ns, hs.p.max_total_staples,
+                                                      hs.p.max_staple_size, tags);
+        } catch (std::runtime_error& x) {
+            throw LdoError(LDO_EINVAL, x.what());
+        }
+        *out = wr.release();
+    });
+}
+
+ldo_status ldo_writer_write(ldo_writer* w, int64_t step) {
+    if (!w || !w->e) return LDO_EINVAL;
+    return guard(w->e, [&]() { w->w->write(step, replica_snapshot(w->e, w->replica, w->op_index)); });
+}
+
+void ldo_writer_close(ldo_writer* w) { delete w; }
 
 } // extern "C"

@@ -22,6 +22,7 @@ EXPORTS = [
     "ldo_energy_tables", "ldo_us_run", "ldo_us_get_biases", "ldo_us_get_windows", "ldo_replica_status_noalloc",
     "ldo_learn_collect", "ldo_learn_reset_counts", "ldo_learn_get_counts", "ldo_learn_train", "ldo_learn_set_params",
     "ldo_learn_get_params", "ldo_learn_get_table", "ldo_learn_set_table", "ldo_learn_loss_grad",
+    "ldo_writer_open", "ldo_writer_write", "ldo_writer_close",
 ]
 
 LEARN_TABLE = 524288      # network inputs (ldo_learn.h)
@@ -96,6 +97,9 @@ def load_library(path=None):
     lib.ldo_learn_get_table.argtypes = [vp, dp, ip]
     lib.ldo_learn_set_table.argtypes = [vp, dp, ip]
     lib.ldo_learn_loss_grad.argtypes = [fp, i32p, fp, fp, ip, dp, fp]
+    lib.ldo_writer_open.argtypes = [vp, ip, ctypes.c_char_p, ctypes.c_uint32, ctypes.POINTER(vp)]
+    lib.ldo_writer_write.argtypes = [vp, ctypes.c_int64]
+    lib.ldo_writer_close.argtypes = [vp]
     lib.ldo_nn_duplex_thermo.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, dp, dp]
     lib.ldo_energy_tables.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
                                       dp, dp, dp, dp, dp, ip]
@@ -232,6 +236,14 @@ class Engine:
         self._check(self.lib.ldo_us_get_biases(self.h, _dptr(out), self.n, gl))
         return out
 
+    def open_writer(self, replica, filebase, kinds=31):
+        """Output files of one replica in the reference's formats
+        (1 .trj, 2 .vcf/.states/.ores, 4 .counts/.staples/.staplestates,
+        8 .ene, 16 .ops); returns a Writer."""
+        w = ctypes.c_void_p()
+        self._check(self.lib.ldo_writer_open(self.h, replica, os.fsencode(filebase), kinds, ctypes.byref(w)))
+        return Writer(self, w)
+
     # learned insertion proposal
     def learn_collect(self):
         self._check(self.lib.ldo_learn_collect(self.h))
@@ -280,6 +292,24 @@ class Engine:
         self._check(self.lib.ldo_pt_get_stats(self.h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
                                               b.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), n_pairs))
         return a, b
+
+
+class Writer:
+    """Appends one replica's state to its output files (ldo_writer_*)."""
+
+    def __init__(self, eng, handle):
+        self.eng = eng
+        self.h = handle
+
+    def write(self, step):
+        self.eng._check(self.eng.lib.ldo_writer_write(self.h, int(step)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.eng.lib.ldo_writer_close(self.h)
+            self.h = None
+
+    __del__ = close
 
 
 def _fptr(a):

@@ -146,13 +146,14 @@ void fill_params(parser::InputParameters& p, std::map<string, string>& kv) {
     p.m_read_biases = false;
     p.m_multi_window = false;
     p.m_output_filebase = S("output_filebase", "/tmp/ldo_ref_trace");
-    p.m_configs_output_freq = 0;
-    p.m_vtf_output_freq = 0;
+    // the reference's output writers (src/simulation.cpp:47), when asked for
+    p.m_configs_output_freq = (int)I("configs_output_freq", 0);
+    p.m_vtf_output_freq = (int)I("vtf_output_freq", 0);
     p.m_vcf_per_domain = false;
-    p.m_counts_output_freq = 0;
+    p.m_counts_output_freq = (int)I("counts_output_freq", 0);
     p.m_times_output_freq = 0;
-    p.m_energies_output_freq = 0;
-    p.m_order_params_output_freq = 0;
+    p.m_energies_output_freq = (int)I("energies_output_freq", 0);
+    p.m_order_params_output_freq = (int)I("order_params_output_freq", 0);
     p.m_rand_engine_state_output_freq = 0;
     p.m_vmd_pipe_freq = 0;
     p.m_create_vmd_instance = false;
@@ -184,6 +185,9 @@ class TraceSim : public simulation::GCMCSimulation {
              std::ostream& out)
         : GCMCSimulation(o, ops, b, p), m_every(every), m_out(out) {
         m_logging_stream = &std::cerr;
+        if (p.m_configs_output_freq || p.m_vtf_output_freq || p.m_counts_output_freq || p.m_energies_output_freq ||
+            p.m_order_params_output_freq)
+            m_output_files = simulation::setup_output_files(p, p.m_output_filebase, o, ops, b, m_random_gens);
     }
     void run() override {}
     bool m_first {true};

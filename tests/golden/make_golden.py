@@ -78,6 +78,31 @@ def enumerate_c1(tmp):
     print(path, weights)
 
 
+# reference output files: case, seed, steps, write frequency
+OUTPUT_RUNS = [("g24a", 3, 2000, 400), ("g24b", 4, 2000, 400), ("c3", 8, 2000, 400)]
+OUTPUT_EXTS = [".vsf", ".trj", ".vcf", ".states", ".ores", ".counts", ".staples", ".staplestates", ".ene", ".ops"]
+
+
+def make_outputs(tmp, only=None):
+    """The reference's own output writers (setup_output_files,
+    src/simulation.cpp:47) on the traced runs: every file of every kind the
+    engine's ldo_writer_* reproduces, written every `freq` steps."""
+    out_dir = os.path.join(HERE, "outputs")
+    os.makedirs(out_dir, exist_ok=True)
+    for case, seed, steps, freq in OUTPUT_RUNS:
+        if only and case not in only:
+            continue
+        base = os.path.join(tmp, "%s_out" % case)
+        inp = systems.write_case(tmp, case, extra=dict(
+            configs_output_freq=freq, vtf_output_freq=freq, counts_output_freq=freq, energies_output_freq=freq,
+            order_params_output_freq=freq, ops_to_output="numstaples numfulldomains", output_filebase=base))
+        ref_trace(inp, seed, steps)
+        for ext in OUTPUT_EXTS:
+            with open(base + ext) as f, open(os.path.join(out_dir, "%s_s%d%s" % (case, seed, ext)), "w") as g:
+                g.write(f.read())
+        print(out_dir, case, "outputs")
+
+
 def main(only=None):
     if not os.path.exists(REF):
         sys.exit("build the reference first: make -C oracle/ref")
@@ -95,6 +120,7 @@ def main(only=None):
             print(path, len(d["steps"]), "steps, draws", d["draws"])
         if not only or "c1" in only:
             enumerate_c1(tmp)
+        make_outputs(tmp, only)
 
 
 if __name__ == "__main__":
