@@ -142,10 +142,24 @@ ldo_status ldo_set_window(ldo_engine* e, const char* tag, int replica, int min_o
 ldo_status ldo_pt_run(ldo_engine* e, int n_rungs, int64_t swaps, int exchange_interval, int exchange_q,
                       double* device_ms);
 
+/* Two-dimensional parallel tempering over temperature x stacking multiplier
+ * (TwoDPTGCMCSimulation, src/ptmc_simulation.cpp:428-560): the .inp's temps
+ * and stacking_mults span n_temps x n_stacking slots (slot i * n_stacking + j),
+ * pairs are attempted in the reference's four alternating sets (even / odd
+ * along temperature, even / odd along stacking), and temperature, staple
+ * chemical potential and stacking multiplier are exchanged.  Replicas form
+ * ladders of n_temps * n_stacking consecutive replicas. */
+ldo_status ldo_pt2d_run(ldo_engine* e, int n_temps, int n_stacking, int64_t swaps, int exchange_interval,
+                        double* device_ms);
+
 /* Current control-slot to replica permutation (the .swp file row) for all
  * ladders: out[ladder * n_rungs + slot] = replica. */
 ldo_status ldo_pt_get_permutation(ldo_engine* e, int32_t* out, int n);
-/* Swap attempts and acceptances per neighbouring slot pair, summed over ladders. */
+/* Swap attempts and acceptances summed over ladders: per neighbouring slot
+ * pair i (n_pairs = n_rungs - 1) for a 1-D ladder; for a 2-D ladder per
+ * direction v (0 temperature, 1 stacking) and lower slot (i, j),
+ * index v * n_temps * n_stacking + i * n_stacking + j (n_pairs =
+ * 2 * n_temps * n_stacking, the reference's m_attempt_count[v][i][j]). */
 ldo_status ldo_pt_get_stats(ldo_engine* e, int64_t* attempts, int64_t* accepts, int n_pairs);
 
 /* Multi-window umbrella sampling with adaptive grid biases

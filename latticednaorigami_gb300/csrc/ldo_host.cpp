@@ -395,6 +395,8 @@ struct ldo_engine {
     DevBuf<int> d_perm, d_tab_slot;
     DevBuf<unsigned long long> d_pt_draws;
     DevBuf<long long> d_pt_att, d_pt_acc;
+    DevBuf<int> d_pt_sched;
+    int pt_dim2 {0}, pt_nctr {0};
     cudaGraphExec_t pt_graph {nullptr};
     LdoPT pt {};
 
@@ -789,7 +791,12 @@ struct ldo_engine {
 
     // PTGCMCSimulation constructor + OneDPTGCMCSimulation::initialize_control_qs
     // (src/ptmc_simulation.cpp:24-90, 337-358) for n_rep / n_rungs ladders.
-    void pt_setup(int n_rungs, int exchange_q) {
+    // dim2 = 0: one-dimensional ladder over the .inp's temps (and the other
+    // per-rung lists).  dim2 > 0: TwoDPTGCMCSimulation's grid of temps x
+    // stacking_mults (dim2 = number of stacking multipliers), slot
+    // k = i * dim2 + j, exchanging temperature, staple chemical potential and
+    // stacking multiplier (src/ptmc_simulation.cpp:428-481).
+    void pt_setup(int n_rungs, int exchange_q, int dim2 = 0) {
         if (n_rungs < 2 || n_rep % n_rungs != 0) throw LdoError(LDO_EINVAL, "replicas must form whole ladders of n_rungs");
         if (!(exchange_q & 1)) throw LdoError(LDO_EINVAL, "every exchange variant exchanges the temperature");
         int nl = n_rep / n_rungs;
@@ -801,16 +808,56 @@ struct ldo_engine {
             if (&s != &hs && s.desc.n_types != hs.desc.n_types)
                 throw LdoError(LDO_EINVAL, "ladders must have the same staple types");
         const ldo_io::Params& p = hs.p;
-        if ((int)p.temps.size() != n_rungs) throw LdoError(LDO_EINVAL, "temps must list one temperature per rung");
-        auto fill = [&](const vector<double>& v, const char* what) {
-            if (v.empty()) return vector<double>(n_rungs, 1.0);
-            if ((int)v.size() != n_rungs) throw LdoError(LDO_EINVAL, string(what) + " must list one value per rung");
-            return v;
-        };
-        vector<double> tq = p.temps;
-        vector<double> uq = fill(p.chem_pot_mults, "chem_pot_mults");
-        vector<double> bq = fill(p.bias_mults, "bias_mults");
-        vector<double> sq = fill(p.stacking_mults, "stacking_mults");
+        vector<double> tq, uq, bq, sq;
+        // pair schedule: sets of (slot a, slot b, counter) in the reference's loop order
+        vector<vector<std::tuple<int, int, int>>> sets;
+        int n_ctr = 0;
+        if (dim2 == 0) {
+            if ((int)p.temps.size() != n_rungs) throw LdoError(LDO_EINVAL, "temps must list one temperature per rung");
+            auto fill = [&](const vector<double>& v, const char* what) {
+                if (v.empty()) return vector<double>(n_rungs, 1.0);
+                if ((int)v.size() != n_rungs)
+                    throw LdoError(LDO_EINVAL, string(what) + " must list one value per rung");
+                return v;
+            };
+            tq = p.temps;
+            uq = fill(p.chem_pot_mults, "chem_pot_mults");
+            bq = fill(p.bias_mults, "bias_mults");
+            sq = fill(p.stacking_mults, "stacking_mults");
+            // OneDPTGCMCSimulation::attempt_exchange (:360): i = swap_i % 2, i + 2, ...
+            sets.resize(2);
+            for (int set = 0; set < 2; ++set)
+                for (int i = set; i < n_rungs - 1; i += 2) sets[set].push_back(std::make_tuple(i, i + 1, i));
+            n_ctr = n_rungs - 1;
+        }
+        else {
+            int d1 = (int)p.temps.size(), d2 = (int)p.stacking_mults.size();
+            if (d2 != dim2 || d1 * d2 != n_rungs || d1 < 1 || d2 < 1)
+                throw LdoError(LDO_EINVAL, "a 2-D ladder needs temps x stacking_mults slots");
+            for (int i = 0; i < d1; ++i)
+                for (int j = 0; j < d2; ++j) {
+                    tq.push_back(p.temps[i]);
+                    uq.push_back(p.staple_u_mult);
+                    bq.push_back(1.0);
+                    sq.push_back(p.stacking_mults[j]);
+                }
+            // TwoDPTGCMCSimulation::attempt_exchange (:495) with the set tables
+            // of include/.../ptmc_simulation.hpp:158-164
+            const int i_start[4] = {0, 0, 1, 0}, j_start[4] = {0, 0, 0, 1};
+            const int i_incr[4] = {2, 1, 2, 1}, j_incr[4] = {1, 2, 1, 2};
+            const int i_end[4] = {d1 - 1, d1, d1 - 1, d1}, j_end[4] = {d2, d2 - 1, d2, d2 - 1};
+            const int rep_incr[4] = {d2, 1, d2, 1};
+            sets.resize(4);
+            for (int set = 0; set < 4; ++set) {
+                int v = set % 2;
+                for (int i = i_start[set]; i < i_end[set]; i += i_incr[set])
+                    for (int j = j_start[set]; j < j_end[set]; j += j_incr[set]) {
+                        int a = i * d2 + j;
+                        sets[set].push_back(std::make_tuple(a, a + rep_incr[set], v * d1 * d2 + i * d2 + j));
+                    }
+            }
+            n_ctr = 2 * d1 * d2;
+        }
         vector<double> slot(4 * n_rungs);
         for (int k = 0; k < n_rungs; ++k) {
             slot[k] = tq[k];
@@ -859,10 +906,25 @@ struct ldo_engine {
         CU(cudaMemcpy(d_tab_slot.p, tab_slot.data(), n_rungs * sizeof(int), cudaMemcpyHostToDevice));
         d_pt_draws.alloc(nl);
         CU(cudaMemset(d_pt_draws.p, 0, nl * sizeof(unsigned long long)));
-        d_pt_att.alloc(n_rungs);
-        d_pt_acc.alloc(n_rungs);
-        CU(cudaMemset(d_pt_att.p, 0, n_rungs * sizeof(long long)));
-        CU(cudaMemset(d_pt_acc.p, 0, n_rungs * sizeof(long long)));
+        d_pt_att.alloc(std::max(n_ctr, 1));
+        d_pt_acc.alloc(std::max(n_ctr, 1));
+        CU(cudaMemset(d_pt_att.p, 0, std::max(n_ctr, 1) * sizeof(long long)));
+        CU(cudaMemset(d_pt_acc.p, 0, std::max(n_ctr, 1) * sizeof(long long)));
+        vector<int> set_start(1, 0), pa, pb, pc;
+        for (auto& st : sets) {
+            for (auto& t : st) {
+                pa.push_back(std::get<0>(t));
+                pb.push_back(std::get<1>(t));
+                pc.push_back(std::get<2>(t));
+            }
+            set_start.push_back((int)pa.size());
+        }
+        vector<int> sched(set_start);
+        sched.insert(sched.end(), pa.begin(), pa.end());
+        sched.insert(sched.end(), pb.begin(), pb.end());
+        sched.insert(sched.end(), pc.begin(), pc.end());
+        d_pt_sched.alloc(std::max<size_t>(sched.size(), 1));
+        CU(cudaMemcpy(d_pt_sched.p, sched.data(), sched.size() * sizeof(int), cudaMemcpyHostToDevice));
         pt = LdoPT {};
         pt.n_ladders = nl;
         pt.n_rungs = n_rungs;
@@ -883,8 +945,15 @@ struct ldo_engine {
         pt.att = d_pt_att.p;
         pt.acc = d_pt_acc.p;
         pt.seed = seed;
+        pt.n_sets = (int)sets.size();
+        pt.set_start = d_pt_sched.p;
+        pt.pair_a = d_pt_sched.p + set_start.size();
+        pt.pair_b = pt.pair_a + pa.size();
+        pt.pair_ctr = pt.pair_b + pb.size();
         pt_rungs = n_rungs;
         pt_q = exchange_q;
+        pt_dim2 = dim2;
+        pt_nctr = n_ctr;
         pt_swap_i = 0;
         if (pt_graph) {
             cudaGraphExecDestroy(pt_graph);
@@ -901,38 +970,45 @@ struct ldo_engine {
         L.want_dep = 1;
         CU(ldo_launch_mc(L, stream));
         LdoPT P = pt;
-        P.swap_i = (int)(swap_i % 2);
+        P.swap_i = (int)(swap_i % pt.n_sets);
         CU(ldo_launch_pt_swap(P, stream));
     }
 
-    void pt_run(int n_rungs, long long swaps, int exchange_interval, int exchange_q, double* ms) {
-        if (n_rungs != pt_rungs || exchange_q != pt_q) pt_setup(n_rungs, exchange_q);
+    void pt_run(int n_rungs, long long swaps, int exchange_interval, int exchange_q, double* ms, int dim2 = 0) {
+        if (n_rungs != pt_rungs || exchange_q != pt_q || dim2 != pt_dim2) {
+            if (pt_graph) {
+                cudaGraphExecDestroy(pt_graph);
+                pt_graph = nullptr;
+            }
+            pt_setup(n_rungs, exchange_q, dim2);
+        }
         if (swaps < 0 || exchange_interval < 0) throw LdoError(LDO_EINVAL, "negative swaps or interval");
         CU(cudaEventRecord(ev0, stream));
         long long done = 0;
-        // Rounds alternate even/odd pair sets; two rounds form one CUDA graph.
-        if (swaps >= 4) {
+        // Rounds cycle through the pair sets; one cycle of rounds (swap
+        // counters 1..n_sets) forms one CUDA graph.
+        int period = pt.n_sets;
+        if (swaps >= 2 * period) {
             if (!pt_graph) {
                 cudaGraph_t g;
                 CU(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-                pt_round(1, exchange_interval);
-                pt_round(2, exchange_interval);
+                for (int k = 1; k <= period; ++k) pt_round(k, exchange_interval);
                 CU(cudaStreamEndCapture(stream, &g));
                 CU(cudaGraphInstantiate(&pt_graph, g, 0));
                 cudaGraphDestroy(g);
                 pt_graph_interval = exchange_interval;
             }
             if (pt_graph_interval != exchange_interval) throw LdoError(LDO_EINVAL, "exchange interval changed");
-            // the graph starts with an odd round: align with the swap counter
-            if (pt_swap_i % 2 == 1) {
+            // the graph starts with swap counter 1 (mod period): align
+            while (pt_swap_i % period != 0 && done < swaps) {
                 pt_round(pt_swap_i + 1, exchange_interval);
                 ++pt_swap_i;
                 ++done;
             }
-            while (swaps - done >= 2) {
+            while (swaps - done >= period) {
                 CU(cudaGraphLaunch(pt_graph, stream));
-                pt_swap_i += 2;
-                done += 2;
+                pt_swap_i += period;
+                done += period;
             }
         }
         while (done < swaps) {
@@ -1433,8 +1509,16 @@ ldo_status ldo_pt_get_permutation(ldo_engine* e, int32_t* out, int n) {
     return guard(e, [&]() { CU(cudaMemcpy(out, e->d_perm.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost)); });
 }
 
+ldo_status ldo_pt2d_run(ldo_engine* e, int n_temps, int n_stacking, int64_t swaps, int exchange_interval,
+                        double* device_ms) {
+    if (!e || n_temps < 1 || n_stacking < 1) return LDO_EINVAL;
+    return guard(e, [&]() {
+        e->pt_run(n_temps * n_stacking, swaps, exchange_interval, 1 | 2 | 8, device_ms, n_stacking);
+    });
+}
+
 ldo_status ldo_pt_get_stats(ldo_engine* e, int64_t* attempts, int64_t* accepts, int n_pairs) {
-    if (!e || !attempts || !accepts || e->pt_rungs == 0 || n_pairs != e->pt_rungs - 1) return LDO_EINVAL;
+    if (!e || !attempts || !accepts || e->pt_rungs == 0 || n_pairs != e->pt_nctr) return LDO_EINVAL;
     return guard(e, [&]() {
         CU(cudaMemcpy(attempts, e->d_pt_att.p, n_pairs * sizeof(int64_t), cudaMemcpyDeviceToHost));
         CU(cudaMemcpy(accepts, e->d_pt_acc.p, n_pairs * sizeof(int64_t), cudaMemcpyDeviceToHost));

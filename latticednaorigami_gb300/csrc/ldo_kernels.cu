@@ -218,21 +218,23 @@ __global__ void ldo_status_kernel(const unsigned char* arena, int bytes, int o_h
 
 // One thread per ladder: the exchange attempts of one swap round between
 // neighbouring control slots (OneDPTGCMCSimulation::attempt_exchange,
-// src/ptmc_simulation.cpp:360-412), acceptance from calc_acceptance_p
-// (:275-313) over staple types 1..S, and the master's control broadcast
-// (master_send, :212).
+// src/ptmc_simulation.cpp:360-412, or the four-set T x stacking schedule of
+// TwoDPTGCMCSimulation::attempt_exchange, :495-560), acceptance from
+// calc_acceptance_p (:275-313) over staple types 1..S, and the master's
+// control broadcast (master_send, :212).
 __global__ void ldo_pt_swap_kernel(LdoPT P) {
     int lad = blockIdx.x * blockDim.x + threadIdx.x;
     if (lad >= P.n_ladders) return;
     int* perm = P.perm + (size_t)lad * P.n_rungs;
     ldo::Rng rng;
     rng.init(P.seed, (uint32_t)lad, 1u, P.draws[lad]);
-    int set = P.swap_i % 2;
-    for (int i = set; i < P.n_rungs - 1; i += 2) {
-        atomicAdd((unsigned long long*)&P.att[i], 1ull);
-        double temp1 = P.slot_temp[i], temp2 = P.slot_temp[i + 1];
-        double sm1 = P.slot_stack[i], sm2 = P.slot_stack[i + 1];
-        int r1 = perm[i], r2 = perm[i + 1];
+    int set = P.swap_i;
+    for (int q = P.set_start[set]; q < P.set_start[set + 1]; ++q) {
+        int i = P.pair_a[q], i2 = P.pair_b[q], ctr = P.pair_ctr[q];
+        atomicAdd((unsigned long long*)&P.att[ctr], 1ull);
+        double temp1 = P.slot_temp[i], temp2 = P.slot_temp[i2];
+        double sm1 = P.slot_stack[i], sm2 = P.slot_stack[i2];
+        int r1 = perm[i], r2 = perm[i2];
         const LdoHdr* h1 = reinterpret_cast<const LdoHdr*>(P.arena + (size_t)r1 * P.lay.bytes + P.lay.o_hdr);
         const LdoHdr* h2 = reinterpret_cast<const LdoHdr*>(P.arena + (size_t)r2 * P.lay.bytes + P.lay.o_hdr);
         const int16_t* n1 = reinterpret_cast<const int16_t*>(P.arena + (size_t)r1 * P.lay.bytes + P.lay.o_type_count);
@@ -254,9 +256,9 @@ __global__ void ldo_pt_swap_kernel(LdoPT P) {
         double p = fmin(1.0, exp(DB * (DH + DBias) + DBM * Dst - dbu_dn));
         bool accept = (p == 1) ? true : (p > rng.uniform_real());
         if (accept) {
-            atomicAdd((unsigned long long*)&P.acc[i], 1ull);
+            atomicAdd((unsigned long long*)&P.acc[ctr], 1ull);
             perm[i] = r2;
-            perm[i + 1] = r1;
+            perm[i2] = r1;
         }
     }
     P.draws[lad] = rng.draws;

@@ -69,10 +69,18 @@ struct LdoPT {
     const unsigned char* arena;
     LdoLayout lay;
     unsigned long long* draws;   // [n_ladders] swap stream counters
-    long long* att;              // [n_rungs - 1]
+    long long* att;              // [n_counters] attempts / accepts per pair counter
     long long* acc;
     uint32_t seed;
-    int swap_i;
+    int swap_i;                  // pair set of this round (swap counter mod n_sets)
+    // Pair schedule: set s holds the slot pairs (pair_a[q], pair_b[q]) for
+    // q in [set_start[s], set_start[s+1]), in the reference's loop order,
+    // each with its attempt/accept counter pair_ctr[q].
+    int n_sets;
+    const int* set_start;
+    const int* pair_a;
+    const int* pair_b;
+    const int* pair_ctr;
 };
 cudaError_t ldo_launch_pt_swap(const LdoPT& P, cudaStream_t stream);
 

@@ -22,7 +22,7 @@ EXPORTS = [
     "ldo_energy_tables", "ldo_us_run", "ldo_us_get_biases", "ldo_us_get_windows", "ldo_replica_status_noalloc",
     "ldo_learn_collect", "ldo_learn_reset_counts", "ldo_learn_get_counts", "ldo_learn_train", "ldo_learn_set_params",
     "ldo_learn_get_params", "ldo_learn_get_table", "ldo_learn_set_table", "ldo_learn_loss_grad",
-    "ldo_writer_open", "ldo_writer_write", "ldo_writer_close",
+    "ldo_writer_open", "ldo_writer_write", "ldo_writer_close", "ldo_pt2d_run",
 ]
 
 LEARN_TABLE = 524288      # network inputs (ldo_learn.h)
@@ -80,6 +80,7 @@ def load_library(path=None):
     lib.ldo_set_grid_bias.argtypes = [vp, ctypes.c_char_p, ip, dp, ip]
     lib.ldo_set_window.argtypes = [vp, ctypes.c_char_p, ip, ip, ip]
     lib.ldo_pt_run.argtypes = [vp, ip, ctypes.c_int64, ip, ip, dp]
+    lib.ldo_pt2d_run.argtypes = [vp, ip, ip, ctypes.c_int64, ip, dp]
     lib.ldo_pt_get_permutation.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ip]
     lib.ldo_pt_get_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64), ip]
     lib.ldo_us_run.argtypes = [vp, ctypes.c_char_p, ip, ctypes.c_int64, ctypes.c_int64, ctypes.c_double, ip, dp]
@@ -215,6 +216,12 @@ class Engine:
         ms = ctypes.c_double(0)
         self._check(self.lib.ldo_pt_run(self.h, n_rungs, int(swaps), exchange_interval, exchange_q,
                                         ctypes.byref(ms)))
+        return ms.value
+
+    def pt2d_run(self, n_temps, n_stacking, swaps, exchange_interval):
+        ms = ctypes.c_double(0)
+        self._check(self.lib.ldo_pt2d_run(self.h, n_temps, n_stacking, int(swaps), exchange_interval,
+                                          ctypes.byref(ms)))
         return ms.value
 
     def us_run(self, grid_tag, n_iters, equil_steps, iter_steps, max_D_bias, exchange_interval=0):

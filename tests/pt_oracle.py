@@ -16,15 +16,43 @@ from oracle_lib import OracleReplica, staple_counts, swap_uniform
 
 
 class PTOracle:
-    def __init__(self, inp, params, n_ladders, seed, exchange_q=1):
-        self.n_rungs = len(params["temps"])
+    """dim2 = 0: 1-D ladder over params["temps"] (OneDPTGCMCSimulation);
+    dim2 > 0: the temps x stacking_mults grid of TwoDPTGCMCSimulation
+    (src/ptmc_simulation.cpp:428-560), exchanging T, staple u and stacking."""
+
+    def __init__(self, inp, params, n_ladders, seed, exchange_q=1, dim2=0):
+        self.dim2 = dim2
         self.n_ladders = n_ladders
         self.seed = seed
+        if dim2:
+            temps, stacks = list(params["temps"]), list(params["stacking_mults"])
+            d1 = len(temps)
+            self.n_rungs = d1 * dim2
+            R = self.n_rungs
+            self.slot = {"temp": [temps[k // dim2] for k in range(R)],
+                         "u": [params.get("staple_u_mult", 1.0)] * R, "bias": [1.0] * R,
+                         "stack": [stacks[k % dim2] for k in range(R)]}
+            exchange_q = 1 | 2 | 8
+            self.sets = []
+            i_start, j_start, i_incr, j_incr = [0, 0, 1, 0], [0, 0, 0, 1], [2, 1, 2, 1], [1, 2, 1, 2]
+            i_end, j_end, rep_incr = [d1 - 1, d1, d1 - 1, d1], [dim2, dim2 - 1, dim2, dim2 - 1], [dim2, 1, dim2, 1]
+            for st in range(4):
+                pairs = []
+                for i in range(i_start[st], i_end[st], i_incr[st]):
+                    for j in range(j_start[st], j_end[st], j_incr[st]):
+                        a = i * dim2 + j
+                        pairs.append((a, a + rep_incr[st], (st % 2) * d1 * dim2 + i * dim2 + j))
+                self.sets.append(pairs)
+            n_ctr = 2 * d1 * dim2
+        else:
+            self.n_rungs = len(params["temps"])
+            R = self.n_rungs
+            self.slot = {"temp": list(params["temps"]), "u": list(params.get("chem_pot_mults", [1.0] * R)),
+                         "bias": list(params.get("bias_mults", [1.0] * R)),
+                         "stack": list(params.get("stacking_mults", [1.0] * R))}
+            self.sets = [[(i, i + 1, i) for i in range(s0, R - 1, 2)] for s0 in (0, 1)]
+            n_ctr = R - 1
         self.q = exchange_q
-        R = self.n_rungs
-        self.slot = {"temp": list(params["temps"]), "u": list(params.get("chem_pot_mults", [1.0] * R)),
-                     "bias": list(params.get("bias_mults", [1.0] * R)),
-                     "stack": list(params.get("stacking_mults", [1.0] * R))}
         self.reps = [OracleReplica(inp, seed=seed, replica=r) for r in range(R * n_ladders)]
         self.ctrl = []
         for l in range(n_ladders):
@@ -41,8 +69,8 @@ class PTOracle:
             u = temp0 * (math.log(staple_M) - extra)
             self.red_u.append(u / temp0)
         self.bias_mult = params.get("bias_functions_mult", 1.0)
-        self.att = [0] * (R - 1)
-        self.acc = [0] * (R - 1)
+        self.att = [0] * n_ctr
+        self.acc = [0] * n_ctr
 
     def round(self, exchange_interval):
         self.swap_i += 1
@@ -56,11 +84,11 @@ class PTOracle:
             deps.append((H, st, bias, staple_counts(rep)))
         for l in range(self.n_ladders):
             perm = self.perm[l]
-            for i in range(self.swap_i % 2, R - 1, 2):
-                self.att[i] += 1
-                t1, t2 = self.slot["temp"][i], self.slot["temp"][i + 1]
-                sm1, sm2 = self.slot["stack"][i], self.slot["stack"][i + 1]
-                r1, r2 = perm[i], perm[i + 1]
+            for i, i2, ctr in self.sets[self.swap_i % len(self.sets)]:
+                self.att[ctr] += 1
+                t1, t2 = self.slot["temp"][i], self.slot["temp"][i2]
+                sm1, sm2 = self.slot["stack"][i], self.slot["stack"][i2]
+                r1, r2 = perm[i], perm[i2]
                 H1, st1, b1, n1 = deps[r1]
                 H2, st2, b2, n2 = deps[r2]
                 dbu = 0.0
@@ -80,8 +108,8 @@ class PTOracle:
                     accept = p > swap_uniform(self.seed, l, self.draws[l])
                     self.draws[l] += 1
                 if accept:
-                    self.acc[i] += 1
-                    perm[i], perm[i + 1] = r2, r1
+                    self.acc[ctr] += 1
+                    perm[i], perm[i2] = r2, r1
             for k in range(R):
                 c = self.ctrl[perm[k]]
                 if self.q & 1:

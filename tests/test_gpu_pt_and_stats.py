@@ -125,3 +125,34 @@ def test_distribution_matches_exact_enumeration(data_dir):
     chi2 = sum((o - e) ** 2 / e for o, e in zip(obs, exp))
     p = chi2_sf(chi2, len(obs) - 1)
     assert p > 0.01, (obs, exp, chi2, p)
+
+
+def test_pt_2d_temperature_stacking_grid_matches_cpu_restatement():
+    """TwoDPTGCMCSimulation's grid: 3 temperatures x 3 stacking multipliers,
+    the four alternating pair sets, 2 ladders, 14 rounds (CUDA-graph cycles
+    of four rounds plus alignment rounds)."""
+    from pt_oracle import PTOracle
+    temps = [325.0, 333.0, 342.0]
+    stacks = [0.8, 1.0, 1.25]
+    d = tempfile.mkdtemp()
+    inp = systems.write_case(d, "g24a", extra=dict(temps=" ".join(map(str, temps)),
+                                                     stacking_mults=" ".join(map(str, stacks)), num_reps=9,
+                                                     exchange_interval=150))
+    n_ladders, swaps, interval, seed = 2, 14, 150, 53
+    eng = engine(inp, n_replicas=9 * n_ladders, seed=seed)
+    eng.pt2d_run(3, 3, 5, interval)
+    eng.pt2d_run(3, 3, swaps - 5, interval)
+    ora = PTOracle(inp, dict(temps=temps, stacking_mults=stacks, temp=335.0, staple_M=1e-3,
+                             staple_lengths=[2] * 12), n_ladders, seed, dim2=3)
+    for _ in range(swaps):
+        ora.round(interval)
+    np.testing.assert_array_equal(eng.pt_permutation(), ora.permutation())
+    att, acc = eng.pt_stats(18)
+    assert att.tolist() == ora.att and acc.tolist() == ora.acc
+    assert sum(acc) > 0
+    obs = eng.observables()
+    for r, rep in enumerate(ora.reps):
+        ob = rep.observables()
+        assert obs[r]["draws"] == ob["draws"]
+        assert obs[r]["num_staples"] == ob["num_staples"]
+        assert abs(obs[r]["energy"] - ob["energy"]) <= 1e-12 * max(1.0, abs(ob["energy"]))
