@@ -31,6 +31,10 @@ int move_kind(const std::string& t) {
     if (t == "MetStapleRegrowth") return MV_MET_REGROWTH;
     if (t == "CBStapleRegrowth") return MV_CB_REGROWTH;
     if (t == "LearnedStapleExchange") return MV_LEARNED_EXCHANGE;
+    if (t == "CTRGScaffoldRegrowth") return MV_CTRG_SCAFFOLD;
+    if (t == "CTRGJumpScaffoldRegrowth") return MV_CTRG_JUMP;
+    if (t == "CTCBScaffoldRegrowth") return MV_CTCB_SCAFFOLD;
+    if (t == "CTCBJumpScaffoldRegrowth") return MV_CTCB_JUMP;
     throw std::runtime_error(t + ": movetype not supported by the oracle");
 }
 
@@ -91,6 +95,7 @@ Replica* build(const char* inp_path, const char* overrides, uint32_t seed, uint3
         size_t S = c.identities.size() - 1;
         for (auto& mv : moves) {
             c.move_kinds.push_back(move_kind(mv.type));
+            c.move_opts.push_back({mv.max_regrowth, mv.max_seg_regrowth, mv.max_num_recoils, mv.max_c_attempts});
             cum += mv.freq;
             c.move_cum.push_back(cum);
             if (mv.type == "MetStapleExchange" || mv.type == "LearnedStapleExchange") {
@@ -258,6 +263,13 @@ void oracle_observables(void* h, double* out) {
     out[8] = (double)s.rng.draws;
     out[9] = s.current_c_i;
 }
+
+// IdealRandomWalks::num_walks between sites dr apart in `steps` steps.
+double oracle_ideal_walks(int dx, int dy, int dz, int steps) { return (double)ideal_walks(dx, dy, dz, steps); }
+
+// Rosenbluth weights of the configurational-bias moves in long double (the
+// reference's own arithmetic) instead of the engine's FP64.
+void oracle_set_long_double(void* h, int on) { static_cast<Replica*>(h)->sys.ld_weights = on != 0; }
 
 // Per-move attempts/accepts, 2 x n_moves.
 int oracle_move_stats(void* h, long long* out, int cap) {

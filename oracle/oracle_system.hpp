@@ -11,6 +11,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <deque>
+#include <map>
 #include <set>
 #include <stdexcept>
 #include <string>
@@ -81,6 +83,22 @@ struct Delta {
     int stacked {0};
 };
 
+// A Rosenbluth weight.  The reference keeps CBMCMovetype::m_bias and
+// m_new_bias in long double (include/.../cb_movetypes.hpp:126-127), whose
+// width depends on the platform (x87 80-bit on x86-64, 128-bit on AArch64);
+// the engine computes them in FP64.  With `ld` set the oracle follows the
+// reference's long double, otherwise the engine's FP64.  The two choose the
+// same configurations and accept the same moves except where a weight ratio
+// lies within a rounding of 1 (then one side may skip the acceptance draw).
+struct Wt {
+    long double v {1};
+    bool ld {false};
+    void set(long double x) { v = ld ? x : (long double)(double)x; }
+    void mul(long double b) { v = ld ? v * b : (long double)((double)v * (double)b); }
+    void div(long double b) { v = ld ? v / b : (long double)((double)v / (double)b); }
+    long double over(const Wt& b) const { return ld ? v / b.v : (long double)((double)v / (double)b.v); }
+};
+
 struct SiteRec {
     int occ;
     int unbound_dom;   // valid when occ == UNBOUND
@@ -114,7 +132,42 @@ struct BiasRec {
     double bias {0};
 };
 
-enum MoveKind { MV_ORIENTATION = 0, MV_MET_EXCHANGE = 1, MV_MET_REGROWTH = 2, MV_CB_REGROWTH = 3, MV_LEARNED_EXCHANGE = 4 };
+enum MoveKind { MV_ORIENTATION = 0, MV_MET_EXCHANGE = 1, MV_MET_REGROWTH = 2, MV_CB_REGROWTH = 3, MV_LEARNED_EXCHANGE = 4,
+                MV_CTRG_SCAFFOLD = 5, MV_CTRG_JUMP = 6, MV_CTCB_SCAFFOLD = 7, MV_CTCB_JUMP = 8 };
+
+// Options of a scaffold regrowth movetype (src/simulation.cpp:400-560).
+struct ScaffoldMoveOpts {
+    int max_regrowth {0};
+    int max_seg_regrowth {0};
+    int max_num_recoils {0};
+    int max_c_attempts {0};
+};
+
+// IdealRandomWalks::num_walks (src/ideal_random_walk.cpp:14): the number of
+// nearest-neighbour walks of `steps` steps on the cubic lattice between two
+// sites, summed over the numbers of negative x and y steps.
+inline long double ideal_walks(int dx, int dy, int dz, int steps) {
+    int d[3] = {std::abs(dx), std::abs(dy), std::abs(dz)};
+    std::sort(d, d + 3);
+    int DX = d[0], DY = d[1], DZ = d[2];
+    int sum = DX + DY + DZ;
+    if (sum > steps || (steps - sum) % 2 != 0) return 0;
+    int n_minus = (steps - sum) / 2;
+    int n_plus = (steps - DX - DY + DZ) / 2;
+    auto fact = [](int n) {
+        long double f = 1;
+        for (int k = 2; k <= n; ++k) f *= k;
+        return f;
+    };
+    long double walks = 0;
+    for (int yb = 0; yb <= n_minus; ++yb)
+        for (int xb = 0; xb <= n_minus - yb; ++xb) {
+            if (n_plus - xb - yb < 0) continue;
+            walks += fact(steps) / (fact(xb) * fact(xb + DX) * fact(yb) * fact(yb + DY) *
+                                    fact(n_minus - xb - yb) * fact(n_plus - xb - yb));
+        }
+    return walks;
+}
 
 struct Config {
     // chain-type identities, index 0 is the scaffold
@@ -128,6 +181,7 @@ struct Config {
     int max_type_staples {999};
     std::vector<int> move_kinds;
     std::vector<double> move_cum;
+    std::vector<ScaffoldMoveOpts> move_opts;   // per movetype (scaffold regrowth options)
     std::vector<double> exchange_mults;
     bool adaptive_exchange {false};
     bool allow_nonsensical_ps {false};
@@ -1139,7 +1193,9 @@ class System {
     double modifier {1};
     double delta_e {0};
     // CB state (include/.../cb_movetypes.hpp:126-130)
-    double w_bias {1}, w_new_bias {1}, new_modifier {1};
+    Wt w_bias, w_new_bias;
+    double new_modifier {1};
+    bool ld_weights {false};   // Rosenbluth weights in long double (the reference's own arithmetic)
     bool regrow_old {false};
     std::vector<Key> old_keys;
     std::vector<V3> old_pos, old_ore;
@@ -1156,8 +1212,9 @@ class System {
         rejected = false;
         modifier = 1;
         delta_e = 0;
-        w_bias = 1;
-        w_new_bias = 1;
+        w_bias.ld = w_new_bias.ld = ld_weights;
+        w_bias.set(1);
+        w_new_bias.set(1);
         new_modifier = 1;
         regrow_old = false;
     }
@@ -1628,7 +1685,7 @@ class System {
             rejected = true;
             return;
         }
-        w_bias *= ros;
+        w_bias.mul(ros);
         for (double b : bf) w.push_back(b / ros);
         if (!regrow_old) {
             V3 p(0, 0, 0), o(0, 0, 0);
@@ -1668,12 +1725,12 @@ class System {
             while (!(old_keys[n].c == k.c && old_keys[n].d == k.d)) ++n;
             double de = 0;
             de += set_checked(gp.first, doms[gp.second].pos, old_ore[n]);
-            w_bias *= std::exp(-de);
+            w_bias.mul(std::exp(-de));
             assigned.push_back(k);
         }
         else {
             double de = set_growth_point(gp.first, gp.second);
-            w_bias *= std::exp(-de);
+            w_bias.mul(std::exp(-de));
         }
         if (!rejected) grow_staple(doms[gp.first].d, sel, true);
     }
@@ -1685,20 +1742,20 @@ class System {
         std::vector<int> sel = chains[ci];
         if (staple_is_connector(sel)) return false;
         auto bds = find_bound_domains(sel);
-        w_bias *= bds.size();
+        w_bias.mul((long double)bds.size());
         auto gp = bds[rng.uniform_int(0, (int)bds.size() - 1)];
         unassign_domains(sel);
         cb_set_gp_and_grow(gp, sel);
         if (rejected) return false;
-        w_bias /= num_bound_staple_domains(sel);
+        w_bias.div((long double)num_bound_staple_domains(sel));
         update_move_params();
         double tb = calc_move();
-        w_bias *= std::exp(-tb);
+        w_bias.mul(std::exp(-tb));
         // setup_for_regrow_old (:215)
         regrow_old = true;
         w_new_bias = w_bias;
         new_modifier = modifier;
-        w_bias = 1;
+        w_bias.set(1);
         old_keys = modified;
         old_pos = prev_pos;
         old_ore = prev_ore;
@@ -1711,8 +1768,7 @@ class System {
         cb_set_gp_and_grow(gp, sel);
         modifier = new_modifier;
         // test_cb_acceptance (:182)
-        double ratio = w_new_bias / w_bias;
-        if (test_acceptance(ratio)) {
+        if (test_acceptance_ld(w_new_bias.over(w_bias))) {
             reset_origami();
             update_move_params();
             calc_move();
@@ -1723,6 +1779,1023 @@ class System {
         prev_pos.clear();
         prev_ore.clear();
         return false;
+    }
+
+    // ============================== conserved-topology scaffold regrowth ===
+    // topConstraintPoints::StapleNetwork and Constraintpoints
+    // (src/top_constraint_points.cpp:26-602), CTRegrowthMCMovetype
+    // (src/movetypes.cpp:429-720), the recoil-growth movetypes
+    // (src/rg_movetypes.cpp) and the configurational-bias ones
+    // (src/cb_movetypes.cpp:406-984).  The reference's movetype factories
+    // always pass num_excluded_staples = 0 (src/simulation.cpp:409,538), so no
+    // staple is ever excluded and the excluded-staple branches drop out.
+    // Domains are keyed by domain id here (a chain never changes during these
+    // moves); a (chain, segment) key is (chain index, segment number).
+    using CKey = std::pair<int, int>;
+    using Ep = std::pair<int, V3>;   // (domain index in its chain, position)
+    struct CtPoints {
+        std::vector<int> scaffold_domains;
+        std::set<int> regrowth_staples;
+        std::vector<int> d_stack;
+        std::set<int> checked;
+        std::vector<V3> erased;
+        std::map<int, int> segs;
+        std::map<CKey, int> dirs;
+        std::map<int, int> growthpoints, stemdomains, inactive;
+        std::map<CKey, std::vector<Ep>> active, initial_active;
+        std::map<int, std::vector<int>> stemd_to_segs;
+        void clear() {   // Constraintpoints::reset_internal (:208)
+            scaffold_domains.clear();
+            regrowth_staples.clear();
+            d_stack.clear();
+            checked.clear();
+            erased.clear();
+            segs.clear();
+            dirs.clear();
+            growthpoints.clear();
+            stemdomains.clear();
+            inactive.clear();
+            active.clear();
+            initial_active.clear();
+            stemd_to_segs.clear();
+        }
+    } cp;
+    // StapleNetwork::m_domain_to_dir: never cleared by the reference; it only
+    // ever gains (staple, 0) -> +1 and (staple, 1) -> -1.
+    std::map<CKey, int> net_dirs;
+    struct Net {   // one StapleNetwork::scan_network result
+        bool external {false};
+        std::set<int> cs;
+        std::vector<std::pair<int, int>> gps, iaes;
+        std::vector<int> ds;
+        std::map<int, int> segs;
+    };
+
+    int scaffold_len() const { return (int)chains[0].size(); }
+    static bool has(const std::vector<int>& v, int x) { return std::find(v.begin(), v.end(), x) != v.end(); }
+
+    // StapleNetwork::scan_staple_topology (:91) and make_staple_stack (:141)
+    void net_scan(Net& n, int growth_d) {
+        int ci = doms[growth_d].c;
+        n.cs.insert(ci);
+        n.ds.push_back(growth_d);
+        std::vector<int> st = get_chain(ci);
+        int gd = doms[growth_d].d;
+        std::vector<int> stack_;
+        n.segs[growth_d] = 0;
+        net_dirs[{ci, 0}] = 1;
+        for (size_t di = gd + 1; di < st.size(); ++di) {
+            stack_.push_back(st[di]);
+            n.segs[st[di]] = 0;
+        }
+        net_dirs[{ci, 1}] = -1;
+        for (int di = gd - 1; di >= 0; --di) {
+            stack_.push_back(st[di]);
+            n.segs[st[di]] = 1;
+        }
+        for (int d : stack_) {
+            n.ds.push_back(d);
+            int bd = doms[d].bound;
+            if (bd < 0 || doms[bd].c == ci) continue;
+            int bci = doms[bd].c;
+            if (n.cs.count(bci)) {
+                bool external = false;
+                if (bci == 0) external = !has(cp.scaffold_domains, bd);
+                if (!external) {   // add_potential_inactive_endpoint (:166)
+                    if (has(n.ds, bd)) n.iaes.push_back({bd, d});
+                    else n.iaes.push_back({d, bd});
+                }
+                if (external) n.external = true;
+            }
+            else {
+                n.gps.push_back({d, bd});
+                net_scan(n, bd);
+            }
+        }
+    }
+
+    // Constraintpoints::find_growthpoints_endpoints (:461) with its helpers
+    void find_growthpoints_endpoints(const std::vector<int>& sds, int seg) {
+        for (int d : sds) {
+            cp.d_stack.push_back(d);
+            cp.segs[d] = seg;
+            int bd = doms[d].bound;
+            if (bd < 0 || doms[bd].c == doms[d].c || cp.checked.count(doms[bd].c)) continue;
+            Net n;
+            n.cs.insert(0);
+            net_scan(n, bd);
+            n.gps.push_back({d, bd});
+            if (n.external) {
+                // add_active_endpoints_on_scaffold (:547): note that the
+                // inactive-endpoint entries go under the staple's key
+                for (auto& g : n.gps)
+                    if (doms[g.first].c == 0) add_active_endpoint_seg(g.first, doms[g.first].pos, seg);
+                for (auto& e : n.iaes)
+                    if (doms[e.second].c == 0) add_active_endpoint_seg(e.first, doms[e.second].pos, seg);
+            }
+            else {
+                for (auto& g : n.gps) {   // add_growthpoints (:506)
+                    cp.growthpoints[g.first] = g.second;
+                    cp.stemdomains[g.second] = g.first;
+                }
+                for (auto& e : n.iaes) cp.inactive[e.first] = e.second;
+                for (int c : n.cs)
+                    if (c != 0) cp.regrowth_staples.insert(c);
+                cp.d_stack.insert(cp.d_stack.end(), n.ds.begin(), n.ds.end());
+                for (auto& kv : n.segs) cp.segs.insert(kv);
+                for (auto& kv : net_dirs) cp.dirs.insert(kv);
+            }
+            for (int c : n.cs) cp.checked.insert(c);
+        }
+    }
+
+    // Constraintpoints::calculate_constraintpoints, one segment (:225) or
+    // several (:241)
+    void calculate_constraintpoints(const std::vector<int>& sds, int dir) {
+        cp.scaffold_domains = sds;
+        cp.dirs[{doms[sds[0]].c, 0}] = dir;
+        find_growthpoints_endpoints(sds, 0);
+        cp.initial_active = cp.active;
+    }
+    void calculate_constraintpoints(const std::vector<std::vector<int>>& segs, const std::vector<int>& dirs_) {
+        for (auto& sg : segs) cp.scaffold_domains.insert(cp.scaffold_domains.end(), sg.begin(), sg.end());
+        int seg = 0;
+        for (size_t i = 0; i < segs.size(); ++i) {
+            if (!segs[i].empty()) {
+                cp.dirs[{doms[segs[i][0]].c, seg}] = dirs_[i];
+                find_growthpoints_endpoints(segs[i], seg);
+            }
+            seg++;
+        }
+        cp.initial_active = cp.active;
+    }
+
+    void add_active_endpoint_seg(int d, V3 pos, int seg) { cp.active[{doms[d].c, seg}].push_back({doms[d].d, pos}); }
+    void add_active_endpoint(int d, V3 pos) { add_active_endpoint_seg(d, pos, cp.segs.at(d)); }
+    void add_growthpoint(int gp, int stem) {
+        cp.growthpoints[gp] = stem;
+        cp.stemdomains[stem] = gp;
+    }
+
+    // Constraintpoints::remove_active_endpoint (:300)
+    void remove_active_endpoint(int d) {
+        cp.erased.clear();
+        auto& lst = cp.active[{doms[d].c, cp.segs.at(d)}];
+        std::vector<Ep> keep;
+        for (auto& e : lst) {
+            if (e.first == doms[d].d) cp.erased.push_back(e.second);
+            else keep.push_back(e);
+        }
+        lst = keep;
+    }
+    // remove_activated_endpoint (:325)
+    void remove_activated_endpoint(int d) {
+        auto it = cp.inactive.find(d);
+        if (it == cp.inactive.end()) return;
+        int ed = it->second;
+        auto& lst = cp.active[{doms[ed].c, cp.segs.at(ed)}];
+        for (size_t j = 0; j < lst.size(); ++j)
+            if (lst[j].first == doms[ed].d) {
+                lst.erase(lst.begin() + j);
+                break;
+            }
+    }
+    // update_endpoints (:345)
+    void update_endpoints(int d) {
+        remove_active_endpoint(d);
+        auto it = cp.inactive.find(d);
+        if (it != cp.inactive.end()) add_active_endpoint(it->second, doms[d].pos);
+    }
+    bool is_growthpoint(int d) const { return cp.growthpoints.count(d) > 0; }
+    bool is_stemdomain(int d) const { return cp.stemdomains.count(d) > 0; }
+    int get_dir(int d) {   // Constraintpoints::get_dir (:190)
+        int seg = cp.segs[d];
+        return cp.dirs[{doms[d].c, seg}];
+    }
+    // endpoint_reached (:363)
+    bool endpoint_reached(int d, V3 pos) {
+        for (auto& e : cp.active[{doms[d].c, cp.segs.at(d)}])
+            if (e.first == doms[d].d && e.second == pos) return true;
+        return false;
+    }
+    // calc_remaining_steps (:569)
+    int remaining_steps(int end_d, int d, int dir) const {
+        int steps;
+        int dd = doms[d].d;
+        if (cfg.cyclic && doms[d].c == 0) {
+            int N = scaffold_len();
+            if (dir > 0 && end_d < dd) steps = N + end_d - dd;
+            else if (dir < 0 && end_d > dd) steps = dd + N - end_d;
+            else if (dir == 0 || end_d == dd) steps = 0;
+            else steps = std::abs(end_d - dd);
+        }
+        else {
+            steps = std::abs(end_d - dd);
+        }
+        return steps;
+    }
+    // walks_remain (:398, :424)
+    bool walks_remain(int d, V3 pos) {
+        std::vector<int> sl;
+        if (is_stemdomain(d)) sl = cp.stemd_to_segs[d];
+        else sl = {cp.segs.at(d)};
+        for (int seg : sl) {
+            CKey key {doms[d].c, seg};
+            int dir = cp.dirs[key];
+            for (auto& e : cp.active[key]) {
+                int steps = remaining_steps(e.first, d, dir);
+                V3 dr = e.second - pos;
+                if (ideal_walks(dr.x, dr.y, dr.z, steps) == 0) return false;
+            }
+        }
+        return true;
+    }
+
+    // ---------------------------------------------- segment selection ---
+    std::map<int, V3> ct_prev_pos, ct_prev_ore;   // MCMovetype::m_prev_pos/m_prev_ore (keyed)
+    int ct_dir {0};                                // CTRegrowthMCMovetype::m_dir
+
+    // CTRegrowthMCMovetype::select_indices (src/movetypes.cpp:479)
+    std::vector<int> select_indices(int min_length, int seg, int max_regrowth) {
+        const std::vector<int>& sc = chains[0];
+        int seg_length = (int)sc.size();
+        int max_length = std::min(seg_length, max_regrowth);
+        int sel_length = rng.uniform_int(min_length, max_length);
+        int start_i = rng.uniform_int(0, seg_length - 1);
+        ct_dir = rng.uniform_int(0, 1);
+        if (ct_dir == 0) ct_dir = -1;
+        int cur = sc[start_i];
+        std::vector<int> out;
+        while (cur >= 0 && (int)out.size() != sel_length) {
+            out.push_back(cur);
+            cur = next(cur, ct_dir);
+        }
+        int back = next(sc[start_i], -ct_dir);
+        while (back >= 0 && (int)out.size() != sel_length) {
+            out.insert(out.begin(), back);
+            back = next(back, -ct_dir);
+        }
+        if ((int)out.size() < min_length) return select_indices(min_length, seg, max_regrowth);
+        if (cur >= 0) add_active_endpoint_seg(cur, doms[cur].pos, seg);
+        return out;
+    }
+
+    // CTRegrowthMCMovetype::check_for_stemds (src/movetypes.cpp:702)
+    void check_for_stemds(int cur, std::deque<int>& stems) {
+        if (doms[cur].state != BOUND) return;
+        int b = doms[cur].bound;
+        for (int sdir : {-1, 1}) {
+            int nb = next(b, sdir);
+            if (nb >= 0 && doms[nb].state == BOUND) {
+                int bn = doms[nb].bound;
+                if (doms[bn].c == 0) stems.push_back(bn);
+            }
+        }
+    }
+    // fill_seg (src/movetypes.cpp:669)
+    bool fill_seg(int start, int max_length, int seg_max, int dir, std::set<int>& in, std::deque<int>& stems,
+                  std::vector<int>& seg) {
+        int cur = start;
+        check_for_stemds(cur, stems);
+        int nd = start;
+        bool reached = false;
+        while ((int)seg.size() != seg_max && nd >= 0) {
+            nd = next(cur, dir);
+            if (nd < 0) break;
+            int nn = next(nd, dir);
+            if (nn >= 0 && in.count(nn)) break;
+            seg.push_back(nd);
+            in.insert(nd);
+            if ((int)in.size() == max_length) {
+                reached = true;
+                break;
+            }
+            cur = nd;
+            check_for_stemds(cur, stems);
+        }
+        return reached;
+    }
+    // select_noncontig_segs (src/movetypes.cpp:540)
+    void select_noncontig_segs(const ScaffoldMoveOpts& mo, std::vector<std::vector<int>>& segs,
+                               std::vector<std::vector<std::vector<int>>>& paired, std::vector<int>& stems_sel,
+                               std::vector<int>& dirs_) {
+        const std::vector<int>& sc = chains[0];
+        std::set<int> in;
+        int max_length = rng.uniform_int(2, mo.max_regrowth);
+        int seg_max = rng.uniform_int(2, mo.max_seg_regrowth + 1);
+        int start_i = rng.uniform_int(0, (int)sc.size() - 1);
+        int sd0 = sc[start_i];
+        int dir = rng.uniform_int(0, 1);
+        if (dir == 0) dir = -1;
+        if (next(sd0, dir) < 0) dir *= -1;
+        std::vector<int> cur_seg {sd0};
+        in.insert(sd0);
+        std::deque<int> stems;
+        dirs_.push_back(dir);
+        bool reached = fill_seg(sd0, max_length, seg_max, dir, in, stems, cur_seg);
+        segs.push_back(cur_seg);
+        while (!reached && !stems.empty()) {
+            cur_seg.clear();
+            int stemd = stems.front();
+            stems.pop_front();
+            if (in.count(stemd)) continue;
+            bool adjacent = false;
+            for (int td : {-1, 1}) {
+                int nd = next(stemd, td);
+                if (nd >= 0 && in.count(nd)) {
+                    adjacent = true;
+                    break;
+                }
+            }
+            if (adjacent) continue;
+            cur_seg.push_back(stemd);
+            in.insert(stemd);
+            stems_sel.push_back(stemd);
+            if ((int)in.size() == max_length) {
+                reached = true;
+                segs.push_back(cur_seg);
+                segs.push_back({});
+                paired.push_back({{}, {}});
+                dirs_.push_back(1);
+                dirs_.push_back(-1);
+                break;
+            }
+            int dir1 = rng.uniform_int(0, 1);
+            if (dir1 == 0) dir1 = -1;
+            int dp[2] = {dir1, -dir1};
+            dirs_.push_back(dp[0]);
+            dirs_.push_back(dp[1]);
+            std::vector<std::vector<int>> pair_ {{}, {}};
+            segs.push_back({});
+            segs.push_back({});
+            for (int i = 0; i < 2; ++i) {
+                dir = dp[i];
+                seg_max = rng.uniform_int(0, mo.max_seg_regrowth);
+                if (i == 0) max_length++;
+                std::vector<int> sg;
+                reached = fill_seg(stemd, max_length, seg_max, dir, in, stems, sg);
+                pair_[i] = sg;
+                if (!cur_seg.empty()) sg.insert(sg.begin(), cur_seg[0]);
+                segs[segs.size() - 2 + i] = sg;
+                if (reached) break;
+                cur_seg.clear();
+            }
+            paired.push_back(pair_);
+        }
+        int last = segs[0].back();
+        int nd = next(last, dirs_[0]);
+        if (nd >= 0) add_active_endpoint_seg(nd, doms[nd].pos, 0);
+        int seg_i = 1;
+        for (size_t i = 0; i < paired.size(); ++i) {
+            int stem = stems_sel[i];
+            add_growthpoint(doms[stem].bound, stem);
+            cp.stemd_to_segs[stem] = {seg_i, seg_i + 1};
+            for (auto& sg : paired[i]) {
+                int d = dirs_[seg_i];
+                int l = sg.empty() ? stem : sg.back();
+                int n2 = next(l, d);
+                if (n2 >= 0) add_active_endpoint_seg(n2, doms[n2].pos, seg_i);
+                seg_i++;
+            }
+        }
+    }
+
+    // Reference-side bookkeeping of the keyed maps, for reset_origami.
+    void ct_sync_prev() {
+        prev_pos.clear();
+        prev_ore.clear();
+        for (auto& k : modified) {
+            int id = dom_of(k);
+            prev_pos.push_back(ct_prev_pos.at(id));
+            prev_ore.push_back(ct_prev_ore.at(id));
+        }
+    }
+    void ct_save_unassign(int id, double* de) {
+        ct_prev_pos[id] = doms[id].pos;
+        ct_prev_ore[id] = doms[id].ore;
+        modified.push_back(key_of(id));
+        double e = unassign_domain(id);
+        if (de) *de += e;
+    }
+
+    // ------------------------------------------------------ recoil growth ---
+    // CTRGRegrowthMCMovetype state (include/.../rg_movetypes.hpp:73-108)
+    std::vector<int> rg_ds;
+    std::vector<int> catt_q, catt_wq;
+    std::vector<std::vector<int>> avail_q, avail_wq;
+    std::vector<double> c_opens;
+    std::map<int, V3> rg_old_pos, rg_old_ore, rg_new_pos, rg_new_ore;
+    std::vector<std::vector<V3>> erased_q;
+    double rg_delta_e {0}, rg_weight {1}, rg_weight_new {1};
+    int rg_di {0}, rg_d {0}, rg_ref {0};
+    bool rg_stemd {false};
+    int rg_catt {0}, rg_dmax {0};
+    std::vector<int> rg_avail;
+    int rg_max_recoils {0}, rg_max_c_attempts {0};
+
+    void rg_reset() {   // CTRGRegrowthMCMovetype::reset_internal (:63)
+        cp.clear();
+        ct_prev_pos.clear();
+        ct_prev_ore.clear();
+        rg_ds.clear();
+        catt_q.clear();
+        catt_wq.clear();
+        avail_q.clear();
+        avail_wq.clear();
+        c_opens.clear();
+        erased_q.clear();
+        rg_delta_e = 0;
+        rg_weight = 1;
+        rg_weight_new = 1;
+    }
+    static std::vector<int> all_cis() {
+        std::vector<int> v(36);
+        for (int i = 0; i < 36; ++i) v[i] = i;
+        return v;
+    }
+    // unassign_and_save_domains (:81)
+    double rg_unassign_and_save() {
+        double de = 0;
+        int d0 = rg_ds[0];
+        ct_prev_pos[d0] = doms[d0].pos;
+        ct_prev_ore[d0] = doms[d0].ore;
+        for (size_t i = 1; i < rg_ds.size(); ++i) ct_save_unassign(rg_ds[i], &de);
+        erased_q.clear();
+        return de;
+    }
+    void rg_unassign_domains() {   // :116
+        for (size_t i = 1; i < rg_ds.size(); ++i) unassign_domain(rg_ds[i]);
+        erased_q.clear();
+    }
+    double rg_set_config(int d, V3 p, V3 o) {   // set_config (:233)
+        double de = set_checked(d, p, o);
+        assigned.push_back(key_of(d));
+        update_endpoints(rg_d);
+        erased_q.push_back(cp.erased);
+        return de;
+    }
+    void rg_prepare_for_growth() {   // :245
+        rg_di++;
+        rg_d = rg_ds[rg_di];
+        rg_stemd = is_stemdomain(rg_d);
+        ct_dir = get_dir(rg_d);
+        rg_catt = 0;
+        if (rg_stemd) {
+            rg_dmax = 1;
+            rg_avail.clear();
+            rg_ref = cp.stemdomains[rg_d];
+        }
+        else {
+            rg_dmax = rg_max_c_attempts;
+            rg_avail = all_cis();
+            rg_ref = next(rg_d, -ct_dir);
+        }
+    }
+    void rg_restore_endpoints() {   // :289
+        remove_activated_endpoint(rg_d);
+        std::vector<V3> er = erased_q.back();
+        erased_q.pop_back();
+        for (auto& p : er) add_active_endpoint(rg_d, p);
+    }
+    double rg_prepare_for_regrowth() {   // :263
+        rg_di--;
+        rg_d = rg_ds[rg_di];
+        ct_dir = get_dir(rg_d);
+        double de = unassign_domain(rg_d);
+        assigned.pop_back();
+        rg_restore_endpoints();
+        rg_stemd = is_stemdomain(rg_d);
+        if (rg_stemd) {
+            rg_dmax = 1;
+            rg_catt = 1;
+            rg_avail.clear();
+            rg_ref = cp.stemdomains[rg_d];
+        }
+        else {
+            rg_dmax = rg_max_c_attempts;
+            rg_catt = catt_q[rg_di];
+            rg_avail = avail_q[rg_di];
+            rg_ref = next(rg_d, -ct_dir);
+        }
+        return de;
+    }
+    // select_trial_config (:298): configuration ci = 6 * (position step) + orientation
+    void rg_select_trial(V3& p, V3& o) {
+        if (rg_stemd) {
+            p = doms[rg_ref].pos;
+            o = -doms[rg_ref].ore;
+        }
+        else {
+            int k = rng.uniform_int(0, (int)rg_avail.size() - 1);
+            int i = rg_avail[k];
+            rg_avail.erase(rg_avail.begin() + k);
+            p = kUnit[i / 6] + doms[rg_ref].pos;
+            o = kUnit[i % 6];
+        }
+    }
+    // calc_p_config_open (:316)
+    double rg_p_open(V3 p, V3 o) {
+        double de = check_domain_constraints(rg_d, p, o);
+        if (violated) {
+            violated = false;
+            return 0;
+        }
+        if (!walks_remain(rg_d, p)) return 0;
+        if (occupancy(p) == UNBOUND) {
+            int od = unbound_at(p);
+            bool same = doms[od].c == doms[rg_d].c;
+            bool endpoint = endpoint_reached(rg_d, p);
+            if (!(same || endpoint || rg_stemd)) return 0;
+        }
+        return std::fmin(1, std::exp(-de));
+    }
+    bool rg_test_open(double p) {   // test_config_open (:346)
+        p = std::fmin(1, p);
+        if (p == 1) return true;
+        return p > rng.uniform_real();
+    }
+    // recoil_regrow (:177)
+    double recoil_regrow() {
+        double de = 0;
+        rg_di = 0;
+        rg_d = rg_ds[0];
+        ct_dir = get_dir(rg_d);
+        catt_q.assign(rg_ds.size(), 0);
+        avail_q.assign(rg_ds.size(), {});
+        c_opens.assign(rg_ds.size(), 0);
+        c_opens[0] = 1;
+        rg_prepare_for_growth();
+        int recoils = 0;
+        while (true) {
+            V3 p, o;
+            double pc = 0;
+            bool open = false;
+            while (!open && rg_catt != rg_dmax) {
+                rg_catt++;
+                rg_select_trial(p, o);
+                pc = rg_p_open(p, o);
+                open = rg_test_open(pc);
+            }
+            if (open) {
+                if (recoils != 0) recoils--;
+                de += rg_set_config(rg_d, p, o);
+                catt_q[rg_di] = rg_catt;
+                avail_q[rg_di] = rg_avail;
+                c_opens[rg_di] = pc;
+                if (rg_di == (int)rg_ds.size() - 1) break;
+                rg_prepare_for_growth();
+            }
+            else {
+                if (recoils == rg_max_recoils || rg_di == 1) {
+                    rejected = true;
+                    break;
+                }
+                recoils++;
+                de += rg_prepare_for_regrowth();
+            }
+        }
+        return de;
+    }
+    // test_config_avail (:418)
+    bool rg_test_avail() {
+        int feels = 0;
+        if (feels == rg_max_recoils || rg_di == (int)rg_ds.size() - 1) return true;
+        rg_prepare_for_growth();
+        bool avail;
+        while (true) {
+            V3 p, o;
+            bool open = false;
+            while (!open && rg_catt != rg_dmax) {
+                rg_catt++;
+                rg_select_trial(p, o);
+                double pc = rg_p_open(p, o);
+                open = rg_test_open(pc);
+            }
+            if (open) {
+                feels++;
+                if (feels == rg_max_recoils || rg_di == (int)rg_ds.size() - 1) {
+                    feels--;
+                    avail = true;
+                    break;
+                }
+                rg_set_config(rg_d, p, o);
+                catt_q[rg_di] = rg_catt;
+                avail_q[rg_di] = rg_avail;
+                rg_prepare_for_growth();
+            }
+            else {
+                if (feels == 0) {
+                    avail = false;
+                    break;
+                }
+                feels--;
+                rg_prepare_for_regrowth();
+            }
+        }
+        while (feels != 0) {
+            rg_di--;
+            feels--;
+            rg_d = rg_ds[rg_di];
+            unassign_domain(rg_d);
+            rg_restore_endpoints();
+        }
+        rg_di--;
+        rg_d = rg_ds[rg_di];
+        return avail;
+    }
+    // calc_weights (:363): `pos`/`ore` hold the configuration being weighed
+    void rg_calc_weights() {
+        rg_di = 0;
+        rg_d = rg_ds[0];
+        while (rg_di != (int)rg_ds.size() - 1) {
+            rg_di++;
+            rg_d = rg_ds[rg_di];
+            rg_stemd = is_stemdomain(rg_d);
+            ct_dir = get_dir(rg_d);
+            int avail_cs = 1;
+            if (!rg_stemd) {
+                rg_ref = next(rg_d, -ct_dir);
+                int catt = catt_wq[rg_di];
+                rg_avail = avail_wq[rg_di];
+                while (catt != rg_max_c_attempts) {
+                    catt++;
+                    V3 p, o;
+                    rg_select_trial(p, o);
+                    double pc = rg_p_open(p, o);
+                    if (rg_test_open(pc)) {
+                        set_checked(rg_d, p, o);
+                        update_endpoints(rg_d);
+                        erased_q.push_back(cp.erased);
+                        int dir_s = ct_dir, ref_s = rg_ref;
+                        bool stem_s = rg_stemd;
+                        std::vector<int> avail_s = rg_avail;
+                        avail_cs += rg_test_avail();
+                        rg_avail = avail_s;
+                        rg_stemd = stem_s;
+                        rg_ref = ref_s;
+                        ct_dir = dir_s;
+                        unassign_domain(rg_d);
+                        rg_restore_endpoints();
+                    }
+                }
+            }
+            rg_weight *= avail_cs / c_opens[rg_di - 1];
+            set_checked(rg_d, ct_prev_pos.at(rg_d), ct_prev_ore.at(rg_d));
+            update_endpoints(rg_d);
+            erased_q.push_back(cp.erased);
+        }
+        rg_weight /= c_opens[rg_di];
+    }
+    // calc_old_c_opens (:481)
+    void rg_calc_old_c_opens() {
+        rg_di = 0;
+        c_opens[0] = 1;
+        while (rg_di != (int)rg_ds.size() - 1) {
+            rg_di++;
+            rg_d = rg_ds[rg_di];
+            catt_q[rg_di] = 1;
+            V3 p = rg_old_pos.at(rg_d), o = rg_old_ore.at(rg_d);
+            rg_stemd = is_stemdomain(rg_d);
+            c_opens[rg_di] = rg_p_open(p, o);
+            rg_set_config(rg_d, p, o);
+            if (rg_stemd) {
+                avail_q[rg_di].clear();
+            }
+            else {
+                avail_q[rg_di] = all_cis();
+                ct_dir = get_dir(rg_d);
+                rg_ref = next(rg_d, -ct_dir);
+                V3 dp = p - rg_old_pos.at(rg_ref);
+                int k = 0;
+                while (k < 6 && !(kUnit[k] == dp)) ++k;
+                int ko = 0;
+                while (ko < 6 && !(kUnit[ko] == o)) ++ko;
+                if (k == 6 || ko == 6) throw std::runtime_error("old configuration is not a neighbour step");
+                int ci = 6 * k + ko;
+                auto& av = avail_q[rg_di];
+                av.erase(std::remove(av.begin(), av.end(), ci), av.end());
+            }
+        }
+    }
+    // test_rg_acceptance (:515)
+    bool rg_test_acceptance() {
+        long double ratio = rg_weight_new / rg_weight * std::exp(-rg_delta_e);
+        if (test_acceptance_ld(ratio)) {
+            ct_prev_pos = rg_new_pos;
+            ct_prev_ore = rg_new_ore;
+            ct_sync_prev();
+            reset_origami();
+            return true;
+        }
+        modified.clear();
+        assigned.clear();
+        prev_pos.clear();
+        prev_ore.clear();
+        return false;
+    }
+    bool test_acceptance_ld(long double p) {   // MCMovetype::test_acceptance (src/movetypes.cpp:142)
+        if (!ld_weights) return test_acceptance((double)p);
+        double pa = (double)(std::fmin((long double)1, p) * (long double)modifier);
+        if (pa == 1) return true;
+        return pa > rng.uniform_real();
+    }
+    // The weights of the new and old configurations and the acceptance test,
+    // common to both recoil-growth movetypes.  remove_first(k) says whether
+    // the k-th endpoint reset also drops the endpoints of the first domain.
+    bool rg_weigh_and_test(bool remove_first[3]) {
+        update_move_params();   // add_external_bias (:76)
+        rg_delta_e += calc_move();
+        // setup_for_calc_new_weights (:137)
+        catt_wq = catt_q;
+        avail_wq = avail_q;
+        rg_old_pos = ct_prev_pos;
+        rg_old_ore = ct_prev_ore;
+        modified.clear();
+        rg_unassign_and_save();
+        cp.active = cp.initial_active;
+        if (remove_first[0]) remove_active_endpoint(rg_ds[0]);
+        rg_calc_weights();
+        rg_unassign_domains();
+        cp.active = cp.initial_active;
+        if (remove_first[1]) remove_active_endpoint(rg_ds[0]);
+        rg_calc_old_c_opens();
+        // setup_for_calc_old_weights (:146)
+        rg_weight_new = rg_weight;
+        rg_weight = 1;
+        catt_wq = catt_q;
+        avail_wq = avail_q;
+        rg_new_pos = ct_prev_pos;
+        rg_new_ore = ct_prev_ore;
+        modified.clear();
+        rg_unassign_and_save();
+        cp.active = cp.initial_active;
+        if (remove_first[2]) remove_active_endpoint(rg_ds[0]);
+        rg_calc_weights();
+        return rg_test_acceptance();
+    }
+    // CTRGScaffoldRegrowthMCMovetype::internal_attempt_move (:629)
+    bool ctrg_scaffold(const ScaffoldMoveOpts& mo) {
+        rg_reset();
+        rg_max_recoils = mo.max_num_recoils;
+        rg_max_c_attempts = mo.max_c_attempts;
+        std::vector<int> sel = select_indices(2, 0, mo.max_regrowth);
+        calculate_constraintpoints(sel, ct_dir);   // setup_constraints (:126)
+        bool whole = cfg.cyclic && (int)sel.size() == scaffold_len();
+        if (!whole) remove_active_endpoint(sel[0]);
+        rg_ds = cp.d_stack;
+        rg_delta_e += rg_unassign_and_save();
+        rg_delta_e += recoil_regrow();
+        if (rejected) {
+            ct_sync_prev();
+            return false;
+        }
+        bool whole_ds = cfg.cyclic && (int)rg_ds.size() == scaffold_len();
+        // the second reset's condition reads differently in the reference (:673)
+        bool rf[3] = {!whole_ds, !cfg.cyclic && (int)rg_ds.size() == scaffold_len(), !whole_ds};
+        return rg_weigh_and_test(rf);
+    }
+    // CTRGJumpScaffoldRegrowthMCMovetype::internal_attempt_move (:792)
+    bool ctrg_jump(const ScaffoldMoveOpts& mo) {
+        rg_reset();
+        rg_max_recoils = mo.max_num_recoils;
+        rg_max_c_attempts = mo.max_c_attempts;
+        std::vector<std::vector<int>> segs;
+        std::vector<std::vector<std::vector<int>>> paired;
+        std::vector<int> stems, dirs_;
+        select_noncontig_segs(mo, segs, paired, stems, dirs_);
+        calculate_constraintpoints(segs, dirs_);
+        remove_active_endpoint(segs[0][0]);
+        for (int st : stems) add_growthpoint(doms[st].bound, st);
+        rg_ds = cp.d_stack;
+        rg_delta_e += rg_unassign_and_save();
+        rg_delta_e += recoil_regrow();
+        if (rejected) {
+            ct_sync_prev();
+            return false;
+        }
+        bool rf[3] = {true, true, true};
+        return rg_weigh_and_test(rf);
+    }
+
+    // --------------------------------------------- configurational bias ---
+    std::map<int, V3> cb_old_pos, cb_old_ore;
+
+    void ctcb_unassign(const std::vector<int>& ds) {   // CBMCMovetype::unassign_domains (:200)
+        for (int id : ds) ct_save_unassign(id, nullptr);
+    }
+    // CTCBRegrowthMCMovetype::calc_bias (:480) after CBMCMovetype::calc_biases (:58)
+    void ctcb_select_and_set(int i, const std::vector<int>& ds) {
+        int dom = ds[i];
+        V3 p_prev = doms[ds[i - 1]].pos;
+        std::vector<V3> cpos, core;
+        std::vector<double> bf;
+        calc_biases(p_prev, dom, cpos, core, bf);
+        std::vector<long double> w(bf.begin(), bf.end());   // FP64 values unless ld_weights
+        for (size_t k = 0; k < cpos.size(); ++k) {
+            V3 p = cpos[k];
+            if (occupancy(p) == UNBOUND) {
+                int od = unbound_at(p);
+                bool same = doms[od].c == doms[dom].c;
+                bool endpoint = endpoint_reached(dom, p);
+                if (!(same || endpoint)) w[k] = 0;
+            }
+            if (!walks_remain(dom, p)) w[k] = 0;
+        }
+        long double sum = 0;
+        for (auto x : w) sum = ld_weights ? sum + x : (long double)((double)sum + (double)x);
+        if (sum == 0) {
+            rejected = true;
+            return;
+        }
+        w_bias.mul(sum);
+        std::vector<double> nw;
+        for (auto x : w) nw.push_back(ld_weights ? (double)(x / sum) : (double)x / (double)sum);
+        if (!regrow_old) {   // select_and_set_new_config (:132)
+            V3 p(0, 0, 0), o(0, 0, 0);
+            double cum = 0;
+            double r = rng.uniform_real();
+            for (size_t n = 0; n < nw.size(); ++n) {
+                cum += nw[n];
+                if (r < cum) {
+                    p = cpos[n];
+                    o = core[n];
+                    break;
+                }
+            }
+            if (o == V3(0, 0, 0)) o = kUnit[rng.uniform_int(0, 5)];
+            set_checked(dom, p, o);
+        }
+        else {
+            set_checked(dom, cb_old_pos.at(dom), cb_old_ore.at(dom));
+        }
+        assigned.push_back(key_of(dom));
+    }
+    // CTCBRegrowthMCMovetype::grow_chain (:463)
+    void ctcb_grow_chain(const std::vector<int>& ds) {
+        if (ds.size() <= 1) return;
+        for (size_t i = 1; i < ds.size(); ++i) {
+            int d = ds[i];
+            ct_dir = get_dir(d);
+            ctcb_select_and_set((int)i, ds);
+            if (rejected) break;
+            update_endpoints(d);
+            if (is_growthpoint(d)) {
+                ctcb_grow_staple_and_update(d);
+                if (rejected) break;
+            }
+        }
+    }
+    // grow_staple_and_update_endpoints (:533) with RegrowthMCMovetype::grow_staple
+    void ctcb_grow_staple_and_update(int gold) {
+        int gnew = cp.growthpoints[gold];
+        int c_i = doms[gnew].c;
+        if (c_i == 0) return;
+        if (regrow_old) {   // set_old_growth_point (:168)
+            double de = set_checked(gnew, doms[gold].pos, cb_old_ore.at(gnew));
+            w_bias.mul(std::exp(-de));
+            assigned.push_back(key_of(gnew));
+        }
+        else {
+            double de = set_growth_point(gnew, gold);
+            w_bias.mul(std::exp(-de));
+        }
+        if (rejected) return;
+        update_endpoints(gnew);
+        std::vector<int> ch = get_chain(c_i);
+        int d_i = doms[gnew].d;
+        std::vector<int> three(ch.begin() + d_i, ch.end());
+        if (three.size() > 1) ctcb_grow_chain(three);
+        if (rejected) return;
+        std::vector<int> five(ch.begin(), ch.begin() + d_i + 1);
+        std::reverse(five.begin(), five.end());
+        if (five.size() > 1) ctcb_grow_chain(five);
+    }
+    void ctcb_reset() {   // CTCBRegrowthMCMovetype::reset_internal (:459)
+        cp.clear();
+        ct_prev_pos.clear();
+        ct_prev_ore.clear();
+    }
+    void ctcb_setup_regrow_old() {   // CBMCMovetype::setup_for_regrow_old (:215)
+        regrow_old = true;
+        w_new_bias = w_bias;
+        new_modifier = modifier;
+        w_bias.set(1);
+        modified.clear();
+        assigned.clear();
+        cb_old_pos = ct_prev_pos;
+        cb_old_ore = ct_prev_ore;
+    }
+    // test_cb_acceptance (:182) with the long double weights
+    bool ctcb_test_acceptance() {
+        if (test_acceptance_ld(w_new_bias.over(w_bias))) {
+            ct_sync_prev();
+            reset_origami();
+            update_move_params();
+            calc_move();
+            return true;
+        }
+        modified.clear();
+        assigned.clear();
+        prev_pos.clear();
+        prev_ore.clear();
+        return false;
+    }
+    // CTCBScaffoldRegrowthMCMovetype::internal_attempt_move (:691)
+    bool ctcb_scaffold(const ScaffoldMoveOpts& mo) {
+        ctcb_reset();
+        std::vector<int> sd = select_indices(2, 0, mo.max_regrowth);
+        calculate_constraintpoints(sd, ct_dir);
+        bool whole = cfg.cyclic && (int)sd.size() == scaffold_len();
+        if (!whole) remove_active_endpoint(sd[0]);
+        std::set<int> staples = cp.regrowth_staples;
+        std::vector<int> unassign_sc(sd.begin() + 1, sd.end());
+        ctcb_unassign(unassign_sc);
+        for (int c : staples) ctcb_unassign(get_chain(c));
+        if (is_growthpoint(sd[0])) {
+            ctcb_grow_staple_and_update(sd[0]);
+            if (rejected) {
+                ct_sync_prev();
+                return false;
+            }
+        }
+        ctcb_grow_chain(sd);
+        if (rejected) {
+            ct_sync_prev();
+            return false;
+        }
+        update_move_params();   // add_external_bias (:52)
+        w_bias.mul(std::exp(-calc_move()));
+        ctcb_setup_regrow_old();
+        cp.active = cp.initial_active;
+        if (!whole) remove_active_endpoint(sd[0]);
+        ctcb_unassign(unassign_sc);
+        for (int c : staples) ctcb_unassign(get_chain(c));
+        if (is_growthpoint(sd[0])) ctcb_grow_staple_and_update(sd[0]);
+        ctcb_grow_chain(sd);
+        modifier = 1;
+        return ctcb_test_acceptance();
+    }
+    // CTCBJumpScaffoldRegrowthMCMovetype::set_first_seg_domain (:968)
+    void ctcb_first_seg_domain(int dnew) {
+        int dold = cp.stemdomains[dnew];
+        if (!walks_remain(dnew, doms[dold].pos)) {
+            rejected = true;
+            return;
+        }
+        ct_dir = get_dir(dnew);
+        double de = set_growth_point(dnew, dold);
+        w_bias.mul(std::exp(-de));
+    }
+    // the growth sequence of CTCBJumpScaffoldRegrowthMCMovetype (:880-906)
+    bool ctcb_jump_grow(const std::vector<std::vector<int>>& segs,
+                        const std::vector<std::vector<std::vector<int>>>& paired, const std::vector<int>& stems) {
+        if (is_growthpoint(segs[0][0])) {
+            ctcb_grow_staple_and_update(segs[0][0]);
+            if (rejected) return false;
+        }
+        ctcb_grow_chain(segs[0]);
+        if (rejected) return false;
+        for (size_t i = 0; i < stems.size(); ++i) {
+            ctcb_first_seg_domain(stems[i]);
+            if (rejected) return false;
+            for (auto sg : paired[i]) {
+                sg.insert(sg.begin(), stems[i]);
+                ctcb_grow_chain(sg);
+                if (rejected) return false;
+            }
+        }
+        return true;
+    }
+    // CTCBJumpScaffoldRegrowthMCMovetype::internal_attempt_move (:864)
+    bool ctcb_jump(const ScaffoldMoveOpts& mo) {
+        ctcb_reset();
+        std::vector<std::vector<int>> segs;
+        std::vector<std::vector<std::vector<int>>> paired;
+        std::vector<int> stems, dirs_;
+        select_noncontig_segs(mo, segs, paired, stems, dirs_);
+        calculate_constraintpoints(segs, dirs_);
+        remove_active_endpoint(segs[0][0]);
+        std::vector<int> rd = cp.d_stack;
+        std::vector<int> to_unassign(rd.begin() + 1, rd.end());
+        ctcb_unassign(to_unassign);
+        if (!ctcb_jump_grow(segs, paired, stems)) {
+            ct_sync_prev();
+            return false;
+        }
+        update_move_params();   // add_external_bias
+        w_bias.mul(std::exp(-calc_move()));
+        ctcb_setup_regrow_old();
+        cp.active = cp.initial_active;
+        remove_active_endpoint(segs[0][0]);
+        ctcb_unassign(to_unassign);
+        if (!ctcb_jump_grow(segs, paired, stems)) {
+            // the reference returns here with the new configuration saved as
+            // the one to revert to (m_prev_pos, :927)
+            ct_sync_prev();
+            return false;
+        }
+        modifier = 1;
+        return ctcb_test_acceptance();
     }
 
     // OrientationRotationMCMovetype::internal_attempt_move (src/orientation_movetype.cpp:30)
@@ -1767,6 +2840,10 @@ class System {
         case MV_MET_REGROWTH: acc = met_regrowth(); break;
         case MV_CB_REGROWTH: acc = cb_regrowth(); break;
         case MV_LEARNED_EXCHANGE: acc = learned_exchange(); break;
+        case MV_CTRG_SCAFFOLD: acc = ctrg_scaffold(cfg.move_opts[m]); break;
+        case MV_CTRG_JUMP: acc = ctrg_jump(cfg.move_opts[m]); break;
+        case MV_CTCB_SCAFFOLD: acc = ctcb_scaffold(cfg.move_opts[m]); break;
+        case MV_CTCB_JUMP: acc = ctcb_jump(cfg.move_opts[m]); break;
         }
         attempts[m]++;
         if (acc) accepts[m]++;

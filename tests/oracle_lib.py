@@ -57,6 +57,12 @@ class OracleReplica:
             self.L.oracle_destroy(self.h)
             self.h = None
 
+    def set_long_double(self, on=True):
+        """Rosenbluth weights in long double, as the reference computes them
+        (the engine and the oracle's default use FP64)."""
+        self.L.oracle_set_long_double.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        self.L.oracle_set_long_double(self.h, 1 if on else 0)
+
     def run(self, steps, trace=True):
         tr = np.zeros((steps, 8)) if trace else None
         rc = self.L.oracle_run(self.h, steps, self.step, tr.ctypes.data if trace else None)

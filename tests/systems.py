@@ -55,6 +55,22 @@ def linear_pairs(n):
     return [(i, i + 1) for i in range(0, n - 1, 2)]
 
 
+def ring(n):
+    """Positions of n scaffold domains around the edge of a square on the z=0
+    plane (n a multiple of 4): a closed loop, for cyclic scaffolds."""
+    side = n // 4
+    pos = []
+    for k in range(side):
+        pos.append([k, 0, 0])
+    for k in range(side):
+        pos.append([side, k, 0])
+    for k in range(side):
+        pos.append([side - k, side, 0])
+    for k in range(side):
+        pos.append([0, side - k, 0])
+    return pos
+
+
 def make_system(n, pairs, seed, positions, seq_len=16, cyclic=False):
     rng = random.Random(seed)
     scaf_seq = ["".join(rng.choice("ACGT") for _ in range(seq_len)) for _ in range(n)]
@@ -81,15 +97,51 @@ MOVES = {
              ("Met staple exchange", "MetStapleExchange", "1/4"),
              ("Met staple regrowth", "MetStapleRegrowth", "1/4"),
              ("CB staple regrowth", "CBStapleRegrowth", "1/4")],
+    # the reference's standard moveset (examples/moveset_standard.json layout):
+    # staple moves plus conserved-topology recoil-growth scaffold regrowth
+    "ctrg": [("Orientation rotation", "OrientationRotation", "2/6"),
+             ("Met staple exchange", "MetStapleExchange", "1/6"),
+             ("CB staple regrowth", "CBStapleRegrowth", "1/6"),
+             ("Contiguous CTRG scaffold regrowth", "CTRGScaffoldRegrowth", "1/6",
+              dict(max_num_recoils=1, max_c_attempts=36, max_regrowth=4)),
+             ("Non-contiguous CTRG scaffold regrowth", "CTRGJumpScaffoldRegrowth", "1/6",
+              dict(max_num_recoils=1, max_c_attempts=36, max_regrowth=4, max_seg_regrowth=2))],
+    # two recoils and fewer trial configurations per domain
+    "ctrg2": [("Orientation rotation", "OrientationRotation", "1/4"),
+              ("Met staple exchange", "MetStapleExchange", "1/4"),
+              ("CB staple regrowth", "CBStapleRegrowth", "1/4"),
+              ("Contiguous CTRG scaffold regrowth", "CTRGScaffoldRegrowth", "1/4",
+               dict(max_num_recoils=2, max_c_attempts=12, max_regrowth=6))],
+    # every scaffold regrowth movetype together
+    "ctall": [("Orientation rotation", "OrientationRotation", "2/8"),
+              ("Met staple exchange", "MetStapleExchange", "1/8"),
+              ("CB staple regrowth", "CBStapleRegrowth", "1/8"),
+              ("Contiguous CTRG scaffold regrowth", "CTRGScaffoldRegrowth", "1/8",
+               dict(max_num_recoils=1, max_c_attempts=36, max_regrowth=5)),
+              ("Non-contiguous CTRG scaffold regrowth", "CTRGJumpScaffoldRegrowth", "1/8",
+               dict(max_num_recoils=1, max_c_attempts=36, max_regrowth=5, max_seg_regrowth=2)),
+              ("Contiguous CTCB scaffold regrowth", "CTCBScaffoldRegrowth", "1/8", dict(max_regrowth=5)),
+              ("Non-contiguous CTCB scaffold regrowth", "CTCBJumpScaffoldRegrowth", "1/8",
+               dict(max_regrowth=5, max_seg_regrowth=2))],
+    # conserved-topology configurational-bias scaffold regrowth
+    "ctcb": [("Orientation rotation", "OrientationRotation", "2/6"),
+             ("Met staple exchange", "MetStapleExchange", "1/6"),
+             ("CB staple regrowth", "CBStapleRegrowth", "1/6"),
+             ("Contiguous CTCB scaffold regrowth", "CTCBScaffoldRegrowth", "1/6", dict(max_regrowth=4)),
+             ("Non-contiguous CTCB scaffold regrowth", "CTCBJumpScaffoldRegrowth", "1/6",
+              dict(max_regrowth=4, max_seg_regrowth=2))],
 }
 
 
 def moves_json(kind):
     mts = []
-    for label, t, f in MOVES[kind]:
+    for entry in MOVES[kind]:
+        label, t, f = entry[:3]
         m = {"label": label, "type": t, "freq": f}
         if t == "MetStapleExchange":
             m["adaptive_exchange"] = False
+        if len(entry) > 3:
+            m.update(entry[3])
         mts.append(m)
     return {"origami": {"movetypes": mts}}
 
@@ -135,6 +187,21 @@ CASES = {
     # the 48-domain PTMC system's shape: 24 two-domain staple types, NN on random 16-mers, 1 uM
     "c3": ("grid48", "met3", dict(stacking_ene=1000, staple_M=1e-6, temp=340, max_total_staples=48,
                                   max_type_staples=2)),
+    # scaffold regrowth (conserved topology): recoil growth and configurational bias
+    "s24a": ("grid24", "ctrg", dict(stacking_ene=-1000, staple_M=1e-3, temp=335, max_total_staples=24,
+                                    max_type_staples=4)),
+    "s24b": ("grid24", "ctrg2", dict(domain_type="ThreeQuarterTurn", stacking_ene=-1500, staple_M=1e-3,
+                                     temp=325, max_total_staples=24, max_type_staples=4, centering_freq=97,
+                                     constraint_check_freq=101)),
+    "s24c": ("grid24", "ctcb", dict(stacking_ene=-1000, staple_M=1e-3, temp=335, max_total_staples=24,
+                                    max_type_staples=4, bias_functions_file="biases.json",
+                                    bias_functions_mult=0.7)),
+    # cyclic scaffold (a closed ring), every scaffold movetype
+    "r24": ("ring24", "ctall", dict(stacking_ene=-1000, staple_M=1e-3, temp=330, max_total_staples=24,
+                                    max_type_staples=4)),
+    # the 48-domain system's shape with the reference's standard moveset
+    "s48": ("grid48", "ctrg", dict(stacking_ene=-1000, staple_M=1e-4, temp=335, max_total_staples=48,
+                                   max_type_staples=2)),
 }
 
 
@@ -142,6 +209,9 @@ def system_for(name):
     if name == "four":
         pairs = [(1, 0), (3, 2)]
         return make_system(4, pairs, seed=4, positions=[[i, 0, 0] for i in range(4)])
+    if name.startswith("ring"):
+        n = int(name[4:])
+        return make_system(n, linear_pairs(n), seed=n + 1, positions=ring(n), cyclic=True)
     if name.startswith("grid"):
         n = int(name[4:])
         return make_system(n, staple_pairs(n), seed=n, positions=serpentine(n, 4))

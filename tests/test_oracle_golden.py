@@ -1,7 +1,12 @@
 """The oracle against the reference itself: golden per-step traces recorded
 from the reference compiled from its own sources (tests/golden/make_golden.py).
 Energies must agree bit for bit at every step, and the random-draw count and
-final configuration exactly."""
+final configuration exactly.
+
+The oracle runs with its Rosenbluth weights in long double, as the reference
+computes them (include/.../cb_movetypes.hpp:126-127); in its default FP64 mode
+(the engine's arithmetic) it matches every fixture but one, s24a_s11, whose
+run meets a weight ratio within a rounding of 1 at step 19885."""
 import glob
 import gzip
 import json
@@ -25,6 +30,7 @@ def load(path):
 def test_oracle_matches_reference_trace(path):
     fx = load(path)
     o = OracleReplica(inp(fx["case"]), seed=fx["seed"], replica=0)
+    o.set_long_double(True)
     tr = o.run(fx["steps"])
     ref = np.array(fx["trace"], dtype=np.float64)
     assert ref.shape == tr.shape
@@ -39,8 +45,63 @@ def test_oracle_matches_reference_trace(path):
 
 def test_fixtures_cover_the_move_and_potential_variants():
     cases = {load(p)["case"] for p in FIXTURES}
-    assert {"c1", "g24a", "g24b", "g24c", "g24d", "g24e"} <= cases
+    assert {"c1", "g24a", "g24b", "g24c", "g24d", "g24e", "s24a", "s24b", "s24c", "r24", "s48"} <= cases
     # the fixtures exercise bound staples and stacking, not just empty lattices
     fx = load(os.path.join(GOLDEN, "g24a_s3.json.gz"))
     t = np.array(fx["trace"])
     assert t[:, 2].max() >= 4 and t[:, 5].max() >= 2
+
+
+# fixtures whose runs the FP64 weights follow to the end
+FP64_EXACT = [p for p in FIXTURES if not p.endswith("s24a_s11.json.gz")]
+
+
+@pytest.mark.parametrize("path", FP64_EXACT, ids=[os.path.basename(p)[:-8] for p in FP64_EXACT])
+def test_oracle_fp64_weights_match_reference_trace(path):
+    fx = load(path)
+    o = OracleReplica(inp(fx["case"]), seed=fx["seed"], replica=0)
+    tr = o.run(fx["steps"])
+    ref = np.array(fx["trace"], dtype=np.float64)
+    np.testing.assert_array_equal(tr[:, [0, 2, 3, 4, 5, 7]], ref[:, [0, 2, 3, 4, 5, 7]])
+    np.testing.assert_array_equal(tr[:, 1], ref[:, 1])
+    assert o.config() == fx["final_config"]
+
+
+def test_fp64_weights_part_from_long_double_only_at_a_tie():
+    """s24a_s11: at step 19885 (a CB staple regrowth) the new/old weight
+    ratio lies within a rounding of 1, below 1 in the reference's 80-bit long
+    double and not below 1 in FP64, so only the reference draws a number for
+    the acceptance test; the runs agree exactly up to that step."""
+    fx = load(os.path.join(GOLDEN, "s24a_s11.json.gz"))
+    ref = np.array(fx["trace"], dtype=np.float64)
+    o = OracleReplica(inp(fx["case"]), seed=fx["seed"], replica=0)
+    tr = o.run(fx["steps"])
+    k = 19884
+    np.testing.assert_array_equal(tr[:k], ref[:k])
+    assert tr[k, 7] == ref[k, 7] - 1
+
+
+def test_ideal_random_walk_counts():
+    """IdealRandomWalks::num_walks against tests/src/test_ideal_random_walk.cpp:16-92."""
+    import ctypes
+    from oracle_lib import lib
+    L = lib()
+    L.oracle_ideal_walks.restype = ctypes.c_double
+    L.oracle_ideal_walks.argtypes = [ctypes.c_int] * 4
+    nw = lambda d, n: L.oracle_ideal_walks(d[0], d[1], d[2], n)
+    assert nw((0, 2, 3), 5) == 10
+    assert nw((0, 2, 3), 7) == 665
+    assert nw((0, 2, 3), 6) == 0
+    assert abs(nw((0, 2, 3), 51) / 5.947398897268465e+36 - 1) < 1e-12
+    assert nw((2, 2, 2), 8) == nw((-2, -2, -2), 8)
+    base = nw((1, 2, 3), 8)
+    for d in [(-1, 2, 3), (1, -2, 3), (1, 2, -3), (-1, -2, 3), (-1, 2, -3), (1, -2, -3), (-1, -2, -3),
+              (2, 1, 3), (3, 2, 1), (1, 3, 2)]:
+        assert nw(d, 8) == base
+    # zero exactly when the distance exceeds the steps or has the other parity
+    for dx in range(-3, 4):
+        for dy in range(-3, 4):
+            for dz in range(-3, 4):
+                for n in range(0, 10):
+                    l1 = abs(dx) + abs(dy) + abs(dz)
+                    assert (nw((dx, dy, dz), n) == 0) == (l1 > n or (n - l1) % 2 == 1)
