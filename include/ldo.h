@@ -193,6 +193,14 @@ ldo_status ldo_us_get_windows(ldo_engine* e, int32_t* window_of_replica, int n, 
 ldo_status ldo_replica_status_noalloc(ldo_engine* e, int32_t* status_of_replica, int n, int32_t* worst,
                                       int32_t* n_bad);
 
+/* No counterpart in the reference.  The engine's exponential, y[i] =
+ * exp(x[i]) for i < n, evaluated on the GPU: the function every acceptance
+ * probability and Rosenbluth weight of the engine uses (Cody-Waite reduction
+ * and a Taylor series, below one unit in the last place), with the same bits
+ * as its host version, so that host code can repeat the engine's decisions
+ * exactly.  The reference uses the C library's exp instead. */
+ldo_status ldo_engine_exp(const double* x, double* y, int n);
+
 /* Learned insertion proposal (movetype "LearnedStapleExchange"; engine
  * extension with no counterpart in the reference, which only proposes
  * uniformly: src/movetypes.cpp:98-120).  A network of three 256-wide GELU

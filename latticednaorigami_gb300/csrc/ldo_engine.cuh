@@ -20,7 +20,9 @@
 // ns + (k-1)*lmax + d.
 #pragma once
 #include <stdint.h>
+#include "ldo_ct.h"
 #include "ldo_learn.h"
+#include "ldo_math.h"
 #include "ldo_types.h"
 
 #ifndef LDO_DEV
@@ -164,9 +166,10 @@ struct Delta {
     int stacked;
 };
 
-// One out-of-line copy of exp keeps the hot code small (instruction fetch,
-// not arithmetic, limits this kernel).
-__device__ __noinline__ double dexp(double x) { return exp(x); }
+// The engine's own exponential (ldo_math.h: the same bits as host code
+// computing it), one out-of-line copy to keep the hot code small (instruction
+// fetch, not arithmetic, limits this kernel).
+__device__ __noinline__ double dexp(double x) { return ldo_math::exp(x); }
 
 struct Scratch {
     // MCMovetype reversal lists (include/.../movetypes.hpp:156-163)
@@ -193,7 +196,8 @@ struct Scratch {
 #define CMD_SNAP(k) ((k) + 1)
 #define CMD_REST(k) (((k) + 1) << 4)
 enum : int { CMD_MORE = 1 << 8, CMD_REST_FIRST = 1 << 9, CMD_STOP = 1 << 10 };
-enum : int { PH_POST = 1, PH_CB2 = 2, PH_CB3 = 3 };
+enum : int { PH_POST = 1, PH_CB2 = 2, PH_CB3 = 3, PH_RG2 = 4, PH_RG3 = 5, PH_RG4 = 6, PH_RG5 = 7, PH_CT2 = 8,
+             PH_CT3 = 9 };
 constexpr int N_SNAPSHOTS = 3;
 
 // Scratch of the FourBody evaluation.
@@ -237,6 +241,7 @@ struct Rep : public LdoState<C> {
     const LdoRepCtl* ctl;
     const double* grid;
     const double* learn_w;   // learned insertion proposal weights (LDO_LEARN_TABLE)
+    LdoCtWork<C>* ct;        // scaffold regrowth working memory (global), or null
     int learn_tb;            // temperature bin of the current tables
     // scalars of the current table set and controls, cached in the object
     int t_dense, t_stack_dense, imax, dim;
@@ -2202,6 +2207,1285 @@ struct Rep : public LdoState<C> {
         return acc;
     }
 
+    // ================================ conserved-topology scaffold regrowth ===
+    // Constraintpoints / StapleNetwork (src/top_constraint_points.cpp), the
+    // segment selection of CTRegrowthMCMovetype (src/movetypes.cpp:469-720),
+    // recoil growth (src/rg_movetypes.cpp) and configurational bias
+    // (src/cb_movetypes.cpp:406-984).  No staple is ever excluded: the
+    // reference's movetype factories pass num_excluded_staples = 0
+    // (src/simulation.cpp:409,538).  The maps of the reference are arrays over
+    // domain slots in the replica's working memory (LdoCtWork); endpoint lists
+    // keep the reference's insertion order.  Reversal goes through the move
+    // snapshots: 1 = the regrown domains unassigned, 2 = the new configuration.
+    static constexpr unsigned long long CT_ALL36 = (1ull << 36) - 1ull;
+    // index of a domain within its chain (scaffold slots are their index)
+    __device__ int didx(int i) const { return scs[i] == 0 ? i : sd[i]; }
+
+    __device__ __noinline__ void ct_clear() {   // Constraintpoints::reset_internal (:208)
+        LdoCtWork<C>& w = *ct;
+        int dc = sys->dcap;
+        #pragma unroll 1
+        for (int s = 0; s < dc && s < C::DCAP; ++s) {
+            w.seg[s] = -1;
+            w.gp_to[s] = -1;
+            w.stem_of[s] = -1;
+            w.inact[s] = -1;
+            w.nssegs[s] = 0;
+            w.in_scaf[s] = 0;
+            w.in_ds[s] = 0;
+            w.in_sel[s] = 0;
+        }
+        #pragma unroll 1
+        for (int k = 0; k < LDO_CT_MAX_SEGS; ++k) w.sdir[k] = 0;
+        w.checked = 0;
+        w.regrow = 0;
+        w.n_rd = 0;
+        w.n_ep = 0;
+        w.n_ep0 = 0;
+        w.n_er = 0;
+        w.n_eq = 0;
+        w.eq_off[0] = 0;
+        w.n_segs = 0;
+        w.seg_off[0] = 0;
+        w.n_stems = 0;
+        w.pair_off[0] = 0;
+        w.n_fr = 0;
+    }
+
+    // ------------------------------------------------------- endpoints ---
+    __device__ void ct_add_ep(int cs, int seg, int d, V3 p) {
+        LdoCtWork<C>& w = *ct;
+        if (w.n_ep >= LdoCtWork<C>::EPC) {
+            fail(LDO_RS_CAPACITY);
+            return;
+        }
+        LdoCtEp& e = w.ep[w.n_ep++];
+        e.pos = p;
+        e.cs = (int16_t)cs;
+        e.seg = (int8_t)seg;
+        e.d = (int16_t)d;
+    }
+    // add_active_endpoint(domain, pos, seg) (:280)
+    __device__ void ct_add_ep_seg(int i, V3 p, int seg) { ct_add_ep(scs[i], seg, didx(i), p); }
+    // add_active_endpoint(domain, pos) (:272): the segment of the domain
+    __device__ int ct_seg_at(int i) {   // m_segs.at (throws for a domain without one)
+        int sg = ct->seg[i];
+        if (sg < 0) fail(LDO_RS_INVARIANT);
+        return sg;
+    }
+    __device__ void ct_add_ep_at(int i, V3 p) { ct_add_ep_seg(i, p, ct_seg_at(i)); }
+    // remove_active_endpoint (:300): every endpoint on the domain, kept in m_erased_endpoints
+    __device__ __noinline__ void ct_remove_ep(int i) {
+        LdoCtWork<C>& w = *ct;
+        w.n_er = 0;
+        int seg = ct_seg_at(i), cs = scs[i], d = didx(i);
+        int k = 0;
+        #pragma unroll 1
+        for (int j = 0; j < w.n_ep; ++j) {
+            LdoCtEp e = w.ep[j];
+            if (e.cs == cs && e.seg == seg && e.d == d) w.er[w.n_er++] = e.pos;
+            else w.ep[k++] = e;
+        }
+        w.n_ep = k;
+    }
+    // remove_activated_endpoint (:325): the first endpoint the domain activated
+    __device__ __noinline__ void ct_remove_activated(int i) {
+        LdoCtWork<C>& w = *ct;
+        int ed = w.inact[i];
+        if (ed < 0) return;
+        int seg = ct_seg_at(ed), cs = scs[ed], d = didx(ed);
+        #pragma unroll 1
+        for (int j = 0; j < w.n_ep; ++j) {
+            if (w.ep[j].cs == cs && w.ep[j].seg == seg && w.ep[j].d == d) {
+                #pragma unroll 1
+                for (int q = j; q + 1 < w.n_ep; ++q) w.ep[q] = w.ep[q + 1];
+                w.n_ep--;
+                break;
+            }
+        }
+    }
+    // update_endpoints (:345)
+    __device__ __noinline__ void ct_update_endpoints(int i) {
+        ct_remove_ep(i);
+        int ed = ct->inact[i];
+        if (ed >= 0) ct_add_ep_at(ed, pos(i));
+    }
+    // endpoint_reached (:363)
+    __device__ __noinline__ bool ct_endpoint_reached(int i, V3 p) {
+        LdoCtWork<C>& w = *ct;
+        int seg = ct_seg_at(i), cs = scs[i], d = didx(i);
+        #pragma unroll 1
+        for (int j = 0; j < w.n_ep; ++j)
+            if (w.ep[j].cs == cs && w.ep[j].seg == seg && w.ep[j].d == d && w.ep[j].pos == p) return true;
+        return false;
+    }
+    __device__ void ct_reset_endpoints() {   // reset_active_endpoints (:293)
+        LdoCtWork<C>& w = *ct;
+        #pragma unroll 1
+        for (int j = 0; j < w.n_ep0; ++j) w.ep[j] = w.ep0[j];
+        w.n_ep = w.n_ep0;
+    }
+    __device__ void ct_push_erased() {   // m_erased_endpoints_q.push_back(get_erased_endpoints())
+        LdoCtWork<C>& w = *ct;
+        if (w.n_eq + 1 >= C::DCAP + 2 || w.eq_off[w.n_eq] + w.n_er > LdoCtWork<C>::EQC) {
+            fail(LDO_RS_CAPACITY);
+            return;
+        }
+        int o = w.eq_off[w.n_eq];
+        #pragma unroll 1
+        for (int k = 0; k < w.n_er; ++k) w.eq[o + k] = w.er[k];
+        w.eq_off[w.n_eq + 1] = (int16_t)(o + w.n_er);
+        w.n_eq++;
+    }
+    // CTRGRegrowthMCMovetype::restore_endpoints (src/rg_movetypes.cpp:289)
+    __device__ __noinline__ void ct_restore_endpoints(int i) {
+        LdoCtWork<C>& w = *ct;
+        ct_remove_activated(i);
+        if (w.n_eq <= 0) {
+            fail(LDO_RS_INVARIANT);
+            return;
+        }
+        w.n_eq--;
+        #pragma unroll 1
+        for (int k = w.eq_off[w.n_eq]; k < w.eq_off[w.n_eq + 1]; ++k) ct_add_ep_at(i, w.eq[k]);
+    }
+    // direction of growth of a (chain, segment): the scaffold's from the
+    // selection, a staple's +1 (3' segment 0) or -1 (5' segment 1)
+    __device__ int ct_dir_of(int cs, int seg) const {
+        if (cs == 0) return (seg >= 0 && seg < LDO_CT_MAX_SEGS) ? ct->sdir[seg] : 0;
+        return seg == 0 ? 1 : seg == 1 ? -1 : 0;
+    }
+    __device__ int ct_get_dir(int i) {   // Constraintpoints::get_dir (:190)
+        int sg = ct->seg[i];
+        if (sg < 0) {
+            ct->seg[i] = 0;
+            sg = 0;
+        }
+        return ct_dir_of(scs[i], sg);
+    }
+    // calc_remaining_steps (:569)
+    __device__ int ct_remaining(int end_d, int i, int dir) const {
+        int dd = didx(i);
+        if (cyclic && scs[i] == 0) {
+            if (dir > 0 && end_d < dd) return ns + end_d - dd;
+            if (dir < 0 && end_d > dd) return dd + ns - end_d;
+            if (dir == 0 || end_d == dd) return 0;
+        }
+        return end_d > dd ? end_d - dd : dd - end_d;
+    }
+    // walks_remain (:398, :424).  IdealRandomWalks::num_walks
+    // (src/ideal_random_walk.cpp:14) is zero exactly when the lattice distance
+    // exceeds the remaining steps or differs from them in parity, and that
+    // is the only use the reference makes of it here.
+    __device__ __noinline__ bool ct_walks_ok(int i, V3 p) {
+        LdoCtWork<C>& w = *ct;
+        int segs_[2];
+        int n;
+        if (w.stem_of[i] >= 0) {
+            n = w.nssegs[i];
+            segs_[0] = w.ssegs[i][0];
+            segs_[1] = w.ssegs[i][1];
+        }
+        else {
+            n = 1;
+            segs_[0] = ct_seg_at(i);
+        }
+        int cs = scs[i];
+        #pragma unroll 1
+        for (int k = 0; k < n; ++k) {
+            int seg = segs_[k];
+            int dir = ct_dir_of(cs, seg);
+            #pragma unroll 1
+            for (int j = 0; j < w.n_ep; ++j) {
+                if (w.ep[j].cs != cs || w.ep[j].seg != seg) continue;
+                int steps = ct_remaining(w.ep[j].d, i, dir);
+                V3 dr = sub(w.ep[j].pos, p);
+                int x = vx(dr), y = vy(dr), z = vz(dr);
+                int l1 = (x < 0 ? -x : x) + (y < 0 ? -y : y) + (z < 0 ? -z : z);
+                if (l1 > steps || ((steps - l1) & 1)) return false;
+            }
+        }
+        return true;
+    }
+
+    // ------------------------------------------------- staple networks ---
+    // StapleNetwork::scan_network / scan_staple_topology (:35, :91): a depth-
+    // first walk over the staples bound to one another, in the reference's
+    // recursion order (frames: chain slot, growth domain, next stack index).
+    __device__ __noinline__ void ct_scan(int growth) {
+        LdoCtWork<C>& w = *ct;
+        w.external = 0;
+        w.net_cs = 1ull;
+        w.n_gps = 0;
+        w.n_iaes = 0;
+        w.n_nds = 0;
+        int top = 0;
+        w.net_cs |= 1ull << scs[growth];
+        w.nds[w.n_nds++] = (int16_t)growth;
+        w.in_ds[growth] = 1;
+        {
+            int cs = scs[growth], len = chain_len(cs), gd = didx(growth);
+            #pragma unroll 1
+            for (int d = 0; d < len; ++d) w.nseg[slot_of(cs, d)] = (int8_t)(d < gd ? 1 : 0);
+        }
+        w.scan_cs[0] = (int16_t)scs[growth];
+        w.scan_g[0] = (int16_t)didx(growth);
+        w.scan_k[0] = 0;
+        top = 1;
+        #pragma unroll 1
+        while (top > 0 && !bad()) {
+            int f = top - 1;
+            int cs = w.scan_cs[f], gd = w.scan_g[f], len = chain_len(cs);
+            if (w.scan_k[f] >= len - 1) {
+                --top;
+                continue;
+            }
+            int k = w.scan_k[f]++;
+            int n3 = len - 1 - gd;
+            int di = k < n3 ? gd + 1 + k : gd - 1 - (k - n3);
+            int d = slot_of(cs, di);
+            if (w.n_nds >= C::DCAP) {
+                fail(LDO_RS_CAPACITY);
+                return;
+            }
+            w.nds[w.n_nds++] = (int16_t)d;
+            w.in_ds[d] = 1;
+            int bd = bnd[d];
+            if (bd < 0 || scs[bd] == cs) continue;
+            int bcs = scs[bd];
+            if (w.net_cs & (1ull << bcs)) {
+                bool external = false;
+                if (bcs == 0) external = !w.in_scaf[bd];
+                if (!external) {   // add_potential_inactive_endpoint (:166)
+                    if (w.in_ds[bd]) {
+                        w.ia_a[w.n_iaes] = (int16_t)bd;
+                        w.ia_b[w.n_iaes] = (int16_t)d;
+                    }
+                    else {
+                        w.ia_a[w.n_iaes] = (int16_t)d;
+                        w.ia_b[w.n_iaes] = (int16_t)bd;
+                    }
+                    w.n_iaes++;
+                }
+                if (external) w.external = 1;
+            }
+            else {
+                w.gps_a[w.n_gps] = (int16_t)d;
+                w.gps_b[w.n_gps] = (int16_t)bd;
+                w.n_gps++;
+                if (top >= C::KMAX + 2 || w.n_nds >= C::DCAP) {
+                    fail(LDO_RS_CAPACITY);
+                    return;
+                }
+                w.net_cs |= 1ull << bcs;
+                w.nds[w.n_nds++] = (int16_t)bd;
+                w.in_ds[bd] = 1;
+                int blen = chain_len(bcs), bg = didx(bd);
+                #pragma unroll 1
+                for (int q = 0; q < blen; ++q) w.nseg[slot_of(bcs, q)] = (int8_t)(q < bg ? 1 : 0);
+                w.scan_cs[top] = (int16_t)bcs;
+                w.scan_g[top] = (int16_t)bg;
+                w.scan_k[top] = 0;
+                ++top;
+            }
+        }
+    }
+    // Constraintpoints::find_growthpoints_endpoints (:461) over the scaffold
+    // domains seg_dom[off .. off + n) of segment `seg`
+    __device__ __noinline__ void ct_find_gp_ep(const int16_t* list, int n, int seg) {
+        LdoCtWork<C>& w = *ct;
+        #pragma unroll 1
+        for (int t = 0; t < n && !bad(); ++t) {
+            int d = list[t];
+            if (w.n_rd >= C::DCAP) {
+                fail(LDO_RS_CAPACITY);
+                return;
+            }
+            w.rd[w.n_rd++] = (int16_t)d;
+            w.seg[d] = (int8_t)seg;
+            int bd = bnd[d];
+            if (bd < 0 || scs[bd] == scs[d] || (w.checked & (1ull << scs[bd]))) continue;
+            ct_scan(bd);
+            if (bad()) return;
+            w.gps_a[w.n_gps] = (int16_t)d;
+            w.gps_b[w.n_gps] = (int16_t)bd;
+            w.n_gps++;
+            if (w.external) {   // add_active_endpoints_on_scaffold (:547)
+                #pragma unroll 1
+                for (int q = 0; q < w.n_gps; ++q)
+                    if (scs[w.gps_a[q]] == 0) ct_add_ep_seg(w.gps_a[q], pos(w.gps_a[q]), seg);
+                #pragma unroll 1
+                for (int q = 0; q < w.n_iaes; ++q)
+                    if (scs[w.ia_b[q]] == 0) ct_add_ep_seg(w.ia_a[q], pos(w.ia_b[q]), seg);
+            }
+            else {
+                #pragma unroll 1
+                for (int q = 0; q < w.n_gps; ++q) {   // add_growthpoints (:506)
+                    w.gp_to[w.gps_a[q]] = w.gps_b[q];
+                    w.stem_of[w.gps_b[q]] = w.gps_a[q];
+                }
+                #pragma unroll 1
+                for (int q = 0; q < w.n_iaes; ++q) w.inact[w.ia_a[q]] = w.ia_b[q];
+                w.regrow |= w.net_cs & ~1ull;
+                if (w.n_rd + w.n_nds > C::DCAP) {
+                    fail(LDO_RS_CAPACITY);
+                    return;
+                }
+                #pragma unroll 1
+                for (int q = 0; q < w.n_nds; ++q) {
+                    int x = w.nds[q];
+                    w.rd[w.n_rd++] = (int16_t)x;
+                    if (w.seg[x] < 0) w.seg[x] = w.nseg[x];
+                }
+            }
+            w.checked |= w.net_cs;
+            #pragma unroll 1
+            for (int q = 0; q < w.n_nds; ++q) w.in_ds[w.nds[q]] = 0;
+        }
+    }
+    // calculate_constraintpoints over the selected segments (:225, :241)
+    __device__ __noinline__ void ct_calc_constraintpoints() {
+        LdoCtWork<C>& w = *ct;
+        #pragma unroll 1
+        for (int k = w.seg_off[0]; k < w.seg_off[w.n_segs]; ++k) w.in_scaf[w.seg_dom[k]] = 1;
+        #pragma unroll 1
+        for (int k = 0; k < w.n_segs && !bad(); ++k) {
+            int n = w.seg_off[k + 1] - w.seg_off[k];
+            if (n == 0) continue;
+            w.sdir[k] = w.seg_dirin[k];
+            ct_find_gp_ep(w.seg_dom + w.seg_off[k], n, k);
+        }
+        #pragma unroll 1
+        for (int j = 0; j < w.n_ep; ++j) w.ep0[j] = w.ep[j];
+        w.n_ep0 = w.n_ep;
+    }
+
+    // ------------------------------------------------ segment selection ---
+    // CTRegrowthMCMovetype::select_indices (src/movetypes.cpp:479), min length 2
+    __device__ __noinline__ void ct_select_indices(int max_regrowth) {
+        LdoCtWork<C>& w = *ct;
+        int max_length = ns < max_regrowth ? ns : max_regrowth;
+        #pragma unroll 1
+        for (int guard = 0; guard < 1000; ++guard) {
+            int sel = rng.uniform_int(2, max_length);
+            int start = rng.uniform_int(0, ns - 1);
+            int dir = rng.uniform_int(0, 1) == 0 ? -1 : 1;
+            // forward from the start in dir, then backward from before it
+            int nf = 0, cur = start;
+            #pragma unroll 1
+            while (cur >= 0 && nf != sel) {
+                ++nf;
+                cur = next(cur, dir);
+            }
+            int nb = 0, back = next(start, -dir);
+            #pragma unroll 1
+            while (back >= 0 && nf + nb != sel) {
+                ++nb;
+                back = next(back, -dir);
+            }
+            if (nf + nb < 2) continue;
+            w.dir = dir;
+            int x = start;
+            #pragma unroll 1
+            for (int t = 0; t < nf; ++t) {
+                w.seg_dom[nb + t] = (int16_t)x;
+                x = next(x, dir);
+            }
+            x = next(start, -dir);
+            #pragma unroll 1
+            for (int t = 0; t < nb; ++t) {
+                w.seg_dom[nb - 1 - t] = (int16_t)x;
+                x = next(x, -dir);
+            }
+            w.n_segs = 1;
+            w.seg_off[0] = 0;
+            w.seg_off[1] = (int16_t)(nf + nb);
+            w.seg_dirin[0] = (int8_t)dir;
+            if (cur >= 0) ct_add_ep_seg(cur, pos(cur), 0);
+            return;
+        }
+        fail(LDO_RS_ITERCAP);
+    }
+    // check_for_stemds (src/movetypes.cpp:702)
+    __device__ void ct_check_stems(int cur, int& qt) {
+        LdoCtWork<C>& w = *ct;
+        if (st[cur] != BOUND) return;
+        int b = bnd[cur];
+        #pragma unroll 1
+        for (int sdir = -1; sdir <= 1; sdir += 2) {
+            int nb = next(b, sdir);
+            if (nb >= 0 && st[nb] == BOUND) {
+                int bn = bnd[nb];
+                if (scs[bn] == 0) {
+                    if (qt >= 4 * C::DCAP) {
+                        fail(LDO_RS_CAPACITY);
+                        return;
+                    }
+                    w.stemq[qt++] = (int16_t)bn;
+                }
+            }
+        }
+    }
+    // fill_seg (src/movetypes.cpp:669): appends to out[*n] (and to out2 if
+    // given) a segment that already holds cnt0 domains
+    __device__ bool ct_fill_seg(int start, int max_length, int seg_max, int dir, int& n_in, int& qt, int16_t* out,
+                                int* n, int16_t* out2, int* n2, int cnt0) {
+        LdoCtWork<C>& w = *ct;
+        int cur = start;
+        ct_check_stems(cur, qt);
+        int nd = start;
+        int cnt = cnt0;
+        #pragma unroll 1
+        while (cnt != seg_max && nd >= 0 && !bad()) {
+            nd = next(cur, dir);
+            if (nd < 0) break;
+            int nn = next(nd, dir);
+            if (nn >= 0 && w.in_sel[nn]) break;
+            out[(*n)++] = (int16_t)nd;
+            if (out2) out2[(*n2)++] = (int16_t)nd;
+            cnt++;
+            w.in_sel[nd] = 1;
+            n_in++;
+            if (n_in == max_length) return true;
+            cur = nd;
+            ct_check_stems(cur, qt);
+        }
+        return false;
+    }
+    // CTRegrowthMCMovetype::select_noncontig_segs (src/movetypes.cpp:540)
+    __device__ __noinline__ void ct_select_noncontig(int max_regrowth, int max_seg_regrowth) {
+        LdoCtWork<C>& w = *ct;
+        int max_length = rng.uniform_int(2, max_regrowth);
+        int seg_max = rng.uniform_int(2, max_seg_regrowth + 1);
+        int start = rng.uniform_int(0, ns - 1);
+        int dir = rng.uniform_int(0, 1) == 0 ? -1 : 1;
+        if (next(start, dir) < 0) dir = -dir;
+        int n_in = 1, qh = 0, qt = 0;
+        w.in_sel[start] = 1;
+        int nd_ = 0;   // domains written to seg_dom
+        int np = 0;    // domains written to pair_dom
+        w.seg_dom[nd_++] = (int16_t)start;
+        w.seg_dirin[0] = (int8_t)dir;
+        bool reached = ct_fill_seg(start, max_length, seg_max, dir, n_in, qt, w.seg_dom, &nd_, nullptr, nullptr, 1);
+        w.n_segs = 1;
+        w.seg_off[1] = (int16_t)nd_;
+        w.n_stems = 0;
+        #pragma unroll 1
+        while (!reached && qh < qt && !bad()) {
+            int stemd = w.stemq[qh++];
+            if (w.in_sel[stemd]) continue;
+            int a = next(stemd, -1), b = next(stemd, 1);
+            if ((a >= 0 && w.in_sel[a]) || (b >= 0 && w.in_sel[b])) continue;
+            if (w.n_segs + 2 > LDO_CT_MAX_SEGS) {
+                fail(LDO_RS_CAPACITY);
+                return;
+            }
+            w.in_sel[stemd] = 1;
+            n_in++;
+            int si = w.n_stems++;
+            w.stems[si] = (int16_t)stemd;
+            if (n_in == max_length) {
+                reached = true;
+                w.seg_dom[nd_++] = (int16_t)stemd;
+                w.seg_dirin[w.n_segs] = 1;
+                w.seg_off[++w.n_segs] = (int16_t)nd_;
+                w.seg_dirin[w.n_segs] = -1;
+                w.seg_off[++w.n_segs] = (int16_t)nd_;
+                w.pair_off[2 * si + 1] = (int16_t)np;
+                w.pair_off[2 * si + 2] = (int16_t)np;
+                break;
+            }
+            int dir1 = rng.uniform_int(0, 1) == 0 ? -1 : 1;
+            int dp[2] = {dir1, -dir1};
+            // segment a: the stem, then its fill in dir1; segment b: the fill in -dir1
+            int ka = w.n_segs, kb = w.n_segs + 1;
+            w.seg_dirin[ka] = (int8_t)dp[0];
+            w.seg_dirin[kb] = (int8_t)dp[1];
+            w.seg_dom[nd_++] = (int16_t)stemd;
+            bool done_b = false;
+            #pragma unroll 1
+            for (int i = 0; i < 2; ++i) {
+                int smax = rng.uniform_int(0, max_seg_regrowth);
+                if (i == 0) max_length++;
+                reached = ct_fill_seg(stemd, max_length, smax, dp[i], n_in, qt, w.seg_dom, &nd_, w.pair_dom, &np, 0);
+                w.pair_off[2 * si + 1 + i] = (int16_t)np;
+                if (i == 0) w.seg_off[ka + 1] = (int16_t)nd_;
+                else {
+                    w.seg_off[kb + 1] = (int16_t)nd_;
+                    done_b = true;
+                }
+                if (reached) break;
+            }
+            if (!done_b) {
+                w.seg_off[kb + 1] = (int16_t)nd_;
+                w.pair_off[2 * si + 2] = (int16_t)np;
+            }
+            w.n_segs += 2;
+        }
+        // endpoints past the ends of the segments, growth points of the stems
+        int last = w.seg_dom[w.seg_off[1] - 1];
+        int nx = next(last, w.seg_dirin[0]);
+        if (nx >= 0) ct_add_ep_seg(nx, pos(nx), 0);
+        int seg_i = 1;
+        #pragma unroll 1
+        for (int i = 0; i < w.n_stems; ++i) {
+            int stem = w.stems[i];
+            int gp = bnd[stem];
+            if (gp < 0) {
+                fail(LDO_RS_INVARIANT);
+                return;
+            }
+            w.gp_to[gp] = (int16_t)stem;
+            w.stem_of[stem] = (int16_t)gp;
+            w.ssegs[stem][0] = (int8_t)seg_i;
+            w.ssegs[stem][1] = (int8_t)(seg_i + 1);
+            w.nssegs[stem] = 2;
+            #pragma unroll 1
+            for (int k = 0; k < 2; ++k) {
+                int d = w.seg_dirin[seg_i];
+                int a0 = w.pair_off[2 * i + k], a1 = w.pair_off[2 * i + k + 1];
+                int l = a1 > a0 ? w.pair_dom[a1 - 1] : stem;
+                int n2 = next(l, d);
+                if (n2 >= 0) ct_add_ep_seg(n2, pos(n2), seg_i);
+                seg_i++;
+            }
+        }
+    }
+
+    // ---------------------------------------------------- recoil growth ---
+    __device__ __noinline__ void rg_prepare_for_growth() {   // src/rg_movetypes.cpp:245
+        LdoCtWork<C>& w = *ct;
+        w.di++;
+        int d = w.rd[w.di];
+        w.d = d;
+        w.stemd = w.stem_of[d] >= 0;
+        w.dir = ct_get_dir(d);
+        w.catt = 0;
+        if (w.stemd) {
+            w.dmax = 1;
+            w.avail = 0;
+            w.ref = w.stem_of[d];
+        }
+        else {
+            w.dmax = w.max_c_attempts;
+            w.avail = CT_ALL36;
+            w.ref = next(d, -w.dir);
+            if (w.ref < 0) fail(LDO_RS_INVARIANT);
+        }
+    }
+    __device__ __noinline__ double rg_prepare_for_regrowth() {   // :263
+        LdoCtWork<C>& w = *ct;
+        w.di--;
+        int d = w.rd[w.di];
+        w.d = d;
+        w.dir = ct_get_dir(d);
+        double de = unassign_domain(d);
+        ct_restore_endpoints(d);
+        w.stemd = w.stem_of[d] >= 0;
+        if (w.stemd) {
+            w.dmax = 1;
+            w.catt = 1;
+            w.avail = 0;
+            w.ref = w.stem_of[d];
+        }
+        else {
+            w.dmax = w.max_c_attempts;
+            w.catt = w.catt_q[w.di];
+            w.avail = w.av_q[w.di];
+            w.ref = next(d, -w.dir);
+            if (w.ref < 0) fail(LDO_RS_INVARIANT);
+        }
+        return de;
+    }
+    // select_trial_config (:298): configuration ci = 6 * step + orientation,
+    // the k-th of the untried ones (ascending, as the reference's list)
+    __device__ __noinline__ void rg_select_trial(V3& p, int& o) {
+        LdoCtWork<C>& w = *ct;
+        if (w.stemd) {
+            p = pos(w.ref);
+            o = ore[w.ref] ^ 1;
+            return;
+        }
+        unsigned long long av = w.avail;
+        int n = __popcll(av);
+        if (n == 0) {
+            fail(LDO_RS_INVARIANT);
+            p = pos(w.ref);
+            o = 0;
+            return;
+        }
+        int k = rng.uniform_int(0, n - 1);
+        #pragma unroll 1
+        for (int t = 0; t < k; ++t) av &= av - 1ull;
+        int ci = __ffsll((long long)av) - 1;
+        w.avail &= ~(1ull << ci);
+        p = add(pos(w.ref), unit(ci / 6));
+        o = ci % 6;
+    }
+    // calc_p_config_open (:316)
+    __device__ __noinline__ double rg_p_open(V3 p, int o) {
+        LdoCtWork<C>& w = *ct;
+        int d = w.d;
+        Delta dc = probe_domain(d, p, o);
+        if (bad()) return 0;
+        if (hdr.violated) {
+            hdr.violated = 0;
+            return 0;
+        }
+        if (!ct_walks_ok(d, p)) return 0;
+        if (occupancy(p) == UNBOUND) {
+            int od = unbound_at(p);
+            bool same = scs[od] == scs[d];
+            bool endpoint = ct_endpoint_reached(d, p);
+            if (!(same || endpoint || w.stemd)) return 0;
+        }
+        return fmin(1.0, dexp(-dc.e));
+    }
+    __device__ bool rg_test_open(double p) {   // test_config_open (:346)
+        p = fmin(1.0, p);
+        if (p == 1) return true;
+        return p > rng.uniform_real();
+    }
+    __device__ __noinline__ double rg_set_config(int d, V3 p, int o) {   // set_config (:233)
+        double de = set_checked(d, p, o);
+        ct_update_endpoints(ct->d);
+        ct_push_erased();
+        return de;
+    }
+    // recoil_regrow (:177)
+    __device__ __noinline__ double rg_recoil_regrow() {
+        LdoCtWork<C>& w = *ct;
+        double de = 0;
+        w.di = 0;
+        w.d = w.rd[0];
+        w.dir = ct_get_dir(w.d);
+        #pragma unroll 1
+        for (int k = 0; k < w.n_rd; ++k) {
+            w.catt_q[k] = 0;
+            w.av_q[k] = 0;
+            w.c_open[k] = 0;
+        }
+        w.c_open[0] = 1;
+        rg_prepare_for_growth();
+        int recoils = 0;
+        #pragma unroll 1
+        for (int guard = 0; guard < (1 << 22); ++guard) {
+            if (bad()) return de;
+            V3 p = 0;
+            int o = 0;
+            double pc = 0;
+            bool open = false;
+            #pragma unroll 1
+            while (!open && w.catt != w.dmax && !bad()) {
+                w.catt++;
+                rg_select_trial(p, o);
+                pc = rg_p_open(p, o);
+                open = rg_test_open(pc);
+            }
+            if (open) {
+                if (recoils != 0) recoils--;
+                de += rg_set_config(w.d, p, o);
+                w.catt_q[w.di] = (uint8_t)w.catt;
+                w.av_q[w.di] = w.avail;
+                w.c_open[w.di] = pc;
+                if (w.di == w.n_rd - 1) return de;
+                rg_prepare_for_growth();
+            }
+            else {
+                if (recoils == w.max_recoils || w.di == 1) {
+                    rejected = true;
+                    return de;
+                }
+                recoils++;
+                de += rg_prepare_for_regrowth();
+            }
+        }
+        fail(LDO_RS_ITERCAP);
+        return de;
+    }
+    // test_config_avail (:418)
+    __device__ __noinline__ bool rg_test_avail() {
+        LdoCtWork<C>& w = *ct;
+        int feels = 0;
+        if (feels == w.max_recoils || w.di == w.n_rd - 1) return true;
+        rg_prepare_for_growth();
+        bool avail = false;
+        #pragma unroll 1
+        for (int guard = 0; guard < (1 << 22); ++guard) {
+            if (bad()) return false;
+            V3 p = 0;
+            int o = 0;
+            bool open = false;
+            #pragma unroll 1
+            while (!open && w.catt != w.dmax && !bad()) {
+                w.catt++;
+                rg_select_trial(p, o);
+                double pc = rg_p_open(p, o);
+                open = rg_test_open(pc);
+            }
+            if (open) {
+                feels++;
+                if (feels == w.max_recoils || w.di == w.n_rd - 1) {
+                    feels--;
+                    avail = true;
+                    break;
+                }
+                rg_set_config(w.d, p, o);
+                w.catt_q[w.di] = (uint8_t)w.catt;
+                w.av_q[w.di] = w.avail;
+                rg_prepare_for_growth();
+            }
+            else {
+                if (feels == 0) {
+                    avail = false;
+                    break;
+                }
+                feels--;
+                rg_prepare_for_regrowth();
+            }
+            if (guard + 1 == (1 << 22)) fail(LDO_RS_ITERCAP);
+        }
+        #pragma unroll 1
+        while (feels != 0 && !bad()) {
+            w.di--;
+            feels--;
+            w.d = w.rd[w.di];
+            unassign_domain(w.d);
+            ct_restore_endpoints(w.d);
+        }
+        w.di--;
+        w.d = w.rd[w.di];
+        return avail;
+    }
+    // calc_weights (:363) of the configuration src_p / src_o
+    __device__ __noinline__ void rg_calc_weights(const long long* src_p, const uint8_t* src_o) {
+        LdoCtWork<C>& w = *ct;
+        w.di = 0;
+        w.d = w.rd[0];
+        #pragma unroll 1
+        while (w.di != w.n_rd - 1 && !bad()) {
+            w.di++;
+            int d = w.rd[w.di];
+            w.d = d;
+            w.stemd = w.stem_of[d] >= 0;
+            w.dir = ct_get_dir(d);
+            int avail_cs = 1;
+            if (!w.stemd) {
+                w.ref = next(d, -w.dir);
+                int catt = w.catt_wq[w.di];
+                w.avail = w.av_wq[w.di];
+                #pragma unroll 1
+                while (catt != w.max_c_attempts && !bad()) {
+                    catt++;
+                    V3 p;
+                    int o;
+                    rg_select_trial(p, o);
+                    double pc = rg_p_open(p, o);
+                    if (rg_test_open(pc)) {
+                        set_checked(d, p, o);
+                        ct_update_endpoints(d);
+                        ct_push_erased();
+                        int dir_s = w.dir, ref_s = w.ref, stem_s = w.stemd;
+                        unsigned long long av_s = w.avail;
+                        avail_cs += rg_test_avail();
+                        w.avail = av_s;
+                        w.stemd = stem_s;
+                        w.ref = ref_s;
+                        w.dir = dir_s;
+                        unassign_domain(d);
+                        ct_restore_endpoints(d);
+                    }
+                }
+            }
+            w.weight *= avail_cs / w.c_open[w.di - 1];
+            set_checked(d, src_p[d], src_o[d]);
+            ct_update_endpoints(d);
+            ct_push_erased();
+        }
+        w.weight /= w.c_open[w.di];
+    }
+    // calc_old_c_opens (:481)
+    __device__ __noinline__ void rg_calc_old_c_opens() {
+        LdoCtWork<C>& w = *ct;
+        w.di = 0;
+        w.c_open[0] = 1;
+        #pragma unroll 1
+        while (w.di != w.n_rd - 1 && !bad()) {
+            w.di++;
+            int d = w.rd[w.di];
+            w.d = d;
+            w.catt_q[w.di] = 1;
+            V3 p = w.p_old[d];
+            int o = w.o_old[d];
+            w.stemd = w.stem_of[d] >= 0;
+            w.c_open[w.di] = rg_p_open(p, o);
+            rg_set_config(d, p, o);
+            if (w.stemd) {
+                w.av_q[w.di] = 0;
+            }
+            else {
+                w.dir = ct_get_dir(d);
+                int ref = next(d, -w.dir);
+                w.ref = ref;
+                int k = ref >= 0 ? unit_index(sub(p, w.p_old[ref])) : -1;
+                if (k < 0) {
+                    fail(LDO_RS_INVARIANT);   // m_config_to_i.at: not a neighbour step
+                    return;
+                }
+                w.av_q[w.di] = CT_ALL36 & ~(1ull << (6 * k + o));
+            }
+        }
+    }
+    // The first phase of both recoil-growth movetypes: segments, constraint
+    // points, the regrowth stack, and unassign_and_save_domains (:81).
+    __device__ __noinline__ int rg_begin(int kind) {
+        LdoCtWork<C>& w = *ct;
+        ct_clear();
+        w.kind = kind;
+        w.delta_e = 0;
+        w.weight = 1;
+        w.weight_new = 1;
+        const int* mo = sys->move_opt[cur_mv];
+        w.max_recoils = mo[LDO_MO_MAX_RECOILS];
+        w.max_c_attempts = mo[LDO_MO_MAX_C_ATTEMPTS];
+        if (kind == LDO_MV_CTRG) {   // CTRGScaffoldRegrowthMCMovetype (:629)
+            ct_select_indices(mo[LDO_MO_MAX_REGROWTH]);
+            if (bad()) return finish_move(false, 0);
+            ct_calc_constraintpoints();
+            int nsel = w.seg_off[1];
+            bool whole = cyclic && nsel == ns;
+            if (!whole) ct_remove_ep(w.seg_dom[0]);
+            bool whole_ds = cyclic && w.n_rd == ns;
+            w.remove_first[0] = !whole_ds;
+            w.remove_first[1] = !cyclic && w.n_rd == ns;   // the reference's condition at :673
+            w.remove_first[2] = !whole_ds;
+        }
+        else {   // CTRGJumpScaffoldRegrowthMCMovetype (:792)
+            ct_select_noncontig(mo[LDO_MO_MAX_REGROWTH], mo[LDO_MO_MAX_SEG_REGROWTH]);
+            if (bad()) return finish_move(false, 0);
+            ct_calc_constraintpoints();
+            ct_remove_ep(w.seg_dom[0]);
+            #pragma unroll 1
+            for (int i = 0; i < w.n_stems; ++i) {
+                int stem = w.stems[i];
+                w.gp_to[bnd[stem]] = (int16_t)stem;
+                w.stem_of[stem] = (int16_t)bnd[stem];
+            }
+            w.remove_first[0] = w.remove_first[1] = w.remove_first[2] = 1;
+        }
+        if (bad()) return finish_move(false, 0);
+        // a single domain to regrow (a two-domain cyclic scaffold) leaves the
+        // reference reading past its regrowth stack; the move is rejected
+        if (w.n_rd < 2) return finish_move(false, 0);
+        #pragma unroll 1
+        for (int k = 0; k < w.n_rd; ++k) {
+            int d = w.rd[k];
+            w.p_old[d] = pos(d);
+            w.o_old[d] = ore[d];
+        }
+        #pragma unroll 1
+        for (int k = 1; k < w.n_rd; ++k) w.delta_e += unassign_domain(w.rd[k]);
+        w.n_eq = 0;
+        phase = PH_RG2;
+        return CMD_SNAP(1) | CMD_MORE;
+    }
+    __device__ __noinline__ int rg_grow() {
+        LdoCtWork<C>& w = *ct;
+        w.delta_e += rg_recoil_regrow();
+        if (rejected || bad()) return finish_move(false, 0);
+        // add_external_bias (:76)
+        update_move_params();
+        w.delta_e += calc_move();
+        // setup_for_calc_new_weights (:137); the new configuration is kept
+        // for the weight pass and as snapshot 2
+        #pragma unroll 1
+        for (int k = 0; k < w.n_rd; ++k) {
+            int d = w.rd[k];
+            w.p_new[d] = pos(d);
+            w.o_new[d] = ore[d];
+            w.catt_wq[k] = w.catt_q[k];
+            w.av_wq[k] = w.av_q[k];
+        }
+        w.n_eq = 0;
+        phase = PH_RG3;
+        return CMD_SNAP(2) | CMD_REST(1) | CMD_MORE;
+    }
+    __device__ __noinline__ int rg_weigh_new() {
+        LdoCtWork<C>& w = *ct;
+        ct_reset_endpoints();
+        if (w.remove_first[0]) ct_remove_ep(w.rd[0]);
+        rg_calc_weights(w.p_new, w.o_new);
+        if (bad()) return finish_move(false, 0);
+        phase = PH_RG4;
+        return CMD_REST(1) | CMD_MORE;   // unassign_domains (:116)
+    }
+    __device__ __noinline__ int rg_old_opens() {
+        LdoCtWork<C>& w = *ct;
+        w.n_eq = 0;
+        ct_reset_endpoints();
+        if (w.remove_first[1]) ct_remove_ep(w.rd[0]);
+        rg_calc_old_c_opens();
+        if (bad()) return finish_move(false, 0);
+        // setup_for_calc_old_weights (:146)
+        w.weight_new = w.weight;
+        w.weight = 1;
+        #pragma unroll 1
+        for (int k = 0; k < w.n_rd; ++k) {
+            w.catt_wq[k] = w.catt_q[k];
+            w.av_wq[k] = w.av_q[k];
+        }
+        phase = PH_RG5;
+        return CMD_REST(1) | CMD_MORE;   // unassign_and_save_domains
+    }
+    __device__ __noinline__ int rg_weigh_old() {
+        LdoCtWork<C>& w = *ct;
+        w.n_eq = 0;
+        ct_reset_endpoints();
+        if (w.remove_first[2]) ct_remove_ep(w.rd[0]);
+        rg_calc_weights(w.p_old, w.o_old);
+        if (bad()) return finish_move(false, 0);
+        // test_rg_acceptance (:515): accepted, the new configuration
+        double ratio = w.weight_new / w.weight * dexp(-w.delta_e);
+        bool acc = test_acceptance(ratio);
+        return finish_move(acc, acc ? 2 : 0);
+    }
+
+    // ------------------------------------------- configurational bias ---
+    // RegrowthMCMovetype::set_growth_point (src/movetypes.cpp:322) without
+    // the reversal list
+    __device__ double ct_set_growth_point(int gnew, int gold) {
+        double de = set_domain_config(gnew, pos(gold), ore[gold] ^ 1);
+        if (hdr.violated) rejected = true;
+        return de;
+    }
+    // CBMCMovetype::select_and_set_config (:104) with calc_biases (:58) and
+    // CTCBRegrowthMCMovetype::calc_bias (:480)
+    __device__ __noinline__ void ctcb_select_and_set(int dom, int prev) {
+        LdoCtWork<C>& w = *ct;
+        V3 p_prev = pos(prev);
+        int nc = 0;
+        #pragma unroll 1
+        for (int v = 0; v < 6; ++v) {
+            V3 p = add(p_prev, unit(v));
+            int occ = occupancy(p);
+            if (occ == BOUND || occ == MISBOUND) continue;
+            if (occ == UNBOUND) {
+                int ud = unbound_at(p);
+                int o = ore[ud] ^ 1;
+                Delta dc = probe_domain(dom, p, o);
+                if (bad()) return;
+                if (!hdr.violated) {
+                    cb_pos[nc] = p;
+                    cb_ore[nc] = o;
+                    cb_de[nc] = dc.e;
+                    cb_stk[nc] = dc.stacked;
+                    double b = 1;
+                    b *= dexp(-dc.e);
+                    cb_bf[nc] = b;
+                    nc++;
+                }
+                else {
+                    hdr.violated = 0;
+                }
+            }
+            else {
+                cb_pos[nc] = p;
+                cb_ore[nc] = -1;
+                cb_bf[nc] = 6.0;
+                nc++;
+            }
+        }
+        #pragma unroll 1
+        for (int n = 0; n < nc; ++n) {
+            V3 p = cb_pos[n];
+            if (occupancy(p) == UNBOUND) {
+                int od = unbound_at(p);
+                bool same = scs[od] == scs[dom];
+                bool endpoint = ct_endpoint_reached(dom, p);
+                if (!(same || endpoint)) cb_bf[n] = 0;
+            }
+            if (!ct_walks_ok(dom, p)) cb_bf[n] = 0;
+        }
+        double sum = 0;
+        #pragma unroll 1
+        for (int n = 0; n < nc; ++n) sum += cb_bf[n];
+        // a dead end rejects; a rejection from before (the old
+        // configuration's staple growth) still multiplies in this weight
+        if (sum == 0) rejected = true;
+        else w_bias *= sum;
+        if (rejected) return;
+        if (!regrow_old) {
+            V3 p = mk(0, 0, 0);
+            int o = -1, chosen = -1;
+            double cum = 0;
+            double r = rng.uniform_real();
+            #pragma unroll 1
+            for (int n = 0; n < nc; ++n) {
+                cum += cb_bf[n] / sum;
+                if (r < cum) {
+                    p = cb_pos[n];
+                    o = cb_ore[n];
+                    chosen = n;
+                    break;
+                }
+            }
+            if (o < 0) {
+                o = rng.uniform_int(0, 5);
+                set_checked(dom, p, o);
+            }
+            else {
+                set_checked_probed(dom, p, o, cb_de[chosen], cb_stk[chosen]);
+            }
+        }
+        else {
+            V3 p = w.p_old[dom];
+            int o = w.o_old[dom];
+            int c = 0;
+            #pragma unroll 1
+            while (c < nc && !(cb_ore[c] == o && eq(cb_pos[c], p))) ++c;
+            if (c < nc) set_checked_probed(dom, p, o, cb_de[c], cb_stk[c]);
+            else set_checked(dom, p, o);
+        }
+    }
+    __device__ bool ct_push_frame(int kind, int a, int b, int dir, int n) {
+        LdoCtWork<C>& w = *ct;
+        if (w.n_fr >= LdoCtWork<C>::FR) {
+            fail(LDO_RS_CAPACITY);
+            return false;
+        }
+        int f = w.n_fr++;
+        w.fr_kind[f] = (int8_t)kind;
+        w.fr_a[f] = (int16_t)a;
+        w.fr_b[f] = (int16_t)b;
+        w.fr_dir[f] = (int8_t)dir;
+        w.fr_n[f] = (int16_t)n;
+        w.fr_i[f] = (int16_t)(kind == 2 ? 0 : 1);
+        return true;
+    }
+    __device__ int ct_frame_elem(int f, int i) const {
+        const LdoCtWork<C>& w = *ct;
+        if (w.fr_kind[f] == 1) return slot_of(w.fr_a[f], w.fr_b[f] + w.fr_dir[f] * i);
+        return (w.fr_a[f] == 0 ? w.seg_dom : w.list)[w.fr_b[f] + i];
+    }
+    // CTCBRegrowthMCMovetype::grow_staple_and_update_endpoints (:533) up to
+    // the growth of the staple, which the frame loop does
+    __device__ __noinline__ void ct_start_staple(int gold) {
+        LdoCtWork<C>& w = *ct;
+        int gnew = w.gp_to[gold];
+        if (gnew < 0) {
+            fail(LDO_RS_INVARIANT);
+            return;
+        }
+        if (scs[gnew] == 0) return;   // the reference's guard against scaffold segments
+        double de;
+        if (regrow_old) de = set_checked(gnew, pos(gold), w.o_old[gnew]);   // set_old_growth_point (:168)
+        else de = ct_set_growth_point(gnew, gold);
+        w_bias *= dexp(-de);
+        if (rejected || bad()) return;
+        ct_update_endpoints(gnew);
+        ct_push_frame(2, gnew, 0, 0, 0);
+    }
+    // CTCBRegrowthMCMovetype::grow_chain (:463) and RegrowthMCMovetype::
+    // grow_staple (src/movetypes.cpp:343), their recursion as a frame stack:
+    // kind 0 a list of slots, 1 a staple's domains from its growth domain in
+    // one direction, 2 a staple whose 3' then 5' runs are still to grow.
+    __device__ __noinline__ void ct_grow_frames() {
+        LdoCtWork<C>& w = *ct;
+        #pragma unroll 1
+        while (w.n_fr > 0) {
+            if (bad()) {
+                w.n_fr = 0;
+                return;
+            }
+            int f = w.n_fr - 1;
+            if (w.fr_kind[f] != 2) {
+                if (w.fr_i[f] >= w.fr_n[f]) {
+                    w.n_fr--;
+                    continue;
+                }
+                int i = w.fr_i[f]++;
+                int d = ct_frame_elem(f, i), prev = ct_frame_elem(f, i - 1);
+                w.dir = ct_get_dir(d);
+                ctcb_select_and_set(d, prev);
+                if (rejected || bad()) {
+                    w.n_fr = 0;
+                    return;
+                }
+                ct_update_endpoints(d);
+                if (w.gp_to[d] >= 0) {
+                    ct_start_staple(d);
+                    if (rejected || bad()) {
+                        w.n_fr = 0;
+                        return;
+                    }
+                }
+            }
+            else {
+                int g = w.fr_a[f];
+                int cs = scs[g], di = didx(g), len = chain_len(cs);
+                int stage = w.fr_i[f]++;
+                if (stage == 0) {
+                    if (len - di > 1) ct_push_frame(1, cs, di, 1, len - di);
+                }
+                else if (stage == 1) {
+                    if (di + 1 > 1) ct_push_frame(1, cs, di, -1, di + 1);
+                }
+                else {
+                    w.n_fr--;
+                }
+            }
+        }
+    }
+    __device__ void ct_grow_list(int base, int off, int n) {   // grow_chain over a list of slots
+        if (ct_push_frame(0, base, off, 0, n)) ct_grow_frames();
+    }
+    __device__ void ct_grow_from(int gold) {   // grow_staple_and_update_endpoints
+        ct_start_staple(gold);
+        if (!rejected && !bad()) ct_grow_frames();
+    }
+    // CTCBJumpScaffoldRegrowthMCMovetype::set_first_seg_domain (:968)
+    __device__ __noinline__ void ctcb_first_seg_domain(int dnew) {
+        LdoCtWork<C>& w = *ct;
+        int dold = w.stem_of[dnew];
+        if (dold < 0) {
+            fail(LDO_RS_INVARIANT);
+            return;
+        }
+        if (!ct_walks_ok(dnew, pos(dold))) {
+            rejected = true;
+            return;
+        }
+        w.dir = ct_get_dir(dnew);
+        double de = ct_set_growth_point(dnew, dold);
+        w_bias *= dexp(-de);
+    }
+    // The growth of one configuration (new or old) of a CTCB move.
+    __device__ __noinline__ bool ctcb_grow() {
+        LdoCtWork<C>& w = *ct;
+        int first = w.seg_dom[0];
+        if (w.kind == LDO_MV_CTCB) {   // CTCBScaffoldRegrowthMCMovetype (:691)
+            if (w.gp_to[first] >= 0) {
+                ct_grow_from(first);
+                if (rejected && !regrow_old) return false;
+            }
+            ct_grow_list(0, 0, w.seg_off[1]);
+            return !rejected;
+        }
+        // CTCBJumpScaffoldRegrowthMCMovetype (:880-906)
+        if (w.gp_to[first] >= 0) {
+            ct_grow_from(first);
+            if (rejected) return false;
+        }
+        ct_grow_list(0, 0, w.seg_off[1]);
+        if (rejected) return false;
+        #pragma unroll 1
+        for (int i = 0; i < w.n_stems && !bad(); ++i) {
+            int stem = w.stems[i];
+            ctcb_first_seg_domain(stem);
+            if (rejected) return false;
+            #pragma unroll 1
+            for (int k = 0; k < 2; ++k) {
+                int a0 = w.pair_off[2 * i + k], a1 = w.pair_off[2 * i + k + 1];
+                w.list[0] = (int16_t)stem;
+                #pragma unroll 1
+                for (int q = a0; q < a1; ++q) w.list[1 + q - a0] = w.pair_dom[q];
+                ct_grow_list(1, 0, 1 + a1 - a0);
+                if (rejected) return false;
+            }
+        }
+        return true;
+    }
+    __device__ __noinline__ int ctcb_begin(int kind) {
+        LdoCtWork<C>& w = *ct;
+        ct_clear();
+        w.kind = kind;
+        const int* mo = sys->move_opt[cur_mv];
+        if (kind == LDO_MV_CTCB) {
+            ct_select_indices(mo[LDO_MO_MAX_REGROWTH]);
+            if (bad()) return finish_move(false, 0);
+            ct_calc_constraintpoints();
+            bool whole = cyclic && w.seg_off[1] == ns;
+            w.remove_first[0] = !whole;
+            if (!whole) ct_remove_ep(w.seg_dom[0]);
+            if (bad()) return finish_move(false, 0);
+            // unassign the scaffold domains after the first, then the
+            // staples to regrow in the order of their chain indices
+            int n = w.seg_off[1];
+            #pragma unroll 1
+            for (int k = 1; k < n; ++k) {
+                int d = w.seg_dom[k];
+                w.p_old[d] = pos(d);
+                w.o_old[d] = ore[d];
+                unassign_domain(d);
+            }
+            unsigned long long left = w.regrow;
+            #pragma unroll 1
+            while (left) {
+                int best = -1;
+                #pragma unroll 1
+                for (unsigned long long m = left; m; m &= m - 1ull) {
+                    int cs = __ffsll((long long)m) - 1;
+                    if (best < 0 || chain_c[cs] < chain_c[best]) best = cs;
+                }
+                left &= ~(1ull << best);
+                int len = chain_len(best);
+                #pragma unroll 1
+                for (int q = 0; q < len; ++q) {
+                    int d = slot_of(best, q);
+                    w.p_old[d] = pos(d);
+                    w.o_old[d] = ore[d];
+                    unassign_domain(d);
+                }
+            }
+        }
+        else {
+            ct_select_noncontig(mo[LDO_MO_MAX_REGROWTH], mo[LDO_MO_MAX_SEG_REGROWTH]);
+            if (bad()) return finish_move(false, 0);
+            ct_calc_constraintpoints();
+            ct_remove_ep(w.seg_dom[0]);
+            w.remove_first[0] = 1;
+            if (bad()) return finish_move(false, 0);
+            #pragma unroll 1
+            for (int k = 1; k < w.n_rd; ++k) {
+                int d = w.rd[k];
+                w.p_old[d] = pos(d);
+                w.o_old[d] = ore[d];
+                unassign_domain(d);
+            }
+        }
+        phase = PH_CT2;
+        return CMD_SNAP(1) | CMD_MORE;
+    }
+    __device__ __noinline__ int ctcb_new() {
+        LdoCtWork<C>& w = *ct;
+        regrow_old = false;
+        if (!ctcb_grow() || bad()) return finish_move(false, 0);
+        update_move_params();   // add_external_bias (:52)
+        w_bias *= dexp(-calc_move());
+        // setup_for_regrow_old (:215)
+        regrow_old = true;
+        w_new_bias = w_bias;
+        new_modifier = modifier;
+        w_bias = 1;
+        (void)w;
+        phase = PH_CT3;
+        return CMD_SNAP(2) | CMD_REST(1) | CMD_MORE;
+    }
+    __device__ __noinline__ int ctcb_old() {
+        LdoCtWork<C>& w = *ct;
+        ct_reset_endpoints();
+        if (w.remove_first[0]) ct_remove_ep(w.seg_dom[0]);
+        bool ok = ctcb_grow();
+        if (bad()) return finish_move(false, 0);
+        // the jump movetype gives up here with the new configuration as the
+        // one to revert to (its m_prev_pos, src/cb_movetypes.cpp:927)
+        if (!ok && w.kind == LDO_MV_CTCB_JUMP) return finish_move(false, 0, 2);
+        modifier = 1;
+        double ratio = w_new_bias / w_bias;   // test_cb_acceptance (:182)
+        bool acc = test_acceptance(ratio);
+        return finish_move(acc, acc ? 2 : 0);
+    }
+
     // GCMCSimulation::simulate, one step (src/simulation.cpp:575-619), as a
     // state machine: step_begin runs the move until it needs the warp to copy
     // snapshots, step_resume continues it, and each returns the next CMD_*
@@ -2230,14 +3514,29 @@ struct Rep : public LdoState<C> {
         case LDO_MV_MET_REGROWTH: acc = met_regrowth(); break;
         case LDO_MV_LEARNED_EXCHANGE: acc = learned_exchange(); break;
         case LDO_MV_CB_REGROWTH: return cb_begin();
+        case LDO_MV_CTRG:
+        case LDO_MV_CTRG_JUMP:
+            if (!ct) {
+                fail(LDO_RS_INVARIANT);
+                return 0;
+            }
+            return rg_begin(sys->move_kind[mv]);
+        case LDO_MV_CTCB:
+        case LDO_MV_CTCB_JUMP:
+            if (!ct) {
+                fail(LDO_RS_INVARIANT);
+                return 0;
+            }
+            return ctcb_begin(sys->move_kind[mv]);
         }
         return finish_move(acc, 0);
     }
 
     // Move statistics, then the snapshot work: an accepted move refreshes
     // snapshot 0 (CB: restore snapshot `from` first), a rejected move that
-    // changed anything restores it.
-    __device__ __noinline__ int finish_move(bool acc, int from) {
+    // changed anything restores it, or, with rej_from, keeps the state of
+    // snapshot rej_from (a rejection that the reference reverts to it).
+    __device__ __noinline__ int finish_move(bool acc, int from, int rej_from = 0) {
         if (bad()) return 0;
         mstat[2 * cur_mv] += 1;
         int cmd = 0;
@@ -2245,6 +3544,10 @@ struct Rep : public LdoState<C> {
         if (acc) {
             mstat[2 * cur_mv + 1] += 1;
             cmd = from ? (CMD_REST(from) | CMD_SNAP(0) | CMD_REST_FIRST) : CMD_SNAP(0);
+        }
+        else if (rej_from) {
+            cmd = CMD_REST(rej_from) | CMD_SNAP(0) | CMD_REST_FIRST;
+            if (sys->n_biases > 0) recalc = true;
         }
         else {
             // With bias functions the reference's trailing update_move_params
@@ -2272,6 +3575,12 @@ struct Rep : public LdoState<C> {
         if (bad()) return 0;
         if (phase == PH_CB2) return cb_mid();
         if (phase == PH_CB3) return cb_end();
+        if (phase == PH_RG2) return rg_grow();
+        if (phase == PH_RG3) return rg_weigh_new();
+        if (phase == PH_RG4) return rg_old_opens();
+        if (phase == PH_RG5) return rg_weigh_old();
+        if (phase == PH_CT2) return ctcb_new();
+        if (phase == PH_CT3) return ctcb_old();
         phase = 0;
         if (recalc) {
             recalc = false;

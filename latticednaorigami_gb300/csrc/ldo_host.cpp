@@ -67,10 +67,13 @@ int move_kind(const string& t) {
     if (t == "MetStapleRegrowth") return LDO_MV_MET_REGROWTH;
     if (t == "CBStapleRegrowth") return LDO_MV_CB_REGROWTH;
     if (t == "LearnedStapleExchange") return LDO_MV_LEARNED_EXCHANGE;
-    if (t == "CTCBScaffoldRegrowth" || t == "CTCBJumpScaffoldRegrowth" || t == "CTRGScaffoldRegrowth" ||
-        t == "CTRGJumpScaffoldRegrowth" || t == "CTCBLinkerRegrowth" || t == "CTCBClusteredLinkerRegrowth" ||
-        t == "CTRGLinkerRegrowth" || t == "CTRGClusteredLinkerRegrowth")
-        throw LdoError(LDO_EINVAL, t + ": scaffold movetypes are not implemented by this engine");
+    if (t == "CTRGScaffoldRegrowth") return LDO_MV_CTRG;
+    if (t == "CTRGJumpScaffoldRegrowth") return LDO_MV_CTRG_JUMP;
+    if (t == "CTCBScaffoldRegrowth") return LDO_MV_CTCB;
+    if (t == "CTCBJumpScaffoldRegrowth") return LDO_MV_CTCB_JUMP;
+    if (t == "CTCBLinkerRegrowth" || t == "CTCBClusteredLinkerRegrowth" || t == "CTRGLinkerRegrowth" ||
+        t == "CTRGClusteredLinkerRegrowth")
+        throw LdoError(LDO_EINVAL, t + ": linker (scaffold transform) movetypes are not implemented by this engine");
     throw LdoError(LDO_EINVAL, t + ": no such movetype");
 }
 
@@ -165,6 +168,25 @@ HostSystem load_system(const string& inp, const string& overrides) {
         d.move_kind[m] = move_kind(hs.moves[m].type);
         cum += hs.moves[m].freq;
         d.move_cum[m] = cum;
+        const ldo_io::MoveSpec& ms = hs.moves[m];
+        d.move_opt[m][LDO_MO_MAX_REGROWTH] = ms.max_regrowth;
+        d.move_opt[m][LDO_MO_MAX_SEG_REGROWTH] = ms.max_seg_regrowth;
+        d.move_opt[m][LDO_MO_MAX_RECOILS] = ms.max_num_recoils;
+        d.move_opt[m][LDO_MO_MAX_C_ATTEMPTS] = ms.max_c_attempts;
+        int k = d.move_kind[m];
+        if (k >= LDO_MV_CTRG && k <= LDO_MV_CTCB_JUMP) {
+            d.has_ct = 1;
+            // the reference draws uniform_int(2, max_regrowth) and keeps at
+            // most 36 untried configurations per domain (src/movetypes.cpp:479,
+            // src/rg_movetypes.cpp:298)
+            if (ms.max_regrowth < 2) throw LdoError(LDO_EINVAL, ms.type + ": max_regrowth must be at least 2");
+            if (d.ns < 2) throw LdoError(LDO_EINVAL, ms.type + ": the scaffold needs at least 2 domains");
+            if ((k == LDO_MV_CTRG_JUMP || k == LDO_MV_CTCB_JUMP) && ms.max_seg_regrowth < 0)
+                throw LdoError(LDO_EINVAL, ms.type + ": max_seg_regrowth must not be negative");
+            if ((k == LDO_MV_CTRG || k == LDO_MV_CTRG_JUMP) &&
+                (ms.max_c_attempts < 1 || ms.max_c_attempts > 36 || ms.max_num_recoils < 0))
+                throw LdoError(LDO_EINVAL, ms.type + ": max_c_attempts must be 1..36 and max_num_recoils >= 0");
+        }
         if (d.move_kind[m] == LDO_MV_LEARNED_EXCHANGE && d.ns > LDO_MAX_SCAF)
             throw LdoError(LDO_EINVAL, "LearnedStapleExchange: scaffold longer than 320 domains");
         if (d.move_kind[m] == LDO_MV_MET_EXCHANGE || d.move_kind[m] == LDO_MV_LEARNED_EXCHANGE) {
@@ -377,6 +399,8 @@ struct ldo_engine {
     DevBuf<double> d_grid;
     DevBuf<unsigned char> d_arena;
     DevBuf<unsigned char> d_snap;   // move snapshots (run mode)
+    DevBuf<unsigned char> d_ct;     // scaffold regrowth working memory
+    size_t ct_stride {0};
     // learned insertion proposal: weight table, training counts, network
     DevBuf<double> d_learn_w;
     DevBuf<float> d_cnt_b, d_cnt_t;
@@ -484,6 +508,8 @@ struct ldo_engine {
         L.grid = d_grid.p;
         L.arena = d_arena.p;
         L.snap = d_snap.p;
+        L.ct_ws = d_ct.p;
+        L.ct_stride = ct_stride;
         L.lay = lay;
         L.n_rep = n_rep;
         L.warps_per_block = wpb;
@@ -572,6 +598,9 @@ struct ldo_engine {
                 int len = d.type_len[type];
                 if ((int)ch.positions.size() != len) throw LdoError(LDO_EINVAL, "chain length does not match identity");
                 chain_c[cs] = ch.index;
+                // the reference's scaffold moves identify the scaffold by chain index 0
+                if (c == 0 && d.has_ct && ch.index != 0)
+                    throw LdoError(LDO_EINVAL, "scaffold regrowth movetypes need the scaffold's chain index to be 0");
                 chain_type[cs] = (unsigned char)type;
                 clen[cs] = (unsigned char)len;
                 chain_order[c] = (unsigned char)cs;
@@ -698,6 +727,12 @@ struct ldo_engine {
         d_status.alloc(1);
         init_arena();
         d_snap.alloc((size_t)n_rep * LDO_N_SNAPSHOTS * ldo_snapshot_stride(lay.bytes));
+        bool any_ct = false;
+        for (auto& d : h_sys) any_ct = any_ct || d.has_ct;
+        if (any_ct) {
+            ct_stride = ldo_ct_work_bytes(lay.cls);
+            d_ct.alloc((size_t)n_rep * ct_stride);
+        }
         // untrained proposal: every unbound domain weighs 1
         {
             vector<double> ones(LDO_LEARN_TABLE, 1.0);
@@ -1585,6 +1620,22 @@ ldo_status ldo_replica_status_noalloc(ldo_engine* e, int32_t* status_of_replica,
         return LDO_ECUDA;
     }
     return LDO_OK;
+}
+
+// The engine's exponential evaluated by the GPU, for host tools that need
+// its exact bits (the same function as ldo_math::exp on the host).
+ldo_status ldo_engine_exp(const double* x, double* y, int n) {
+    if (n < 0 || (n > 0 && (!x || !y))) return LDO_EINVAL;
+    if (n == 0) return LDO_OK;
+    double *dx = nullptr, *dy = nullptr;
+    cudaError_t err = cudaMalloc(&dx, (size_t)n * sizeof(double));
+    if (err == cudaSuccess) err = cudaMalloc(&dy, (size_t)n * sizeof(double));
+    if (err == cudaSuccess) err = cudaMemcpy(dx, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = ldo_launch_exp(dx, dy, n, 0);
+    if (err == cudaSuccess) err = cudaMemcpy(y, dy, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+    if (dx) cudaFree(dx);
+    if (dy) cudaFree(dy);
+    return err == cudaSuccess ? LDO_OK : LDO_ECUDA;
 }
 
 ldo_status ldo_set_window(ldo_engine* e, const char* tag, int replica, int min_op, int max_op) {

@@ -33,6 +33,7 @@ __device__ void bind_rep(ldo::Rep<C>& r, const LdoLaunch& L, int rep) {
     r.bank = L.bank;
     r.grid = L.grid;
     r.learn_w = L.learn_w;
+    r.ct = L.ct_ws ? reinterpret_cast<LdoCtWork<C>*>(L.ct_ws + (size_t)rep * L.ct_stride) : nullptr;
     r.bind_tables(L.tabs + r.ctl->tab);
     r.imax = r.sys->imax;
     r.dim = r.sys->dim;
@@ -311,6 +312,27 @@ int ldo_warp_smem_bytes(int cls) {
     case LDO_CLASS_M: return warp_bytes<LdoCapM>();
     default: return warp_bytes<LdoCapL>();
     }
+}
+
+__global__ void ldo_exp_kernel(const double* x, double* y, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = ldo::dexp(x[i]);
+}
+
+cudaError_t ldo_launch_exp(const double* x, double* y, int n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    ldo_exp_kernel<<<(n + 255) / 256, 256, 0, stream>>>(x, y, n);
+    return cudaGetLastError();
+}
+
+size_t ldo_ct_work_bytes(int cls) {
+    size_t b;
+    switch (cls) {
+    case LDO_CLASS_S: b = sizeof(LdoCtWork<LdoCapS>); break;
+    case LDO_CLASS_M: b = sizeof(LdoCtWork<LdoCapM>); break;
+    default: b = sizeof(LdoCtWork<LdoCapL>); break;
+    }
+    return (b + 255) / 256 * 256;
 }
 
 cudaError_t ldo_launch_status(const unsigned char* arena, int bytes, int o_hdr, int n_rep, int* d_out,

@@ -41,6 +41,10 @@ struct LdoLaunch {
     const double* learn_w;
     float* learn_cnt_b;          // collect mode: bound / total counts per network input
     float* learn_cnt_t;
+    // Scaffold regrowth working memory, ct_stride bytes per replica (null
+    // when no system regrows its scaffold).
+    unsigned char* ct_ws;
+    size_t ct_stride;
 };
 
 cudaError_t ldo_launch_mc(const LdoLaunch& L, cudaStream_t stream);
@@ -49,6 +53,10 @@ enum { LDO_N_SNAPSHOTS = 3 };
 inline size_t ldo_snapshot_stride(int state_bytes) { return ((size_t)state_bytes + 255) / 256 * 256; }
 // Shared memory one replica's warp needs in capacity class cls.
 int ldo_warp_smem_bytes(int cls);
+// Bytes of one replica's scaffold regrowth working memory in class cls.
+size_t ldo_ct_work_bytes(int cls);
+// y[i] = the engine's exponential (ldo_math::exp) of x[i], on the device.
+cudaError_t ldo_launch_exp(const double* x, double* y, int n, cudaStream_t stream);
 cudaError_t ldo_launch_status(const unsigned char* arena, int bytes, int o_hdr, int n_rep, int* d_out,
                               cudaStream_t stream);
 

@@ -28,8 +28,14 @@ enum LdoMove {
     LDO_MV_MET_EXCHANGE = 1,
     LDO_MV_MET_REGROWTH = 2,
     LDO_MV_CB_REGROWTH = 3,
-    LDO_MV_LEARNED_EXCHANGE = 4   // engine extension: exchange with the learned insertion proposal
+    LDO_MV_LEARNED_EXCHANGE = 4,  // engine extension: exchange with the learned insertion proposal
+    // conserved-topology scaffold regrowth
+    LDO_MV_CTRG = 5,              // CTRGScaffoldRegrowth
+    LDO_MV_CTRG_JUMP = 6,         // CTRGJumpScaffoldRegrowth
+    LDO_MV_CTCB = 7,              // CTCBScaffoldRegrowth
+    LDO_MV_CTCB_JUMP = 8          // CTCBJumpScaffoldRegrowth
 };
+enum LdoMoveOpt { LDO_MO_MAX_REGROWTH = 0, LDO_MO_MAX_SEG_REGROWTH, LDO_MO_MAX_RECOILS, LDO_MO_MAX_C_ATTEMPTS };
 
 enum LdoOp {
     LDO_OP_NUMSTAPLES = 0,
@@ -67,6 +73,8 @@ struct LdoSys {
     int n_moves;
     int move_kind[LDO_MAX_MOVES];
     double move_cum[LDO_MAX_MOVES];
+    int move_opt[LDO_MAX_MOVES][4];   // scaffold regrowth options (LdoMoveOpt)
+    int has_ct;                       // some movetype regrows the scaffold
     int adaptive_exchange, allow_nonsensical;
     double exchange_mults[LDO_MAX_TYPES];
     int n_ops;

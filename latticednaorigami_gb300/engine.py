@@ -22,7 +22,7 @@ EXPORTS = [
     "ldo_energy_tables", "ldo_us_run", "ldo_us_get_biases", "ldo_us_get_windows", "ldo_replica_status_noalloc",
     "ldo_learn_collect", "ldo_learn_reset_counts", "ldo_learn_get_counts", "ldo_learn_train", "ldo_learn_set_params",
     "ldo_learn_get_params", "ldo_learn_get_table", "ldo_learn_set_table", "ldo_learn_loss_grad",
-    "ldo_writer_open", "ldo_writer_write", "ldo_writer_close", "ldo_pt2d_run",
+    "ldo_writer_open", "ldo_writer_write", "ldo_writer_close", "ldo_pt2d_run", "ldo_engine_exp",
 ]
 
 LEARN_TABLE = 524288      # network inputs (ldo_learn.h)
@@ -88,6 +88,8 @@ def load_library(path=None):
     lib.ldo_us_get_windows.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ip, ctypes.POINTER(ctypes.c_int)]
     i32p = ctypes.POINTER(ctypes.c_int32)
     lib.ldo_replica_status_noalloc.argtypes = [vp, i32p, ip, i32p, i32p]
+    lib.ldo_engine_exp.restype = ctypes.c_int
+    lib.ldo_engine_exp.argtypes = [vp, vp, ctypes.c_int]
     fp = ctypes.POINTER(ctypes.c_float)
     lib.ldo_learn_collect.argtypes = [vp]
     lib.ldo_learn_reset_counts.argtypes = [vp]
@@ -337,6 +339,17 @@ def learn_loss_grad(params, idx, cnt_bound, cnt_total):
     if rc != 0:
         raise LdoError(rc, lib.ldo_last_error(None).decode())
     return loss.value, grad
+
+
+def engine_exp(x):
+    """The engine's exponential evaluated on the GPU (ldo_engine_exp)."""
+    lib = load_library()
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.zeros_like(x)
+    rc = lib.ldo_engine_exp(x.ctypes.data, y.ctypes.data, len(x))
+    if rc != 0:
+        raise LdoError(rc, "ldo_engine_exp failed")
+    return y
 
 
 def nn_duplex_thermo(seq, temp, cation_M):

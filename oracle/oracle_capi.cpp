@@ -267,9 +267,14 @@ void oracle_observables(void* h, double* out) {
 // IdealRandomWalks::num_walks between sites dr apart in `steps` steps.
 double oracle_ideal_walks(int dx, int dy, int dz, int steps) { return (double)ideal_walks(dx, dy, dz, steps); }
 
-// Rosenbluth weights of the configurational-bias moves in long double (the
-// reference's own arithmetic) instead of the engine's FP64.
-void oracle_set_long_double(void* h, int on) { static_cast<Replica*>(h)->sys.ld_weights = on != 0; }
+// The reference's own arithmetic (long double Rosenbluth weights, the C
+// library's exp) instead of the engine's (FP64, ldo_math::exp).
+void oracle_set_reference_arithmetic(void* h, int on) { static_cast<Replica*>(h)->sys.ld_weights = on != 0; }
+
+// The engine's exponential on the host (ldo_math::exp), n values.
+void oracle_engine_exp(const double* x, double* y, int n) {
+    for (int i = 0; i < n; ++i) y[i] = ldo_math::exp(x[i]);
+}
 
 // Per-move attempts/accepts, 2 x n_moves.
 int oracle_move_stats(void* h, long long* out, int cap) {

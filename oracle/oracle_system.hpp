@@ -22,6 +22,7 @@
 #include "oracle_philox.hpp"
 #include "oracle_thermo.hpp"
 #include "../latticednaorigami_gb300/csrc/ldo_learn.h"
+#include "../latticednaorigami_gb300/csrc/ldo_math.h"
 
 namespace oracle {
 
@@ -90,6 +91,8 @@ struct Delta {
 // reference's long double, otherwise the engine's FP64.  The two choose the
 // same configurations and accept the same moves except where a weight ratio
 // lies within a rounding of 1 (then one side may skip the acceptance draw).
+// The same holds for the exponential: the reference's is the C library's,
+// the engine's is ldo_math::exp, identical on the GPU and the host.
 struct Wt {
     long double v {1};
     bool ld {false};
@@ -1195,7 +1198,10 @@ class System {
     // CB state (include/.../cb_movetypes.hpp:126-130)
     Wt w_bias, w_new_bias;
     double new_modifier {1};
-    bool ld_weights {false};   // Rosenbluth weights in long double (the reference's own arithmetic)
+    // The reference's own arithmetic (long double Rosenbluth weights and the
+    // C library's exp) instead of the engine's (FP64, ldo_math::exp).
+    bool ld_weights {false};
+    double xexp(double x) const { return ld_weights ? xexp(x) : ldo_math::exp(x); }
     bool regrow_old {false};
     std::vector<Key> old_keys;
     std::vector<V3> old_pos, old_ore;
@@ -1395,7 +1401,7 @@ class System {
             if (doms[id].state == BOUND) { staple_bound = true; break; }
         int nbd = num_bound_staple_domains(st);
         add_external_bias_met();
-        double boltz = std::exp(-delta_e);
+        double boltz = xexp(-delta_e);
         int ni = num_staples_of_ident(ident);
         size_t L = cfg.identities[ident].size();
         double pratio = static_cast<double>(L) / 6.0 / ni * boltz;
@@ -1424,7 +1430,7 @@ class System {
         num_staples--;
         add_external_bias_met();
         num_staples++;
-        double boltz = std::exp(-delta_e);
+        double boltz = xexp(-delta_e);
         int ni = num_staples_of_ident(ident);
         size_t L = cfg.identities[ident].size();
         double pratio = ni * 6.0 / static_cast<double>(L) * boltz;
@@ -1566,7 +1572,7 @@ class System {
             f += learn_q_target(p, z, n_sites, c_i) * learn_q_type(p, ident, (int)d);
         }
         add_external_bias_met();
-        double boltz = std::exp(-delta_e);
+        double boltz = xexp(-delta_e);
         int ni = num_staples_of_ident(ident);
         double pratio = boltz * cfg.staple_M;
         pratio /= 6.0 * ni;
@@ -1599,7 +1605,7 @@ class System {
         num_staples--;
         add_external_bias_met();
         num_staples++;
-        double boltz = std::exp(-delta_e);
+        double boltz = xexp(-delta_e);
         int n_sites = insertion_sites - (int)st.size();
         double z = learn_z();
         double f = 0;
@@ -1635,7 +1641,7 @@ class System {
         if (rejected) return false;
         add_external_bias_met();
         int nbd = num_bound_staple_domains(sel);
-        double boltz = std::exp(-(delta_e));
+        double boltz = xexp(-(delta_e));
         double pratio = boltz * bds.size() / nbd;
         return test_acceptance(pratio);
     }
@@ -1655,7 +1661,7 @@ class System {
                     cpos.push_back(p);
                     core.push_back(o);
                     double b = 1;
-                    b *= std::exp(-de);
+                    b *= xexp(-de);
                     bf.push_back(b);
                 }
                 else {
@@ -1666,7 +1672,7 @@ class System {
                 cpos.push_back(p);
                 core.push_back(V3(0, 0, 0));
                 double de = check_domain_constraints(dom, p, V3(1, 0, 0));
-                bf.push_back(6 * std::exp(-de));
+                bf.push_back(6 * xexp(-de));
             }
         }
     }
@@ -1725,12 +1731,12 @@ class System {
             while (!(old_keys[n].c == k.c && old_keys[n].d == k.d)) ++n;
             double de = 0;
             de += set_checked(gp.first, doms[gp.second].pos, old_ore[n]);
-            w_bias.mul(std::exp(-de));
+            w_bias.mul(xexp(-de));
             assigned.push_back(k);
         }
         else {
             double de = set_growth_point(gp.first, gp.second);
-            w_bias.mul(std::exp(-de));
+            w_bias.mul(xexp(-de));
         }
         if (!rejected) grow_staple(doms[gp.first].d, sel, true);
     }
@@ -1750,7 +1756,7 @@ class System {
         w_bias.div((long double)num_bound_staple_domains(sel));
         update_move_params();
         double tb = calc_move();
-        w_bias.mul(std::exp(-tb));
+        w_bias.mul(xexp(-tb));
         // setup_for_regrow_old (:215)
         regrow_old = true;
         w_new_bias = w_bias;
@@ -2307,7 +2313,7 @@ class System {
             bool endpoint = endpoint_reached(rg_d, p);
             if (!(same || endpoint || rg_stemd)) return 0;
         }
-        return std::fmin(1, std::exp(-de));
+        return std::fmin(1, xexp(-de));
     }
     bool rg_test_open(double p) {   // test_config_open (:346)
         p = std::fmin(1, p);
@@ -2479,7 +2485,7 @@ class System {
     }
     // test_rg_acceptance (:515)
     bool rg_test_acceptance() {
-        long double ratio = rg_weight_new / rg_weight * std::exp(-rg_delta_e);
+        long double ratio = rg_weight_new / rg_weight * xexp(-rg_delta_e);
         if (test_acceptance_ld(ratio)) {
             ct_prev_pos = rg_new_pos;
             ct_prev_ore = rg_new_ore;
@@ -2603,11 +2609,12 @@ class System {
         }
         long double sum = 0;
         for (auto x : w) sum = ld_weights ? sum + x : (long double)((double)sum + (double)x);
-        if (sum == 0) {
-            rejected = true;
-            return;
-        }
-        w_bias.mul(sum);
+        // a dead end rejects; a rejection from before (the old configuration's
+        // staple growth, :717) still multiplies in this domain's weight
+        // (CBMCMovetype::select_and_set_config, :113-116)
+        if (sum == 0) rejected = true;
+        else w_bias.mul(sum);
+        if (rejected) return;
         std::vector<double> nw;
         for (auto x : w) nw.push_back(ld_weights ? (double)(x / sum) : (double)x / (double)sum);
         if (!regrow_old) {   // select_and_set_new_config (:132)
@@ -2652,12 +2659,12 @@ class System {
         if (c_i == 0) return;
         if (regrow_old) {   // set_old_growth_point (:168)
             double de = set_checked(gnew, doms[gold].pos, cb_old_ore.at(gnew));
-            w_bias.mul(std::exp(-de));
+            w_bias.mul(xexp(-de));
             assigned.push_back(key_of(gnew));
         }
         else {
             double de = set_growth_point(gnew, gold);
-            w_bias.mul(std::exp(-de));
+            w_bias.mul(xexp(-de));
         }
         if (rejected) return;
         update_endpoints(gnew);
@@ -2724,7 +2731,7 @@ class System {
             return false;
         }
         update_move_params();   // add_external_bias (:52)
-        w_bias.mul(std::exp(-calc_move()));
+        w_bias.mul(xexp(-calc_move()));
         ctcb_setup_regrow_old();
         cp.active = cp.initial_active;
         if (!whole) remove_active_endpoint(sd[0]);
@@ -2744,7 +2751,7 @@ class System {
         }
         ct_dir = get_dir(dnew);
         double de = set_growth_point(dnew, dold);
-        w_bias.mul(std::exp(-de));
+        w_bias.mul(xexp(-de));
     }
     // the growth sequence of CTCBJumpScaffoldRegrowthMCMovetype (:880-906)
     bool ctcb_jump_grow(const std::vector<std::vector<int>>& segs,
@@ -2783,7 +2790,7 @@ class System {
             return false;
         }
         update_move_params();   // add_external_bias
-        w_bias.mul(std::exp(-calc_move()));
+        w_bias.mul(xexp(-calc_move()));
         ctcb_setup_regrow_old();
         cp.active = cp.initial_active;
         remove_active_endpoint(segs[0][0]);
@@ -2811,7 +2818,7 @@ class System {
             set_domain_orientation(dom, o_new);
             V3 p = doms[dom].pos;
             de += set_domain_config(bd, p, -o_new);
-            if (!violated) acc = test_acceptance(std::exp(-de));
+            if (!violated) acc = test_acceptance(xexp(-de));
             if (!acc) {
                 unassign_domain(bd);
                 set_domain_orientation(dom, o_old);

@@ -57,11 +57,12 @@ class OracleReplica:
             self.L.oracle_destroy(self.h)
             self.h = None
 
-    def set_long_double(self, on=True):
-        """Rosenbluth weights in long double, as the reference computes them
-        (the engine and the oracle's default use FP64)."""
-        self.L.oracle_set_long_double.argtypes = [ctypes.c_void_p, ctypes.c_int]
-        self.L.oracle_set_long_double(self.h, 1 if on else 0)
+    def set_reference_arithmetic(self, on=True):
+        """The reference's own arithmetic: long double Rosenbluth weights and
+        the C library's exp (default: the engine's FP64 weights and its own
+        exp, ldo_math.h, which the GPU computes bit for bit alike)."""
+        self.L.oracle_set_reference_arithmetic.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        self.L.oracle_set_reference_arithmetic(self.h, 1 if on else 0)
 
     def run(self, steps, trace=True):
         tr = np.zeros((steps, 8)) if trace else None
@@ -200,3 +201,13 @@ def set_learn_table(rep, w):
     rep._learn_w = w
     if L.oracle_set_learn_table(rep.h, w.ctypes.data, len(w)) != 0:
         raise OracleError(L.oracle_last_error().decode())
+
+
+def engine_exp(x):
+    """ldo_math::exp evaluated on the host."""
+    L = lib()
+    L.oracle_engine_exp.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.zeros_like(x)
+    L.oracle_engine_exp(x.ctypes.data, y.ctypes.data, len(x))
+    return y

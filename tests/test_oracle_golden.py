@@ -30,7 +30,7 @@ def load(path):
 def test_oracle_matches_reference_trace(path):
     fx = load(path)
     o = OracleReplica(inp(fx["case"]), seed=fx["seed"], replica=0)
-    o.set_long_double(True)
+    o.set_reference_arithmetic(True)
     tr = o.run(fx["steps"])
     ref = np.array(fx["trace"], dtype=np.float64)
     assert ref.shape == tr.shape
