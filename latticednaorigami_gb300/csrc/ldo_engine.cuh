@@ -241,7 +241,6 @@ struct Rep : public LdoState<C> {
     const LdoRepCtl* ctl;
     const double* grid;
     const double* learn_w;   // learned insertion proposal weights (LDO_LEARN_TABLE)
-    LdoCtWork<C>* ct;        // scaffold regrowth working memory (global), or null
     int learn_tb;            // temperature bin of the current tables
     // scalars of the current table set and controls, cached in the object
     int t_dense, t_stack_dense, imax, dim;
@@ -276,6 +275,7 @@ struct Rep : public LdoState<C> {
     int cur_mv;
     long long cur_s;
     int cb_cs;
+    LdoCtWork<C>* ct;        // scaffold regrowth working memory (global), or null
 
     // Accessors used by the FourBody traversal.
     __device__ __forceinline__ int gst(int i) const { return st[i]; }
@@ -3494,6 +3494,9 @@ struct Rep : public LdoState<C> {
     // reference's reset_origami + update_move_params + calc_move: the same
     // lattice state, order parameters and biases; the energy and bias totals
     // come back exactly instead of through the reversal's roundings.
+    // CT: the kernel is built with the scaffold regrowth movetypes (a kernel
+    // without them keeps their code out of its instruction stream).
+    template <bool CT>
     __device__ __noinline__ int step_begin(long long s) {
         cur_s = s;
         double r = rng.uniform_real();
@@ -3507,27 +3510,21 @@ struct Rep : public LdoState<C> {
         }
         cur_mv = mv;
         reset_internal();
+        int kind = sys->move_kind[mv];
+        if (kind >= LDO_MV_CTRG) {   // scaffold regrowth
+            if constexpr (CT) {
+                if (ct) return kind <= LDO_MV_CTRG_JUMP ? rg_begin(kind) : ctcb_begin(kind);
+            }
+            fail(LDO_RS_INVARIANT);
+            return 0;
+        }
         bool acc = false;
-        switch (sys->move_kind[mv]) {
+        switch (kind) {
         case LDO_MV_ORIENT: acc = orientation_rotation(); break;
         case LDO_MV_MET_EXCHANGE: acc = met_exchange(); break;
         case LDO_MV_MET_REGROWTH: acc = met_regrowth(); break;
         case LDO_MV_LEARNED_EXCHANGE: acc = learned_exchange(); break;
         case LDO_MV_CB_REGROWTH: return cb_begin();
-        case LDO_MV_CTRG:
-        case LDO_MV_CTRG_JUMP:
-            if (!ct) {
-                fail(LDO_RS_INVARIANT);
-                return 0;
-            }
-            return rg_begin(sys->move_kind[mv]);
-        case LDO_MV_CTCB:
-        case LDO_MV_CTCB_JUMP:
-            if (!ct) {
-                fail(LDO_RS_INVARIANT);
-                return 0;
-            }
-            return ctcb_begin(sys->move_kind[mv]);
         }
         return finish_move(acc, 0);
     }
@@ -3571,16 +3568,19 @@ struct Rep : public LdoState<C> {
         return cmd;
     }
 
+    template <bool CT>
     __device__ __noinline__ int step_resume() {
         if (bad()) return 0;
         if (phase == PH_CB2) return cb_mid();
         if (phase == PH_CB3) return cb_end();
-        if (phase == PH_RG2) return rg_grow();
-        if (phase == PH_RG3) return rg_weigh_new();
-        if (phase == PH_RG4) return rg_old_opens();
-        if (phase == PH_RG5) return rg_weigh_old();
-        if (phase == PH_CT2) return ctcb_new();
-        if (phase == PH_CT3) return ctcb_old();
+        if constexpr (CT) {
+            if (phase == PH_RG2) return rg_grow();
+            if (phase == PH_RG3) return rg_weigh_new();
+            if (phase == PH_RG4) return rg_old_opens();
+            if (phase == PH_RG5) return rg_weigh_old();
+            if (phase == PH_CT2) return ctcb_new();
+            if (phase == PH_CT3) return ctcb_old();
+        }
         phase = 0;
         if (recalc) {
             recalc = false;

@@ -96,7 +96,7 @@ __device__ __forceinline__ void snapshot_ops(int cmd, ldo::Rep<C>* R, unsigned c
 // Shared memory per warp: Rep (replica state followed by the working fields).
 // Lane 0 runs the moves; the whole warp loads and stores the state and
 // copies the move snapshots (global memory, L.snap).
-template <class C>
+template <class C, bool CT>
 __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
     extern __shared__ __align__(16) unsigned char smem[];
     int warp = threadIdx.x >> 5;
@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
         warp_copy16(snap, base, snap_bytes<C>(), lane);   // snapshot 0: state at the start of the move
         for (long long k = 0; k < nsteps; ++k) {
             int cmd = 0;
-            if (lane == 0) cmd = R->bad() ? ldo::CMD_STOP : R->step_begin(h.steps_done + 1);
+            if (lane == 0) cmd = R->bad() ? ldo::CMD_STOP : R->template step_begin<CT>(h.steps_done + 1);
             cmd = __shfl_sync(0xffffffffu, cmd, 0);
             if (cmd & ldo::CMD_STOP) break;
             // a step has at most four phases (CB: three, then the post-move work)
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
             for (int guard = 0; guard < 8; ++guard) {
                 if (cmd & 0xff) snapshot_ops<C>(cmd, R, base, snap, lane);
                 if (!(cmd & ldo::CMD_MORE)) break;
-                if (lane == 0) cmd = R->step_resume();
+                if (lane == 0) cmd = R->template step_resume<CT>();
                 cmd = __shfl_sync(0xffffffffu, cmd, 0);
             }
             if (lane == 0) {
@@ -287,15 +287,24 @@ cudaError_t ldo_launch_pt_swap(const LdoPT& P, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
-template <class C>
-static cudaError_t launch_mc_class(const LdoLaunch& L, cudaStream_t stream) {
+template <class C, bool CT>
+static cudaError_t launch_mc_variant(const LdoLaunch& L, cudaStream_t stream) {
     int wpb = L.warps_per_block;
     size_t smem = (size_t)wpb * warp_bytes<C>() + (size_t)L.smem_pad;
-    cudaError_t err = cudaFuncSetAttribute(ldo_mc_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t err =
+        cudaFuncSetAttribute(ldo_mc_kernel<C, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
     int blocks = (L.n_rep + wpb - 1) / wpb;
-    ldo_mc_kernel<C><<<blocks, wpb * 32, smem, stream>>>(L);
+    ldo_mc_kernel<C, CT><<<blocks, wpb * 32, smem, stream>>>(L);
     return cudaGetLastError();
+}
+
+// The scaffold regrowth movetypes live in their own kernel variant (the
+// one with working memory): compiled into the staple-move kernel, their code
+// made it 13 % slower (its time is instruction fetch).
+template <class C>
+static cudaError_t launch_mc_class(const LdoLaunch& L, cudaStream_t stream) {
+    return L.ct_ws ? launch_mc_variant<C, true>(L, stream) : launch_mc_variant<C, false>(L, stream);
 }
 
 cudaError_t ldo_launch_mc(const LdoLaunch& L, cudaStream_t stream) {
