@@ -211,6 +211,137 @@ def run_reference_arm(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------- c4 ---
+# The 96-domain umbrella workload: 48 harmonic windows on the number of fully
+# bound domains (k = 0.5 kT/domain^2, centres 0..94 step 2) x 8 temperatures
+# (320..350 K), the 96-domain ThreeQuarterTurn design with 16 three-domain and
+# 24 two-domain staple types (8 bp domains, NN energies), 1 uM, and the
+# reference's standard moveset (orientation rotation, Met exchange, CB staple
+# regrowth, CTRG contiguous and jump scaffold regrowth).  Each replica keeps
+# its window and temperature (no exchange in the timed region).
+C4_WINDOWS, C4_TEMPS, C4_K = 48, 8, 0.5
+C4_SWEEPS_PER_STEP = 10
+C4_CPU_REPS = 48
+
+
+def write_c4(d):
+    import systems
+    with open(os.path.join(d, "c4_windows.json"), "w") as f:
+        json.dump({"origami": {"bias_functions": [
+            {"label": "window", "tag": "win", "type": "Harmonic", "k": C4_K, "centre": 0,
+             "ops": ["numfulldomains"], "level": 0}]}}, f)
+    return systems.write_case(d, "c4", extra=dict(bias_functions_file="c4_windows.json"))
+
+
+def c4_controls():
+    """(temperature, window centre) of every replica: replica r holds window
+    r % 48 at temperature r // 48."""
+    n = C4_WINDOWS * C4_TEMPS
+    temps = np.repeat(np.linspace(320.0, 350.0, C4_TEMPS), C4_WINDOWS)
+    centres = np.tile(2.0 * np.arange(C4_WINDOWS), C4_TEMPS)
+    return n, temps, centres
+
+
+def c4_cpu(inp, burn, rec):
+    """The oracle port on all host cores: C4_CPU_REPS replicas spread over the
+    windows and temperatures, the same burn-in and recorded sweeps."""
+    from oracle_lib import run_batch_sampled_centres
+    from latticednaorigami_gb300.analysis import effective_samples
+    n, temps, centres = c4_controls()
+    pick = np.linspace(0, n - 1, C4_CPU_REPS).astype(int)
+    cores = os.cpu_count() or 1
+    t, smp = run_batch_sampled_centres(inp, 0, C4_CPU_REPS, burn + rec, 96, cores, temps[pick], "win", centres[pick])
+    ess, tau = effective_samples(list(smp[:, burn:]))
+    t_rec = t * rec / float(burn + rec)
+    return {"value": ess / t_rec, "unit": "effective samples/s", "cores": cores, "kind": "port",
+            "sample": "%d replicas (every %dth window x temperature) x %d recorded sweeps after %d burn-in, "
+                      "%d threads" % (C4_CPU_REPS, n // C4_CPU_REPS, rec, burn, cores),
+            "sweeps_per_s": C4_CPU_REPS * rec / t_rec, "tau_int_median": tau}
+
+
+def run_c4(args, impl):
+    from latticednaorigami_gb300.analysis import effective_samples
+    tmp = tempfile.mkdtemp()
+    inp = write_c4(tmp)
+    n, temps, centres = c4_controls()
+    total = args.steps * C4_SWEEPS_PER_STEP
+    metric = "effective samples/s (tau_int of #bound domains), umbrella windows x temperatures, scaffold regrowth"
+    workload = ("c4: 96-domain ThreeQuarterTurn design (16 three- and 24 two-domain staple types, 8 bp, NN), "
+                "48 harmonic windows (k=0.5, centres 0..94) x 8 temperatures 320..350 K = 384 replicas, 1 uM; "
+                "reference standard moveset with CTRG contiguous and jump scaffold regrowth")
+    if impl == "reference":
+        cpu = c4_cpu(inp, args.warmup * C4_SWEEPS_PER_STEP, total)
+        line = {"impl": "reference", "metric": metric, "value": cpu["value"], "unit": "effective samples/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": workload}, "cpu_baseline": cpu,
+                "e2e": {"value": cpu["value"], "unit": "effective samples/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    from latticednaorigami_gb300 import Engine
+    eng = Engine(inp, n_replicas=n, seed=0)
+    eng.set_controls(temps=temps)
+    for r in range(n):
+        eng.set_bias_centre("win", r, centres[r])
+    eng.set_sampling(1, total)
+    for _ in range(args.warmup):
+        eng.run_sweeps(C4_SWEEPS_PER_STEP)
+    eng.set_sampling(1, total)
+    clocks = ClockSampler()
+    clocks.start()
+    dev_ms = [eng.run_sweeps(C4_SWEEPS_PER_STEP) for _ in range(args.steps)]
+    clk = clocks.stop()
+    t_dev = sum(dev_ms) / 1000.0
+    smp, cnt = eng.samples()
+    ess, tau = effective_samples([smp[r, :cnt[r], 0] for r in range(n)])
+    stats = eng.move_stats(5)
+    # e2e: the same loop with controls uploaded and samples read every step
+    eng2 = Engine(inp, n_replicas=n, seed=1)
+    for r in range(n):
+        eng2.set_bias_centre("win", r, centres[r])
+    eng2.set_controls(temps=temps)
+    eng2.set_sampling(1, C4_SWEEPS_PER_STEP)
+    for _ in range(args.warmup):
+        eng2.run_sweeps(C4_SWEEPS_PER_STEP)
+    series = [[] for _ in range(n)]
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng2.set_controls(temps=temps)
+        eng2.set_sampling(1, C4_SWEEPS_PER_STEP)
+        eng2.run_sweeps(C4_SWEEPS_PER_STEP)
+        s2, c2 = eng2.samples()
+        for r in range(n):
+            series[r].append(s2[r, :c2[r], 0])
+    t_e2e = time.perf_counter() - t0
+    e2e_ess, _ = effective_samples([np.concatenate(x) for x in series])
+    lay_bytes = eng.state_bytes()
+    alg_bytes = n * lay_bytes * 2 + n * C4_SWEEPS_PER_STEP * 4
+    achieved = alg_bytes / (np.mean(dev_ms) / 1000.0) / 1e9
+    peak, peak_kind = measured_peaks()
+    obs = eng.observables()
+    line = {"metric": metric, "value": ess / t_dev, "unit": "effective samples/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(dev_ms)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload, "sweeps_per_step": C4_SWEEPS_PER_STEP, "replicas": n,
+                       "l2": "state resident in shared memory; no L2 flush needed"},
+            "sweeps_per_s": n * total / t_dev, "move_attempts_per_s": n * 96 * total / t_dev,
+            "tau_int_median": tau,
+            "fully_bound_mean_by_temperature": [float(np.mean([obs[r]["num_fully_bound"]
+                                                               for r in range(t * C4_WINDOWS, (t + 1) * C4_WINDOWS)]))
+                                                for t in range(C4_TEMPS)],
+            "move_stats": stats.tolist(),
+            "e2e": {"value": e2e_ess / t_e2e, "unit": "effective samples/s",
+                    "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * C4_SWEEPS_PER_STEP * 4},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind},
+            "clocks": clk}
+    if not args.no_cpu:
+        line["cpu_baseline"] = c4_cpu(inp, args.warmup * C4_SWEEPS_PER_STEP, total)
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -218,8 +349,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c4"],
+                    help="c2: the learned-vs-plain headline workload; c4: the 96-domain umbrella workload")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
+    if args.workload == "c4":
+        if rank == 0:
+            run_c4(args, args.impl)
+        return
     if args.impl == "reference":
         if rank == 0:
             run_reference_arm(args)

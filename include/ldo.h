@@ -131,6 +131,11 @@ ldo_status ldo_set_grid_bias(ldo_engine* e, const char* tag, int replica, const 
  * (SquareWellBiasFunction::set_min_op/set_max_op, src/bias_functions.cpp:218-220). */
 ldo_status ldo_set_window(ldo_engine* e, const char* tag, int replica, int min_op, int max_op);
 
+/* Centre of one replica's Harmonic bias `tag` (engine extension: the
+ * reference has no harmonic bias; 0.5 k (x - centre)^2 restrains an umbrella
+ * window).  Like ldo_set_window, the new bias enters at the next move. */
+ldo_status ldo_set_bias_centre(ldo_engine* e, const char* tag, int replica, double centre);
+
 /* Parallel tempering: `swaps` rounds of (update controls, exchange_interval
  * steps, exchange attempt between neighbouring control slots), the 1-D
  * even/odd schedule of PTGCMCSimulation::run / OneDPTGCMCSimulation::
@@ -195,10 +200,11 @@ ldo_status ldo_replica_status_noalloc(ldo_engine* e, int32_t* status_of_replica,
 
 /* No counterpart in the reference.  The engine's exponential, y[i] =
  * exp(x[i]) for i < n, evaluated on the GPU: the function every acceptance
- * probability and Rosenbluth weight of the engine uses (Cody-Waite reduction
- * and a Taylor series, below one unit in the last place), with the same bits
- * as its host version, so that host code can repeat the engine's decisions
- * exactly.  The reference uses the C library's exp instead. */
+ * probability and Rosenbluth weight of the engine uses (Tang's table-driven
+ * method, about half a unit in the last place), with the same bits as its
+ * host version, so that host code can repeat the engine's decisions exactly.
+ * The reference uses the C library's exp instead.  Allocates and frees two
+ * device buffers of n doubles. */
 ldo_status ldo_engine_exp(const double* x, double* y, int n);
 
 /* Learned insertion proposal (movetype "LearnedStapleExchange"; engine

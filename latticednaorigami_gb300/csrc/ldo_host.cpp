@@ -1654,6 +1654,23 @@ ldo_status ldo_set_window(ldo_engine* e, const char* tag, int replica, int min_o
     });
 }
 
+ldo_status ldo_set_bias_centre(ldo_engine* e, const char* tag, int replica, double centre) {
+    if (!e || !tag || replica < 0 || replica >= e->n_rep) return LDO_EINVAL;
+    return guard(e, [&]() {
+        const HostSystem& hs = e->systems[e->sys_of[replica]];
+        bool found = false;
+        for (int b = 0; b < hs.desc.n_biases; ++b)
+            if (hs.biases[b].tag == tag) {
+                if (hs.desc.bias_kind[b] != LDO_B_HARMONIC)
+                    throw LdoError(LDO_EINVAL, string("bias function ") + tag + " is not Harmonic");
+                found = true;
+                e->h_ctl[replica].centre[b] = centre;
+            }
+        if (!found) throw LdoError(LDO_EINVAL, string("no bias function tagged ") + tag);
+        e->upload_ctl();
+    });
+}
+
 } // extern "C"
 
 extern "C" {

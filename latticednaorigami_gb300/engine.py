@@ -23,6 +23,7 @@ EXPORTS = [
     "ldo_learn_collect", "ldo_learn_reset_counts", "ldo_learn_get_counts", "ldo_learn_train", "ldo_learn_set_params",
     "ldo_learn_get_params", "ldo_learn_get_table", "ldo_learn_set_table", "ldo_learn_loss_grad",
     "ldo_writer_open", "ldo_writer_write", "ldo_writer_close", "ldo_pt2d_run", "ldo_engine_exp",
+    "ldo_set_bias_centre",
 ]
 
 LEARN_TABLE = 524288      # network inputs (ldo_learn.h)
@@ -79,6 +80,7 @@ def load_library(path=None):
     lib.ldo_get_move_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ip]
     lib.ldo_set_grid_bias.argtypes = [vp, ctypes.c_char_p, ip, dp, ip]
     lib.ldo_set_window.argtypes = [vp, ctypes.c_char_p, ip, ip, ip]
+    lib.ldo_set_bias_centre.argtypes = [vp, ctypes.c_char_p, ip, ctypes.c_double]
     lib.ldo_pt_run.argtypes = [vp, ip, ctypes.c_int64, ip, ip, dp]
     lib.ldo_pt2d_run.argtypes = [vp, ip, ip, ctypes.c_int64, ip, dp]
     lib.ldo_pt_get_permutation.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ip]
@@ -213,6 +215,9 @@ class Engine:
 
     def set_window(self, tag, replica, min_op, max_op):
         self._check(self.lib.ldo_set_window(self.h, tag.encode(), replica, min_op, max_op))
+
+    def set_bias_centre(self, tag, replica, centre):
+        self._check(self.lib.ldo_set_bias_centre(self.h, tag.encode(), replica, float(centre)))
 
     def pt_run(self, n_rungs, swaps, exchange_interval, exchange_q=1):
         ms = ctypes.c_double(0)

@@ -360,6 +360,17 @@ int oracle_set_window(void* h, const char* tag, int min_op, int max_op) {
     return -1;
 }
 
+int oracle_set_bias_centre(void* h, const char* tag, double centre) {
+    System& s = static_cast<Replica*>(h)->sys;
+    for (auto& b : s.biases)
+        if (b.tag == tag && b.kind == B_HARMONIC) {
+            b.centre = centre;
+            return 0;
+        }
+    g_err = std::string("no harmonic bias ") + tag;
+    return -1;
+}
+
 // `count` uniform reals of Philox key (seed, key1), stream `stream`, from draw `first`.
 void oracle_uniforms(uint32_t seed, uint32_t key1, uint32_t stream, unsigned long long first, int count, double* out) {
     Stream st;
@@ -485,12 +496,14 @@ int oracle_run_batch_states(const char* inp_path, const char* overrides, uint32_
 // CPU baseline with order-parameter samples: n_rep replicas (key (seed0, r)),
 // each `sweeps` sweeps of sweep_len steps; after every sweep the number of
 // fully bound domain pairs goes to out[r * sweeps + k].  Returns wall seconds.
-double oracle_run_batch_sampled(const char* inp_path, const char* overrides, uint32_t seed0, int n_rep,
-                                long long sweeps, int sweep_len, int threads, const double* temps, short* out) {
+double oracle_run_batch_sampled_centres(const char* inp_path, const char* overrides, uint32_t seed0, int n_rep,
+                                        long long sweeps, int sweep_len, int threads, const double* temps,
+                                        const char* centre_tag, const double* centres, short* out) {
     std::vector<Replica*> reps(n_rep, nullptr);
     for (int i = 0; i < n_rep; ++i) {
         reps[i] = build(inp_path, overrides, seed0, (uint32_t)i);
-        if (!reps[i] || (temps && oracle_update_temp(reps[i], temps[i], 1.0) != 0)) {
+        if (!reps[i] || (temps && oracle_update_temp(reps[i], temps[i], 1.0) != 0) ||
+            (centres && oracle_set_bias_centre(reps[i], centre_tag, centres[i]) != 0)) {
             for (auto* r : reps) delete r;
             return -1;
         }
@@ -519,6 +532,12 @@ double oracle_run_batch_sampled(const char* inp_path, const char* overrides, uin
     double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     for (auto* r : reps) delete r;
     return failed.load() ? -2 : dt;
+}
+
+double oracle_run_batch_sampled(const char* inp_path, const char* overrides, uint32_t seed0, int n_rep,
+                                long long sweeps, int sweep_len, int threads, const double* temps, short* out) {
+    return oracle_run_batch_sampled_centres(inp_path, overrides, seed0, n_rep, sweeps, sweep_len, threads, temps,
+                                            nullptr, nullptr, out);
 }
 
 } // extern "C"

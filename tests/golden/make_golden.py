@@ -28,6 +28,8 @@ RUNS = [("c1", 1, 20000), ("c1", 2, 20000), ("g24a", 3, 20000), ("g24b", 4, 2000
         ("g24d", 6, 10000), ("g24e", 7, 20000), ("c3", 8, 10000),
         # scaffold regrowth (conserved topology, recoil growth and configurational bias)
         ("s24a", 3, 20000), ("s24b", 4, 20000), ("s24c", 5, 20000), ("r24", 6, 20000), ("s48", 7, 10000),
+        # the 96-domain ThreeQuarterTurn design with two- and three-domain staples
+        ("c4", 9, 20000),
         # a run with a weight ratio within a rounding of 1 at step 19885 (long double vs FP64)
         ("s24a", 11, 20000)]
 

@@ -159,6 +159,33 @@ def run_batch_sampled(inp, seed, n_rep, sweeps, sweep_len, threads, overrides=""
     return t, out
 
 
+def run_batch_sampled_centres(inp, seed, n_rep, sweeps, sweep_len, threads, temps, centre_tag, centres,
+                              overrides=""):
+    """run_batch_sampled with one Harmonic bias centre per replica."""
+    L = lib()
+    L.oracle_run_batch_sampled_centres.restype = ctypes.c_double
+    L.oracle_run_batch_sampled_centres.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_int,
+                                                   ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                                   ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p]
+    out = np.zeros((n_rep, sweeps), np.int16)
+    temps = np.ascontiguousarray(temps, np.float64)
+    centres = np.ascontiguousarray(centres, np.float64)
+    assert len(temps) == n_rep and len(centres) == n_rep
+    t = L.oracle_run_batch_sampled_centres(os.fsencode(inp), overrides.encode(), seed, n_rep, sweeps, sweep_len,
+                                           threads, temps.ctypes.data, centre_tag.encode(), centres.ctypes.data,
+                                           out.ctypes.data)
+    if t < 0:
+        raise OracleError(L.oracle_last_error().decode() or "oracle batch failed")
+    return t, out
+
+
+def set_bias_centre(rep, tag, centre):
+    L = rep.L
+    L.oracle_set_bias_centre.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_double]
+    if L.oracle_set_bias_centre(rep.h, tag.encode(), float(centre)) != 0:
+        raise OracleError(L.oracle_last_error().decode())
+
+
 def uniform(seed, key1, stream, index):
     L = lib()
     L.oracle_uniforms.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_ulonglong,

@@ -51,6 +51,30 @@ def staple_pairs(n, row_len=4):
     return pairs
 
 
+def staple_groups_mixed(n, n_three_pairs):
+    """Scaffold index groups of a mixed staple set on rows of 4: the first
+    n_three_pairs row pairs each get two three-domain staples (a crossover and
+    its neighbour along the row, at both ends) and one helix staple in the
+    middle of the first row; the remaining row pairs get the four two-domain
+    staples of staple_pairs.  Every group's consecutive scaffold domains are
+    lattice neighbours in the serpentine layout."""
+    assert n % 8 == 0
+    rows = n // 4
+    idx = lambda r, x: 4 * r + (x if r % 2 == 0 else 3 - x)
+    groups = []
+    for k, r in enumerate(range(0, rows, 2)):
+        if k < n_three_pairs:
+            groups.append((idx(r, 0), idx(r + 1, 0), idx(r + 1, 1)))
+            groups.append((idx(r, 3), idx(r + 1, 3), idx(r + 1, 2)))
+            groups.append((idx(r, 1), idx(r, 2)))
+        else:
+            groups.append((idx(r, 0), idx(r + 1, 0)))
+            groups.append((idx(r, 3), idx(r + 1, 3)))
+            groups.append((idx(r, 1), idx(r, 2)))
+            groups.append((idx(r + 1, 1), idx(r + 1, 2)))
+    return groups
+
+
 def linear_pairs(n):
     return [(i, i + 1) for i in range(0, n - 1, 2)]
 
@@ -76,9 +100,9 @@ def make_system(n, pairs, seed, positions, seq_len=16, cyclic=False):
     scaf_seq = ["".join(rng.choice("ACGT") for _ in range(seq_len)) for _ in range(n)]
     idents = [[i + 1 for i in range(n)]]
     seqs = [scaf_seq]
-    for a, b in pairs:
-        idents.append([-(a + 1), -(b + 1)])
-        seqs.append([revcomp(scaf_seq[a]), revcomp(scaf_seq[b])])
+    for group in pairs:
+        idents.append([-(a + 1) for a in group])
+        seqs.append([revcomp(scaf_seq[a]) for a in group])
     return {"origami": {
         "cyclic": cyclic,
         "identities": idents,
@@ -112,6 +136,14 @@ MOVES = {
               ("CB staple regrowth", "CBStapleRegrowth", "1/4"),
               ("Contiguous CTRG scaffold regrowth", "CTRGScaffoldRegrowth", "1/4",
                dict(max_num_recoils=2, max_c_attempts=12, max_regrowth=6))],
+    # examples/moveset_standard.json of the reference
+    "std": [("Orientation rotation", "OrientationRotation", "2/6"),
+            ("Met staple exchange", "MetStapleExchange", "1/6"),
+            ("CB staple regrowth", "CBStapleRegrowth", "1/6"),
+            ("Contiguous CTRG scaffold regrowth", "CTRGScaffoldRegrowth", "1/6",
+             dict(max_num_recoils=1, max_c_attempts=36, max_regrowth=12)),
+            ("Non-contiguous CTRG scaffold regrowth", "CTRGJumpScaffoldRegrowth", "1/6",
+             dict(max_num_recoils=1, max_c_attempts=36, max_regrowth=12, max_seg_regrowth=2))],
     # every scaffold regrowth movetype together
     "ctall": [("Orientation rotation", "OrientationRotation", "2/8"),
               ("Met staple exchange", "MetStapleExchange", "1/8"),
@@ -199,6 +231,10 @@ CASES = {
     # cyclic scaffold (a closed ring), every scaffold movetype
     "r24": ("ring24", "ctall", dict(stacking_ene=-1000, staple_M=1e-3, temp=330, max_total_staples=24,
                                     max_type_staples=4)),
+    # the 96-domain ThreeQuarterTurn design (40 staple types of 2-3 domains,
+    # 8 bp domains) with the reference's standard moveset
+    "c4": ("mixed96", "std", dict(domain_type="ThreeQuarterTurn", stacking_ene=-1000, staple_M=1e-6, temp=310,
+                                  max_total_staples=40, max_type_staples=1, max_staple_size=3)),
     # the 48-domain system's shape with the reference's standard moveset
     "s48": ("grid48", "ctrg", dict(stacking_ene=-1000, staple_M=1e-4, temp=335, max_total_staples=48,
                                    max_type_staples=2)),
@@ -212,6 +248,9 @@ def system_for(name):
     if name.startswith("ring"):
         n = int(name[4:])
         return make_system(n, linear_pairs(n), seed=n + 1, positions=ring(n), cyclic=True)
+    if name == "mixed96":
+        # the 96-domain design: 16 three-domain and 24 two-domain staple types, 8 bp domains
+        return make_system(96, staple_groups_mixed(96, 8), seed=96, positions=serpentine(96, 4), seq_len=8)
     if name.startswith("grid"):
         n = int(name[4:])
         return make_system(n, staple_pairs(n), seed=n, positions=serpentine(n, 4))

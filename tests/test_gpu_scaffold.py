@@ -6,18 +6,20 @@ agree exactly at every step, the FP64 energies within 1e-12 relative."""
 import gzip
 import json
 import os
+import tempfile
 
 import numpy as np
 import pytest
 
 from conftest import GOLDEN, inp
-from oracle_lib import OracleReplica
+from oracle_lib import OracleReplica, set_bias_centre
+import systems
 
 pytestmark = pytest.mark.gpu
 
 EXACT = [0, 2, 3, 4, 5, 7]   # step, staples, fully bound, bound, stacked, draws
-CASES = ["s24a", "s24b", "s24c", "r24", "s48"]
-FIXTURES = ["s24a_s3", "s24b_s4", "s24c_s5", "r24_s6", "s48_s7"]
+CASES = ["s24a", "s24b", "s24c", "r24", "s48", "c4"]
+FIXTURES = ["s24a_s3", "s24b_s4", "s24c_s5", "r24_s6", "s48_s7", "c4_s9"]
 
 
 def engine(*a, **k):
@@ -115,3 +117,33 @@ def test_engine_exp_same_bits_on_gpu_and_host():
     m = (np.abs(x) < 700)
     ulp = np.spacing(np.exp(x[m]))
     assert np.max(np.abs(g[m] - np.exp(x[m])) / ulp) <= 1.5
+
+
+def test_harmonic_windows_with_scaffold_moves():
+    """Umbrella windows of the 96-domain design: a Harmonic bias on the number
+    of fully bound domains with a different centre per replica
+    (ldo_set_bias_centre), the reference's standard moveset, two temperatures."""
+    d = tempfile.mkdtemp()
+    with open(os.path.join(d, "harm.json"), "w") as f:
+        json.dump({"origami": {"bias_functions": [
+            {"label": "window", "tag": "win", "type": "Harmonic", "k": 0.5, "centre": 0,
+             "ops": ["numfulldomains"], "level": 0}]}}, f)
+    p = systems.write_case(d, "c4", extra=dict(bias_functions_file="harm.json"))
+    centres = [0, 6, 14, 24, 40, 60]
+    temps = [310.0, 320.0, 310.0, 320.0, 310.0, 320.0]
+    n, seed, steps = len(centres), 23, 3000
+    eng = engine(p, n_replicas=n, seed=seed)
+    eng.set_controls(temps=np.array(temps))
+    for r, c in enumerate(centres):
+        eng.set_bias_centre("win", r, c)
+    eng.set_trace(n, steps)
+    eng.run(steps)
+    tr = eng.trace()
+    for r in range(n):
+        o = OracleReplica(p, seed=seed, replica=r)
+        o.update_temp(temps[r])
+        set_bias_centre(o, "win", centres[r])
+        check_trace(tr[r], o.run(steps))
+        assert eng.config(r) == o.config()
+    # each replica is restrained by its own centre
+    assert tr[5, -1, 6] > tr[4, -1, 6] > tr[2, -1, 6]
