@@ -2841,6 +2841,72 @@ struct Rep : public LdoState<C> {
         }
         return fmin(1.0, dexp(-dc.e));
     }
+    // calc_p_config_open of the configurations of one trial loop, evaluated
+    // per neighbour site: the trials of a loop all see the same state (an
+    // open trial that grows feelers restores it), and of the six
+    // orientations at a site only one can bind.  An empty site is open for
+    // every orientation when its walks remain (no potential is evaluated:
+    // e^-0); an occupied one is closed; an unbound one is open at most for the
+    // orientation opposite to its domain's, and only if the domain is on the
+    // same chain or at an active endpoint (the FourBody probe runs only
+    // then).  The same values as probing every configuration, with at most
+    // six walk checks and six probes per loop.
+    struct RgSites {
+        int8_t kind[6];        // -1 unknown, 0 closed, 1 open (p = 1), 2 open for orientation opp only
+        int8_t opp[6];
+        double pv[6];
+    };
+    __device__ static void rg_sites_reset(RgSites& c) {
+        #pragma unroll
+        for (int k = 0; k < 6; ++k) c.kind[k] = -1;
+    }
+    __device__ __noinline__ double rg_p_open_site(V3 p, int o, int k, RgSites& c) {
+        LdoCtWork<C>& w = *ct;
+        if (w.stemd) return rg_p_open(p, o);
+        if (c.kind[k] < 0) {
+            int d = w.d;
+            int occ = occupancy(p);
+            if (occ == BOUND || occ == MISBOUND || !ct_walks_ok(d, p)) {
+                c.kind[k] = 0;
+            }
+            else if (occ == UNBOUND) {
+                int od = unbound_at(p);
+                bool same = scs[od] == scs[d];
+                if (!(same || ct_endpoint_reached(d, p))) {
+                    c.kind[k] = 0;
+                }
+                else {
+                    int op = ore[od] ^ 1;
+                    c.kind[k] = 2;
+                    c.opp[k] = (int8_t)op;
+                    Delta dc = probe_domain(d, p, op);
+                    if (hdr.violated) {
+                        hdr.violated = 0;
+                        c.pv[k] = 0;
+                    }
+                    else {
+                        c.pv[k] = fmin(1.0, dexp(-dc.e));
+                    }
+                }
+            }
+            else {
+                c.kind[k] = 1;
+            }
+        }
+        if (c.kind[k] == 0) return 0;
+        if (c.kind[k] == 1) return 1.0;
+        return o == c.opp[k] ? c.pv[k] : 0;
+    }
+    __device__ __noinline__ void rg_select_trial_site(V3& p, int& o, int& k) {
+        LdoCtWork<C>& w = *ct;
+        if (w.stemd) {
+            rg_select_trial(p, o);
+            k = 0;
+            return;
+        }
+        rg_select_trial(p, o);
+        k = unit_index(sub(p, pos(w.ref)));
+    }
     __device__ bool rg_test_open(double p) {   // test_config_open (:346)
         p = fmin(1.0, p);
         if (p == 1) return true;
@@ -2875,11 +2941,14 @@ struct Rep : public LdoState<C> {
             int o = 0;
             double pc = 0;
             bool open = false;
+            RgSites sc;
+            rg_sites_reset(sc);
             #pragma unroll 1
             while (!open && w.catt != w.dmax && !bad()) {
                 w.catt++;
-                rg_select_trial(p, o);
-                pc = rg_p_open(p, o);
+                int k;
+                rg_select_trial_site(p, o, k);
+                pc = rg_p_open_site(p, o, k, sc);
                 open = rg_test_open(pc);
             }
             if (open) {
@@ -2916,11 +2985,14 @@ struct Rep : public LdoState<C> {
             V3 p = 0;
             int o = 0;
             bool open = false;
+            RgSites sc;
+            rg_sites_reset(sc);
             #pragma unroll 1
             while (!open && w.catt != w.dmax && !bad()) {
                 w.catt++;
-                rg_select_trial(p, o);
-                double pc = rg_p_open(p, o);
+                int k;
+                rg_select_trial_site(p, o, k);
+                double pc = rg_p_open_site(p, o, k, sc);
                 open = rg_test_open(pc);
             }
             if (open) {
@@ -2974,13 +3046,15 @@ struct Rep : public LdoState<C> {
                 w.ref = next(d, -w.dir);
                 int catt = w.catt_wq[w.di];
                 w.avail = w.av_wq[w.di];
+                RgSites sc;
+                rg_sites_reset(sc);
                 #pragma unroll 1
                 while (catt != w.max_c_attempts && !bad()) {
                     catt++;
                     V3 p;
-                    int o;
-                    rg_select_trial(p, o);
-                    double pc = rg_p_open(p, o);
+                    int o, k;
+                    rg_select_trial_site(p, o, k);
+                    double pc = rg_p_open_site(p, o, k, sc);
                     if (rg_test_open(pc)) {
                         set_checked(d, p, o);
                         ct_update_endpoints(d);
@@ -3164,14 +3238,21 @@ struct Rep : public LdoState<C> {
         LdoCtWork<C>& w = *ct;
         V3 p_prev = pos(prev);
         int nc = 0;
+        // calc_biases (:58) and the zero weights of calc_bias (:480): a site
+        // whose weight calc_bias sets to zero is not probed (its weight
+        // would be zero either way; zero terms leave the sum and the
+        // selection unchanged)
         #pragma unroll 1
         for (int v = 0; v < 6; ++v) {
             V3 p = add(p_prev, unit(v));
             int occ = occupancy(p);
             if (occ == BOUND || occ == MISBOUND) continue;
+            bool zero = !ct_walks_ok(dom, p);
             if (occ == UNBOUND) {
                 int ud = unbound_at(p);
                 int o = ore[ud] ^ 1;
+                if (!zero && !(scs[ud] == scs[dom] || ct_endpoint_reached(dom, p))) zero = true;
+                if (zero) continue;
                 Delta dc = probe_domain(dom, p, o);
                 if (bad()) return;
                 if (!hdr.violated) {
@@ -3189,22 +3270,12 @@ struct Rep : public LdoState<C> {
                 }
             }
             else {
+                if (zero) continue;
                 cb_pos[nc] = p;
                 cb_ore[nc] = -1;
                 cb_bf[nc] = 6.0;
                 nc++;
             }
-        }
-        #pragma unroll 1
-        for (int n = 0; n < nc; ++n) {
-            V3 p = cb_pos[n];
-            if (occupancy(p) == UNBOUND) {
-                int od = unbound_at(p);
-                bool same = scs[od] == scs[dom];
-                bool endpoint = ct_endpoint_reached(dom, p);
-                if (!(same || endpoint)) cb_bf[n] = 0;
-            }
-            if (!ct_walks_ok(dom, p)) cb_bf[n] = 0;
         }
         double sum = 0;
         #pragma unroll 1
