@@ -343,6 +343,7 @@ def run_c4(args, impl):
 
 
 def main():
+    global C4_SWEEPS_PER_STEP
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -351,7 +352,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="c2", choices=["c2", "c4"],
                     help="c2: the learned-vs-plain headline workload; c4: the 96-domain umbrella workload")
+    ap.add_argument("--sweeps-per-step", type=int, default=0,
+                    help="c4 only: sweeps per launch (default %d); small values make short profiler captures"
+                         % C4_SWEEPS_PER_STEP)
     args = ap.parse_args()
+    if args.sweeps_per_step > 0:
+        C4_SWEEPS_PER_STEP = args.sweeps_per_step
     rank = int(os.environ.get("RANK", "0"))
     if args.workload == "c4":
         if rank == 0:

@@ -2815,9 +2815,24 @@ struct Rep : public LdoState<C> {
             return;
         }
         int k = rng.uniform_int(0, n - 1);
-        #pragma unroll 1
-        for (int t = 0; t < k; ++t) av &= av - 1ull;
-        int ci = __ffsll((long long)av) - 1;
+        // the k-th set bit (0-based) of the mask, by halving (k < popcount)
+        int ci = 0;
+        int c = __popc((unsigned)av);
+        if (k >= c) {
+            k -= c;
+            av >>= 32;
+            ci = 32;
+        }
+        unsigned v = (unsigned)av;
+        #pragma unroll
+        for (int half = 16; half >= 1; half >>= 1) {
+            c = __popc(v & ((1u << half) - 1u));
+            if (k >= c) {
+                k -= c;
+                v >>= half;
+                ci += half;
+            }
+        }
         w.avail &= ~(1ull << ci);
         p = add(pos(w.ref), unit(ci / 6));
         o = ci % 6;
