@@ -1024,6 +1024,13 @@ struct ldo_engine {
         // counters 1..n_sets) forms one CUDA graph.
         int period = pt.n_sets;
         if (swaps >= 2 * period) {
+            // the graph holds the launch parameters by value (interval,
+            // sampling and trace buffers): capture again when they changed
+            LdoLaunch now = launch_params(LDO_MODE_RUN, exchange_interval);
+            if (pt_graph && std::memcmp(&now, &pt_graph_L, sizeof(LdoLaunch)) != 0) {
+                cudaGraphExecDestroy(pt_graph);
+                pt_graph = nullptr;
+            }
             if (!pt_graph) {
                 cudaGraph_t g;
                 CU(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
@@ -1031,9 +1038,8 @@ struct ldo_engine {
                 CU(cudaStreamEndCapture(stream, &g));
                 CU(cudaGraphInstantiate(&pt_graph, g, 0));
                 cudaGraphDestroy(g);
-                pt_graph_interval = exchange_interval;
+                pt_graph_L = now;
             }
-            if (pt_graph_interval != exchange_interval) throw LdoError(LDO_EINVAL, "exchange interval changed");
             // the graph starts with swap counter 1 (mod period): align
             while (pt_swap_i % period != 0 && done < swaps) {
                 pt_round(pt_swap_i + 1, exchange_interval);
@@ -1065,7 +1071,7 @@ struct ldo_engine {
         CU(cudaMemcpy(h_ctl.data(), d_ctl.p, h_ctl.size() * sizeof(LdoRepCtl), cudaMemcpyDeviceToHost));
         check_status();
     }
-    int pt_graph_interval {0};
+    LdoLaunch pt_graph_L {};
 
     // ------------------------------------------------ umbrella sampling ----
     static uint64_t host_philox_word(uint32_t seed, uint32_t key1, uint32_t stream, unsigned long long draw) {

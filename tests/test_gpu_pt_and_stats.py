@@ -156,3 +156,21 @@ def test_pt_2d_temperature_stacking_grid_matches_cpu_restatement():
         assert obs[r]["draws"] == ob["draws"]
         assert obs[r]["num_staples"] == ob["num_staples"]
         assert abs(obs[r]["energy"] - ob["energy"]) <= 1e-12 * max(1.0, abs(ob["energy"]))
+
+
+def test_pt_graph_follows_sampling_and_interval_changes():
+    """The captured PT cycle holds the kernel's launch parameters: a run after
+    set_sampling (or with another exchange interval) must use the new ones."""
+    temps = [325.0, 330.0, 336.0, 343.0]
+    d = tempfile.mkdtemp()
+    inp = systems.write_case(d, "g24a", extra=dict(temps=" ".join(map(str, temps)), num_reps=4))
+    eng = engine(inp, n_replicas=8, seed=5)
+    eng.pt_run(4, 8, 100, 1)              # captures the graph without sampling
+    eng.set_sampling(50, 64)
+    eng.pt_run(4, 8, 100, 1)              # 800 steps: a sample every 50
+    smp, cnt = eng.samples()
+    assert (cnt == 16).all(), cnt
+    eng.set_sampling(50, 64)
+    eng.pt_run(4, 8, 150, 1)              # another interval: 1200 steps
+    smp, cnt = eng.samples()
+    assert (cnt == 24).all(), cnt
