@@ -242,11 +242,29 @@ ldo_status ldo_learn_loss_grad(const float* params, const int32_t* idx, const fl
  * 519-789): <filebase>.vsf at open, then on every ldo_writer_write the
  * replica's current state, for the kinds set in `kinds`: 1 .trj, 2 .vcf
  * .states .ores, 4 .counts .staples .staplestates, 8 .ene, 16 .ops (the
- * .inp's ops_to_output, or every order parameter). */
+ * .inp's ops_to_output, or every order parameter), 32 .times (wall seconds
+ * since the writer was opened, as the reference's seconds since the start of
+ * its run). */
 typedef struct ldo_writer ldo_writer;
 ldo_status ldo_writer_open(ldo_engine* e, int replica, const char* filebase, uint32_t kinds, ldo_writer** out);
 ldo_status ldo_writer_write(ldo_writer* w, int64_t step);
 void ldo_writer_close(ldo_writer* w);
+
+/* The .swp file of one ladder of parallel tempering
+ * (PTGCMCSimulation::initialize_swap_file / write_swap_entry,
+ * src/ptmc_simulation.cpp:91,315): opens <filebase>.swp and writes the
+ * header (the exchanged controls of every slot, as the reference's
+ * "temp/u/ " columns), sets up the ladder as ldo_pt_run(n_rungs, exchange_q)
+ * would and starts recording the permutation (slot -> replica within the
+ * ladder) before every exchange attempt of later ldo_pt_run calls.
+ * ldo_writer_write(w, step) appends the recorded rows whose step is a
+ * multiple of freq (the reference's configs_output_freq) and, when step >= 0
+ * and a multiple of freq, the current permutation as the end-of-run row (the
+ * reference writes it once at the end of its run; pass -1 to only append the
+ * recorded rows).  The device keeps the last 4096 rows per ladder: write at
+ * least that often.  Close with ldo_writer_close. */
+ldo_status ldo_swap_writer_open(ldo_engine* e, int n_rungs, int exchange_q, int ladder, const char* filebase,
+                                int64_t freq, ldo_writer** out);
 
 /* Host-only helpers (no GPU needed). */
 

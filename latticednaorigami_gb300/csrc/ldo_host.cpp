@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <fstream>
 #include <functional>
 #include <map>
 #include <memory>
@@ -421,6 +422,11 @@ struct ldo_engine {
     DevBuf<long long> d_pt_att, d_pt_acc;
     DevBuf<int> d_pt_sched;
     int pt_dim2 {0}, pt_nctr {0};
+    vector<double> pt_slot_q;          // host copy of the slots' controls (4 x n_rungs)
+    // swap history (.swp): ring of hist_cap rows per ladder
+    DevBuf<int> d_hist_perm;
+    DevBuf<long long> d_hist_step, d_hist_n;
+    long long hist_cap {0};
     cudaGraphExec_t pt_graph {nullptr};
     LdoPT pt {};
 
@@ -990,10 +996,27 @@ struct ldo_engine {
         pt_dim2 = dim2;
         pt_nctr = n_ctr;
         pt_swap_i = 0;
+        pt_slot_q = slot;
+        hist_cap = 0;   // a new ladder shape drops the swap history
         if (pt_graph) {
             cudaGraphExecDestroy(pt_graph);
             pt_graph = nullptr;
         }
+    }
+
+    // Record the pre-exchange permutation of every round (ring of cap rows
+    // per ladder, the .swp rows).
+    void pt_record_swaps(long long cap) {
+        int nl = n_rep / pt_rungs;
+        d_hist_perm.alloc((size_t)cap * nl * pt_rungs);
+        d_hist_step.alloc((size_t)cap * nl);
+        d_hist_n.alloc(nl);
+        CU(cudaMemset(d_hist_n.p, 0, nl * sizeof(long long)));
+        hist_cap = cap;
+        pt.hist_perm = d_hist_perm.p;
+        pt.hist_step = d_hist_step.p;
+        pt.hist_n = d_hist_n.p;
+        pt.hist_cap = cap;
     }
 
     // One PTGCMCSimulation::run iteration (src/ptmc_simulation.cpp:110-141):
@@ -1027,7 +1050,8 @@ struct ldo_engine {
             // the graph holds the launch parameters by value (interval,
             // sampling and trace buffers): capture again when they changed
             LdoLaunch now = launch_params(LDO_MODE_RUN, exchange_interval);
-            if (pt_graph && std::memcmp(&now, &pt_graph_L, sizeof(LdoLaunch)) != 0) {
+            if (pt_graph && (std::memcmp(&now, &pt_graph_L, sizeof(LdoLaunch)) != 0 ||
+                             std::memcmp(&pt, &pt_graph_P, sizeof(LdoPT)) != 0)) {
                 cudaGraphExecDestroy(pt_graph);
                 pt_graph = nullptr;
             }
@@ -1039,6 +1063,7 @@ struct ldo_engine {
                 CU(cudaGraphInstantiate(&pt_graph, g, 0));
                 cudaGraphDestroy(g);
                 pt_graph_L = now;
+                pt_graph_P = pt;
             }
             // the graph starts with swap counter 1 (mod period): align
             while (pt_swap_i % period != 0 && done < swaps) {
@@ -1072,6 +1097,7 @@ struct ldo_engine {
         check_status();
     }
     LdoLaunch pt_graph_L {};
+    LdoPT pt_graph_P {};
 
     // ------------------------------------------------ umbrella sampling ----
     static uint64_t host_philox_word(uint32_t seed, uint32_t key1, uint32_t stream, unsigned long long draw) {
@@ -1813,6 +1839,12 @@ struct ldo_writer {
     int replica {0};
     std::unique_ptr<ldo_out::Writer> w;
     vector<int> op_index;
+    // .swp writer of one ladder (PTGCMCSimulation::initialize_swap_file /
+    // write_swap_entry, src/ptmc_simulation.cpp:91,315)
+    int swp_ladder {-1};
+    long long swp_freq {0};
+    long long swp_read {0};
+    std::ofstream swp;
 };
 
 namespace {
@@ -1899,8 +1931,80 @@ ldo_status ldo_writer_open(ldo_engine* e, int replica, const char* filebase, uin
     });
 }
 
+// .swp of one ladder: the header of PTGCMCSimulation::initialize_swap_file
+// (the exchanged controls of every slot, "v1/v2/ " per slot), then the rows
+// that pt runs record.
+ldo_status ldo_swap_writer_open(ldo_engine* e, int n_rungs, int exchange_q, int ladder, const char* filebase,
+                                int64_t freq, ldo_writer** out) {
+    if (!e || !filebase || !out || n_rungs < 2 || freq <= 0) return LDO_EINVAL;
+    *out = nullptr;
+    return guard(e, [&]() {
+        if (n_rungs != e->pt_rungs || exchange_q != e->pt_q || e->pt_dim2 != 0) {
+            if (e->pt_graph) {
+                cudaGraphExecDestroy(e->pt_graph);
+                e->pt_graph = nullptr;
+            }
+            e->pt_setup(n_rungs, exchange_q, 0);
+        }
+        int nl = e->n_rep / n_rungs;
+        if (ladder < 0 || ladder >= nl) throw LdoError(LDO_EINVAL, "ladder out of range");
+        if (e->hist_cap == 0) e->pt_record_swaps(4096);
+        auto wr = std::make_unique<ldo_writer>();
+        wr->e = e;
+        wr->swp_ladder = ladder;
+        wr->swp_freq = freq;
+        long long n = 0;
+        CU(cudaMemcpy(&n, e->d_hist_n.p + ladder, sizeof(long long), cudaMemcpyDeviceToHost));
+        wr->swp_read = n;
+        string name = string(filebase) + ".swp";
+        wr->swp.open(name);
+        if (!wr->swp.good()) throw LdoError(LDO_EINVAL, name + ": output path does not exist");
+        for (int rep = 0; rep < n_rungs; ++rep) {
+            for (int q = 0; q < 4; ++q)
+                if (exchange_q & (1 << q)) wr->swp << e->pt_slot_q[(size_t)q * n_rungs + rep] << "/";
+            wr->swp << " ";
+        }
+        wr->swp << "\n";
+        wr->swp.flush();
+        *out = wr.release();
+    });
+}
+
+namespace {
+// write_swap_entry rows: the rows recorded since the last call whose step is
+// a multiple of the frequency, then (step >= 0) the current permutation as
+// the end-of-run row at `step`.
+void swap_writer_write(ldo_writer* w, int64_t step) {
+    ldo_engine* e = w->e;
+    int R = e->pt_rungs, nl = e->n_rep / R, lad = w->swp_ladder;
+    if (e->hist_cap == 0) throw LdoError(LDO_EINVAL, "the swap history was dropped (the ladder was set up again)");
+    long long n = 0;
+    CU(cudaMemcpy(&n, e->d_hist_n.p + lad, sizeof(long long), cudaMemcpyDeviceToHost));
+    if (n - w->swp_read > e->hist_cap)
+        throw LdoError(LDO_EINVAL, "swap history overflow: write the .swp file at least every 4096 exchanges");
+    vector<int> row(R);
+    for (long long k = w->swp_read; k < n; ++k) {
+        size_t r = (size_t)(k % e->hist_cap) * nl + lad;
+        long long st = 0;
+        CU(cudaMemcpy(&st, e->d_hist_step.p + r, sizeof(long long), cudaMemcpyDeviceToHost));
+        if (st % w->swp_freq != 0) continue;
+        CU(cudaMemcpy(row.data(), e->d_hist_perm.p + r * R, R * sizeof(int), cudaMemcpyDeviceToHost));
+        for (int q = 0; q < R; ++q) w->swp << row[q] - lad * R << " ";
+        w->swp << "\n";
+    }
+    w->swp_read = n;
+    if (step >= 0 && step % w->swp_freq == 0) {
+        CU(cudaMemcpy(row.data(), e->d_perm.p + (size_t)lad * R, R * sizeof(int), cudaMemcpyDeviceToHost));
+        for (int q = 0; q < R; ++q) w->swp << row[q] - lad * R << " ";
+        w->swp << "\n";
+    }
+    w->swp.flush();
+}
+} // namespace
+
 ldo_status ldo_writer_write(ldo_writer* w, int64_t step) {
     if (!w || !w->e) return LDO_EINVAL;
+    if (w->swp_ladder >= 0) return guard(w->e, [&]() { swap_writer_write(w, step); });
     return guard(w->e, [&]() { w->w->write(step, replica_snapshot(w->e, w->replica, w->op_index)); });
 }
 

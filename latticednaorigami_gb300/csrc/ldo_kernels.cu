@@ -227,6 +227,14 @@ __global__ void ldo_pt_swap_kernel(LdoPT P) {
     int lad = blockIdx.x * blockDim.x + threadIdx.x;
     if (lad >= P.n_ladders) return;
     int* perm = P.perm + (size_t)lad * P.n_rungs;
+    if (P.hist_perm && P.hist_cap > 0) {
+        long long k = P.hist_n[lad];
+        size_t row = (size_t)(k % P.hist_cap) * P.n_ladders + lad;
+        for (int q = 0; q < P.n_rungs; ++q) P.hist_perm[row * P.n_rungs + q] = perm[q];
+        const LdoHdr* h0 = reinterpret_cast<const LdoHdr*>(P.arena + (size_t)perm[0] * P.lay.bytes + P.lay.o_hdr);
+        P.hist_step[row] = h0->steps_done;
+        P.hist_n[lad] = k + 1;
+    }
     ldo::Rng rng;
     rng.init(P.seed, (uint32_t)lad, 1u, P.draws[lad]);
     int set = P.swap_i;

@@ -89,6 +89,14 @@ struct LdoPT {
     const int* pair_a;
     const int* pair_b;
     const int* pair_ctr;
+    // Swap history for the .swp file (PTGCMCSimulation::write_swap_entry,
+    // src/ptmc_simulation.cpp:315): before its exchange attempts each ladder
+    // stores its permutation (slot -> replica) and step count in row
+    // hist_n[ladder] % hist_cap and counts the row (null: not recorded).
+    int* hist_perm;              // [hist_cap][n_ladders][n_rungs]
+    long long* hist_step;        // [hist_cap][n_ladders]
+    long long* hist_n;           // [n_ladders]
+    long long hist_cap;
 };
 cudaError_t ldo_launch_pt_swap(const LdoPT& P, cudaStream_t stream);
 

@@ -3,6 +3,7 @@
 // src/simulation.cpp:47-147), written from a host copy of the replica's
 // state.  Host code only.
 #pragma once
+#include <chrono>
 #include <fstream>
 #include <stdexcept>
 #include <string>
@@ -31,7 +32,8 @@ enum Kind : unsigned {
     VTF = 2,       // .vcf .states .ores
     COUNTS = 4,    // .counts .staples .staplestates
     ENE = 8,       // .ene
-    OPS = 16       // .ops
+    OPS = 16,      // .ops
+    TIMES = 32     // .times (seconds since the writer was opened)
 };
 
 class Writer {
@@ -66,6 +68,12 @@ class Writer {
             m_ene << "step tenergy henthalpy hentropy stacking bias\n";
             m_ene.precision(10);
         }
+        if (kinds & TIMES) {
+            // OrigamiTimesOutputFile (src/files.cpp:723)
+            open(m_times, base + ".times");
+            m_times << "step time\n";
+            m_start = std::chrono::steady_clock::now();
+        }
         if (kinds & OPS) {
             open(m_ops, base + ".ops");
             for (auto& t : op_tags) {
@@ -89,6 +97,13 @@ class Writer {
             m_ene << step << " " << s.energy << " " << s.enthalpy << " " << s.entropy << " " << s.stacking << " "
                   << s.bias << " \n";
             m_ene.flush();
+        }
+        if (m_kinds & TIMES) {   // OrigamiTimesOutputFile::write (src/files.cpp:739)
+            std::chrono::duration<double> dt {std::chrono::steady_clock::now() - m_start};
+            m_times << step << " ";
+            m_times << dt.count();
+            m_times << "\n";
+            m_times.flush();
         }
         if (m_kinds & OPS) {
             m_ops << step;
@@ -202,7 +217,8 @@ class Writer {
 
     unsigned m_kinds;
     int m_max_staple_size, m_max_num_domains;
-    std::ofstream m_trj, m_vcf, m_states, m_ores, m_counts, m_staples, m_staplestates, m_ene, m_ops;
+    std::ofstream m_trj, m_vcf, m_states, m_ores, m_counts, m_staples, m_staplestates, m_ene, m_ops, m_times;
+    std::chrono::steady_clock::time_point m_start;
 };
 
 } // namespace ldo_out

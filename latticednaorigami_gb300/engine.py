@@ -23,7 +23,7 @@ EXPORTS = [
     "ldo_learn_collect", "ldo_learn_reset_counts", "ldo_learn_get_counts", "ldo_learn_train", "ldo_learn_set_params",
     "ldo_learn_get_params", "ldo_learn_get_table", "ldo_learn_set_table", "ldo_learn_loss_grad",
     "ldo_writer_open", "ldo_writer_write", "ldo_writer_close", "ldo_pt2d_run", "ldo_engine_exp",
-    "ldo_set_bias_centre",
+    "ldo_set_bias_centre", "ldo_swap_writer_open",
 ]
 
 LEARN_TABLE = 524288      # network inputs (ldo_learn.h)
@@ -81,6 +81,7 @@ def load_library(path=None):
     lib.ldo_set_grid_bias.argtypes = [vp, ctypes.c_char_p, ip, dp, ip]
     lib.ldo_set_window.argtypes = [vp, ctypes.c_char_p, ip, ip, ip]
     lib.ldo_set_bias_centre.argtypes = [vp, ctypes.c_char_p, ip, ctypes.c_double]
+    lib.ldo_swap_writer_open.argtypes = [vp, ip, ip, ip, ctypes.c_char_p, ctypes.c_int64, ctypes.POINTER(vp)]
     lib.ldo_pt_run.argtypes = [vp, ip, ctypes.c_int64, ip, ip, dp]
     lib.ldo_pt2d_run.argtypes = [vp, ip, ip, ctypes.c_int64, ip, dp]
     lib.ldo_pt_get_permutation.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ip]
@@ -250,10 +251,19 @@ class Engine:
         self._check(self.lib.ldo_us_get_biases(self.h, _dptr(out), self.n, gl))
         return out
 
+    def open_swap_writer(self, n_rungs, exchange_q, ladder, filebase, freq):
+        """The .swp file of one parallel-tempering ladder (ldo_swap_writer_open);
+        Writer.write(step) appends the rows recorded by pt_run (step >= 0 adds
+        the end-of-run row)."""
+        w = ctypes.c_void_p()
+        self._check(self.lib.ldo_swap_writer_open(self.h, n_rungs, exchange_q, ladder, os.fsencode(filebase),
+                                                  int(freq), ctypes.byref(w)))
+        return Writer(self, w)
+
     def open_writer(self, replica, filebase, kinds=31):
         """Output files of one replica in the reference's formats
         (1 .trj, 2 .vcf/.states/.ores, 4 .counts/.staples/.staplestates,
-        8 .ene, 16 .ops); returns a Writer."""
+        8 .ene, 16 .ops, 32 .times); returns a Writer."""
         w = ctypes.c_void_p()
         self._check(self.lib.ldo_writer_open(self.h, replica, os.fsencode(filebase), kinds, ctypes.byref(w)))
         return Writer(self, w)
