@@ -9,6 +9,7 @@
 //
 // Extra keys: trace_steps, trace_seed, trace_replica, trace_every,
 //             trace_mode (simulate | enumerate)
+#include <chrono>
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -192,8 +193,11 @@ class TraceSim : public simulation::GCMCSimulation {
     void run() override {}
     bool m_first {true};
 
+    bool m_quiet {false};
+
   protected:
     void update_internal(long long int step) override {
+        if (m_quiet) return;
         auto& o = m_origami_system;
         char buf[512];
         std::snprintf(buf, sizeof buf, "%s[%lld,%.17g,%d,%d,%d,%d,%.17g,%llu]",
@@ -249,11 +253,15 @@ int main(int argc, char** argv) {
         std::snprintf(buf, sizeof buf, ", \"initial_energy\": %.17g, \"steps\": [", o->energy());
         std::cout << buf;
         TraceSim sim(*o, ops, biases, params, every, std::cout);
+        // trace_quiet=1: no per-step records (for timing the move loop)
+        sim.m_quiet = kv.count("trace_quiet") && kv["trace_quiet"] == "1";
+        auto t0 = std::chrono::steady_clock::now();
         sim.simulate(steps, 0, false);
+        double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         std::cout << "], \"dumps\": [";
         for (size_t i = 0; i < sim.m_dumps.size(); ++i) std::cout << (i ? "," : "") << sim.m_dumps[i];
-        std::snprintf(buf, sizeof buf, "], \"final_energy\": %.17g, \"draws\": %llu}\n", o->energy(),
-                      (unsigned long long)ldo_ref_rng_draws());
+        std::snprintf(buf, sizeof buf, "], \"final_energy\": %.17g, \"draws\": %llu, \"seconds\": %.6f}\n",
+                      o->energy(), (unsigned long long)ldo_ref_rng_draws(), secs);
         std::cout << buf;
         delete o;
     } catch (std::exception& e) {
