@@ -16,6 +16,10 @@ fully bound domains (one sample per replica per sweep, tau_int by Sokal
 windowing) of the learned moveset, from the device-timed region; `plain`
 holds the same figures for the plain moveset; `e2e` repeats the timed loop
 through the C ABI with host buffers (temperatures in, samples out every step).
+
+Under torchrun (N > 1) every rank runs the same per-GPU workload on its own
+GPU with its own seed (replicas only); value = effective samples of all ranks
+/ the slowest rank's time.
 """
 import argparse
 import json
@@ -105,6 +109,52 @@ class ClockSampler:
                     reasons.add(nme)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+class Ranks:
+    """One process per GPU under torchrun (replicas only: no data-path
+    collective).  Each rank takes the GPU of its LOCAL_RANK (through
+    CUDA_VISIBLE_DEVICES, set before the engine library initialises CUDA),
+    runs the whole per-GPU workload with its own Philox seed, and meets the
+    others in a host-side (gloo) group only for the barriers around the timed
+    region and the reductions of its results: work is summed, time is the
+    maximum over ranks."""
+
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = None
+        if self.world > 1:
+            vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+            devs = [v for v in vis.split(",") if v] if vis else [str(i) for i in range(self.world)]
+            os.environ["CUDA_VISIBLE_DEVICES"] = devs[self.local % len(devs)]
+            import torch.distributed as dist
+            if not dist.is_initialized():
+                dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def _reduce(self, x, op):
+        if not self.dist:
+            return float(x)
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=op)
+        return float(t.item())
+
+    def max(self, x):
+        return self._reduce(x, self.dist.ReduceOp.MAX if self.dist else None)
+
+    def sum(self, x):
+        return self._reduce(x, self.dist.ReduceOp.SUM if self.dist else None)
+
+    def close(self):
+        if self.dist and self.dist.is_initialized():
+            self.dist.destroy_process_group()
 
 
 def measured_peaks():
@@ -360,6 +410,7 @@ def main():
         C4_SWEEPS_PER_STEP = args.sweeps_per_step
     rank = int(os.environ.get("RANK", "0"))
     if args.workload == "c4":
+        # single-GPU workload (384 replicas): other ranks have nothing to do
         if rank == 0:
             run_c4(args, args.impl)
         return
@@ -367,6 +418,7 @@ def main():
         if rank == 0:
             run_reference_arm(args)
         return
+    ranks = Ranks()
     from latticednaorigami_gb300 import Engine
     from latticednaorigami_gb300.analysis import effective_samples, tau_int
 
@@ -382,7 +434,7 @@ def main():
     def timed_arm(overrides, table, collect):
         """W warm-up launches, then K timed launches of SWEEPS_PER_STEP sweeps
         with one numfulldomains sample per replica per sweep."""
-        eng = Engine(files, n_replicas=N_REP, seed=0, sys_of_replica=sys_of.tolist(), overrides=overrides)
+        eng = Engine(files, n_replicas=N_REP, seed=ranks.rank, sys_of_replica=sys_of.tolist(), overrides=overrides)
         eng.set_controls(temps=temps)
         if table is not None:
             eng.learn_set_table(table)
@@ -392,12 +444,15 @@ def main():
         eng.set_sampling(1, total_sweeps)
         clocks = ClockSampler()
         clocks.start()
-        dev_ms = [eng.run_sweeps(SWEEPS_PER_STEP) for _ in range(args.steps)]
+        ranks.barrier()
+        dev_ms = [eng.run_sweeps(SWEEPS_PER_STEP) for _ in range(args.steps)]   # each call ends synchronised
+        ranks.barrier()
         clk = clocks.stop()
-        t_dev = sum(dev_ms) / 1000.0
+        t_dev = ranks.max(sum(dev_ms) / 1000.0)
         smp, cnt = eng.samples()
         series = [smp[r, :cnt[r], 0] for r in range(N_REP)]
         ess, tau_med = effective_samples(series)
+        ess = ranks.sum(ess)
         taus = {}
         for i, n in enumerate(SIZES):
             ts = [tau_int(series[r]) for r in range(i * per, (i + 1) * per)]
@@ -421,7 +476,8 @@ def main():
     def e2e_arm(overrides, table):
         """The same loop through the C ABI with host buffers: temperatures in,
         samples out, every step."""
-        eng2 = Engine(files, n_replicas=N_REP, seed=1, sys_of_replica=sys_of.tolist(), overrides=overrides)
+        eng2 = Engine(files, n_replicas=N_REP, seed=1000 + ranks.rank, sys_of_replica=sys_of.tolist(),
+                      overrides=overrides)
         eng2.set_controls(temps=temps)
         if table is not None:
             eng2.learn_set_table(table)
@@ -429,6 +485,7 @@ def main():
         for _ in range(args.warmup):
             eng2.run_sweeps(SWEEPS_PER_STEP)
         e2e_series = [[] for _ in range(N_REP)]
+        ranks.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             eng2.set_controls(temps=temps)
@@ -438,8 +495,10 @@ def main():
             for r in range(N_REP):
                 e2e_series[r].append(s2[r, :c2[r], 0])
         t_e2e = time.perf_counter() - t0
+        ranks.barrier()
+        t_e2e = ranks.max(t_e2e)
         e2e_ess, _ = effective_samples([np.concatenate(x) for x in e2e_series])
-        return e2e_ess / t_e2e
+        return ranks.sum(e2e_ess) / t_e2e
 
     plain = timed_arm("", None, collect=True)
     table = plain["train"]["table"]
@@ -474,21 +533,23 @@ def main():
 
     def rates(arm):
         t = arm["t_dev"]
-        return {"value": arm["ess"] / t, "sweeps_per_s": N_REP * total_sweeps / t,
-                "move_attempts_per_s": float(np.sum(ns_of)) * total_sweeps / t,
+        W = ranks.world
+        return {"value": arm["ess"] / t, "sweeps_per_s": W * N_REP * total_sweeps / t,
+                "move_attempts_per_s": W * float(np.sum(ns_of)) * total_sweeps / t,
                 "ms_per_step": float(np.mean(arm["dev_ms"])), "tau_int_median": arm["tau_med"],
                 "tau_int_by_size": arm["taus"]}
 
     tr = plain["train"]
     line = {"metric": "effective samples/s (tau_int of #bound domains), learned vs plain MC", "value": value,
-            "unit": "effective samples/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "unit": "effective samples/s", "n_gpus": ranks.world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": float(np.mean(dev_ms)), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "c2: 4096 constant-T chains, scaffolds 8/12/16/24 (1024 each), uniform hyb "
                                    "dH=-120 kcal/mol dS=-0.33 kcal/mol/K, T~U[320,350] K, 1 uM; moveset "
                                    "learned staple exchange + Met regrowth + CB regrowth (value) vs Met "
                                    "exchange + Met regrowth + CB regrowth (plain)",
-                       "sweeps_per_step": SWEEPS_PER_STEP, "replicas": N_REP,
+                       "sweeps_per_step": SWEEPS_PER_STEP, "replicas": N_REP * ranks.world,
+                       "replicas_per_gpu": N_REP, "parallelism": "replicas only, one process per GPU",
                        "l2": "state resident in shared memory; no L2 flush needed"},
             "learned": rates(learned), "plain": rates(plain),
             "learned_over_plain": value / plain_value,
@@ -505,7 +566,9 @@ def main():
             "clocks": learned["clk"], "clocks_plain": plain["clk"]}
     if not args.no_cpu and rank == 0:
         line["cpu_baseline"] = cpu_baseline(files, args.warmup * SWEEPS_PER_STEP, total_sweeps)
-    print(json.dumps(line))
+    if rank == 0:
+        print(json.dumps(line))
+    ranks.close()
 
 
 if __name__ == "__main__":
