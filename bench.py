@@ -6,8 +6,9 @@ layout, n/2 two-domain staple types), uniform hybridisation dH = -120 kcal/mol
 and dS = -0.33 kcal/mol/K per bound domain, T ~ U[320, 350] K (seeded),
 1 uM staples, FourBody, Opposing misbinding, constant stacking 1000 K.  Plain
 moveset: Met exchange / Met regrowth / CB regrowth at 1/3 each; learned
-moveset: the exchange replaced by LearnedStapleExchange, whose network is
-trained (on the GPU) on states of the plain run.  Philox seeds: replica r uses
+moveset: the exchange and the Met regrowth replaced by LearnedStapleExchange
+and LearnedStapleRegrowth, whose network is trained (on the GPU) on states of
+the plain run.  Philox seeds: replica r uses
 key (0, r).  Inputs are synthetic (tests/systems.py).
 
 A step is one launch of SWEEPS sweeps of every replica (a sweep = n_scaffold
@@ -172,13 +173,14 @@ LEARN_LR = 2e-3
 
 
 def write_learned_moves(d):
-    """The c2 moveset with the staple exchange replaced by the learned one."""
+    """The c2 moveset with the staple exchange and the Met regrowth replaced
+    by the learned ones (insertion sites; regrowth directions)."""
     p = os.path.join(d, "moves_learned.json")
     with open(p, "w") as f:
         json.dump({"origami": {"movetypes": [
             {"label": "Learned staple exchange", "type": "LearnedStapleExchange", "freq": "1/3",
              "adaptive_exchange": False},
-            {"label": "Met staple regrowth", "type": "MetStapleRegrowth", "freq": "1/3"},
+            {"label": "Learned staple regrowth", "type": "LearnedStapleRegrowth", "freq": "1/3"},
             {"label": "CB staple regrowth", "type": "CBStapleRegrowth", "freq": "1/3"}]}}, f)
     return p
 
@@ -470,8 +472,10 @@ def main():
             loss0, loss1 = eng.learn_train(LEARN_ITERS, lr=LEARN_LR, seed=0)
             train = {"loss_first": loss0, "loss_last": loss1, "iters": LEARN_ITERS,
                      "train_s": time.perf_counter() - t0, "table": eng.learn_table()}
+        st = eng.move_stats(3)
+        acc = [float(st[k, 1]) / max(1.0, float(st[k, 0])) for k in range(3)]
         return {"eng": eng, "dev_ms": dev_ms, "t_dev": t_dev, "ess": ess, "tau_med": tau_med, "taus": taus,
-                "clk": clk, "hists": hists, "train": train}
+                "clk": clk, "hists": hists, "train": train, "acc": acc}
 
     def e2e_arm(overrides, table):
         """The same loop through the C ABI with host buffers: temperatures in,
@@ -537,7 +541,8 @@ def main():
         return {"value": arm["ess"] / t, "sweeps_per_s": W * N_REP * total_sweeps / t,
                 "move_attempts_per_s": W * float(np.sum(ns_of)) * total_sweeps / t,
                 "ms_per_step": float(np.mean(arm["dev_ms"])), "tau_int_median": arm["tau_med"],
-                "tau_int_by_size": arm["taus"]}
+                "tau_int_by_size": arm["taus"],
+                "acceptance": {"exchange": arm["acc"][0], "regrowth": arm["acc"][1], "cb_regrowth": arm["acc"][2]}}
 
     tr = plain["train"]
     line = {"metric": "effective samples/s (tau_int of #bound domains), learned vs plain MC", "value": value,
@@ -546,7 +551,7 @@ def main():
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "c2: 4096 constant-T chains, scaffolds 8/12/16/24 (1024 each), uniform hyb "
                                    "dH=-120 kcal/mol dS=-0.33 kcal/mol/K, T~U[320,350] K, 1 uM; moveset "
-                                   "learned staple exchange + Met regrowth + CB regrowth (value) vs Met "
+                                   "learned staple exchange + learned regrowth + CB regrowth (value) vs Met "
                                    "exchange + Met regrowth + CB regrowth (plain)",
                        "sweeps_per_step": SWEEPS_PER_STEP, "replicas": N_REP * ranks.world,
                        "replicas_per_gpu": N_REP, "parallelism": "replicas only, one process per GPU",

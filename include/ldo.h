@@ -218,7 +218,8 @@ ldo_status ldo_engine_exp(const double* x, double* y, int n);
  * (per network input). */
 ldo_status ldo_learn_collect(ldo_engine* e);
 ldo_status ldo_learn_reset_counts(ldo_engine* e);
-/* Training counts per network input (n = LDO_LEARN_TABLE = 524288). */
+/* Training counts per network input (n = LDO_LEARN_TABLE = 524544: 524288
+ * insertion inputs, then 256 regrowth-direction inputs, ldo_learn.h). */
 ldo_status ldo_learn_get_counts(ldo_engine* e, float* cnt_bound, float* cnt_total, int n);
 /* Full-batch Adam (lr) on the weighted logistic loss of the counts, starting
  * from seeded parameters the first time; then the proposal's weight table.
@@ -228,7 +229,7 @@ ldo_status ldo_learn_train(ldo_engine* e, int iters, double lr, uint32_t seed, d
  * recomputes the weight table. */
 ldo_status ldo_learn_set_params(ldo_engine* e, const float* params, int n);
 ldo_status ldo_learn_get_params(ldo_engine* e, float* params, int n);
-/* Proposal weight exp(clamped logit) of every network input (n = 524288). */
+/* Proposal weight exp(clamped logit) of every network input (n = 524544). */
 ldo_status ldo_learn_get_table(ldo_engine* e, double* weights, int n);
 ldo_status ldo_learn_set_table(ldo_engine* e, const double* weights, int n);
 /* Loss and gradient of the network for given parameters on a batch of n

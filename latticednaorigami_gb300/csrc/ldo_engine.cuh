@@ -1800,6 +1800,101 @@ struct Rep : public LdoState<C> {
                 if (s == BOUND) atomicAdd(cnt_b + k, 1.f);
             }
         }
+        // regrowth directions: for every placed staple domain next to a
+        // placed chain neighbour, the six sites next to that neighbour as
+        // they would be without the domain, labelled by where it is
+        #pragma unroll 1
+        for (int c = 1; c < nc; ++c) {
+            int cs = chain_order[c];
+            int len = chain_len(cs);
+            #pragma unroll 1
+            for (int d = 0; d < len; ++d) {
+                int i = slot_of(cs, d);
+                if (st[i] == UNASSIGNED) continue;
+                #pragma unroll 1
+                for (int side = 0; side < 2; ++side) {
+                    int prev = side == 0 ? bwd(i) : fwd(i);
+                    if (prev < 0 || st[prev] == UNASSIGNED) continue;
+                    int vstar = unit_index(sub(pos(i), pos(prev)));
+                    #pragma unroll 1
+                    for (int v = 0; v < 6; ++v) {
+                        int f;
+                        if (v == vstar) {
+                            int j = bnd[i];
+                            f = (st[i] == UNBOUND || j < 0) ? 0 : (did[i] == -did[j] ? 1 : 2);
+                        }
+                        else {
+                            f = lr_site_class(i, add(pos(prev), unit(v)), nullptr);
+                        }
+                        int k = ldo_learn_dir_index(learn_tb, f);
+                        atomicAdd(cnt_t + k, 1.f);
+                        if (v == vstar) atomicAdd(cnt_b + k, 1.f);
+                    }
+                }
+            }
+        }
+    }
+    // Class of site p for growing domain i: 0 empty, 1 an unbound domain
+    // complementary to i, 2 another unbound domain, 3 a bound pair; *ob (if
+    // given) the orientation that binds to the unbound domain, else -1.
+    __device__ int lr_site_class(int i, V3 p, int* ob) const {
+        int occ = occupancy(p);
+        if (ob) *ob = -1;
+        if (occ == UNASSIGNED) return 0;
+        if (occ == UNBOUND) {
+            int j = unbound_at(p);
+            if (ob) *ob = ore[j] ^ 1;
+            return did[i] == -did[j] ? 1 : 2;
+        }
+        return 3;
+    }
+    // The learned direction and orientation proposal of domain i grown from
+    // its placed chain neighbour prev: q(v) = eps_d/6 + (1 - eps_d) w(v)/Z over
+    // the six sites, then q(o | v) = eps_o/6 + (1 - eps_o)[o binds] at a site
+    // with an unbound domain, 1/6 elsewhere.  With sample set it draws (v, o)
+    // (one uniform real for v, then at an unbound site one for the binding
+    // choice and, if not taken, a uniform orientation); it returns q(v) q(o|v)
+    // of (*v, *o).
+    __device__ __noinline__ double lr_propose(int i, int prev, bool sample, int* vo, int* oo) {
+        double w[6];
+        int ob[6];
+        double z = 0;
+        V3 base = pos(prev);
+        #pragma unroll 1
+        for (int v = 0; v < 6; ++v) {
+            int f = lr_site_class(i, add(base, unit(v)), &ob[v]);
+            w[v] = __ldg(learn_w + ldo_learn_dir_index(learn_tb, f));
+            z += w[v];
+        }
+        int v = *vo;
+        if (sample) {
+            double r = rng.uniform_real();
+            double cum = 0;
+            v = 5;
+            #pragma unroll 1
+            for (int k = 0; k < 6; ++k) {
+                cum += z > 0 ? LDO_LEARN_EPS_D / 6.0 + (1.0 - LDO_LEARN_EPS_D) * (w[k] / z) : 1.0 / 6.0;
+                if (r < cum) {
+                    v = k;
+                    break;
+                }
+            }
+            int o;
+            if (ob[v] >= 0) {
+                double r2 = rng.uniform_real();
+                o = r2 < 1.0 - LDO_LEARN_EPS_O ? ob[v] : rng.uniform_int(0, 5);
+            }
+            else {
+                o = rng.uniform_int(0, 5);
+            }
+            *vo = v;
+            *oo = o;
+        }
+        double qv = z > 0 ? LDO_LEARN_EPS_D / 6.0 + (1.0 - LDO_LEARN_EPS_D) * (w[v] / z) : 1.0 / 6.0;
+        double qo = ob[v] >= 0 ? (*oo == ob[v] ? (1.0 - LDO_LEARN_EPS_O) + LDO_LEARN_EPS_O / 6.0
+                                               : LDO_LEARN_EPS_O / 6.0)
+                               : 1.0 / 6.0;
+        return qv * qo;
     }
     // Z over the unbound scaffold domains, in scaffold order.
     __device__ __noinline__ double learn_z() const {
@@ -1983,6 +2078,128 @@ struct Rep : public LdoState<C> {
     __device__ __noinline__ int pick_staple_chain() {   // uniform_int(1, num_staples) -> get_chains()[i]
         int ci = rng.uniform_int(1, hdr.num_staples);
         return chain_order[ci];
+    }
+
+    // LearnedStapleRegrowth (engine extension): MetStapleRegrowthMCMovetype
+    // (src/met_movetypes.cpp:470) whose grown domains take direction and
+    // orientation from the learned proposal (lr_propose).  The reverse move
+    // picks the same growth point among the new configuration's bound pairs
+    // and grows the old configuration, so the acceptance is the reference's
+    // e^-dE n_bd,old / n_bd,new times Q(old) / Q(new), the products of the
+    // proposal probabilities along each growth.
+
+    // Class of site p in a partial growth of staple cs from the state before
+    // the move: the staple's domains in `placed` (bit = index in chain) are
+    // where they are, the others absent (a partner left behind is unbound).
+    __device__ int lr_site_class_partial(int i, V3 p, int cs, unsigned placed, int* ob) const {
+        int len = chain_len(cs);
+        #pragma unroll 1
+        for (int k = 0; k < len; ++k) {
+            int x = slot_of(cs, k);
+            if (st[x] == UNASSIGNED || pos(x) != p) continue;
+            int y = bnd[x];
+            bool y_gone = y >= 0 && scs[y] == cs && !(placed >> sd[y] & 1u);
+            int alone;   // the domain left alone at p, or -1 for an empty site
+            if (placed >> k & 1u) {
+                if (st[x] != UNBOUND && !y_gone) {
+                    *ob = -1;
+                    return 3;
+                }
+                alone = x;
+            }
+            else {
+                alone = (st[x] == UNBOUND || y_gone) ? -1 : y;
+            }
+            if (alone < 0) {
+                *ob = -1;
+                return 0;
+            }
+            *ob = ore[alone] ^ 1;
+            return did[i] == -did[alone] ? 1 : 2;
+        }
+        return lr_site_class(i, p, ob);
+    }
+    // Q(old): the proposal probability of growing the current configuration
+    // of staple cs from its domain d0, evaluated in the partial states of
+    // that growth without building them.
+    __device__ __noinline__ double lr_q_old(int cs, int d0) {
+        int len = chain_len(cs);
+        unsigned placed = 1u << d0;
+        double q = 1;
+        #pragma unroll 1
+        for (int pass = 0; pass < 2; ++pass) {
+            int dir = pass == 0 ? 1 : -1;
+            int n = pass == 0 ? len - d0 : d0 + 1;
+            #pragma unroll 1
+            for (int k = 1; k < n; ++k) {
+                int di = d0 + dir * k;
+                int i = slot_of(cs, di), prev = slot_of(cs, di - dir);
+                double w[6];
+                int ob[6];
+                double z = 0;
+                V3 base = pos(prev);
+                #pragma unroll 1
+                for (int v = 0; v < 6; ++v) {
+                    int f = lr_site_class_partial(i, add(base, unit(v)), cs, placed, &ob[v]);
+                    w[v] = __ldg(learn_w + ldo_learn_dir_index(learn_tb, f));
+                    z += w[v];
+                }
+                int v = unit_index(sub(pos(i), base));
+                int o = ore[i];
+                if (v < 0) {
+                    fail(LDO_RS_INVARIANT);
+                    return 1;
+                }
+                double qv = z > 0 ? LDO_LEARN_EPS_D / 6.0 + (1.0 - LDO_LEARN_EPS_D) * (w[v] / z) : 1.0 / 6.0;
+                double qo = ob[v] >= 0 ? (o == ob[v] ? (1.0 - LDO_LEARN_EPS_O) + LDO_LEARN_EPS_O / 6.0
+                                                     : LDO_LEARN_EPS_O / 6.0)
+                                       : 1.0 / 6.0;
+                q *= qv * qo;
+                placed |= 1u << di;
+            }
+        }
+        return q;
+    }
+    __device__ __noinline__ bool learned_regrowth() {
+        dirty = false;
+        if (hdr.num_staples == 0) return false;
+        int cs = pick_staple_chain();
+        if (staple_is_connector(cs)) return false;
+        dirty = true;
+        find_bound_domains(cs);
+        if (bad()) return false;
+        int g = rng.uniform_int(0, m.n_bd - 1);
+        int gnew = m.bd_new[g], gold = m.bd_old[g];
+        int d0 = sd[gnew];
+        double q_old = lr_q_old(cs, d0);
+        unassign_domains(cs);
+        delta_e += set_growth_point(gnew, gold);
+        if (rejected || bad()) return false;
+        double q_new = 1;
+        int len = chain_len(cs);
+        #pragma unroll 1
+        for (int pass = 0; pass < 2; ++pass) {
+            int dir = pass == 0 ? 1 : -1;
+            int n = pass == 0 ? len - d0 : d0 + 1;
+            #pragma unroll 1
+            for (int k = 1; k < n; ++k) {
+                int i = slot_of(cs, d0 + dir * k), prev = slot_of(cs, d0 + dir * (k - 1));
+                int v = 0, o = 0;
+                q_new *= lr_propose(i, prev, true, &v, &o);
+                delta_e += set_domain_config(i, add(pos(prev), unit(v)), o);
+                if (hdr.violated) {
+                    rejected = true;
+                    return false;
+                }
+                if (bad()) return false;
+            }
+        }
+        add_external_bias_met();
+        int nbd = num_bound_staple_domains(cs);
+        double boltz = dexp(-(delta_e));
+        double pratio = boltz * (double)(unsigned long long)m.n_bd / nbd;
+        pratio *= q_old / q_new;
+        return test_acceptance(pratio);
     }
 
     // MetStapleRegrowthMCMovetype::internal_attempt_move (src/met_movetypes.cpp:470)
@@ -3597,7 +3814,7 @@ struct Rep : public LdoState<C> {
         cur_mv = mv;
         reset_internal();
         int kind = sys->move_kind[mv];
-        if (kind >= LDO_MV_CTRG) {   // scaffold regrowth
+        if (kind >= LDO_MV_CTRG && kind <= LDO_MV_CTCB_JUMP) {   // scaffold regrowth
             if constexpr (CT) {
                 if (ct) return kind <= LDO_MV_CTRG_JUMP ? rg_begin(kind) : ctcb_begin(kind);
             }
@@ -3610,6 +3827,7 @@ struct Rep : public LdoState<C> {
         case LDO_MV_MET_EXCHANGE: acc = met_exchange(); break;
         case LDO_MV_MET_REGROWTH: acc = met_regrowth(); break;
         case LDO_MV_LEARNED_EXCHANGE: acc = learned_exchange(); break;
+        case LDO_MV_LEARNED_REGROWTH: acc = learned_regrowth(); break;
         case LDO_MV_CB_REGROWTH: return cb_begin();
         }
         return finish_move(acc, 0);

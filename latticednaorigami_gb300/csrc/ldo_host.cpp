@@ -68,6 +68,7 @@ int move_kind(const string& t) {
     if (t == "MetStapleRegrowth") return LDO_MV_MET_REGROWTH;
     if (t == "CBStapleRegrowth") return LDO_MV_CB_REGROWTH;
     if (t == "LearnedStapleExchange") return LDO_MV_LEARNED_EXCHANGE;
+    if (t == "LearnedStapleRegrowth") return LDO_MV_LEARNED_REGROWTH;
     if (t == "CTRGScaffoldRegrowth") return LDO_MV_CTRG;
     if (t == "CTRGJumpScaffoldRegrowth") return LDO_MV_CTRG_JUMP;
     if (t == "CTCBScaffoldRegrowth") return LDO_MV_CTCB;

@@ -1,15 +1,19 @@
-// Learned staple-insertion proposal: feature encoding and network shape,
-// shared by the MC kernel, the network kernels, the host library and the
-// oracle.
+// Learned proposals: feature encoding and network shape, shared by the MC
+// kernel, the network kernels, the host library and the oracle.
 //
-// The proposal scores a candidate growth-point domain g from its local
-// neighbourhood along its chain: the states of the domains two and one step
-// before and after g (none / unbound / bound / misbound), the type slot of
-// the staple complementary to g, and the temperature bin.  The network maps
-// that input to a logit; exp(logit) weighs g among the unbound domains.  The
-// input space is finite (LDO_LEARN_TABLE entries), so the network is
+// Insertion: the network scores a candidate growth-point domain g from its
+// local neighbourhood along its chain: the states of the domains two and one
+// step before and after g (none / unbound / bound / misbound), the type slot
+// of the staple complementary to g, and the temperature bin; exp(logit)
+// weighs g among the unbound domains (LDO_LEARN_INS entries).
+// Regrowth directions: the same network, with a task flag in its input,
+// scores the six lattice sites next to a growing staple domain's chain
+// neighbour by what the site holds (empty / an unbound domain complementary
+// to the growing one / another unbound domain / a bound pair) and the
+// temperature bin (LDO_LEARN_DIRS entries after the insertion entries).
+// The input space is finite (LDO_LEARN_TABLE entries), so the network is
 // evaluated once for every input on the tensor cores and the MC kernel reads
-// the weights from that table: the proposal is an exact function of the
+// the weights from that table: the proposals are exact functions of the
 // current state, as the Metropolis-Hastings ratio requires.
 #pragma once
 #include <math.h>
@@ -26,7 +30,10 @@ enum {
     LDO_LEARN_NTYPE = 32,     // type slots: 0 = no complementary staple
     LDO_LEARN_NTB = 64,       // temperature bins of 1 K from 300 K
     LDO_LEARN_NCOMBO = 256,   // 4 neighbour states x 4 positions
-    LDO_LEARN_TABLE = LDO_LEARN_NTB * LDO_LEARN_NTYPE * LDO_LEARN_NCOMBO,
+    LDO_LEARN_NDIRF = 4,      // regrowth site classes
+    LDO_LEARN_INS = LDO_LEARN_NTB * LDO_LEARN_NTYPE * LDO_LEARN_NCOMBO,
+    LDO_LEARN_DIRS = LDO_LEARN_NTB * LDO_LEARN_NDIRF,
+    LDO_LEARN_TABLE = LDO_LEARN_INS + LDO_LEARN_DIRS,
     // parameter vector: W1[64][256] b1[256] W2[256][256] b2 W3[256][256] b3 w4[256] b4
     LDO_LEARN_OFF_W1 = 0,
     LDO_LEARN_OFF_B1 = LDO_LEARN_OFF_W1 + LDO_LEARN_DIN * LDO_LEARN_H,
@@ -45,6 +52,12 @@ enum {
 // possible.
 #define LDO_LEARN_EPS 0.05
 #define LDO_LEARN_EPS_T 0.05
+// Regrowth: with probability LDO_LEARN_EPS_D the direction is uniform over
+// the six sites, with LDO_LEARN_EPS_O the orientation at a site holding an
+// unbound domain is uniform (otherwise the one opposite to that domain's);
+// every configuration the reference's uniform regrowth makes stays possible.
+#define LDO_LEARN_EPS_D 0.05
+#define LDO_LEARN_EPS_O 0.05
 #define LDO_LEARN_LOGIT_CLAMP 30.0f
 
 LDO_LHD inline int ldo_learn_tbin(double temp) {
@@ -54,14 +67,27 @@ LDO_LHD inline int ldo_learn_tbin(double temp) {
 LDO_LHD inline int ldo_learn_index(int tbin, int tslot, int combo) {
     return (tbin * LDO_LEARN_NTYPE + tslot) * LDO_LEARN_NCOMBO + combo;
 }
+// Regrowth site class f (0 empty, 1 unbound complementary, 2 unbound other,
+// 3 bound or misbound) at temperature bin tbin.
+LDO_LHD inline int ldo_learn_dir_index(int tbin, int f) { return LDO_LEARN_INS + tbin * LDO_LEARN_NDIRF + f; }
 // Type slot of staple type t (1..S) in the one-hot (types above 31 share slots).
 LDO_LHD inline int ldo_learn_tslot(int t) { return t <= 0 ? 0 : 1 + (t - 1) % (LDO_LEARN_NTYPE - 1); }
 // Input vector of table entry k (written as floats; the kernels round to bf16):
-// [0,16) one-hot neighbour states (position-major: two before, one before,
-// one after, two after), [16,48) type-slot one-hot, [48] (T - 335 K) / 15 K,
-// [49] 1, the rest 0.
+// insertion entries: [0,16) one-hot neighbour states (position-major: two
+// before, one before, one after, two after), [16,48) type-slot one-hot,
+// [48] (T - 335 K) / 15 K, [49] 1, the rest 0; regrowth entries: [0,4)
+// one-hot site class, [48] and [49] as above, [50] 1 (the task flag).
 LDO_LHD inline void ldo_learn_input(int k, float* x) {
     for (int i = 0; i < LDO_LEARN_DIN; ++i) x[i] = 0.f;
+    if (k >= LDO_LEARN_INS) {
+        int kk = k - LDO_LEARN_INS;
+        int tb = kk / LDO_LEARN_NDIRF;
+        x[kk % LDO_LEARN_NDIRF] = 1.f;
+        x[48] = (float)(tb - 35) / 15.f;
+        x[49] = 1.f;
+        x[50] = 1.f;
+        return;
+    }
     int combo = k % LDO_LEARN_NCOMBO;
     int tslot = (k / LDO_LEARN_NCOMBO) % LDO_LEARN_NTYPE;
     int tbin = k / (LDO_LEARN_NCOMBO * LDO_LEARN_NTYPE);

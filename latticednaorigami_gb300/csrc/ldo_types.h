@@ -33,7 +33,8 @@ enum LdoMove {
     LDO_MV_CTRG = 5,              // CTRGScaffoldRegrowth
     LDO_MV_CTRG_JUMP = 6,         // CTRGJumpScaffoldRegrowth
     LDO_MV_CTCB = 7,              // CTCBScaffoldRegrowth
-    LDO_MV_CTCB_JUMP = 8          // CTCBJumpScaffoldRegrowth
+    LDO_MV_CTCB_JUMP = 8,         // CTCBJumpScaffoldRegrowth
+    LDO_MV_LEARNED_REGROWTH = 9   // engine extension: Met regrowth with learned directions
 };
 enum LdoMoveOpt { LDO_MO_MAX_REGROWTH = 0, LDO_MO_MAX_SEG_REGROWTH, LDO_MO_MAX_RECOILS, LDO_MO_MAX_C_ATTEMPTS };
 

@@ -26,7 +26,7 @@ EXPORTS = [
     "ldo_set_bias_centre", "ldo_swap_writer_open",
 ]
 
-LEARN_TABLE = 524288      # network inputs (ldo_learn.h)
+LEARN_TABLE = 524544      # network inputs: 524288 insertion + 256 regrowth-direction (ldo_learn.h)
 LEARN_NPARAM = 148481     # network parameters
 
 

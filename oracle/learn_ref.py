@@ -12,8 +12,9 @@ import numpy as np
 from scipy.special import erf
 
 DIN, H = 64, 256
-NTYPE, NTB, NCOMBO = 32, 64, 256
-TABLE = NTB * NTYPE * NCOMBO
+NTYPE, NTB, NCOMBO, NDIRF = 32, 64, 256, 4
+INS = NTB * NTYPE * NCOMBO
+TABLE = INS + NTB * NDIRF   # insertion entries, then regrowth-direction entries
 OFF_W1 = 0
 OFF_B1 = OFF_W1 + DIN * H
 OFF_W2 = OFF_B1 + H
@@ -41,18 +42,26 @@ def tslot(t):
 
 
 def inputs(idx):
-    """Input rows (float32) of table entries idx."""
+    """Input rows (float32) of table entries idx (ldo_learn_input)."""
     idx = np.asarray(idx, np.int64)
     x = np.zeros((len(idx), DIN), np.float32)
-    combo = idx % NCOMBO
-    ts = (idx // NCOMBO) % NTYPE
-    tb = idx // (NCOMBO * NTYPE)
-    r = np.arange(len(idx))
+    ins = idx < INS
+    r = np.arange(len(idx))[ins]
+    k = idx[ins]
+    combo = k % NCOMBO
+    ts = (k // NCOMBO) % NTYPE
+    tb = k // (NCOMBO * NTYPE)
     for o in range(4):
         x[r, 4 * o + ((combo >> (2 * o)) & 3)] = 1.0
     x[r, 16 + ts] = 1.0
-    x[:, 48] = ((tb - 35) / np.float32(15.0)).astype(np.float32)
-    x[:, 49] = 1.0
+    x[r, 48] = ((tb - 35) / np.float32(15.0)).astype(np.float32)
+    x[r, 49] = 1.0
+    r = np.arange(len(idx))[~ins]
+    kk = idx[~ins] - INS
+    x[r, kk % NDIRF] = 1.0
+    x[r, 48] = (((kk // NDIRF) - 35) / np.float32(15.0)).astype(np.float32)
+    x[r, 49] = 1.0
+    x[r, 50] = 1.0
     return x
 
 

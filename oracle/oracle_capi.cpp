@@ -31,6 +31,7 @@ int move_kind(const std::string& t) {
     if (t == "MetStapleRegrowth") return MV_MET_REGROWTH;
     if (t == "CBStapleRegrowth") return MV_CB_REGROWTH;
     if (t == "LearnedStapleExchange") return MV_LEARNED_EXCHANGE;
+    if (t == "LearnedStapleRegrowth") return MV_LEARNED_REGROWTH;
     if (t == "CTRGScaffoldRegrowth") return MV_CTRG_SCAFFOLD;
     if (t == "CTRGJumpScaffoldRegrowth") return MV_CTRG_JUMP;
     if (t == "CTCBScaffoldRegrowth") return MV_CTCB_SCAFFOLD;

@@ -136,7 +136,8 @@ struct BiasRec {
 };
 
 enum MoveKind { MV_ORIENTATION = 0, MV_MET_EXCHANGE = 1, MV_MET_REGROWTH = 2, MV_CB_REGROWTH = 3, MV_LEARNED_EXCHANGE = 4,
-                MV_CTRG_SCAFFOLD = 5, MV_CTRG_JUMP = 6, MV_CTCB_SCAFFOLD = 7, MV_CTCB_JUMP = 8 };
+                MV_CTRG_SCAFFOLD = 5, MV_CTRG_JUMP = 6, MV_CTCB_SCAFFOLD = 7, MV_CTCB_JUMP = 8,
+                MV_LEARNED_REGROWTH = 9 };
 
 // Options of a scaffold regrowth movetype (src/simulation.cpp:400-560).
 struct ScaffoldMoveOpts {
@@ -1626,6 +1627,117 @@ class System {
         return learned_delete();
     }
 
+    // ----------------------------- learned regrowth directions (engine only) ---
+    // CPU restatement of the engine's LearnedStapleRegrowth: the same site
+    // classes, weights (the engine's table), sums in the same order, draws at
+    // the same points.
+    int lr_site_class(int i, V3 p, V3* ob, bool* has_ob) const {
+        *has_ob = false;
+        int occ = occupancy(p);
+        if (occ == UNASSIGNED) return 0;
+        if (occ == UNBOUND) {
+            int j = unbound_at(p);
+            *ob = -doms[j].ore;
+            *has_ob = true;
+            return doms[i].dident == -doms[j].dident ? 1 : 2;
+        }
+        return 3;
+    }
+    double lr_propose(int i, int prev, bool sample, int& v, V3& o) {
+        if (!learn_w) throw std::runtime_error("LearnedStapleRegrowth needs the weight table");
+        double w[6];
+        V3 ob[6];
+        bool hob[6];
+        double z = 0;
+        for (int k = 0; k < 6; ++k) {
+            int f = lr_site_class(i, doms[prev].pos + kUnit[k], &ob[k], &hob[k]);
+            w[k] = learn_w[ldo_learn_dir_index(learn_tb, f)];
+            z += w[k];
+        }
+        if (sample) {
+            double r = rng.uniform_real();
+            double cum = 0;
+            v = 5;
+            for (int k = 0; k < 6; ++k) {
+                cum += z > 0 ? LDO_LEARN_EPS_D / 6.0 + (1.0 - LDO_LEARN_EPS_D) * (w[k] / z) : 1.0 / 6.0;
+                if (r < cum) {
+                    v = k;
+                    break;
+                }
+            }
+            if (hob[v]) {
+                double r2 = rng.uniform_real();
+                o = r2 < 1.0 - LDO_LEARN_EPS_O ? ob[v] : kUnit[rng.uniform_int(0, 5)];
+            }
+            else {
+                o = kUnit[rng.uniform_int(0, 5)];
+            }
+        }
+        double qv = z > 0 ? LDO_LEARN_EPS_D / 6.0 + (1.0 - LDO_LEARN_EPS_D) * (w[v] / z) : 1.0 / 6.0;
+        double qo = hob[v] ? (o == ob[v] ? (1.0 - LDO_LEARN_EPS_O) + LDO_LEARN_EPS_O / 6.0 : LDO_LEARN_EPS_O / 6.0)
+                           : 1.0 / 6.0;
+        return qv * qo;
+    }
+    bool learned_regrowth() {
+        if (num_staples == 0) return false;
+        int ci = rng.uniform_int(1, num_staples);
+        std::vector<int> sel = chains[ci];
+        if (staple_is_connector(sel)) return false;
+        auto bds = find_bound_domains(sel);
+        auto gp = bds[rng.uniform_int(0, (int)bds.size() - 1)];
+        std::vector<V3> old_pos, old_ore;
+        for (int id : sel) {
+            old_pos.push_back(doms[id].pos);
+            old_ore.push_back(doms[id].ore);
+        }
+        unassign_domains(sel);
+        delta_e += set_growth_point(gp.first, gp.second);
+        if (rejected) return false;
+        int d0 = doms[gp.first].d, len = (int)sel.size();
+        std::vector<std::pair<int, int>> grown;   // (domain index, previous domain index) in growth order
+        for (int k = d0 + 1; k < len; ++k) grown.push_back({k, k - 1});
+        for (int k = d0 - 1; k >= 0; --k) grown.push_back({k, k + 1});
+        double qn = 1;
+        for (auto& gk : grown) {
+            int i = sel[gk.first], prev = sel[gk.second];
+            int v = 0;
+            V3 o;
+            qn *= lr_propose(i, prev, true, v, o);
+            delta_e += set_domain_config(i, doms[prev].pos + kUnit[v], o);
+            if (violated) {
+                rejected = true;
+                return false;
+            }
+            assigned.push_back(key_of(i));
+        }
+        add_external_bias_met();
+        int nbd = num_bound_staple_domains(sel);
+        // Q(old): the old configuration grown again from the growth point
+        std::vector<V3> new_pos, new_ore;
+        for (auto& gk : grown) {
+            new_pos.push_back(doms[sel[gk.first]].pos);
+            new_ore.push_back(doms[sel[gk.first]].ore);
+        }
+        for (size_t n = grown.size(); n-- > 0;) unassign_domain(sel[grown[n].first]);
+        double qo = 1;
+        for (auto& gk : grown) {
+            int i = sel[gk.first], prev = sel[gk.second];
+            V3 dv = old_pos[gk.first] - doms[prev].pos;
+            int v = 0;
+            while (v < 6 && !(kUnit[v] == dv)) ++v;
+            if (v == 6) throw std::runtime_error("old staple configuration is not a chain of neighbours");
+            V3 o = old_ore[gk.first];
+            qo *= lr_propose(i, prev, false, v, o);
+            set_checked(i, old_pos[gk.first], o);
+        }
+        for (size_t n = grown.size(); n-- > 0;) unassign_domain(sel[grown[n].first]);
+        for (size_t n = 0; n < grown.size(); ++n) set_checked(sel[grown[n].first], new_pos[n], new_ore[n]);
+        double boltz = xexp(-(delta_e));
+        double pratio = boltz * (double)bds.size() / nbd;
+        pratio *= qo / qn;
+        return test_acceptance(pratio);
+    }
+
     // MetStapleRegrowthMCMovetype (src/met_movetypes.cpp:470)
     bool met_regrowth() {
         if (num_staples == 0) return false;
@@ -2847,6 +2959,7 @@ class System {
         case MV_MET_REGROWTH: acc = met_regrowth(); break;
         case MV_CB_REGROWTH: acc = cb_regrowth(); break;
         case MV_LEARNED_EXCHANGE: acc = learned_exchange(); break;
+        case MV_LEARNED_REGROWTH: acc = learned_regrowth(); break;
         case MV_CTRG_SCAFFOLD: acc = ctrg_scaffold(cfg.move_opts[m]); break;
         case MV_CTRG_JUMP: acc = ctrg_jump(cfg.move_opts[m]); break;
         case MV_CTCB_SCAFFOLD: acc = ctcb_scaffold(cfg.move_opts[m]); break;

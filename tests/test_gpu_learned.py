@@ -1,8 +1,8 @@
-"""Learned insertion proposal on the GPU.
+"""Learned proposals on the GPU.
 
-- LearnedStapleExchange trajectories of the engine equal those of the CPU
-  restatement (same weight table, same Philox streams): lattice state, counts
-  and draws exactly, energies within 1e-12.
+- LearnedStapleExchange and LearnedStapleRegrowth trajectories of the engine
+  equal those of the CPU restatement (same weight table, same Philox
+  streams): lattice state, counts and draws exactly, energies within 1e-12.
 - The network's GPU loss and gradient (the training kernels) against the
   numpy reference oracle/learn_ref.py, and the GPU weight table against the
   reference forward pass.
@@ -33,10 +33,10 @@ def engine(*a, **k):
     return Engine(*a, **k)
 
 
-@pytest.mark.parametrize("case", ["c1", "g24a"])
-def test_learned_exchange_matches_oracle_per_step(case):
+@pytest.mark.parametrize("case,regrowth", [("c1", False), ("g24a", False), ("c1", True), ("g24a", True)])
+def test_learned_moves_match_oracle_per_step(case, regrowth):
     d = tempfile.mkdtemp()
-    over = "movetype_file = %s" % learned_moves(d)
+    over = "movetype_file = %s" % learned_moves(d, regrowth)
     table = np.exp(np.random.default_rng(17).normal(0.0, 2.0, learn_ref.TABLE))
     steps, n, seed = 3000, 6, 99
     eng = engine(inp(case), n_replicas=n, seed=seed, overrides=over)
@@ -131,15 +131,38 @@ def test_trained_network_gains_over_plain_and_untrained():
     assert trained > 5 * plain
     assert trained >= 0.98 * untrained
 
+    # regrowth: the trained direction weights against the uniform Met regrowth
+    over_lr = "movetype_file = %s" % learned_moves(d, regrowth=True)
+
+    def regrowth_acceptance(overrides, tab):
+        e = engine(f, n_replicas=n, seed=3, overrides=overrides)
+        e.set_controls(temps=temps)
+        if tab is not None:
+            e.learn_set_table(tab)
+        e.run_sweeps(100)
+        s0 = e.move_stats(3)
+        e.run_sweeps(200)
+        s = e.move_stats(3) - s0
+        return s[1, 1] / s[1, 0]
+
+    met = regrowth_acceptance(over, table)
+    lr_untrained = regrowth_acceptance(over_lr, None)
+    lr_trained = regrowth_acceptance(over_lr, table)
+    print("regrowth acceptance: Met %.4f, learned untrained %.4f, learned trained %.4f"
+          % (met, lr_untrained, lr_trained))
+    assert lr_trained > 2 * met
+    assert lr_trained > lr_untrained
+
 
 def test_learned_distribution_matches_plain_on_c2():
     """KL divergence between the bound-domain distributions of plain and
-    learned-proposal MC on the 12-domain c2 system (both relaxed from the
-    empty start for 4000 sweeps, then 4000 sweeps sampled every 10)."""
+    learned-proposal MC (learned exchange and learned regrowth) on the
+    12-domain c2 system (both relaxed from the empty start for 4000 sweeps,
+    then 4000 sweeps sampled every 10)."""
     import bench
     d = tempfile.mkdtemp()
     f = bench.write_c2(d)[1]
-    over = "movetype_file = %s" % learned_moves(d)
+    over = "movetype_file = %s" % learned_moves(d, regrowth=True)
     n = 1024
     temps = np.linspace(320.0, 350.0, n)
     eng = engine(f, n_replicas=n, seed=5)

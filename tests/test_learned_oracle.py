@@ -1,10 +1,10 @@
-"""Learned insertion proposal on the CPU (no GPU needed).
+"""Learned proposals on the CPU (no GPU needed).
 
-- Exactness of the Metropolis-Hastings ratio: the CPU restatement of
-  LearnedStapleExchange, driven by a strongly non-uniform random weight table,
-  samples the 4-domain system's (staples, fully bound) distribution of the
-  reference's exact enumeration (chi-square p > 0.01), as the plain moveset
-  does.
+- Exactness of the Metropolis-Hastings ratios: the CPU restatements of
+  LearnedStapleExchange and LearnedStapleRegrowth, driven by a strongly
+  non-uniform random weight table, sample the 4-domain system's (staples,
+  fully bound) distribution of the reference's exact enumeration (chi-square
+  p > 0.01), as the plain moveset does.
 - The numpy network (oracle/learn_ref.py) that the GPU kernels are checked
   against: its analytic gradient against central finite differences."""
 import json
@@ -23,13 +23,16 @@ sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(
 import learn_ref  # noqa: E402
 
 
-def learned_moves(d):
+def learned_moves(d, regrowth=False):
+    """The c2 moveset with the learned exchange (and, with regrowth, the
+    learned regrowth in place of the Met regrowth)."""
     mv = {"origami": {"movetypes": [
         {"label": "Learned staple exchange", "type": "LearnedStapleExchange", "freq": "1/3",
          "adaptive_exchange": False},
-        {"label": "Met staple regrowth", "type": "MetStapleRegrowth", "freq": "1/3"},
+        {"label": "Met staple regrowth", "type": "LearnedStapleRegrowth" if regrowth else "MetStapleRegrowth",
+         "freq": "1/3"},
         {"label": "CB staple regrowth", "type": "CBStapleRegrowth", "freq": "1/3"}]}}
-    p = os.path.join(d, "moves_learned.json")
+    p = os.path.join(d, "moves_learned%s.json" % ("_lr" if regrowth else ""))
     with open(p, "w") as f:
         json.dump(mv, f)
     return p
@@ -64,6 +67,24 @@ def test_learned_exchange_samples_exact_distribution():
     table = np.exp(rng.normal(0.0, 2.0, learn_ref.TABLE))
     # one state per replica after 60000 steps (the empty start has relaxed)
     states = run_batch_states(inp("c1"), 77, 1024, 60000, 1, 1, os.cpu_count() or 1,
+                              overrides="movetype_file = %s" % mv, learn_w=table)
+    p, obs, exp = chi2_against_enumeration(states)
+    assert p > 0.01, (obs, exp, p)
+
+
+def test_learned_regrowth_samples_exact_distribution():
+    """LearnedStapleRegrowth (learned directions and orientations) with a
+    strongly non-uniform random table: the enumeration's distribution."""
+    d = tempfile.mkdtemp()
+    mv = os.path.join(d, "moves_lr.json")
+    with open(mv, "w") as f:
+        json.dump({"origami": {"movetypes": [
+            {"label": "Met staple exchange", "type": "MetStapleExchange", "freq": "1/3", "adaptive_exchange": False},
+            {"label": "Learned staple regrowth", "type": "LearnedStapleRegrowth", "freq": "1/3"},
+            {"label": "CB staple regrowth", "type": "CBStapleRegrowth", "freq": "1/3"}]}}, f)
+    rng = np.random.default_rng(6)
+    table = np.exp(rng.normal(0.0, 2.0, learn_ref.TABLE))
+    states = run_batch_states(inp("c1"), 78, 1024, 60000, 1, 1, os.cpu_count() or 1,
                               overrides="movetype_file = %s" % mv, learn_w=table)
     p, obs, exp = chi2_against_enumeration(states)
     assert p > 0.01, (obs, exp, p)
