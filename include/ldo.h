@@ -207,15 +207,16 @@ ldo_status ldo_replica_status_noalloc(ldo_engine* e, int32_t* status_of_replica,
  * device buffers of n doubles. */
 ldo_status ldo_engine_exp(const double* x, double* y, int n);
 
-/* Learned insertion proposal (movetype "LearnedStapleExchange"; engine
- * extension with no counterpart in the reference, which only proposes
- * uniformly: src/movetypes.cpp:98-120).  A network of three 256-wide GELU
- * layers scores growth-point targets from their chain neighbourhood and the
- * temperature; ldo_learn.h describes the input encoding.  Until trained, every
- * unbound target weighs 1. */
+/* Learned proposals (movetypes "LearnedStapleExchange" and
+ * "LearnedStapleRegrowth"; engine extensions with no counterpart in the
+ * reference, which only proposes uniformly: src/movetypes.cpp:98-140).  A
+ * network of three 256-wide GELU layers scores growth-point targets from their
+ * chain neighbourhood and the temperature, and the six sites a regrown staple
+ * domain can take from what they hold; ldo_learn.h describes the input
+ * encoding.  Until trained, every input weighs 1. */
 
-/* Adds every replica's current bound / unbound domains to the training counts
- * (per network input). */
+/* Adds every replica's current bound / unbound domains and the sites of its
+ * placed staple domains to the training counts (per network input). */
 ldo_status ldo_learn_collect(ldo_engine* e);
 ldo_status ldo_learn_reset_counts(ldo_engine* e);
 /* Training counts per network input (n = LDO_LEARN_TABLE = 524544: 524288
