@@ -460,8 +460,6 @@ def main():
             ts = [tau_int(series[r]) for r in range(i * per, (i + 1) * per)]
             ts = [t for t in ts if t is not None]
             taus[n] = float(np.median(ts)) if ts else None
-        hists = [np.bincount(np.concatenate(series[i * per:(i + 1) * per]).astype(np.int64), minlength=2 * n + 1)
-                 for i, n in enumerate(SIZES)]
         train = None
         if collect:
             # training data for the proposal network from the plain sampler (untimed)
@@ -475,7 +473,7 @@ def main():
         st = eng.move_stats(3)
         acc = [float(st[k, 1]) / max(1.0, float(st[k, 0])) for k in range(3)]
         return {"eng": eng, "dev_ms": dev_ms, "t_dev": t_dev, "ess": ess, "tau_med": tau_med, "taus": taus,
-                "clk": clk, "hists": hists, "train": train, "acc": acc}
+                "clk": clk, "train": train, "acc": acc}
 
     def e2e_arm(overrides, table):
         """The same loop through the C ABI with host buffers: temperatures in,
@@ -514,14 +512,6 @@ def main():
     h2d = N_REP * 8
     d2h = N_REP * SWEEPS_PER_STEP * 2 * 2
 
-    def kl(p, q):
-        p = p / p.sum()
-        q = (q + 0.5) / (q + 0.5).sum()
-        m = p > 0
-        return float(np.sum(p[m] * np.log(p[m] / q[m])))
-
-    kls = {n: kl(plain["hists"][i].astype(float), learned["hists"][i].astype(float)) for i, n in enumerate(SIZES)}
-
     # roofline of the MC kernel: algorithmic DRAM bytes = state in + out + samples
     eng = learned["eng"]
     dev_ms = learned["dev_ms"]
@@ -558,7 +548,11 @@ def main():
                        "l2": "state resident in shared memory; no L2 flush needed"},
             "learned": rates(learned), "plain": rates(plain),
             "learned_over_plain": value / plain_value,
-            "kl_plain_learned_by_size": kls,
+            # the two arms' recorded sweeps start 300 sweeps after empty
+            # lattices, too short for plain MC to forget its start (its tau_int
+            # is tens of sweeps); the equality of the sampled distributions is
+            # tested on equilibrated runs instead
+            "distribution_check": "tests/test_gpu_learned.py::test_learned_distribution_matches_plain_on_c2",
             "network": {"layers": "64-256-256-256-1 GELU, bf16 weights/activations, fp32 accumulation",
                         "train_iters": tr["iters"], "loss_first": tr["loss_first"], "loss_last": tr["loss_last"],
                         "train_s": tr["train_s"]},

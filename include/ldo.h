@@ -13,6 +13,12 @@
  *   ldo_get_observables   OrigamiSystem counters + energy + SystemBiases
  *                         (include/.../origami_system.hpp:99-130)
  *   ldo_get_config        OrigamiSystem::chains (src/origami_system.cpp:175)
+ *   ldo_set_config        OrigamiSystem ctor from given chains
+ *                         (src/origami_system.cpp:588-615, 991-1003)
+ *   ldo_read_trj_frame    OrigamiTrajInputFile::read_config (src/files.cpp:129)
+ *   ldo_checkpoint_*      restart_traj_file + .randstate + .swp restart
+ *                         (src/origami_system.cpp:1000, src/simulation.cpp:204,
+ *                         src/ptmc_simulation.cpp:62)
  *   ldo_pt_run            PTGCMCSimulation::run (src/ptmc_simulation.cpp:106)
  *
  * Conventions: every call is synchronous at return; input buffers are
@@ -107,6 +113,34 @@ ldo_status ldo_get_observables(ldo_engine* e, ldo_observables* out, int n);
  * length, length x (x, y, z, ox, oy, oz, state)).  *written receives the
  * number of ints; LDO_EINVAL if cap is too small. */
 ldo_status ldo_get_config(ldo_engine* e, int replica, int32_t* buf, int cap, int* written);
+
+/* Replaces one replica's configuration with buf (ldo_get_config's format;
+ * the states are ignored): the replica is rebuilt as the OrigamiSystem
+ * constructor builds a system from given chains (energy, counters, order
+ * parameters and biases of the new configuration) and keeps its
+ * random-number position, step counter and move statistics.  A
+ * configuration that violates a constraint returns LDO_EINVAL ("Constaints
+ * in violation after move complete") and leaves the replica unchanged. */
+ldo_status ldo_set_config(ldo_engine* e, int replica, const int32_t* buf, int n);
+
+/* Frame `frame` (0 = first written) of a .trj trajectory file in
+ * ldo_get_config's format, states 0 (OrigamiTrajInputFile::read_config,
+ * src/files.cpp:129).  Host only; error text via ldo_last_error(NULL).
+ * The .inp keys restart_traj_file / restart_step start every replica of a
+ * system from such a frame, as the reference's setup_origami does. */
+ldo_status ldo_read_trj_frame(const char* path, int frame, int32_t* buf, int cap, int* written);
+
+/* Checkpoint / resume: one binary file with every replica's state
+ * (configuration, counters, random-number position, move statistics), its
+ * controls (temperature, multipliers, windows, centres, grid biases, seed),
+ * the learned proposal's table and network, and a parallel-tempering
+ * ladder's permutation, swap counter, swap random-number positions and
+ * statistics.  An engine created from the same input files with the same
+ * replica count loads it and continues bit for bit as the saved engine
+ * would have; LDO_EINVAL for a file of other systems.  Sample and trace
+ * buffers, the .swp history and umbrella-sampling iterations are not saved. */
+ldo_status ldo_checkpoint_save(ldo_engine* e, const char* path);
+ldo_status ldo_checkpoint_load(ldo_engine* e, const char* path);
 
 /* Order-parameter sampling: every `interval` steps each replica appends
  * (num_fully_bound, num_staples) to a ring of `capacity` samples. */

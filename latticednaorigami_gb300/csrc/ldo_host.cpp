@@ -106,9 +106,11 @@ HostSystem load_system(const string& inp, const string& overrides) {
                 ldo_io::set_param(p, ldo_io::trim(line.substr(0, eq)), ldo_io::trim(line.substr(eq + 1)));
             }
         }
-        if (!p.restart_traj_file.empty())
-            throw LdoError(LDO_EINVAL, "restart_traj_file: restart from a trajectory is not implemented by this engine");
         hs.sf = ldo_io::read_system(ldo_io::resolve(p, p.origami_input_filename));
+        // setup_origami (src/origami_system.cpp:1000-1003): the configuration
+        // of frame restart_step of a trajectory replaces the system file's
+        if (!p.restart_traj_file.empty())
+            hs.sf.chains = ldo_io::read_trj_frame(ldo_io::resolve(p, p.restart_traj_file), p.restart_step);
         hs.moves = ldo_io::read_movetypes(ldo_io::resolve(p, p.movetype_file));
         if (!p.order_parameter_file.empty()) hs.ops = ldo_io::read_ops(ldo_io::resolve(p, p.order_parameter_file));
         if (!p.bias_functions_file.empty())
@@ -519,6 +521,7 @@ struct ldo_engine {
         L.ct_stride = ct_stride;
         L.lay = lay;
         L.n_rep = n_rep;
+        L.only_rep = -1;
         L.warps_per_block = wpb;
         L.smem_pad = smem_pad;
         L.mode = mode;
@@ -553,12 +556,14 @@ struct ldo_engine {
         }
     }
 
-    void init_arena() {
-        vector<unsigned char> host((size_t)n_rep * lay.bytes, 0);
-        for (int r = 0; r < n_rep; ++r) {
+    // Replica r's state bytes (b: lay.bytes zero bytes) for configuration
+    // `chains`, as the OrigamiSystem constructor leaves them before
+    // set_all_domains (src/origami_system.cpp:659-678); the kernel's init
+    // mode then sets every domain.
+    void fill_replica(int r, const vector<ldo_io::ChainConf>& chains, unsigned char* b) {
+        {
             const HostSystem& hs = systems[sys_of[r]];
             const LdoSys& d = hs.desc;
-            unsigned char* b = host.data() + (size_t)r * lay.bytes;
             auto* h = reinterpret_cast<LdoHdr*>(b + lay.o_hdr);
             auto* pp = reinterpret_cast<long long*>(b + lay.o_pp);
             auto* nxt = reinterpret_cast<int16_t*>(b + lay.o_nxt);
@@ -592,7 +597,8 @@ struct ldo_engine {
                 }
             }
             for (int k = 0; k <= lay.kmax; ++k) chain_type[k] = 0xff;
-            const auto& chains = hs.sf.chains;
+            if (chains.empty() || (int)chains.size() - 1 > d.kmax)
+                throw LdoError(LDO_ECAPACITY, "configuration has more staples than staple slots");
             int total = 0;
             int maxc = 0;
             for (size_t c = 0; c < chains.size(); ++c) {
@@ -654,6 +660,12 @@ struct ldo_engine {
             h->energy += nst * h_tabs[h_ctl[r].tab].init_e;
             h->tab = h_ctl[r].tab;
         }
+    }
+
+    void init_arena() {
+        vector<unsigned char> host((size_t)n_rep * lay.bytes, 0);
+        for (int r = 0; r < n_rep; ++r)
+            fill_replica(r, systems[sys_of[r]].sf.chains, host.data() + (size_t)r * lay.bytes);
         d_arena.alloc(host.size());
         CU(cudaMemcpy(d_arena.p, host.data(), host.size(), cudaMemcpyHostToDevice));
     }
@@ -769,6 +781,281 @@ struct ldo_engine {
             *ms = f;
         }
         check_status();
+    }
+
+    // ---------------------------------------- configuration import ---
+    // Chains of a configuration buffer in ldo_get_config's format (n_chains,
+    // then per chain index, identity, length, length x (x, y, z, ox, oy, oz,
+    // state)); the states are ignored.
+    static vector<ldo_io::ChainConf> parse_config(const int32_t* buf, int n) {
+        int p = 0;
+        auto next = [&]() {
+            if (p >= n) throw LdoError(LDO_EINVAL, "configuration buffer ends early");
+            return buf[p++];
+        };
+        int nc = next();
+        if (nc < 1 || nc > 100000) throw LdoError(LDO_EINVAL, "configuration: bad number of chains");
+        vector<ldo_io::ChainConf> chains(nc);
+        for (auto& c : chains) {
+            c.index = next();
+            c.identity = next();
+            int len = next();
+            if (len < 1 || len > 100000) throw LdoError(LDO_EINVAL, "configuration: bad chain length");
+            for (int d = 0; d < len; ++d) {
+                std::array<int, 3> pos, ore;
+                for (int q = 0; q < 3; ++q) pos[q] = next();
+                for (int q = 0; q < 3; ++q) ore[q] = next();
+                next();
+                c.positions.push_back(pos);
+                c.orientations.push_back(ore);
+            }
+        }
+        if (p != n) throw LdoError(LDO_EINVAL, "configuration buffer has trailing values");
+        return chains;
+    }
+
+    // Replaces replica r's configuration, as the OrigamiSystem constructor
+    // builds a system from given chains (src/origami_system.cpp:991-1003):
+    // energy, counters, order parameters and biases become those of the new
+    // configuration; the replica keeps its random-number position, step
+    // counter, sample count and move statistics.  A configuration that
+    // violates a constraint leaves the replica as it was
+    // (set_all_domains: "Constaints in violation after move complete").
+    void set_config(int r, const int32_t* buf, int n) {
+        if (r < 0 || r >= n_rep) throw LdoError(LDO_EINVAL, "replica out of range");
+        vector<ldo_io::ChainConf> chains = parse_config(buf, n);
+        size_t off = (size_t)r * lay.bytes;
+        vector<unsigned char> old(lay.bytes), fresh(lay.bytes, 0);
+        CU(cudaMemcpy(old.data(), d_arena.p + off, lay.bytes, cudaMemcpyDeviceToHost));
+        fill_replica(r, chains, fresh.data());
+        const auto* ho = reinterpret_cast<const LdoHdr*>(old.data() + lay.o_hdr);
+        auto* hn = reinterpret_cast<LdoHdr*>(fresh.data() + lay.o_hdr);
+        hn->draws = ho->draws;
+        hn->steps_done = ho->steps_done;
+        hn->sample_count = ho->sample_count;
+        std::memcpy(fresh.data() + lay.o_mstat, old.data() + lay.o_mstat, 2 * lay.nmv * sizeof(long long));
+        CU(cudaMemcpy(d_arena.p + off, fresh.data(), lay.bytes, cudaMemcpyHostToDevice));
+        LdoLaunch L = launch_params(LDO_MODE_INIT, 0);
+        L.only_rep = r;
+        CU(ldo_launch_mc(L, stream));
+        CU(cudaStreamSynchronize(stream));
+        LdoHdr h;
+        CU(cudaMemcpy(&h, d_arena.p + off + lay.o_hdr, sizeof h, cudaMemcpyDeviceToHost));
+        if (h.status != 0) {
+            CU(cudaMemcpy(d_arena.p + off, old.data(), lay.bytes, cudaMemcpyHostToDevice));
+            throw LdoError(LDO_EINVAL, h.status == LDO_RS_INVARIANT
+                                           ? "Constaints in violation after move complete"
+                                           : "configuration does not fit the replica's capacity");
+        }
+    }
+
+    // ---------------------------------------- checkpoint / resume ---
+    // One binary file from which a run continues bit for bit: every
+    // replica's state (configuration, counters, random-number position,
+    // move statistics), its controls (temperature, chemical-potential and
+    // stacking multipliers, windows, centres, grid biases, seed), the
+    // learned proposal's weight table and network, and a parallel-tempering
+    // ladder's permutation, swap counter, swap random-number positions and
+    // statistics.  It stands for the reference's restart pieces: the .trj
+    // configuration (src/origami_system.cpp:1000), the .randstate file
+    // (src/simulation.cpp:204-212) and the permutation of the last .swp line
+    // (src/ptmc_simulation.cpp:62-83).  Energy-table indices are stored as
+    // (system, temperature, stacking multiplier) keys and rebuilt, so any
+    // engine created from the same input files and replica count can load
+    // it.  Not stored: sample and trace buffers, the .swp history, the
+    // network optimiser's moments, umbrella-sampling iterations.
+    struct CkptHead {
+        char magic[8];
+        uint32_t version, n_rep, n_sys, seed;
+        uint64_t sys_hash;
+        uint32_t n_tabs, has_mlp;
+        uint64_t n_grid;
+        int32_t pt_rungs, pt_q, pt_dim2, pt_nctr;
+        int64_t pt_swap_i;
+        LdoLayout lay;
+    };
+    struct CkptTab {
+        int32_t sys, pad;
+        double temp, mult;
+    };
+
+    uint64_t systems_hash() const {
+        uint64_t h = 1469598103934665603ull;   // FNV-1a
+        const unsigned char* b = reinterpret_cast<const unsigned char*>(h_sys.data());
+        for (size_t i = 0; i < h_sys.size() * sizeof(LdoSys); ++i) h = (h ^ b[i]) * 1099511628211ull;
+        for (int s : sys_of) h = (h ^ (uint64_t)(uint32_t)s) * 1099511628211ull;
+        return h;
+    }
+
+    void checkpoint_save(const string& path) {
+        CkptHead H;
+        std::memset(&H, 0, sizeof H);
+        std::memcpy(H.magic, "LDOCKPT", 8);
+        H.version = 1;
+        H.n_rep = (uint32_t)n_rep;
+        H.n_sys = (uint32_t)systems.size();
+        H.seed = seed;
+        H.sys_hash = systems_hash();
+        H.n_tabs = (uint32_t)h_tabs.size();
+        H.has_mlp = mlp_init ? 1 : 0;
+        H.n_grid = h_grid.size();
+        H.pt_rungs = pt_rungs;
+        H.pt_q = pt_q;
+        H.pt_dim2 = pt_dim2;
+        H.pt_nctr = pt_nctr;
+        H.pt_swap_i = pt_swap_i;
+        H.lay = lay;
+        vector<CkptTab> keys(h_tabs.size());
+        for (auto& kv : tab_index) {
+            CkptTab& k = keys[kv.second];
+            std::memset(&k, 0, sizeof k);
+            k.sys = std::get<0>(kv.first);
+            k.temp = std::get<1>(kv.first);
+            k.mult = std::get<2>(kv.first);
+        }
+        vector<unsigned char> arena((size_t)n_rep * lay.bytes);
+        CU(cudaMemcpy(arena.data(), d_arena.p, arena.size(), cudaMemcpyDeviceToHost));
+        vector<double> table(LDO_LEARN_TABLE);
+        CU(cudaMemcpy(table.data(), d_learn_w.p, table.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        std::ofstream f(path, std::ios::binary);
+        if (!f) throw LdoError(LDO_EINVAL, path + ": cannot open checkpoint file for writing");
+        auto put = [&](const void* p, size_t bytes) { f.write(reinterpret_cast<const char*>(p), (std::streamsize)bytes); };
+        put(&H, sizeof H);
+        put(keys.data(), keys.size() * sizeof(CkptTab));
+        put(h_ctl.data(), h_ctl.size() * sizeof(LdoRepCtl));
+        put(temps.data(), n_rep * sizeof(double));
+        put(stack_mults.data(), n_rep * sizeof(double));
+        put(u_mults.data(), n_rep * sizeof(double));
+        put(h_grid.data(), h_grid.size() * sizeof(double));
+        put(arena.data(), arena.size());
+        put(table.data(), table.size() * sizeof(double));
+        if (mlp_init) {
+            vector<float> params(LDO_LEARN_NPARAM);
+            CU(cudaMemcpy(params.data(), mlp.params, params.size() * sizeof(float), cudaMemcpyDeviceToHost));
+            put(params.data(), params.size() * sizeof(float));
+        }
+        if (pt_rungs) {
+            int nl = n_rep / pt_rungs;
+            vector<int> perm(n_rep);
+            vector<double> rep_q(4 * (size_t)n_rep);
+            vector<unsigned long long> draws(nl);
+            vector<long long> att(std::max(pt_nctr, 1)), acc(std::max(pt_nctr, 1));
+            CU(cudaMemcpy(perm.data(), d_perm.p, perm.size() * sizeof(int), cudaMemcpyDeviceToHost));
+            CU(cudaMemcpy(rep_q.data(), d_rep_q.p, rep_q.size() * sizeof(double), cudaMemcpyDeviceToHost));
+            CU(cudaMemcpy(draws.data(), d_pt_draws.p, draws.size() * sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost));
+            CU(cudaMemcpy(att.data(), d_pt_att.p, att.size() * sizeof(long long), cudaMemcpyDeviceToHost));
+            CU(cudaMemcpy(acc.data(), d_pt_acc.p, acc.size() * sizeof(long long), cudaMemcpyDeviceToHost));
+            put(perm.data(), perm.size() * sizeof(int));
+            put(rep_q.data(), rep_q.size() * sizeof(double));
+            put(draws.data(), draws.size() * sizeof(unsigned long long));
+            put(att.data(), att.size() * sizeof(long long));
+            put(acc.data(), acc.size() * sizeof(long long));
+        }
+        f.flush();
+        if (!f) throw LdoError(LDO_EINVAL, path + ": writing the checkpoint failed");
+    }
+
+    void checkpoint_load(const string& path) {
+        std::ifstream f(path, std::ios::binary);
+        if (!f) throw LdoError(LDO_EINVAL, path + ": checkpoint file does not exist");
+        auto get = [&](void* p, size_t bytes) {
+            f.read(reinterpret_cast<char*>(p), (std::streamsize)bytes);
+            if ((size_t)f.gcount() != bytes) throw LdoError(LDO_EINVAL, path + ": checkpoint file is truncated");
+        };
+        CkptHead H;
+        get(&H, sizeof H);
+        if (std::memcmp(H.magic, "LDOCKPT", 8) != 0 || H.version != 1)
+            throw LdoError(LDO_EINVAL, path + ": not a checkpoint of this engine");
+        if (H.n_rep != (uint32_t)n_rep || H.n_sys != systems.size() || H.sys_hash != systems_hash() ||
+            std::memcmp(&H.lay, &lay, sizeof lay) != 0 || H.n_grid != h_grid.size())
+            throw LdoError(LDO_EINVAL, path + ": checkpoint of other systems or another replica count");
+        if (H.n_tabs == 0 || H.n_tabs > 1000000) throw LdoError(LDO_EINVAL, path + ": bad table count");
+        if (H.pt_rungs < 0 || (H.pt_rungs && (H.pt_rungs < 2 || n_rep % H.pt_rungs != 0)))
+            throw LdoError(LDO_EINVAL, path + ": bad ladder shape");
+        vector<CkptTab> keys(H.n_tabs);
+        get(keys.data(), keys.size() * sizeof(CkptTab));
+        vector<LdoRepCtl> ctl(n_rep);
+        get(ctl.data(), ctl.size() * sizeof(LdoRepCtl));
+        vector<double> t(n_rep), sm(n_rep), um(n_rep), grid(h_grid.size());
+        get(t.data(), n_rep * sizeof(double));
+        get(sm.data(), n_rep * sizeof(double));
+        get(um.data(), n_rep * sizeof(double));
+        get(grid.data(), grid.size() * sizeof(double));
+        vector<unsigned char> arena((size_t)n_rep * lay.bytes);
+        get(arena.data(), arena.size());
+        vector<double> table(LDO_LEARN_TABLE);
+        get(table.data(), table.size() * sizeof(double));
+        vector<float> params;
+        if (H.has_mlp) {
+            params.resize(LDO_LEARN_NPARAM);
+            get(params.data(), params.size() * sizeof(float));
+        }
+        // energy tables of the saved keys, in this engine's numbering
+        vector<int> remap(H.n_tabs);
+        for (size_t i = 0; i < keys.size(); ++i) {
+            if (keys[i].sys < 0 || keys[i].sys >= (int)systems.size())
+                throw LdoError(LDO_EINVAL, path + ": bad table key");
+            remap[i] = table_for(keys[i].sys, keys[i].temp, keys[i].mult);
+        }
+        auto tab = [&](int k) {
+            if (k < 0 || k >= (int)remap.size()) throw LdoError(LDO_EINVAL, path + ": bad table index");
+            return remap[k];
+        };
+        for (int r = 0; r < n_rep; ++r) {
+            ctl[r].tab = tab(ctl[r].tab);
+            auto* h = reinterpret_cast<LdoHdr*>(arena.data() + (size_t)r * lay.bytes + lay.o_hdr);
+            h->tab = tab(h->tab);
+        }
+        // ladder: set up its shape, then the saved permutation and counters
+        if (pt_graph) {
+            cudaGraphExecDestroy(pt_graph);
+            pt_graph = nullptr;
+        }
+        seed = H.seed;
+        pt_rungs = 0;
+        if (H.pt_rungs) {
+            pt_setup(H.pt_rungs, H.pt_q, H.pt_dim2);
+            if (pt_nctr != H.pt_nctr) throw LdoError(LDO_EINVAL, path + ": ladder does not match the input files");
+            int nl = n_rep / pt_rungs;
+            vector<int> perm(n_rep);
+            vector<double> rep_q(4 * (size_t)n_rep);
+            vector<unsigned long long> draws(nl);
+            vector<long long> att(std::max(pt_nctr, 1)), acc(std::max(pt_nctr, 1));
+            get(perm.data(), perm.size() * sizeof(int));
+            get(rep_q.data(), rep_q.size() * sizeof(double));
+            get(draws.data(), draws.size() * sizeof(unsigned long long));
+            get(att.data(), att.size() * sizeof(long long));
+            get(acc.data(), acc.size() * sizeof(long long));
+            vector<char> seen(n_rep, 0);
+            for (int r : perm) {
+                if (r < 0 || r >= n_rep || seen[r]) throw LdoError(LDO_EINVAL, path + ": bad ladder permutation");
+                seen[r] = 1;
+            }
+            CU(cudaMemcpy(d_perm.p, perm.data(), perm.size() * sizeof(int), cudaMemcpyHostToDevice));
+            CU(cudaMemcpy(d_rep_q.p, rep_q.data(), rep_q.size() * sizeof(double), cudaMemcpyHostToDevice));
+            CU(cudaMemcpy(d_pt_draws.p, draws.data(), draws.size() * sizeof(unsigned long long),
+                          cudaMemcpyHostToDevice));
+            CU(cudaMemcpy(d_pt_att.p, att.data(), att.size() * sizeof(long long), cudaMemcpyHostToDevice));
+            CU(cudaMemcpy(d_pt_acc.p, acc.data(), acc.size() * sizeof(long long), cudaMemcpyHostToDevice));
+            pt_swap_i = H.pt_swap_i;
+        }
+        h_ctl = ctl;
+        temps = t;
+        stack_mults = sm;
+        u_mults = um;
+        h_grid = grid;
+        upload_tables();
+        upload_ctl();
+        upload_grid();
+        CU(cudaMemcpy(d_arena.p, arena.data(), arena.size(), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(d_learn_w.p, table.data(), table.size() * sizeof(double), cudaMemcpyHostToDevice));
+        if (H.has_mlp) {
+            mlp_ensure(0);
+            CU(cudaMemcpy(mlp.params, params.data(), params.size() * sizeof(float), cudaMemcpyHostToDevice));
+            CU(ldo_mlp_sync_weights(mlp, stream));
+        }
+        CU(cudaStreamSynchronize(stream));
     }
 
     // ---------------------------------------- learned insertion proposal ---
@@ -1486,6 +1773,46 @@ ldo_status ldo_get_config(ldo_engine* e, int replica, int32_t* buf, int cap, int
         std::memcpy(buf, out.data(), out.size() * sizeof(int32_t));
         if (written) *written = (int)out.size();
     });
+}
+
+ldo_status ldo_set_config(ldo_engine* e, int replica, const int32_t* buf, int n) {
+    if (!e || !buf || n <= 0) return LDO_EINVAL;
+    return guard(e, [&]() { e->set_config(replica, buf, n); });
+}
+
+ldo_status ldo_read_trj_frame(const char* path, int frame, int32_t* buf, int cap, int* written) {
+    if (!path || !buf || cap < 0) {
+        g_create_err = "invalid arguments";
+        return LDO_EINVAL;
+    }
+    return guard(nullptr, [&]() {
+        vector<ldo_io::ChainConf> chains = ldo_io::read_trj_frame(path, frame);
+        vector<int32_t> out;
+        out.push_back((int32_t)chains.size());
+        for (auto& c : chains) {
+            out.push_back(c.index);
+            out.push_back(c.identity);
+            out.push_back((int32_t)c.positions.size());
+            for (size_t d = 0; d < c.positions.size(); ++d) {
+                for (int q = 0; q < 3; ++q) out.push_back(c.positions[d][q]);
+                for (int q = 0; q < 3; ++q) out.push_back(c.orientations[d][q]);
+                out.push_back(0);
+            }
+        }
+        if ((int)out.size() > cap) throw LdoError(LDO_EINVAL, "config buffer too small");
+        std::memcpy(buf, out.data(), out.size() * sizeof(int32_t));
+        if (written) *written = (int)out.size();
+    });
+}
+
+ldo_status ldo_checkpoint_save(ldo_engine* e, const char* path) {
+    if (!e || !path) return LDO_EINVAL;
+    return guard(e, [&]() { e->checkpoint_save(path); });
+}
+
+ldo_status ldo_checkpoint_load(ldo_engine* e, const char* path) {
+    if (!e || !path) return LDO_EINVAL;
+    return guard(e, [&]() { e->checkpoint_load(path); });
 }
 
 ldo_status ldo_set_sampling(ldo_engine* e, int interval, int capacity) {

@@ -520,6 +520,62 @@ inline SystemFile read_system(const string& fname) {
     return system_from_json(read_json(fname, "Origami input file"));
 }
 
+// ------------------------------------------------------ trajectory ----
+// Configuration of frame `frame` (0 = the first configuration written) of a
+// .trj file (OrigamiTrajInputFile::read_config, src/files.cpp:129-189): frames
+// are separated by an empty line; a frame is its step line, then per chain a
+// line "index identity", a line of x y z triples and a line of orientation
+// triples.  The reference's reader appends one (0, 0, 0) triple for the
+// trailing space of each line, which its constructor never reads (it takes
+// as many triples as the chain's identity has domains); this reader keeps
+// every whole triple and leaves the length check to the caller.
+inline vector<ChainConf> read_trj_frame(const string& fname, int frame) {
+    std::ifstream f(fname);
+    if (!f) throw std::runtime_error("Trajectory input file " + fname + " does not exist");
+    if (frame < 0) throw std::runtime_error("restart_step must not be negative");
+    string line;
+    // OrigamiTrajInputFile::go_to_step (src/files.cpp:191): skip `frame` frames
+    for (int i = 0; i < frame; ++i) {
+        while (true) {
+            bool got = (bool)std::getline(f, line);
+            if (!got || f.eof())
+                throw std::runtime_error("Step " + std::to_string(frame) + " not found in trajectory input file" +
+                                         fname);
+            if (line.empty()) break;
+        }
+    }
+    if (!std::getline(f, line)) throw std::runtime_error("Step " + std::to_string(frame) +
+                                                         " not found in trajectory input file" + fname);
+    auto triples = [&](const string& s) {
+        std::istringstream is(s);
+        vector<std::array<int, 3>> v;
+        long long a, b, c;
+        while (is >> a >> b >> c) v.push_back({(int)a, (int)b, (int)c});
+        return v;
+    };
+    vector<ChainConf> chains;
+    while (std::getline(f, line) && !line.empty()) {
+        std::istringstream id(line);
+        ChainConf cc;
+        if (!(id >> cc.index >> cc.identity))
+            throw std::runtime_error("Trajetory input file " + fname + " is not well formed: chain line '" + line +
+                                     "'");
+        string pos, ore;
+        std::getline(f, pos);
+        std::getline(f, ore);
+        cc.positions = triples(pos);
+        cc.orientations = triples(ore);
+        if (cc.positions.size() != cc.orientations.size())
+            throw std::runtime_error("Trajetory input file " + fname +
+                                     " is not well formed: positions and orientations differ in number");
+        chains.push_back(cc);
+    }
+    if (chains.empty())
+        throw std::runtime_error("Trajetory input file " + fname + " is not well formed: frame " +
+                                 std::to_string(frame) + " has no chains");
+    return chains;
+}
+
 // ------------------------------------------------------ movetype JSON ----
 struct MoveSpec {
     string type;

@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
     int warp = threadIdx.x >> 5;
     int lane = threadIdx.x & 31;
     int rep = blockIdx.x * L.warps_per_block + warp;
-    if (rep >= L.n_rep) return;
+    if (rep >= L.n_rep || (L.only_rep >= 0 && rep != L.only_rep)) return;
     unsigned char* base = smem + (size_t)warp * warp_bytes<C>();
     ldo::Rep<C>* R = reinterpret_cast<ldo::Rep<C>*>(base);
     unsigned char* gbase = L.arena + (size_t)rep * sizeof(LdoState<C>);

@@ -19,6 +19,7 @@ struct LdoLaunch {
     unsigned char* snap;
     LdoLayout lay;
     int n_rep;
+    int only_rep;                // >= 0: only this replica runs (configuration import)
     int warps_per_block;
     int smem_pad;                // extra dynamic shared memory per block (occupancy tuning)
     int mode;

@@ -23,7 +23,8 @@ EXPORTS = [
     "ldo_learn_collect", "ldo_learn_reset_counts", "ldo_learn_get_counts", "ldo_learn_train", "ldo_learn_set_params",
     "ldo_learn_get_params", "ldo_learn_get_table", "ldo_learn_set_table", "ldo_learn_loss_grad",
     "ldo_writer_open", "ldo_writer_write", "ldo_writer_close", "ldo_pt2d_run", "ldo_engine_exp",
-    "ldo_set_bias_centre", "ldo_swap_writer_open",
+    "ldo_set_bias_centre", "ldo_swap_writer_open", "ldo_set_config", "ldo_read_trj_frame", "ldo_checkpoint_save",
+    "ldo_checkpoint_load",
 ]
 
 LEARN_TABLE = 524544      # network inputs: 524288 insertion + 256 regrowth-direction (ldo_learn.h)
@@ -73,6 +74,11 @@ def load_library(path=None):
     lib.ldo_state_bytes.argtypes = [vp]
     lib.ldo_get_observables.argtypes = [vp, ctypes.POINTER(Observables), ip]
     lib.ldo_get_config.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int32), ip, ctypes.POINTER(ctypes.c_int)]
+    lib.ldo_set_config.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int32), ip]
+    lib.ldo_read_trj_frame.argtypes = [ctypes.c_char_p, ip, ctypes.POINTER(ctypes.c_int32), ip,
+                                       ctypes.POINTER(ctypes.c_int)]
+    lib.ldo_checkpoint_save.argtypes = [vp, ctypes.c_char_p]
+    lib.ldo_checkpoint_load.argtypes = [vp, ctypes.c_char_p]
     lib.ldo_set_sampling.argtypes = [vp, ip, ip]
     lib.ldo_get_samples.argtypes = [vp, ctypes.POINTER(ctypes.c_int16), ip, ctypes.POINTER(ctypes.c_int)]
     lib.ldo_set_trace.argtypes = [vp, ip, ip]
@@ -182,6 +188,17 @@ class Engine:
         n = ctypes.c_int(0)
         self._check(self.lib.ldo_get_config(self.h, replica, buf, cap, ctypes.byref(n)))
         return list(buf[:n.value])
+
+    def set_config(self, replica, flat):
+        """Replaces a replica's configuration (ldo_get_config's flat format)."""
+        buf = (ctypes.c_int32 * len(flat))(*flat)
+        self._check(self.lib.ldo_set_config(self.h, replica, buf, len(flat)))
+
+    def save_checkpoint(self, path):
+        self._check(self.lib.ldo_checkpoint_save(self.h, os.fsencode(path)))
+
+    def load_checkpoint(self, path):
+        self._check(self.lib.ldo_checkpoint_load(self.h, os.fsencode(path)))
 
     def set_trace(self, n_trace, max_steps):
         self._check(self.lib.ldo_set_trace(self.h, n_trace, max_steps))
@@ -354,6 +371,18 @@ def learn_loss_grad(params, idx, cnt_bound, cnt_total):
     if rc != 0:
         raise LdoError(rc, lib.ldo_last_error(None).decode())
     return loss.value, grad
+
+
+def read_trj_frame(path, frame):
+    """Frame `frame` of a .trj file in ldo_get_config's flat format (host only)."""
+    lib = load_library()
+    cap = 1 << 20
+    buf = (ctypes.c_int32 * cap)()
+    n = ctypes.c_int(0)
+    rc = lib.ldo_read_trj_frame(os.fsencode(path), frame, buf, cap, ctypes.byref(n))
+    if rc != 0:
+        raise LdoError(rc, lib.ldo_last_error(None).decode())
+    return list(buf[:n.value])
 
 
 def engine_exp(x):

@@ -55,8 +55,10 @@ Replica* build(const char* inp_path, const char* overrides, uint32_t seed, uint3
                 ldo_io::set_param(p, ldo_io::trim(line.substr(0, eq)), ldo_io::trim(line.substr(eq + 1)));
             }
         }
-        if (!p.restart_traj_file.empty()) throw std::runtime_error("restart_traj_file is not supported by the oracle");
         r->sf = ldo_io::read_system(ldo_io::resolve(p, p.origami_input_filename));
+        // setup_origami (src/origami_system.cpp:1000-1003)
+        if (!p.restart_traj_file.empty())
+            r->sf.chains = ldo_io::read_trj_frame(ldo_io::resolve(p, p.restart_traj_file), p.restart_step);
         if (p.domain_type != "HalfTurn" && p.domain_type != "ThreeQuarterTurn")
             throw std::runtime_error(p.domain_type + ": No such domain type");
         if (p.binding_pot != "FourBody") throw std::runtime_error(p.binding_pot + ": No such binding potential");

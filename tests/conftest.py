@@ -22,3 +22,12 @@ def data_dir():
 
 def inp(name):
     return os.path.join(DATA, name + ".inp")
+
+
+def golden_overrides(fx):
+    """The .inp lines a golden fixture's run adds to its case: a restart from
+    frame `frame` of a reference-written trajectory under golden/outputs."""
+    if "restart" not in fx:
+        return ""
+    trj, frame = fx["restart"]
+    return "restart_traj_file=%s\nrestart_step=%d\n" % (os.path.join(GOLDEN, "outputs", trj), frame)

@@ -84,6 +84,35 @@ def enumerate_c1(tmp):
     print(path, weights)
 
 
+# restarts from a frame of a reference-written trajectory (restart_traj_file /
+# restart_step, src/origami_system.cpp:1000): case, trajectory under
+# outputs/, frame, seed, steps
+RESTART_RUNS = [("g24a", "g24a_s3.trj", 3, 21, 10000), ("c3", "c3_s8.trj", 4, 22, 10000),
+                ("g24b", "g24b_s4.trj", 0, 23, 10000)]
+
+
+def restart_overrides(trj, frame):
+    """The .inp lines of a restart from frame `frame` of outputs/<trj>."""
+    return "restart_traj_file=%s\nrestart_step=%d\n" % (os.path.join(HERE, "outputs", trj), frame)
+
+
+def make_restarts(tmp, only=None):
+    for case, trj, frame, seed, steps in RESTART_RUNS:
+        if only and case not in only:
+            continue
+        inp = systems.write_case(tmp, case)
+        with open(inp, "a") as f:
+            f.write(restart_overrides(trj, frame))
+        d = ref_trace(inp, seed, steps)
+        fx = {"case": case, "seed": seed, "steps": steps, "restart": [trj, frame],
+              "initial_energy": d["initial_energy"], "trace": d["steps"], "final_config": flatten(d["dumps"][-1][1]),
+              "draws": d["draws"]}
+        path = os.path.join(HERE, "%s_r%d_s%d.json.gz" % (case, frame, seed))
+        with gzip.open(path, "wt") as f:
+            json.dump(fx, f)
+        print(path, len(d["steps"]), "steps, draws", d["draws"])
+
+
 # reference output files: case, seed, steps, write frequency
 OUTPUT_RUNS = [("g24a", 3, 2000, 400), ("g24b", 4, 2000, 400), ("c3", 8, 2000, 400)]
 OUTPUT_EXTS = [".vsf", ".trj", ".vcf", ".states", ".ores", ".counts", ".staples", ".staplestates", ".ene", ".ops"]
@@ -127,6 +156,7 @@ def main(only=None):
         if not only or "c1" in only:
             enumerate_c1(tmp)
         make_outputs(tmp, only)
+        make_restarts(tmp, only)
 
 
 if __name__ == "__main__":

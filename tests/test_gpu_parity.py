@@ -10,7 +10,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, inp
+from conftest import GOLDEN, golden_overrides, inp
 from oracle_lib import OracleReplica
 
 pytestmark = pytest.mark.gpu
@@ -53,7 +53,7 @@ def test_engine_matches_reference_golden(path):
     with gzip.open(path, "rt") as f:
         fx = json.load(f)
     steps = fx["steps"]
-    eng = engine(inp(fx["case"]), n_replicas=1, seed=fx["seed"])
+    eng = engine(inp(fx["case"]), n_replicas=1, seed=fx["seed"], overrides=golden_overrides(fx))
     eng.set_trace(1, steps)
     eng.run(steps)
     tr = eng.trace()[0]

@@ -15,7 +15,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, inp
+from conftest import GOLDEN, golden_overrides, inp
 from oracle_lib import OracleReplica
 
 FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "*.json.gz")))
@@ -29,7 +29,7 @@ def load(path):
 @pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p)[:-8] for p in FIXTURES])
 def test_oracle_matches_reference_trace(path):
     fx = load(path)
-    o = OracleReplica(inp(fx["case"]), seed=fx["seed"], replica=0)
+    o = OracleReplica(inp(fx["case"]), seed=fx["seed"], replica=0, overrides=golden_overrides(fx))
     o.set_reference_arithmetic(True)
     tr = o.run(fx["steps"])
     ref = np.array(fx["trace"], dtype=np.float64)
@@ -59,7 +59,7 @@ FP64_EXACT = [p for p in FIXTURES if not p.endswith("s24a_s11.json.gz")]
 @pytest.mark.parametrize("path", FP64_EXACT, ids=[os.path.basename(p)[:-8] for p in FP64_EXACT])
 def test_oracle_fp64_weights_match_reference_trace(path):
     fx = load(path)
-    o = OracleReplica(inp(fx["case"]), seed=fx["seed"], replica=0)
+    o = OracleReplica(inp(fx["case"]), seed=fx["seed"], replica=0, overrides=golden_overrides(fx))
     tr = o.run(fx["steps"])
     ref = np.array(fx["trace"], dtype=np.float64)
     np.testing.assert_array_equal(tr[:, [0, 2, 3, 4, 5, 7]], ref[:, [0, 2, 3, 4, 5, 7]])
@@ -74,7 +74,7 @@ def test_fp64_weights_part_from_long_double_only_at_a_tie():
     the acceptance test; the runs agree exactly up to that step."""
     fx = load(os.path.join(GOLDEN, "s24a_s11.json.gz"))
     ref = np.array(fx["trace"], dtype=np.float64)
-    o = OracleReplica(inp(fx["case"]), seed=fx["seed"], replica=0)
+    o = OracleReplica(inp(fx["case"]), seed=fx["seed"], replica=0, overrides=golden_overrides(fx))
     tr = o.run(fx["steps"])
     k = 19884
     np.testing.assert_array_equal(tr[:k], ref[:k])
