@@ -1921,9 +1921,10 @@ struct Rep : public LdoState<C> {
         if (ct == type && (int)sys->comp_dom[sd[g]] == d) q += 1.0 - LDO_LEARN_EPS_T;
         return q;
     }
-    // Sum over the domains of chain cs bound to another chain of
-    // q(partner) q(type, domain | partner).
-    __device__ __noinline__ double learn_forward(int cs, int type, double z, int n_sites, int fresh) const {
+    // Sum over the domains d of chain cs bound to another chain of
+    // q(partner) q(type, d | partner) G(d), G(d) the growth factor of the
+    // chain's other domains grown from d (lr_q_old with scale 36).
+    __device__ __noinline__ double learn_forward(int cs, int type, double z, int n_sites, int fresh) {
         double f = 0;
         int len = chain_len(cs);
         #pragma unroll 1
@@ -1931,7 +1932,7 @@ struct Rep : public LdoState<C> {
             int b = slot_of(cs, d);
             int p = bnd[b];
             if (p < 0 || scs[p] == cs) continue;
-            f += learn_q_target(p, z, n_sites, fresh) * learn_q_type(p, type, d);
+            f += learn_q_target(p, z, n_sites, fresh) * learn_q_type(p, type, d) * lr_q_old(cs, d, 36.0);
         }
         return f;
     }
@@ -1989,7 +1990,7 @@ struct Rep : public LdoState<C> {
         int gnew = slot_of(cs, gi);
         delta_e += set_growth_point(gnew, g);
         if (rejected || bad()) return false;
-        grow_staple(gi, cs, false);
+        lr_grow(cs, gi);
         if (rejected || bad()) return false;
         #pragma unroll 1
         for (int d = 0; d < len; ++d)
@@ -2035,8 +2036,10 @@ struct Rep : public LdoState<C> {
         #pragma unroll 1
         for (int d = 0; d < len; ++d)
             if (st[slot_of(cs, d)] == BOUND) { staple_bound = true; break; }
-        // growth-point alternatives of the reverse insertion: (domain, partner)
+        // growth-point alternatives of the reverse insertion: (domain,
+        // partner) and the growth factor of the other domains from there
         int na = 0;
+        double gf[LDO_MAX_LEN];
         #pragma unroll 1
         for (int d = 0; d < len; ++d) {
             int b = slot_of(cs, d);
@@ -2044,8 +2047,10 @@ struct Rep : public LdoState<C> {
             if (p < 0 || scs[p] == cs) continue;
             m.bd_new[na] = d;
             m.bd_old[na] = p;
+            gf[na] = lr_q_old(cs, d, 36.0);
             na++;
         }
+        if (bad()) return false;
         unassign_domains(cs);
         if (mean_field) delta_e -= log6;
         delta_e -= t_init_e;
@@ -2058,7 +2063,7 @@ struct Rep : public LdoState<C> {
         double f = 0;
         #pragma unroll 1
         for (int a = 0; a < na; ++a)
-            f += learn_q_target(m.bd_old[a], z, n_sites, -1) * learn_q_type(m.bd_old[a], type, m.bd_new[a]);
+            f += learn_q_target(m.bd_old[a], z, n_sites, -1) * learn_q_type(m.bd_old[a], type, m.bd_new[a]) * gf[a];
         int ni = type_count[type];
         double pratio = (double)ni * 6.0 * boltz;
         pratio *= (double)S * f;
@@ -2121,8 +2126,9 @@ struct Rep : public LdoState<C> {
     }
     // Q(old): the proposal probability of growing the current configuration
     // of staple cs from its domain d0, evaluated in the partial states of
-    // that growth without building them.
-    __device__ __noinline__ double lr_q_old(int cs, int d0) {
+    // that growth without building them: the product over the grown domains
+    // of scale q(v) q(o | v).
+    __device__ __noinline__ double lr_q_old(int cs, int d0, double scale) {
         int len = chain_len(cs);
         unsigned placed = 1u << d0;
         double q = 1;
@@ -2154,8 +2160,34 @@ struct Rep : public LdoState<C> {
                 double qo = ob[v] >= 0 ? (o == ob[v] ? (1.0 - LDO_LEARN_EPS_O) + LDO_LEARN_EPS_O / 6.0
                                                      : LDO_LEARN_EPS_O / 6.0)
                                        : 1.0 / 6.0;
-                q *= qv * qo;
+                q *= scale * (qv * qo);
                 placed |= 1u << di;
+            }
+        }
+        return q;
+    }
+    // Grows the domains of staple cs other than its placed domain d0 with
+    // the learned direction proposal (forward to the chain's end, then
+    // backward to its start, as grow_staple does); returns the product of the
+    // proposal probabilities, or sets rejected on a constraint violation.
+    __device__ __noinline__ double lr_grow(int cs, int d0) {
+        double q = 1;
+        int len = chain_len(cs);
+        #pragma unroll 1
+        for (int pass = 0; pass < 2; ++pass) {
+            int dir = pass == 0 ? 1 : -1;
+            int n = pass == 0 ? len - d0 : d0 + 1;
+            #pragma unroll 1
+            for (int k = 1; k < n; ++k) {
+                int i = slot_of(cs, d0 + dir * k), prev = slot_of(cs, d0 + dir * (k - 1));
+                int v = 0, o = 0;
+                q *= lr_propose(i, prev, true, &v, &o);
+                delta_e += set_domain_config(i, add(pos(prev), unit(v)), o);
+                if (hdr.violated) {
+                    rejected = true;
+                    return 0;
+                }
+                if (bad()) return 0;
             }
         }
         return q;
@@ -2171,29 +2203,12 @@ struct Rep : public LdoState<C> {
         int g = rng.uniform_int(0, m.n_bd - 1);
         int gnew = m.bd_new[g], gold = m.bd_old[g];
         int d0 = sd[gnew];
-        double q_old = lr_q_old(cs, d0);
+        double q_old = lr_q_old(cs, d0, 1.0);
         unassign_domains(cs);
         delta_e += set_growth_point(gnew, gold);
         if (rejected || bad()) return false;
-        double q_new = 1;
-        int len = chain_len(cs);
-        #pragma unroll 1
-        for (int pass = 0; pass < 2; ++pass) {
-            int dir = pass == 0 ? 1 : -1;
-            int n = pass == 0 ? len - d0 : d0 + 1;
-            #pragma unroll 1
-            for (int k = 1; k < n; ++k) {
-                int i = slot_of(cs, d0 + dir * k), prev = slot_of(cs, d0 + dir * (k - 1));
-                int v = 0, o = 0;
-                q_new *= lr_propose(i, prev, true, &v, &o);
-                delta_e += set_domain_config(i, add(pos(prev), unit(v)), o);
-                if (hdr.violated) {
-                    rejected = true;
-                    return false;
-                }
-                if (bad()) return false;
-            }
-        }
+        double q_new = lr_grow(cs, d0);
+        if (rejected || bad()) return false;
         add_external_bias_met();
         int nbd = num_bound_staple_domains(cs);
         double boltz = dexp(-(delta_e));

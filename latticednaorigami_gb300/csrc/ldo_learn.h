@@ -11,6 +11,8 @@
 // neighbour by what the site holds (empty / an unbound domain complementary
 // to the growing one / another unbound domain / a bound pair) and the
 // temperature bin (LDO_LEARN_DIRS entries after the insertion entries).
+// LearnedStapleRegrowth grows staples with these directions, and so does
+// LearnedStapleExchange after placing an inserted staple's growth point.
 // The input space is finite (LDO_LEARN_TABLE entries), so the network is
 // evaluated once for every input on the tensor cores and the MC kernel reads
 // the weights from that table: the proposals are exact functions of the

@@ -1560,8 +1560,19 @@ class System {
         int gnew = ch[gi];
         delta_e += set_growth_point(gnew, g);
         if (rejected) return false;
-        grow_staple(doms[gnew].d, ch, false);
-        if (rejected) return false;
+        // the other domains grown with the learned direction proposal
+        for (auto& gk : growth_order(gi, (int)ch.size())) {
+            int i = ch[gk.first], prev = ch[gk.second];
+            int v = 0;
+            V3 o;
+            lr_propose(i, prev, true, v, o);
+            delta_e += set_domain_config(i, doms[prev].pos + kUnit[v], o);
+            if (violated) {
+                rejected = true;
+                return false;
+            }
+            assigned.push_back(key_of(i));
+        }
         std::vector<int> st = get_chain(c_i);
         for (int id : st)
             if (doms[id].state == BOUND) { staple_bound = true; break; }
@@ -1570,7 +1581,7 @@ class System {
             int b = st[d];
             int p = doms[b].bound;
             if (p < 0 || doms[p].c == c_i) continue;
-            f += learn_q_target(p, z, n_sites, c_i) * learn_q_type(p, ident, (int)d);
+            f += learn_q_target(p, z, n_sites, c_i) * learn_q_type(p, ident, (int)d) * lr_growth_literal(st, (int)d);
         }
         add_external_bias_met();
         double boltz = xexp(-delta_e);
@@ -1595,10 +1606,12 @@ class System {
         for (int id : st)
             if (doms[id].state == BOUND) { staple_bound = true; break; }
         std::vector<std::pair<int, int>> alt;   // (domain index, partner)
+        std::vector<double> gf;                 // growth factor from that domain
         for (size_t d = 0; d < st.size(); ++d) {
             int p = doms[st[d]].bound;
             if (p < 0 || doms[p].c == c_i) continue;
             alt.push_back({(int)d, p});
+            gf.push_back(lr_growth_literal(st, (int)d));
         }
         unassign_domains(st);
         if (cfg.mean_field) delta_e -= std::log(6);
@@ -1610,7 +1623,9 @@ class System {
         int n_sites = insertion_sites - (int)st.size();
         double z = learn_z();
         double f = 0;
-        for (auto& a : alt) f += learn_q_target(a.second, z, n_sites, -1) * learn_q_type(a.second, ident, a.first);
+        for (size_t a = 0; a < alt.size(); ++a)
+            f += learn_q_target(alt[a].second, z, n_sites, -1) * learn_q_type(alt[a].second, ident, alt[a].first) *
+                 gf[a];
         int ni = num_staples_of_ident(ident);
         double pratio = (double)ni * 6.0 * boltz;
         pratio *= (double)S * f;
@@ -1677,6 +1692,47 @@ class System {
         double qo = hob[v] ? (o == ob[v] ? (1.0 - LDO_LEARN_EPS_O) + LDO_LEARN_EPS_O / 6.0 : LDO_LEARN_EPS_O / 6.0)
                            : 1.0 / 6.0;
         return qv * qo;
+    }
+    // Growth order of a staple of len domains from domain d0, as grow_staple
+    // grows it: (domain index, previous domain index), forward to the end,
+    // then backward to the start.
+    static std::vector<std::pair<int, int>> growth_order(int d0, int len) {
+        std::vector<std::pair<int, int>> g;
+        for (int k = d0 + 1; k < len; ++k) g.push_back({k, k - 1});
+        for (int k = d0 - 1; k >= 0; --k) g.push_back({k, k + 1});
+        return g;
+    }
+    // Growth factor of staple st grown from its domain d0 by the learned
+    // direction proposal: the product over the grown domains of 36 q(v) q(o|v)
+    // (36: the uniform growth's 1/36 per domain), evaluated literally by
+    // removing the other domains and setting them again one by one in growth
+    // order.  The state, energy and counters are left as they were.
+    double lr_growth_literal(const std::vector<int>& st, int d0) {
+        double e0 = energy;
+        int nst0 = num_stacked, nu0 = num_unassigned;
+        int len = (int)st.size();
+        std::vector<V3> p(len), o(len);
+        for (int k = 0; k < len; ++k) {
+            p[k] = doms[st[k]].pos;
+            o[k] = doms[st[k]].ore;
+        }
+        auto order = growth_order(d0, len);
+        for (size_t n = order.size(); n-- > 0;) unassign_domain(st[order[n].first]);
+        double g = 1;
+        for (auto& gk : order) {
+            int i = st[gk.first], prev = st[gk.second];
+            V3 dv = p[gk.first] - doms[prev].pos;
+            int v = 0;
+            while (v < 6 && !(kUnit[v] == dv)) ++v;
+            if (v == 6) throw std::runtime_error("staple configuration is not a chain of neighbours");
+            V3 ov = o[gk.first];
+            g *= 36.0 * lr_propose(i, prev, false, v, ov);
+            set_checked(i, p[gk.first], o[gk.first]);
+        }
+        energy = e0;
+        num_stacked = nst0;
+        num_unassigned = nu0;
+        return g;
     }
     bool learned_regrowth() {
         if (num_staples == 0) return false;
