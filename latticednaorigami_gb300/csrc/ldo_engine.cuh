@@ -1897,13 +1897,63 @@ struct Rep : public LdoState<C> {
         return qv * qo;
     }
     // Z over the unbound scaffold domains, in scaffold order.
-    __device__ __noinline__ double learn_z() const {
+    // Weights of the unbound scaffold domains in scaffold order.  With pick
+    // null: their sum Z.  Otherwise: the first domain at which the running
+    // sum exceeds target goes to *pick (the last unbound domain if rounding
+    // leaves target at or above Z, -1 if none is unbound).  The scaffold's
+    // domains hold slots 0..ns-1 in chain order, so the neighbour codes of
+    // learn_weight are kept in a sliding window instead of being looked up
+    // four times per domain; the sums are the same, term by term.
+    __device__ __noinline__ double learn_scan(double target, int* pick) const {
+        if (ns < 5) {
+            double z = 0;
+            int last = -1;
+            #pragma unroll 1
+            for (int g = 0; g < ns; ++g) {
+                if (st[g] != UNBOUND) continue;
+                z += learn_weight(g, -1);
+                last = g;
+                if (pick && target < z) {
+                    *pick = g;
+                    return z;
+                }
+            }
+            if (pick) *pick = last;
+            return z;
+        }
+        bool cyc = sys->cyclic;
+        auto code_at = [&](int x) {
+            if (x < 0 || x >= ns) {
+                if (!cyc) return 0;
+                x = x < 0 ? x + ns : x - ns;
+            }
+            return learn_code(x, -1);
+        };
+        int cm2 = code_at(-2), cm1 = code_at(-1), c0 = code_at(0), cp1 = code_at(1), cp2 = code_at(2);
+        const double* tab = learn_w + ldo_learn_index(learn_tb, 0, 0);
         double z = 0;
+        int last = -1;
         #pragma unroll 1
-        for (int g = 0; g < ns; ++g)
-            if (st[g] == UNBOUND) z += learn_weight(g, -1);
+        for (int g = 0; g < ns; ++g) {
+            if (st[g] == UNBOUND) {
+                int combo = cm2 | (cm1 << 2) | (cp1 << 4) | (cp2 << 6);
+                z += __ldg(tab + (int)sys->learn_tslot[g] * LDO_LEARN_NCOMBO + combo);
+                last = g;
+                if (pick && target < z) {
+                    *pick = g;
+                    return z;
+                }
+            }
+            cm2 = cm1;
+            cm1 = c0;
+            c0 = cp1;
+            cp1 = cp2;
+            cp2 = code_at(g + 3);
+        }
+        if (pick) *pick = last;
         return z;
     }
+    __device__ double learn_z() const { return learn_scan(0.0, nullptr); }
     // q(g) for a target that was unbound in the state the proposal is made in.
     __device__ double learn_q_target(int g, double z, int n_sites, int fresh) const {
         if (z == 0) return 1.0 / n_sites;
@@ -1948,19 +1998,7 @@ struct Rep : public LdoState<C> {
         }
         else {
             double target = rng.uniform_real() * z;
-            double cum = 0;
-            int last = -1;
-            #pragma unroll 1
-            for (int x = 0; x < ns; ++x) {
-                if (st[x] != UNBOUND) continue;
-                cum += learn_weight(x, -1);
-                last = x;
-                if (target < cum) {
-                    g = x;
-                    break;
-                }
-            }
-            if (g < 0) g = last;   // rounding left target >= Z
+            learn_scan(target, &g);
         }
         if (g < 0) {
             fail(LDO_RS_INVARIANT);
