@@ -168,6 +168,15 @@ def measured_peaks():
 
 
 CPU_REPS_PER_SIZE = 128
+# Equilibration.  From empty scaffolds the plain sampler relaxes over hundreds
+# of sweeps (low temperatures, large scaffolds slowest), and tau_int of a
+# series that still drifts is inflated.  The GPU arms therefore start from
+# configurations relaxed for RELAX_SWEEPS sweeps by the learned moveset (which
+# samples the same distribution: tests against the exact enumeration and the
+# plain sampler), the CPU arms from CPU_BURN_SWEEPS sweeps of their own plain
+# sampler; every arm then records only stationary sweeps.
+RELAX_SWEEPS = 2000
+CPU_BURN_SWEEPS = 3000
 LEARN_ITERS = 400
 LEARN_LR = 2e-3
 
@@ -194,21 +203,24 @@ def replica_temps():
 def cpu_effective_rate(files, cores, burn_sweeps, rec_sweeps):
     """The oracle port on all host cores over a bounded sample of the same
     workload: CPU_REPS_PER_SIZE replicas of each scaffold size at the
-    temperatures of the first replicas of that size in the GPU run, the same
-    burn-in and recorded sweeps as the GPU run, tau_int estimated from its own
-    samples by the same estimator.  Only the recorded sweeps are timed
-    (pro rata).  Returns (effective samples/s, sweeps/s, median tau)."""
+    temperatures of the first replicas of that size in the GPU run, burn_sweeps
+    of burn-in from the empty scaffold, then the recorded sweeps, tau_int
+    estimated from its own samples by the same estimator.  Only the recorded
+    sweeps are timed (pro rata).  Returns (effective samples/s, sweeps/s,
+    median tau, mean fully bound domains per scaffold size)."""
     from oracle_lib import run_batch_sampled
     from latticednaorigami_gb300.analysis import effective_samples
     temps = replica_temps()
     per = N_REP // len(SIZES)
     ess_total, t_total, sweeps_total = 0.0, 0.0, 0.0
     taus = []
+    means = {}
     for i, f in enumerate(files):
         n = SIZES[i]
         tt = temps[i * per:i * per + CPU_REPS_PER_SIZE]
         t, smp = run_batch_sampled(f, 0, CPU_REPS_PER_SIZE, burn_sweeps + rec_sweeps, n, cores, temps=tt)
         rec = smp[:, burn_sweeps:]
+        means[n] = float(rec.mean())
         ess, tau = effective_samples(list(rec))
         frac = rec_sweeps / float(burn_sweeps + rec_sweeps)
         ess_total += ess
@@ -216,16 +228,17 @@ def cpu_effective_rate(files, cores, burn_sweeps, rec_sweeps):
         sweeps_total += CPU_REPS_PER_SIZE * rec_sweeps
         if tau is not None:
             taus.append(tau)
-    return ess_total / t_total, sweeps_total / t_total, (float(np.median(taus)) if taus else None)
+    return ess_total / t_total, sweeps_total / t_total, (float(np.median(taus)) if taus else None), means
 
 
 def cpu_baseline(files, burn_sweeps, rec_sweeps):
     cores = os.cpu_count() or 1
-    rate, sweeps_per_s, tau = cpu_effective_rate(files, cores, burn_sweeps, rec_sweeps)
+    rate, sweeps_per_s, tau, means = cpu_effective_rate(files, cores, burn_sweeps, rec_sweeps)
     return {"value": rate, "unit": "effective samples/s", "cores": cores, "kind": "port",
             "sample": "%d replicas of each scaffold size (GPU-run temperatures) x %d recorded sweeps after %d "
-                      "burn-in, %d threads" % (CPU_REPS_PER_SIZE, rec_sweeps, burn_sweeps, cores),
-            "sweeps_per_s": sweeps_per_s, "tau_int_median": tau}
+                      "burn-in sweeps from the empty scaffold, %d threads"
+                      % (CPU_REPS_PER_SIZE, rec_sweeps, burn_sweeps, cores),
+            "sweeps_per_s": sweeps_per_s, "tau_int_median": tau, "mean_fully_bound_by_size": means}
 
 
 def run_reference_arm(args):
@@ -237,11 +250,11 @@ def run_reference_arm(args):
     from oracle_lib import run_batch
     for _ in range(args.warmup):
         run_batch(files[0], 0, cores, 20 * SIZES[0], cores)
-    burn, rec = args.warmup * SWEEPS_PER_STEP, args.steps * SWEEPS_PER_STEP
+    burn, rec = CPU_BURN_SWEEPS, args.steps * SWEEPS_PER_STEP
     rates, sps, taus, times = [], [], [], []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        r, s_, tau = cpu_effective_rate(files, cores, burn, rec)
+        r, s_, tau, _ = cpu_effective_rate(files, cores, burn, rec)
         times.append(time.perf_counter() - t0)
         rates.append(r)
         sps.append(s_)
@@ -256,7 +269,8 @@ def run_reference_arm(args):
                                    "proposal)"},
             "cpu_baseline": {"value": value, "unit": "effective samples/s", "cores": cores, "kind": "port",
                              "sample": "%d replicas of each scaffold size (GPU-run temperatures) x %d recorded "
-                                       "sweeps after %d burn-in per step" % (CPU_REPS_PER_SIZE, rec, burn)},
+                                       "sweeps after %d burn-in sweeps from the empty scaffold, per step"
+                                       % (CPU_REPS_PER_SIZE, rec, burn)},
             "e2e": {"value": value, "unit": "effective samples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "sweeps_per_s": float(np.mean(sps)), "tau_int_median": taus[-1]}
@@ -433,13 +447,50 @@ def main():
     ns_of = np.array(SIZES)[sys_of]
     total_sweeps = args.steps * SWEEPS_PER_STEP
 
-    def timed_arm(overrides, table, collect):
-        """W warm-up launches, then K timed launches of SWEEPS_PER_STEP sweeps
-        with one numfulldomains sample per replica per sweep."""
+    def collect_and_train(eng):
+        """Network inputs and labels from 10 states 10 sweeps apart, then
+        LEARN_ITERS Adam steps (untimed)."""
+        for _ in range(10):
+            eng.run_sweeps(10)
+            eng.learn_collect()
+        t0 = time.perf_counter()
+        loss0, loss1 = eng.learn_train(LEARN_ITERS, lr=LEARN_LR, seed=0)
+        return {"loss_first": loss0, "loss_last": loss1, "iters": LEARN_ITERS,
+                "train_s": time.perf_counter() - t0, "table": eng.learn_table()}
+
+    def relax():
+        """Stationary starting configurations: a first network trained on a
+        short plain run from the empty scaffolds, RELAX_SWEEPS sweeps of the
+        learned moveset with it, the network trained again on those states."""
+        e0 = Engine(files, n_replicas=N_REP, seed=500 + ranks.rank, sys_of_replica=sys_of.tolist())
+        e0.set_controls(temps=temps)
+        for _ in range(3):
+            e0.run_sweeps(SWEEPS_PER_STEP)
+        table0 = collect_and_train(e0)["table"]
+        e0.close()
+        e1 = Engine(files, n_replicas=N_REP, seed=600 + ranks.rank, sys_of_replica=sys_of.tolist(),
+                    overrides=learned_over)
+        e1.set_controls(temps=temps)
+        e1.learn_set_table(table0)
+        for _ in range(RELAX_SWEEPS // SWEEPS_PER_STEP):
+            e1.run_sweeps(SWEEPS_PER_STEP)
+        train = collect_and_train(e1)
+        start = [e1.config(r) for r in range(N_REP)]
+        e1.close()
+        return start, train
+
+    start, train = relax()
+
+    def timed_arm(overrides, table):
+        """From the relaxed configurations: W warm-up launches, then K timed
+        launches of SWEEPS_PER_STEP sweeps with one numfulldomains sample per
+        replica per sweep."""
         eng = Engine(files, n_replicas=N_REP, seed=ranks.rank, sys_of_replica=sys_of.tolist(), overrides=overrides)
         eng.set_controls(temps=temps)
         if table is not None:
             eng.learn_set_table(table)
+        for r in range(N_REP):
+            eng.set_config(r, start[r])
         eng.set_sampling(1, total_sweeps)
         for _ in range(args.warmup):
             eng.run_sweeps(SWEEPS_PER_STEP)
@@ -455,25 +506,16 @@ def main():
         series = [smp[r, :cnt[r], 0] for r in range(N_REP)]
         ess, tau_med = effective_samples(series)
         ess = ranks.sum(ess)
-        taus = {}
+        taus, means = {}, {}
         for i, n in enumerate(SIZES):
             ts = [tau_int(series[r]) for r in range(i * per, (i + 1) * per)]
             ts = [t for t in ts if t is not None]
             taus[n] = float(np.median(ts)) if ts else None
-        train = None
-        if collect:
-            # training data for the proposal network from the plain sampler (untimed)
-            for _ in range(10):
-                eng.run_sweeps(10)
-                eng.learn_collect()
-            t0 = time.perf_counter()
-            loss0, loss1 = eng.learn_train(LEARN_ITERS, lr=LEARN_LR, seed=0)
-            train = {"loss_first": loss0, "loss_last": loss1, "iters": LEARN_ITERS,
-                     "train_s": time.perf_counter() - t0, "table": eng.learn_table()}
+            means[n] = float(np.mean(np.concatenate(series[i * per:(i + 1) * per])))
         st = eng.move_stats(3)
         acc = [float(st[k, 1]) / max(1.0, float(st[k, 0])) for k in range(3)]
         return {"eng": eng, "dev_ms": dev_ms, "t_dev": t_dev, "ess": ess, "tau_med": tau_med, "taus": taus,
-                "clk": clk, "train": train, "acc": acc}
+                "means": means, "clk": clk, "acc": acc}
 
     def e2e_arm(overrides, table):
         """The same loop through the C ABI with host buffers: temperatures in,
@@ -483,6 +525,8 @@ def main():
         eng2.set_controls(temps=temps)
         if table is not None:
             eng2.learn_set_table(table)
+        for r in range(N_REP):
+            eng2.set_config(r, start[r])
         eng2.set_sampling(1, SWEEPS_PER_STEP)
         for _ in range(args.warmup):
             eng2.run_sweeps(SWEEPS_PER_STEP)
@@ -502,9 +546,9 @@ def main():
         e2e_ess, _ = effective_samples([np.concatenate(x) for x in e2e_series])
         return ranks.sum(e2e_ess) / t_e2e
 
-    plain = timed_arm("", None, collect=True)
-    table = plain["train"]["table"]
-    learned = timed_arm(learned_over, table, collect=False)
+    table = train["table"]
+    plain = timed_arm("", None)
+    learned = timed_arm(learned_over, table)
     value = learned["ess"] / learned["t_dev"]
     plain_value = plain["ess"] / plain["t_dev"]
     e2e_learned = e2e_arm(learned_over, table)
@@ -531,10 +575,10 @@ def main():
         return {"value": arm["ess"] / t, "sweeps_per_s": W * N_REP * total_sweeps / t,
                 "move_attempts_per_s": W * float(np.sum(ns_of)) * total_sweeps / t,
                 "ms_per_step": float(np.mean(arm["dev_ms"])), "tau_int_median": arm["tau_med"],
-                "tau_int_by_size": arm["taus"],
+                "tau_int_by_size": arm["taus"], "mean_fully_bound_by_size": arm["means"],
                 "acceptance": {"exchange": arm["acc"][0], "regrowth": arm["acc"][1], "cb_regrowth": arm["acc"][2]}}
 
-    tr = plain["train"]
+    tr = train
     line = {"metric": "effective samples/s (tau_int of #bound domains), learned vs plain MC", "value": value,
             "unit": "effective samples/s", "n_gpus": ranks.world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": float(np.mean(dev_ms)), "higher_is_better": True, "scaling": "weak",
@@ -545,13 +589,11 @@ def main():
                                    "exchange + Met regrowth + CB regrowth (plain)",
                        "sweeps_per_step": SWEEPS_PER_STEP, "replicas": N_REP * ranks.world,
                        "replicas_per_gpu": N_REP, "parallelism": "replicas only, one process per GPU",
+                       "start": "both arms from the same configurations, relaxed %d sweeps by the learned "
+                                "moveset, then %d warm-up sweeps" % (RELAX_SWEEPS, args.warmup * SWEEPS_PER_STEP),
                        "l2": "state resident in shared memory; no L2 flush needed"},
             "learned": rates(learned), "plain": rates(plain),
             "learned_over_plain": value / plain_value,
-            # the two arms' recorded sweeps start 300 sweeps after empty
-            # lattices, too short for plain MC to forget its start (its tau_int
-            # is tens of sweeps); the equality of the sampled distributions is
-            # tested on equilibrated runs instead
             "distribution_check": "tests/test_gpu_learned.py::test_learned_distribution_matches_plain_on_c2",
             "network": {"layers": "64-256-256-256-1 GELU, bf16 weights/activations, fp32 accumulation",
                         "train_iters": tr["iters"], "loss_first": tr["loss_first"], "loss_last": tr["loss_last"],
@@ -564,7 +606,7 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind},
             "clocks": learned["clk"], "clocks_plain": plain["clk"]}
     if not args.no_cpu and rank == 0:
-        line["cpu_baseline"] = cpu_baseline(files, args.warmup * SWEEPS_PER_STEP, total_sweeps)
+        line["cpu_baseline"] = cpu_baseline(files, CPU_BURN_SWEEPS, total_sweeps)
     if rank == 0:
         print(json.dumps(line))
     ranks.close()

@@ -314,9 +314,15 @@ struct Rep : public LdoState<C> {
         while (i >= 0 && incr < 0) { i = bwd(i); ++incr; }
         return i;
     }
+    // A scaffold domain's state changed: the cached Z of the learned
+    // insertion no longer holds (snapshot restores bring back both).
+    __device__ __forceinline__ void z_touch(int i) {
+        if (i < ns) hdr.z_valid = 0;
+    }
     __device__ void bind_tables(const LdoTab* t) {
         tab = t;
         learn_tb = ldo_learn_tbin(t->temp);
+        hdr.z_valid = 0;
         t_dense = t->dense;
         t_stack_dense = t->stack_dense;
         t_off_e = t->off_e;
@@ -477,12 +483,15 @@ struct Rep : public LdoState<C> {
             }
             st[i] = (uint8_t)ns_;
             st[j] = (uint8_t)ns_;
+            z_touch(i);
+            z_touch(j);
             hash[k] = mkent(key, ns_, 0);
             bnd[j] = (int16_t)i;
             bnd[i] = (int16_t)j;
         }
         else if (occ == UNASSIGNED) {
             st[i] = UNBOUND;
+            z_touch(i);
             if (emp < 0) {
                 fail(LDO_RS_CAPACITY);
                 return;
@@ -503,6 +512,8 @@ struct Rep : public LdoState<C> {
         st[i] = UNASSIGNED;
         hset(pos(i), UNBOUND, j);
         st[j] = UNBOUND;
+        z_touch(i);
+        z_touch(j);
         return de;
     }
 
@@ -535,6 +546,7 @@ struct Rep : public LdoState<C> {
             int k = hfind(pkey(pos(i)), nullptr);
             if (k >= 0) herase(k);
             st[i] = UNASSIGNED;
+            z_touch(i);
             break;
         }
         default:
@@ -660,11 +672,14 @@ struct Rep : public LdoState<C> {
             st[i] = UNASSIGNED;
             hset(pos(i), UNBOUND, j);
             st[j] = UNBOUND;
+            z_touch(i);
+            z_touch(j);
         }
         else if (occ == UNBOUND) {
             int k = hfind(pkey(pos(i)), nullptr);
             if (k >= 0) herase(k);
             st[i] = UNASSIGNED;
+            z_touch(i);
         }
         else {
             hdr.num_unassigned--;
@@ -1953,7 +1968,15 @@ struct Rep : public LdoState<C> {
         if (pick) *pick = last;
         return z;
     }
-    __device__ double learn_z() const { return learn_scan(0.0, nullptr); }
+    // Z of the current state, cached in the header until a scaffold domain's
+    // state or the table changes.
+    __device__ double learn_z() {
+        if (hdr.z_valid) return hdr.z_cache;
+        double z = learn_scan(0.0, nullptr);
+        hdr.z_cache = z;
+        hdr.z_valid = 1;
+        return z;
+    }
     // q(g) for a target that was unbound in the state the proposal is made in.
     __device__ double learn_q_target(int g, double z, int n_sites, int fresh) const {
         if (z == 0) return 1.0 / n_sites;

@@ -129,6 +129,7 @@ struct LdoHdr {
     double energy;
     double move_bias;
     double H, S, stacking;
+    double z_cache;       // learned insertion: Z of the scaffold states it was computed for
     unsigned long long draws;
     long long steps_done;
     int num_domains, num_staples, num_bound, num_fully, num_self, num_unassigned, num_stacked;
@@ -138,7 +139,8 @@ struct LdoHdr {
     int violated;
     int tab;              // table set the energy was last computed with
     int sample_count;
-    int pad[3];
+    int z_valid;          // z_cache holds for the current scaffold states and table
+    int pad[2];
 };
 
 struct LdoLayout {
