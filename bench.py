@@ -489,8 +489,7 @@ def main():
         eng.set_controls(temps=temps)
         if table is not None:
             eng.learn_set_table(table)
-        for r in range(N_REP):
-            eng.set_config(r, start[r])
+        eng.set_configs(start)
         eng.set_sampling(1, total_sweeps)
         for _ in range(args.warmup):
             eng.run_sweeps(SWEEPS_PER_STEP)
@@ -525,8 +524,7 @@ def main():
         eng2.set_controls(temps=temps)
         if table is not None:
             eng2.learn_set_table(table)
-        for r in range(N_REP):
-            eng2.set_config(r, start[r])
+        eng2.set_configs(start)
         eng2.set_sampling(1, SWEEPS_PER_STEP)
         for _ in range(args.warmup):
             eng2.run_sweeps(SWEEPS_PER_STEP)

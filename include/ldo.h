@@ -13,7 +13,7 @@
  *   ldo_get_observables   OrigamiSystem counters + energy + SystemBiases
  *                         (include/.../origami_system.hpp:99-130)
  *   ldo_get_config        OrigamiSystem::chains (src/origami_system.cpp:175)
- *   ldo_set_config        OrigamiSystem ctor from given chains
+ *   ldo_set_config(s)     OrigamiSystem ctor from given chains
  *                         (src/origami_system.cpp:588-615, 991-1003)
  *   ldo_read_trj_frame    OrigamiTrajInputFile::read_config (src/files.cpp:129)
  *   ldo_checkpoint_*      restart_traj_file + .randstate + .swp restart
@@ -122,6 +122,13 @@ ldo_status ldo_get_config(ldo_engine* e, int replica, int32_t* buf, int cap, int
  * configuration that violates a constraint returns LDO_EINVAL ("Constaints
  * in violation after move complete") and leaves the replica unchanged. */
 ldo_status ldo_set_config(ldo_engine* e, int replica, const int32_t* buf, int n);
+
+/* Every replica at once, with one device launch: bufs holds n_replicas
+ * configurations in ldo_get_config's format, replica r's in
+ * [offsets[r], offsets[r+1]) (offsets has n_replicas + 1 entries).  All or
+ * nothing: a violating configuration returns LDO_EINVAL naming the replica
+ * and leaves every replica unchanged. */
+ldo_status ldo_set_configs(ldo_engine* e, const int32_t* bufs, const int32_t* offsets, int n_replicas);
 
 /* Frame `frame` (0 = first written) of a .trj trajectory file in
  * ldo_get_config's format, states 0 (OrigamiTrajInputFile::read_config,

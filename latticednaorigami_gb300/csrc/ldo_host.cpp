@@ -849,6 +849,42 @@ struct ldo_engine {
         }
     }
 
+    // Every replica's configuration at once (ldo_set_configs): bufs holds
+    // n_rep configurations, replica r's at [off[r], off[r+1]).  One init
+    // launch for the batch; all or nothing.
+    void set_configs(const int32_t* bufs, const int32_t* off) {
+        vector<unsigned char> old((size_t)n_rep * lay.bytes), fresh((size_t)n_rep * lay.bytes, 0);
+        CU(cudaMemcpy(old.data(), d_arena.p, old.size(), cudaMemcpyDeviceToHost));
+        for (int r = 0; r < n_rep; ++r) {
+            if (off[r] < 0 || off[r + 1] < off[r]) throw LdoError(LDO_EINVAL, "configuration offsets not increasing");
+            vector<ldo_io::ChainConf> chains = parse_config(bufs + off[r], off[r + 1] - off[r]);
+            unsigned char* b = fresh.data() + (size_t)r * lay.bytes;
+            fill_replica(r, chains, b);
+            const unsigned char* o = old.data() + (size_t)r * lay.bytes;
+            const auto* ho = reinterpret_cast<const LdoHdr*>(o + lay.o_hdr);
+            auto* hn = reinterpret_cast<LdoHdr*>(b + lay.o_hdr);
+            hn->draws = ho->draws;
+            hn->steps_done = ho->steps_done;
+            hn->sample_count = ho->sample_count;
+            std::memcpy(b + lay.o_mstat, o + lay.o_mstat, 2 * lay.nmv * sizeof(long long));
+        }
+        CU(cudaMemcpy(d_arena.p, fresh.data(), fresh.size(), cudaMemcpyHostToDevice));
+        LdoLaunch L = launch_params(LDO_MODE_INIT, 0);
+        CU(ldo_launch_mc(L, stream));
+        CU(cudaStreamSynchronize(stream));
+        CU(cudaMemcpy(fresh.data(), d_arena.p, fresh.size(), cudaMemcpyDeviceToHost));
+        for (int r = 0; r < n_rep; ++r) {
+            const auto* h = reinterpret_cast<const LdoHdr*>(fresh.data() + (size_t)r * lay.bytes + lay.o_hdr);
+            if (h->status != 0) {
+                CU(cudaMemcpy(d_arena.p, old.data(), old.size(), cudaMemcpyHostToDevice));
+                throw LdoError(LDO_EINVAL, "replica " + std::to_string(r) + ": " +
+                                               (h->status == LDO_RS_INVARIANT
+                                                    ? "Constaints in violation after move complete"
+                                                    : "configuration does not fit the replica's capacity"));
+            }
+        }
+    }
+
     // ---------------------------------------- checkpoint / resume ---
     // One binary file from which a run continues bit for bit: every
     // replica's state (configuration, counters, random-number position,
@@ -1778,6 +1814,11 @@ ldo_status ldo_get_config(ldo_engine* e, int replica, int32_t* buf, int cap, int
 ldo_status ldo_set_config(ldo_engine* e, int replica, const int32_t* buf, int n) {
     if (!e || !buf || n <= 0) return LDO_EINVAL;
     return guard(e, [&]() { e->set_config(replica, buf, n); });
+}
+
+ldo_status ldo_set_configs(ldo_engine* e, const int32_t* bufs, const int32_t* offsets, int n_replicas) {
+    if (!e || !bufs || !offsets || n_replicas != e->n_rep) return LDO_EINVAL;
+    return guard(e, [&]() { e->set_configs(bufs, offsets); });
 }
 
 ldo_status ldo_read_trj_frame(const char* path, int frame, int32_t* buf, int cap, int* written) {

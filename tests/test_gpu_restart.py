@@ -102,6 +102,33 @@ def test_set_config_refuses_a_violating_configuration():
     assert b.observables()[1]["status"] == 0
 
 
+def test_set_configs_batch_equals_one_by_one():
+    from latticednaorigami_gb300 import LdoError
+    n, seed = 6, 12
+    a = engine(inp("c3"), n_replicas=n, seed=seed)
+    a.run(2500)
+    cfgs = [a.config(r) for r in range(n)][::-1]
+    b = engine(inp("c3"), n_replicas=n, seed=seed + 1)
+    c = engine(inp("c3"), n_replicas=n, seed=seed + 1)
+    b.set_configs(cfgs)
+    for r in range(n):
+        c.set_config(r, cfgs[r])
+    assert [b.config(r) for r in range(n)] == cfgs
+    assert b.observables() == c.observables()
+    tb, ob, cb = run_traced(b, n, 1500)
+    tc, oc, cc = run_traced(c, n, 1500)
+    np.testing.assert_array_equal(tb, tc)
+    assert cb == cc
+    # all or nothing
+    before = [b.config(r) for r in range(n)]
+    bad = [list(x) for x in before]
+    bad[2][4 + 7:4 + 10] = bad[2][4:7]
+    bad[2][4 + 14:4 + 17] = bad[2][4:7]
+    with pytest.raises(LdoError, match="replica 2: Constaints in violation"):
+        b.set_configs(bad)
+    assert [b.config(r) for r in range(n)] == before
+
+
 def run_traced(e, n, steps):
     e.set_trace(n, steps)
     e.run(steps)
