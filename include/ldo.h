@@ -123,6 +123,16 @@ ldo_status ldo_get_config(ldo_engine* e, int replica, int32_t* buf, int cap, int
  * in violation after move complete") and leaves the replica unchanged. */
 ldo_status ldo_set_config(ldo_engine* e, int replica, const int32_t* buf, int n);
 
+/* Annealing (AnnealingGCMCSimulation::run, src/annealing_simulation.cpp:40):
+ * temperatures max_temp, max_temp - temp_interval, ... down to min_temp; at
+ * each, every replica gets that temperature (stacking multiplier 1; staple
+ * chemical-potential multiplier 1 unless constant_staple_M) and runs
+ * steps_per_temp steps.  LDO_EINVAL "Bad temperature interval" when
+ * temp_interval does not divide max_temp - min_temp, as the reference throws.
+ * The .inp keys of the same names hold the reference's values. */
+ldo_status ldo_anneal_run(ldo_engine* e, double max_temp, double min_temp, double temp_interval,
+                          int64_t steps_per_temp, int constant_staple_M, double* device_ms);
+
 /* Every replica at once, with one device launch: bufs holds n_replicas
  * configurations in ldo_get_config's format, replica r's in
  * [offsets[r], offsets[r+1]) (offsets has n_replicas + 1 entries).  All or

@@ -1816,6 +1816,39 @@ ldo_status ldo_set_config(ldo_engine* e, int replica, const int32_t* buf, int n)
     return guard(e, [&]() { e->set_config(replica, buf, n); });
 }
 
+// AnnealingGCMCSimulation (src/annealing_simulation.cpp:12-50): from
+// max_temp down to min_temp in steps of temp_interval, every replica is set to
+// the temperature (update_temp with stacking multiplier 1; update_staple_us
+// with multiplier 1 unless the staple concentration is held constant) and
+// runs steps_per_temp steps; step numbers continue across temperatures.
+ldo_status ldo_anneal_run(ldo_engine* e, double max_temp, double min_temp, double temp_interval,
+                          int64_t steps_per_temp, int constant_staple_M, double* device_ms) {
+    if (!e) return LDO_EINVAL;
+    return guard(e, [&]() {
+        if (!(temp_interval > 0) || steps_per_temp < 0)
+            throw LdoError(LDO_EINVAL, "temp_interval must be positive and steps_per_temp not negative");
+        if (std::fmod(max_temp - min_temp, temp_interval) != 0) throw LdoError(LDO_EINVAL, "Bad temperature interval");
+        double total = 0;
+        double temp = max_temp;
+        while (temp >= min_temp) {
+            for (int r = 0; r < e->n_rep; ++r) {
+                e->temps[r] = temp;
+                e->stack_mults[r] = 1.0;
+                if (!constant_staple_M) e->u_mults[r] = 1.0;
+                e->h_ctl[r].tab = e->table_for(e->sys_of[r], temp, 1.0);
+                e->h_ctl[r].staple_u_mult = e->u_mults[r];
+            }
+            e->upload_tables();
+            e->upload_ctl();
+            double ms = 0;
+            e->run(steps_per_temp, &ms);   // recomputes the energy with the new tables first
+            total += ms;
+            temp -= temp_interval;
+        }
+        if (device_ms) *device_ms = total;
+    });
+}
+
 ldo_status ldo_set_configs(ldo_engine* e, const int32_t* bufs, const int32_t* offsets, int n_replicas) {
     if (!e || !bufs || !offsets || n_replicas != e->n_rep) return LDO_EINVAL;
     return guard(e, [&]() { e->set_configs(bufs, offsets); });

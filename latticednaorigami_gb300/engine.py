@@ -23,7 +23,7 @@ EXPORTS = [
     "ldo_learn_collect", "ldo_learn_reset_counts", "ldo_learn_get_counts", "ldo_learn_train", "ldo_learn_set_params",
     "ldo_learn_get_params", "ldo_learn_get_table", "ldo_learn_set_table", "ldo_learn_loss_grad",
     "ldo_writer_open", "ldo_writer_write", "ldo_writer_close", "ldo_pt2d_run", "ldo_engine_exp",
-    "ldo_set_bias_centre", "ldo_swap_writer_open", "ldo_set_config", "ldo_set_configs", "ldo_read_trj_frame", "ldo_checkpoint_save",
+    "ldo_set_bias_centre", "ldo_swap_writer_open", "ldo_set_config", "ldo_set_configs", "ldo_anneal_run", "ldo_read_trj_frame", "ldo_checkpoint_save",
     "ldo_checkpoint_load",
 ]
 
@@ -75,6 +75,7 @@ def load_library(path=None):
     lib.ldo_get_observables.argtypes = [vp, ctypes.POINTER(Observables), ip]
     lib.ldo_get_config.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int32), ip, ctypes.POINTER(ctypes.c_int)]
     lib.ldo_set_config.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int32), ip]
+    lib.ldo_anneal_run.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int64, ip, dp]
     lib.ldo_set_configs.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32), ip]
     lib.ldo_read_trj_frame.argtypes = [ctypes.c_char_p, ip, ctypes.POINTER(ctypes.c_int32), ip,
                                        ctypes.POINTER(ctypes.c_int)]
@@ -194,6 +195,13 @@ class Engine:
         """Replaces a replica's configuration (ldo_get_config's flat format)."""
         buf = (ctypes.c_int32 * len(flat))(*flat)
         self._check(self.lib.ldo_set_config(self.h, replica, buf, len(flat)))
+
+    def anneal(self, max_temp, min_temp, temp_interval, steps_per_temp, constant_staple_M=True):
+        """AnnealingGCMCSimulation::run over every replica (ldo_anneal_run)."""
+        ms = ctypes.c_double(0)
+        self._check(self.lib.ldo_anneal_run(self.h, float(max_temp), float(min_temp), float(temp_interval),
+                                            int(steps_per_temp), 1 if constant_staple_M else 0, ctypes.byref(ms)))
+        return ms.value
 
     def set_configs(self, flats):
         """Replaces every replica's configuration (one flat list per replica)."""
