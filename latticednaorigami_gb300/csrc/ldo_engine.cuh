@@ -2010,6 +2010,25 @@ struct Rep : public LdoState<C> {
         return f;
     }
 
+    // Learned deletion choice: weight of staple chain cs, the weights' sum
+    // over the staples in chain order, and the probability of choosing cs.
+    __device__ double del_weight(int cs) const {
+        int len = chain_len(cs);
+        #pragma unroll 1
+        for (int d = 0; d < len; ++d)
+            if (st[slot_of(cs, d)] != BOUND) return LDO_LEARN_DEL_PART;
+        return 1.0;
+    }
+    __device__ __noinline__ double del_total() const {
+        double u = 0;
+        #pragma unroll 1
+        for (int c = 1; c < hdr.n_chains; ++c) u += del_weight(chain_order[c]);
+        return u;
+    }
+    __device__ double del_q(int cs, double u) const {
+        return LDO_LEARN_EPS_DEL / (double)hdr.num_staples + (1.0 - LDO_LEARN_EPS_DEL) * (del_weight(cs) / u);
+    }
+
     __device__ __noinline__ bool learned_insert() {
         int S = sys->n_types - 1;
         int n_sites = hdr.num_domains;
@@ -2059,36 +2078,42 @@ struct Rep : public LdoState<C> {
         double f = learn_forward(cs, type, z, n_sites, cs);
         add_external_bias_met();
         double boltz = dexp(-delta_e);
-        int ni = type_count[type];
+        // reverse move: the learned deletion choosing this staple
+        double qd = del_q(cs, del_total());
         double pratio = boltz * c_staple_M;
-        pratio /= 6.0 * ni;
-        pratio /= (double)S * f;
+        pratio *= qd;
+        pratio /= 6.0 * f;
         return exchange_accept_common(type, pratio);
     }
 
     __device__ __noinline__ bool learned_delete() {
-        int S = sys->n_types - 1;
-        int type = rng.uniform_int(1, S);
-        int n = type_count[type];
-        if (n == 0) {
+        if (hdr.num_staples == 0) {
             rejected = true;
             dirty = false;
             return false;
         }
-        int which = rng.uniform_int(0, n - 1);
+        // the staple: uniform with probability eps, else by deletion weight
+        double u_tot = del_total();
         int cs = -1;
-        #pragma unroll 1
-        for (int c = 1; c < hdr.n_chains; ++c) {
-            int x = chain_order[c];
-            if (chain_type[x] == type) {
-                if (which == 0) { cs = x; break; }
-                --which;
+        if (rng.uniform_real() < LDO_LEARN_EPS_DEL) {
+            cs = pick_staple_chain();
+        }
+        else {
+            double target = rng.uniform_real() * u_tot;
+            double cum = 0;
+            #pragma unroll 1
+            for (int c = 1; c < hdr.n_chains; ++c) {
+                cs = chain_order[c];
+                cum += del_weight(cs);
+                if (target < cum) break;
             }
         }
         if (cs < 0) {
             fail(LDO_RS_INVARIANT);
             return false;
         }
+        int type = chain_type[cs];
+        double qd = del_q(cs, u_tot);
         if (staple_is_connector(cs)) {
             dirty = false;
             return false;
@@ -2125,9 +2150,9 @@ struct Rep : public LdoState<C> {
         #pragma unroll 1
         for (int a = 0; a < na; ++a)
             f += learn_q_target(m.bd_old[a], z, n_sites, -1) * learn_q_type(m.bd_old[a], type, m.bd_new[a]) * gf[a];
-        int ni = type_count[type];
-        double pratio = (double)ni * 6.0 * boltz;
-        pratio *= (double)S * f;
+        double pratio = 6.0 * boltz;
+        pratio *= f;
+        pratio /= qd;
         pratio /= c_staple_M;
         bool acc = exchange_accept_common(type, pratio);
         if (acc) delete_chain(cs);

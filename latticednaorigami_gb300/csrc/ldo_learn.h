@@ -60,6 +60,11 @@ enum {
 // every configuration the reference's uniform regrowth makes stays possible.
 #define LDO_LEARN_EPS_D 0.05
 #define LDO_LEARN_EPS_O 0.05
+// Deletion: with probability LDO_LEARN_EPS_DEL the staple is uniform over the
+// staples, otherwise it is drawn with weight LDO_LEARN_DEL_PART when one of
+// its domains is not fully bound (unbound or misbound) and 1 when all are.
+#define LDO_LEARN_EPS_DEL 0.05
+#define LDO_LEARN_DEL_PART 8.0
 #define LDO_LEARN_LOGIT_CLAMP 30.0f
 
 LDO_LHD inline int ldo_learn_tbin(double temp) {

@@ -1509,6 +1509,21 @@ class System {
         return q;
     }
 
+    // learned deletion choice (the engine's del_weight / del_total / del_q)
+    double del_weight(int c_i) const {
+        for (int id : get_chain(c_i))
+            if (doms[id].state != BOUND) return LDO_LEARN_DEL_PART;
+        return 1.0;
+    }
+    double del_total() const {
+        double u = 0;
+        for (size_t c = 1; c < chains.size(); ++c) u += del_weight(doms[chains[c][0]].c);
+        return u;
+    }
+    double del_q(int c_i, double u) const {
+        return LDO_LEARN_EPS_DEL / (double)num_staples + (1.0 - LDO_LEARN_EPS_DEL) * (del_weight(c_i) / u);
+    }
+
     bool learned_insert() {
         if (!learn_w) throw std::runtime_error("LearnedStapleExchange needs the weight table");
         int S = (int)cfg.identities.size() - 1;
@@ -1585,22 +1600,34 @@ class System {
         }
         add_external_bias_met();
         double boltz = xexp(-delta_e);
-        int ni = num_staples_of_ident(ident);
+        double qd = del_q(c_i, del_total());
         double pratio = boltz * cfg.staple_M;
-        pratio /= 6.0 * ni;
-        pratio /= (double)S * f;
+        pratio *= qd;
+        pratio /= 6.0 * f;
         return exchange_accept_common(ident, pratio);
     }
 
     bool learned_delete() {
-        int S = (int)cfg.identities.size() - 1;
-        int ident = rng.uniform_int(1, S);
-        int n = num_staples_of_ident(ident);
-        if (n == 0) {
+        if (num_staples == 0) {
             rejected = true;
             return false;
         }
-        int c_i = ident_to_index[ident][rng.uniform_int(0, n - 1)];
+        double u_tot = del_total();
+        int c_i = -1;
+        if (rng.uniform_real() < LDO_LEARN_EPS_DEL) {
+            c_i = doms[chains[rng.uniform_int(1, num_staples)][0]].c;
+        }
+        else {
+            double target = rng.uniform_real() * u_tot;
+            double cum = 0;
+            for (size_t c = 1; c < chains.size(); ++c) {
+                c_i = doms[chains[c][0]].c;
+                cum += del_weight(c_i);
+                if (target < cum) break;
+            }
+        }
+        int ident = doms[chains[chain_pos(c_i)][0]].cident;
+        double qd = del_q(c_i, u_tot);
         std::vector<int> st = get_chain(c_i);
         if (staple_is_connector(st)) return false;
         for (int id : st)
@@ -1626,9 +1653,9 @@ class System {
         for (size_t a = 0; a < alt.size(); ++a)
             f += learn_q_target(alt[a].second, z, n_sites, -1) * learn_q_type(alt[a].second, ident, alt[a].first) *
                  gf[a];
-        int ni = num_staples_of_ident(ident);
-        double pratio = (double)ni * 6.0 * boltz;
-        pratio *= (double)S * f;
+        double pratio = 6.0 * boltz;
+        pratio *= f;
+        pratio /= qd;
         pratio /= cfg.staple_M;
         bool acc = exchange_accept_common(ident, pratio);
         if (acc) delete_chain(c_i);

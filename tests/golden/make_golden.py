@@ -58,14 +58,19 @@ def flatten(chains):
     return flat
 
 
-def enumerate_c1(tmp):
-    """Exact staple-only enumeration of the 4-domain system with the
-    reference's enumerator (src/enumerate.cpp:687), weights over
-    (numstaples, numfulldomains)."""
-    base = os.path.join(tmp, "c1enum")
-    inp = systems.write_case(tmp, "c1", extra=dict(
-        simulation_type="enumerate", enumerate_staples_only="true", ops_to_output="numstaples numfulldomains",
-        output_filebase=base))
+# exact enumerations: fixture name, case (the 4-domain system, whose staples
+# never bind both domains; the capped 8-domain system, where they do)
+ENUMERATIONS = [("c1_enumeration", "c1"), ("e8_enumeration", "e8")]
+
+
+def enumerate_case(tmp, name, case):
+    """Exact staple-only enumeration of a small system with the reference's
+    enumerator (src/enumerate.cpp:687), weights over (numstaples,
+    numfulldomains)."""
+    base = os.path.join(tmp, name)
+    opts = dict(simulation_type="enumerate", enumerate_staples_only="true",
+                ops_to_output="numstaples numfulldomains", output_filebase=base)
+    inp = systems.write_case(tmp, case, extra=opts)
     with open(inp, "a") as f:
         f.write("trace_mode=enumerate\n")
     subprocess.run([REF, inp], capture_output=True, text=True, cwd=tmp, check=True)
@@ -78,9 +83,9 @@ def enumerate_c1(tmp):
                 continue
             key, w = line.rsplit(" ", 1)
             weights[" ".join(key.strip("()").split())] = float(w)
-    path = os.path.join(HERE, "c1_enumeration.json")
+    path = os.path.join(HERE, name + ".json")
     with open(path, "w") as f:
-        json.dump({"case": "c1", "ops": tags, "weights": weights}, f, indent=1, sort_keys=True)
+        json.dump({"case": case, "ops": tags, "weights": weights}, f, indent=1, sort_keys=True)
     print(path, weights)
 
 
@@ -153,8 +158,9 @@ def main(only=None):
             with gzip.open(path, "wt") as f:
                 json.dump(fx, f)
             print(path, len(d["steps"]), "steps, draws", d["draws"])
-        if not only or "c1" in only:
-            enumerate_c1(tmp)
+        for name, case in ENUMERATIONS:
+            if not only or case in only:
+                enumerate_case(tmp, name, case)
         make_outputs(tmp, only)
         make_restarts(tmp, only)
 

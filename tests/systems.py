@@ -235,6 +235,11 @@ CASES = {
     # 8 bp domains) with the reference's standard moveset
     "c4": ("mixed96", "std", dict(domain_type="ThreeQuarterTurn", stacking_ene=-1000, staple_M=1e-6, temp=310,
                                   max_total_staples=40, max_type_staples=1, max_staple_size=3)),
+    # an 8-domain scaffold small enough for the reference's exact enumeration,
+    # capped at one staple per type and two in all, where most weight sits in
+    # states with one fully and one partly bound staple (or one staple)
+    "e8": ("grid8", "met3", dict(stacking_ene=-1000, staple_M=1e-4, temp=355, max_total_staples=2,
+                                 max_type_staples=1)),
     # the 48-domain system's shape with the reference's standard moveset
     "s48": ("grid48", "ctrg", dict(stacking_ene=-1000, staple_M=1e-4, temp=335, max_total_staples=48,
                                    max_type_staples=2)),

@@ -12,6 +12,7 @@ import os
 import tempfile
 
 import numpy as np
+import pytest
 
 from conftest import GOLDEN, inp
 from oracle_lib import run_batch_states
@@ -38,8 +39,8 @@ def learned_moves(d, regrowth=False):
     return p
 
 
-def chi2_against_enumeration(states):
-    with open(os.path.join(GOLDEN, "c1_enumeration.json")) as f:
+def chi2_against_enumeration(states, name="c1_enumeration"):
+    with open(os.path.join(GOLDEN, name + ".json")) as f:
         ref = json.load(f)["weights"]
     counts = {}
     for s, fb in states.reshape(-1, 2):
@@ -69,6 +70,22 @@ def test_learned_exchange_samples_exact_distribution():
     states = run_batch_states(inp("c1"), 77, 1024, 60000, 1, 1, os.cpu_count() or 1,
                               overrides="movetype_file = %s" % mv, learn_w=table)
     p, obs, exp = chi2_against_enumeration(states)
+    assert p > 0.01, (obs, exp, p)
+
+
+@pytest.mark.parametrize("moves", ["plain", "learned"])
+def test_capped_8_domain_system_samples_exact_distribution(moves):
+    """The 8-domain system capped at two staples, where a third of the weight
+    is one fully and one partly bound staple: the learned exchange (sites,
+    growth directions, deletion choice weighted by how a staple is bound)
+    with a strongly non-uniform random table, and the plain moveset, against
+    the reference's exact enumeration."""
+    d = tempfile.mkdtemp()
+    over = "movetype_file = %s" % learned_moves(d, regrowth=True) if moves == "learned" else ""
+    table = np.exp(np.random.default_rng(9).normal(0.0, 2.0, learn_ref.TABLE))
+    states = run_batch_states(inp("e8"), 81, 2048, 40000, 1, 1, os.cpu_count() or 1,
+                              overrides=over, learn_w=table if moves == "learned" else None)
+    p, obs, exp = chi2_against_enumeration(states, "e8_enumeration")
     assert p > 0.01, (obs, exp, p)
 
 
