@@ -1762,13 +1762,16 @@ struct Rep : public LdoState<C> {
     // Z = sum of w over the unbound scaffold domains (q = 1/N when Z = 0),
     // w(g) = exp(network logit) of g's neighbourhood
     // (ldo_learn.h), then the staple type and domain complementary to g with
-    // probability 1 - eps_t (uniform type and domain otherwise).  The forward
-    // probability of the new configuration sums q over the staple's bound
-    // domains (each could have been the growth point), so the Metropolis-
-    // Hastings ratio is the reference's (src/met_movetypes.cpp:212-301) with
-    // its uniform proposal factor n_bd / (S L N) replaced by that sum; the
-    // deletion proposal stays the reference's and its ratio uses the same sum
-    // evaluated in the state after the deletion.
+    // probability 1 - eps_t (uniform type and domain otherwise); the other
+    // domains grow with the learned directions (lr_grow).  The forward
+    // probability of the new configuration sums q(partner) q(type, d) G(d)
+    // over the staple's bound domains d (each could have been the growth
+    // point; G the growth factor), so the Metropolis-Hastings ratio is the
+    // reference's (src/met_movetypes.cpp:212-301) with its uniform proposal
+    // factor n_bd / (S L N) replaced by that sum.  Deletions choose the staple
+    // by del_q (weighted towards partly bound staples) instead of the
+    // reference's 1 / (S N_i); both ratios use del_q for the staple that the
+    // deletion removes or the reverse deletion would remove.
 
     // Neighbour-state code: 0 none, 1 unbound or unassigned, 2 bound,
     // 3 misbound; a domain bound to chain `fresh` (the staple being inserted)
