@@ -12,6 +12,7 @@
 #include <memory>
 #include <sstream>
 #include <string>
+#include <iterator>
 #include <tuple>
 #include <vector>
 
@@ -909,12 +910,18 @@ struct ldo_engine {
         int32_t pt_rungs, pt_q, pt_dim2, pt_nctr;
         int64_t pt_swap_i;
         LdoLayout lay;
+        uint64_t payload_bytes, payload_hash;   // everything after the header (FNV-1a)
     };
     struct CkptTab {
         int32_t sys, pad;
         double temp, mult;
     };
 
+    static uint64_t fnv1a(const unsigned char* b, size_t n) {
+        uint64_t h = 1469598103934665603ull;
+        for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+        return h;
+    }
     uint64_t systems_hash() const {
         uint64_t h = 1469598103934665603ull;   // FNV-1a
         const unsigned char* b = reinterpret_cast<const unsigned char*>(h_sys.data());
@@ -927,7 +934,7 @@ struct ldo_engine {
         CkptHead H;
         std::memset(&H, 0, sizeof H);
         std::memcpy(H.magic, "LDOCKPT", 8);
-        H.version = 1;
+        H.version = 2;
         H.n_rep = (uint32_t)n_rep;
         H.n_sys = (uint32_t)systems.size();
         H.seed = seed;
@@ -953,10 +960,8 @@ struct ldo_engine {
         CU(cudaMemcpy(arena.data(), d_arena.p, arena.size(), cudaMemcpyDeviceToHost));
         vector<double> table(LDO_LEARN_TABLE);
         CU(cudaMemcpy(table.data(), d_learn_w.p, table.size() * sizeof(double), cudaMemcpyDeviceToHost));
-        std::ofstream f(path, std::ios::binary);
-        if (!f) throw LdoError(LDO_EINVAL, path + ": cannot open checkpoint file for writing");
-        auto put = [&](const void* p, size_t bytes) { f.write(reinterpret_cast<const char*>(p), (std::streamsize)bytes); };
-        put(&H, sizeof H);
+        std::string out(sizeof H, '\0');
+        auto put = [&](const void* p, size_t bytes) { out.append(reinterpret_cast<const char*>(p), bytes); };
         put(keys.data(), keys.size() * sizeof(CkptTab));
         put(h_ctl.data(), h_ctl.size() * sizeof(LdoRepCtl));
         put(temps.data(), n_rep * sizeof(double));
@@ -988,6 +993,12 @@ struct ldo_engine {
             put(att.data(), att.size() * sizeof(long long));
             put(acc.data(), acc.size() * sizeof(long long));
         }
+        H.payload_bytes = out.size() - sizeof H;
+        H.payload_hash = fnv1a(reinterpret_cast<const unsigned char*>(out.data()) + sizeof H, H.payload_bytes);
+        std::memcpy(&out[0], &H, sizeof H);
+        std::ofstream f(path, std::ios::binary);
+        if (!f) throw LdoError(LDO_EINVAL, path + ": cannot open checkpoint file for writing");
+        f.write(out.data(), (std::streamsize)out.size());
         f.flush();
         if (!f) throw LdoError(LDO_EINVAL, path + ": writing the checkpoint failed");
     }
@@ -995,14 +1006,20 @@ struct ldo_engine {
     void checkpoint_load(const string& path) {
         std::ifstream f(path, std::ios::binary);
         if (!f) throw LdoError(LDO_EINVAL, path + ": checkpoint file does not exist");
+        std::string in((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+        size_t cur = 0;
         auto get = [&](void* p, size_t bytes) {
-            f.read(reinterpret_cast<char*>(p), (std::streamsize)bytes);
-            if ((size_t)f.gcount() != bytes) throw LdoError(LDO_EINVAL, path + ": checkpoint file is truncated");
+            if (in.size() - cur < bytes) throw LdoError(LDO_EINVAL, path + ": checkpoint file is truncated");
+            std::memcpy(p, in.data() + cur, bytes);
+            cur += bytes;
         };
         CkptHead H;
         get(&H, sizeof H);
-        if (std::memcmp(H.magic, "LDOCKPT", 8) != 0 || H.version != 1)
+        if (std::memcmp(H.magic, "LDOCKPT", 8) != 0 || H.version != 2)
             throw LdoError(LDO_EINVAL, path + ": not a checkpoint of this engine");
+        if (H.payload_bytes != in.size() - sizeof H ||
+            H.payload_hash != fnv1a(reinterpret_cast<const unsigned char*>(in.data()) + sizeof H, H.payload_bytes))
+            throw LdoError(LDO_EINVAL, path + ": checkpoint file is truncated or corrupt");
         if (H.n_rep != (uint32_t)n_rep || H.n_sys != systems.size() || H.sys_hash != systems_hash() ||
             std::memcmp(&H.lay, &lay, sizeof lay) != 0 || H.n_grid != h_grid.size())
             throw LdoError(LDO_EINVAL, path + ": checkpoint of other systems or another replica count");
@@ -1039,6 +1056,11 @@ struct ldo_engine {
             return remap[k];
         };
         for (int r = 0; r < n_rep; ++r) {
+            if (ctl[r].sys != sys_of[r] || ctl[r].rep != (uint32_t)r)
+                throw LdoError(LDO_EINVAL, path + ": replica controls do not match this engine");
+            for (int b = 0; b < LDO_MAX_BIASES; ++b)
+                if (ctl[r].grid_off[b] != h_ctl[r].grid_off[b])
+                    throw LdoError(LDO_EINVAL, path + ": grid layout does not match this engine");
             ctl[r].tab = tab(ctl[r].tab);
             auto* h = reinterpret_cast<LdoHdr*>(arena.data() + (size_t)r * lay.bytes + lay.o_hdr);
             h->tab = tab(h->tab);

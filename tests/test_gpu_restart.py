@@ -209,3 +209,10 @@ def test_checkpoint_refuses_other_systems(tmp_path):
         f.write(head)
     with pytest.raises(LdoError, match="truncated"):
         engine(inp("g24a"), n_replicas=4, seed=1).load_checkpoint(str(tmp_path / "t.ckpt"))
+    # one flipped byte in the payload
+    data = bytearray(open(ck, "rb").read())
+    data[len(data) // 2] ^= 0x40
+    with open(str(tmp_path / "c.ckpt"), "wb") as f:
+        f.write(bytes(data))
+    with pytest.raises(LdoError, match="corrupt"):
+        engine(inp("g24a"), n_replicas=4, seed=1).load_checkpoint(str(tmp_path / "c.ckpt"))
