@@ -154,7 +154,9 @@ ldo_status ldo_read_trj_frame(const char* path, int frame, int32_t* buf, int cap
  * ladder's permutation, swap counter, swap random-number positions and
  * statistics.  An engine created from the same input files with the same
  * replica count loads it and continues bit for bit as the saved engine
- * would have; LDO_EINVAL for a file of other systems.  Sample and trace
+ * would have; LDO_EINVAL for a file of other systems, or one that is
+ * truncated or corrupt (the header carries the payload's length and FNV-1a
+ * hash).  Sample and trace
  * buffers, the .swp history and umbrella-sampling iterations are not saved. */
 ldo_status ldo_checkpoint_save(ldo_engine* e, const char* path);
 ldo_status ldo_checkpoint_load(ldo_engine* e, const char* path);
