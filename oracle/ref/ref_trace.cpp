@@ -8,7 +8,8 @@
 // and every trace_every steps the full configuration, as JSON on stdout.
 //
 // Extra keys: trace_steps, trace_seed, trace_replica, trace_every,
-//             trace_mode (simulate | enumerate)
+//             trace_mode (simulate | enumerate | anneal: the reference's
+//             annealing loop over max_temp .. min_temp)
 #include <chrono>
 #include <cstdio>
 #include <fstream>
@@ -18,6 +19,7 @@
 #include <string>
 #include <vector>
 
+#include "LatticeDNAOrigami/annealing_simulation.hpp"
 #include "LatticeDNAOrigami/bias_functions.hpp"
 #include "LatticeDNAOrigami/enumerate.hpp"
 #include "LatticeDNAOrigami/order_params.hpp"
@@ -127,10 +129,10 @@ void fill_params(parser::InputParameters& p, std::map<string, string>& kv) {
     p.m_allow_nonsensical_ps = B("allow_nonsensical_ps", false);
     p.m_max_duration = 10e9;
     p.m_ct_steps = 0;
-    p.m_max_temp = 400;
-    p.m_min_temp = 300;
-    p.m_temp_interval = 1;
-    p.m_steps_per_temp = 0;
+    p.m_max_temp = D("max_temp", 400);
+    p.m_min_temp = D("min_temp", 300);
+    p.m_temp_interval = D("temp_interval", 1);
+    p.m_steps_per_temp = I("steps_per_temp", 0);
     p.m_num_reps = 1;
     p.m_exchange_interval = 0;
     p.m_swaps = 0;
@@ -222,6 +224,32 @@ class TraceSim : public simulation::GCMCSimulation {
     vector<string> m_dumps;
 };
 
+// The reference's own annealing loop (AnnealingGCMCSimulation::run,
+// src/annealing_simulation.cpp:40) with the per-step record of TraceSim.
+class TraceAnneal : public annealing::AnnealingGCMCSimulation {
+  public:
+    TraceAnneal(origami::OrigamiSystem& o, orderParams::SystemOrderParams& ops, biasFunctions::SystemBiases& b,
+                parser::InputParameters& p, std::ostream& out)
+        : AnnealingGCMCSimulation(o, ops, b, p), m_out(out) {
+        m_logging_stream = &std::cerr;
+    }
+
+  private:
+    bool m_first {true};
+    std::ostream& m_out;
+    void update_internal(long long int step) override {
+        auto& o = m_origami_system;
+        char buf[512];
+        std::snprintf(buf, sizeof buf, "%s[%lld,%.17g,%d,%d,%d,%d,%.17g,%llu]",
+                      m_first ? "" : ",", step, o.energy(), o.num_staples(),
+                      o.num_fully_bound_domain_pairs(), o.num_bound_domain_pairs(),
+                      o.num_stacked_domain_pairs(), m_biases.get_total_bias(),
+                      (unsigned long long)ldo_ref_rng_draws());
+        m_out << buf;
+        m_first = false;
+    }
+};
+
 } // namespace
 
 int main(int argc, char** argv) {
@@ -252,14 +280,23 @@ int main(int argc, char** argv) {
         char buf[256];
         std::snprintf(buf, sizeof buf, ", \"initial_energy\": %.17g, \"steps\": [", o->energy());
         std::cout << buf;
-        TraceSim sim(*o, ops, biases, params, every, std::cout);
-        // trace_quiet=1: no per-step records (for timing the move loop)
-        sim.m_quiet = kv.count("trace_quiet") && kv["trace_quiet"] == "1";
         auto t0 = std::chrono::steady_clock::now();
-        sim.simulate(steps, 0, false);
+        if (mode == "anneal") {
+            TraceAnneal sim(*o, ops, biases, params, std::cout);
+            sim.run();
+            std::cout << "], \"dumps\": [[-1,";
+            dump_config(*o, std::cout);
+            std::cout << "]";
+        }
+        else {
+            TraceSim sim(*o, ops, biases, params, every, std::cout);
+            // trace_quiet=1: no per-step records (for timing the move loop)
+            sim.m_quiet = kv.count("trace_quiet") && kv["trace_quiet"] == "1";
+            sim.simulate(steps, 0, false);
+            std::cout << "], \"dumps\": [";
+            for (size_t i = 0; i < sim.m_dumps.size(); ++i) std::cout << (i ? "," : "") << sim.m_dumps[i];
+        }
         double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        std::cout << "], \"dumps\": [";
-        for (size_t i = 0; i < sim.m_dumps.size(); ++i) std::cout << (i ? "," : "") << sim.m_dumps[i];
         std::snprintf(buf, sizeof buf, "], \"final_energy\": %.17g, \"draws\": %llu, \"seconds\": %.6f}\n",
                       o->energy(), (unsigned long long)ldo_ref_rng_draws(), secs);
         std::cout << buf;

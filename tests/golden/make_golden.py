@@ -118,6 +118,38 @@ def make_restarts(tmp, only=None):
         print(path, len(d["steps"]), "steps, draws", d["draws"])
 
 
+# the reference's annealing loop (AnnealingGCMCSimulation::run,
+# src/annealing_simulation.cpp:40): case, seed, max_temp, min_temp,
+# temp_interval, steps_per_temp, constant_staple_M
+ANNEAL_RUNS = [("g24a", 31, 350.0, 330.0, 5.0, 1500, True), ("c3", 32, 350.0, 335.0, 5.0, 2000, False)]
+
+
+def anneal_options(run):
+    case, seed, tmax, tmin, dt, steps, const = run
+    return dict(max_temp=tmax, min_temp=tmin, temp_interval=dt, steps_per_temp=steps,
+                constant_staple_M="true" if const else "false")
+
+
+def make_anneals(tmp, only=None):
+    for run in ANNEAL_RUNS:
+        case, seed = run[0], run[1]
+        if only and case not in only:
+            continue
+        opts = anneal_options(run)
+        opts["output_filebase"] = os.path.join(tmp, "%s_anneal" % case)
+        inp = systems.write_case(tmp, case, extra=opts)
+        with open(inp, "a") as f:
+            f.write("trace_mode=anneal\n")
+        d = ref_trace(inp, seed, 0)
+        fx = {"case": case, "seed": seed, "steps": len(d["steps"]), "anneal": list(run[2:]),
+              "initial_energy": d["initial_energy"], "trace": d["steps"], "final_config": flatten(d["dumps"][-1][1]),
+              "draws": d["draws"]}
+        path = os.path.join(HERE, "%s_anneal_s%d.json.gz" % (case, seed))
+        with gzip.open(path, "wt") as f:
+            json.dump(fx, f)
+        print(path, len(d["steps"]), "steps, draws", d["draws"])
+
+
 # reference output files: case, seed, steps, write frequency
 OUTPUT_RUNS = [("g24a", 3, 2000, 400), ("g24b", 4, 2000, 400), ("c3", 8, 2000, 400)]
 OUTPUT_EXTS = [".vsf", ".trj", ".vcf", ".states", ".ores", ".counts", ".staples", ".staplestates", ".ene", ".ops"]
@@ -163,6 +195,7 @@ def main(only=None):
                 enumerate_case(tmp, name, case)
         make_outputs(tmp, only)
         make_restarts(tmp, only)
+        make_anneals(tmp, only)
 
 
 if __name__ == "__main__":

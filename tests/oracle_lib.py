@@ -137,6 +137,33 @@ def swap_uniform(seed, ladder, index):
     return float(out[0])
 
 
+def run_golden(o, fx):
+    """The run a golden fixture records: fx["steps"] steps, or, for a fixture
+    of the reference's annealing loop (AnnealingGCMCSimulation::run), the
+    temperatures max_temp, max_temp - interval, ... down to min_temp with
+    update_temp before steps_per_temp steps at each (the systems of these
+    fixtures have no biases, so the staple chemical potentials that
+    update_staple_us changes do not enter)."""
+    if "anneal" not in fx:
+        return o.run(fx["steps"])
+    tmax, tmin, dt, steps, _ = fx["anneal"]
+    steps = int(steps)
+    parts = []
+    t = tmax
+    step = 0
+    while t >= tmin:
+        o.update_temp(t)
+        # the reference's step counter: step += simulate(steps, step), and
+        # simulate returns its last step + 1 (src/annealing_simulation.cpp:47,
+        # src/simulation.cpp:568), so every temperature after the first starts
+        # at a step number that jumps ahead
+        o.step = step
+        parts.append(o.run(steps))
+        step += step + steps + 1
+        t -= dt
+    return np.concatenate(parts)
+
+
 def run_batch_sampled(inp, seed, n_rep, sweeps, sweep_len, threads, overrides="", temps=None):
     """CPU baseline with one numfulldomains sample per replica per sweep:
     returns (wall seconds, samples[n_rep, sweeps]).  temps[n_rep], if given,

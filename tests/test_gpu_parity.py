@@ -46,8 +46,10 @@ def test_engine_matches_oracle_per_step(case):
 
 # s24a_s11 meets a weight ratio within a rounding of 1 (long double vs FP64):
 # tests/test_gpu_scaffold.py compares it up to that step
+# (the annealing fixtures pin the oracle's annealing to the reference's;
+# tests/test_gpu_anneal.py pins the engine's to the oracle's)
 @pytest.mark.parametrize("path", [p for p in sorted(glob.glob(os.path.join(GOLDEN, "*.json.gz")))
-                                  if not p.endswith("s24a_s11.json.gz")],
+                                  if not p.endswith("s24a_s11.json.gz") and "_anneal_" not in p],
                          ids=lambda p: os.path.basename(p)[:-8])
 def test_engine_matches_reference_golden(path):
     with gzip.open(path, "rt") as f:

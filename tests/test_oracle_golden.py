@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN, golden_overrides, inp
-from oracle_lib import OracleReplica
+from oracle_lib import OracleReplica, run_golden
 
 FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "*.json.gz")))
 
@@ -31,7 +31,7 @@ def test_oracle_matches_reference_trace(path):
     fx = load(path)
     o = OracleReplica(inp(fx["case"]), seed=fx["seed"], replica=0, overrides=golden_overrides(fx))
     o.set_reference_arithmetic(True)
-    tr = o.run(fx["steps"])
+    tr = run_golden(o, fx)
     ref = np.array(fx["trace"], dtype=np.float64)
     assert ref.shape == tr.shape
     # step, staples, fully bound, bound, stacked, draws: exact
@@ -60,7 +60,7 @@ FP64_EXACT = [p for p in FIXTURES if not p.endswith("s24a_s11.json.gz")]
 def test_oracle_fp64_weights_match_reference_trace(path):
     fx = load(path)
     o = OracleReplica(inp(fx["case"]), seed=fx["seed"], replica=0, overrides=golden_overrides(fx))
-    tr = o.run(fx["steps"])
+    tr = run_golden(o, fx)
     ref = np.array(fx["trace"], dtype=np.float64)
     np.testing.assert_array_equal(tr[:, [0, 2, 3, 4, 5, 7]], ref[:, [0, 2, 3, 4, 5, 7]])
     np.testing.assert_array_equal(tr[:, 1], ref[:, 1])
@@ -75,7 +75,7 @@ def test_fp64_weights_part_from_long_double_only_at_a_tie():
     fx = load(os.path.join(GOLDEN, "s24a_s11.json.gz"))
     ref = np.array(fx["trace"], dtype=np.float64)
     o = OracleReplica(inp(fx["case"]), seed=fx["seed"], replica=0, overrides=golden_overrides(fx))
-    tr = o.run(fx["steps"])
+    tr = run_golden(o, fx)
     k = 19884
     np.testing.assert_array_equal(tr[:k], ref[:k])
     assert tr[k, 7] == ref[k, 7] - 1
