@@ -8,7 +8,10 @@ Needs the reference sources (only present where the fixtures are made):
 Each fixture <case>_s<seed>.json.gz holds the per-step trace (step, energy,
 staples, fully bound pairs, bound pairs, stacked pairs, total bias, random
 draws) and the final configuration (chains: index, identity, per domain
-x y z ox oy oz state)."""
+x y z ox oy oz state); <case>_r<frame>_s<seed> starts from a frame of a
+reference-written trajectory under outputs/, <case>_anneal_s<seed> runs the
+reference's annealing loop.  <name>_enumeration.json holds the reference's
+exact staple-only enumerations, outputs/ the reference's own output files."""
 import gzip
 import json
 import os
