@@ -244,10 +244,12 @@ ldo_status ldo_us_get_windows(ldo_engine* e, int32_t* window_of_replica, int n, 
  * (an ldo_status code) to status_of_replica[n] (may be NULL), the largest to
  * *worst and the number of nonzero ones to *n_bad; n must equal the replica
  * count and be at most 65536 (LDO_EINVAL otherwise).  Its scratch is a fixed
- * 256 KiB device array of the library, shared by every call: the first call
- * on a device looks up its address, so make that first call before any stream
- * capture, and do not let two calls overlap on the GPU (they race on the
- * array).  Returns after the results are in host memory. */
+ * 256 KiB device array of the library, shared by every call.  Each call looks
+ * up the array's device address anew (a device reset can move it); the first
+ * call on a device may also load the library's device code, so make that
+ * first call before any stream capture.  Do not let two calls overlap on the
+ * GPU (they race on the array).  Returns after the results are in host
+ * memory. */
 ldo_status ldo_replica_status_noalloc(ldo_engine* e, int32_t* status_of_replica, int n, int32_t* worst,
                                       int32_t* n_bad);
 

@@ -388,6 +388,17 @@ struct ldo_engine {
     int smem_pad {0};
     cudaStream_t stream {nullptr};
     cudaEvent_t ev0 {nullptr}, ev1 {nullptr};
+    // Every host-device copy of the engine is ordered on its stream and
+    // complete when this returns.  The stream is non-blocking, so a copy on
+    // the legacy default stream (plain cudaMemcpy) would be ordered with none
+    // of the engine's kernels, and a pageable host-to-device cudaMemcpy may
+    // return before its transfer has finished.
+    cudaError_t copy(void* dst, const void* src, size_t n, cudaMemcpyKind kind) {
+        if (n == 0) return cudaSuccess;
+        cudaError_t err = cudaMemcpyAsync(dst, src, n, kind, stream);
+        if (err != cudaSuccess) return err;
+        return cudaStreamSynchronize(stream);
+    }
 
     vector<LdoSys> h_sys;
     vector<LdoTab> h_tabs;
@@ -497,16 +508,16 @@ struct ldo_engine {
 
     void upload_tables() {
         d_tabs.alloc(h_tabs.size());
-        CU(cudaMemcpy(d_tabs.p, h_tabs.data(), h_tabs.size() * sizeof(LdoTab), cudaMemcpyHostToDevice));
+        CU(copy(d_tabs.p, h_tabs.data(), h_tabs.size() * sizeof(LdoTab), cudaMemcpyHostToDevice));
         d_bank.alloc(h_bank.size());
-        CU(cudaMemcpy(d_bank.p, h_bank.data(), h_bank.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CU(copy(d_bank.p, h_bank.data(), h_bank.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
     void upload_ctl() {
-        CU(cudaMemcpy(d_ctl.p, h_ctl.data(), h_ctl.size() * sizeof(LdoRepCtl), cudaMemcpyHostToDevice));
+        CU(copy(d_ctl.p, h_ctl.data(), h_ctl.size() * sizeof(LdoRepCtl), cudaMemcpyHostToDevice));
     }
     void upload_grid() {
         if (h_grid.empty()) return;
-        CU(cudaMemcpy(d_grid.p, h_grid.data(), h_grid.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CU(copy(d_grid.p, h_grid.data(), h_grid.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
 
     LdoLaunch launch_params(int mode, long long steps) {
@@ -668,7 +679,7 @@ struct ldo_engine {
         for (int r = 0; r < n_rep; ++r)
             fill_replica(r, systems[sys_of[r]].sf.chains, host.data() + (size_t)r * lay.bytes);
         d_arena.alloc(host.size());
-        CU(cudaMemcpy(d_arena.p, host.data(), host.size(), cudaMemcpyHostToDevice));
+        CU(copy(d_arena.p, host.data(), host.size(), cudaMemcpyHostToDevice));
     }
 
     void create(const vector<string>& inps, const string& overrides, const vector<int>& sys_of_replica,
@@ -706,7 +717,7 @@ struct ldo_engine {
         }
         for (auto& hs : systems) h_sys.push_back(hs.desc);
         d_sys.alloc(h_sys.size());
-        CU(cudaMemcpy(d_sys.p, h_sys.data(), h_sys.size() * sizeof(LdoSys), cudaMemcpyHostToDevice));
+        CU(copy(d_sys.p, h_sys.data(), h_sys.size() * sizeof(LdoSys), cudaMemcpyHostToDevice));
         h_ctl.resize(n_rep);
         temps.resize(n_rep);
         stack_mults.assign(n_rep, 1.0);
@@ -757,11 +768,11 @@ struct ldo_engine {
         {
             vector<double> ones(LDO_LEARN_TABLE, 1.0);
             d_learn_w.alloc(LDO_LEARN_TABLE);
-            CU(cudaMemcpy(d_learn_w.p, ones.data(), ones.size() * sizeof(double), cudaMemcpyHostToDevice));
+            CU(copy(d_learn_w.p, ones.data(), ones.size() * sizeof(double), cudaMemcpyHostToDevice));
             d_cnt_b.alloc(LDO_LEARN_TABLE);
             d_cnt_t.alloc(LDO_LEARN_TABLE);
-            CU(cudaMemset(d_cnt_b.p, 0, LDO_LEARN_TABLE * sizeof(float)));
-            CU(cudaMemset(d_cnt_t.p, 0, LDO_LEARN_TABLE * sizeof(float)));
+            CU(cudaMemsetAsync(d_cnt_b.p, 0, LDO_LEARN_TABLE * sizeof(float), stream));
+            CU(cudaMemsetAsync(d_cnt_t.p, 0, LDO_LEARN_TABLE * sizeof(float), stream));
         }
         LdoLaunch L = launch_params(LDO_MODE_INIT, 0);
         CU(ldo_launch_mc(L, stream));
@@ -827,7 +838,7 @@ struct ldo_engine {
         vector<ldo_io::ChainConf> chains = parse_config(buf, n);
         size_t off = (size_t)r * lay.bytes;
         vector<unsigned char> old(lay.bytes), fresh(lay.bytes, 0);
-        CU(cudaMemcpy(old.data(), d_arena.p + off, lay.bytes, cudaMemcpyDeviceToHost));
+        CU(copy(old.data(), d_arena.p + off, lay.bytes, cudaMemcpyDeviceToHost));
         fill_replica(r, chains, fresh.data());
         const auto* ho = reinterpret_cast<const LdoHdr*>(old.data() + lay.o_hdr);
         auto* hn = reinterpret_cast<LdoHdr*>(fresh.data() + lay.o_hdr);
@@ -835,15 +846,15 @@ struct ldo_engine {
         hn->steps_done = ho->steps_done;
         hn->sample_count = ho->sample_count;
         std::memcpy(fresh.data() + lay.o_mstat, old.data() + lay.o_mstat, 2 * lay.nmv * sizeof(long long));
-        CU(cudaMemcpy(d_arena.p + off, fresh.data(), lay.bytes, cudaMemcpyHostToDevice));
+        CU(copy(d_arena.p + off, fresh.data(), lay.bytes, cudaMemcpyHostToDevice));
         LdoLaunch L = launch_params(LDO_MODE_INIT, 0);
         L.only_rep = r;
         CU(ldo_launch_mc(L, stream));
         CU(cudaStreamSynchronize(stream));
         LdoHdr h;
-        CU(cudaMemcpy(&h, d_arena.p + off + lay.o_hdr, sizeof h, cudaMemcpyDeviceToHost));
+        CU(copy(&h, d_arena.p + off + lay.o_hdr, sizeof h, cudaMemcpyDeviceToHost));
         if (h.status != 0) {
-            CU(cudaMemcpy(d_arena.p + off, old.data(), lay.bytes, cudaMemcpyHostToDevice));
+            CU(copy(d_arena.p + off, old.data(), lay.bytes, cudaMemcpyHostToDevice));
             throw LdoError(LDO_EINVAL, h.status == LDO_RS_INVARIANT
                                            ? "Constaints in violation after move complete"
                                            : "configuration does not fit the replica's capacity");
@@ -855,7 +866,7 @@ struct ldo_engine {
     // launch for the batch; all or nothing.
     void set_configs(const int32_t* bufs, const int32_t* off) {
         vector<unsigned char> old((size_t)n_rep * lay.bytes), fresh((size_t)n_rep * lay.bytes, 0);
-        CU(cudaMemcpy(old.data(), d_arena.p, old.size(), cudaMemcpyDeviceToHost));
+        CU(copy(old.data(), d_arena.p, old.size(), cudaMemcpyDeviceToHost));
         for (int r = 0; r < n_rep; ++r) {
             if (off[r] < 0 || off[r + 1] < off[r]) throw LdoError(LDO_EINVAL, "configuration offsets not increasing");
             vector<ldo_io::ChainConf> chains = parse_config(bufs + off[r], off[r + 1] - off[r]);
@@ -869,15 +880,15 @@ struct ldo_engine {
             hn->sample_count = ho->sample_count;
             std::memcpy(b + lay.o_mstat, o + lay.o_mstat, 2 * lay.nmv * sizeof(long long));
         }
-        CU(cudaMemcpy(d_arena.p, fresh.data(), fresh.size(), cudaMemcpyHostToDevice));
+        CU(copy(d_arena.p, fresh.data(), fresh.size(), cudaMemcpyHostToDevice));
         LdoLaunch L = launch_params(LDO_MODE_INIT, 0);
         CU(ldo_launch_mc(L, stream));
         CU(cudaStreamSynchronize(stream));
-        CU(cudaMemcpy(fresh.data(), d_arena.p, fresh.size(), cudaMemcpyDeviceToHost));
+        CU(copy(fresh.data(), d_arena.p, fresh.size(), cudaMemcpyDeviceToHost));
         for (int r = 0; r < n_rep; ++r) {
             const auto* h = reinterpret_cast<const LdoHdr*>(fresh.data() + (size_t)r * lay.bytes + lay.o_hdr);
             if (h->status != 0) {
-                CU(cudaMemcpy(d_arena.p, old.data(), old.size(), cudaMemcpyHostToDevice));
+                CU(copy(d_arena.p, old.data(), old.size(), cudaMemcpyHostToDevice));
                 throw LdoError(LDO_EINVAL, "replica " + std::to_string(r) + ": " +
                                                (h->status == LDO_RS_INVARIANT
                                                     ? "Constaints in violation after move complete"
@@ -957,9 +968,9 @@ struct ldo_engine {
             k.mult = std::get<2>(kv.first);
         }
         vector<unsigned char> arena((size_t)n_rep * lay.bytes);
-        CU(cudaMemcpy(arena.data(), d_arena.p, arena.size(), cudaMemcpyDeviceToHost));
+        CU(copy(arena.data(), d_arena.p, arena.size(), cudaMemcpyDeviceToHost));
         vector<double> table(LDO_LEARN_TABLE);
-        CU(cudaMemcpy(table.data(), d_learn_w.p, table.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        CU(copy(table.data(), d_learn_w.p, table.size() * sizeof(double), cudaMemcpyDeviceToHost));
         std::string out(sizeof H, '\0');
         auto put = [&](const void* p, size_t bytes) { out.append(reinterpret_cast<const char*>(p), bytes); };
         put(keys.data(), keys.size() * sizeof(CkptTab));
@@ -972,7 +983,7 @@ struct ldo_engine {
         put(table.data(), table.size() * sizeof(double));
         if (mlp_init) {
             vector<float> params(LDO_LEARN_NPARAM);
-            CU(cudaMemcpy(params.data(), mlp.params, params.size() * sizeof(float), cudaMemcpyDeviceToHost));
+            CU(copy(params.data(), mlp.params, params.size() * sizeof(float), cudaMemcpyDeviceToHost));
             put(params.data(), params.size() * sizeof(float));
         }
         if (pt_rungs) {
@@ -981,12 +992,12 @@ struct ldo_engine {
             vector<double> rep_q(4 * (size_t)n_rep);
             vector<unsigned long long> draws(nl);
             vector<long long> att(std::max(pt_nctr, 1)), acc(std::max(pt_nctr, 1));
-            CU(cudaMemcpy(perm.data(), d_perm.p, perm.size() * sizeof(int), cudaMemcpyDeviceToHost));
-            CU(cudaMemcpy(rep_q.data(), d_rep_q.p, rep_q.size() * sizeof(double), cudaMemcpyDeviceToHost));
-            CU(cudaMemcpy(draws.data(), d_pt_draws.p, draws.size() * sizeof(unsigned long long),
+            CU(copy(perm.data(), d_perm.p, perm.size() * sizeof(int), cudaMemcpyDeviceToHost));
+            CU(copy(rep_q.data(), d_rep_q.p, rep_q.size() * sizeof(double), cudaMemcpyDeviceToHost));
+            CU(copy(draws.data(), d_pt_draws.p, draws.size() * sizeof(unsigned long long),
                           cudaMemcpyDeviceToHost));
-            CU(cudaMemcpy(att.data(), d_pt_att.p, att.size() * sizeof(long long), cudaMemcpyDeviceToHost));
-            CU(cudaMemcpy(acc.data(), d_pt_acc.p, acc.size() * sizeof(long long), cudaMemcpyDeviceToHost));
+            CU(copy(att.data(), d_pt_att.p, att.size() * sizeof(long long), cudaMemcpyDeviceToHost));
+            CU(copy(acc.data(), d_pt_acc.p, acc.size() * sizeof(long long), cudaMemcpyDeviceToHost));
             put(perm.data(), perm.size() * sizeof(int));
             put(rep_q.data(), rep_q.size() * sizeof(double));
             put(draws.data(), draws.size() * sizeof(unsigned long long));
@@ -1044,42 +1055,20 @@ struct ldo_engine {
             params.resize(LDO_LEARN_NPARAM);
             get(params.data(), params.size() * sizeof(float));
         }
-        // energy tables of the saved keys, in this engine's numbering
-        vector<int> remap(H.n_tabs);
-        for (size_t i = 0; i < keys.size(); ++i) {
-            if (keys[i].sys < 0 || keys[i].sys >= (int)systems.size())
-                throw LdoError(LDO_EINVAL, path + ": bad table key");
-            remap[i] = table_for(keys[i].sys, keys[i].temp, keys[i].mult);
-        }
-        auto tab = [&](int k) {
-            if (k < 0 || k >= (int)remap.size()) throw LdoError(LDO_EINVAL, path + ": bad table index");
-            return remap[k];
-        };
-        for (int r = 0; r < n_rep; ++r) {
-            if (ctl[r].sys != sys_of[r] || ctl[r].rep != (uint32_t)r)
-                throw LdoError(LDO_EINVAL, path + ": replica controls do not match this engine");
-            for (int b = 0; b < LDO_MAX_BIASES; ++b)
-                if (ctl[r].grid_off[b] != h_ctl[r].grid_off[b])
-                    throw LdoError(LDO_EINVAL, path + ": grid layout does not match this engine");
-            ctl[r].tab = tab(ctl[r].tab);
-            auto* h = reinterpret_cast<LdoHdr*>(arena.data() + (size_t)r * lay.bytes + lay.o_hdr);
-            h->tab = tab(h->tab);
-        }
-        // ladder: set up its shape, then the saved permutation and counters
-        if (pt_graph) {
-            cudaGraphExecDestroy(pt_graph);
-            pt_graph = nullptr;
-        }
-        seed = H.seed;
-        pt_rungs = 0;
+        // ladder payload, read and checked before anything of the engine changes
+        vector<int> perm;
+        vector<double> rep_q;
+        vector<unsigned long long> draws;
+        vector<long long> att, acc;
         if (H.pt_rungs) {
-            pt_setup(H.pt_rungs, H.pt_q, H.pt_dim2);
-            if (pt_nctr != H.pt_nctr) throw LdoError(LDO_EINVAL, path + ": ladder does not match the input files");
-            int nl = n_rep / pt_rungs;
-            vector<int> perm(n_rep);
-            vector<double> rep_q(4 * (size_t)n_rep);
-            vector<unsigned long long> draws(nl);
-            vector<long long> att(std::max(pt_nctr, 1)), acc(std::max(pt_nctr, 1));
+            if (pt_check(H.pt_rungs, H.pt_q, H.pt_dim2) != H.pt_nctr)
+                throw LdoError(LDO_EINVAL, path + ": ladder does not match the input files");
+            int nl = n_rep / H.pt_rungs;
+            perm.resize(n_rep);
+            rep_q.resize(4 * (size_t)n_rep);
+            draws.resize(nl);
+            att.resize(std::max(H.pt_nctr, 1));
+            acc.resize(std::max(H.pt_nctr, 1));
             get(perm.data(), perm.size() * sizeof(int));
             get(rep_q.data(), rep_q.size() * sizeof(double));
             get(draws.data(), draws.size() * sizeof(unsigned long long));
@@ -1090,12 +1079,46 @@ struct ldo_engine {
                 if (r < 0 || r >= n_rep || seen[r]) throw LdoError(LDO_EINVAL, path + ": bad ladder permutation");
                 seen[r] = 1;
             }
-            CU(cudaMemcpy(d_perm.p, perm.data(), perm.size() * sizeof(int), cudaMemcpyHostToDevice));
-            CU(cudaMemcpy(d_rep_q.p, rep_q.data(), rep_q.size() * sizeof(double), cudaMemcpyHostToDevice));
-            CU(cudaMemcpy(d_pt_draws.p, draws.data(), draws.size() * sizeof(unsigned long long),
+        }
+        for (size_t i = 0; i < keys.size(); ++i)
+            if (keys[i].sys < 0 || keys[i].sys >= (int)systems.size())
+                throw LdoError(LDO_EINVAL, path + ": bad table key");
+        auto check_tab = [&](int k) {
+            if (k < 0 || k >= (int)keys.size()) throw LdoError(LDO_EINVAL, path + ": bad table index");
+        };
+        for (int r = 0; r < n_rep; ++r) {
+            if (ctl[r].sys != sys_of[r] || ctl[r].rep != (uint32_t)r)
+                throw LdoError(LDO_EINVAL, path + ": replica controls do not match this engine");
+            for (int b = 0; b < LDO_MAX_BIASES; ++b)
+                if (ctl[r].grid_off[b] != h_ctl[r].grid_off[b])
+                    throw LdoError(LDO_EINVAL, path + ": grid layout does not match this engine");
+            check_tab(ctl[r].tab);
+            check_tab(reinterpret_cast<const LdoHdr*>(arena.data() + (size_t)r * lay.bytes + lay.o_hdr)->tab);
+        }
+        // Every check has passed: from here on the engine takes the file's
+        // state.  Energy tables of the saved keys, in this engine's numbering.
+        vector<int> remap(H.n_tabs);
+        for (size_t i = 0; i < keys.size(); ++i) remap[i] = table_for(keys[i].sys, keys[i].temp, keys[i].mult);
+        for (int r = 0; r < n_rep; ++r) {
+            ctl[r].tab = remap[ctl[r].tab];
+            auto* h = reinterpret_cast<LdoHdr*>(arena.data() + (size_t)r * lay.bytes + lay.o_hdr);
+            h->tab = remap[h->tab];
+        }
+        // ladder: set up its shape, then the saved permutation and counters
+        if (pt_graph) {
+            cudaGraphExecDestroy(pt_graph);
+            pt_graph = nullptr;
+        }
+        seed = H.seed;
+        pt_rungs = 0;
+        if (H.pt_rungs) {
+            pt_setup(H.pt_rungs, H.pt_q, H.pt_dim2);
+            CU(copy(d_perm.p, perm.data(), perm.size() * sizeof(int), cudaMemcpyHostToDevice));
+            CU(copy(d_rep_q.p, rep_q.data(), rep_q.size() * sizeof(double), cudaMemcpyHostToDevice));
+            CU(copy(d_pt_draws.p, draws.data(), draws.size() * sizeof(unsigned long long),
                           cudaMemcpyHostToDevice));
-            CU(cudaMemcpy(d_pt_att.p, att.data(), att.size() * sizeof(long long), cudaMemcpyHostToDevice));
-            CU(cudaMemcpy(d_pt_acc.p, acc.data(), acc.size() * sizeof(long long), cudaMemcpyHostToDevice));
+            CU(copy(d_pt_att.p, att.data(), att.size() * sizeof(long long), cudaMemcpyHostToDevice));
+            CU(copy(d_pt_acc.p, acc.data(), acc.size() * sizeof(long long), cudaMemcpyHostToDevice));
             pt_swap_i = H.pt_swap_i;
         }
         h_ctl = ctl;
@@ -1106,11 +1129,11 @@ struct ldo_engine {
         upload_tables();
         upload_ctl();
         upload_grid();
-        CU(cudaMemcpy(d_arena.p, arena.data(), arena.size(), cudaMemcpyHostToDevice));
-        CU(cudaMemcpy(d_learn_w.p, table.data(), table.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CU(copy(d_arena.p, arena.data(), arena.size(), cudaMemcpyHostToDevice));
+        CU(copy(d_learn_w.p, table.data(), table.size() * sizeof(double), cudaMemcpyHostToDevice));
         if (H.has_mlp) {
             mlp_ensure(0);
-            CU(cudaMemcpy(mlp.params, params.data(), params.size() * sizeof(float), cudaMemcpyHostToDevice));
+            CU(copy(mlp.params, params.data(), params.size() * sizeof(float), cudaMemcpyHostToDevice));
             CU(ldo_mlp_sync_weights(mlp, stream));
         }
         CU(cudaStreamSynchronize(stream));
@@ -1123,7 +1146,7 @@ struct ldo_engine {
         if (!mlp.params) CU(ldo_mlp_alloc(mlp, kMlpCap));
         if (!mlp_init) {
             vector<float> p = ldo_learn_init_params(seed);
-            CU(cudaMemcpy(mlp.params, p.data(), p.size() * sizeof(float), cudaMemcpyHostToDevice));
+            CU(copy(mlp.params, p.data(), p.size() * sizeof(float), cudaMemcpyHostToDevice));
             CU(ldo_mlp_sync_weights(mlp, stream));
             mlp_init = true;
         }
@@ -1140,8 +1163,8 @@ struct ldo_engine {
     // batch), then the weight table.
     void learn_train(int iters, double lr, uint32_t seed, double* loss0, double* loss1) {
         vector<float> cb(LDO_LEARN_TABLE), ct(LDO_LEARN_TABLE);
-        CU(cudaMemcpy(cb.data(), d_cnt_b.p, cb.size() * sizeof(float), cudaMemcpyDeviceToHost));
-        CU(cudaMemcpy(ct.data(), d_cnt_t.p, ct.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        CU(copy(cb.data(), d_cnt_b.p, cb.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        CU(copy(ct.data(), d_cnt_t.p, ct.size() * sizeof(float), cudaMemcpyDeviceToHost));
         vector<int32_t> idx;
         vector<float> bb, tt;
         double norm = 0;
@@ -1156,9 +1179,9 @@ struct ldo_engine {
         if ((int)idx.size() > kMlpCap) throw LdoError(LDO_EINVAL, "too many distinct network inputs");
         mlp_ensure(seed);
         int n = (int)idx.size();
-        CU(cudaMemcpy(mlp.idx, idx.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice));
-        CU(cudaMemcpy(mlp.cnt_b, bb.data(), n * sizeof(float), cudaMemcpyHostToDevice));
-        CU(cudaMemcpy(mlp.cnt_t, tt.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+        CU(copy(mlp.idx, idx.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice));
+        CU(copy(mlp.cnt_b, bb.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+        CU(copy(mlp.cnt_t, tt.data(), n * sizeof(float), cudaMemcpyHostToDevice));
         for (int it = 0; it < iters; ++it) {
             CU(ldo_mlp_loss_grad(mlp, n, norm, stream));
             if (it == 0 && loss0) CU(cudaMemcpyAsync(loss0, mlp.loss, sizeof(double), cudaMemcpyDeviceToHost, stream));
@@ -1183,10 +1206,12 @@ struct ldo_engine {
     // stacking_mults (dim2 = number of stacking multipliers), slot
     // k = i * dim2 + j, exchanging temperature, staple chemical potential and
     // stacking multiplier (src/ptmc_simulation.cpp:428-481).
-    void pt_setup(int n_rungs, int exchange_q, int dim2 = 0) {
+    // The checks of pt_setup, without changing the engine: throws for a
+    // ladder these input files cannot form, else returns its number of
+    // attempt/accept counters.
+    int pt_check(int n_rungs, int exchange_q, int dim2) const {
         if (n_rungs < 2 || n_rep % n_rungs != 0) throw LdoError(LDO_EINVAL, "replicas must form whole ladders of n_rungs");
         if (!(exchange_q & 1)) throw LdoError(LDO_EINVAL, "every exchange variant exchanges the temperature");
-        int nl = n_rep / n_rungs;
         for (int r = 0; r < n_rep; ++r)
             if (sys_of[r] != sys_of[(r / n_rungs) * n_rungs])
                 throw LdoError(LDO_EINVAL, "replicas of one ladder must share a system");
@@ -1194,6 +1219,24 @@ struct ldo_engine {
         for (auto& s : systems)
             if (&s != &hs && s.desc.n_types != hs.desc.n_types)
                 throw LdoError(LDO_EINVAL, "ladders must have the same staple types");
+        const ldo_io::Params& p = hs.p;
+        if (dim2 == 0) {
+            if ((int)p.temps.size() != n_rungs) throw LdoError(LDO_EINVAL, "temps must list one temperature per rung");
+            for (auto* v : {&p.chem_pot_mults, &p.bias_mults, &p.stacking_mults})
+                if (!v->empty() && (int)v->size() != n_rungs)
+                    throw LdoError(LDO_EINVAL, "chem_pot_mults, bias_mults and stacking_mults must list one value per rung");
+            return n_rungs - 1;
+        }
+        int d1 = (int)p.temps.size(), d2 = (int)p.stacking_mults.size();
+        if (d2 != dim2 || d1 * d2 != n_rungs || d1 < 1 || d2 < 1)
+            throw LdoError(LDO_EINVAL, "a 2-D ladder needs temps x stacking_mults slots");
+        return 2 * d1 * d2;
+    }
+
+    void pt_setup(int n_rungs, int exchange_q, int dim2 = 0) {
+        pt_check(n_rungs, exchange_q, dim2);
+        int nl = n_rep / n_rungs;
+        const HostSystem& hs = systems[sys_of[0]];
         const ldo_io::Params& p = hs.p;
         vector<double> tq, uq, bq, sq;
         // pair schedule: sets of (slot a, slot b, counter) in the reference's loop order
@@ -1282,21 +1325,21 @@ struct ldo_engine {
         upload_tables();
         upload_ctl();
         d_slot_q.alloc(slot.size());
-        CU(cudaMemcpy(d_slot_q.p, slot.data(), slot.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CU(copy(d_slot_q.p, slot.data(), slot.size() * sizeof(double), cudaMemcpyHostToDevice));
         d_red_u.alloc(red.size());
-        CU(cudaMemcpy(d_red_u.p, red.data(), red.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CU(copy(d_red_u.p, red.data(), red.size() * sizeof(double), cudaMemcpyHostToDevice));
         d_rep_q.alloc(rep_q.size());
-        CU(cudaMemcpy(d_rep_q.p, rep_q.data(), rep_q.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CU(copy(d_rep_q.p, rep_q.data(), rep_q.size() * sizeof(double), cudaMemcpyHostToDevice));
         d_perm.alloc(perm.size());
-        CU(cudaMemcpy(d_perm.p, perm.data(), perm.size() * sizeof(int), cudaMemcpyHostToDevice));
+        CU(copy(d_perm.p, perm.data(), perm.size() * sizeof(int), cudaMemcpyHostToDevice));
         d_tab_slot.alloc(n_rungs);
-        CU(cudaMemcpy(d_tab_slot.p, tab_slot.data(), n_rungs * sizeof(int), cudaMemcpyHostToDevice));
+        CU(copy(d_tab_slot.p, tab_slot.data(), n_rungs * sizeof(int), cudaMemcpyHostToDevice));
         d_pt_draws.alloc(nl);
-        CU(cudaMemset(d_pt_draws.p, 0, nl * sizeof(unsigned long long)));
+        CU(cudaMemsetAsync(d_pt_draws.p, 0, nl * sizeof(unsigned long long), stream));
         d_pt_att.alloc(std::max(n_ctr, 1));
         d_pt_acc.alloc(std::max(n_ctr, 1));
-        CU(cudaMemset(d_pt_att.p, 0, std::max(n_ctr, 1) * sizeof(long long)));
-        CU(cudaMemset(d_pt_acc.p, 0, std::max(n_ctr, 1) * sizeof(long long)));
+        CU(cudaMemsetAsync(d_pt_att.p, 0, std::max(n_ctr, 1) * sizeof(long long), stream));
+        CU(cudaMemsetAsync(d_pt_acc.p, 0, std::max(n_ctr, 1) * sizeof(long long), stream));
         vector<int> set_start(1, 0), pa, pb, pc;
         for (auto& st : sets) {
             for (auto& t : st) {
@@ -1311,7 +1354,7 @@ struct ldo_engine {
         sched.insert(sched.end(), pb.begin(), pb.end());
         sched.insert(sched.end(), pc.begin(), pc.end());
         d_pt_sched.alloc(std::max<size_t>(sched.size(), 1));
-        CU(cudaMemcpy(d_pt_sched.p, sched.data(), sched.size() * sizeof(int), cudaMemcpyHostToDevice));
+        CU(copy(d_pt_sched.p, sched.data(), sched.size() * sizeof(int), cudaMemcpyHostToDevice));
         pt = LdoPT {};
         pt.n_ladders = nl;
         pt.n_rungs = n_rungs;
@@ -1357,7 +1400,7 @@ struct ldo_engine {
         d_hist_perm.alloc((size_t)cap * nl * pt_rungs);
         d_hist_step.alloc((size_t)cap * nl);
         d_hist_n.alloc(nl);
-        CU(cudaMemset(d_hist_n.p, 0, nl * sizeof(long long)));
+        CU(cudaMemsetAsync(d_hist_n.p, 0, nl * sizeof(long long), stream));
         hist_cap = cap;
         pt.hist_perm = d_hist_perm.p;
         pt.hist_step = d_hist_step.p;
@@ -1437,9 +1480,9 @@ struct ldo_engine {
         }
         // host mirror of the replicas' current temperatures
         vector<double> rq(4 * n_rep);
-        CU(cudaMemcpy(rq.data(), d_rep_q.p, rq.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        CU(copy(rq.data(), d_rep_q.p, rq.size() * sizeof(double), cudaMemcpyDeviceToHost));
         for (int r = 0; r < n_rep; ++r) temps[r] = rq[4 * r];
-        CU(cudaMemcpy(h_ctl.data(), d_ctl.p, h_ctl.size() * sizeof(LdoRepCtl), cudaMemcpyDeviceToHost));
+        CU(copy(h_ctl.data(), d_ctl.p, h_ctl.size() * sizeof(LdoRepCtl), cudaMemcpyDeviceToHost));
         check_status();
     }
     LdoLaunch pt_graph_L {};
@@ -1534,7 +1577,7 @@ struct ldo_engine {
         }
         upload_ctl();
         upload_grid();
-        CU(cudaMemcpy(d_us_window.p, us_window_of.data(), n_rep * sizeof(int), cudaMemcpyHostToDevice));
+        CU(copy(d_us_window.p, us_window_of.data(), n_rep * sizeof(int), cudaMemcpyHostToDevice));
     }
 
     void us_launch(long long steps, bool record) {
@@ -1663,7 +1706,7 @@ struct ldo_engine {
 
     vector<unsigned char> download_arena() {
         vector<unsigned char> host((size_t)n_rep * lay.bytes);
-        CU(cudaMemcpy(host.data(), d_arena.p, host.size(), cudaMemcpyDeviceToHost));
+        CU(copy(host.data(), d_arena.p, host.size(), cudaMemcpyDeviceToHost));
         return host;
     }
 };
@@ -1791,7 +1834,7 @@ ldo_status ldo_get_config(ldo_engine* e, int replica, int32_t* buf, int cap, int
     if (!e || replica < 0 || replica >= e->n_rep || !buf) return LDO_EINVAL;
     return guard(e, [&]() {
         vector<unsigned char> b(e->lay.bytes);
-        CU(cudaMemcpy(b.data(), e->d_arena.p + (size_t)replica * e->lay.bytes, b.size(), cudaMemcpyDeviceToHost));
+        CU(e->copy(b.data(), e->d_arena.p + (size_t)replica * e->lay.bytes, b.size(), cudaMemcpyDeviceToHost));
         const LdoLayout& y = e->lay;
         const LdoSys& d = e->systems[e->sys_of[replica]].desc;
         const auto* h = reinterpret_cast<const LdoHdr*>(b.data() + y.o_hdr);
@@ -1917,19 +1960,19 @@ ldo_status ldo_set_sampling(ldo_engine* e, int interval, int capacity) {
         e->sample_interval = interval;
         e->sample_cap = capacity;
         e->d_samples.alloc((size_t)e->n_rep * std::max(capacity, 1) * 2);
-        CU(cudaMemset(e->d_samples.p, 0, e->d_samples.n * sizeof(int16_t)));
+        CU(cudaMemsetAsync(e->d_samples.p, 0, e->d_samples.n * sizeof(int16_t), e->stream));
         // restart the per-replica sample counters
         auto host = e->download_arena();
         for (int r = 0; r < e->n_rep; ++r)
             reinterpret_cast<LdoHdr*>(host.data() + (size_t)r * e->lay.bytes + e->lay.o_hdr)->sample_count = 0;
-        CU(cudaMemcpy(e->d_arena.p, host.data(), host.size(), cudaMemcpyHostToDevice));
+        CU(e->copy(e->d_arena.p, host.data(), host.size(), cudaMemcpyHostToDevice));
     });
 }
 
 ldo_status ldo_get_samples(ldo_engine* e, int16_t* out, int capacity, int* count) {
     if (!e || !out || capacity != e->sample_cap) return LDO_EINVAL;
     return guard(e, [&]() {
-        CU(cudaMemcpy(out, e->d_samples.p, (size_t)e->n_rep * capacity * 2 * sizeof(int16_t), cudaMemcpyDeviceToHost));
+        CU(e->copy(out, e->d_samples.p, (size_t)e->n_rep * capacity * 2 * sizeof(int16_t), cudaMemcpyDeviceToHost));
         if (count) {
             auto host = e->download_arena();
             for (int r = 0; r < e->n_rep; ++r)
@@ -1945,14 +1988,14 @@ ldo_status ldo_set_trace(ldo_engine* e, int n_trace, int max_steps) {
         e->n_trace = std::min(n_trace, e->n_rep);
         e->trace_max = max_steps;
         e->d_trace.alloc((size_t)std::max(e->n_trace, 1) * std::max(max_steps, 1) * 8);
-        CU(cudaMemset(e->d_trace.p, 0, e->d_trace.n * sizeof(double)));
+        CU(cudaMemsetAsync(e->d_trace.p, 0, e->d_trace.n * sizeof(double), e->stream));
     });
 }
 
 ldo_status ldo_get_trace(ldo_engine* e, double* out, int n_trace, int max_steps) {
     if (!e || !out || n_trace != e->n_trace || max_steps != e->trace_max) return LDO_EINVAL;
     return guard(e, [&]() {
-        CU(cudaMemcpy(out, e->d_trace.p, (size_t)n_trace * max_steps * 8 * sizeof(double), cudaMemcpyDeviceToHost));
+        CU(e->copy(out, e->d_trace.p, (size_t)n_trace * max_steps * 8 * sizeof(double), cudaMemcpyDeviceToHost));
     });
 }
 
@@ -1997,7 +2040,7 @@ ldo_status ldo_pt_run(ldo_engine* e, int n_rungs, int64_t swaps, int exchange_in
 
 ldo_status ldo_pt_get_permutation(ldo_engine* e, int32_t* out, int n) {
     if (!e || !out || e->pt_rungs == 0 || n != e->n_rep) return LDO_EINVAL;
-    return guard(e, [&]() { CU(cudaMemcpy(out, e->d_perm.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost)); });
+    return guard(e, [&]() { CU(e->copy(out, e->d_perm.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost)); });
 }
 
 ldo_status ldo_pt2d_run(ldo_engine* e, int n_temps, int n_stacking, int64_t swaps, int exchange_interval,
@@ -2011,8 +2054,8 @@ ldo_status ldo_pt2d_run(ldo_engine* e, int n_temps, int n_stacking, int64_t swap
 ldo_status ldo_pt_get_stats(ldo_engine* e, int64_t* attempts, int64_t* accepts, int n_pairs) {
     if (!e || !attempts || !accepts || e->pt_rungs == 0 || n_pairs != e->pt_nctr) return LDO_EINVAL;
     return guard(e, [&]() {
-        CU(cudaMemcpy(attempts, e->d_pt_att.p, n_pairs * sizeof(int64_t), cudaMemcpyDeviceToHost));
-        CU(cudaMemcpy(accepts, e->d_pt_acc.p, n_pairs * sizeof(int64_t), cudaMemcpyDeviceToHost));
+        CU(e->copy(attempts, e->d_pt_att.p, n_pairs * sizeof(int64_t), cudaMemcpyDeviceToHost));
+        CU(e->copy(accepts, e->d_pt_acc.p, n_pairs * sizeof(int64_t), cudaMemcpyDeviceToHost));
     });
 }
 
@@ -2181,16 +2224,16 @@ ldo_status ldo_learn_collect(ldo_engine* e) {
 ldo_status ldo_learn_reset_counts(ldo_engine* e) {
     if (!e) return LDO_EINVAL;
     return guard(e, [&]() {
-        CU(cudaMemset(e->d_cnt_b.p, 0, LDO_LEARN_TABLE * sizeof(float)));
-        CU(cudaMemset(e->d_cnt_t.p, 0, LDO_LEARN_TABLE * sizeof(float)));
+        CU(cudaMemsetAsync(e->d_cnt_b.p, 0, LDO_LEARN_TABLE * sizeof(float), e->stream));
+        CU(cudaMemsetAsync(e->d_cnt_t.p, 0, LDO_LEARN_TABLE * sizeof(float), e->stream));
     });
 }
 
 ldo_status ldo_learn_get_counts(ldo_engine* e, float* cnt_bound, float* cnt_total, int n) {
     if (!e || !cnt_bound || !cnt_total || n != LDO_LEARN_TABLE) return LDO_EINVAL;
     return guard(e, [&]() {
-        CU(cudaMemcpy(cnt_bound, e->d_cnt_b.p, n * sizeof(float), cudaMemcpyDeviceToHost));
-        CU(cudaMemcpy(cnt_total, e->d_cnt_t.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+        CU(e->copy(cnt_bound, e->d_cnt_b.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+        CU(e->copy(cnt_total, e->d_cnt_t.p, n * sizeof(float), cudaMemcpyDeviceToHost));
     });
 }
 
@@ -2203,7 +2246,7 @@ ldo_status ldo_learn_set_params(ldo_engine* e, const float* params, int n) {
     if (!e || !params || n != LDO_LEARN_NPARAM) return LDO_EINVAL;
     return guard(e, [&]() {
         e->mlp_ensure(0);
-        CU(cudaMemcpy(e->mlp.params, params, n * sizeof(float), cudaMemcpyHostToDevice));
+        CU(e->copy(e->mlp.params, params, n * sizeof(float), cudaMemcpyHostToDevice));
         CU(ldo_mlp_sync_weights(e->mlp, e->stream));
         CU(ldo_mlp_table(e->mlp, e->d_learn_w.p, e->stream));
         e->mlp_check();
@@ -2214,18 +2257,18 @@ ldo_status ldo_learn_get_params(ldo_engine* e, float* params, int n) {
     if (!e || !params || n != LDO_LEARN_NPARAM) return LDO_EINVAL;
     return guard(e, [&]() {
         e->mlp_ensure(0);
-        CU(cudaMemcpy(params, e->mlp.params, n * sizeof(float), cudaMemcpyDeviceToHost));
+        CU(e->copy(params, e->mlp.params, n * sizeof(float), cudaMemcpyDeviceToHost));
     });
 }
 
 ldo_status ldo_learn_get_table(ldo_engine* e, double* weights, int n) {
     if (!e || !weights || n != LDO_LEARN_TABLE) return LDO_EINVAL;
-    return guard(e, [&]() { CU(cudaMemcpy(weights, e->d_learn_w.p, n * sizeof(double), cudaMemcpyDeviceToHost)); });
+    return guard(e, [&]() { CU(e->copy(weights, e->d_learn_w.p, n * sizeof(double), cudaMemcpyDeviceToHost)); });
 }
 
 ldo_status ldo_learn_set_table(ldo_engine* e, const double* weights, int n) {
     if (!e || !weights || n != LDO_LEARN_TABLE) return LDO_EINVAL;
-    return guard(e, [&]() { CU(cudaMemcpy(e->d_learn_w.p, weights, n * sizeof(double), cudaMemcpyHostToDevice)); });
+    return guard(e, [&]() { CU(e->copy(e->d_learn_w.p, weights, n * sizeof(double), cudaMemcpyHostToDevice)); });
 }
 
 ldo_status ldo_learn_loss_grad(const float* params, const int32_t* idx, const float* cnt_bound, const float* cnt_total,
@@ -2279,7 +2322,7 @@ ldo_out::Snapshot replica_snapshot(ldo_engine* e, int replica, const vector<int>
     CU(ldo_launch_mc(L, e->stream));
     CU(cudaStreamSynchronize(e->stream));
     vector<unsigned char> b(e->lay.bytes);
-    CU(cudaMemcpy(b.data(), e->d_arena.p + (size_t)replica * e->lay.bytes, b.size(), cudaMemcpyDeviceToHost));
+    CU(e->copy(b.data(), e->d_arena.p + (size_t)replica * e->lay.bytes, b.size(), cudaMemcpyDeviceToHost));
     const LdoLayout& y = e->lay;
     const LdoSys& d = e->systems[e->sys_of[replica]].desc;
     const auto* h = reinterpret_cast<const LdoHdr*>(b.data() + y.o_hdr);
@@ -2378,7 +2421,7 @@ ldo_status ldo_swap_writer_open(ldo_engine* e, int n_rungs, int exchange_q, int 
         wr->swp_ladder = ladder;
         wr->swp_freq = freq;
         long long n = 0;
-        CU(cudaMemcpy(&n, e->d_hist_n.p + ladder, sizeof(long long), cudaMemcpyDeviceToHost));
+        CU(e->copy(&n, e->d_hist_n.p + ladder, sizeof(long long), cudaMemcpyDeviceToHost));
         wr->swp_read = n;
         string name = string(filebase) + ".swp";
         wr->swp.open(name);
@@ -2403,22 +2446,22 @@ void swap_writer_write(ldo_writer* w, int64_t step) {
     int R = e->pt_rungs, nl = e->n_rep / R, lad = w->swp_ladder;
     if (e->hist_cap == 0) throw LdoError(LDO_EINVAL, "the swap history was dropped (the ladder was set up again)");
     long long n = 0;
-    CU(cudaMemcpy(&n, e->d_hist_n.p + lad, sizeof(long long), cudaMemcpyDeviceToHost));
+    CU(e->copy(&n, e->d_hist_n.p + lad, sizeof(long long), cudaMemcpyDeviceToHost));
     if (n - w->swp_read > e->hist_cap)
         throw LdoError(LDO_EINVAL, "swap history overflow: write the .swp file at least every 4096 exchanges");
     vector<int> row(R);
     for (long long k = w->swp_read; k < n; ++k) {
         size_t r = (size_t)(k % e->hist_cap) * nl + lad;
         long long st = 0;
-        CU(cudaMemcpy(&st, e->d_hist_step.p + r, sizeof(long long), cudaMemcpyDeviceToHost));
+        CU(e->copy(&st, e->d_hist_step.p + r, sizeof(long long), cudaMemcpyDeviceToHost));
         if (st % w->swp_freq != 0) continue;
-        CU(cudaMemcpy(row.data(), e->d_hist_perm.p + r * R, R * sizeof(int), cudaMemcpyDeviceToHost));
+        CU(e->copy(row.data(), e->d_hist_perm.p + r * R, R * sizeof(int), cudaMemcpyDeviceToHost));
         for (int q = 0; q < R; ++q) w->swp << row[q] - lad * R << " ";
         w->swp << "\n";
     }
     w->swp_read = n;
     if (step >= 0 && step % w->swp_freq == 0) {
-        CU(cudaMemcpy(row.data(), e->d_perm.p + (size_t)lad * R, R * sizeof(int), cudaMemcpyDeviceToHost));
+        CU(e->copy(row.data(), e->d_perm.p + (size_t)lad * R, R * sizeof(int), cudaMemcpyDeviceToHost));
         for (int q = 0; q < R; ++q) w->swp << row[q] - lad * R << " ";
         w->swp << "\n";
     }

@@ -12,8 +12,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <mutex>
-
 #include "ldo_engine.cuh"
 #include "ldo_kernels.h"
 
@@ -390,26 +388,16 @@ __global__ void ldo_status_gather_kernel(const unsigned char* arena, int bytes, 
     }
 }
 
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_lock;
-int* g_scratch_ptr[kMaxDevices] = {};
-
 // Device address of g_status_scratch on the current device.  In host code the
-// array's name is only a host-side stand-in, so the address must come from
-// cudaGetSymbolAddress, called once per device with that device current.
+// array's name is only a host-side stand-in, so the address comes from
+// cudaGetSymbolAddress with the device current.  It is looked up on every
+// call, not cached: after a device reset the module, and with it the array,
+// can be loaded at another address.  The lookup allocates nothing.
 cudaError_t scratch_on_current_device(int** out) {
-    int dev = 0;
-    cudaError_t err = cudaGetDevice(&dev);
+    void* p = nullptr;
+    cudaError_t err = cudaGetSymbolAddress(&p, g_status_scratch);
     if (err != cudaSuccess) return err;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> hold(g_scratch_lock);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        err = cudaGetSymbolAddress(&p, g_status_scratch);
-        if (err != cudaSuccess) return err;
-        g_scratch_ptr[dev] = static_cast<int*>(p);
-    }
-    *out = g_scratch_ptr[dev];
+    *out = static_cast<int*>(p);
     return cudaSuccess;
 }
 

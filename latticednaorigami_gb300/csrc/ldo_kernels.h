@@ -104,8 +104,8 @@ cudaError_t ldo_launch_pt_swap(const LdoPT& P, cudaStream_t stream);
 // Allocation-free status read-out.  The reduction cells and the per-replica
 // copy live in a fixed device array inside the library instead of engine
 // buffers, so the call allocates no memory.  At most LDO_NOALLOC_MAX_REPLICAS
-// replicas.  The first call on a device looks up the array's device address
-// (once per device, under a lock).  Every call uses the same array: calls
+// replicas.  Every call looks up the array's device address with the device
+// current (not cached: a device reset can move it).  Every call uses the same array: calls
 // whose work overlaps on the GPU race.  Copies the results to host memory and
 // synchronises `stream` before returning.
 enum { LDO_NOALLOC_MAX_REPLICAS = 65536 };

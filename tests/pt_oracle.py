@@ -20,7 +20,7 @@ class PTOracle:
     dim2 > 0: the temps x stacking_mults grid of TwoDPTGCMCSimulation
     (src/ptmc_simulation.cpp:428-560), exchanging T, staple u and stacking."""
 
-    def __init__(self, inp, params, n_ladders, seed, exchange_q=1, dim2=0):
+    def __init__(self, inp, params, n_ladders, seed, exchange_q=1, dim2=0, reference_initial_controls=False):
         self.dim2 = dim2
         self.n_ladders = n_ladders
         self.seed = seed
@@ -58,6 +58,17 @@ class PTOracle:
         for l in range(n_ladders):
             for k in range(R):
                 self.ctrl.append({n: self.slot[n][k] for n in self.slot})
+        if reference_initial_controls:
+            # initialize_control_qs (OneD :375-392, TwoD :428-470) stores the
+            # bias multiplier of slot k at index m_bias_i = 1 of the control
+            # vector, the staple-u slot: until a replica's first exchange its
+            # staple u multiplier is that bias multiplier (bias_mults[k]; 1 in
+            # 2-D) and its bias multiplier 0.  The engine starts from
+            # chem_pot_mults (staple_u_mult in 2-D) and bias_mults instead.
+            for l in range(n_ladders):
+                for k in range(R):
+                    c = self.ctrl[l * R + k]
+                    c["u"], c["bias"] = self.slot["bias"][k], 0.0
         self.perm = [[l * R + k for k in range(R)] for l in range(n_ladders)]
         self.draws = [0] * n_ladders
         self.swap_i = 0
@@ -73,8 +84,18 @@ class PTOracle:
         self.acc = [0] * n_ctr
 
     def round(self, exchange_interval):
+        """One PTGCMCSimulation::run round (:106-150): every replica takes its
+        controls and runs exchange_interval steps, then every ladder's master
+        attempts the exchanges of this round's pair set."""
         self.swap_i += 1
-        R = self.n_rungs
+        deps = self.run_interval(exchange_interval)
+        for l in range(self.n_ladders):
+            self.exchange(l, deps)
+
+    def run_interval(self, exchange_interval):
+        """update_control_qs (new energy tables and a full recomputation), the
+        steps, then update_dependent_qs (:152): per replica (H, stacking,
+        bias, staple counts by type) with counts[0] unused."""
         deps = []
         for r, rep in enumerate(self.reps):
             c = self.ctrl[r]
@@ -82,44 +103,71 @@ class PTOracle:
             rep.run(exchange_interval, trace=False)
             H, S, st, bias = rep.dependent_qs()
             deps.append((H, st, bias, staple_counts(rep)))
-        for l in range(self.n_ladders):
-            perm = self.perm[l]
-            for i, i2, ctr in self.sets[self.swap_i % len(self.sets)]:
-                self.att[ctr] += 1
-                t1, t2 = self.slot["temp"][i], self.slot["temp"][i2]
-                sm1, sm2 = self.slot["stack"][i], self.slot["stack"][i2]
-                r1, r2 = perm[i], perm[i2]
-                H1, st1, b1, n1 = deps[r1]
-                H2, st2, b2, n2 = deps[r2]
-                dbu = 0.0
-                for t in range(1, len(n1)):
-                    u1 = self.red_u[t - 1] * self.ctrl[r1]["temp"] * self.ctrl[r1]["u"]
-                    u2 = self.red_u[t - 1] * self.ctrl[r2]["temp"] * self.ctrl[r2]["u"]
-                    dbu += (u2 / t2 - u1 / t1) * (float(n2[t]) - float(n1[t]))
-                DB = 1 / t2 - 1 / t1
-                DH = H2 * t2 - H1 * t1
-                Dst = st2 * t2 - st1 * t1
-                DBM = sm2 / t2 - sm1 / t1
-                DBias = b2 * t2 - b1 * t1
-                p = min(1.0, math.exp(DB * (DH + DBias) + DBM * Dst - dbu))
-                if p == 1:
-                    accept = True
-                else:
-                    accept = p > swap_uniform(self.seed, l, self.draws[l])
-                    self.draws[l] += 1
-                if accept:
-                    self.acc[ctr] += 1
-                    perm[i], perm[i2] = r2, r1
-            for k in range(R):
-                c = self.ctrl[perm[k]]
-                if self.q & 1:
-                    c["temp"] = self.slot["temp"][k]
-                if self.q & 2:
-                    c["u"] = self.slot["u"][k]
-                if self.q & 4:
-                    c["bias"] = self.slot["bias"][k]
-                if self.q & 8:
-                    c["stack"] = self.slot["stack"][k]
+        return deps
+
+    def pairs(self):
+        """(slot a, slot b, counter) tried this round, in the reference's
+        loop order."""
+        return self.sets[self.swap_i % len(self.sets)]
+
+    def staple_u(self, r, t):
+        """Staple chemical potential of type t (1..S) of replica r:
+        update_staple_us, m_reduced_staple_us[t-1] * T * u_mult
+        (src/origami_system.cpp:624)."""
+        return self.red_u[t - 1] * self.ctrl[r]["temp"] * self.ctrl[r]["u"]
+
+    def acceptance(self, i, i2, r1, r2, deps):
+        """calc_acceptance_p (src/ptmc_simulation.cpp:275-313) of exchanging
+        the replicas r1 at slot i and r2 at slot i2, summed over staple types
+        1..S."""
+        t1, t2 = self.slot["temp"][i], self.slot["temp"][i2]
+        sm1, sm2 = self.slot["stack"][i], self.slot["stack"][i2]
+        H1, st1, b1, n1 = deps[r1]
+        H2, st2, b2, n2 = deps[r2]
+        dbu = 0.0
+        for t in range(1, len(n1)):
+            u1 = self.staple_u(r1, t)
+            u2 = self.staple_u(r2, t)
+            dbu += (u2 / t2 - u1 / t1) * (float(n2[t]) - float(n1[t]))
+        DB = 1 / t2 - 1 / t1
+        DH = H2 * t2 - H1 * t1
+        Dst = st2 * t2 - st1 * t1
+        DBM = sm2 / t2 - sm1 / t1
+        DBias = b2 * t2 - b1 * t1
+        return min(1.0, math.exp(DB * (DH + DBias) + DBM * Dst - dbu))
+
+    def exchange(self, l, deps):
+        """attempt_exchange of ladder l (OneD :360-412, TwoD :495-560):
+        acceptance draws only when p != 1 (test_acceptance, :262), then
+        master_send (:212): each replica takes the controls of its slot."""
+        perm = self.perm[l]
+        for i, i2, ctr in self.pairs():
+            self.att[ctr] += 1
+            r1, r2 = perm[i], perm[i2]
+            p = self.acceptance(i, i2, r1, r2, deps)
+            if p == 1:
+                accept = True
+            else:
+                accept = p > swap_uniform(self.seed, l, self.draws[l])
+                self.draws[l] += 1
+            if accept:
+                self.acc[ctr] += 1
+                perm[i], perm[i2] = r2, r1
+        self.send_controls(l)
+
+    def send_controls(self, l):
+        R = self.n_rungs
+        perm = self.perm[l]
+        for k in range(R):
+            c = self.ctrl[perm[k]]
+            if self.q & 1:
+                c["temp"] = self.slot["temp"][k]
+            if self.q & 2:
+                c["u"] = self.slot["u"][k]
+            if self.q & 4:
+                c["bias"] = self.slot["bias"][k]
+            if self.q & 8:
+                c["stack"] = self.slot["stack"][k]
 
     def permutation(self):
         return np.array([x for p in self.perm for x in p], np.int32)

@@ -291,6 +291,26 @@ def write_case(dirname, name, extra=None):
     return path
 
 
+US_WINDOWS = [(0, 8), (4, 14), (10, 20), (16, 24)]
+
+
+def write_us_case(d):
+    """The multi-window umbrella case: the 24-domain g24a system with a
+    square-well window on the number of fully bound domains (tag "win"), a
+    grid bias on it (tag "grid") and the windows file of US_WINDOWS."""
+    os.makedirs(d, exist_ok=True)
+    biases = {"origami": {"bias_functions": [
+        {"label": "window", "tag": "win", "type": "SquareWell", "min_op": 0, "max_op": 24, "well_bias": 0,
+         "outside_bias": 6.0, "ops": ["numfulldomains"], "level": 0},
+        {"label": "grid", "tag": "grid", "type": "Grid", "ops": ["numfulldomains"], "level": 0}]}}
+    with open(os.path.join(d, "us_biases.json"), "w") as f:
+        json.dump(biases, f)
+    with open(os.path.join(d, "us.windows"), "w") as f:
+        f.write("win\n" + "".join("%d, %d\n" % w for w in US_WINDOWS))
+    return write_case(d, "g24a", extra=dict(bias_functions_file="us_biases.json", windows_file="us.windows",
+                                            us_grid_bias_tag="grid", staple_M=1e-2, temp=330))
+
+
 def write_all(dirname):
     return {name: write_case(dirname, name) for name in CASES}
 

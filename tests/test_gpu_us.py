@@ -14,22 +14,11 @@ import systems
 
 pytestmark = pytest.mark.gpu
 
-WINDOWS = [(0, 8), (4, 14), (10, 20), (16, 24)]
+WINDOWS = systems.US_WINDOWS
 
 
 def write_us_case():
-    d = tempfile.mkdtemp()
-    biases = {"origami": {"bias_functions": [
-        {"label": "window", "tag": "win", "type": "SquareWell", "min_op": 0, "max_op": 24, "well_bias": 0,
-         "outside_bias": 6.0, "ops": ["numfulldomains"], "level": 0},
-        {"label": "grid", "tag": "grid", "type": "Grid", "ops": ["numfulldomains"], "level": 0}]}}
-    with open(os.path.join(d, "us_biases.json"), "w") as f:
-        json.dump(biases, f)
-    with open(os.path.join(d, "us.windows"), "w") as f:
-        f.write("win\n" + "".join("%d, %d\n" % w for w in WINDOWS))
-    return systems.write_case(d, "g24a", extra=dict(bias_functions_file="us_biases.json",
-                                                    windows_file="us.windows", us_grid_bias_tag="grid",
-                                                    staple_M=1e-2, temp=330))
+    return systems.write_us_case(tempfile.mkdtemp())
 
 
 @pytest.mark.parametrize("exchange_interval", [0, 50])

@@ -53,6 +53,14 @@ class USOracle:
 
     def exchange(self, swap_i):
         point = [int(self.reps[self.replica_of[w]].observables()["num_fully_bound"]) for w in range(self.nw)]
+        self.exchange_points(point, swap_i)
+        self.apply()
+
+    def exchange_points(self, point, swap_i):
+        """PTMWUSGCMCSimulation::attempt_exchange (:770-864) on the grid
+        points of the windows: pairs (i, i+1) from swap_i % 2, both points
+        inside the other window, acceptance min(1, exp(bias differences))
+        with a draw only when it is not 1 and the points differ."""
         for i in range(swap_i % 2, self.nw - 1, 2):
             self.att[i] += 1
             w1, w2 = i, i + 1
@@ -74,36 +82,42 @@ class USOracle:
                 r1, r2 = self.replica_of[w1], self.replica_of[w2]
                 self.replica_of[w1], self.replica_of[w2] = r2, r1
                 self.window_of[r1], self.window_of[r2] = w2, w1
-        self.apply()
 
     def process(self, hist, max_D):
         for w in range(self.nw):
-            f = hist[w]
-            E = self.E[w]
-            ave = 0.0
-            for x in range(self.len):
-                if f[x] > 0:
-                    ave += f[x] * math.exp(E[x])
-            p = [0.0] * self.len
-            for x in range(self.len):
-                if f[x] > 0:
-                    p[x] = f[x] * math.exp(E[x]) / ave
-                    self.inS[w][x] = True
-            for x in range(self.len):
-                if not self.inS[w][x]:
-                    continue
-                old = E[x]
-                if p[x] == 0:
-                    D = -max_D
-                    nb = old + D
-                else:
-                    nb = math.log(p[x])
-                    D = nb - old
-                upd = nb
-                if abs(D) > max_D:
-                    upd = old + max_D if D > 0 else old - max_D
-                E[x] = upd
+            self.update_window(w, hist[w], max_D)
         self.apply()
+
+    def update_window(self, w, f, max_D):
+        """SimpleUSGCMCSimulation::process_iteration (:160) of window w from
+        its visit counts f: estimate_current_weights (:286) reweights the
+        visited points by the running biases, update_bias (:385) sets
+        ln p for them and -max_D for points seen only before, each change
+        limited to max_D."""
+        E = self.E[w]
+        ave = 0.0
+        for x in range(self.len):
+            if f[x] > 0:
+                ave += f[x] * math.exp(E[x])
+        p = [0.0] * self.len
+        for x in range(self.len):
+            if f[x] > 0:
+                p[x] = f[x] * math.exp(E[x]) / ave
+                self.inS[w][x] = True
+        for x in range(self.len):
+            if not self.inS[w][x]:
+                continue
+            old = E[x]
+            if p[x] == 0:
+                D = -max_D
+                nb = old + D
+            else:
+                nb = math.log(p[x])
+                D = nb - old
+            upd = nb
+            if abs(D) > max_D:
+                upd = old + max_D if D > 0 else old - max_D
+            E[x] = upd
 
     def run(self, n_iters, equil_steps, iter_steps, max_D, exchange_interval=0):
         if equil_steps > 0:
