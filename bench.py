@@ -37,7 +37,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
-SWEEPS_PER_STEP = 100
+# 250 sweeps per step: the default 20 timed steps record 5000 sweeps per
+# replica, more than 50 integrated autocorrelation times of the slowest
+# (24-domain) plain chains, so that tau_int and its confidence interval are
+# settled (the tau_vs_length fields of the line show it).
+SWEEPS_PER_STEP = 250
 N_REP = 4096
 SIZES = [8, 12, 16, 24]
 R_KCAL = 8.3144598 / 4184.0
@@ -167,6 +171,58 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def host_cores():
+    """(threads this process may use, CPUs present on the host)."""
+    try:
+        usable = len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        usable = os.cpu_count() or 1
+    present = usable
+    try:
+        with open("/sys/devices/system/cpu/present") as f:
+            present = 0
+            for part in f.read().strip().split(","):
+                a, _, b = part.partition("-")
+                present += (int(b) - int(a) + 1) if b else 1
+    except OSError:
+        pass
+    return usable, present
+
+
+# Shared-memory roofline of the MC kernel (each replica's state lives in
+# shared memory for a whole launch).  Algorithmic bytes per move attempt of
+# the c2 workload, from the reference's algorithm as the oracle restates it
+# (oracle/touch_counts.py: 16 bytes per domain-record access, 8 per
+# occupancy-map operation, after burn-in, both movesets):
+B_ATTEMPT = {"plain": 8599.0, "learned": 12202.0}
+SMEM_BYTES_PER_CLK_PER_SM = 128
+N_SM = 152
+KERNEL_SOURCES = ["ldo_engine.cuh", "ldo_kernels.cu", "ldo_types.h", "ldo_ct.h", "ldo_math.h", "ldo_learn.h"]
+
+
+def kernel_source_sha():
+    import hashlib
+    h = hashlib.sha256()
+    for name in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, "latticednaorigami_gb300", "csrc", name), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def measured_traffic(workload):
+    """DRAM bytes per launch of the MC kernel from the ncu capture committed
+    under profiles/ for this workload, if it was taken of the current kernel
+    sources (same source hash); else None."""
+    p = os.path.join(ROOT, "profiles", "ldo_mc_kernel_%s_traffic.json" % workload)
+    if not os.path.exists(p):
+        return None, "no capture"
+    with open(p) as f:
+        d = json.load(f)
+    if d.get("kernel_source_sha") != kernel_source_sha():
+        return None, "capture of other kernel sources"
+    return d, "ncu capture of these kernel sources (%s)" % os.path.relpath(p, ROOT)
+
+
 CPU_REPS_PER_SIZE = 128
 # Equilibration.  From empty scaffolds the plain sampler relaxes over hundreds
 # of sweeps (low temperatures, large scaffolds slowest), and tau_int of a
@@ -200,66 +256,79 @@ def replica_temps():
     return np.random.default_rng(0).uniform(320.0, 350.0, N_REP)
 
 
-def cpu_effective_rate(files, cores, burn_sweeps, rec_sweeps):
-    """The oracle port on all host cores over a bounded sample of the same
-    workload: CPU_REPS_PER_SIZE replicas of each scaffold size at the
-    temperatures of the first replicas of that size in the GPU run, burn_sweeps
-    of burn-in from the empty scaffold, then the recorded sweeps, tau_int
-    estimated from its own samples by the same estimator.  Only the recorded
-    sweeps are timed (pro rata).  Returns (effective samples/s, sweeps/s,
-    median tau, mean fully bound domains per scaffold size)."""
-    from oracle_lib import run_batch_sampled
-    from latticednaorigami_gb300.analysis import effective_samples
+def cpu_temperatures(i):
+    """Temperatures of the CPU sample of scaffold size SIZES[i]: the GPU
+    run's temperatures of that size, stratified (every per/128-th of them in
+    ascending order), so that the sample spans the same range."""
     temps = replica_temps()
     per = N_REP // len(SIZES)
-    ess_total, t_total, sweeps_total = 0.0, 0.0, 0.0
-    taus = []
+    t = np.sort(temps[i * per:(i + 1) * per])
+    return t[np.linspace(0, per - 1, CPU_REPS_PER_SIZE).round().astype(int)]
+
+
+def cpu_effective_rate(files, cores, burn_sweeps, rec_sweeps):
+    """The oracle port on all usable host cores over a bounded sample of the
+    same workload: CPU_REPS_PER_SIZE replicas of each scaffold size at
+    stratified GPU-run temperatures, burn_sweeps of burn-in from the empty
+    scaffold, then the recorded sweeps, tau_int estimated from its own
+    samples by the same estimator.  Only the recorded sweeps are timed (pro
+    rata).  Returns a dict: effective samples/s with its 95 % bootstrap
+    interval, sweeps/s, median tau, mean fully bound domains per size."""
+    from oracle_lib import run_batch_sampled
+    from latticednaorigami_gb300.analysis import replica_ess, bootstrap_sum, tau_int
+    t_total, sweeps_total = 0.0, 0.0
+    ess, groups, taus = [], [], []
     means = {}
     for i, f in enumerate(files):
         n = SIZES[i]
-        tt = temps[i * per:i * per + CPU_REPS_PER_SIZE]
-        t, smp = run_batch_sampled(f, 0, CPU_REPS_PER_SIZE, burn_sweeps + rec_sweeps, n, cores, temps=tt)
+        t, smp = run_batch_sampled(f, 0, CPU_REPS_PER_SIZE, burn_sweeps + rec_sweeps, n, cores,
+                                   temps=cpu_temperatures(i))
         rec = smp[:, burn_sweeps:]
         means[n] = float(rec.mean())
-        ess, tau = effective_samples(list(rec))
-        frac = rec_sweeps / float(burn_sweeps + rec_sweeps)
-        ess_total += ess
-        t_total += t * frac
+        series = list(rec)
+        ess.append(replica_ess(series))
+        groups += [i] * len(series)
+        taus += [x for x in (tau_int(s_) for s_ in series) if x is not None]
+        t_total += t * rec_sweeps / float(burn_sweeps + rec_sweeps)
         sweeps_total += CPU_REPS_PER_SIZE * rec_sweeps
-        if tau is not None:
-            taus.append(tau)
-    return ess_total / t_total, sweeps_total / t_total, (float(np.median(taus)) if taus else None), means
+    ess = np.concatenate(ess)
+    (lo, hi), _ = bootstrap_sum(ess, groups)
+    return {"value": float(ess.sum()) / t_total, "ci95": [lo / t_total, hi / t_total],
+            "sweeps_per_s": sweeps_total / t_total, "tau_int_median": float(np.median(taus)) if taus else None,
+            "mean_fully_bound_by_size": means}
 
 
 def cpu_baseline(files, burn_sweeps, rec_sweeps):
-    cores = os.cpu_count() or 1
-    rate, sweeps_per_s, tau, means = cpu_effective_rate(files, cores, burn_sweeps, rec_sweeps)
-    return {"value": rate, "unit": "effective samples/s", "cores": cores, "kind": "port",
-            "sample": "%d replicas of each scaffold size (GPU-run temperatures) x %d recorded sweeps after %d "
-                      "burn-in sweeps from the empty scaffold, %d threads"
-                      % (CPU_REPS_PER_SIZE, rec_sweeps, burn_sweeps, cores),
-            "sweeps_per_s": sweeps_per_s, "tau_int_median": tau, "mean_fully_bound_by_size": means}
+    cores, present = host_cores()
+    r = cpu_effective_rate(files, cores, burn_sweeps, rec_sweeps)
+    out = {"value": r["value"], "unit": "effective samples/s", "cores": cores, "cores_present_on_host": present,
+           "kind": "port",
+           "sample": "%d replicas of each scaffold size (GPU-run temperatures, stratified) x %d recorded sweeps "
+                     "after %d burn-in sweeps from the empty scaffold, %d threads"
+                     % (CPU_REPS_PER_SIZE, rec_sweeps, burn_sweeps, cores)}
+    out.update({k: v for k, v in r.items() if k != "value"})
+    if present > cores:
+        # the port's threads are independent replicas: linear in cores
+        out["value_all_host_cores_linear"] = r["value"] * present / cores
+    return out
 
 
 def run_reference_arm(args):
     """Reference arm: the CPU restatement of the reference (oracle port; the
-    reference itself cannot be built on the GPU machine) on all host cores."""
+    reference itself cannot be built on the GPU machine) on all usable host cores."""
     tmp = tempfile.mkdtemp()
     files = write_c2(tmp)
-    cores = os.cpu_count() or 1
+    cores, present = host_cores()
     from oracle_lib import run_batch
     for _ in range(args.warmup):
         run_batch(files[0], 0, cores, 20 * SIZES[0], cores)
     burn, rec = CPU_BURN_SWEEPS, args.steps * SWEEPS_PER_STEP
-    rates, sps, taus, times = [], [], [], []
+    res, times = [], []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        r, s_, tau, _ = cpu_effective_rate(files, cores, burn, rec)
+        res.append(cpu_effective_rate(files, cores, burn, rec))
         times.append(time.perf_counter() - t0)
-        rates.append(r)
-        sps.append(s_)
-        taus.append(tau)
-    value = float(np.mean(rates))
+    value = float(np.mean([r["value"] for r in res]))
     line = {"impl": "reference", "metric": "effective samples/s (tau_int of #bound domains), learned vs plain MC",
             "value": value, "unit": "effective samples/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(times)), "higher_is_better": True,
@@ -267,13 +336,16 @@ def run_reference_arm(args):
             "config": {"workload": "c2: constant-T chains, scaffolds 8/12/16/24, uniform hyb, T~U[320,350] K; "
                                    "bounded CPU sample per step; plain moveset (the reference has no learned "
                                    "proposal)"},
-            "cpu_baseline": {"value": value, "unit": "effective samples/s", "cores": cores, "kind": "port",
-                             "sample": "%d replicas of each scaffold size (GPU-run temperatures) x %d recorded "
-                                       "sweeps after %d burn-in sweeps from the empty scaffold, per step"
+            "cpu_baseline": {"value": value, "unit": "effective samples/s", "cores": cores,
+                             "cores_present_on_host": present, "kind": "port",
+                             "sample": "%d replicas of each scaffold size (GPU-run temperatures, stratified) x %d "
+                                       "recorded sweeps after %d burn-in sweeps from the empty scaffold, per step"
                                        % (CPU_REPS_PER_SIZE, rec, burn)},
             "e2e": {"value": value, "unit": "effective samples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "sweeps_per_s": float(np.mean(sps)), "tau_int_median": taus[-1]}
+            "ci95_last_step": res[-1]["ci95"],
+            "sweeps_per_s": float(np.mean([r["sweeps_per_s"] for r in res])),
+            "tau_int_median": res[-1]["tau_int_median"]}
     print(json.dumps(line))
 
 
@@ -436,7 +508,8 @@ def main():
         return
     ranks = Ranks()
     from latticednaorigami_gb300 import Engine
-    from latticednaorigami_gb300.analysis import effective_samples, tau_int
+    from latticednaorigami_gb300.analysis import (bootstrap_sum, effective_samples, replica_ess, tau_int,
+                                                  tau_vs_length)
 
     tmp = tempfile.mkdtemp()
     files = write_c2(tmp)
@@ -447,16 +520,23 @@ def main():
     ns_of = np.array(SIZES)[sys_of]
     total_sweeps = args.steps * SWEEPS_PER_STEP
 
+    overhead = {"collect_s": 0.0, "train_s": 0.0}
+
     def collect_and_train(eng):
         """Network inputs and labels from 10 states 10 sweeps apart, then
-        LEARN_ITERS Adam steps (untimed)."""
+        LEARN_ITERS Adam steps (untimed; their wall time is the learned
+        proposal's own overhead, amortised in value_amortised)."""
+        t0 = time.perf_counter()
         for _ in range(10):
             eng.run_sweeps(10)
             eng.learn_collect()
+        overhead["collect_s"] += time.perf_counter() - t0
         t0 = time.perf_counter()
         loss0, loss1 = eng.learn_train(LEARN_ITERS, lr=LEARN_LR, seed=0)
-        return {"loss_first": loss0, "loss_last": loss1, "iters": LEARN_ITERS,
-                "train_s": time.perf_counter() - t0, "table": eng.learn_table()}
+        dt = time.perf_counter() - t0
+        overhead["train_s"] += dt
+        return {"loss_first": loss0, "loss_last": loss1, "iters": LEARN_ITERS, "train_s": dt,
+                "table": eng.learn_table()}
 
     def relax():
         """Stationary starting configurations: a first network trained on a
@@ -465,15 +545,15 @@ def main():
         e0 = Engine(files, n_replicas=N_REP, seed=500 + ranks.rank, sys_of_replica=sys_of.tolist())
         e0.set_controls(temps=temps)
         for _ in range(3):
-            e0.run_sweeps(SWEEPS_PER_STEP)
+            e0.run_sweeps(100)
         table0 = collect_and_train(e0)["table"]
         e0.close()
         e1 = Engine(files, n_replicas=N_REP, seed=600 + ranks.rank, sys_of_replica=sys_of.tolist(),
                     overrides=learned_over)
         e1.set_controls(temps=temps)
         e1.learn_set_table(table0)
-        for _ in range(RELAX_SWEEPS // SWEEPS_PER_STEP):
-            e1.run_sweeps(SWEEPS_PER_STEP)
+        for _ in range(RELAX_SWEEPS // 100):
+            e1.run_sweeps(100)
         train = collect_and_train(e1)
         start = [e1.config(r) for r in range(N_REP)]
         e1.close()
@@ -490,6 +570,11 @@ def main():
         if table is not None:
             eng.learn_set_table(table)
         eng.set_configs(start)
+        # the engine's autotuner picks the launch shape on this batch (state
+        # restored after every probe: the trajectories are unchanged)
+        tune = eng.autotune(probe_sweeps=4)
+        tune = {k: v for k, v in tune.items() if k != "candidates"}
+        tune["gain_over_default"] = tune["default_ms"] / tune["best_ms"] if tune["best_ms"] > 0 else None
         eng.set_sampling(1, total_sweeps)
         for _ in range(args.warmup):
             eng.run_sweeps(SWEEPS_PER_STEP)
@@ -503,18 +588,23 @@ def main():
         t_dev = ranks.max(sum(dev_ms) / 1000.0)
         smp, cnt = eng.samples()
         series = [smp[r, :cnt[r], 0] for r in range(N_REP)]
-        ess, tau_med = effective_samples(series)
-        ess = ranks.sum(ess)
+        per_rep = replica_ess(series)
+        ess = ranks.sum(float(per_rep.sum()))
+        (lo, hi), boot = bootstrap_sum(per_rep, sys_of)
         taus, means = {}, {}
         for i, n in enumerate(SIZES):
             ts = [tau_int(series[r]) for r in range(i * per, (i + 1) * per)]
             ts = [t for t in ts if t is not None]
             taus[n] = float(np.median(ts)) if ts else None
             means[n] = float(np.mean(np.concatenate(series[i * per:(i + 1) * per])))
+        big = [series[r] for r in range(3 * per, 4 * per)]
+        tvl = tau_vs_length(big, [L for L in (500, 1000, 2000, 5000, 10000) if L <= total_sweeps])
+        tau_med = float(np.median([t for t in (tau_int(x) for x in series) if t is not None]))
         st = eng.move_stats(3)
         acc = [float(st[k, 1]) / max(1.0, float(st[k, 0])) for k in range(3)]
-        return {"eng": eng, "dev_ms": dev_ms, "t_dev": t_dev, "ess": ess, "tau_med": tau_med, "taus": taus,
-                "means": means, "clk": clk, "acc": acc}
+        return {"eng": eng, "dev_ms": dev_ms, "t_dev": t_dev, "ess": ess, "boot": boot / t_dev,
+                "ci95": [lo / t_dev, hi / t_dev], "tau_med": tau_med, "taus": taus, "tau_vs_length_24": tvl,
+                "means": means, "clk": clk, "acc": acc, "tune": tune}
 
     def e2e_arm(overrides, table):
         """The same loop through the C ABI with host buffers: temperatures in,
@@ -525,6 +615,7 @@ def main():
         if table is not None:
             eng2.learn_set_table(table)
         eng2.set_configs(start)
+        eng2.autotune(probe_sweeps=4)   # the shape found for the timed arm (cached)
         eng2.set_sampling(1, SWEEPS_PER_STEP)
         for _ in range(args.warmup):
             eng2.run_sweeps(SWEEPS_PER_STEP)
@@ -542,6 +633,7 @@ def main():
         ranks.barrier()
         t_e2e = ranks.max(t_e2e)
         e2e_ess, _ = effective_samples([np.concatenate(x) for x in e2e_series])
+        eng2.close()
         return ranks.sum(e2e_ess) / t_e2e
 
     table = train["table"]
@@ -549,37 +641,64 @@ def main():
     learned = timed_arm(learned_over, table)
     value = learned["ess"] / learned["t_dev"]
     plain_value = plain["ess"] / plain["t_dev"]
+    ratio_boot = learned["boot"] / plain["boot"]
     e2e_learned = e2e_arm(learned_over, table)
     e2e_plain = e2e_arm("", None)
     h2d = N_REP * 8
     d2h = N_REP * SWEEPS_PER_STEP * 2 * 2
 
-    # roofline of the MC kernel: algorithmic DRAM bytes = state in + out + samples
-    eng = learned["eng"]
-    dev_ms = learned["dev_ms"]
-    lay_bytes = eng.state_bytes()
-    alg_bytes = N_REP * lay_bytes * 2 + N_REP * SWEEPS_PER_STEP * 4
-    achieved = alg_bytes / (np.mean(dev_ms) / 1000.0) / 1e9
-    peak, peak_kind = measured_peaks()
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "c2_traffic.json")
-    if os.path.exists(tp):
-        with open(tp) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+    # Roofline of the MC kernel: shared memory (the replica state stays in it
+    # for a whole launch).  achieved = move attempts per launch x algorithmic
+    # bytes per attempt / launch time; peak = 152 SMs x 128 B/clk x the
+    # median SM clock sampled during the timed launches.  HBM as a second
+    # figure: state in + out + samples per launch against the measured copy
+    # bandwidth.
+    attempts_per_launch = float(np.sum(ns_of)) * SWEEPS_PER_STEP
 
-    def rates(arm):
+    def roofline(arm, kind):
+        t_launch = float(np.mean(arm["dev_ms"])) / 1000.0
+        sm_mhz = arm["clk"].get("sm_mhz") or 2070.0
+        peak = N_SM * SMEM_BYTES_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e9
+        achieved = attempts_per_launch * B_ATTEMPT[kind] / t_launch / 1e9
+        eng_ = arm["eng"]
+        alg_hbm = N_REP * eng_.state_bytes() * 2 + N_REP * SWEEPS_PER_STEP * 4
+        hbm_peak, hbm_kind = measured_peaks()
+        hbm_ach = alg_hbm / t_launch / 1e9
+        return {"bound": "smem", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_kind": "derived: 152 SMs x 128 B/clk x median SM clock %.0f MHz" % sm_mhz,
+                "bytes_per_attempt": B_ATTEMPT[kind], "attempts_per_launch": attempts_per_launch,
+                "hbm": {"achieved": hbm_ach, "peak": hbm_peak, "frac": hbm_ach / hbm_peak, "peak_kind": hbm_kind,
+                        "algorithmic_bytes_per_launch": alg_hbm}}
+
+    rl = roofline(learned, "learned")
+    tr_d, tr_src = measured_traffic("c2")
+    rl["traffic"] = None
+    rl["traffic_source"] = tr_src
+    if tr_d:
+        # per launch of SWEEPS_PER_STEP sweeps, scaled from the captured launch
+        rl["traffic"] = tr_d["dram_bytes_per_launch"] * SWEEPS_PER_STEP / tr_d["sweeps_per_launch"]
+    overhead_s = overhead["collect_s"] + overhead["train_s"]
+
+    def rates(arm, kind):
         t = arm["t_dev"]
         W = ranks.world
-        return {"value": arm["ess"] / t, "sweeps_per_s": W * N_REP * total_sweeps / t,
+        return {"value": arm["ess"] / t, "ci95": arm["ci95"], "sweeps_per_s": W * N_REP * total_sweeps / t,
                 "move_attempts_per_s": W * float(np.sum(ns_of)) * total_sweeps / t,
                 "ms_per_step": float(np.mean(arm["dev_ms"])), "tau_int_median": arm["tau_med"],
-                "tau_int_by_size": arm["taus"], "mean_fully_bound_by_size": arm["means"],
-                "acceptance": {"exchange": arm["acc"][0], "regrowth": arm["acc"][1], "cb_regrowth": arm["acc"][2]}}
+                "tau_int_by_size": arm["taus"], "tau_vs_record_length_24_domain": arm["tau_vs_length_24"],
+                "mean_fully_bound_by_size": arm["means"],
+                "acceptance": {"exchange": arm["acc"][0], "regrowth": arm["acc"][1], "cb_regrowth": arm["acc"][2]},
+                "roofline_smem_frac": roofline(arm, kind)["frac"], "autotune": arm["tune"]}
 
     tr = train
+    lrates = rates(learned, "learned")
+    lrates["value_amortised"] = learned["ess"] / (learned["t_dev"] + overhead_s)
+    lrates["learned_overhead_s"] = {"collect_s": overhead["collect_s"], "train_s": overhead["train_s"],
+                                    "note": "two collections of 10 states and two trainings; value_amortised "
+                                            "adds them to the timed region of this run"}
     line = {"metric": "effective samples/s (tau_int of #bound domains), learned vs plain MC", "value": value,
             "unit": "effective samples/s", "n_gpus": ranks.world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": float(np.mean(dev_ms)), "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": float(np.mean(learned["dev_ms"])), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "c2: 4096 constant-T chains, scaffolds 8/12/16/24 (1024 each), uniform hyb "
                                    "dH=-120 kcal/mol dS=-0.33 kcal/mol/K, T~U[320,350] K, 1 uM; moveset "
@@ -590,18 +709,20 @@ def main():
                        "start": "both arms from the same configurations, relaxed %d sweeps by the learned "
                                 "moveset, then %d warm-up sweeps" % (RELAX_SWEEPS, args.warmup * SWEEPS_PER_STEP),
                        "l2": "state resident in shared memory; no L2 flush needed"},
-            "learned": rates(learned), "plain": rates(plain),
+            "ci95": learned["ci95"],
+            "learned": lrates, "plain": rates(plain, "plain"),
             "learned_over_plain": value / plain_value,
+            "learned_over_plain_ci95": [float(np.quantile(ratio_boot, 0.025)), float(np.quantile(ratio_boot, 0.975))],
+            "ci_method": "percentile bootstrap over replicas (resampled within scaffold size), 2000 resamples",
             "distribution_check": "tests/test_gpu_learned.py::test_learned_distribution_matches_plain_on_c2",
             "network": {"layers": "64-256-256-256-1 GELU, bf16 weights/activations, fp32 accumulation",
                         "train_iters": tr["iters"], "loss_first": tr["loss_first"], "loss_last": tr["loss_last"],
                         "train_s": tr["train_s"]},
-            "sweeps_per_s": rates(learned)["sweeps_per_s"],
+            "sweeps_per_s": lrates["sweeps_per_s"],
             "e2e": {"value": e2e_learned, "unit": "effective samples/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "plain_value": e2e_plain},
             "gpu_launches": 2 * args.steps,   # per step: the MC kernel and the status fold
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind},
+            "roofline": rl,
             "clocks": learned["clk"], "clocks_plain": plain["clk"]}
     if not args.no_cpu and rank == 0:
         line["cpu_baseline"] = cpu_baseline(files, CPU_BURN_SWEEPS, total_sweeps)

@@ -237,6 +237,31 @@ ldo_status ldo_us_get_biases(ldo_engine* e, double* out, int n_windows, int grid
 /* Window held by each replica, and the grid length. */
 ldo_status ldo_us_get_windows(ldo_engine* e, int32_t* window_of_replica, int n, int* grid_len);
 
+/* No counterpart in the reference: the engine's autotuner of the MC kernel's
+ * launch shape (the reference runs one replica per MPI process and has no
+ * launch shape).  Times probe_sweeps sweeps of this engine's own batch for
+ * every candidate -- 1, 2 or 4 replicas (warps) per block, each number of
+ * resident blocks per SM the occupancy calculator allows (set through extra
+ * shared memory per block), replicas in the given order or interleaved over
+ * the systems -- best of two probes each, restores the replicas' state after
+ * every probe (tuning changes no trajectory), and keeps the fastest shape for
+ * the following runs.  With use_cache, a shape found before in this process
+ * for the same capacity class, systems and replica count is reused without
+ * probing. */
+typedef struct {
+    int32_t warps_per_block;
+    int32_t smem_pad_bytes;
+    int32_t blocks_per_sm;      /* resident blocks per SM of the chosen shape */
+    int32_t interleaved;        /* 1: replicas interleaved over the systems */
+    double best_ms;             /* probe time of the chosen shape */
+    double default_ms;          /* probe time of the shape before tuning */
+    int32_t n_candidates;
+} ldo_tune_report;
+ldo_status ldo_autotune(ldo_engine* e, int32_t probe_sweeps, int32_t use_cache, ldo_tune_report* out);
+/* The candidates of the last probing autotune: shape[4k..4k+3] = warps per
+ * block, padding bytes, blocks per SM, interleaved; ms[k] its probe time. */
+ldo_status ldo_autotune_candidates(ldo_engine* e, int32_t* shape, double* ms, int32_t cap);
+
 /* No counterpart in the reference.  Status of every replica without
  * allocating: for a caller that may not allocate device memory at this point
  * (its own pool allocator owns all device memory, or its step loop must not

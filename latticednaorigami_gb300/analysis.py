@@ -43,3 +43,39 @@ def effective_samples(series):
         taus.append(t)
         total += len(s) / (2.0 * t)
     return total, (float(np.median(taus)) if taus else None)
+
+
+def replica_ess(series):
+    """Effective samples of each replica's series, n / (2 tau) (one for a
+    series that never changed)."""
+    out = np.empty(len(series))
+    for i, s in enumerate(series):
+        t = tau_int(s)
+        out[i] = 1.0 if t is None else len(s) / (2.0 * t)
+    return out
+
+
+def bootstrap_sum(per_replica, groups=None, n_boot=2000, seed=0, level=0.95):
+    """Percentile bootstrap of a sum over independent replicas: replicas are
+    resampled with replacement, within each group (e.g. scaffold size) if
+    groups is given.  Returns (lo, hi) and the bootstrap sums."""
+    x = np.asarray(per_replica, dtype=np.float64)
+    rng = np.random.default_rng(seed)
+    g = np.zeros(len(x), int) if groups is None else np.asarray(groups)
+    sums = np.zeros(n_boot)
+    for key in np.unique(g):
+        idx = np.flatnonzero(g == key)
+        pick = rng.integers(0, len(idx), size=(n_boot, len(idx)))
+        sums += x[idx][pick].sum(axis=1)
+    a = (1.0 - level) / 2.0
+    return (float(np.quantile(sums, a)), float(np.quantile(sums, 1.0 - a))), sums
+
+
+def tau_vs_length(series, lengths):
+    """Median tau_int over replicas of the first L samples, for each L."""
+    out = {}
+    for L in lengths:
+        ts = [tau_int(s[:L]) for s in series if len(s) >= L]
+        ts = [t for t in ts if t is not None]
+        out[int(L)] = float(np.median(ts)) if ts else None
+    return out

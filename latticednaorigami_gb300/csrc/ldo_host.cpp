@@ -423,6 +423,8 @@ struct ldo_engine {
     LdoMlp mlp;
     bool mlp_init {false};
     DevBuf<int> d_status;
+    DevBuf<int> d_rep_map;          // autotuner's replica order (warp -> replica)
+    bool use_rep_map {false};
     DevBuf<int16_t> d_samples;
     DevBuf<double> d_trace;
     int sample_interval {0}, sample_cap {0};
@@ -550,7 +552,153 @@ struct ldo_engine {
         L.learn_w = d_learn_w.p;
         L.learn_cnt_b = d_cnt_b.p;
         L.learn_cnt_t = d_cnt_t.p;
+        L.rep_map = use_rep_map ? d_rep_map.p : nullptr;
         return L;
+    }
+
+    // ------------------------------------------------------- autotuner ---
+    // The engine's own autotuner of the MC kernel's launch shape (no
+    // counterpart in the reference).  Knobs: warps (replicas) per block, the
+    // number of resident blocks per SM (set through extra dynamic shared
+    // memory per block), and the replica order (as given, or interleaved over
+    // the systems so that every block and SM holds a mix of sizes).  Every
+    // candidate is timed on probe_sweeps sweeps of the engine's own batch,
+    // best of two, and the replicas' state is restored after every probe, so
+    // tuning leaves the trajectories exactly those of an untuned engine.  The
+    // choice is kept per (capacity class, kernel variant, systems, replica
+    // count) for the life of the process.
+    struct TuneCand {
+        int wpb, pad, blocks, order;
+        double ms;
+    };
+    vector<TuneCand> tune_log;
+    TuneCand tune_default {};
+    static std::map<string, TuneCand>& tune_cache() {
+        static std::map<string, TuneCand> c;
+        return c;
+    }
+
+    vector<int> interleaved_order() const {
+        std::map<int, vector<int>> by_sys;
+        for (int r = 0; r < n_rep; ++r) by_sys[sys_of[r]].push_back(r);
+        vector<int> order;
+        for (size_t k = 0; order.size() < (size_t)n_rep; ++k)
+            for (auto& kv : by_sys)
+                if (k < kv.second.size()) order.push_back(kv.second[k]);
+        return order;
+    }
+
+    double probe(int sweeps) {
+        LdoLaunch L = launch_params(LDO_MODE_RUN, sweeps);
+        L.sweep_units = 1;
+        L.sample_interval = 0;
+        L.n_trace = 0;
+        CU(cudaEventRecord(ev0, stream));
+        CU(ldo_launch_mc(L, stream));
+        CU(cudaEventRecord(ev1, stream));
+        CU(cudaStreamSynchronize(stream));
+        float f = 0;
+        CU(cudaEventElapsedTime(&f, ev0, ev1));
+        return f;
+    }
+
+    TuneCand autotune(int probe_sweeps, bool use_cache) {
+        int wb = ldo_warp_smem_bytes(lay.cls);
+        int ct = d_ct.p ? 1 : 0;
+        std::ostringstream key;
+        key << lay.cls << "/" << ct << "/" << systems_hash() << "/" << n_rep;
+        tune_default = TuneCand {wpb, smem_pad, 0, use_rep_map ? 1 : 0, 0.0};
+        if (use_cache) {
+            auto it = tune_cache().find(key.str());
+            if (it != tune_cache().end()) {
+                apply_tune(it->second);
+                return it->second;
+            }
+        }
+        // candidates: (warps per block, resident blocks per SM) pairs that the
+        // occupancy calculator confirms, each with the smallest padding
+        vector<TuneCand> cands;
+        const size_t kMaxSmem = 227 * 1024;
+        for (int w : {1, 2, 4}) {
+            size_t base = (size_t)w * wb;
+            if (base > kMaxSmem) continue;
+            int full = 0;
+            CU(ldo_mc_occupancy(lay.cls, ct, w, base, &full));
+            for (int want = full; want >= 1; --want) {
+                if (w * want > 32 || (w * want) % 4 != 0) continue;
+                size_t lo = 0, hi = kMaxSmem - base;
+                int occ = 0;
+                CU(ldo_mc_occupancy(lay.cls, ct, w, base + hi, &occ));
+                if (occ > want) continue;
+                while (lo < hi) {   // smallest padding with at most `want` blocks per SM
+                    size_t mid = (lo + hi) / 2;
+                    CU(ldo_mc_occupancy(lay.cls, ct, w, base + mid, &occ));
+                    if (occ <= want) hi = mid;
+                    else lo = mid + 1;
+                }
+                CU(ldo_mc_occupancy(lay.cls, ct, w, base + lo, &occ));
+                if (occ == want) cands.push_back(TuneCand {w, (int)lo, want, 0, 0.0});
+            }
+        }
+        bool multi = false;
+        for (int r = 1; r < n_rep; ++r) multi = multi || sys_of[r] != sys_of[0];
+        if (multi) {
+            size_t n = cands.size();
+            for (size_t i = 0; i < n; ++i) {
+                TuneCand c = cands[i];
+                c.order = 1;
+                cands.push_back(c);
+            }
+        }
+        vector<int> order = interleaved_order();
+        d_rep_map.alloc(n_rep);
+        CU(copy(d_rep_map.p, order.data(), n_rep * sizeof(int), cudaMemcpyHostToDevice));
+        DevBuf<unsigned char> saved;
+        saved.alloc(d_arena.n);
+        CU(cudaMemcpyAsync(saved.p, d_arena.p, d_arena.n, cudaMemcpyDeviceToDevice, stream));
+        auto restore = [&]() {
+            CU(cudaMemcpyAsync(d_arena.p, saved.p, d_arena.n, cudaMemcpyDeviceToDevice, stream));
+            CU(cudaStreamSynchronize(stream));
+        };
+        TuneCand keep = tune_default;
+        // the default shape, timed the same way
+        apply_tune(keep);
+        probe(probe_sweeps);
+        restore();
+        tune_default.ms = probe(probe_sweeps);
+        restore();
+        tune_default.ms = std::min(tune_default.ms, probe(probe_sweeps));
+        restore();
+        tune_log.clear();
+        TuneCand best = tune_default;
+        for (auto& c : cands) {
+            apply_tune(c);
+            double t = probe(probe_sweeps);
+            restore();
+            t = std::min(t, probe(probe_sweeps));
+            restore();
+            c.ms = t;
+            tune_log.push_back(c);
+            if (c.ms < best.ms) best = c;
+        }
+        check_status();
+        apply_tune(best);
+        tune_cache()[key.str()] = best;
+        return best;
+    }
+
+    void apply_tune(const TuneCand& c) {
+        wpb = c.wpb;
+        smem_pad = c.pad;
+        use_rep_map = c.order == 1 && d_rep_map.p;
+        if (c.order == 1 && !d_rep_map.p) {
+            vector<int> order = interleaved_order();
+            d_rep_map.alloc(n_rep);
+            CU(copy(d_rep_map.p, order.data(), n_rep * sizeof(int), cudaMemcpyHostToDevice));
+            use_rep_map = true;
+        }
+        // a captured PT cycle graph holds the launch shape: pt_run compares
+        // the launch parameters and captures again
     }
 
     void check_status() {
@@ -1779,6 +1927,33 @@ ldo_status ldo_run_sweeps(ldo_engine* e, int64_t n_sweeps, double* device_ms) {
 
 int ldo_state_bytes(const ldo_engine* e) { return e ? e->lay.bytes : 0; }
 
+ldo_status ldo_autotune(ldo_engine* e, int32_t probe_sweeps, int32_t use_cache, ldo_tune_report* out) {
+    if (!e || probe_sweeps < 1 || !out) return LDO_EINVAL;
+    return guard(e, [&]() {
+        auto best = e->autotune(probe_sweeps, use_cache != 0);
+        out->warps_per_block = best.wpb;
+        out->smem_pad_bytes = best.pad;
+        out->blocks_per_sm = best.blocks;
+        out->interleaved = best.order;
+        out->best_ms = best.ms;
+        out->default_ms = e->tune_default.ms;
+        out->n_candidates = (int32_t)e->tune_log.size();
+    });
+}
+
+ldo_status ldo_autotune_candidates(ldo_engine* e, int32_t* shape, double* ms, int32_t cap) {
+    if (!e || !shape || !ms || cap < (int32_t)e->tune_log.size()) return LDO_EINVAL;
+    for (size_t k = 0; k < e->tune_log.size(); ++k) {
+        const auto& c = e->tune_log[k];
+        shape[4 * k] = c.wpb;
+        shape[4 * k + 1] = c.pad;
+        shape[4 * k + 2] = c.blocks;
+        shape[4 * k + 3] = c.order;
+        ms[k] = c.ms;
+    }
+    return LDO_OK;
+}
+
 ldo_status ldo_set_controls(ldo_engine* e, const double* temps, const double* stacking_mults,
                             const double* staple_u_mults, int n) {
     if (!e || n != e->n_rep) return LDO_EINVAL;
@@ -2087,8 +2262,8 @@ ldo_status ldo_us_get_windows(ldo_engine* e, int32_t* window_of_replica, int n, 
 // Status read-out for callers that may not allocate device memory (a program
 // whose pool allocator owns all device memory, a step loop that must not stall
 // the device on cudaMalloc/cudaFree).  The scratch is a fixed device array of
-// the library, found on the first call on a device; nothing is allocated on
-// the success path, on the device or the host.
+// the library, whose device address is looked up on every call; nothing is
+// allocated on the success path, on the device or the host.
 ldo_status ldo_replica_status_noalloc(ldo_engine* e, int32_t* status_of_replica, int n, int32_t* worst,
                                       int32_t* n_bad) {
     if (!e || !worst || !n_bad) return LDO_EINVAL;

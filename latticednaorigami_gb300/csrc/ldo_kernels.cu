@@ -99,8 +99,10 @@ __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
     extern __shared__ __align__(16) unsigned char smem[];
     int warp = threadIdx.x >> 5;
     int lane = threadIdx.x & 31;
-    int rep = blockIdx.x * L.warps_per_block + warp;
-    if (rep >= L.n_rep || (L.only_rep >= 0 && rep != L.only_rep)) return;
+    int slot = blockIdx.x * L.warps_per_block + warp;
+    if (slot >= L.n_rep) return;
+    int rep = L.rep_map ? L.rep_map[slot] : slot;
+    if (L.only_rep >= 0 && rep != L.only_rep) return;
     unsigned char* base = smem + (size_t)warp * warp_bytes<C>();
     ldo::Rep<C>* R = reinterpret_cast<ldo::Rep<C>*>(base);
     unsigned char* gbase = L.arena + (size_t)rep * sizeof(LdoState<C>);
@@ -318,6 +320,25 @@ cudaError_t ldo_launch_mc(const LdoLaunch& L, cudaStream_t stream) {
     case LDO_CLASS_S: return launch_mc_class<LdoCapS>(L, stream);
     case LDO_CLASS_M: return launch_mc_class<LdoCapM>(L, stream);
     default: return launch_mc_class<LdoCapL>(L, stream);
+    }
+}
+
+template <class C, bool CT>
+static cudaError_t occupancy_variant(int wpb, size_t smem, int* blocks) {
+    cudaError_t err =
+        cudaFuncSetAttribute(ldo_mc_kernel<C, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, ldo_mc_kernel<C, CT>, wpb * 32, smem);
+}
+
+cudaError_t ldo_mc_occupancy(int cls, int ct, int wpb, size_t smem, int* blocks) {
+    switch (cls) {
+    case LDO_CLASS_S:
+        return ct ? occupancy_variant<LdoCapS, true>(wpb, smem, blocks) : occupancy_variant<LdoCapS, false>(wpb, smem, blocks);
+    case LDO_CLASS_M:
+        return ct ? occupancy_variant<LdoCapM, true>(wpb, smem, blocks) : occupancy_variant<LdoCapM, false>(wpb, smem, blocks);
+    default:
+        return ct ? occupancy_variant<LdoCapL, true>(wpb, smem, blocks) : occupancy_variant<LdoCapL, false>(wpb, smem, blocks);
     }
 }
 

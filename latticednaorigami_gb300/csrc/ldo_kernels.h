@@ -46,9 +46,16 @@ struct LdoLaunch {
     // when no system regrows its scaffold).
     unsigned char* ct_ws;
     size_t ct_stride;
+    // Warp w of the grid runs replica rep_map[w] (null: replica w).  The
+    // autotuner's replica order: which replicas share a block and an SM.
+    const int* rep_map;
 };
 
 cudaError_t ldo_launch_mc(const LdoLaunch& L, cudaStream_t stream);
+// Resident blocks per SM of the MC kernel of class cls (ct: the scaffold-
+// move variant) with wpb warps per block and smem bytes of dynamic shared
+// memory per block, from the CUDA occupancy calculator.
+cudaError_t ldo_mc_occupancy(int cls, int ct, int wpb, size_t smem, int* blocks);
 enum { LDO_N_SNAPSHOTS = 3 };
 // Bytes between a replica's move snapshots for a state of lay.bytes bytes.
 inline size_t ldo_snapshot_stride(int state_bytes) { return ((size_t)state_bytes + 255) / 256 * 256; }

@@ -24,7 +24,7 @@ EXPORTS = [
     "ldo_learn_get_params", "ldo_learn_get_table", "ldo_learn_set_table", "ldo_learn_loss_grad",
     "ldo_writer_open", "ldo_writer_write", "ldo_writer_close", "ldo_pt2d_run", "ldo_engine_exp",
     "ldo_set_bias_centre", "ldo_swap_writer_open", "ldo_set_config", "ldo_set_configs", "ldo_anneal_run", "ldo_read_trj_frame", "ldo_checkpoint_save",
-    "ldo_checkpoint_load",
+    "ldo_checkpoint_load", "ldo_autotune", "ldo_autotune_candidates",
 ]
 
 LEARN_TABLE = 524544      # network inputs: 524288 insertion + 256 regrowth-direction (ldo_learn.h)
@@ -35,6 +35,12 @@ class LdoError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("%s: %s" % (STATUS.get(code, code), msg))
         self.code = code
+
+
+class TuneReport(ctypes.Structure):
+    _fields_ = [("warps_per_block", ctypes.c_int32), ("smem_pad_bytes", ctypes.c_int32),
+                ("blocks_per_sm", ctypes.c_int32), ("interleaved", ctypes.c_int32), ("best_ms", ctypes.c_double),
+                ("default_ms", ctypes.c_double), ("n_candidates", ctypes.c_int32)]
 
 
 class Observables(ctypes.Structure):
@@ -72,6 +78,8 @@ def load_library(path=None):
     lib.ldo_run.argtypes = [vp, ctypes.c_int64, dp]
     lib.ldo_run_sweeps.argtypes = [vp, ctypes.c_int64, dp]
     lib.ldo_state_bytes.argtypes = [vp]
+    lib.ldo_autotune.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(TuneReport)]
+    lib.ldo_autotune_candidates.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), dp, ctypes.c_int32]
     lib.ldo_get_observables.argtypes = [vp, ctypes.POINTER(Observables), ip]
     lib.ldo_get_config.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int32), ip, ctypes.POINTER(ctypes.c_int)]
     lib.ldo_set_config.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int32), ip]
@@ -172,6 +180,24 @@ class Engine:
 
     def state_bytes(self):
         return self.lib.ldo_state_bytes(self.h)
+
+    def autotune(self, probe_sweeps=4, use_cache=True):
+        """The engine's autotuner (ldo_autotune): the fastest launch shape for
+        this batch, kept for the following runs; returns its report and the
+        candidate table (warps per block, padding, blocks per SM,
+        interleaved, probe ms)."""
+        rep = TuneReport()
+        self._check(self.lib.ldo_autotune(self.h, int(probe_sweeps), 1 if use_cache else 0, ctypes.byref(rep)))
+        out = {f[0]: getattr(rep, f[0]) for f in TuneReport._fields_}
+        n = rep.n_candidates
+        cands = []
+        if n > 0:
+            shape = (ctypes.c_int32 * (4 * n))()
+            ms = (ctypes.c_double * n)()
+            self._check(self.lib.ldo_autotune_candidates(self.h, shape, ms, n))
+            cands = [[shape[4 * k], shape[4 * k + 1], shape[4 * k + 2], shape[4 * k + 3], ms[k]] for k in range(n)]
+        out["candidates"] = cands
+        return out
 
     def set_controls(self, temps=None, stacking_mults=None, staple_u_mults=None):
         def arr(x):

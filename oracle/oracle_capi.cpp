@@ -280,6 +280,27 @@ void oracle_engine_exp(const double* x, double* y, int n) {
 }
 
 // Per-move attempts/accepts, 2 x n_moves.
+// Per movetype: attempts, domain-record accesses, occupancy-map operations
+// (the ORACLE_COUNT_TOUCHES build; -1 in the normal one).
+int oracle_touch_counts(void* h, long long* out, int cap) {
+#ifdef ORACLE_COUNT_TOUCHES
+    auto& sy = static_cast<Replica*>(h)->sys;
+    int n = (int)sy.attempts.size();
+    if (cap < 3 * n) return -1;
+    for (int m = 0; m < n; ++m) {
+        out[3 * m] = sy.attempts[m];
+        out[3 * m + 1] = sy.touch_dom[m];
+        out[3 * m + 2] = sy.touch_site[m];
+    }
+    return n;
+#else
+    (void)h;
+    (void)out;
+    (void)cap;
+    return -1;
+#endif
+}
+
 int oracle_move_stats(void* h, long long* out, int cap) {
     System& s = static_cast<Replica*>(h)->sys;
     int n = (int)s.attempts.size();

@@ -107,6 +107,62 @@ struct SiteRec {
     int unbound_dom;   // valid when occ == UNBOUND
 };
 
+// State touches of the reference's algorithm, counted only in the build with
+// ORACLE_COUNT_TOUCHES (liboracle_touch.so): every access to a domain record
+// and every operation on the occupancy map, per thread.  They give the
+// algorithmic bytes per move attempt of the engine's throughput roofline.
+// In the normal build the containers below are plain std containers.
+#ifdef ORACLE_COUNT_TOUCHES
+struct TouchCounts {
+    long long dom {0}, site {0};
+};
+inline thread_local TouchCounts g_touch;
+#define ORACLE_TOUCH(field) (++g_touch.field)
+#else
+#define ORACLE_TOUCH(field) ((void)0)
+#endif
+
+template <class T>
+struct DomVec : std::vector<T> {
+    using std::vector<T>::vector;
+    T& operator[](size_t i) {
+        ORACLE_TOUCH(dom);
+        return std::vector<T>::operator[](i);
+    }
+    const T& operator[](size_t i) const {
+        ORACLE_TOUCH(dom);
+        return std::vector<T>::operator[](i);
+    }
+};
+
+struct SiteMap : std::unordered_map<uint64_t, SiteRec> {
+    using Base = std::unordered_map<uint64_t, SiteRec>;
+    iterator find(uint64_t k) {
+        ORACLE_TOUCH(site);
+        return Base::find(k);
+    }
+    const_iterator find(uint64_t k) const {
+        ORACLE_TOUCH(site);
+        return Base::find(k);
+    }
+    SiteRec& at(uint64_t k) {
+        ORACLE_TOUCH(site);
+        return Base::at(k);
+    }
+    const SiteRec& at(uint64_t k) const {
+        ORACLE_TOUCH(site);
+        return Base::at(k);
+    }
+    SiteRec& operator[](uint64_t k) {
+        ORACLE_TOUCH(site);
+        return Base::operator[](k);
+    }
+    size_t erase(uint64_t k) {
+        ORACLE_TOUCH(site);
+        return Base::erase(k);
+    }
+};
+
 // ------------------------------------------------------- order params ----
 enum OpKind { OP_NUMSTAPLES, OP_NUMSTAPLESTYPE, OP_STAPLETYPEFULLYBOUND, OP_NUMBOUND, OP_NUMMISBOUND,
               OP_NUMSTACKED, OP_NUMLINEARHELICES, OP_NUMSTACKEDJUNCTS, OP_SUM };
@@ -207,13 +263,13 @@ class System {
     Stream rng;
 
     // Bookkeeping (OrigamiSystem members, include/.../origami_system.hpp:175-205)
-    std::vector<Dom> doms;
+    DomVec<Dom> doms;
     std::vector<int> free_doms;
     std::vector<std::vector<int>> chains;   // domain ids, m_domains order
     std::vector<int> chain_index;           // unique chain index per chain
     std::vector<int> chain_ident;
     std::vector<std::vector<int>> ident_to_index;
-    std::unordered_map<uint64_t, SiteRec> sites;
+    SiteMap sites;
     int num_domains {0}, num_staples {0}, num_bound {0}, num_fully {0}, num_self {0}, num_unassigned {0},
         num_stacked {0};
     int current_c_i {0};
@@ -226,6 +282,8 @@ class System {
 
     // move-loop statistics
     std::vector<long long> attempts, accepts;
+    // state touches per movetype (ORACLE_COUNT_TOUCHES build)
+    std::vector<long long> touch_dom, touch_site;
 
     // ---------------------------------------------------- construction ---
     void init(const Config& c, const EnergyTables& t, const std::vector<ChainInit>& config) {
@@ -234,6 +292,8 @@ class System {
         ident_to_index.assign(cfg.identities.size(), {});
         attempts.assign(cfg.move_kinds.size(), 0);
         accepts.assign(cfg.move_kinds.size(), 0);
+        touch_dom.assign(cfg.move_kinds.size(), 0);
+        touch_site.assign(cfg.move_kinds.size(), 0);
         // initialize_scaffold (src/origami_system.cpp:680)
         add_chain_with_index(config[0].identity, config[0].index);
         num_staples--;
@@ -3034,6 +3094,9 @@ class System {
         for (m = 0; m < cfg.move_cum.size(); ++m)
             if (r < cfg.move_cum[m]) break;
         if (m == cfg.move_cum.size()) throw std::runtime_error("movetype selection fell off the end");
+#ifdef ORACLE_COUNT_TOUCHES
+        TouchCounts t0 = g_touch;
+#endif
         reset_internal();
         bool acc = false;
         switch (cfg.move_kinds[m]) {
@@ -3055,6 +3118,10 @@ class System {
             update_move_params();
             calc_move();
         }
+#ifdef ORACLE_COUNT_TOUCHES
+        touch_dom[m] += g_touch.dom - t0.dom;
+        touch_site[m] += g_touch.site - t0.site;
+#endif
         if (cfg.centering_freq != 0 && s % cfg.centering_freq == 0) center(cfg.centering_domain);
         if (cfg.constraint_check_freq != 0 && s % cfg.constraint_check_freq == 0) check_all_constraints();
         return acc;
