@@ -480,6 +480,226 @@ def run_c4(args, impl):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------- c3 ---
+# The 48-domain parallel-tempering workload (the learned proposal's target
+# system): the 48-domain HalfTurn scaffold with 24 two-domain staple types,
+# nearest-neighbour energies of seeded 16-mers, 1 uM; 64 temperatures
+# geometric over 310-370 K x 32 independent ladders = 2048 replicas, uT
+# exchange (temperature and staple chemical potential, UTPTGCMCSimulation)
+# every 1000 steps.  Both arms start from the same configurations: a plain PT
+# burn-in of C3_BURN_ROUNDS rounds from the empty scaffold, imported by
+# temperature slot.  Samples: the number of fully bound domains every 100
+# steps; effective samples are counted on the per-temperature series (the
+# replica at each slot, followed through the permutations of the .swp rows).
+C3_RUNGS, C3_LADDERS, C3_INTERVAL, C3_SAMPLE = 64, 32, 1000, 100
+C3_TEMPS = [310.0 * (370.0 / 310.0) ** (k / 63.0) for k in range(64)]
+C3_ROUNDS_PER_STEP = 25
+C3_BURN_ROUNDS = 1000
+C3_CPU_REPS = 128
+
+
+def write_c3(d):
+    import systems
+    return systems.write_case(d, "c3", extra=dict(temps=" ".join(repr(t) for t in C3_TEMPS), num_reps=C3_RUNGS,
+                                                    exchange_interval=C3_INTERVAL))
+
+
+def c3_slot_series(smp, rows, rounds):
+    """Per-temperature-slot series: rows[l][k] is ladder l's permutation
+    (slot -> replica within the ladder) during round k; every round holds
+    C3_INTERVAL / C3_SAMPLE samples of each replica."""
+    per = C3_INTERVAL // C3_SAMPLE
+    out = {}
+    for l in range(C3_LADDERS):
+        for q in range(C3_RUNGS):
+            parts = []
+            for k in range(rounds):
+                r = l * C3_RUNGS + rows[l][k][q]
+                parts.append(smp[r, k * per:(k + 1) * per, 0])
+            out[(l, q)] = np.concatenate(parts).astype(np.float64)
+    return out
+
+
+def read_swp_rows(path, rounds):
+    with open(path) as f:
+        lines = [x.split() for x in f.read().splitlines()]
+    rows = [[int(v) for v in x] for x in lines[1:] if x]
+    return rows[:rounds]
+
+
+def kl_divergence(p_counts, q_counts, eps=1e-9):
+    p = np.asarray(p_counts, np.float64) + eps
+    q = np.asarray(q_counts, np.float64) + eps
+    p /= p.sum()
+    q /= q.sum()
+    return float(np.sum(p * np.log(p / q)))
+
+
+def run_c3(args, impl):
+    from latticednaorigami_gb300.analysis import replica_ess, bootstrap_sum, tau_int
+    tmp = tempfile.mkdtemp()
+    inp = write_c3(tmp)
+    learned_over = "movetype_file = %s" % write_learned_moves(tmp)
+    n = C3_RUNGS * C3_LADDERS
+    rounds = args.steps * C3_ROUNDS_PER_STEP
+    metric = "effective samples/s (tau_int of #bound domains per temperature), learned vs plain PTMC"
+    workload = ("c3: 48-domain HalfTurn scaffold, 24 two-domain staple types, NN energies of seeded 16-mers, 1 uM; "
+                "64 temperatures geometric 310-370 K x 32 ladders = 2048 replicas, uT exchange every 1000 steps; "
+                "learned staple exchange + learned regrowth + CB regrowth (value) vs Met exchange + Met regrowth + "
+                "CB regrowth (plain)")
+    if impl == "reference":
+        cpu = c3_cpu(inp, rounds)
+        line = {"impl": "reference", "metric": metric, "value": cpu["value"], "unit": "effective samples/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": workload}, "cpu_baseline": cpu,
+                "e2e": {"value": cpu["value"], "unit": "effective samples/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    from latticednaorigami_gb300 import Engine
+    t_burn0 = time.perf_counter()
+    # plain PT burn-in from the empty scaffold, then the network's training data
+    burn = Engine(inp, n_replicas=n, seed=900)
+    burn.autotune(probe_sweeps=2)
+    done = 0
+    while done < C3_BURN_ROUNDS:
+        k = min(100, C3_BURN_ROUNDS - done)
+        burn.pt_run(C3_RUNGS, k, C3_INTERVAL, 3)
+        done += k
+    perm = burn.pt_permutation()
+    start = [burn.config(int(perm[s])) for s in range(n)]   # by slot
+    t_train0 = time.perf_counter()
+    for _ in range(10):
+        burn.pt_run(C3_RUNGS, 2, C3_INTERVAL, 3)
+        burn.learn_collect()
+    loss0, loss1 = burn.learn_train(LEARN_ITERS, lr=LEARN_LR, seed=0)
+    table = burn.learn_table()
+    train_s = time.perf_counter() - t_train0
+    low_slot_configs = [start[l * C3_RUNGS] for l in range(C3_LADDERS)]
+    burn.close()
+    burn_s = time.perf_counter() - t_burn0
+
+    def arm(overrides, tab, seed):
+        eng = Engine(inp, n_replicas=n, seed=seed, overrides=overrides)
+        if tab is not None:
+            eng.learn_set_table(tab)
+        eng.set_configs(start)
+        tune = eng.autotune(probe_sweeps=2)
+        writers = [eng.open_swap_writer(C3_RUNGS, 3, l, os.path.join(tmp, "%d_lad%d" % (seed, l)), C3_INTERVAL)
+                   for l in range(C3_LADDERS)]
+        for _ in range(args.warmup):
+            eng.pt_run(C3_RUNGS, C3_ROUNDS_PER_STEP, C3_INTERVAL, 3)
+        for w in writers:
+            w.close()
+        writers = [eng.open_swap_writer(C3_RUNGS, 3, l, os.path.join(tmp, "%d_rec%d" % (seed, l)), C3_INTERVAL)
+                   for l in range(C3_LADDERS)]
+        eng.set_sampling(C3_SAMPLE, rounds * (C3_INTERVAL // C3_SAMPLE))
+        clocks = ClockSampler()
+        clocks.start()
+        dev_ms = []
+        for _ in range(args.steps):
+            dev_ms.append(eng.pt_run(C3_RUNGS, C3_ROUNDS_PER_STEP, C3_INTERVAL, 3))
+            for w in writers:
+                w.write(-1)
+        clk = clocks.stop()
+        for w in writers:
+            w.close()
+        smp, cnt = eng.samples()
+        rows = [read_swp_rows(os.path.join(tmp, "%d_rec%d.swp" % (seed, l)), rounds) for l in range(C3_LADDERS)]
+        series = c3_slot_series(smp, rows, rounds)
+        keys = sorted(series)
+        ess = replica_ess([series[k] for k in keys])
+        t = sum(dev_ms) / 1000.0
+        (lo, hi), boot = bootstrap_sum(ess, [q for (_, q) in keys])
+        hist = np.zeros((C3_RUNGS, 49))
+        for (l, q), x in series.items():
+            hist[q] += np.bincount(x.astype(int), minlength=49)[:49]
+        half = len(series[keys[0]]) // 2
+        top = [series[(l, C3_RUNGS - 1)] for l in range(C3_LADDERS)]
+        taus = [tau_int(series[k]) for k in keys]
+        st = eng.move_stats(3)
+        att, acc = eng.pt_stats(C3_RUNGS - 1)
+        res = {"value": float(ess.sum()) / t, "ci95": [lo / t, hi / t], "boot": boot / t,
+               "sweeps_per_s": n * rounds * C3_INTERVAL / 48.0 / t,
+               "ms_per_step": float(np.mean(dev_ms)), "tau_int_median_samples": float(np.median([x for x in taus if x])),
+               "mean_fully_bound_by_temperature": [float(hist[q] @ np.arange(49) / hist[q].sum()) for q in
+                                                   range(C3_RUNGS)],
+               "top_rung_mean_first_half": float(np.mean([x[:half].mean() for x in top])),
+               "top_rung_mean_second_half": float(np.mean([x[half:].mean() for x in top])),
+               "acceptance": {"exchange": float(st[0, 1]) / max(1.0, float(st[0, 0])),
+                              "regrowth": float(st[1, 1]) / max(1.0, float(st[1, 0])),
+                              "cb_regrowth": float(st[2, 1]) / max(1.0, float(st[2, 0]))},
+               "swap_acceptance_mean": float(acc.sum()) / max(1.0, float(att.sum())),
+               "autotune": {k: v for k, v in tune.items() if k != "candidates"}, "clocks": clk}
+        eng.close()
+        return res, hist
+
+    plain, h_plain = arm("", None, 0)
+    learned, h_learned = arm(learned_over, table, 1)
+    kl = [kl_divergence(h_plain[q], h_learned[q]) for q in range(C3_RUNGS)]
+    ratio_boot = learned.pop("boot") / plain.pop("boot")
+
+    # constant-temperature references at the top temperature: from the empty
+    # scaffold and from the burn-in's lowest-temperature configurations
+    def const_t(configs):
+        e = Engine(inp, n_replicas=C3_LADDERS, seed=77)
+        e.set_controls(temps=[C3_TEMPS[-1]] * C3_LADDERS)
+        if configs is not None:
+            e.set_configs(configs)
+        e.run(rounds * C3_INTERVAL // 2)
+        e.set_sampling(C3_SAMPLE, rounds * C3_INTERVAL // 2 // C3_SAMPLE)
+        e.run(rounds * C3_INTERVAL // 2)
+        s_, c_ = e.samples()
+        e.close()
+        return float(np.mean([s_[r, :c_[r], 0].mean() for r in range(C3_LADDERS)]))
+
+    ref_empty = const_t(None)
+    ref_assembled = const_t(low_slot_configs)
+    value = learned["value"]
+    line = {"metric": metric, "value": value, "unit": "effective samples/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": learned["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload, "rounds_per_step": C3_ROUNDS_PER_STEP, "replicas": n,
+                       "start": "both arms from the same configurations: %d rounds of plain PT from the empty "
+                                "scaffold, imported by temperature slot" % C3_BURN_ROUNDS,
+                       "l2": "state resident in shared memory; no L2 flush needed"},
+            "ci95": learned["ci95"], "learned": learned, "plain": plain,
+            "learned_over_plain": value / plain["value"],
+            "learned_over_plain_ci95": [float(np.quantile(ratio_boot, 0.025)), float(np.quantile(ratio_boot, 0.975))],
+            "kl_plain_learned_by_temperature": {"max": max(kl), "mean": float(np.mean(kl)),
+                                                "top": kl[-1], "bottom": kl[0]},
+            "stationarity": {"top_rung_370K_plain": plain["mean_fully_bound_by_temperature"][-1],
+                             "top_rung_370K_learned": learned["mean_fully_bound_by_temperature"][-1],
+                             "constant_T_370K_from_empty": ref_empty,
+                             "constant_T_370K_from_assembled": ref_assembled},
+            "network": {"train_iters": LEARN_ITERS, "loss_first": loss0, "loss_last": loss1, "train_s": train_s},
+            "burn_in_s": burn_s, "gpu_launches": None}
+    print(json.dumps(line))
+
+
+def c3_cpu(inp, rounds):
+    """The oracle port on all usable host cores: two constant-temperature
+    chains at each of the 64 temperatures (the PT exchange is omitted, as in
+    the reference's CPU baseline plan), burn-in then recorded samples every
+    100 steps."""
+    from oracle_lib import run_batch_sampled
+    from latticednaorigami_gb300.analysis import replica_ess, bootstrap_sum
+    cores, present = host_cores()
+    temps = np.repeat(C3_TEMPS, C3_CPU_REPS // C3_RUNGS)
+    burn = 2000
+    rec = rounds * C3_INTERVAL // C3_SAMPLE
+    t, smp = run_batch_sampled(inp, 0, C3_CPU_REPS, burn + rec, C3_SAMPLE, cores, temps=temps)
+    ess = replica_ess(list(smp[:, burn:]))
+    t_rec = t * rec / float(burn + rec)
+    (lo, hi), _ = bootstrap_sum(ess)
+    return {"value": float(ess.sum()) / t_rec, "ci95": [lo / t_rec, hi / t_rec], "unit": "effective samples/s",
+            "cores": cores, "cores_present_on_host": present, "kind": "port",
+            "sample": "%d constant-T chains (2 per temperature, no exchange) x %d samples every 100 steps after %d "
+                      "burn-in samples, %d threads" % (C3_CPU_REPS, rec, burn, cores),
+            "sweeps_per_s": C3_CPU_REPS * (rec * C3_SAMPLE / 48.0) / t_rec}
+
+
 def main():
     global C4_SWEEPS_PER_STEP
     ap = argparse.ArgumentParser()
@@ -488,8 +708,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c4"],
-                    help="c2: the learned-vs-plain headline workload; c4: the 96-domain umbrella workload")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4"],
+                    help="c2: the learned-vs-plain headline workload; c3: the 48-domain PTMC learned-vs-plain "
+                         "workload; c4: the 96-domain umbrella workload")
+    ap.add_argument("--c3-burn-rounds", type=int, default=0, help="c3 only: PT rounds of the plain burn-in")
+    ap.add_argument("--c3-rounds-per-step", type=int, default=0, help="c3 only: PT rounds per timed step")
     ap.add_argument("--sweeps-per-step", type=int, default=0,
                     help="c4 only: sweeps per launch (default %d); small values make short profiler captures"
                          % C4_SWEEPS_PER_STEP)
@@ -497,6 +720,15 @@ def main():
     if args.sweeps_per_step > 0:
         C4_SWEEPS_PER_STEP = args.sweeps_per_step
     rank = int(os.environ.get("RANK", "0"))
+    global C3_BURN_ROUNDS, C3_ROUNDS_PER_STEP
+    if args.c3_burn_rounds > 0:
+        C3_BURN_ROUNDS = args.c3_burn_rounds
+    if args.c3_rounds_per_step > 0:
+        C3_ROUNDS_PER_STEP = args.c3_rounds_per_step
+    if args.workload == "c3":
+        if rank == 0:
+            run_c3(args, args.impl)
+        return
     if args.workload == "c4":
         # single-GPU workload (384 replicas): other ranks have nothing to do
         if rank == 0:

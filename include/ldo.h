@@ -229,9 +229,30 @@ ldo_status ldo_pt_get_stats(ldo_engine* e, int64_t* attempts, int64_t* accepts, 
  * grid point of `grid_tag` after every step, then sets each visited point's
  * bias to ln of its reweighted probability, changes limited to max_D_bias.
  * exchange_interval > 0 attempts neighbouring-window exchanges every that
- * many steps (PTMWUS); window assignments move, configurations stay. */
+ * many steps (PTMWUS); window assignments move, configurations stay.  A
+ * second call with the same grid_tag continues the iterations (biases,
+ * visited points, windows and exchange stream kept; ldo_us_reset starts
+ * over); ldo_checkpoint_save/load carry that state between processes, as the
+ * reference's restart_us_iter archives do. */
 ldo_status ldo_us_run(ldo_engine* e, const char* grid_tag, int n_iters, int64_t equil_steps, int64_t iter_steps,
                       double max_D_bias, int exchange_interval, double* device_ms);
+/* USGCMCSimulation::output_weights (src/us_simulation.cpp:208): the grid
+ * biases of window `window` (every point visited or read) as a .biases JSON
+ * file in the reference's layout. */
+ldo_status ldo_us_write_biases(ldo_engine* e, int window, const char* path);
+/* USGCMCSimulation::read_weights (src/us_simulation.cpp:192, the read_biases
+ * restart): the grid biases of window `window` from a .biases file; sets up
+ * the umbrella state of grid bias grid_tag if there is none.  The .inp keys
+ * read_biases / biases_file / biases_filebase do the same for every window
+ * when ldo_us_run sets up (biases_filebase + "_win-<min>--<max>.biases" with
+ * a windows file, as MWUSGCMCSimulation::setup_window_sims names them). */
+ldo_status ldo_us_read_biases(ldo_engine* e, const char* grid_tag, int window, const char* path);
+/* Drops the umbrella-sampling state: the next ldo_us_run starts from zero
+ * biases (ldo_us_run otherwise continues the iterations of the last one). */
+ldo_status ldo_us_reset(ldo_engine* e);
+/* read_weights without an engine: n entries of dimension dim; points[i*dim+j],
+ * biases[i] (pass NULL buffers to get n and dim only). */
+ldo_status ldo_read_biases(const char* path, int32_t* points, double* biases, int cap, int* n, int* dim);
 /* Grid biases per window: out[w * grid_len + point]. */
 ldo_status ldo_us_get_biases(ldo_engine* e, double* out, int n_windows, int grid_len);
 /* Window held by each replica, and the grid length. */

@@ -452,8 +452,11 @@ struct ldo_engine {
         int min_op {0}, max_op {0};
         std::vector<double> E_w;        // bias per grid point (0 off grid)
         std::vector<char> in_S;         // point visited in an earlier iteration (m_S_n)
+        std::vector<char> in_file;      // point read from a .biases file (an entry of m_E_w)
     };
     std::vector<USWindow> us_win;
+    string us_tag;                      // grid bias of the current US state (empty: none)
+    long long us_iters_done {0};
     std::vector<int> us_window_of;      // replica -> window
     std::vector<int> us_replica_of;     // window -> replica
     DevBuf<int> d_us_hist, d_us_window;
@@ -1093,7 +1096,7 @@ struct ldo_engine {
         CkptHead H;
         std::memset(&H, 0, sizeof H);
         std::memcpy(H.magic, "LDOCKPT", 8);
-        H.version = 2;
+        H.version = 3;
         H.n_rep = (uint32_t)n_rep;
         H.n_sys = (uint32_t)systems.size();
         H.seed = seed;
@@ -1152,6 +1155,30 @@ struct ldo_engine {
             put(att.data(), att.size() * sizeof(long long));
             put(acc.data(), acc.size() * sizeof(long long));
         }
+        // umbrella sampling between iterations (what the reference restarts
+        // from its .S_n/.s_i/.f_i archives and .biases files,
+        // src/us_simulation.cpp:192-344): windows, biases, visited points
+        int32_t us_on = us_win.empty() ? 0 : 1;
+        put(&us_on, sizeof us_on);
+        if (us_on) {
+            int32_t nw = (int32_t)us_win.size(), tl = (int32_t)us_tag.size();
+            int32_t ints[5] = {tl, us_bias, us_len, us_sq_bias, nw};
+            put(ints, sizeof ints);
+            put(us_tag.data(), us_tag.size());
+            for (auto& w : us_win) {
+                int32_t mm[2] = {w.min_op, w.max_op};
+                put(mm, sizeof mm);
+                put(w.E_w.data(), us_len * sizeof(double));
+                put(w.in_S.data(), us_len);
+                put(w.in_file.data(), us_len);
+            }
+            put(us_window_of.data(), n_rep * sizeof(int));
+            put(us_replica_of.data(), nw * sizeof(int));
+            put(us_att.data(), us_att.size() * sizeof(long long));
+            put(us_acc.data(), us_acc.size() * sizeof(long long));
+            put(&us_swap_draws, sizeof us_swap_draws);
+            put(&us_iters_done, sizeof us_iters_done);
+        }
         H.payload_bytes = out.size() - sizeof H;
         H.payload_hash = fnv1a(reinterpret_cast<const unsigned char*>(out.data()) + sizeof H, H.payload_bytes);
         std::memcpy(&out[0], &H, sizeof H);
@@ -1174,7 +1201,7 @@ struct ldo_engine {
         };
         CkptHead H;
         get(&H, sizeof H);
-        if (std::memcmp(H.magic, "LDOCKPT", 8) != 0 || H.version != 2)
+        if (std::memcmp(H.magic, "LDOCKPT", 8) != 0 || H.version != 3)
             throw LdoError(LDO_EINVAL, path + ": not a checkpoint of this engine");
         if (H.payload_bytes != in.size() - sizeof H ||
             H.payload_hash != fnv1a(reinterpret_cast<const unsigned char*>(in.data()) + sizeof H, H.payload_bytes))
@@ -1228,6 +1255,55 @@ struct ldo_engine {
                 seen[r] = 1;
             }
         }
+        // umbrella-sampling section
+        int32_t us_on = 0;
+        get(&us_on, sizeof us_on);
+        vector<USWindow> uw;
+        string utag;
+        int32_t uints[5] = {0, -1, 0, -1, 0};
+        vector<int> u_wof, u_rof;
+        vector<long long> u_att, u_acc;
+        unsigned long long u_draws = 0;
+        long long u_iters = 0;
+        if (us_on) {
+            get(uints, sizeof uints);
+            int32_t tl = uints[0], ub = uints[1], ul = uints[2], nw = uints[4];
+            if (tl < 1 || tl > 4096 || nw != n_rep || ul < 1 || ul > 1 << 20)
+                throw LdoError(LDO_EINVAL, path + ": bad umbrella-sampling section");
+            utag.resize(tl);
+            get(&utag[0], tl);
+            const HostSystem& hs = systems[sys_of[0]];
+            if (ub < 0 || ub >= hs.desc.n_biases || hs.biases[ub].tag != utag || hs.desc.bias_kind[ub] != LDO_B_GRID ||
+                hs.desc.bias_grid_len[ub] != ul || uints[3] >= hs.desc.n_biases)
+                throw LdoError(LDO_EINVAL, path + ": umbrella-sampling grid does not match the input files");
+            uw.resize(nw);
+            for (auto& w : uw) {
+                int32_t mm[2];
+                get(mm, sizeof mm);
+                w.min_op = mm[0];
+                w.max_op = mm[1];
+                w.E_w.resize(ul);
+                w.in_S.resize(ul);
+                w.in_file.resize(ul);
+                get(w.E_w.data(), ul * sizeof(double));
+                get(w.in_S.data(), ul);
+                get(w.in_file.data(), ul);
+            }
+            u_wof.resize(n_rep);
+            u_rof.resize(nw);
+            u_att.resize(std::max(nw - 1, 1));
+            u_acc.resize(std::max(nw - 1, 1));
+            get(u_wof.data(), n_rep * sizeof(int));
+            get(u_rof.data(), nw * sizeof(int));
+            get(u_att.data(), u_att.size() * sizeof(long long));
+            get(u_acc.data(), u_acc.size() * sizeof(long long));
+            get(&u_draws, sizeof u_draws);
+            get(&u_iters, sizeof u_iters);
+            for (int r = 0; r < n_rep; ++r)
+                if (u_wof[r] < 0 || u_wof[r] >= nw || u_rof[u_wof[r]] != r)
+                    throw LdoError(LDO_EINVAL, path + ": bad umbrella window assignment");
+        }
+        if (cur != in.size()) throw LdoError(LDO_EINVAL, path + ": checkpoint file has trailing bytes");
         for (size_t i = 0; i < keys.size(); ++i)
             if (keys[i].sys < 0 || keys[i].sys >= (int)systems.size())
                 throw LdoError(LDO_EINVAL, path + ": bad table key");
@@ -1274,6 +1350,24 @@ struct ldo_engine {
         stack_mults = sm;
         u_mults = um;
         h_grid = grid;
+        us_win.clear();
+        us_tag.clear();
+        if (us_on) {
+            us_win = std::move(uw);
+            us_tag = utag;
+            us_bias = uints[1];
+            us_len = uints[2];
+            us_sq_bias = uints[3];
+            us_window_of = u_wof;
+            us_replica_of = u_rof;
+            us_att = u_att;
+            us_acc = u_acc;
+            us_swap_draws = u_draws;
+            us_iters_done = u_iters;
+            d_us_hist.alloc(us_win.size() * (size_t)us_len);
+            d_us_window.alloc(n_rep);
+            CU(copy(d_us_window.p, us_window_of.data(), n_rep * sizeof(int), cudaMemcpyHostToDevice));
+        }
         upload_tables();
         upload_ctl();
         upload_grid();
@@ -1696,6 +1790,20 @@ struct ldo_engine {
         for (auto& w : us_win) {
             w.E_w.assign(us_len, 0.0);
             w.in_S.assign(us_len, 0);
+            w.in_file.assign(us_len, 0);
+        }
+        // read_biases (USGCMCSimulation constructor, src/us_simulation.cpp:48-66,
+        // with the window's file name of MWUSGCMCSimulation::setup_window_sims,
+        // :527-531): each window's grid biases from a .biases file
+        if (hs.p.read_biases) {
+            for (int i = 0; i < nw; ++i) {
+                string f = hs.p.windows_file.empty()
+                                   ? hs.p.biases_file
+                                   : hs.p.biases_filebase +
+                                             ldo_io::window_postfix({us_win[i].min_op}, {us_win[i].max_op}) +
+                                             ".biases";
+                us_read_biases(i, ldo_io::resolve(hs.p, f));
+            }
         }
         us_window_of.resize(n_rep);
         us_replica_of.resize(nw);
@@ -1706,9 +1814,45 @@ struct ldo_engine {
         us_att.assign(std::max(nw - 1, 1), 0);
         us_acc.assign(std::max(nw - 1, 1), 0);
         us_swap_draws = 0;
+        us_iters_done = 0;
+        us_tag = grid_tag;
         d_us_hist.alloc((size_t)nw * us_len);
         d_us_window.alloc(n_rep);
         us_apply_windows();
+    }
+
+    // USGCMCSimulation::read_weights (src/us_simulation.cpp:192) into window
+    // w: every 1-D grid point of the file becomes an entry of its biases.
+    void us_read_biases(int w, const string& path) {
+        vector<ldo_io::GridBias> g;
+        try {
+            if (!ldo_io::file_exists(path)) throw std::runtime_error("Restart bias file " + path + " does not exist");
+            g = ldo_io::read_biases_json(path);
+        } catch (std::exception& x) {
+            throw LdoError(LDO_EINVAL, x.what());
+        }
+        USWindow& W = us_win.at(w);
+        for (auto& e : g) {
+            if (e.point.size() != 1) throw LdoError(LDO_EINVAL, path + ": the grid order parameter is one-dimensional");
+            int x = e.point[0];
+            if (x < 0 || x >= us_len) throw LdoError(LDO_EINVAL, path + ": grid point outside the order parameter's range");
+            W.E_w[x] = e.bias;
+            W.in_file[x] = 1;
+        }
+    }
+
+    // USGCMCSimulation::output_weights (src/us_simulation.cpp:208) of window
+    // w: the points that have a bias entry (visited or read), in ascending
+    // order.
+    void us_write_biases(int w, const string& path) const {
+        const USWindow& W = us_win.at(w);
+        vector<ldo_io::GridBias> g;
+        for (int x = 0; x < us_len; ++x)
+            if (W.in_S[x] || W.in_file[x]) g.push_back(ldo_io::GridBias {{x}, W.E_w[x]});
+        std::ofstream f(path);
+        if (!f) throw LdoError(LDO_EINVAL, path + ": cannot open for writing");
+        f << ldo_io::biases_json_text(g);
+        if (!f) throw LdoError(LDO_EINVAL, path + ": writing failed");
     }
 
     // Window restraint and grid values of every replica follow the window it holds
@@ -1819,7 +1963,10 @@ struct ldo_engine {
 
     void us_run(const string& tag, int n_iters, long long equil_steps, long long iter_steps, double max_D,
                 int exchange_interval, double* ms) {
-        us_setup(tag);
+        // A second run with the same grid bias continues the iterations (the
+        // reference restarts them from its archives, :312-344); equil_steps
+        // run before this call's first iteration.
+        if (us_tag != tag || us_win.empty()) us_setup(tag);
         CU(cudaEventRecord(ev0, stream));
         // USGCMCSimulation::run_equilibration
         if (equil_steps > 0) us_launch(equil_steps, false);
@@ -1841,6 +1988,7 @@ struct ldo_engine {
             CU(cudaStreamSynchronize(stream));
             check_status();
             us_process_iteration(hist, max_D);
+            ++us_iters_done;
         }
         CU(cudaEventRecord(ev1, stream));
         CU(cudaStreamSynchronize(stream));
@@ -2240,6 +2388,50 @@ ldo_status ldo_us_run(ldo_engine* e, const char* grid_tag, int n_iters, int64_t 
         return LDO_EINVAL;
     return guard(e, [&]() {
         e->us_run(grid_tag, n_iters, equil_steps, iter_steps, max_D_bias, exchange_interval, device_ms);
+    });
+}
+
+ldo_status ldo_us_write_biases(ldo_engine* e, int window, const char* path) {
+    if (!e || !path) return LDO_EINVAL;
+    return guard(e, [&]() {
+        if (e->us_win.empty()) throw LdoError(LDO_EINVAL, "no umbrella-sampling state: run ldo_us_run first");
+        if (window < 0 || window >= (int)e->us_win.size()) throw LdoError(LDO_EINVAL, "no such window");
+        e->us_write_biases(window, path);
+    });
+}
+
+ldo_status ldo_us_read_biases(ldo_engine* e, const char* grid_tag, int window, const char* path) {
+    if (!e || !grid_tag || !path) return LDO_EINVAL;
+    return guard(e, [&]() {
+        if (e->us_tag != grid_tag || e->us_win.empty()) e->us_setup(grid_tag);
+        if (window < 0 || window >= (int)e->us_win.size()) throw LdoError(LDO_EINVAL, "no such window");
+        e->us_read_biases(window, path);
+        e->us_apply_windows();
+    });
+}
+
+ldo_status ldo_us_reset(ldo_engine* e) {
+    if (!e) return LDO_EINVAL;
+    return guard(e, [&]() {
+        e->us_win.clear();
+        e->us_tag.clear();
+    });
+}
+
+ldo_status ldo_read_biases(const char* path, int32_t* points, double* biases, int cap, int* n, int* dim) {
+    if (!path || !n || !dim) return LDO_EINVAL;
+    return guard(nullptr, [&]() {
+        auto g = ldo_io::read_biases_json(path);
+        *n = (int)g.size();
+        *dim = g.empty() ? 0 : (int)g[0].point.size();
+        for (auto& x : g)
+            if ((int)x.point.size() != *dim) throw LdoError(LDO_EINVAL, string(path) + ": points of mixed dimension");
+        if (!points || !biases) return;
+        if (cap < *n) throw LdoError(LDO_EINVAL, "output buffers too small");
+        for (int i = 0; i < *n; ++i) {
+            for (int j = 0; j < *dim; ++j) points[(size_t)i * *dim + j] = g[i].point[j];
+            biases[i] = g[i].bias;
+        }
     });
 }
 

@@ -307,6 +307,11 @@ struct Params {
     double max_rel_P_diff {0.1};
     bool multi_window {false};
     string windows_file;
+    // umbrella-sampling restart (USGCMCSimulation constructor,
+    // src/us_simulation.cpp:48-87): grid biases read from .biases files
+    bool read_biases {false};
+    string biases_file;
+    string biases_filebase;
     string output_filebase;
     int logging_freq {0};
     int configs_output_freq {0};
@@ -408,6 +413,9 @@ inline void set_param(Params& p, const string& k, const string& v) {
     else if (k == "max_rel_P_diff") p.max_rel_P_diff = D();
     else if (k == "multi_window") p.multi_window = parse_bool(v);
     else if (k == "windows_file") p.windows_file = v;
+    else if (k == "read_biases") p.read_biases = parse_bool(v);
+    else if (k == "biases_file") p.biases_file = v;
+    else if (k == "biases_filebase") p.biases_filebase = v;
     else if (k == "output_filebase") p.output_filebase = v;
     else if (k == "logging_freq") p.logging_freq = I();
     else if (k == "configs_output_freq") p.configs_output_freq = I();
@@ -451,6 +459,11 @@ inline Params parse_inp_text(const string& text, const string& base_dir = "") {
 inline string dir_of(const string& path) {
     auto s = path.find_last_of('/');
     return s == string::npos ? string() : path.substr(0, s + 1);
+}
+
+inline bool file_exists(const string& f) {
+    std::ifstream in(f);
+    return (bool)in;
 }
 
 inline string resolve(const Params& p, const string& f) {
@@ -744,6 +757,63 @@ inline Windows read_windows(const string& fname) {
         w.bounds.push_back({std::stoi(t[0]), std::stoi(t[1])});
     }
     return w;
+}
+
+// ------------------------------------------------------ .biases files ----
+// Grid biases of an umbrella-sampling window: {"biases": [{"point": [..],
+// "bias": x}, ..]}, read by USGCMCSimulation::read_weights
+// (src/us_simulation.cpp:192) and written by output_weights (:208).
+struct GridBias {
+    vector<int> point;
+    double bias;
+};
+
+inline vector<GridBias> read_biases_json(const string& fname) {
+    JVal root = read_json(fname, "Restart bias file");
+    const JVal& arr = root["biases"];
+    if (arr.kind != JVal::Arr) throw std::runtime_error("Restart bias file " + fname + " has no biases array");
+    vector<GridBias> out;
+    for (size_t i = 0; i < arr.size(); ++i) {
+        const JVal& e = arr[i];
+        GridBias g;
+        for (size_t j = 0; j < e["point"].size(); ++j) g.point.push_back(e["point"][j].as_int());
+        if (g.point.empty()) throw std::runtime_error("Restart bias file " + fname + ": an entry has no point");
+        g.bias = e["bias"].as_double();
+        out.push_back(g);
+    }
+    return out;
+}
+
+// output_weights' layout: one entry per grid point, each bias printed by
+// std::to_string (six decimals), no trailing comma.
+inline string biases_json_text(const vector<GridBias>& entries) {
+    std::ostringstream os;
+    os << "{\n";
+    os << "    \"biases\": [";
+    for (size_t i = 0; i < entries.size(); ++i) {
+        os << (i == 0 ? "\n" : ",\n");
+        const auto& g = entries[i];
+        os << "        {\n";
+        os << "            \"point\": [\n";
+        for (size_t j = 0; j + 1 < g.point.size(); ++j) os << "                " << std::to_string(g.point[j]) << ",\n";
+        os << "                " << std::to_string(g.point.back()) << "\n";
+        os << "            ],\n";
+        os << "            \"bias\": " << std::to_string(g.bias) << "\n";
+        os << "        }";
+    }
+    os << "\n    ]\n";
+    os << "}\n";
+    return os.str();
+}
+
+// MWUSGCMCSimulation::setup_window_variables (src/us_simulation.cpp:487):
+// the file-name postfix of a window, "_win-" + each min + "-", then "-" +
+// each max (a 1-D window 0..8 gives "_win-0--8").
+inline string window_postfix(const vector<int>& mins, const vector<int>& maxs) {
+    string s = "_win-";
+    for (int j : mins) s += std::to_string(j) + "-";
+    for (int j : maxs) s += "-" + std::to_string(j);
+    return s;
 }
 
 } // namespace ldo_io

@@ -24,7 +24,8 @@ EXPORTS = [
     "ldo_learn_get_params", "ldo_learn_get_table", "ldo_learn_set_table", "ldo_learn_loss_grad",
     "ldo_writer_open", "ldo_writer_write", "ldo_writer_close", "ldo_pt2d_run", "ldo_engine_exp",
     "ldo_set_bias_centre", "ldo_swap_writer_open", "ldo_set_config", "ldo_set_configs", "ldo_anneal_run", "ldo_read_trj_frame", "ldo_checkpoint_save",
-    "ldo_checkpoint_load", "ldo_autotune", "ldo_autotune_candidates",
+    "ldo_checkpoint_load", "ldo_autotune", "ldo_autotune_candidates", "ldo_us_write_biases",
+    "ldo_us_read_biases", "ldo_us_reset", "ldo_read_biases",
 ]
 
 LEARN_TABLE = 524544      # network inputs: 524288 insertion + 256 regrowth-direction (ldo_learn.h)
@@ -78,6 +79,11 @@ def load_library(path=None):
     lib.ldo_run.argtypes = [vp, ctypes.c_int64, dp]
     lib.ldo_run_sweeps.argtypes = [vp, ctypes.c_int64, dp]
     lib.ldo_state_bytes.argtypes = [vp]
+    lib.ldo_us_write_biases.argtypes = [vp, ip, ctypes.c_char_p]
+    lib.ldo_us_read_biases.argtypes = [vp, ctypes.c_char_p, ip, ctypes.c_char_p]
+    lib.ldo_us_reset.argtypes = [vp]
+    lib.ldo_read_biases.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int32), dp, ip,
+                                    ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     lib.ldo_autotune.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(TuneReport)]
     lib.ldo_autotune_candidates.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), dp, ctypes.c_int32]
     lib.ldo_get_observables.argtypes = [vp, ctypes.POINTER(Observables), ip]
@@ -311,6 +317,17 @@ class Engine:
         self._check(self.lib.ldo_us_get_biases(self.h, _dptr(out), self.n, gl))
         return out
 
+    def us_write_biases(self, window, path):
+        """The window's grid biases as a .biases file (output_weights)."""
+        self._check(self.lib.ldo_us_write_biases(self.h, int(window), os.fsencode(path)))
+
+    def us_read_biases(self, grid_tag, window, path):
+        """Grid biases of a window from a .biases file (read_weights)."""
+        self._check(self.lib.ldo_us_read_biases(self.h, grid_tag.encode(), int(window), os.fsencode(path)))
+
+    def us_reset(self):
+        self._check(self.lib.ldo_us_reset(self.h))
+
     def open_swap_writer(self, n_rungs, exchange_q, ladder, filebase, freq):
         """The .swp file of one parallel-tempering ladder (ldo_swap_writer_open);
         Writer.write(step) appends the rows recorded by pt_run (step >= 0 adds
@@ -414,6 +431,23 @@ def learn_loss_grad(params, idx, cnt_bound, cnt_total):
     if rc != 0:
         raise LdoError(rc, lib.ldo_last_error(None).decode())
     return loss.value, grad
+
+
+def read_biases(path):
+    """A .biases file (USGCMCSimulation::read_weights) without an engine:
+    (points int32[n, dim], biases float64[n])."""
+    lib = load_library()
+    n, dim = ctypes.c_int(0), ctypes.c_int(0)
+    rc = lib.ldo_read_biases(os.fsencode(path), None, None, 0, ctypes.byref(n), ctypes.byref(dim))
+    if rc != 0:
+        raise LdoError(rc, "cannot read %s" % path)
+    pts = np.zeros((n.value, max(dim.value, 1)), np.int32)
+    b = np.zeros(n.value)
+    rc = lib.ldo_read_biases(os.fsencode(path), pts.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _dptr(b),
+                             n.value, ctypes.byref(n), ctypes.byref(dim))
+    if rc != 0:
+        raise LdoError(rc, "cannot read %s" % path)
+    return pts[:, :dim.value], b
 
 
 def read_trj_frame(path, frame):

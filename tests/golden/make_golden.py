@@ -376,6 +376,11 @@ def make_us_update(tmp, only=None):
     ora = RefUS(inp, seed, US_WINDOWS, "grid", "win", 25)
     ora.run(iters, equil, steps, max_D, 0)
     ref.close()
+    # the .biases file the reference's output_weights wrote for window 1
+    # after the last iteration (process_iteration, src/us_simulation.cpp:169)
+    with open(os.path.join(os.path.dirname(inp), "ref_trace_out_win1.biases")) as f, \
+            open(os.path.join(HERE, "outputs", "us_update_win1.biases"), "w") as g:
+        g.write(f.read())
     fx = {"seed": seed, "iters": iters, "equil": equil, "steps": steps, "max_D": max_D, "windows": US_WINDOWS,
           "grid_len": 25, "iterations": record, "window_of": ora.window_of,
           "draws": [int(r.observables()["draws"]) for r in ora.reps]}

