@@ -1407,6 +1407,23 @@ struct Rep : public LdoState<C> {
                 }
                 break;
             }
+            case LDO_OP_DIST:
+            case LDO_OP_ADJACENT: {
+                // DistOrderParam / AdjacentSiteOrderParam::calc_param
+                // (src/order_params.cpp:35, :84): defined while both domains
+                // are assigned; the value is kept while undefined
+                int a = s->op_parts[q][0], b = s->op_parts[q][1];
+                if (st[a] != UNASSIGNED && st[b] != UNASSIGNED) {
+                    V3 d = pos(b) - pos(a);
+                    int l1 = abs(d.x) + abs(d.y) + abs(d.z);
+                    v = s->op_kind[q] == LDO_OP_DIST ? l1 : (l1 == 1 ? 1 : 0);
+                }
+                else {
+                    defined = 0;
+                    v = op[2 * q];
+                }
+                break;
+            }
             }
             op[2 * q] = v;
             op[2 * q + 1] = defined;

@@ -231,14 +231,32 @@ HostSystem load_system(const string& inp, const string& overrides) {
         else if (o.type == "NumStackedPairs") k = LDO_OP_NUMSTACKED;
         else if (o.type == "NumLinearHelices" || o.type == "NumStackedJuncts") k = LDO_OP_ZERO;
         else if (o.type == "Sum") k = LDO_OP_SUM;
-        else if (o.type == "Dist" || o.type == "AdjacentSite")
-            throw LdoError(LDO_EINVAL, o.type + ": per-domain order parameters are not implemented by this engine");
+        else if (o.type == "Dist") k = LDO_OP_DIST;
+        else if (o.type == "AdjacentSite") k = LDO_OP_ADJACENT;
         else throw LdoError(LDO_EINVAL, o.type + ": order parameter type does not exist");
         d.op_kind[q] = k;
         d.op_arg[q] = o.staple;
         if (k == LDO_OP_NUMSTAPLESTYPE || k == LDO_OP_STAPLETYPEFULLYBOUND)
             if (o.staple < 1 || o.staple >= d.n_types) throw LdoError(LDO_EINVAL, "order parameter staple out of range");
         if (k == LDO_OP_NUMBOUND && d.fully_op < 0) d.fully_op = (int)q;
+        if (k == LDO_OP_DIST || k == LDO_OP_ADJACENT) {
+            // the pair of domains (chain index, domain index) the reference
+            // looks up once at set-up (SystemOrderParams::setup_ops,
+            // src/order_params.cpp:495-512); this engine takes scaffold domains
+            // and the move-level update (update_per_domain false)
+            int sc = hs.sf.chains.empty() ? 0 : hs.sf.chains[0].index;
+            if (o.update_per_domain)
+                throw LdoError(LDO_EINVAL, o.type + " order parameter " + o.tag +
+                                                   ": update_per_domain is not supported by this engine");
+            if (o.chain1 != sc || o.chain2 != sc)
+                throw LdoError(LDO_EINVAL, o.type + " order parameter " + o.tag +
+                                                   ": this engine takes scaffold domains only");
+            if (o.domain1 < 0 || o.domain1 >= d.ns || o.domain2 < 0 || o.domain2 >= d.ns)
+                throw LdoError(LDO_EINVAL, o.type + " order parameter " + o.tag + ": domain out of range");
+            d.op_nparts[q] = 2;
+            d.op_parts[q][0] = o.domain1;
+            d.op_parts[q][1] = o.domain2;
+        }
         if (k == LDO_OP_SUM) {
             if (o.ops.size() > LDO_MAX_PARTS) throw LdoError(LDO_EINVAL, "Sum over too many order parameters");
             d.op_nparts[q] = (int)o.ops.size();

@@ -46,7 +46,9 @@ enum LdoOp {
     LDO_OP_NUMMISBOUND,
     LDO_OP_NUMSTACKED,
     LDO_OP_ZERO,   // NumLinearHelices / NumStackedJuncts: never updated by the reference
-    LDO_OP_SUM
+    LDO_OP_SUM,
+    LDO_OP_DIST,       // DistOrderParam: L1 distance of two scaffold domains (op_parts[q][0..1])
+    LDO_OP_ADJACENT    // AdjacentSiteOrderParam: 1 if that distance is 1
 };
 
 enum LdoBias { LDO_B_LINEARSTEPWELL = 0, LDO_B_SQUAREWELL, LDO_B_GRID, LDO_B_HARMONIC };

@@ -137,6 +137,12 @@ Replica* build(const char* inp_path, const char* overrides, uint32_t seed, uint3
                 else if (o.type == "NumStackedPairs") rec.kind = OP_NUMSTACKED;
                 else if (o.type == "NumLinearHelices") rec.kind = OP_NUMLINEARHELICES;
                 else if (o.type == "NumStackedJuncts") rec.kind = OP_NUMSTACKEDJUNCTS;
+                else if (o.type == "Dist" || o.type == "AdjacentSite") {
+                    // scaffold domains, updated per move (update_per_domain false)
+                    rec.kind = o.type == "Dist" ? OP_DIST : OP_ADJACENT;
+                    if (o.update_per_domain) throw std::runtime_error(o.type + ": update_per_domain not supported");
+                    rec.parts = {o.domain1, o.domain2};
+                }
                 else if (o.type == "Sum") {
                     rec.kind = OP_SUM;
                     for (auto& t : o.ops) {

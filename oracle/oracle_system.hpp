@@ -165,7 +165,7 @@ struct SiteMap : std::unordered_map<uint64_t, SiteRec> {
 
 // ------------------------------------------------------- order params ----
 enum OpKind { OP_NUMSTAPLES, OP_NUMSTAPLESTYPE, OP_STAPLETYPEFULLYBOUND, OP_NUMBOUND, OP_NUMMISBOUND,
-              OP_NUMSTACKED, OP_NUMLINEARHELICES, OP_NUMSTACKEDJUNCTS, OP_SUM };
+              OP_NUMSTACKED, OP_NUMLINEARHELICES, OP_NUMSTACKEDJUNCTS, OP_SUM, OP_DIST, OP_ADJACENT };
 
 struct OpRec {
     OpKind kind;
@@ -1195,6 +1195,20 @@ class System {
                     else { op.defined = false; s = op.param; break; }
                 }
                 op.param = s;
+                break;
+            }
+            case OP_DIST:            // DistOrderParam::calc_param (src/order_params.cpp:35)
+            case OP_ADJACENT: {      // AdjacentSiteOrderParam::calc_param (:84)
+                const Dom& a = doms[chains[0][op.parts[0]]];
+                const Dom& b = doms[chains[0][op.parts[1]]];
+                if (a.state != UNASSIGNED && b.state != UNASSIGNED) {
+                    op.defined = true;
+                    int l1 = (b.pos - a.pos).abssum();
+                    op.param = op.kind == OP_DIST ? l1 : (l1 == 1 ? 1 : 0);
+                }
+                else {
+                    op.defined = false;
+                }
                 break;
             }
             }

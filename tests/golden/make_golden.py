@@ -47,7 +47,9 @@ RUNS = [("c1", 1, 20000), ("c1", 2, 20000), ("g24a", 3, 20000), ("g24b", 4, 2000
         # the 96-domain ThreeQuarterTurn design with two- and three-domain staples
         ("c4", 9, 20000),
         # a run with a weight ratio within a rounding of 1 at step 19885 (long double vs FP64)
-        ("s24a", 11, 20000)]
+        ("s24a", 11, 20000),
+        # Dist / AdjacentSite order parameters with biases, on a moving scaffold
+        ("d24", 12, 20000)]
 
 
 def ref_trace(inp, seed, steps, replica=0):

@@ -196,6 +196,23 @@ BIASES = {"origami": {"bias_functions": [
      "outside_bias": 1.25, "ops": ["numstaples"], "level": 0},
     {"label": "grid", "tag": "grid", "type": "Grid", "ops": ["numfulldomains"], "level": 0}]}}
 
+# Per-domain order parameters between scaffold domains (DistOrderParam,
+# AdjacentSiteOrderParam, src/order_params.cpp:25-133), updated per move, with
+# bias functions on them.
+OPS_DIST = {"origami": {"order_params": OPS["origami"]["order_params"] + [
+    {"label": "End-to-end distance", "tag": "dist0_23", "type": "Dist", "chain1": 0, "domain1": 0, "chain2": 0,
+     "domain2": 23, "update_per_domain": False, "level": 0},
+    {"label": "Domains 4 and 19 adjacent", "tag": "adj4_19", "type": "AdjacentSite", "chain1": 0, "domain1": 4,
+     "chain2": 0, "domain2": 19, "update_per_domain": False, "level": 0},
+    {"label": "Distance plus bound", "tag": "distplusbound", "type": "Sum", "ops": ["dist0_23", "numfulldomains"],
+     "level": 1}]}}
+
+BIASES_DIST = {"origami": {"bias_functions": [
+    {"label": "dist well", "tag": "distwell", "type": "LinearStepWell", "min_op": 2, "max_op": 6, "well_bias": 0,
+     "min_bias": 0.5, "slope": 0.75, "ops": ["dist0_23"], "level": 0},
+    {"label": "adjacent", "tag": "adj", "type": "SquareWell", "min_op": 1, "max_op": 1, "well_bias": -1.5,
+     "outside_bias": 0.0, "ops": ["adj4_19"], "level": 0}]}}
+
 BASE = dict(domain_type="HalfTurn", binding_pot="FourBody", misbinding_pot="Opposing", stacking_pot="Constant",
             hybridization_pot="NearestNeighbour", temp=330, staple_M=1e-6, cation_M=0.5, max_staple_size=2,
             order_parameter_file="ops.json")
@@ -229,6 +246,10 @@ CASES = {
                                     max_type_staples=4, bias_functions_file="biases.json",
                                     bias_functions_mult=0.7)),
     # cyclic scaffold (a closed ring), every scaffold movetype
+    # Dist / AdjacentSite order parameters with biases on a scaffold that moves
+    "d24": ("grid24", "ctrg", dict(stacking_ene=-1000, staple_M=1e-3, temp=335, max_total_staples=24,
+                                   max_type_staples=4, order_parameter_file="ops_dist.json",
+                                   bias_functions_file="biases_dist.json")),
     "r24": ("ring24", "ctall", dict(stacking_ene=-1000, staple_M=1e-3, temp=330, max_total_staples=24,
                                     max_type_staples=4)),
     # the 96-domain ThreeQuarterTurn design (40 staple types of 2-3 domains,
@@ -280,6 +301,10 @@ def write_case(dirname, name, extra=None):
         json.dump(OPS, f)
     with open(os.path.join(dirname, "biases.json"), "w") as f:
         json.dump(BIASES, f)
+    with open(os.path.join(dirname, "ops_dist.json"), "w") as f:
+        json.dump(OPS_DIST, f)
+    with open(os.path.join(dirname, "biases_dist.json"), "w") as f:
+        json.dump(BIASES_DIST, f)
     opts = dict(BASE)
     opts["origami_input_filename"] = sysname + ".json"
     opts["movetype_file"] = "moves_%s.json" % moves
