@@ -494,7 +494,13 @@ def run_c4(args, impl):
 C3_RUNGS, C3_LADDERS, C3_INTERVAL, C3_SAMPLE = 64, 32, 1000, 100
 C3_TEMPS = [310.0 * (370.0 / 310.0) ** (k / 63.0) for k in range(64)]
 C3_ROUNDS_PER_STEP = 25
-C3_BURN_ROUNDS = 1000
+# Burn-in: C3_BURN_ROUNDS rounds of plain PT from the empty scaffold (the
+# network's first training data), then C3_RELAX_ROUNDS rounds of PT with the
+# learned moveset, which samples the same distribution and assembles the
+# low-temperature rungs far faster, then the network trained again on those
+# states.  Both timed arms start from the result, imported by slot.
+C3_BURN_ROUNDS = 200
+C3_RELAX_ROUNDS = 800
 C3_CPU_REPS = 128
 
 
@@ -567,17 +573,37 @@ def run_c3(args, impl):
         k = min(100, C3_BURN_ROUNDS - done)
         burn.pt_run(C3_RUNGS, k, C3_INTERVAL, 3)
         done += k
-    perm = burn.pt_permutation()
-    start = [burn.config(int(perm[s])) for s in range(n)]   # by slot
     t_train0 = time.perf_counter()
-    for _ in range(10):
-        burn.pt_run(C3_RUNGS, 2, C3_INTERVAL, 3)
-        burn.learn_collect()
-    loss0, loss1 = burn.learn_train(LEARN_ITERS, lr=LEARN_LR, seed=0)
-    table = burn.learn_table()
+
+    def collect_train(e):
+        for _ in range(10):
+            e.pt_run(C3_RUNGS, 2, C3_INTERVAL, 3)
+            e.learn_collect()
+        return e.learn_train(LEARN_ITERS, lr=LEARN_LR, seed=0)
+
+    collect_train(burn)
+    table0 = burn.learn_table()
     train_s = time.perf_counter() - t_train0
-    low_slot_configs = [start[l * C3_RUNGS] for l in range(C3_LADDERS)]
+    perm = burn.pt_permutation()
+    mid = [burn.config(int(perm[s])) for s in range(n)]   # by slot
     burn.close()
+    relax = Engine(inp, n_replicas=n, seed=901, overrides=learned_over)
+    relax.learn_set_table(table0)
+    relax.set_configs(mid)
+    relax.autotune(probe_sweeps=2)
+    done = 0
+    while done < C3_RELAX_ROUNDS:
+        k = min(100, C3_RELAX_ROUNDS - done)
+        relax.pt_run(C3_RUNGS, k, C3_INTERVAL, 3)
+        done += k
+    t_train1 = time.perf_counter()
+    loss0, loss1 = collect_train(relax)
+    table = relax.learn_table()
+    train_s += time.perf_counter() - t_train1
+    perm = relax.pt_permutation()
+    start = [relax.config(int(perm[s])) for s in range(n)]   # by slot
+    relax.close()
+    low_slot_configs = [start[l * C3_RUNGS] for l in range(C3_LADDERS)]
     burn_s = time.perf_counter() - t_burn0
 
     def arm(overrides, tab, seed):
@@ -625,6 +651,10 @@ def run_c3(args, impl):
                "ms_per_step": float(np.mean(dev_ms)), "tau_int_median_samples": float(np.median([x for x in taus if x])),
                "mean_fully_bound_by_temperature": [float(hist[q] @ np.arange(49) / hist[q].sum()) for q in
                                                    range(C3_RUNGS)],
+               "max_rung_drift_between_halves": float(max(
+                   abs(np.mean([series[(l, q)][:half].mean() for l in range(C3_LADDERS)]) -
+                       np.mean([series[(l, q)][half:].mean() for l in range(C3_LADDERS)]))
+                   for q in range(C3_RUNGS))),
                "top_rung_mean_first_half": float(np.mean([x[:half].mean() for x in top])),
                "top_rung_mean_second_half": float(np.mean([x[half:].mean() for x in top])),
                "acceptance": {"exchange": float(st[0, 1]) / max(1.0, float(st[0, 0])),
@@ -662,7 +692,8 @@ def run_c3(args, impl):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": workload, "rounds_per_step": C3_ROUNDS_PER_STEP, "replicas": n,
                        "start": "both arms from the same configurations: %d rounds of plain PT from the empty "
-                                "scaffold, imported by temperature slot" % C3_BURN_ROUNDS,
+                                "scaffold, then %d rounds of PT with the learned moveset, imported by temperature "
+                                "slot" % (C3_BURN_ROUNDS, C3_RELAX_ROUNDS),
                        "l2": "state resident in shared memory; no L2 flush needed"},
             "ci95": learned["ci95"], "learned": learned, "plain": plain,
             "learned_over_plain": value / plain["value"],
@@ -701,7 +732,7 @@ def c3_cpu(inp, rounds):
 
 
 def main():
-    global C4_SWEEPS_PER_STEP
+    global C4_SWEEPS_PER_STEP, SWEEPS_PER_STEP
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -712,17 +743,22 @@ def main():
                     help="c2: the learned-vs-plain headline workload; c3: the 48-domain PTMC learned-vs-plain "
                          "workload; c4: the 96-domain umbrella workload")
     ap.add_argument("--c3-burn-rounds", type=int, default=0, help="c3 only: PT rounds of the plain burn-in")
+    ap.add_argument("--c3-relax-rounds", type=int, default=0,
+                    help="c3 only: PT rounds of the learned relaxation after the burn-in")
     ap.add_argument("--c3-rounds-per-step", type=int, default=0, help="c3 only: PT rounds per timed step")
     ap.add_argument("--sweeps-per-step", type=int, default=0,
-                    help="c4 only: sweeps per launch (default %d); small values make short profiler captures"
-                         % C4_SWEEPS_PER_STEP)
+                    help="sweeps per launch (default c2 %d, c4 %d); small values make short profiler captures"
+                         % (SWEEPS_PER_STEP, C4_SWEEPS_PER_STEP))
     args = ap.parse_args()
     if args.sweeps_per_step > 0:
         C4_SWEEPS_PER_STEP = args.sweeps_per_step
+        SWEEPS_PER_STEP = args.sweeps_per_step
     rank = int(os.environ.get("RANK", "0"))
-    global C3_BURN_ROUNDS, C3_ROUNDS_PER_STEP
+    global C3_BURN_ROUNDS, C3_ROUNDS_PER_STEP, C3_RELAX_ROUNDS
     if args.c3_burn_rounds > 0:
         C3_BURN_ROUNDS = args.c3_burn_rounds
+    if args.c3_relax_rounds > 0:
+        C3_RELAX_ROUNDS = args.c3_relax_rounds
     if args.c3_rounds_per_step > 0:
         C3_ROUNDS_PER_STEP = args.c3_rounds_per_step
     if args.workload == "c3":

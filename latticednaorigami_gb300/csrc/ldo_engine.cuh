@@ -1414,8 +1414,8 @@ struct Rep : public LdoState<C> {
                 // are assigned; the value is kept while undefined
                 int a = s->op_parts[q][0], b = s->op_parts[q][1];
                 if (st[a] != UNASSIGNED && st[b] != UNASSIGNED) {
-                    V3 d = pos(b) - pos(a);
-                    int l1 = abs(d.x) + abs(d.y) + abs(d.z);
+                    V3 d = sub(pos(b), pos(a));
+                    int l1 = abs(vx(d)) + abs(vy(d)) + abs(vz(d));
                     v = s->op_kind[q] == LDO_OP_DIST ? l1 : (l1 == 1 ? 1 : 0);
                 }
                 else {
