@@ -16,7 +16,7 @@
 #define LDO_MAX_TYPES 96
 #define LDO_MAX_IDENTS 1024
 #define LDO_MAX_MOVES 8
-#define LDO_MAX_OPS 8
+#define LDO_MAX_OPS 16
 #define LDO_MAX_BIASES 4
 #define LDO_MAX_PARTS 4
 #define LDO_MAX_LEN 4

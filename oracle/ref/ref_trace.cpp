@@ -130,8 +130,50 @@ int main(int argc, char** argv) {
     try {
         origami::OrigamiSystem* o = origami::setup_origami(params);
         if (mode == "enumerate") {
-            enumerator::enumerate_main(*o, o->get_system_order_params(), o->get_system_biases(), params);
-            std::cout << "{\"enumerated\": true}\n";
+            // enumerate_main (src/enumerate.cpp:19) with the weights printed
+            // at full precision instead of print_weights' six digits
+            auto& ops = o->get_system_order_params();
+            auto& biases = o->get_system_biases();
+            enumerator::OvercountCalculator* oc;
+            if (params.m_max_staple_size == 2) oc = new enumerator::MaxTwoDomainOvercountCalculator {};
+            else if (params.m_misbinding_pot == "Disallowed") oc = new enumerator::MisbindingOnlyOvercountCalculator {};
+            else throw std::runtime_error("No enumerator available for system");
+            enumerator::ConformationalEnumerator* ce;
+            if (params.m_enumerate_staples_only)
+                ce = new enumerator::StapleConformationalEnumerator {*o, *oc, ops, biases, params.m_ops_to_output,
+                                                                      params.m_apply_mean_field_cor};
+            else
+                ce = new enumerator::ConformationalEnumerator {*o, *oc, ops, biases, params.m_ops_to_output,
+                                                               params.m_apply_mean_field_cor};
+            enumerator::GrowthpointEnumerator* ge;
+            if (params.m_misbinding_pot == "Disallowed")
+                ge = new enumerator::NoMisbindingGrowthpointEnumerator {*ce, *o};
+            else
+                ge = new enumerator::MisbindingGrowthpointEnumerator {*ce, *o};
+            enumerator::StapleEnumerator se {*ge, *ce, *o, params.m_excluded_staples};
+            auto t0 = std::chrono::steady_clock::now();
+            se.enumerate(params.m_min_total_staples, params.m_max_total_staples, params.m_max_type_staples);
+            double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            ce->normalize_weights();
+            std::map<vector<int>, double> sorted(ce->m_normalized_weights.begin(), ce->m_normalized_weights.end());
+            std::ostringstream js;
+            js << "@@{\"weights\": {";
+            bool first = true;
+            for (auto& kv : sorted) {
+                js << (first ? "" : ", ") << "\"";
+                for (size_t i = 0; i < kv.first.size(); ++i) js << (i ? " " : "") << kv.first[i];
+                char b[64];
+                std::snprintf(b, sizeof b, "\": %.17g", kv.second);
+                js << b;
+                first = false;
+            }
+            char b[128];
+            std::snprintf(b, sizeof b, "}, \"num_configs\": %.17Lg, \"seconds\": %.6f}", ce->num_configs(), secs);
+            js << b;
+            std::cout << "\n" << js.str() << "\n";
+            delete ge;
+            delete ce;
+            delete oc;
             return 0;
         }
         ldo_ref_rng_configure(seed, rep, 0);

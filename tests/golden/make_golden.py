@@ -79,32 +79,29 @@ def flatten(chains):
 # exact enumerations: fixture name, case (the 4-domain system, whose staples
 # never bind both domains; the capped 8-domain system, where they do)
 ENUMERATIONS = [("c1_enumeration", "c1"), ("e8_enumeration", "e8")]
+# extra .inp options of an enumeration (defaults: the case's own)
+ENUM_OPTS = {}
 
 
 def enumerate_case(tmp, name, case):
     """Exact staple-only enumeration of a small system with the reference's
     enumerator (src/enumerate.cpp:687), weights over (numstaples,
-    numfulldomains)."""
+    numfulldomains) at full precision (oracle/ref/ref_trace.cpp's enumerate
+    mode runs enumerate_main's sequence and prints the normalised weights)."""
     base = os.path.join(tmp, name)
     opts = dict(simulation_type="enumerate", enumerate_staples_only="true",
                 ops_to_output="numstaples numfulldomains", output_filebase=base)
+    opts.update(ENUM_OPTS.get(name, {}))
     inp = systems.write_case(tmp, case, extra=opts)
     with open(inp, "a") as f:
         f.write("trace_mode=enumerate\n")
-    subprocess.run([REF, inp], capture_output=True, text=True, cwd=tmp, check=True)
-    weights = {}
-    with open(base + ".weights") as f:
-        tags = f.readline().split()
-        for line in f:
-            line = line.strip()
-            if not line:
-                continue
-            key, w = line.rsplit(" ", 1)
-            weights[" ".join(key.strip("()").split())] = float(w)
+    out = subprocess.run([REF, inp], capture_output=True, text=True, cwd=tmp, check=True).stdout
+    d = json.loads([x for x in out.splitlines() if x.startswith("@@")][-1][2:])
     path = os.path.join(HERE, name + ".json")
     with open(path, "w") as f:
-        json.dump({"case": case, "ops": tags, "weights": weights}, f, indent=1, sort_keys=True)
-    print(path, weights)
+        json.dump({"case": case, "ops": ["numstaples", "numfulldomains"], "options": ENUM_OPTS.get(name, {}),
+                   "weights": d["weights"], "num_configs": d["num_configs"]}, f, indent=1, sort_keys=True)
+    print(path, d["weights"], "%.1f s" % d["seconds"])
 
 
 # restarts from a frame of a reference-written trajectory (restart_traj_file /
