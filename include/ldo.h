@@ -258,6 +258,20 @@ ldo_status ldo_us_get_biases(ldo_engine* e, double* out, int n_windows, int grid
 /* Window held by each replica, and the grid length. */
 ldo_status ldo_us_get_windows(ldo_engine* e, int32_t* window_of_replica, int n, int* grid_len);
 
+/* enumerate_main with enumerate_staples_only (src/enumerate.cpp:19-81): the
+ * exact partition function of replica 0's system at its temperature over
+ * every staple configuration on the fixed scaffold, with min_total..max_total
+ * staples and at most max_type of a type (the .inp's min_total_staples,
+ * max_total_staples, max_type_staples), the reference's growth-point sets
+ * and overcount corrections.  The staple sets times growth-point sets are
+ * enumerated on the GPU in parallel.  weights[k1 * n2 + k2] receives the
+ * normalised weight of (op1, op2) = (k1, k2) (order parameter tags), the
+ * reference's .weights entries; num_configs its number of configurations.
+ * The system starts without staples and has no bias functions. */
+ldo_status ldo_enumerate(ldo_engine* e, int32_t min_total, int32_t max_total, int32_t max_type, const char* op1_tag,
+                         const char* op2_tag, int32_t n1, int32_t n2, double* weights, double* num_configs,
+                         int32_t* n_units, double* device_ms);
+
 /* No counterpart in the reference: the engine's autotuner of the MC kernel's
  * launch shape (the reference runs one replica per MPI process and has no
  * launch shape).  Times probe_sweeps sweeps of this engine's own batch for

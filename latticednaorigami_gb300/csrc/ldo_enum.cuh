@@ -1,0 +1,287 @@
+// Exact staple-only enumeration on the GPU (StapleConformationalEnumerator,
+// src/enumerate.cpp:666-811, with the base ConformationalEnumerator's
+// enumerate_domain / set_growthpoint_domains / set_bound_domain,
+// :378-550, and the overcount calculators, :83-159).
+//
+// The host lists the independent work units the reference walks through in
+// series -- each staple set (StapleEnumerator::recurse, :1103) times each
+// distinct growth-point set (GrowthpointEnumerator, :819-1067) -- and one
+// thread per unit runs the reference's conformational recursion on its own
+// replica state in shared memory, with the engine's set_domain_config /
+// unassign_domain (the same energies as the MC moves), and writes the
+// Boltzmann weight of every configuration into its own row of a histogram
+// over two order parameters.  The host adds the rows in unit order.
+//
+// Orientations: the staple-only recursion places an unbound staple domain
+// with the orientation (0, 0, 0) (:781-791), which the engine's orientation
+// indices cannot hold.  Such a domain is stored with index 0 and marked; a
+// domain that later binds to it takes the opposite index, so the reference's
+// test that paired orientations are opposite (-0 == 0) passes as it does
+// there.  Only misbound pairs can form at such a site (staple domains are
+// not complementary to each other), and misbound pairs are not read by the
+// stacking and twist terms, so no energy depends on the stand-in index.
+#pragma once
+#include "ldo_engine.cuh"
+#include "ldo_kernels.h"
+
+namespace ldo {
+
+template <class C>
+struct EnumWork {
+    int16_t stack[C::DCAP];       // m_domains
+    int sp;
+    long long pgp[C::DCAP];       // m_prev_growthpoint_ps
+    int npgp;
+    int16_t gp_of[C::DCAP];       // m_growthpoints
+    int16_t inv_gp[C::DCAP];      // m_inverse_growthpoints
+    uint8_t zero_ore[C::DCAP];    // orientation (0, 0, 0) in the reference
+    double E, mult, prefix;
+    double part, nconf, sumE;
+    double* row;                  // this unit's histogram row
+    int op1, op2, n1, n2;         // key order parameters and histogram shape
+    int overcount;                // 0 MaxTwoDomain, 1 MisbindingOnly
+    int bad;                      // a key outside the histogram
+};
+
+template <class C>
+struct Enumerator {
+    Rep<C>& R;
+    EnumWork<C>& W;
+
+    __device__ void push(int d) { W.stack[W.sp++] = (int16_t)d; }
+    __device__ int pop() { return W.stack[--W.sp]; }
+
+    __device__ double set(int d, V3 p, int o) {
+        W.zero_ore[d] = 0;
+        return R.set_domain_config(d, p, o);
+    }
+    __device__ double unset(int d) { return R.unassign_domain(d); }
+
+    // ConformationalEnumerator::calc_and_save_weights (:639)
+    __device__ __noinline__ void save() {
+        W.nconf += W.mult;
+        R.update_move_params();
+        double w = W.prefix * exp(-W.E) * W.mult;
+        W.part += w;
+        W.sumE += W.E * w;
+        int k1 = R.op[2 * W.op1], k2 = R.op[2 * W.op2];
+        if (k1 < 0 || k1 >= W.n1 || k2 < 0 || k2 >= W.n2) {
+            W.bad = 1;
+            return;
+        }
+        W.row[k1 * W.n2 + k2] += w;
+    }
+
+    // MaxTwoDomainOvercountCalculator::count_involved_staples (:131)
+    __device__ int involved(int d) {
+        if (R.scs[d] == 0) return 0;
+        int n = 1;
+        int x = d;
+        #pragma unroll 1
+        for (int guard = 0; guard < C::DCAP; ++guard) {
+            int nx = R.nxt[x] < 0 ? R.prv[x] : R.nxt[x];
+            if (nx < 0) break;
+            x = R.bnd[nx];
+            if (x < 0 || R.scs[x] == 0) break;
+            ++n;
+        }
+        return n;
+    }
+
+    // OvercountCalculator::calc_multiplier (:83, :112)
+    __device__ __noinline__ double overcount(int d, int other) {
+        if (W.overcount == 0) {
+            if (R.scs[d] == R.scs[other]) return 1.0;
+            double m = 1.0;
+            m /= (involved(d) + involved(other) + 1);
+            return m;
+        }
+        double m = 1.0;
+        #pragma unroll 1
+        for (int x = R.nxt[d]; x >= 0; x = R.nxt[x]) {
+            if (R.st[x] == BOUND) m += 1;
+            else if (R.st[x] == UNASSIGNED) return 1.0;
+        }
+        #pragma unroll 1
+        for (int x = R.prv[d]; x >= 0; x = R.prv[x]) {
+            if (R.st[x] == BOUND) m += 1;
+            else if (R.st[x] == UNASSIGNED) return 1.0;
+        }
+        return m;
+    }
+
+    // ConformationalEnumerator::create_staple_stack (:610)
+    __device__ __noinline__ void staple_stack(int d) {
+        push(d);
+        int cs = R.scs[d], len = R.clen[cs], di = R.sd[d];
+        #pragma unroll 1
+        for (int k = di + 1; k < len; ++k) {
+            int x = R.slot_of(cs, k);
+            push(x);
+            if (W.gp_of[x] >= 0) staple_stack(W.gp_of[x]);
+        }
+        #pragma unroll 1
+        for (int k = di - 1; k >= 0; --k) {
+            int x = R.slot_of(cs, k);
+            push(x);
+            if (W.gp_of[x] >= 0) staple_stack(W.gp_of[x]);
+        }
+    }
+
+    // StapleConformationalEnumerator::create_domains_stack (:793)
+    __device__ void domains_stack() {
+        W.sp = 0;
+        #pragma unroll 1
+        for (int d = 0; d < R.ns; ++d) {
+            if (W.gp_of[d] >= 0) {
+                W.inv_gp[W.gp_of[d]] = (int16_t)d;
+                staple_stack(W.gp_of[d]);
+            }
+        }
+        #pragma unroll 1
+        for (int a = 0, b = W.sp - 1; a < b; ++a, --b) {
+            int16_t t = W.stack[a];
+            W.stack[a] = W.stack[b];
+            W.stack[b] = t;
+        }
+    }
+
+    __device__ void next_from(int nd, V3 p) {
+        if (W.inv_gp[nd] >= 0) grow_off_scaffold(nd);
+        else enumerate_domain(nd, p);
+    }
+
+    // StapleConformationalEnumerator::grow_next_domain (:729)
+    __device__ __noinline__ void grow_next(int d, V3 p) {
+        if (W.sp != 0) next_from(pop(), p);
+        else save();
+        W.E += unset(d);
+    }
+
+    // StapleConformationalEnumerator::grow_off_scaffold (:754)
+    __device__ __noinline__ void grow_off_scaffold(int nd) {
+        int g = W.inv_gp[nd];
+        V3 p = R.pos(g);
+        W.E += set(nd, p, R.ore[g] ^ 1);
+        if (R.hdr.violated) {
+            R.hdr.violated = 0;
+            push(nd);
+        }
+        else {
+            if (W.sp != 0) {
+                next_from(pop(), p);
+                push(nd);
+            }
+            W.E += unset(nd);
+        }
+    }
+
+    // StapleConformationalEnumerator::set_unbound_domain (:781)
+    __device__ __noinline__ void set_unbound(int d, V3 p) {
+        W.E += set(d, p, 0);
+        W.zero_ore[d] = 1;
+        W.mult *= 6.0;
+        grow_next(d, p);
+        W.mult /= 6.0;
+    }
+
+    // ConformationalEnumerator::set_bound_domain (:499)
+    __device__ __noinline__ void set_bound(int d, V3 p) {
+        int occ = R.unbound_at(p);
+        int zero = W.zero_ore[occ];
+        W.E += set(d, p, R.ore[occ] ^ 1);
+        W.zero_ore[d] = (uint8_t)zero;
+        if (R.hdr.violated) {
+            R.hdr.violated = 0;
+            return;
+        }
+        double m = overcount(d, occ);
+        W.mult *= m;
+        grow_next(d, p);
+        W.mult /= m;
+    }
+
+    // ConformationalEnumerator::set_comp_growthpoint_domains (:451)
+    __device__ __noinline__ void set_comp_gp(int d, int bd, V3 p) {
+        #pragma unroll 1
+        for (int o = 0; o < 6; ++o) {
+            W.E += set(d, p, o);
+            W.E += set(bd, p, o ^ 1);
+            if (R.hdr.violated) {
+                R.hdr.violated = 0;
+                W.E += unset(d);
+                continue;
+            }
+            grow_next(bd, p);
+            W.E += unset(d);
+        }
+    }
+
+    // ConformationalEnumerator::set_mis_growthpoint_domains (:477)
+    __device__ __noinline__ void set_mis_gp(int d, int bd, V3 p) {
+        W.E += set(d, p, 0);
+        W.E += set(bd, p, 1);
+        W.mult *= 6.0;
+        grow_next(bd, p);
+        W.E += unset(d);
+        W.mult /= 6.0;
+    }
+
+    // ConformationalEnumerator::set_growthpoint_domains (:413)
+    __device__ __noinline__ void set_gp(int d, V3 p) {
+        bool terminal = false;
+        int f = R.nxt[d], b = R.prv[d];
+        if (f >= 0 && R.st[f] == UNASSIGNED) {
+            if (b >= 0) terminal = true;
+        }
+        else if (f >= 0) {
+            terminal = true;
+        }
+        if (terminal) W.pgp[W.npgp++] = p;
+        int bd = pop();
+        if (R.did[d] == -R.did[bd]) set_comp_gp(d, bd, p);
+        else set_mis_gp(d, bd, p);
+        push(bd);
+        if (terminal) --W.npgp;
+    }
+
+    // ConformationalEnumerator::enumerate_domain (:378)
+    __device__ __noinline__ void enumerate_domain(int d, V3 p_prev) {
+        #pragma unroll 1
+        for (int k = 0; k < 6 && !R.bad(); ++k) {
+            V3 p = add(p_prev, unit(k));
+            bool is_gp = W.gp_of[d] >= 0;
+            int occ = R.occupancy(p);
+            bool occupied = occ == UNBOUND;
+            bool bound = occ == BOUND || occ == MISBOUND;
+            if ((is_gp && occupied) || bound) continue;
+            if (is_gp) set_gp(d, p);
+            else if (occupied) set_bound(d, p);
+            else set_unbound(d, p);
+        }
+        push(d);
+    }
+
+    // StapleConformationalEnumerator::enumerate (:687)
+    __device__ void run() {
+        domains_stack();
+        if (W.sp == 0) {
+            save();
+            return;
+        }
+        int start = pop();
+        int g = W.inv_gp[start];
+        V3 p = R.pos(g);
+        W.E += set(start, p, R.ore[g] ^ 1);
+        if (W.sp != 0) {
+            int nd = pop();
+            next_from(nd, p);
+        }
+        else {
+            save();
+        }
+        if (R.st[start] != UNASSIGNED) W.E += unset(start);
+    }
+};
+
+} // namespace ldo

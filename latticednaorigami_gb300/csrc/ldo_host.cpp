@@ -395,6 +395,174 @@ vector<float> ldo_learn_init_params(uint32_t seed) {
     return p;
 }
 
+// Work units of the exact staple-only enumeration, in the order the reference
+// walks them: StapleEnumerator::enumerate / recurse (src/enumerate.cpp:1082,
+// :1103) over staple sets, and for each set GrowthpointEnumerator::enumerate
+// (:819) with the misbinding (:869-966) or no-misbinding (:968-1067) rules,
+// skipping growth-point sets enumerated before (growthpoints_repeated).  Each
+// unit is one call of the reference's conformational enumeration.
+struct EnumBuilder {
+    typedef std::pair<int, int> DRef;                  // (chain, domain); chain -1: scaffold
+    typedef std::tuple<int, int, int, int> GP;         // (staple identity, domain, old chain, old domain)
+    const vector<vector<int>>& ids;                    // identities of each chain type (0: scaffold)
+    int S;
+    bool misbinding;
+    size_t max_units;
+    vector<LdoEnumUnit> units;
+    vector<int> chains;                                // identity of the k-th added staple
+    std::map<int, vector<int>> id_to_idx;              // m_identity_to_indices
+    vector<std::pair<int, int>> staples;               // m_staples
+    vector<DRef> usd;                                  // misbinding: m_unbound_system_domains
+    vector<vector<DRef>> usd_nm;                       // no misbinding: per staple identity
+    std::map<DRef, DRef> gmap;                         // m_growthpoints
+    vector<GP> gp;                                     // m_growthpoints of the growth-point enumerator
+    vector<vector<GP>> enumerated;
+
+    EnumBuilder(const vector<vector<int>>& identities, bool mis, size_t cap)
+        : ids(identities), S((int)identities.size() - 1), misbinding(mis), max_units(cap) {
+        int ns = (int)ids[0].size();
+        for (int d = 0; d < ns; ++d) usd.push_back({-1, d});
+        // OrigamiSystem::initialize_complementary_associations (src/origami_system.cpp:630)
+        usd_nm.resize(S);
+        for (int t = 1; t <= S; ++t)
+            for (int di : ids[t]) {
+                auto it = std::find(ids[0].begin(), ids[0].end(), -di);
+                if (it != ids[0].end()) usd_nm[t - 1].push_back({-1, (int)(it - ids[0].begin())});
+            }
+    }
+
+    void emit() {
+        if (units.size() >= max_units) throw LdoError(LDO_EINVAL, "enumeration: too many growth-point sets");
+        if (gmap.size() > LDO_ENUM_MAX_STAPLES) throw LdoError(LDO_EINVAL, "enumeration: too many growth points");
+        LdoEnumUnit u {};
+        u.n_chains = (int)chains.size();
+        for (size_t k = 0; k < chains.size(); ++k) u.ident[k] = chains[k];
+        u.n_gp = 0;
+        for (auto& kv : gmap) {
+            u.gp_old_chain[u.n_gp] = kv.first.first;
+            u.gp_old_dom[u.n_gp] = kv.first.second;
+            u.gp_new_chain[u.n_gp] = kv.second.first;
+            u.gp_new_dom[u.n_gp] = kv.second.second;
+            ++u.n_gp;
+        }
+        units.push_back(u);
+    }
+
+    bool repeated() const {   // growthpoints_repeated (:944, :1046)
+        for (auto& e : enumerated) {
+            if (e.size() != gp.size()) continue;
+            bool all = true;
+            for (auto& g : e)
+                if (std::find(gp.begin(), gp.end(), g) == gp.end()) {
+                    all = false;
+                    break;
+                }
+            if (all) return true;
+        }
+        return false;
+    }
+
+    void recurse_or_enumerate(int ident, int d_i, DRef old) {
+        int L = (int)ids[ident].size();
+        gp.push_back(GP {ident, d_i, old.first < 0 ? -1 : old.first + 1, old.second});
+        // ConformationalEnumerator::add_growthpoint (:317)
+        int k = id_to_idx[ident].back();
+        id_to_idx[ident].pop_back();
+        gmap[old] = DRef {k, d_i};
+        if (!staples.empty()) {
+            if (misbinding) {
+                for (int d = 0; d < L; ++d)
+                    if (d != d_i) usd.push_back({k, d});
+            }
+            iterate_staple_identities();
+            if (misbinding)
+                for (int d = 0; d + 1 < L; ++d) usd.pop_back();
+        }
+        else if (!repeated()) {
+            emit();
+            enumerated.push_back(gp);
+        }
+        // remove_growthpoint (:336)
+        DRef nw = gmap[old];
+        gmap.erase(old);
+        id_to_idx[chains[nw.first]].push_back(nw.first);
+        gp.pop_back();
+    }
+
+    void iterate_domain_growthpoints(int ident) {
+        int L = (int)ids[ident].size();
+        vector<DRef>& lst = misbinding ? usd : usd_nm[ident - 1];
+        for (size_t j = 0; j != lst.size(); ++j) {
+            DRef old = lst[j];
+            lst.erase(lst.begin() + j);
+            for (int d_i = 0; d_i < L; ++d_i) {
+                if (!misbinding && ids[ident][d_i] != -ids[0][old.second]) continue;
+                recurse_or_enumerate(ident, d_i, old);
+            }
+            lst.insert(lst.begin() + j, old);
+        }
+    }
+
+    void iterate_staple_identities() {   // :834
+        for (size_t i = 0; i != staples.size(); ++i) {
+            int ident = staples[i].first;
+            int rem = staples[i].second - 1;
+            if (rem == 0) staples.erase(staples.begin() + i);
+            else staples[i] = {ident, rem};
+            iterate_domain_growthpoints(ident);
+            bool found = false;
+            for (auto& st : staples)
+                if (st.first == ident) {
+                    st.second++;
+                    found = true;
+                    break;
+                }
+            if (!found) staples.insert(staples.begin() + i, {ident, rem + 1});
+        }
+    }
+
+    void growthpoints() {   // GrowthpointEnumerator::enumerate (:819)
+        enumerated.clear();
+        staples.clear();
+        for (int t = 1; t <= S; ++t) {
+            int n = (int)std::count(chains.begin(), chains.end(), t);
+            if (n) staples.push_back({t, n});
+        }
+        iterate_staple_identities();
+    }
+
+    void recurse(int cur, int type_i, int cur_i, int cur_max, int max_type) {   // :1103
+        if (cur == cur_max) {
+            growthpoints();
+            return;
+        }
+        while (type_i != S + 1) {
+            if (cur_i < max_type) {
+                chains.push_back(type_i);
+                id_to_idx[type_i].push_back((int)chains.size() - 1);
+                recurse(cur + 1, type_i, cur_i + 1, cur_max, max_type);
+                id_to_idx[type_i].pop_back();
+                chains.pop_back();
+            }
+            type_i++;
+            cur_i = 0;
+        }
+    }
+
+    void run(int min_total, int max_total, int max_type) {   // :1082
+        if (max_total > LDO_ENUM_MAX_STAPLES) throw LdoError(LDO_EINVAL, "enumeration: at most 8 staples");
+        int cur_max;
+        if (min_total == 0) {
+            emit();
+            cur_max = 1;
+        }
+        else {
+            cur_max = min_total;
+        }
+        for (; cur_max <= max_total; ++cur_max) recurse(0, 1, 0, cur_max, max_type);
+    }
+};
+
 struct ldo_engine {
     string err;
     vector<HostSystem> systems;
@@ -2018,6 +2186,84 @@ struct ldo_engine {
         check_status();
     }
 
+    // Exact staple-only enumeration (enumerate_main with
+    // enumerate_staples_only, src/enumerate.cpp:19) of replica 0's system at
+    // its temperature: normalised weights over (op1, op2) into w[n1 * n2].
+    void enumerate(int min_total, int max_total, int max_type, int op1, int op2, int n1, int n2, double* w,
+                   double* num_configs, int* n_units, double* ms) {
+        const HostSystem& hs = systems[sys_of[0]];
+        if (hs.desc.n_biases != 0) throw LdoError(LDO_EINVAL, "enumeration: bias functions are not supported");
+        if (hs.desc.has_ct) throw LdoError(LDO_EINVAL, "enumeration: the scaffold must stay fixed");
+        if (op1 < 0 || op1 >= hs.desc.n_ops || op2 < 0 || op2 >= hs.desc.n_ops || n1 < 1 || n2 < 1)
+            throw LdoError(LDO_EINVAL, "enumeration: bad order parameters or histogram shape");
+        if (hs.sf.chains.size() != 1) throw LdoError(LDO_EINVAL, "enumeration: the system must start without staples");
+        LdoHdr h0 {};
+        CU(copy(&h0, d_arena.p + lay.o_hdr, sizeof h0, cudaMemcpyDeviceToHost));
+        if (h0.num_staples != 0 || h0.n_chains != 1)
+            throw LdoError(LDO_EINVAL, "enumeration: replica 0 must hold the scaffold only (enumerate before any run)");
+        int overcount;
+        if (hs.p.max_staple_size == 2) overcount = 0;
+        else if (hs.p.misbinding_pot == "Disallowed") overcount = 1;
+        else throw LdoError(LDO_EINVAL, "No enumerator available for system");
+        EnumBuilder b(hs.sf.identities, hs.p.misbinding_pot != "Disallowed", 1u << 22);
+        b.run(min_total, max_total, max_type);
+        int nu = (int)b.units.size();
+        DevBuf<LdoEnumUnit> d_units;
+        d_units.alloc(nu);
+        CU(copy(d_units.p, b.units.data(), nu * sizeof(LdoEnumUnit), cudaMemcpyHostToDevice));
+        size_t stride = ldo_enum_work_bytes(lay.cls);
+        DevBuf<unsigned char> d_work;
+        d_work.alloc((size_t)nu * stride);
+        DevBuf<double> d_hist, d_stats;
+        d_hist.alloc((size_t)nu * n1 * n2);
+        d_stats.alloc((size_t)nu * 4);
+        LdoEnumLaunch E {};
+        E.L = launch_params(LDO_MODE_RUN, 0);
+        E.state = d_arena.p;
+        E.units = d_units.p;
+        E.n_units = nu;
+        E.work = d_work.p;
+        E.work_stride = stride;
+        E.hist = d_hist.p;
+        E.stats = d_stats.p;
+        E.op1 = op1;
+        E.op2 = op2;
+        E.n1 = n1;
+        E.n2 = n2;
+        E.overcount = overcount;
+        // the recursion is deep: a larger per-thread stack for this launch
+        size_t old_stack = 0;
+        CU(cudaDeviceGetLimit(&old_stack, cudaLimitStackSize));
+        CU(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
+        CU(cudaEventRecord(ev0, stream));
+        cudaError_t err = ldo_launch_enum(E, stream);
+        if (err == cudaSuccess) err = cudaEventRecord(ev1, stream);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(stream);
+        cudaDeviceSetLimit(cudaLimitStackSize, old_stack);
+        CU(err);
+        if (ms) {
+            float f = 0;
+            CU(cudaEventElapsedTime(&f, ev0, ev1));
+            *ms = f;
+        }
+        vector<double> hist((size_t)nu * n1 * n2), stats((size_t)nu * 4);
+        CU(copy(hist.data(), d_hist.p, hist.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        CU(copy(stats.data(), d_stats.p, stats.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        double part = 0, nconf = 0;
+        for (int k = 0; k < n1 * n2; ++k) w[k] = 0;
+        for (int u = 0; u < nu; ++u) {
+            if (stats[4 * u + 3] < 0) throw LdoError(LDO_EINVAL, "enumeration: an order parameter value outside the histogram");
+            if (stats[4 * u + 3] > 0) throw LdoError((ldo_status)(int)stats[4 * u + 3], "enumeration: a unit failed");
+            part += stats[4 * u];
+            nconf += stats[4 * u + 1];
+            for (int k = 0; k < n1 * n2; ++k) w[k] += hist[(size_t)u * n1 * n2 + k];
+        }
+        // ConformationalEnumerator::normalize_weights (:344)
+        for (int k = 0; k < n1 * n2; ++k) w[k] /= part;
+        if (num_configs) *num_configs = nconf;
+        if (n_units) *n_units = nu;
+    }
+
     vector<unsigned char> download_arena() {
         vector<unsigned char> host((size_t)n_rep * lay.bytes);
         CU(copy(host.data(), d_arena.p, host.size(), cudaMemcpyDeviceToHost));
@@ -2092,6 +2338,25 @@ ldo_status ldo_run_sweeps(ldo_engine* e, int64_t n_sweeps, double* device_ms) {
 }
 
 int ldo_state_bytes(const ldo_engine* e) { return e ? e->lay.bytes : 0; }
+
+ldo_status ldo_enumerate(ldo_engine* e, int32_t min_total, int32_t max_total, int32_t max_type, const char* op1_tag,
+                         const char* op2_tag, int32_t n1, int32_t n2, double* weights, double* num_configs,
+                         int32_t* n_units, double* device_ms) {
+    if (!e || !op1_tag || !op2_tag || !weights || min_total < 0 || max_total < min_total || max_type < 1)
+        return LDO_EINVAL;
+    return guard(e, [&]() {
+        const HostSystem& hs = e->systems[e->sys_of[0]];
+        auto find = [&](const char* tag) {
+            for (size_t q = 0; q < hs.ops.size(); ++q)
+                if (hs.ops[q].tag == tag) return (int)q;
+            throw LdoError(LDO_EINVAL, string("enumeration: no order parameter ") + tag);
+        };
+        int nu = 0;
+        e->enumerate(min_total, max_total, max_type, find(op1_tag), find(op2_tag), n1, n2, weights, num_configs, &nu,
+                     device_ms);
+        if (n_units) *n_units = nu;
+    });
+}
 
 ldo_status ldo_autotune(ldo_engine* e, int32_t probe_sweeps, int32_t use_cache, ldo_tune_report* out) {
     if (!e || probe_sweeps < 1 || !out) return LDO_EINVAL;

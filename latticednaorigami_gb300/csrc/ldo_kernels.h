@@ -118,3 +118,34 @@ cudaError_t ldo_launch_pt_swap(const LdoPT& P, cudaStream_t stream);
 enum { LDO_NOALLOC_MAX_REPLICAS = 65536 };
 cudaError_t ldo_status_noalloc(const unsigned char* arena, int bytes, int o_hdr, int n_rep, cudaStream_t stream,
                                int* status_of_replica, int* worst, int* n_bad);
+
+// Exact staple-only enumeration (csrc/ldo_enum.cuh).  One work unit: the
+// staples added (identities in the reference's add order) and the
+// growth-point map (old domain -> new staple domain) as the reference's
+// m_growthpoints holds it when its conformational enumeration starts.  A
+// domain reference is (chain, domain index) with chain -1 for the scaffold
+// and k for the k-th added staple.
+#define LDO_ENUM_MAX_STAPLES 8
+struct LdoEnumUnit {
+    int n_chains;
+    int ident[LDO_ENUM_MAX_STAPLES];
+    int n_gp;
+    int gp_old_chain[LDO_ENUM_MAX_STAPLES];
+    int gp_old_dom[LDO_ENUM_MAX_STAPLES];
+    int gp_new_chain[LDO_ENUM_MAX_STAPLES];
+    int gp_new_dom[LDO_ENUM_MAX_STAPLES];
+};
+struct LdoEnumLaunch {
+    LdoLaunch L;                  // system, tables and controls of replica 0
+    const unsigned char* state;   // the replica's state with the scaffold placed and no staples
+    const LdoEnumUnit* units;
+    int n_units;
+    unsigned char* work;          // per unit: recursion state (ldo_enum_work_bytes)
+    size_t work_stride;
+    double* hist;                 // per unit: n1 x n2 weights over (op1, op2)
+    double* stats;                // per unit: partition sum, configurations, sum of E w, status
+    int op1, op2, n1, n2;
+    int overcount;                // 0 MaxTwoDomain, 1 MisbindingOnly
+};
+cudaError_t ldo_launch_enum(const LdoEnumLaunch& E, cudaStream_t stream);
+size_t ldo_enum_work_bytes(int cls);

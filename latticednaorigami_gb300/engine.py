@@ -25,7 +25,7 @@ EXPORTS = [
     "ldo_writer_open", "ldo_writer_write", "ldo_writer_close", "ldo_pt2d_run", "ldo_engine_exp",
     "ldo_set_bias_centre", "ldo_swap_writer_open", "ldo_set_config", "ldo_set_configs", "ldo_anneal_run", "ldo_read_trj_frame", "ldo_checkpoint_save",
     "ldo_checkpoint_load", "ldo_autotune", "ldo_autotune_candidates", "ldo_us_write_biases",
-    "ldo_us_read_biases", "ldo_us_reset", "ldo_read_biases",
+    "ldo_us_read_biases", "ldo_us_reset", "ldo_read_biases", "ldo_enumerate",
 ]
 
 LEARN_TABLE = 524544      # network inputs: 524288 insertion + 256 regrowth-direction (ldo_learn.h)
@@ -84,6 +84,9 @@ def load_library(path=None):
     lib.ldo_us_reset.argtypes = [vp]
     lib.ldo_read_biases.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int32), dp, ip,
                                     ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    lib.ldo_enumerate.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p,
+                                  ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, dp, dp,
+                                  ctypes.POINTER(ctypes.c_int32), dp]
     lib.ldo_autotune.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(TuneReport)]
     lib.ldo_autotune_candidates.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), dp, ctypes.c_int32]
     lib.ldo_get_observables.argtypes = [vp, ctypes.POINTER(Observables), ip]
@@ -186,6 +189,20 @@ class Engine:
 
     def state_bytes(self):
         return self.lib.ldo_state_bytes(self.h)
+
+    def enumerate(self, min_total, max_total, max_type, ops=("numstaples", "numfulldomains"), shape=(9, 49)):
+        """Exact staple-only enumeration on the GPU (ldo_enumerate): dict
+        "k1 k2" -> normalised weight, and a dict of counts and timing."""
+        w = np.zeros(shape[0] * shape[1])
+        nconf = ctypes.c_double(0)
+        nu = ctypes.c_int32(0)
+        ms = ctypes.c_double(0)
+        self._check(self.lib.ldo_enumerate(self.h, int(min_total), int(max_total), int(max_type), ops[0].encode(),
+                                           ops[1].encode(), shape[0], shape[1], _dptr(w), ctypes.byref(nconf),
+                                           ctypes.byref(nu), ctypes.byref(ms)))
+        w = w.reshape(shape)
+        out = {"%d %d" % (a, b): float(w[a, b]) for a in range(shape[0]) for b in range(shape[1]) if w[a, b] != 0}
+        return out, {"num_configs": nconf.value, "units": nu.value, "ms": ms.value}
 
     def autotune(self, probe_sweeps=4, use_cache=True):
         """The engine's autotuner (ldo_autotune): the fastest launch shape for
