@@ -78,9 +78,9 @@ def flatten(chains):
 
 # exact enumerations: fixture name, case (the 4-domain system, whose staples
 # never bind both domains; the capped 8-domain system, where they do)
-ENUMERATIONS = [("c1_enumeration", "c1"), ("e8_enumeration", "e8")]
+ENUMERATIONS = [("c1_enumeration", "c1"), ("e8_enumeration", "e8"), ("e8s3_enumeration", "e8")]
 # extra .inp options of an enumeration (defaults: the case's own)
-ENUM_OPTS = {}
+ENUM_OPTS = {"e8s3_enumeration": {"max_total_staples": 3}}
 
 
 def enumerate_case(tmp, name, case):

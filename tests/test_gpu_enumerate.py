@@ -15,7 +15,8 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("name,case,max_total,max_type", [("c1_enumeration", "c1", 4, 4),
-                                                          ("e8_enumeration", "e8", 2, 1)])
+                                                          ("e8_enumeration", "e8", 2, 1),
+                                                          ("e8s3_enumeration", "e8", 3, 1)])
 def test_enumeration_matches_reference(name, case, max_total, max_type, data_dir):
     from latticednaorigami_gb300 import Engine
     with open(os.path.join(GOLDEN, name + ".json")) as f:
