@@ -43,6 +43,19 @@ using ldo_refdrv::dump_config;
 using ldo_refdrv::fill_params;
 using ldo_refdrv::read_kv;
 
+// The staple-only enumerator with the partition-function increment of every
+// conformational enumeration (one growth-point set) recorded in order.
+class UnitStapleEnum : public enumerator::StapleConformationalEnumerator {
+  public:
+    using StapleConformationalEnumerator::StapleConformationalEnumerator;
+    void enumerate() override {
+        long double z0 = m_partition_f, n0 = m_num_configs;
+        StapleConformationalEnumerator::enumerate();
+        units.push_back({(double)(m_partition_f - z0), (double)(m_num_configs - n0)});
+    }
+    vector<std::pair<double, double>> units;
+};
+
 class TraceSim : public simulation::GCMCSimulation {
   public:
     TraceSim(origami::OrigamiSystem& o, orderParams::SystemOrderParams& ops,
@@ -140,8 +153,7 @@ int main(int argc, char** argv) {
             else throw std::runtime_error("No enumerator available for system");
             enumerator::ConformationalEnumerator* ce;
             if (params.m_enumerate_staples_only)
-                ce = new enumerator::StapleConformationalEnumerator {*o, *oc, ops, biases, params.m_ops_to_output,
-                                                                      params.m_apply_mean_field_cor};
+                ce = new UnitStapleEnum {*o, *oc, ops, biases, params.m_ops_to_output, params.m_apply_mean_field_cor};
             else
                 ce = new enumerator::ConformationalEnumerator {*o, *oc, ops, biases, params.m_ops_to_output,
                                                                params.m_apply_mean_field_cor};
@@ -168,8 +180,20 @@ int main(int argc, char** argv) {
                 first = false;
             }
             char b[128];
-            std::snprintf(b, sizeof b, "}, \"num_configs\": %.17Lg, \"seconds\": %.6f}", ce->num_configs(), secs);
+            std::snprintf(b, sizeof b, "}, \"num_configs\": %.17Lg, \"seconds\": %.6f", ce->num_configs(), secs);
             js << b;
+            // trace_units=1: the partition-function increment of every
+            // growth-point set, in enumeration order
+            if (kv.count("trace_units") && kv["trace_units"] == "1" && params.m_enumerate_staples_only) {
+                js << ", \"units\": [";
+                auto& us = static_cast<UnitStapleEnum*>(ce)->units;
+                for (size_t i = 0; i < us.size(); ++i) {
+                    std::snprintf(b, sizeof b, "%s[%.17g, %.17g]", i ? ", " : "", us[i].first, us[i].second);
+                    js << b;
+                }
+                js << "]";
+            }
+            js << "}";
             std::cout << "\n" << js.str() << "\n";
             delete ge;
             delete ce;
