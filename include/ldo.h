@@ -272,6 +272,12 @@ ldo_status ldo_enumerate(ldo_engine* e, int32_t min_total, int32_t max_total, in
                          const char* op2_tag, int32_t n1, int32_t n2, double* weights, double* num_configs,
                          int32_t* n_units, double* device_ms);
 
+/* The last ldo_enumerate's work units (the reference's growth-point sets, in
+ * its enumeration order): out[2u] the unit's partition-function sum before
+ * normalisation, out[2u+1] its number of configurations (NULL out: count
+ * only). */
+ldo_status ldo_enumerate_units(ldo_engine* e, double* out, int32_t cap, int32_t* n_units);
+
 /* No counterpart in the reference: the engine's autotuner of the MC kernel's
  * launch shape (the reference runs one replica per MPI process and has no
  * launch shape).  Times probe_sweeps sweeps of this engine's own batch for

@@ -2186,6 +2186,8 @@ struct ldo_engine {
         check_status();
     }
 
+    vector<double> enum_units;   // last enumeration: (partition sum, configurations) per unit
+
     // Exact staple-only enumeration (enumerate_main with
     // enumerate_staples_only, src/enumerate.cpp:19) of replica 0's system at
     // its temperature: normalised weights over (op1, op2) into w[n1 * n2].
@@ -2257,6 +2259,11 @@ struct ldo_engine {
             part += stats[4 * u];
             nconf += stats[4 * u + 1];
             for (int k = 0; k < n1 * n2; ++k) w[k] += hist[(size_t)u * n1 * n2 + k];
+        }
+        enum_units.assign(2 * (size_t)nu, 0.0);
+        for (int u = 0; u < nu; ++u) {
+            enum_units[2 * u] = stats[4 * u];
+            enum_units[2 * u + 1] = stats[4 * u + 1];
         }
         // ConformationalEnumerator::normalize_weights (:344)
         for (int k = 0; k < n1 * n2; ++k) w[k] /= part;
@@ -2356,6 +2363,16 @@ ldo_status ldo_enumerate(ldo_engine* e, int32_t min_total, int32_t max_total, in
                      device_ms);
         if (n_units) *n_units = nu;
     });
+}
+
+ldo_status ldo_enumerate_units(ldo_engine* e, double* out, int32_t cap, int32_t* n_units) {
+    if (!e || !n_units) return LDO_EINVAL;
+    int nu = (int)(e->enum_units.size() / 2);
+    *n_units = nu;
+    if (!out) return LDO_OK;
+    if (cap < nu) return LDO_EINVAL;
+    std::copy(e->enum_units.begin(), e->enum_units.end(), out);
+    return LDO_OK;
 }
 
 ldo_status ldo_autotune(ldo_engine* e, int32_t probe_sweeps, int32_t use_cache, ldo_tune_report* out) {

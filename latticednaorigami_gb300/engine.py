@@ -25,7 +25,7 @@ EXPORTS = [
     "ldo_writer_open", "ldo_writer_write", "ldo_writer_close", "ldo_pt2d_run", "ldo_engine_exp",
     "ldo_set_bias_centre", "ldo_swap_writer_open", "ldo_set_config", "ldo_set_configs", "ldo_anneal_run", "ldo_read_trj_frame", "ldo_checkpoint_save",
     "ldo_checkpoint_load", "ldo_autotune", "ldo_autotune_candidates", "ldo_us_write_biases",
-    "ldo_us_read_biases", "ldo_us_reset", "ldo_read_biases", "ldo_enumerate",
+    "ldo_us_read_biases", "ldo_us_reset", "ldo_read_biases", "ldo_enumerate", "ldo_enumerate_units",
 ]
 
 LEARN_TABLE = 524544      # network inputs: 524288 insertion + 256 regrowth-direction (ldo_learn.h)
@@ -87,6 +87,7 @@ def load_library(path=None):
     lib.ldo_enumerate.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p,
                                   ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, dp, dp,
                                   ctypes.POINTER(ctypes.c_int32), dp]
+    lib.ldo_enumerate_units.argtypes = [vp, dp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
     lib.ldo_autotune.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(TuneReport)]
     lib.ldo_autotune_candidates.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), dp, ctypes.c_int32]
     lib.ldo_get_observables.argtypes = [vp, ctypes.POINTER(Observables), ip]
@@ -203,6 +204,15 @@ class Engine:
         w = w.reshape(shape)
         out = {"%d %d" % (a, b): float(w[a, b]) for a in range(shape[0]) for b in range(shape[1]) if w[a, b] != 0}
         return out, {"num_configs": nconf.value, "units": nu.value, "ms": ms.value}
+
+    def enumerate_units(self):
+        """(partition sum, configurations) of every unit of the last
+        enumeration, in the reference's growth-point-set order."""
+        n = ctypes.c_int32(0)
+        self._check(self.lib.ldo_enumerate_units(self.h, None, 0, ctypes.byref(n)))
+        out = np.zeros(2 * n.value)
+        self._check(self.lib.ldo_enumerate_units(self.h, _dptr(out), n.value, ctypes.byref(n)))
+        return out.reshape(-1, 2)
 
     def autotune(self, probe_sweeps=4, use_cache=True):
         """The engine's autotuner (ldo_autotune): the fastest launch shape for

@@ -81,6 +81,8 @@ def flatten(chains):
 ENUMERATIONS = [("c1_enumeration", "c1"), ("e8_enumeration", "e8"), ("e8s3_enumeration", "e8")]
 # extra .inp options of an enumeration (defaults: the case's own)
 ENUM_OPTS = {"e8s3_enumeration": {"max_total_staples": 3}}
+# enumerations recorded with the partition sum of every growth-point set
+ENUM_UNITS = {"e8_enumeration"}
 
 
 def enumerate_case(tmp, name, case):
@@ -95,12 +97,15 @@ def enumerate_case(tmp, name, case):
     inp = systems.write_case(tmp, case, extra=opts)
     with open(inp, "a") as f:
         f.write("trace_mode=enumerate\n")
+        if name in ENUM_UNITS:
+            f.write("trace_units=1\n")
     out = subprocess.run([REF, inp], capture_output=True, text=True, cwd=tmp, check=True).stdout
     d = json.loads([x for x in out.splitlines() if x.startswith("@@")][-1][2:])
     path = os.path.join(HERE, name + ".json")
     with open(path, "w") as f:
         json.dump({"case": case, "ops": ["numstaples", "numfulldomains"], "options": ENUM_OPTS.get(name, {}),
-                   "weights": d["weights"], "num_configs": d["num_configs"]}, f, indent=1, sort_keys=True)
+                   "weights": d["weights"], "num_configs": d["num_configs"],
+                   **({"units": d["units"]} if "units" in d else {})}, f, sort_keys=True)
     print(path, d["weights"], "%.1f s" % d["seconds"])
 
 

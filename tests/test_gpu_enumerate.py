@@ -27,3 +27,18 @@ def test_enumeration_matches_reference(name, case, max_total, max_type, data_dir
     for k, v in fx["weights"].items():
         assert abs(w[k] - v) <= 1e-10 * v, (k, w[k], v)
     assert abs(info["num_configs"] - fx["num_configs"]) <= 1e-9 * fx["num_configs"]
+
+
+def test_enumeration_units_match_reference(data_dir):
+    """Unit by unit: the growth-point sets in the reference's order, each
+    with its partition-function sum and number of configurations."""
+    import numpy as np
+    from latticednaorigami_gb300 import Engine
+    with open(os.path.join(GOLDEN, "e8_enumeration.json")) as f:
+        fx = json.load(f)
+    eng = Engine(os.path.join(data_dir, "e8.inp"), n_replicas=1, seed=0)
+    eng.enumerate(0, 2, 1)
+    units = eng.enumerate_units()
+    ref = np.array(fx["units"])
+    assert units.shape == ref.shape
+    np.testing.assert_allclose(units, ref, rtol=1e-10, atol=0)
