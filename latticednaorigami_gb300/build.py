@@ -1,5 +1,5 @@
 """Compiles the engine's CUDA kernels and C++ host library into an in-tree
-shared library (libldo_gb300.so) for sm_103a.  No CMake: two compiler
+shared library (libldo_gb300.so) for sm_103a.  No CMake: the compiler
 invocations run in parallel, then one link."""
 import os
 import shutil
@@ -38,18 +38,21 @@ def build(verbose=False):
     nvcc = nvcc_path()
     k_obj = os.path.join(BUILD, "ldo_kernels.o")
     m_obj = os.path.join(BUILD, "ldo_mlp.o")
+    e_obj = os.path.join(BUILD, "ldo_enum.o")
     h_obj = os.path.join(BUILD, "ldo_host.o")
     cmds = [
         [nvcc] + ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-c", os.path.join(CSRC, "ldo_kernels.cu"), "-o", k_obj],
         [nvcc] + ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-c", os.path.join(CSRC, "ldo_mlp.cu"), "-o", m_obj],
+        [nvcc] + ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+                         "-c", os.path.join(CSRC, "ldo_enum.cu"), "-o", e_obj],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + cuda_include(),
          "-c", os.path.join(CSRC, "ldo_host.cpp"), "-o", h_obj],
     ]
     _run_all(cmds)
     tmp = LIB + ".tmp"
-    _run_all([[nvcc] + ARCH + ["-shared", "-Xcompiler", "-fPIC", k_obj, m_obj, h_obj, "-o", tmp]])
+    _run_all([[nvcc] + ARCH + ["-shared", "-Xcompiler", "-fPIC", k_obj, m_obj, e_obj, h_obj, "-o", tmp]])
     os.replace(tmp, LIB)
     if verbose:
         print("built", LIB)

@@ -169,7 +169,7 @@ struct Delta {
 // The engine's own exponential (ldo_math.h: the same bits as host code
 // computing it), one out-of-line copy to keep the hot code small (instruction
 // fetch, not arithmetic, limits this kernel).
-__device__ __noinline__ double dexp(double x) { return ldo_math::exp(x); }
+static __device__ __noinline__ double dexp(double x) { return ldo_math::exp(x); }
 
 struct Scratch {
     // MCMovetype reversal lists (include/.../movetypes.hpp:156-163)

@@ -1,0 +1,108 @@
+// Exact staple-only enumeration kernel (csrc/ldo_enum.cuh).  It lives in its
+// own translation unit: compiled beside the MC kernel, its calls into the
+// replica's methods changed the compiler's inlining there and grew the MC
+// kernel's code by a tenth (that kernel is bound by instruction fetch).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ldo_bind.cuh"
+#include "ldo_enum.cuh"
+
+namespace {
+
+template <class C>
+__host__ __device__ constexpr int enum_smem_bytes() { return (int)((sizeof(ldo::Rep<C>) + 15) / 16 * 16); }
+
+// One block per enumeration unit; its first lane runs the recursion on the
+// replica state in shared memory (the other lanes only copy it in).
+template <class C>
+__global__ void __launch_bounds__(32) ldo_enum_kernel(LdoEnumLaunch E) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    int u = blockIdx.x;
+    int lane = threadIdx.x;
+    if (u >= E.n_units) return;
+    warp_copy16(smem, E.state, (int)sizeof(LdoState<C>), lane);
+    __syncwarp();
+    if (lane != 0) return;
+    ldo::Rep<C>* R = reinterpret_cast<ldo::Rep<C>*>(smem);
+    bind_rep<C>(*R, E.L, 0);
+    auto* W = reinterpret_cast<ldo::EnumWork<C>*>(E.work + (size_t)u * E.work_stride);
+    const LdoEnumUnit& U = E.units[u];
+    for (int d = 0; d < C::DCAP; ++d) {
+        W->gp_of[d] = -1;
+        W->inv_gp[d] = -1;
+        W->zero_ore[d] = 0;
+    }
+    W->sp = 0;
+    W->npgp = 0;
+    W->E = 0;
+    W->mult = 1;
+    W->prefix = 1;
+    W->part = 0;
+    W->nconf = 0;
+    W->sumE = 0;
+    W->row = E.hist + (size_t)u * E.n1 * E.n2;
+    for (int k = 0; k < E.n1 * E.n2; ++k) W->row[k] = 0;
+    W->op1 = E.op1;
+    W->op2 = E.op2;
+    W->n1 = E.n1;
+    W->n2 = E.n2;
+    W->overcount = E.overcount;
+    W->bad = 0;
+    // ConformationalEnumerator::add_staple (src/enumerate.cpp:260)
+    int cs[LDO_ENUM_MAX_STAPLES];
+    for (int k = 0; k < U.n_chains; ++k) {
+        W->prefix *= R->c_staple_M;
+        cs[k] = R->add_chain(U.ident[k]);
+        if (R->mean_field) W->E += R->log6;
+        W->E += R->t_init_e;
+        int len = R->sys->type_len[U.ident[k]];
+        double six = 1;
+        for (int q = 0; q < 2 * len - 1; ++q) six *= 6.0;
+        W->prefix /= six;
+    }
+    if (!R->bad()) {
+        for (int g = 0; g < U.n_gp; ++g) {
+            int oc = U.gp_old_chain[g];
+            int old = oc < 0 ? U.gp_old_dom[g] : R->slot_of(cs[oc], U.gp_old_dom[g]);
+            W->gp_of[old] = (int16_t)R->slot_of(cs[U.gp_new_chain[g]], U.gp_new_dom[g]);
+        }
+        ldo::Enumerator<C> en {*R, *W};
+        en.run();
+    }
+    double* st = E.stats + 4 * (size_t)u;
+    st[0] = W->part;
+    st[1] = W->nconf;
+    st[2] = W->sumE;
+    st[3] = R->bad() ? (double)R->hdr.status : (W->bad ? -1.0 : 0.0);
+}
+
+} // namespace
+
+template <class C>
+static cudaError_t launch_enum_class(const LdoEnumLaunch& E, cudaStream_t stream) {
+    size_t smem = (size_t)enum_smem_bytes<C>();
+    cudaError_t err = cudaFuncSetAttribute(ldo_enum_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    if (E.n_units > 0) ldo_enum_kernel<C><<<E.n_units, 32, smem, stream>>>(E);
+    return cudaGetLastError();
+}
+
+cudaError_t ldo_launch_enum(const LdoEnumLaunch& E, cudaStream_t stream) {
+    switch (E.L.lay.cls) {
+    case LDO_CLASS_S: return launch_enum_class<LdoCapS>(E, stream);
+    case LDO_CLASS_M: return launch_enum_class<LdoCapM>(E, stream);
+    default: return launch_enum_class<LdoCapL>(E, stream);
+    }
+}
+
+size_t ldo_enum_work_bytes(int cls) {
+    size_t b;
+    switch (cls) {
+    case LDO_CLASS_S: b = sizeof(ldo::EnumWork<LdoCapS>); break;
+    case LDO_CLASS_M: b = sizeof(ldo::EnumWork<LdoCapM>); break;
+    default: b = sizeof(ldo::EnumWork<LdoCapL>); break;
+    }
+    return (b + 255) / 256 * 256;
+}
+

@@ -13,41 +13,10 @@
 #include <stdint.h>
 
 #include "ldo_engine.cuh"
-#include "ldo_enum.cuh"
 #include "ldo_kernels.h"
+#include "ldo_bind.cuh"
 
 namespace {
-
-__device__ __forceinline__ void warp_copy16(void* dst, const void* src, int bytes, int lane) {
-    uint4* d = reinterpret_cast<uint4*>(dst);
-    const uint4* s = reinterpret_cast<const uint4*>(src);
-    int n = bytes >> 4;
-    for (int k = lane; k < n; k += 32) d[k] = s[k];
-}
-
-template <class C>
-__device__ void bind_rep(ldo::Rep<C>& r, const LdoLaunch& L, int rep) {
-    r.ctl = L.ctl + rep;
-    r.sys = L.sys + r.ctl->sys;
-    r.bank = L.bank;
-    r.grid = L.grid;
-    r.learn_w = L.learn_w;
-    r.ct = L.ct_ws ? reinterpret_cast<LdoCtWork<C>*>(L.ct_ws + (size_t)rep * L.ct_stride) : nullptr;
-    r.bind_tables(L.tabs + r.ctl->tab);
-    r.imax = r.sys->imax;
-    r.dim = r.sys->dim;
-    r.c_staple_M = r.ctl->staple_M;
-    r.c_bias_mult = r.ctl->bias_mult;
-    r.ns = r.sys->ns;
-    r.lmax = r.sys->lmax;
-    r.nmv = r.sys->n_moves;
-    r.cyclic = r.sys->cyclic;
-    r.tqt = r.sys->tqt;
-    r.mean_field = r.sys->mean_field;
-    r.log6 = log(6.0);
-    r.log3 = log(3.0);
-    r.rng.init(r.ctl->seed, r.ctl->rep, 0u, r.hdr.draws);
-}
 
 template <class C>
 __host__ __device__ constexpr int rep_bytes() { return (int)((sizeof(ldo::Rep<C>) + 15) / 16 * 16); }
@@ -211,70 +180,6 @@ __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
     warp_copy16(gbase, base, (int)sizeof(LdoState<C>), lane);
 }
 
-// One block per enumeration unit; its first lane runs the recursion on the
-// replica state in shared memory (the other lanes only copy it in).
-template <class C>
-__global__ void __launch_bounds__(32) ldo_enum_kernel(LdoEnumLaunch E) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    int u = blockIdx.x;
-    int lane = threadIdx.x;
-    if (u >= E.n_units) return;
-    warp_copy16(smem, E.state, (int)sizeof(LdoState<C>), lane);
-    __syncwarp();
-    if (lane != 0) return;
-    ldo::Rep<C>* R = reinterpret_cast<ldo::Rep<C>*>(smem);
-    bind_rep<C>(*R, E.L, 0);
-    auto* W = reinterpret_cast<ldo::EnumWork<C>*>(E.work + (size_t)u * E.work_stride);
-    const LdoEnumUnit& U = E.units[u];
-    for (int d = 0; d < C::DCAP; ++d) {
-        W->gp_of[d] = -1;
-        W->inv_gp[d] = -1;
-        W->zero_ore[d] = 0;
-    }
-    W->sp = 0;
-    W->npgp = 0;
-    W->E = 0;
-    W->mult = 1;
-    W->prefix = 1;
-    W->part = 0;
-    W->nconf = 0;
-    W->sumE = 0;
-    W->row = E.hist + (size_t)u * E.n1 * E.n2;
-    for (int k = 0; k < E.n1 * E.n2; ++k) W->row[k] = 0;
-    W->op1 = E.op1;
-    W->op2 = E.op2;
-    W->n1 = E.n1;
-    W->n2 = E.n2;
-    W->overcount = E.overcount;
-    W->bad = 0;
-    // ConformationalEnumerator::add_staple (src/enumerate.cpp:260)
-    int cs[LDO_ENUM_MAX_STAPLES];
-    for (int k = 0; k < U.n_chains; ++k) {
-        W->prefix *= R->c_staple_M;
-        cs[k] = R->add_chain(U.ident[k]);
-        if (R->mean_field) W->E += R->log6;
-        W->E += R->t_init_e;
-        int len = R->sys->type_len[U.ident[k]];
-        double six = 1;
-        for (int q = 0; q < 2 * len - 1; ++q) six *= 6.0;
-        W->prefix /= six;
-    }
-    if (!R->bad()) {
-        for (int g = 0; g < U.n_gp; ++g) {
-            int oc = U.gp_old_chain[g];
-            int old = oc < 0 ? U.gp_old_dom[g] : R->slot_of(cs[oc], U.gp_old_dom[g]);
-            W->gp_of[old] = (int16_t)R->slot_of(cs[U.gp_new_chain[g]], U.gp_new_dom[g]);
-        }
-        ldo::Enumerator<C> en {*R, *W};
-        en.run();
-    }
-    double* st = E.stats + 4 * (size_t)u;
-    st[0] = W->part;
-    st[1] = W->nconf;
-    st[2] = W->sumE;
-    st[3] = R->bad() ? (double)R->hdr.status : (W->bad ? -1.0 : 0.0);
-}
-
 __global__ void ldo_status_kernel(const unsigned char* arena, int bytes, int o_hdr, int n_rep, int* out) {
     int rep = blockIdx.x * blockDim.x + threadIdx.x;
     if (rep >= n_rep) return;
@@ -405,33 +310,6 @@ cudaError_t ldo_mc_occupancy(int cls, int ct, int wpb, size_t smem, int* blocks)
     default:
         return ct ? occupancy_variant<LdoCapL, true>(wpb, smem, blocks) : occupancy_variant<LdoCapL, false>(wpb, smem, blocks);
     }
-}
-
-template <class C>
-static cudaError_t launch_enum_class(const LdoEnumLaunch& E, cudaStream_t stream) {
-    size_t smem = (size_t)warp_bytes<C>();
-    cudaError_t err = cudaFuncSetAttribute(ldo_enum_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (err != cudaSuccess) return err;
-    if (E.n_units > 0) ldo_enum_kernel<C><<<E.n_units, 32, smem, stream>>>(E);
-    return cudaGetLastError();
-}
-
-cudaError_t ldo_launch_enum(const LdoEnumLaunch& E, cudaStream_t stream) {
-    switch (E.L.lay.cls) {
-    case LDO_CLASS_S: return launch_enum_class<LdoCapS>(E, stream);
-    case LDO_CLASS_M: return launch_enum_class<LdoCapM>(E, stream);
-    default: return launch_enum_class<LdoCapL>(E, stream);
-    }
-}
-
-size_t ldo_enum_work_bytes(int cls) {
-    size_t b;
-    switch (cls) {
-    case LDO_CLASS_S: b = sizeof(ldo::EnumWork<LdoCapS>); break;
-    case LDO_CLASS_M: b = sizeof(ldo::EnumWork<LdoCapM>); break;
-    default: b = sizeof(ldo::EnumWork<LdoCapL>); break;
-    }
-    return (b + 255) / 256 * 256;
 }
 
 int ldo_warp_smem_bytes(int cls) {
