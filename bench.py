@@ -73,6 +73,23 @@ def write_c2(d):
     return files
 
 
+class nvtx_range:
+    """An NVTX push/pop range around a timed region, so that a profiler can
+    select exactly its launches (`ncu --nvtx --nvtx-include "<name>/"`)."""
+
+    def __init__(self, name):
+        self.name = name
+
+    def __enter__(self):
+        import torch
+        torch.cuda.nvtx.range_push(self.name)
+
+    def __exit__(self, *exc):
+        import torch
+        torch.cuda.nvtx.range_pop()
+        return False
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -195,9 +212,13 @@ def host_cores():
 # (oracle/touch_counts.py: 16 bytes per domain-record access, 8 per
 # occupancy-map operation, after burn-in, both movesets):
 B_ATTEMPT = {"plain": 8599.0, "learned": 12202.0}
+# the same count on the c3 system (python oracle/touch_counts.py c3: two
+# constant-temperature replicas at every ninth of the 64 temperatures)
+B_ATTEMPT_C3 = {"plain": 7867.0, "learned": 12279.0}
 SMEM_BYTES_PER_CLK_PER_SM = 128
 N_SM = 152
-KERNEL_SOURCES = ["ldo_engine.cuh", "ldo_kernels.cu", "ldo_types.h", "ldo_ct.h", "ldo_math.h", "ldo_learn.h"]
+KERNEL_SOURCES = ["ldo_engine.cuh", "ldo_kernels.cu", "ldo_kernels.h", "ldo_bind.cuh", "ldo_types.h",
+                  "ldo_ct.h", "ldo_math.h", "ldo_learn.h"]
 
 
 def kernel_source_sha():
@@ -428,7 +449,9 @@ def run_c4(args, impl):
     eng.set_sampling(1, total)
     clocks = ClockSampler()
     clocks.start()
+    n0 = eng.counters()[0]
     dev_ms = [eng.run_sweeps(C4_SWEEPS_PER_STEP) for _ in range(args.steps)]
+    launches = eng.counters()[0] - n0
     clk = clocks.stop()
     t_dev = sum(dev_ms) / 1000.0
     smp, cnt = eng.samples()
@@ -443,6 +466,7 @@ def run_c4(args, impl):
     for _ in range(args.warmup):
         eng2.run_sweeps(C4_SWEEPS_PER_STEP)
     series = [[] for _ in range(n)]
+    c0 = eng2.counters()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         eng2.set_controls(temps=temps)
@@ -452,6 +476,7 @@ def run_c4(args, impl):
         for r in range(n):
             series[r].append(s2[r, :c2[r], 0])
     t_e2e = time.perf_counter() - t0
+    c1 = eng2.counters()
     e2e_ess, _ = effective_samples([np.concatenate(x) for x in series])
     lay_bytes = eng.state_bytes()
     alg_bytes = n * lay_bytes * 2 + n * C4_SWEEPS_PER_STEP * 4
@@ -470,8 +495,9 @@ def run_c4(args, impl):
                                                 for t in range(C4_TEMPS)],
             "move_stats": stats.tolist(),
             "e2e": {"value": e2e_ess / t_e2e, "unit": "effective samples/s",
-                    "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * C4_SWEEPS_PER_STEP * 4},
-            "gpu_launches": 2 * args.steps,   # per step: the MC kernel and the status fold
+                    "h2d_bytes_per_step": (c1[1] - c0[1]) / args.steps, "d2h_bytes_per_step": (c1[2] - c0[2]) / args.steps,
+                    "gpu_launches_per_step": (c1[0] - c0[0]) / args.steps},
+            "gpu_launches": launches,   # counted by the engine: per step the MC kernel and the status fold
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind},
             "clocks": clk}
@@ -531,6 +557,14 @@ def read_swp_rows(path, rounds):
         lines = [x.split() for x in f.read().splitlines()]
     rows = [[int(v) for v in x] for x in lines[1:] if x]
     return rows[:rounds]
+
+
+def kl_noise(p_counts, q_counts, ess_p, ess_q):
+    """Expected plug-in KL of two samples of one distribution: (k - 1) / 2 x
+    (1/N_p + 1/N_q), k occupied bins, N the effective sample counts (the
+    first-order bias of the plug-in estimator)."""
+    k = int(np.count_nonzero(np.asarray(p_counts) + np.asarray(q_counts)))
+    return 0.5 * max(k - 1, 0) * (1.0 / max(ess_p, 1e-9) + 1.0 / max(ess_q, 1e-9))
 
 
 def kl_divergence(p_counts, q_counts, eps=1e-9):
@@ -624,10 +658,12 @@ def run_c3(args, impl):
         clocks = ClockSampler()
         clocks.start()
         dev_ms = []
+        n0 = eng.counters()[0]
         for _ in range(args.steps):
             dev_ms.append(eng.pt_run(C3_RUNGS, C3_ROUNDS_PER_STEP, C3_INTERVAL, 3))
             for w in writers:
                 w.write(-1)
+        launches = eng.counters()[0] - n0
         clk = clocks.stop()
         for w in writers:
             w.close()
@@ -646,7 +682,12 @@ def run_c3(args, impl):
         taus = [tau_int(series[k]) for k in keys]
         st = eng.move_stats(3)
         att, acc = eng.pt_stats(C3_RUNGS - 1)
+        ess_by_rung = np.zeros(C3_RUNGS)
+        for (l, q), e_ in zip(keys, ess):
+            ess_by_rung[q] += e_
         res = {"value": float(ess.sum()) / t, "ci95": [lo / t, hi / t], "boot": boot / t,
+               "ess_by_rung": ess_by_rung, "dev_ms": dev_ms, "attempts": float(st[:, 0].sum()),
+               "launches": launches,
                "sweeps_per_s": n * rounds * C3_INTERVAL / 48.0 / t,
                "ms_per_step": float(np.mean(dev_ms)), "tau_int_median_samples": float(np.median([x for x in taus if x])),
                "mean_fully_bound_by_temperature": [float(hist[q] @ np.arange(49) / hist[q].sum()) for q in
@@ -665,10 +706,73 @@ def run_c3(args, impl):
         eng.close()
         return res, hist
 
+    def e2e_arm(overrides, tab, seed):
+        """The learned arm end to end through the C ABI with host buffers:
+        inside the timed region the start configurations are uploaded from
+        host memory, then every step runs its rounds and reads back that
+        step's samples and slot permutations (the .swp rows)."""
+        eng = Engine(inp, n_replicas=n, seed=seed, overrides=overrides)
+        eng.learn_set_table(tab)
+        eng.autotune(probe_sweeps=2)   # the timed arm's shape (cached)
+        writers = [eng.open_swap_writer(C3_RUNGS, 3, l, os.path.join(tmp, "%d_e2e%d" % (seed, l)), C3_INTERVAL)
+                   for l in range(C3_LADDERS)]
+        per = C3_INTERVAL // C3_SAMPLE
+        flat = [np.asarray(c, np.int32) for c in start]
+        parts = []
+        c0 = eng.counters()
+        t0 = time.perf_counter()
+        eng.set_configs(flat)
+        for _ in range(args.steps):
+            eng.set_sampling(C3_SAMPLE, C3_ROUNDS_PER_STEP * per)
+            eng.pt_run(C3_RUNGS, C3_ROUNDS_PER_STEP, C3_INTERVAL, 3)
+            s_, c_ = eng.samples()
+            for w in writers:
+                w.write(-1)
+            parts.append(s_)
+        t = time.perf_counter() - t0
+        c1 = eng.counters()
+        for w in writers:
+            w.close()
+        eng.close()
+        smp = np.concatenate(parts, axis=1)
+        rows = [read_swp_rows(os.path.join(tmp, "%d_e2e%d.swp" % (seed, l)), rounds) for l in range(C3_LADDERS)]
+        series = c3_slot_series(smp, rows, rounds)
+        ess = replica_ess([series[k] for k in sorted(series)])
+        return {"value": float(ess.sum()) / t, "unit": "effective samples/s",
+                "h2d_bytes_per_step": (c1[1] - c0[1]) / args.steps, "d2h_bytes_per_step": (c1[2] - c0[2]) / args.steps,
+                "gpu_launches_per_step": (c1[0] - c0[0]) / args.steps,
+                "note": "start configurations uploaded once inside the timed region (bytes spread over the steps); "
+                        "bytes and launches counted by the engine"}
+
     plain, h_plain = arm("", None, 0)
     learned, h_learned = arm(learned_over, table, 1)
+    e2e = e2e_arm(learned_over, table, 2)
     kl = [kl_divergence(h_plain[q], h_learned[q]) for q in range(C3_RUNGS)]
+    noise = [kl_noise(h_plain[q], h_learned[q], plain["ess_by_rung"][q], learned["ess_by_rung"][q])
+             for q in range(C3_RUNGS)]
+    q_max = int(np.argmax(kl))
     ratio_boot = learned.pop("boot") / plain.pop("boot")
+
+    def roofline(res, kind):
+        # shared-memory roofline as for c2: algorithmic bytes per attempt
+        # (oracle touch counts on this system) x attempts per launch
+        t_launch = float(np.mean(res["dev_ms"])) / 1000.0 / C3_ROUNDS_PER_STEP
+        att = res["attempts"] / (rounds + args.warmup * C3_ROUNDS_PER_STEP)
+        sm_mhz = res["clocks"].get("sm_mhz") or 2070.0
+        peak = N_SM * SMEM_BYTES_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e9
+        achieved = att * B_ATTEMPT_C3[kind] / t_launch / 1e9
+        return {"bound": "smem", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_kind": "derived: 152 SMs x 128 B/clk x median SM clock %.0f MHz" % sm_mhz,
+                "bytes_per_attempt": B_ATTEMPT_C3[kind], "attempts_per_launch": att,
+                "launch": "one round: 1000 steps of every replica (then the exchange kernel)",
+                "traffic": None, "traffic_source": "no capture of this workload"}
+
+    for res in (plain, learned):
+        res["roofline"] = roofline(res, "learned" if res is learned else "plain")
+        res.pop("dev_ms")
+        res.pop("attempts")
+        res["gpu_launches"] = res.pop("launches")
+        res["ess_by_rung"] = [float(x) for x in res["ess_by_rung"]]
 
     # constant-temperature references at the top temperature: from the empty
     # scaffold and from the burn-in's lowest-temperature configurations
@@ -699,13 +803,22 @@ def run_c3(args, impl):
             "learned_over_plain": value / plain["value"],
             "learned_over_plain_ci95": [float(np.quantile(ratio_boot, 0.025)), float(np.quantile(ratio_boot, 0.975))],
             "kl_plain_learned_by_temperature": {"max": max(kl), "mean": float(np.mean(kl)),
-                                                "top": kl[-1], "bottom": kl[0]},
+                                                "top": kl[-1], "bottom": kl[0], "argmax_K": C3_TEMPS[q_max],
+                                                "sampling_noise_at_argmax": noise[q_max],
+                                                "max_excess_over_noise": float(max(k - z for k, z in zip(kl, noise))),
+                                                "noise": "(occupied bins - 1)/2 x (1/ESS_plain + 1/ESS_learned) "
+                                                         "per temperature"},
             "stationarity": {"top_rung_370K_plain": plain["mean_fully_bound_by_temperature"][-1],
                              "top_rung_370K_learned": learned["mean_fully_bound_by_temperature"][-1],
                              "constant_T_370K_from_empty": ref_empty,
                              "constant_T_370K_from_assembled": ref_assembled},
             "network": {"train_iters": LEARN_ITERS, "loss_first": loss0, "loss_last": loss1, "train_s": train_s},
-            "burn_in_s": burn_s, "gpu_launches": None}
+            "burn_in_s": burn_s, "roofline": learned["roofline"], "e2e": e2e,
+            # counted by the engine: per step C3_ROUNDS_PER_STEP rounds of the MC
+            # kernel and the exchange kernel (graph replays), and the status fold
+            "gpu_launches": learned["gpu_launches"]}
+    if not args.no_cpu:
+        line["cpu_baseline"] = c3_cpu(inp, min(rounds, 500))
     print(json.dumps(line))
 
 
@@ -829,10 +942,10 @@ def main():
 
     start, train = relax()
 
-    def timed_arm(overrides, table):
+    def timed_arm(overrides, table, label):
         """From the relaxed configurations: W warm-up launches, then K timed
         launches of SWEEPS_PER_STEP sweeps with one numfulldomains sample per
-        replica per sweep."""
+        replica per sweep (inside the NVTX range "<label>_timed")."""
         eng = Engine(files, n_replicas=N_REP, seed=ranks.rank, sys_of_replica=sys_of.tolist(), overrides=overrides)
         eng.set_controls(temps=temps)
         if table is not None:
@@ -850,7 +963,10 @@ def main():
         clocks = ClockSampler()
         clocks.start()
         ranks.barrier()
-        dev_ms = [eng.run_sweeps(SWEEPS_PER_STEP) for _ in range(args.steps)]   # each call ends synchronised
+        n0 = eng.counters()[0]
+        with nvtx_range(label + "_timed"):
+            dev_ms = [eng.run_sweeps(SWEEPS_PER_STEP) for _ in range(args.steps)]   # each call ends synchronised
+        launches = eng.counters()[0] - n0
         ranks.barrier()
         clk = clocks.stop()
         t_dev = ranks.max(sum(dev_ms) / 1000.0)
@@ -872,7 +988,7 @@ def main():
         acc = [float(st[k, 1]) / max(1.0, float(st[k, 0])) for k in range(3)]
         return {"eng": eng, "dev_ms": dev_ms, "t_dev": t_dev, "ess": ess, "boot": boot / t_dev,
                 "ci95": [lo / t_dev, hi / t_dev], "tau_med": tau_med, "taus": taus, "tau_vs_length_24": tvl,
-                "means": means, "clk": clk, "acc": acc, "tune": tune}
+                "means": means, "clk": clk, "acc": acc, "tune": tune, "launches": launches}
 
     def e2e_arm(overrides, table):
         """The same loop through the C ABI with host buffers: temperatures in,
@@ -889,6 +1005,7 @@ def main():
             eng2.run_sweeps(SWEEPS_PER_STEP)
         e2e_series = [[] for _ in range(N_REP)]
         ranks.barrier()
+        c0 = eng2.counters()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             eng2.set_controls(temps=temps)
@@ -898,22 +1015,26 @@ def main():
             for r in range(N_REP):
                 e2e_series[r].append(s2[r, :c2[r], 0])
         t_e2e = time.perf_counter() - t0
+        c1 = eng2.counters()
         ranks.barrier()
         t_e2e = ranks.max(t_e2e)
         e2e_ess, _ = effective_samples([np.concatenate(x) for x in e2e_series])
         eng2.close()
-        return ranks.sum(e2e_ess) / t_e2e
+        return ranks.sum(e2e_ess) / t_e2e, [(b - a) / args.steps for a, b in zip(c0, c1)]
 
     table = train["table"]
-    plain = timed_arm("", None)
-    learned = timed_arm(learned_over, table)
+    plain = timed_arm("", None, "plain")
+    learned = timed_arm(learned_over, table, "learned")
     value = learned["ess"] / learned["t_dev"]
     plain_value = plain["ess"] / plain["t_dev"]
     ratio_boot = learned["boot"] / plain["boot"]
-    e2e_learned = e2e_arm(learned_over, table)
-    e2e_plain = e2e_arm("", None)
-    h2d = N_REP * 8
-    d2h = N_REP * SWEEPS_PER_STEP * 2 * 2
+    e2e_learned, e2e_counts = e2e_arm(learned_over, table)
+    e2e_plain, _ = e2e_arm("", None)
+    # per step, counted by the engine: the temperature upload (control
+    # records and the energy tables of the replicas' temperatures), the
+    # recompute and MC launches with their status folds, and the samples
+    # read back with their counts
+    e2e_launches, h2d, d2h = e2e_counts
 
     # Roofline of the MC kernel: shared memory (the replica state stays in it
     # for a whole launch).  achieved = move attempts per launch x algorithmic
@@ -988,8 +1109,8 @@ def main():
                         "train_s": tr["train_s"]},
             "sweeps_per_s": lrates["sweeps_per_s"],
             "e2e": {"value": e2e_learned, "unit": "effective samples/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "plain_value": e2e_plain},
-            "gpu_launches": 2 * args.steps,   # per step: the MC kernel and the status fold
+                    "d2h_bytes_per_step": d2h, "plain_value": e2e_plain, "gpu_launches_per_step": e2e_launches},
+            "gpu_launches": learned["launches"],   # counted by the engine: per step the MC kernel and the status fold
             "roofline": rl,
             "clocks": learned["clk"], "clocks_plain": plain["clk"]}
     if not args.no_cpu and rank == 0:

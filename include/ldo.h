@@ -167,6 +167,13 @@ ldo_status ldo_set_sampling(ldo_engine* e, int interval, int capacity);
 /* Copies samples[replica][k][2] (int16) for the first min(count, capacity). */
 ldo_status ldo_get_samples(ldo_engine* e, int16_t* out, int capacity, int* count);
 
+/* Work counters since the engine was created (no reference counterpart: the
+ * end-to-end accounting of a caller): kernel launches of the MC, exchange,
+ * status and enumeration kernels (a replayed CUDA graph counts the kernels
+ * it holds; network training is not counted), and bytes copied host to
+ * device and device to host.  Any pointer may be NULL. */
+ldo_status ldo_get_counters(ldo_engine* e, int64_t* launches, int64_t* h2d_bytes, int64_t* d2h_bytes);
+
 /* Step trace for replicas [0, n_trace): per step 8 doubles (step, energy,
  * staples, fully bound, bound, stacked, total bias, draws). */
 ldo_status ldo_set_trace(ldo_engine* e, int n_trace, int max_steps);

@@ -581,9 +581,27 @@ struct ldo_engine {
     // return before its transfer has finished.
     cudaError_t copy(void* dst, const void* src, size_t n, cudaMemcpyKind kind) {
         if (n == 0) return cudaSuccess;
+        count_copy(n, kind);
         cudaError_t err = cudaMemcpyAsync(dst, src, n, kind, stream);
         if (err != cudaSuccess) return err;
         return cudaStreamSynchronize(stream);
+    }
+
+    // Counters of the engine's own work (ldo_get_counters): kernel launches
+    // (the MC, exchange, status and enumeration kernels; a replayed graph
+    // counts its kernels) and bytes copied between host and device.
+    long long n_launches {0}, bytes_h2d {0}, bytes_d2h {0};
+    bool capturing {false};
+    void count_copy(size_t n, cudaMemcpyKind kind) {
+        if (kind == cudaMemcpyHostToDevice) bytes_h2d += (long long)n;
+        else if (kind == cudaMemcpyDeviceToHost) bytes_d2h += (long long)n;
+    }
+    void count_launch(int k = 1) {
+        if (!capturing) n_launches += k;
+    }
+    cudaError_t launch_mc(const LdoLaunch& L) {
+        count_launch();
+        return ldo_launch_mc(L, stream);
     }
 
     vector<LdoSys> h_sys;
@@ -783,7 +801,7 @@ struct ldo_engine {
         L.sample_interval = 0;
         L.n_trace = 0;
         CU(cudaEventRecord(ev0, stream));
-        CU(ldo_launch_mc(L, stream));
+        CU(launch_mc(L));
         CU(cudaEventRecord(ev1, stream));
         CU(cudaStreamSynchronize(stream));
         float f = 0;
@@ -892,8 +910,10 @@ struct ldo_engine {
 
     void check_status() {
         CU(cudaMemsetAsync(d_status.p, 0, sizeof(int), stream));
+        count_launch();
         CU(ldo_launch_status(d_arena.p, lay.bytes, lay.o_hdr, n_rep, d_status.p, stream));
         int st = 0;
+        count_copy(sizeof(int), cudaMemcpyDeviceToHost);
         CU(cudaMemcpyAsync(&st, d_status.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
         CU(cudaStreamSynchronize(stream));
         if (st != 0) {
@@ -1112,7 +1132,7 @@ struct ldo_engine {
             CU(cudaMemsetAsync(d_cnt_t.p, 0, LDO_LEARN_TABLE * sizeof(float), stream));
         }
         LdoLaunch L = launch_params(LDO_MODE_INIT, 0);
-        CU(ldo_launch_mc(L, stream));
+        CU(launch_mc(L));
         CU(cudaStreamSynchronize(stream));
         check_status();
     }
@@ -1121,7 +1141,7 @@ struct ldo_engine {
         LdoLaunch L = launch_params(LDO_MODE_RUN, steps);
         L.sweep_units = sweeps;
         CU(cudaEventRecord(ev0, stream));
-        CU(ldo_launch_mc(L, stream));
+        CU(launch_mc(L));
         CU(cudaEventRecord(ev1, stream));
         CU(cudaStreamSynchronize(stream));
         if (ms) {
@@ -1186,7 +1206,7 @@ struct ldo_engine {
         CU(copy(d_arena.p + off, fresh.data(), lay.bytes, cudaMemcpyHostToDevice));
         LdoLaunch L = launch_params(LDO_MODE_INIT, 0);
         L.only_rep = r;
-        CU(ldo_launch_mc(L, stream));
+        CU(launch_mc(L));
         CU(cudaStreamSynchronize(stream));
         LdoHdr h;
         CU(copy(&h, d_arena.p + off + lay.o_hdr, sizeof h, cudaMemcpyDeviceToHost));
@@ -1219,7 +1239,7 @@ struct ldo_engine {
         }
         CU(copy(d_arena.p, fresh.data(), fresh.size(), cudaMemcpyHostToDevice));
         LdoLaunch L = launch_params(LDO_MODE_INIT, 0);
-        CU(ldo_launch_mc(L, stream));
+        CU(launch_mc(L));
         CU(cudaStreamSynchronize(stream));
         CU(copy(fresh.data(), d_arena.p, fresh.size(), cudaMemcpyDeviceToHost));
         for (int r = 0; r < n_rep; ++r) {
@@ -1582,7 +1602,7 @@ struct ldo_engine {
 
     void learn_collect() {
         LdoLaunch L = launch_params(LDO_MODE_COLLECT, 0);
-        CU(ldo_launch_mc(L, stream));
+        CU(launch_mc(L));
         CU(cudaStreamSynchronize(stream));
         check_status();
     }
@@ -1843,9 +1863,10 @@ struct ldo_engine {
         LdoLaunch L = launch_params(LDO_MODE_RUN, exchange_interval);
         L.force_recompute = 1;
         L.want_dep = 1;
-        CU(ldo_launch_mc(L, stream));
+        CU(launch_mc(L));
         LdoPT P = pt;
         P.swap_i = (int)(swap_i % pt.n_sets);
+        count_launch();
         CU(ldo_launch_pt_swap(P, stream));
     }
 
@@ -1875,7 +1896,15 @@ struct ldo_engine {
             if (!pt_graph) {
                 cudaGraph_t g;
                 CU(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-                for (int k = 1; k <= period; ++k) pt_round(k, exchange_interval);
+                {
+                    // captured launches run (and count) when the graph is launched
+                    struct Flag {
+                        bool& f;
+                        ~Flag() { f = false; }
+                    } flag {capturing};
+                    capturing = true;
+                    for (int k = 1; k <= period; ++k) pt_round(k, exchange_interval);
+                }
                 CU(cudaStreamEndCapture(stream, &g));
                 CU(cudaGraphInstantiate(&pt_graph, g, 0));
                 cudaGraphDestroy(g);
@@ -1890,6 +1919,7 @@ struct ldo_engine {
             }
             while (swaps - done >= period) {
                 CU(cudaGraphLaunch(pt_graph, stream));
+                count_launch(2 * period);
                 pt_swap_i += period;
                 done += period;
             }
@@ -2066,7 +2096,7 @@ struct ldo_engine {
             L.us_bias = us_bias;
             L.us_len = us_len;
         }
-        CU(ldo_launch_mc(L, stream));
+        CU(launch_mc(L));
     }
 
     // PTMWUSGCMCSimulation::attempt_exchange (src/us_simulation.cpp:770-864):
@@ -2170,6 +2200,7 @@ struct ldo_engine {
             else {
                 us_launch(iter_steps, true);
             }
+            count_copy(hist.size() * sizeof(int), cudaMemcpyDeviceToHost);
             CU(cudaMemcpyAsync(hist.data(), d_us_hist.p, hist.size() * sizeof(int), cudaMemcpyDeviceToHost, stream));
             CU(cudaStreamSynchronize(stream));
             check_status();
@@ -2199,6 +2230,8 @@ struct ldo_engine {
         if (op1 < 0 || op1 >= hs.desc.n_ops || op2 < 0 || op2 >= hs.desc.n_ops || n1 < 1 || n2 < 1)
             throw LdoError(LDO_EINVAL, "enumeration: bad order parameters or histogram shape");
         if (hs.sf.chains.size() != 1) throw LdoError(LDO_EINVAL, "enumeration: the system must start without staples");
+        if (max_total > hs.desc.kmax)
+            throw LdoError(LDO_EINVAL, "enumeration: more staples than the system's max_total_staples");
         LdoHdr h0 {};
         CU(copy(&h0, d_arena.p + lay.o_hdr, sizeof h0, cudaMemcpyDeviceToHost));
         if (h0.num_staples != 0 || h0.n_chains != 1)
@@ -2238,6 +2271,7 @@ struct ldo_engine {
         CU(cudaDeviceGetLimit(&old_stack, cudaLimitStackSize));
         CU(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
         CU(cudaEventRecord(ev0, stream));
+        count_launch();
         cudaError_t err = ldo_launch_enum(E, stream);
         if (err == cudaSuccess) err = cudaEventRecord(ev1, stream);
         if (err == cudaSuccess) err = cudaStreamSynchronize(stream);
@@ -2269,6 +2303,11 @@ struct ldo_engine {
         for (int k = 0; k < n1 * n2; ++k) w[k] /= part;
         if (num_configs) *num_configs = nconf;
         if (n_units) *n_units = nu;
+    }
+
+    // replica 0's sample counter; replica r's is lay.bytes * r further
+    unsigned char* sample_count_ptr() {
+        return reinterpret_cast<unsigned char*>(d_arena.p) + lay.o_hdr + offsetof(LdoHdr, sample_count);
     }
 
     vector<unsigned char> download_arena() {
@@ -2417,7 +2456,7 @@ ldo_status ldo_set_controls(ldo_engine* e, const double* temps, const double* st
         e->upload_tables();
         e->upload_ctl();
         LdoLaunch L = e->launch_params(LDO_MODE_RECOMPUTE, 0);
-        CU(ldo_launch_mc(L, e->stream));
+        CU(e->launch_mc(L));
         CU(cudaStreamSynchronize(e->stream));
         e->check_status();
     });
@@ -2428,7 +2467,7 @@ ldo_status ldo_get_observables(ldo_engine* e, ldo_observables* out, int n) {
     return guard(e, [&]() {
         LdoLaunch L = e->launch_params(LDO_MODE_OBSERVE, 0);
         L.want_dep = 1;
-        CU(ldo_launch_mc(L, e->stream));
+        CU(e->launch_mc(L));
         CU(cudaStreamSynchronize(e->stream));
         auto host = e->download_arena();
         for (int r = 0; r < n; ++r) {
@@ -2584,11 +2623,10 @@ ldo_status ldo_set_sampling(ldo_engine* e, int interval, int capacity) {
         e->sample_cap = capacity;
         e->d_samples.alloc((size_t)e->n_rep * std::max(capacity, 1) * 2);
         CU(cudaMemsetAsync(e->d_samples.p, 0, e->d_samples.n * sizeof(int16_t), e->stream));
-        // restart the per-replica sample counters
-        auto host = e->download_arena();
-        for (int r = 0; r < e->n_rep; ++r)
-            reinterpret_cast<LdoHdr*>(host.data() + (size_t)r * e->lay.bytes + e->lay.o_hdr)->sample_count = 0;
-        CU(e->copy(e->d_arena.p, host.data(), host.size(), cudaMemcpyHostToDevice));
+        // restart the per-replica sample counters: one int in each replica's
+        // header, a strided set over the arena
+        CU(cudaMemset2DAsync(e->sample_count_ptr(), e->lay.bytes, 0, sizeof(int), e->n_rep, e->stream));
+        CU(cudaStreamSynchronize(e->stream));
     });
 }
 
@@ -2597,12 +2635,21 @@ ldo_status ldo_get_samples(ldo_engine* e, int16_t* out, int capacity, int* count
     return guard(e, [&]() {
         CU(e->copy(out, e->d_samples.p, (size_t)e->n_rep * capacity * 2 * sizeof(int16_t), cudaMemcpyDeviceToHost));
         if (count) {
-            auto host = e->download_arena();
-            for (int r = 0; r < e->n_rep; ++r)
-                count[r] =
-                    reinterpret_cast<const LdoHdr*>(host.data() + (size_t)r * e->lay.bytes + e->lay.o_hdr)->sample_count;
+            // the counters alone: a strided copy of one int per replica
+            e->count_copy(sizeof(int) * e->n_rep, cudaMemcpyDeviceToHost);
+            CU(cudaMemcpy2DAsync(count, sizeof(int), e->sample_count_ptr(), e->lay.bytes, sizeof(int), e->n_rep,
+                                 cudaMemcpyDeviceToHost, e->stream));
+            CU(cudaStreamSynchronize(e->stream));
         }
     });
+}
+
+ldo_status ldo_get_counters(ldo_engine* e, int64_t* launches, int64_t* h2d_bytes, int64_t* d2h_bytes) {
+    if (!e) return LDO_EINVAL;
+    if (launches) *launches = e->n_launches;
+    if (h2d_bytes) *h2d_bytes = e->bytes_h2d;
+    if (d2h_bytes) *d2h_bytes = e->bytes_d2h;
+    return LDO_OK;
 }
 
 ldo_status ldo_set_trace(ldo_engine* e, int n_trace, int max_steps) {
@@ -2986,7 +3033,7 @@ namespace {
 ldo_out::Snapshot replica_snapshot(ldo_engine* e, int replica, const vector<int>& op_index) {
     LdoLaunch L = e->launch_params(LDO_MODE_OBSERVE, 0);
     L.want_dep = 1;
-    CU(ldo_launch_mc(L, e->stream));
+    CU(e->launch_mc(L));
     CU(cudaStreamSynchronize(e->stream));
     vector<unsigned char> b(e->lay.bytes);
     CU(e->copy(b.data(), e->d_arena.p + (size_t)replica * e->lay.bytes, b.size(), cudaMemcpyDeviceToHost));

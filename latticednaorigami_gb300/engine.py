@@ -17,7 +17,7 @@ STATUS = {0: "LDO_OK", 1: "LDO_EINVAL", 2: "LDO_ENOMEM", 3: "LDO_ECUDA",
 EXPORTS = [
     "ldo_create_from_inp", "ldo_create_multi", "ldo_destroy", "ldo_last_error", "ldo_num_replicas",
     "ldo_set_controls", "ldo_run", "ldo_run_sweeps", "ldo_state_bytes", "ldo_get_observables", "ldo_get_config", "ldo_set_sampling",
-    "ldo_get_samples", "ldo_set_trace", "ldo_get_trace", "ldo_get_move_stats", "ldo_set_grid_bias",
+    "ldo_get_samples", "ldo_get_counters", "ldo_set_trace", "ldo_get_trace", "ldo_get_move_stats", "ldo_set_grid_bias",
     "ldo_set_window", "ldo_pt_run", "ldo_pt_get_permutation", "ldo_pt_get_stats", "ldo_nn_duplex_thermo",
     "ldo_energy_tables", "ldo_us_run", "ldo_us_get_biases", "ldo_us_get_windows", "ldo_replica_status_noalloc",
     "ldo_learn_collect", "ldo_learn_reset_counts", "ldo_learn_get_counts", "ldo_learn_train", "ldo_learn_set_params",
@@ -104,6 +104,8 @@ def load_library(path=None):
     lib.ldo_set_trace.argtypes = [vp, ip, ip]
     lib.ldo_get_trace.argtypes = [vp, dp, ip, ip]
     lib.ldo_get_move_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ip]
+    i64p = ctypes.POINTER(ctypes.c_int64)
+    lib.ldo_get_counters.argtypes = [vp, i64p, i64p, i64p]
     lib.ldo_set_grid_bias.argtypes = [vp, ctypes.c_char_p, ip, dp, ip]
     lib.ldo_set_window.argtypes = [vp, ctypes.c_char_p, ip, ip, ip]
     lib.ldo_set_bias_centre.argtypes = [vp, ctypes.c_char_p, ip, ctypes.c_double]
@@ -297,6 +299,13 @@ class Engine:
         self._check(self.lib.ldo_get_samples(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int16)), cap,
                                              cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
         return out, cnt
+
+    def counters(self):
+        """(kernel launches, host-to-device bytes, device-to-host bytes) of
+        this engine so far (ldo_get_counters)."""
+        v = [ctypes.c_int64(0) for _ in range(3)]
+        self._check(self.lib.ldo_get_counters(self.h, *[ctypes.byref(x) for x in v]))
+        return tuple(int(x.value) for x in v)
 
     def move_stats(self, n_moves):
         out = np.zeros(2 * n_moves, np.int64)

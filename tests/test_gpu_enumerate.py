@@ -1,8 +1,9 @@
 """Exact staple-only enumeration on the GPU (ldo_enumerate, csrc/ldo_enum.cuh)
 against the reference's own enumerator (src/enumerate.cpp, golden weights at
 full precision from tests/golden/make_golden.py): the 4-domain system with up
-to four staples and the 8-domain system with up to two, where staples bind
-both of their domains.  The reference sums its weights in long double, the
+to four staples and the 8-domain system with up to two and up to three
+(max_total_staples raised to 3 as in the fixture), where staples bind both
+of their domains.  The reference sums its weights in long double, the
 engine in FP64: weights agree to 1e-10 relative."""
 import json
 import os
@@ -21,7 +22,8 @@ def test_enumeration_matches_reference(name, case, max_total, max_type, data_dir
     from latticednaorigami_gb300 import Engine
     with open(os.path.join(GOLDEN, name + ".json")) as f:
         fx = json.load(f)
-    eng = Engine(os.path.join(data_dir, case + ".inp"), n_replicas=1, seed=0)
+    over = "\n".join("%s = %s" % kv for kv in sorted(fx["options"].items()))
+    eng = Engine(os.path.join(data_dir, case + ".inp"), n_replicas=1, seed=0, overrides=over)
     w, info = eng.enumerate(0, max_total, max_type)
     assert set(w) == set(fx["weights"]), (sorted(w), sorted(fx["weights"]))
     for k, v in fx["weights"].items():

@@ -174,3 +174,29 @@ def test_pt_graph_follows_sampling_and_interval_changes():
     eng.pt_run(4, 8, 150, 1)              # another interval: 1200 steps
     smp, cnt = eng.samples()
     assert (cnt == 24).all(), cnt
+
+
+def test_counters_count_launches_and_copies():
+    """ldo_get_counters: a run is one MC launch and the status fold; a PT run
+    of k rounds is k MC and k exchange launches (graph replays counted per
+    kernel) and the status fold; reading the samples copies exactly the
+    sample buffer and the per-replica counters."""
+    temps = [325.0, 330.0, 336.0, 343.0]
+    d = tempfile.mkdtemp()
+    inp = systems.write_case(d, "g24a", extra=dict(temps=" ".join(map(str, temps)), num_reps=4))
+    eng = engine(inp, n_replicas=8, seed=5)
+    eng.set_sampling(10, 32)
+    l0, h0, d0 = eng.counters()
+    eng.run(100)
+    l1, h1, d1 = eng.counters()
+    assert l1 - l0 == 2
+    assert h1 == h0
+    smp, cnt = eng.samples()
+    l2, h2, d2 = eng.counters()
+    assert (cnt == 10).all(), cnt
+    assert l2 == l1 and h2 == h1
+    assert d2 - d1 == smp.nbytes + cnt.nbytes
+    for swaps in (3, 12):                 # below and above the graph threshold
+        a = eng.counters()[0]
+        eng.pt_run(4, swaps, 100, 1)
+        assert eng.counters()[0] - a == 2 * swaps + 1, swaps
