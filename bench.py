@@ -401,6 +401,70 @@ def c4_controls():
     return n, temps, centres
 
 
+# ------------------------------------------------------------- mixed ---
+# Batching across capacity classes: the c2 systems (8-24 domains, small
+# class, staple moves) and the c4 design (96 domains, large class, scaffold
+# regrowth) in one batch of 4096 + 384 replicas.  The per-class batch
+# (ldo_batch_*: one engine per class, launched together) against one engine
+# that promotes every replica to the largest class and compiles the scaffold
+# moves in for all; both autotuned, the same replicas, seeds and steps (the
+# trajectories are identical, only the time differs).
+MIXED_STEPS_PER_STEP = 960   # 10 sweeps of the 96-domain design, 40-120 of the c2 systems
+
+
+def run_mixed(args):
+    from latticednaorigami_gb300 import Batch, Engine
+    tmp = tempfile.mkdtemp()
+    files = write_c2(tmp) + [write_c4(tmp)]
+    per = N_REP // len(SIZES)
+    n4, temps4, _ = c4_controls()
+    sys_of = np.concatenate([np.repeat(np.arange(len(SIZES)), per), np.full(n4, len(SIZES))])
+    temps = np.concatenate([replica_temps(), temps4])
+    n = len(sys_of)
+    steps = MIXED_STEPS_PER_STEP
+    attempts = n * steps
+
+    def arm(make):
+        x = make()
+        x.set_controls(temps=temps)
+        tune = x.autotune(probe_sweeps=1)
+        for _ in range(args.warmup):
+            x.run(steps)
+        clocks = ClockSampler()
+        clocks.start()
+        c0 = x.counters()[0]
+        dev_ms = [x.run(steps) for _ in range(args.steps)]
+        launches = x.counters()[0] - c0
+        clk = clocks.stop()
+        x.close()
+        tune = tune if isinstance(tune, list) else [tune]
+        return {"ms_per_step": float(np.mean(dev_ms)), "move_attempts_per_s": attempts / (np.mean(dev_ms) / 1000.0),
+                "autotune": [{k: v for k, v in t.items() if k != "candidates"} for t in tune],
+                "gpu_launches": launches, "clocks": clk}
+
+    def groups():
+        b = Batch(files, n, seed=0, sys_of_replica=sys_of.tolist())
+        info = [{"class": g["cls"], "replicas": int(len(g["replicas"])),
+                 "state_bytes": int(g["engine"].state_bytes())} for g in b.groups]
+        b.close()
+        return info
+
+    batch = arm(lambda: Batch(files, n, seed=0, sys_of_replica=sys_of.tolist()))
+    one = arm(lambda: Engine(files, n, seed=0, sys_of_replica=sys_of.tolist()))
+    line = {"metric": "move attempts/s, mixed-class batch", "value": batch["move_attempts_per_s"],
+            "unit": "move attempts/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": batch["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "mixed: the c2 systems (4096 replicas, 8-24 domains) and the c4 design (384 "
+                                   "replicas, 96 domains, scaffold regrowth) in one batch, %d steps of every "
+                                   "replica per step" % steps, "replicas": n,
+                       "l2": "state resident in shared memory; no L2 flush needed"},
+            "groups": groups(), "per_class_batch": batch, "one_engine_largest_class": one,
+            "gain_over_one_engine": one["ms_per_step"] / batch["ms_per_step"],
+            "gpu_launches": batch["gpu_launches"], "clocks": batch["clocks"]}
+    print(json.dumps(line))
+
+
 def c4_cpu(inp, burn, rec):
     """The oracle port on all host cores: C4_CPU_REPS replicas spread over the
     windows and temperatures, the same burn-in and recorded sweeps."""
@@ -852,9 +916,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "mixed"],
                     help="c2: the learned-vs-plain headline workload; c3: the 48-domain PTMC learned-vs-plain "
-                         "workload; c4: the 96-domain umbrella workload")
+                         "workload; c4: the 96-domain umbrella workload; mixed: c2 and c4 in one batch, split "
+                         "by capacity class against one engine")
     ap.add_argument("--c3-burn-rounds", type=int, default=0, help="c3 only: PT rounds of the plain burn-in")
     ap.add_argument("--c3-relax-rounds", type=int, default=0,
                     help="c3 only: PT rounds of the learned relaxation after the burn-in")
@@ -882,6 +947,14 @@ def main():
         # single-GPU workload (384 replicas): other ranks have nothing to do
         if rank == 0:
             run_c4(args, args.impl)
+        return
+    if args.workload == "mixed":
+        if rank == 0:
+            if args.impl == "reference":
+                print(json.dumps({"impl": "reference", "unavailable": "the reference runs one system per "
+                                  "process; it has no batch to split"}))
+            else:
+                run_mixed(args)
         return
     if args.impl == "reference":
         if rank == 0:

@@ -396,6 +396,39 @@ void ldo_writer_close(ldo_writer* w);
 ldo_status ldo_swap_writer_open(ldo_engine* e, int n_rungs, int exchange_q, int ladder, const char* filebase,
                                 int64_t freq, ldo_writer** out);
 
+/* Batches split by capacity class (no reference counterpart: the reference
+ * runs one system per process).  A batch holds replicas of several systems
+ * like ldo_create_multi, but groups them by the state-layout class each
+ * system needs on its own (small, medium, large) and gives every group its
+ * own engine: its own layout, kernel instantiation (scaffold moves compiled
+ * in only where a group's systems use them) and launch shape.  A run forks
+ * one MC launch per group from the batch's stream onto the groups' streams
+ * and joins them, so the groups run concurrently.  Replica r keeps the
+ * random stream of replica r of one engine holding the whole batch: the
+ * trajectories equal those of ldo_create_multi with the same arguments. */
+typedef struct ldo_batch ldo_batch;
+ldo_status ldo_batch_create(const char* const* inp_paths, int n_systems, const char* overrides,
+                            const int* sys_of_replica, int n_replicas, uint32_t seed, ldo_batch** out);
+void ldo_batch_destroy(ldo_batch* b);
+const char* ldo_batch_last_error(const ldo_batch* b);   /* NULL batch: last failed create */
+int ldo_batch_num_groups(const ldo_batch* b);
+/* Group g: its class (LDO_CLASS_S/M/L = 0/1/2), replica count, the batch
+ * indices of its replicas (n_rep entries; may be NULL) and its engine, owned
+ * by the batch, for every other engine call on that group. */
+ldo_status ldo_batch_group(ldo_batch* b, int g, int* cls, int* n_rep, int32_t* replicas, ldo_engine** engine);
+/* As ldo_set_controls / ldo_run / ldo_run_sweeps / ldo_set_sampling /
+ * ldo_get_samples / ldo_get_counters over the whole batch (arrays indexed by
+ * batch replica); device_ms spans the fork and join of all groups. */
+ldo_status ldo_batch_set_controls(ldo_batch* b, const double* temps, const double* stacking_mults,
+                                  const double* staple_u_mults, int n);
+ldo_status ldo_batch_run(ldo_batch* b, int64_t n_steps, double* device_ms);
+ldo_status ldo_batch_run_sweeps(ldo_batch* b, int64_t n_sweeps, double* device_ms);
+ldo_status ldo_batch_set_sampling(ldo_batch* b, int interval, int capacity);
+ldo_status ldo_batch_get_samples(ldo_batch* b, int16_t* out, int capacity, int* count);
+ldo_status ldo_batch_get_counters(ldo_batch* b, int64_t* launches, int64_t* h2d_bytes, int64_t* d2h_bytes);
+/* ldo_autotune of every group on its own replicas: out[g] for g < n groups. */
+ldo_status ldo_batch_autotune(ldo_batch* b, int32_t probe_sweeps, int32_t use_cache, ldo_tune_report* out, int n);
+
 /* Host-only helpers (no GPU needed). */
 
 /* Reduced hybridisation enthalpy H/(RT) and entropy S/R of a fully paired

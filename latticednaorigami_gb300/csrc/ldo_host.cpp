@@ -1039,6 +1039,10 @@ struct ldo_engine {
         CU(copy(d_arena.p, host.data(), host.size(), cudaMemcpyHostToDevice));
     }
 
+    // Philox stream key of each replica (ldo_batch: its index in the whole
+    // batch); empty: the replica's own index.
+    vector<uint32_t> rep_ids;
+
     void create(const vector<string>& inps, const string& overrides, const vector<int>& sys_of_replica,
                 uint32_t seed_) {
         seed = seed_;
@@ -1104,7 +1108,7 @@ struct ldo_engine {
                 }
             }
             c.seed = seed;
-            c.rep = (uint32_t)r;
+            c.rep = rep_ids.empty() ? (uint32_t)r : rep_ids[r];
         }
         h_grid.assign(std::max<size_t>(grid_total, 1), 0.0);
         d_grid.alloc(h_grid.size());
@@ -1517,7 +1521,7 @@ struct ldo_engine {
             if (k < 0 || k >= (int)keys.size()) throw LdoError(LDO_EINVAL, path + ": bad table index");
         };
         for (int r = 0; r < n_rep; ++r) {
-            if (ctl[r].sys != sys_of[r] || ctl[r].rep != (uint32_t)r)
+            if (ctl[r].sys != sys_of[r] || ctl[r].rep != h_ctl[r].rep)
                 throw LdoError(LDO_EINVAL, path + ": replica controls do not match this engine");
             for (int b = 0; b < LDO_MAX_BIASES; ++b)
                 if (ctl[r].grid_off[b] != h_ctl[r].grid_off[b])
@@ -3190,5 +3194,245 @@ ldo_status ldo_writer_write(ldo_writer* w, int64_t step) {
 }
 
 void ldo_writer_close(ldo_writer* w) { delete w; }
+
+} // extern "C"
+
+// ------------------------------------------------------------ batches ---
+// A batch of replicas over systems of different sizes, split by capacity
+// class: one engine per class, each with its own state layout, kernel
+// instantiation and launch shape, launched together (their streams fork
+// from and join into the batch's stream).  Replica r keeps the Philox
+// stream key r of the whole batch, so every trajectory equals that of one
+// engine holding all the replicas in the largest class.
+struct ldo_batch {
+    string err;
+    int n_rep {0};
+    vector<ldo_engine*> groups;
+    vector<int> cls;
+    vector<vector<int>> reps;          // batch indices of each group's replicas
+    vector<int> group_of, local_of;    // per batch replica
+    cudaStream_t stream {nullptr};
+    cudaEvent_t ev0 {nullptr}, ev1 {nullptr};
+    vector<cudaEvent_t> done;
+
+    ~ldo_batch() {
+        for (auto ev : done) cudaEventDestroy(ev);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+        for (auto* g : groups) delete g;
+    }
+
+    void create(const vector<string>& inps, const string& overrides, const vector<int>& sys_of, uint32_t seed) {
+        n_rep = (int)sys_of.size();
+        if (n_rep <= 0) throw LdoError(LDO_EINVAL, "need at least one replica");
+        vector<int> sys_cls(inps.size());
+        for (size_t i = 0; i < inps.size(); ++i) {
+            HostSystem hs = load_system(inps[i], overrides);
+            sys_cls[i] = make_layout(hs.desc.dcap, hs.desc.kmax, hs.desc.n_types, hs.desc.n_biases, hs.desc.n_ops,
+                                     hs.desc.n_moves).cls;
+        }
+        for (int r = 0; r < n_rep; ++r)
+            if (sys_of[r] < 0 || sys_of[r] >= (int)inps.size())
+                throw LdoError(LDO_EINVAL, "sys_of_replica out of range");
+        group_of.assign(n_rep, -1);
+        local_of.assign(n_rep, -1);
+        CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        CU(cudaEventCreate(&ev0));
+        CU(cudaEventCreate(&ev1));
+        for (int c = LDO_CLASS_S; c <= LDO_CLASS_L; ++c) {
+            vector<int> sys_map(inps.size(), -1), so, rr;
+            vector<string> sub;
+            vector<uint32_t> ids;
+            for (int r = 0; r < n_rep; ++r) {
+                int s = sys_of[r];
+                if (sys_cls[s] != c) continue;
+                if (sys_map[s] < 0) {
+                    sys_map[s] = (int)sub.size();
+                    sub.push_back(inps[s]);
+                }
+                group_of[r] = (int)groups.size();
+                local_of[r] = (int)rr.size();
+                so.push_back(sys_map[s]);
+                ids.push_back((uint32_t)r);
+                rr.push_back(r);
+            }
+            if (rr.empty()) continue;
+            auto* e = new ldo_engine;
+            groups.push_back(e);
+            e->rep_ids = ids;
+            e->create(sub, overrides, so, seed);
+            if (e->lay.cls != c) throw LdoError(LDO_EINVAL, "batch: a group's layout class differs from its systems'");
+            cls.push_back(c);
+            reps.push_back(rr);
+            cudaEvent_t ev;
+            CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            done.push_back(ev);
+        }
+    }
+
+    // One MC launch per group on the group's stream, all forked from and
+    // joined into the batch's stream; device_ms spans the whole fork/join.
+    void run(long long steps, int sweeps, double* ms) {
+        CU(cudaEventRecord(ev0, stream));
+        for (size_t g = 0; g < groups.size(); ++g) {
+            ldo_engine& e = *groups[g];
+            CU(cudaStreamWaitEvent(e.stream, ev0, 0));
+            LdoLaunch L = e.launch_params(LDO_MODE_RUN, steps);
+            L.sweep_units = sweeps;
+            CU(e.launch_mc(L));
+            CU(cudaEventRecord(done[g], e.stream));
+            CU(cudaStreamWaitEvent(stream, done[g], 0));
+        }
+        CU(cudaEventRecord(ev1, stream));
+        CU(cudaStreamSynchronize(stream));
+        if (ms) {
+            float f = 0;
+            CU(cudaEventElapsedTime(&f, ev0, ev1));
+            *ms = f;
+        }
+        for (auto* g : groups) g->check_status();
+    }
+};
+
+namespace {
+
+ldo_status bguard(ldo_batch* b, const std::function<void()>& f) {
+    try {
+        f();
+        if (b) b->err.clear();
+        return LDO_OK;
+    } catch (LdoError& x) {
+        if (b) b->err = x.what();
+        else g_create_err = x.what();
+        return x.code;
+    } catch (std::exception& x) {
+        if (b) b->err = x.what();
+        else g_create_err = x.what();
+        return LDO_EINVAL;
+    }
+}
+
+// a group engine's call inside a batch call: its error becomes the batch's
+void group_ok(ldo_engine* e, ldo_status st) {
+    if (st != LDO_OK) throw LdoError(st, e->err);
+}
+
+} // namespace
+
+extern "C" {
+
+ldo_status ldo_batch_create(const char* const* inp_paths, int n_systems, const char* overrides,
+                            const int* sys_of_replica, int n_replicas, uint32_t seed, ldo_batch** out) {
+    if (!out || !inp_paths || n_systems <= 0 || n_replicas <= 0) {
+        g_create_err = "invalid arguments";
+        return LDO_EINVAL;
+    }
+    *out = nullptr;
+    auto* b = new ldo_batch;
+    vector<string> inps;
+    for (int i = 0; i < n_systems; ++i) inps.push_back(inp_paths[i]);
+    vector<int> so(n_replicas, 0);
+    if (sys_of_replica)
+        for (int r = 0; r < n_replicas; ++r) so[r] = sys_of_replica[r];
+    ldo_status st = bguard(nullptr, [&]() { b->create(inps, overrides ? overrides : "", so, seed); });
+    if (st != LDO_OK) {
+        delete b;
+        return st;
+    }
+    *out = b;
+    return LDO_OK;
+}
+
+void ldo_batch_destroy(ldo_batch* b) { delete b; }
+
+const char* ldo_batch_last_error(const ldo_batch* b) { return b ? b->err.c_str() : g_create_err.c_str(); }
+
+int ldo_batch_num_groups(const ldo_batch* b) { return b ? (int)b->groups.size() : 0; }
+
+ldo_status ldo_batch_group(ldo_batch* b, int g, int* cls, int* n_rep, int32_t* replicas, ldo_engine** engine) {
+    if (!b || g < 0 || g >= (int)b->groups.size()) return LDO_EINVAL;
+    if (cls) *cls = b->cls[g];
+    if (n_rep) *n_rep = (int)b->reps[g].size();
+    if (replicas)
+        for (size_t k = 0; k < b->reps[g].size(); ++k) replicas[k] = b->reps[g][k];
+    if (engine) *engine = b->groups[g];
+    return LDO_OK;
+}
+
+ldo_status ldo_batch_set_controls(ldo_batch* b, const double* temps, const double* stacking_mults,
+                                  const double* staple_u_mults, int n) {
+    if (!b || n != b->n_rep) return LDO_EINVAL;
+    return bguard(b, [&]() {
+        for (size_t g = 0; g < b->groups.size(); ++g) {
+            const auto& rr = b->reps[g];
+            vector<double> t(rr.size()), s(rr.size()), u(rr.size());
+            for (size_t k = 0; k < rr.size(); ++k) {
+                if (temps) t[k] = temps[rr[k]];
+                if (stacking_mults) s[k] = stacking_mults[rr[k]];
+                if (staple_u_mults) u[k] = staple_u_mults[rr[k]];
+            }
+            group_ok(b->groups[g], ldo_set_controls(b->groups[g], temps ? t.data() : nullptr,
+                                                    stacking_mults ? s.data() : nullptr,
+                                                    staple_u_mults ? u.data() : nullptr, (int)rr.size()));
+        }
+    });
+}
+
+ldo_status ldo_batch_run(ldo_batch* b, int64_t n_steps, double* device_ms) {
+    if (!b || n_steps < 0) return LDO_EINVAL;
+    return bguard(b, [&]() { b->run(n_steps, 0, device_ms); });
+}
+
+ldo_status ldo_batch_run_sweeps(ldo_batch* b, int64_t n_sweeps, double* device_ms) {
+    if (!b || n_sweeps < 0) return LDO_EINVAL;
+    return bguard(b, [&]() { b->run(n_sweeps, 1, device_ms); });
+}
+
+ldo_status ldo_batch_set_sampling(ldo_batch* b, int interval, int capacity) {
+    if (!b || interval < 0 || capacity < 0) return LDO_EINVAL;
+    return bguard(b, [&]() {
+        for (auto* g : b->groups) group_ok(g, ldo_set_sampling(g, interval, capacity));
+    });
+}
+
+ldo_status ldo_batch_get_samples(ldo_batch* b, int16_t* out, int capacity, int* count) {
+    if (!b || !out) return LDO_EINVAL;
+    return bguard(b, [&]() {
+        for (size_t g = 0; g < b->groups.size(); ++g) {
+            const auto& rr = b->reps[g];
+            vector<int16_t> part(rr.size() * (size_t)capacity * 2);
+            vector<int> cnt(rr.size());
+            group_ok(b->groups[g], ldo_get_samples(b->groups[g], part.data(), capacity, cnt.data()));
+            for (size_t k = 0; k < rr.size(); ++k) {
+                std::memcpy(out + (size_t)rr[k] * capacity * 2, part.data() + k * (size_t)capacity * 2,
+                            (size_t)capacity * 2 * sizeof(int16_t));
+                if (count) count[rr[k]] = cnt[k];
+            }
+        }
+    });
+}
+
+ldo_status ldo_batch_autotune(ldo_batch* b, int32_t probe_sweeps, int32_t use_cache, ldo_tune_report* out, int n) {
+    if (!b || probe_sweeps < 1 || !out || n < (int)b->groups.size()) return LDO_EINVAL;
+    return bguard(b, [&]() {
+        for (size_t g = 0; g < b->groups.size(); ++g)
+            group_ok(b->groups[g], ldo_autotune(b->groups[g], probe_sweeps, use_cache, out + g));
+    });
+}
+
+ldo_status ldo_batch_get_counters(ldo_batch* b, int64_t* launches, int64_t* h2d_bytes, int64_t* d2h_bytes) {
+    if (!b) return LDO_EINVAL;
+    int64_t l = 0, h = 0, d = 0;
+    for (auto* g : b->groups) {
+        l += g->n_launches;
+        h += g->bytes_h2d;
+        d += g->bytes_d2h;
+    }
+    if (launches) *launches = l;
+    if (h2d_bytes) *h2d_bytes = h;
+    if (d2h_bytes) *d2h_bytes = d;
+    return LDO_OK;
+}
 
 } // extern "C"

@@ -26,6 +26,9 @@ EXPORTS = [
     "ldo_set_bias_centre", "ldo_swap_writer_open", "ldo_set_config", "ldo_set_configs", "ldo_anneal_run", "ldo_read_trj_frame", "ldo_checkpoint_save",
     "ldo_checkpoint_load", "ldo_autotune", "ldo_autotune_candidates", "ldo_us_write_biases",
     "ldo_us_read_biases", "ldo_us_reset", "ldo_read_biases", "ldo_enumerate", "ldo_enumerate_units",
+    "ldo_batch_create", "ldo_batch_destroy", "ldo_batch_last_error", "ldo_batch_num_groups", "ldo_batch_group",
+    "ldo_batch_set_controls", "ldo_batch_run", "ldo_batch_run_sweeps", "ldo_batch_set_sampling",
+    "ldo_batch_get_samples", "ldo_batch_get_counters", "ldo_batch_autotune",
 ]
 
 LEARN_TABLE = 524544      # network inputs: 524288 insertion + 256 regrowth-direction (ldo_learn.h)
@@ -106,6 +109,21 @@ def load_library(path=None):
     lib.ldo_get_move_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ip]
     i64p = ctypes.POINTER(ctypes.c_int64)
     lib.ldo_get_counters.argtypes = [vp, i64p, i64p, i64p]
+    lib.ldo_batch_create.argtypes = [ctypes.POINTER(ctypes.c_char_p), ip, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int),
+                                     ip, ctypes.c_uint32, ctypes.POINTER(vp)]
+    lib.ldo_batch_destroy.argtypes = [vp]
+    lib.ldo_batch_destroy.restype = None
+    lib.ldo_batch_last_error.argtypes = [vp]
+    lib.ldo_batch_last_error.restype = ctypes.c_char_p
+    lib.ldo_batch_num_groups.argtypes = [vp]
+    lib.ldo_batch_group.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                    ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(vp)]
+    lib.ldo_batch_set_controls.argtypes = [vp, dp, dp, dp, ip]
+    lib.ldo_batch_run.argtypes = [vp, ctypes.c_int64, dp]
+    lib.ldo_batch_run_sweeps.argtypes = [vp, ctypes.c_int64, dp]
+    lib.ldo_batch_set_sampling.argtypes = [vp, ip, ip]
+    lib.ldo_batch_get_samples.argtypes = [vp, ctypes.POINTER(ctypes.c_int16), ip, ctypes.POINTER(ctypes.c_int)]
+    lib.ldo_batch_get_counters.argtypes = [vp, i64p, i64p, i64p]
     lib.ldo_set_grid_bias.argtypes = [vp, ctypes.c_char_p, ip, dp, ip]
     lib.ldo_set_window.argtypes = [vp, ctypes.c_char_p, ip, ip, ip]
     lib.ldo_set_bias_centre.argtypes = [vp, ctypes.c_char_p, ip, ctypes.c_double]
@@ -169,9 +187,17 @@ class Engine:
         self._trace = None
         self._samples = None
 
+    @classmethod
+    def _borrowed(cls, lib, handle, n_replicas):
+        """An Engine over a handle owned by someone else (a Batch group)."""
+        e = cls.__new__(cls)
+        e.lib, e.h, e.n, e._trace, e._samples, e._owned = lib, handle, n_replicas, None, None, False
+        return e
+
     def close(self):
         if getattr(self, "h", None):
-            self.lib.ldo_destroy(self.h)
+            if getattr(self, "_owned", True):
+                self.lib.ldo_destroy(self.h)
             self.h = None
 
     __del__ = close
@@ -535,3 +561,86 @@ def energy_tables(inp, temp, stacking_mult=1.0):
     if rc != 0:
         raise LdoError(rc, lib.ldo_last_error(None).decode())
     return imax.value, [a.reshape(d, d) for a in arrs], init
+
+
+class Batch:
+    """Replicas of several systems split by capacity class (ldo_batch_*): one
+    engine per class with its own layout and kernel, launched together.
+    Replica r follows the trajectory it has in Engine(inps, n_replicas, seed,
+    overrides, sys_of_replica)."""
+
+    def __init__(self, inps, n_replicas, seed=0, overrides="", sys_of_replica=None):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        arr = (ctypes.c_char_p * len(inps))(*[os.fsencode(p) for p in inps])
+        so = None
+        if sys_of_replica is not None:
+            so = (ctypes.c_int * n_replicas)(*[int(x) for x in sys_of_replica])
+        rc = self.lib.ldo_batch_create(arr, len(inps), overrides.encode(), so, n_replicas, seed, ctypes.byref(h))
+        if rc != 0:
+            raise LdoError(rc, self.lib.ldo_batch_last_error(None).decode())
+        self.h = h
+        self.n = n_replicas
+        self._samples = None
+        self.groups = []
+        for g in range(self.lib.ldo_batch_num_groups(self.h)):
+            cls, n = ctypes.c_int(0), ctypes.c_int(0)
+            self._check(self.lib.ldo_batch_group(self.h, g, ctypes.byref(cls), ctypes.byref(n), None, None))
+            reps = np.zeros(n.value, np.int32)
+            eh = ctypes.c_void_p()
+            self._check(self.lib.ldo_batch_group(self.h, g, None, None,
+                                                 reps.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), ctypes.byref(eh)))
+            self.groups.append({"cls": "SML"[cls.value], "replicas": reps,
+                                "engine": Engine._borrowed(self.lib, eh, n.value)})
+
+    def close(self):
+        if getattr(self, "h", None):
+            for g in self.groups:
+                g["engine"].h = None
+            self.lib.ldo_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def _check(self, rc):
+        if rc != 0:
+            raise LdoError(rc, self.lib.ldo_batch_last_error(self.h).decode())
+
+    def set_controls(self, temps=None, stacking_mults=None, staple_u_mults=None):
+        def arr(x):
+            return None if x is None else np.ascontiguousarray(np.broadcast_to(np.asarray(x, np.float64), (self.n,)))
+        t, s, u = arr(temps), arr(stacking_mults), arr(staple_u_mults)
+        self._check(self.lib.ldo_batch_set_controls(self.h, _dptr(t), _dptr(s), _dptr(u), self.n))
+
+    def run(self, steps):
+        ms = ctypes.c_double(0)
+        self._check(self.lib.ldo_batch_run(self.h, int(steps), ctypes.byref(ms)))
+        return ms.value
+
+    def run_sweeps(self, sweeps):
+        ms = ctypes.c_double(0)
+        self._check(self.lib.ldo_batch_run_sweeps(self.h, int(sweeps), ctypes.byref(ms)))
+        return ms.value
+
+    def set_sampling(self, interval, capacity):
+        self._check(self.lib.ldo_batch_set_sampling(self.h, interval, capacity))
+        self._samples = capacity
+        for g in self.groups:
+            g["engine"]._samples = capacity
+
+    def samples(self):
+        cap = self._samples
+        out = np.zeros((self.n, cap, 2), np.int16)
+        cnt = np.zeros(self.n, np.int32)
+        self._check(self.lib.ldo_batch_get_samples(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int16)), cap,
+                                                   cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return out, cnt
+
+    def counters(self):
+        v = [ctypes.c_int64(0) for _ in range(3)]
+        self._check(self.lib.ldo_batch_get_counters(self.h, *[ctypes.byref(x) for x in v]))
+        return tuple(int(x.value) for x in v)
+
+    def autotune(self, probe_sweeps=4, use_cache=True):
+        """Each group's autotuner on its own replicas: one report per group."""
+        return [g["engine"].autotune(probe_sweeps, use_cache) for g in self.groups]
