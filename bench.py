@@ -739,8 +739,11 @@ def run_c3(args, impl):
         t = sum(dev_ms) / 1000.0
         (lo, hi), boot = bootstrap_sum(ess, [q for (_, q) in keys])
         hist = np.zeros((C3_RUNGS, 49))
+        halves = np.zeros((2, C3_RUNGS, 49))   # ladders 0-15 and 16-31 apart
         for (l, q), x in series.items():
-            hist[q] += np.bincount(x.astype(int), minlength=49)[:49]
+            hb = np.bincount(x.astype(int), minlength=49)[:49]
+            hist[q] += hb
+            halves[l * 2 // C3_LADDERS, q] += hb
         half = len(series[keys[0]]) // 2
         top = [series[(l, C3_RUNGS - 1)] for l in range(C3_LADDERS)]
         taus = [tau_int(series[k]) for k in keys]
@@ -766,7 +769,8 @@ def run_c3(args, impl):
                               "regrowth": float(st[1, 1]) / max(1.0, float(st[1, 0])),
                               "cb_regrowth": float(st[2, 1]) / max(1.0, float(st[2, 0]))},
                "swap_acceptance_mean": float(acc.sum()) / max(1.0, float(att.sum())),
-               "autotune": {k: v for k, v in tune.items() if k != "candidates"}, "clocks": clk}
+               "autotune": {k: v for k, v in tune.items() if k != "candidates"}, "clocks": clk,
+               "kl_between_ladder_halves": [kl_divergence(halves[0, q], halves[1, q]) for q in range(C3_RUNGS)]}
         eng.close()
         return res, hist
 
@@ -832,6 +836,11 @@ def run_c3(args, impl):
                 "traffic": None, "traffic_source": "no capture of this workload"}
 
     for res in (plain, learned):
+        # the arm's own spread: KL between its two halves of ladders, at the
+        # temperature of the largest plain-vs-learned KL and at its largest
+        self_kl = res.pop("kl_between_ladder_halves")
+        res["kl_between_ladder_halves"] = {"at_argmax_K": self_kl[q_max], "max": max(self_kl),
+                                           "mean": float(np.mean(self_kl))}
         res["roofline"] = roofline(res, "learned" if res is learned else "plain")
         res.pop("dev_ms")
         res.pop("attempts")
