@@ -8,6 +8,7 @@
 // replica's move lane touches it, so it needs no layout for coalescing.
 #pragma once
 #include <stdint.h>
+#include "ldo_types.h"
 
 // Scaffold segments of one move (CTRegrowthMCMovetype::select_noncontig_segs
 // makes 1 + 2 per stem domain).
@@ -84,6 +85,21 @@ struct LdoCtWork {
     int16_t fr_a[FR], fr_b[FR], fr_n[FR], fr_i[FR];
     int8_t fr_dir[FR];
     int16_t list[D + 1];      // a scaffold list being grown: the stem then a paired segment
+    // ---- linker movetypes (LinkerRegrowthMCMovetype, src/transform_movetypes.cpp):
+    // the central segment, the domains transformed with it (the segment, then
+    // the staples bound to it in chain-index order), the two linkers (each
+    // from its central end outwards: lk[0 .. n_lk1) and lk[n_lk1 .. n_lk1 +
+    // n_lk2)), the domains that end them (m_linker_endpoints, -1: none), and
+    // the trial transformations kept for the Rosenbluth choice
+    int n_cen, n_cdom, n_lk1, n_lk2;
+    int16_t cen[D], cdom[D], lk[2 * D + 2];
+    int16_t lk_end[2];
+    int16_t fs_cs[C::KMAX + 2], fs_k[C::KMAX + 2];   // chain scans (find_staples, domains_bound_externally)
+    int16_t fs_d[C::KMAX + 2];
+    int n_tr;
+    long long tr_center[LDO_CT_MAX_TRANSFORMS], tr_disp[LDO_CT_MAX_TRANSFORMS];
+    int8_t tr_axis[LDO_CT_MAX_TRANSFORMS], tr_turns[LDO_CT_MAX_TRANSFORMS];
+    double tr_bf[LDO_CT_MAX_TRANSFORMS];
     // ---- scalar move state
     int kind;                 // LDO_MV_CT* of the move in progress
     int dir;                  // CTRegrowthMCMovetype::m_dir

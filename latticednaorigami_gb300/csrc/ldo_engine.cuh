@@ -197,7 +197,7 @@ struct Scratch {
 #define CMD_REST(k) (((k) + 1) << 4)
 enum : int { CMD_MORE = 1 << 8, CMD_REST_FIRST = 1 << 9, CMD_STOP = 1 << 10 };
 enum : int { PH_POST = 1, PH_CB2 = 2, PH_CB3 = 3, PH_RG2 = 4, PH_RG3 = 5, PH_RG4 = 6, PH_RG5 = 7, PH_CT2 = 8,
-             PH_CT3 = 9 };
+             PH_CT3 = 9, PH_LK2 = 10, PH_LK3 = 11, PH_LKR2 = 12 };
 constexpr int N_SNAPSHOTS = 3;
 
 // Scratch of the FourBody evaluation.
@@ -2899,13 +2899,14 @@ struct Rep : public LdoState<C> {
     }
 
     // ------------------------------------------------ segment selection ---
-    // CTRegrowthMCMovetype::select_indices (src/movetypes.cpp:479), min length 2
-    __device__ __noinline__ void ct_select_indices(int max_regrowth) {
+    // CTRegrowthMCMovetype::select_indices (src/movetypes.cpp:469): min
+    // length 2 for the scaffold regrowth movetypes, 1 for the linker ones
+    __device__ __noinline__ void ct_select_indices(int max_regrowth, int min_length = 2) {
         LdoCtWork<C>& w = *ct;
         int max_length = ns < max_regrowth ? ns : max_regrowth;
         #pragma unroll 1
         for (int guard = 0; guard < 1000; ++guard) {
-            int sel = rng.uniform_int(2, max_length);
+            int sel = rng.uniform_int(min_length, max_length);
             int start = rng.uniform_int(0, ns - 1);
             int dir = rng.uniform_int(0, 1) == 0 ? -1 : 1;
             // forward from the start in dir, then backward from before it
@@ -2921,7 +2922,7 @@ struct Rep : public LdoState<C> {
                 ++nb;
                 back = next(back, -dir);
             }
-            if (nf + nb < 2) continue;
+            if (nf + nb < min_length) continue;
             w.dir = dir;
             int x = start;
             #pragma unroll 1
@@ -3689,7 +3690,7 @@ struct Rep : public LdoState<C> {
     __device__ int ct_frame_elem(int f, int i) const {
         const LdoCtWork<C>& w = *ct;
         if (w.fr_kind[f] == 1) return slot_of(w.fr_a[f], w.fr_b[f] + w.fr_dir[f] * i);
-        return (w.fr_a[f] == 0 ? w.seg_dom : w.list)[w.fr_b[f] + i];
+        return (w.fr_a[f] == 0 ? w.seg_dom : w.fr_a[f] == 1 ? w.list : w.lk)[w.fr_b[f] + i];
     }
     // CTCBRegrowthMCMovetype::grow_staple_and_update_endpoints (:533) up to
     // the growth of the staple, which the frame loop does
@@ -3910,6 +3911,633 @@ struct Rep : public LdoState<C> {
         return finish_move(acc, acc ? 2 : 0);
     }
 
+    // ================================= scaffold transforms with linkers ===
+    // LinkerRegrowthMCMovetype and its variants (src/transform_movetypes.cpp):
+    // a central scaffold segment, with the staples bound only within it, is
+    // unassigned and placed again by a rigid lattice transformation (turns
+    // about a basis axis through one of its domains, then a translation),
+    // chosen among num_transforms trials by their Boltzmann factors (modified
+    // Rosenbluth); the scaffold linkers on both sides and the staples bound
+    // to them regrow with configurational bias (CTCB) or recoil growth
+    // (CTRG).  The reverse move's weight comes from num_transforms - 1 trial
+    // transformations of the new configuration plus the old one.  Snapshots:
+    // CTCB 1 = everything unassigned, 2 = the new configuration; CTRG 2.
+
+    // VectorThree::rotate(axis, turns) (src/utility.cpp:102) about basis axis
+    // 0 x, 1 y, 2 z, turns > 0: an even count is a half turn (rotate_half,
+    // :68), an odd one a quarter turn whose sense alternates every two turns
+    __device__ static V3 lk_rot(V3 v, int axis, int turns) {
+        int x = vx(v), y = vy(v), z = vz(v), t;
+        if (turns % 2 == 0) {
+            if (axis == 0) { y = -y; z = -z; }
+            else if (axis == 1) { x = -x; z = -z; }
+            else { x = -x; y = -y; }
+        }
+        else {
+            int dir = ((turns - 1) / 2 % 2 == 0) ? 1 : -1;
+            if (axis == 0) { t = y; y = -dir * z; z = dir * t; }
+            else if (axis == 1) { t = x; x = -dir * z; z = dir * t; }
+            else { t = x; x = -dir * y; y = dir * t; }
+        }
+        return mk(x, y, z);
+    }
+    // pos.rotate(center, axis, turns) + disp; no rotation for zero turns
+    __device__ static V3 lk_place(V3 p, V3 center, int axis, int turns, V3 disp) {
+        if (turns != 0) p = add(lk_rot(sub(p, center), axis, turns), center);
+        return add(p, disp);
+    }
+    __device__ static int lk_orient(int o, int axis, int turns) {
+        return turns == 0 ? o : unit_index(lk_rot(unit_c(o), axis, turns));
+    }
+    __device__ bool lk_in(const int16_t* list, int n, int d) const {
+        #pragma unroll 1
+        for (int k = 0; k < n; ++k)
+            if (list[k] == d) return true;
+        return false;
+    }
+    // LinkerRegrowthMCMovetype::domains_bound_externally (:238) with
+    // scan_for_external_scaffold_domain (:262): from each central domain
+    // bound to a staple, the staples reached through their other domains,
+    // depth first in chain order; true at the first one bound to a scaffold
+    // domain outside the central segment
+    __device__ __noinline__ bool lk_bound_externally() {
+        LdoCtWork<C>& w = *ct;
+        #pragma unroll 1
+        for (int c = 0; c < w.n_cen; ++c) {
+            int d = w.cen[c];
+            if (st[d] == UNBOUND) continue;
+            int bd = bnd[d];
+            if (bd < 0) {
+                fail(LDO_RS_INVARIANT);
+                return false;
+            }
+            if (scs[bd] == 0) continue;
+            unsigned long long part = (1ull << scs[d]) | (1ull << scs[bd]);
+            int top = 0;
+            w.fs_cs[top] = (int16_t)scs[bd];
+            w.fs_d[top] = (int16_t)bd;
+            w.fs_k[top] = 0;
+            ++top;
+            #pragma unroll 1
+            while (top > 0) {
+                int f = top - 1;
+                int cs = w.fs_cs[f];
+                if (w.fs_k[f] >= chain_len(cs)) {
+                    --top;
+                    continue;
+                }
+                int cur = slot_of(cs, w.fs_k[f]++);
+                if (cur == w.fs_d[f]) continue;
+                int b = bnd[cur];
+                if (b < 0 || scs[b] == cs) continue;
+                if (scs[b] == 0) {
+                    if (!lk_in(w.cen, w.n_cen, b)) return true;
+                    continue;
+                }
+                if (part & (1ull << scs[b])) continue;
+                if (top >= C::KMAX + 2) {
+                    fail(LDO_RS_CAPACITY);
+                    return false;
+                }
+                part |= 1ull << scs[b];
+                w.fs_cs[top] = (int16_t)scs[b];
+                w.fs_d[top] = (int16_t)b;
+                w.fs_k[top] = 0;
+                ++top;
+            }
+        }
+        return false;
+    }
+    // MCMovetype::find_staples (src/movetypes.cpp:179) with
+    // scan_for_scaffold_domain (:191): the staples reached from the central
+    // segment, depth first in chain order, each scan ending (at every level)
+    // at the first domain bound to the scaffold; then the central domains:
+    // the segment, then those staples' domains in chain-index order
+    __device__ __noinline__ void lk_central_domains() {
+        LdoCtWork<C>& w = *ct;
+        unsigned long long part = 0;
+        #pragma unroll 1
+        for (int c = 0; c < w.n_cen; ++c) {
+            int bd = bnd[w.cen[c]];
+            if (bd < 0 || scs[bd] == 0) continue;
+            part |= 1ull << scs[bd];
+            int top = 0;
+            w.fs_cs[top] = (int16_t)scs[bd];
+            w.fs_d[top] = (int16_t)bd;
+            w.fs_k[top] = 0;
+            ++top;
+            #pragma unroll 1
+            while (top > 0) {
+                int f = top - 1;
+                int cs = w.fs_cs[f];
+                if (w.fs_k[f] >= chain_len(cs)) {
+                    --top;
+                    continue;
+                }
+                int cur = slot_of(cs, w.fs_k[f]++);
+                if (cur == w.fs_d[f]) continue;
+                int b = bnd[cur];
+                if (b < 0 || scs[b] == cs) continue;
+                if (scs[b] == 0) {   // bound to the scaffold: true returns through every level
+                    top = 0;
+                    continue;
+                }
+                if (part & (1ull << scs[b])) continue;
+                if (top >= C::KMAX + 2) {
+                    fail(LDO_RS_CAPACITY);
+                    return;
+                }
+                part |= 1ull << scs[b];
+                w.fs_cs[top] = (int16_t)scs[b];
+                w.fs_d[top] = (int16_t)b;
+                w.fs_k[top] = 0;
+                ++top;
+            }
+        }
+        w.n_cdom = 0;
+        #pragma unroll 1
+        for (int c = 0; c < w.n_cen; ++c) w.cdom[w.n_cdom++] = w.cen[c];
+        #pragma unroll 1
+        while (part) {
+            int best = -1;
+            #pragma unroll 1
+            for (unsigned long long m = part; m; m &= m - 1ull) {
+                int cs = __ffsll((long long)m) - 1;
+                if (best < 0 || chain_c[cs] < chain_c[best]) best = cs;
+            }
+            part &= ~(1ull << best);
+            int len = chain_len(best);
+            if (w.n_cdom + len > C::DCAP) {
+                fail(LDO_RS_CAPACITY);
+                return;
+            }
+            #pragma unroll 1
+            for (int q = 0; q < len; ++q) w.cdom[w.n_cdom++] = (int16_t)slot_of(best, q);
+        }
+    }
+    // LinkerRegrowthMCMovetype::select_and_setup_segments (:156) up to the
+    // fixed-end biases: central segment by select_indices with minimum
+    // length 1, linkers from its ends outwards; false: the move is rejected
+    __device__ __noinline__ bool lk_select() {
+        LdoCtWork<C>& w = *ct;
+        const int* mo = sys->move_opt[cur_mv];
+        int maxl = mo[LDO_MO_MAX_LINKER];
+        bool ext = true;
+        #pragma unroll 1
+        for (int att = 0; ext && att != 10; ++att) {
+            ct_select_indices(mo[LDO_MO_MAX_REGROWTH], 1);
+            if (bad()) return false;
+            int n = w.seg_off[1];
+            #pragma unroll 1
+            for (int k = 0; k < n; ++k) w.cen[k] = w.seg_dom[k];
+            w.n_cen = n;
+            int dir = w.dir;
+            int len1 = rng.uniform_int(2, maxl + 1);
+            int stop = next(w.cen[n - 1], 2 * dir);
+            int x = w.cen[0];
+            w.n_lk1 = 0;
+            #pragma unroll 1
+            while (w.n_lk1 != len1 && x >= 0 && x != stop) {
+                w.lk[w.n_lk1++] = (int16_t)x;
+                x = next(x, -dir);
+            }
+            if (cyclic && w.n_lk1 == 1) return false;
+            int len2 = rng.uniform_int(2, maxl + 1);
+            stop = next(w.lk[w.n_lk1 - 1], -dir);
+            x = w.cen[n - 1];
+            w.n_lk2 = 0;
+            #pragma unroll 1
+            while (w.n_lk2 != len2 && x >= 0 && x != stop) {
+                w.lk[w.n_lk1 + w.n_lk2++] = (int16_t)x;
+                x = next(x, dir);
+            }
+            ext = lk_bound_externally();
+            if (bad()) return false;
+        }
+        return !ext;
+    }
+    // ClusteredLinkerRegrowthMCMovetype::linear_select_central_segment (:670)
+    // and cyclic_select_central_segment (:734): the run of bound scaffold
+    // domains at or next to a random kernel domain
+    __device__ void lk_reverse_cen() {
+        LdoCtWork<C>& w = *ct;
+        #pragma unroll 1
+        for (int a = 0, b = w.n_cen - 1; a < b; ++a, --b) {
+            int16_t t = w.cen[a];
+            w.cen[a] = w.cen[b];
+            w.cen[b] = t;
+        }
+    }
+    __device__ __noinline__ void lk_central_run() {
+        LdoCtWork<C>& w = *ct;
+        w.dir = 1;
+        w.n_cen = 0;
+        int kd = rng.uniform_int(1, ns - 2);
+        bool started = false;
+        if (st[kd] == BOUND) {
+            started = true;
+            w.cen[w.n_cen++] = (int16_t)kd;
+            int p = next(kd, -1);
+            #pragma unroll 1
+            while (p >= 0 && st[p] == BOUND && w.n_cen != ns - 1) {
+                w.cen[w.n_cen++] = (int16_t)p;
+                p = next(p, -1);
+            }
+        }
+        if (w.n_cen == ns - 1) {
+            w.n_cen = 0;
+            return;
+        }
+        lk_reverse_cen();
+        bool ended = false;
+        int n = next(kd, 1);
+        #pragma unroll 1
+        while (!ended && n >= 0 && n != kd && w.n_cen < ns) {
+            if (st[n] == BOUND) {
+                started = true;
+                w.cen[w.n_cen++] = (int16_t)n;
+            }
+            else if (started) {
+                ended = true;
+            }
+            n = next(n, 1);
+        }
+        if (cyclic || started) return;
+        n = next(kd, -1);
+        #pragma unroll 1
+        while (!ended && n >= 0 && w.n_cen < ns) {
+            if (st[n] == BOUND) {
+                started = true;
+                w.cen[w.n_cen++] = (int16_t)n;
+            }
+            else if (started) {
+                ended = true;
+            }
+            n = next(n, -1);
+        }
+        lk_reverse_cen();
+    }
+    // ClusteredLinkerRegrowthMCMovetype::select_and_setup_segments (:607):
+    // linkers run outwards from the cluster over domains that are not bound
+    __device__ __noinline__ bool lk_select_clustered() {
+        LdoCtWork<C>& w = *ct;
+        int maxl = sys->move_opt[cur_mv][LDO_MO_MAX_LINKER];
+        bool ext = true;
+        #pragma unroll 1
+        for (int att = 0; ext && att != 10; ++att) {
+            lk_central_run();
+            if (w.n_cen == 0) return false;
+            ext = lk_bound_externally();
+            if (bad()) return false;
+        }
+        if (ext) return false;
+        int first = w.cen[0], last = w.cen[w.n_cen - 1];
+        w.n_lk1 = 0;
+        w.lk[w.n_lk1++] = (int16_t)first;
+        int p = next(first, -1);
+        if (p != last && p != next(last, 1)) {
+            int stop = next(last, 2);
+            #pragma unroll 1
+            while (p >= 0 && st[p] != BOUND && w.n_lk1 != maxl && p != stop) {
+                w.lk[w.n_lk1++] = (int16_t)p;
+                p = next(p, -1);
+            }
+        }
+        if (w.n_lk1 == 1) return false;
+        int l1end = w.lk[w.n_lk1 - 1];
+        w.n_lk2 = 0;
+        w.lk[w.n_lk1 + w.n_lk2++] = (int16_t)last;
+        int q = next(last, 1);
+        if (q != l1end) {
+            int stop = next(l1end, -1);
+            #pragma unroll 1
+            while (q >= 0 && st[q] != BOUND && w.n_lk2 != maxl && q != stop) {
+                w.lk[w.n_lk1 + w.n_lk2++] = (int16_t)q;
+                q = next(q, 1);
+            }
+        }
+        return true;
+    }
+    // setup_fixed_end_biases (:210): the domains past the linkers' far ends as
+    // active endpoints of segments 0 and 1, then the constraint points of
+    // linker 1 (without its central domain, growing against m_dir) and
+    // linker 2 (along it); the recoil-growth stack starts at linker 1's
+    // central domain (CTRGLinkerRegrowthMCMovetype, :1161)
+    __device__ __noinline__ void lk_setup_constraints() {
+        LdoCtWork<C>& w = *ct;
+        int dir = w.dir;
+        int e1 = next(w.lk[w.n_lk1 - 1], -dir);
+        int e2 = next(w.lk[w.n_lk1 + w.n_lk2 - 1], dir);
+        w.lk_end[0] = (int16_t)e1;
+        w.lk_end[1] = (int16_t)e2;
+        if (e1 >= 0) ct_add_ep_seg(e1, pos(e1), 0);
+        if (e2 >= 0) ct_add_ep_seg(e2, pos(e2), 1);
+        int n = 0;
+        #pragma unroll 1
+        for (int k = 1; k < w.n_lk1; ++k) w.seg_dom[n++] = w.lk[k];
+        w.seg_off[0] = 0;
+        w.seg_off[1] = (int16_t)n;
+        #pragma unroll 1
+        for (int k = 1; k < w.n_lk2; ++k) w.seg_dom[n++] = w.lk[w.n_lk1 + k];
+        w.seg_off[2] = (int16_t)n;
+        w.n_segs = 2;
+        w.seg_dirin[0] = (int8_t)(-dir);
+        w.seg_dirin[1] = (int8_t)dir;
+        w.rd[0] = w.lk[0];
+        w.n_rd = 1;
+        ct_calc_constraintpoints();
+    }
+    __device__ void lk_save_unassign(int d) {
+        LdoCtWork<C>& w = *ct;
+        w.p_old[d] = pos(d);
+        w.o_old[d] = ore[d];
+        unassign_domain(d);
+    }
+    __device__ void lk_reset_segment(int n) {   // reset_segment (:145)
+        LdoCtWork<C>& w = *ct;
+        #pragma unroll 1
+        for (int k = 0; k < n; ++k) unassign_domain(w.cdom[k]);
+    }
+    // steps_less_than_distance (:524): a linker's central end farther (in
+    // lattice steps) from its far end than the linker has domains
+    __device__ bool lk_steps_less() {
+        LdoCtWork<C>& w = *ct;
+        int dist[2] = {0, 0};
+        #pragma unroll 1
+        for (int k = 0; k < 2; ++k) {
+            int e = w.lk_end[k];
+            if (e < 0) continue;
+            V3 d = sub(pos(w.lk[k == 0 ? 0 : w.n_lk1]), pos(e));
+            dist[k] = abs(vx(d)) + abs(vy(d)) + abs(vz(d));
+        }
+        return !(dist[0] <= w.n_lk1 && dist[1] <= w.n_lk2);
+    }
+    // apply_transformation (:401) of the central domains from src
+    __device__ __noinline__ double lk_apply(const long long* src_p, const uint8_t* src_o, V3 disp, V3 center,
+                                            int axis, int turns) {
+        LdoCtWork<C>& w = *ct;
+        double de = 0;
+        #pragma unroll 1
+        for (int k = 0; k < w.n_cdom; ++k) {
+            int d = w.cdom[k];
+            V3 p = lk_place(src_p[d], center, axis, turns, disp);
+            int o = lk_orient(src_o[d], axis, turns);
+            int occ = occupancy(p);
+            if (occ == BOUND || occ == MISBOUND) {
+                lk_reset_segment(k);
+                return 0;
+            }
+            if (occ == UNBOUND) {
+                int ud = unbound_at(p);
+                bool scaf_mis = scs[d] == 0 && scs[ud] == 0;
+                bool new_pair = !lk_in(w.cdom, w.n_cdom, ud);
+                if (!scaf_mis && new_pair) {
+                    lk_reset_segment(k);
+                    return 0;
+                }
+                if (scaf_mis && new_pair) {   // check_domain_constraints
+                    probe_domain(d, p, o);
+                    if (bad()) return 0;
+                    if (hdr.violated) {
+                        hdr.violated = 0;
+                        lk_reset_segment(k);
+                        return 0;
+                    }
+                }
+            }
+            de += set_checked(d, p, o);
+            if (bad()) return 0;
+        }
+        return dexp(-de);
+    }
+    // transform_segment (:316), and with rev revert_transformation (:467):
+    // the trial transformations of the central domains from src (centre: a
+    // central segment domain's src position), each counted with its
+    // Boltzmann factor when both linkers can still reach their ends; the
+    // forward move then places one chosen by those weights, the reverse
+    // places the old configuration and adds its per-domain factors
+    __device__ __noinline__ double lk_transform(const long long* src_p, const uint8_t* src_o, bool rev) {
+        LdoCtWork<C>& w = *ct;
+        const int* mo = sys->move_opt[cur_mv];
+        int K = mo[LDO_MO_NUM_TRANSFORMS] - (rev ? 1 : 0);
+        int maxt = mo[LDO_MO_MAX_TURNS], maxd = mo[LDO_MO_MAX_DISP];
+        double bias = 0;
+        w.n_tr = 0;
+        #pragma unroll 1
+        for (int k = 0; k < K && !bad(); ++k) {
+            int ci = rng.uniform_int(0, w.n_cen - 1);
+            V3 center = src_p[w.cen[ci]];
+            int axis = rng.uniform_int(0, 2);
+            int turns = rng.uniform_int(0, maxt);
+            int dx = rng.uniform_int(-maxd, maxd);
+            int dy = rng.uniform_int(-maxd, maxd);
+            int dz = rng.uniform_int(-maxd, maxd);
+            V3 disp = mk(dx, dy, dz);
+            double bf = lk_apply(src_p, src_o, disp, center, axis, turns);
+            if (bf == 0) continue;
+            if (!lk_steps_less()) {
+                if (rev) {
+                    bias += bf;
+                }
+                else {
+                    int t = w.n_tr++;
+                    w.tr_center[t] = center;
+                    w.tr_disp[t] = disp;
+                    w.tr_axis[t] = (int8_t)axis;
+                    w.tr_turns[t] = (int8_t)turns;
+                    w.tr_bf[t] = bf;
+                }
+            }
+            lk_reset_segment(w.n_cdom);
+        }
+        if (bad()) return 0;
+        if (rev) {
+            #pragma unroll 1
+            for (int k = 0; k < w.n_cdom; ++k) {
+                int d = w.cdom[k];
+                bias += dexp(-set_checked(d, w.p_old[d], w.o_old[d]));
+            }
+            return bias;
+        }
+        #pragma unroll 1
+        for (int t = 0; t < w.n_tr; ++t) bias += w.tr_bf[t];
+        if (bias == 0) {
+            rejected = true;
+            return bias;
+        }
+        double r = bias * rng.uniform_real();
+        double cum = 0;
+        int t = 0;
+        #pragma unroll 1
+        for (; t < w.n_tr - 1; ++t) {
+            cum += w.tr_bf[t];
+            if (r < cum) break;
+        }
+        lk_apply(src_p, src_o, w.tr_disp[t], w.tr_center[t], w.tr_axis[t], w.tr_turns[t]);
+        return bias;
+    }
+    // The first phase of the linker movetypes: selection, constraint points,
+    // the central domains, and the unassignment of everything that moves
+    // (CTCB: linkers, regrown staples, central domains, then snapshot 1;
+    // CTRG: the regrowth stack and the central domains, then the new
+    // configuration's transformation and recoil growth).
+    __device__ __noinline__ int lk_begin(int kind) {
+        LdoCtWork<C>& w = *ct;
+        ct_clear();
+        w.kind = kind;
+        w.delta_e = 0;
+        w.weight = 1;
+        w.weight_new = 1;
+        const int* mo = sys->move_opt[cur_mv];
+        w.max_recoils = mo[LDO_MO_MAX_RECOILS];
+        w.max_c_attempts = mo[LDO_MO_MAX_C_ATTEMPTS];
+        bool ok = kind == LDO_MV_CTCB_CLINKER ? lk_select_clustered() : lk_select();
+        if (!ok || bad()) return finish_move(false, 0);
+        lk_setup_constraints();
+        if (bad()) return finish_move(false, 0);
+        lk_central_domains();
+        if (bad()) return finish_move(false, 0);
+        if (kind == LDO_MV_CTRG_LINKER) {   // CTRGLinkerRegrowthMCMovetype::internal_attempt_move (:1148)
+            if (w.n_rd < 2) return finish_move(false, 0);   // nothing to regrow: the reference reads past its stack
+            w.p_old[w.rd[0]] = pos(w.rd[0]);
+            w.o_old[w.rd[0]] = ore[w.rd[0]];
+            #pragma unroll 1
+            for (int k = 1; k < w.n_rd; ++k) {
+                int d = w.rd[k];
+                w.p_old[d] = pos(d);
+                w.o_old[d] = ore[d];
+                w.delta_e += unassign_domain(d);
+            }
+            w.n_eq = 0;
+            #pragma unroll 1
+            for (int k = 0; k < w.n_cdom; ++k) lk_save_unassign(w.cdom[k]);
+            w.weight *= lk_transform(w.p_old, w.o_old, false);
+            if (rejected || bad()) return finish_move(false, 0);
+            w.delta_e += rg_recoil_regrow();
+            if (rejected || bad()) return finish_move(false, 0);
+            update_move_params();   // add_external_bias (:84)
+            w.delta_e += calc_move();
+            // setup_for_calc_new_weights (:137): the new configuration
+            #pragma unroll 1
+            for (int k = 0; k < w.n_rd; ++k) {
+                int d = w.rd[k];
+                w.p_new[d] = pos(d);
+                w.o_new[d] = ore[d];
+                w.catt_wq[k] = w.catt_q[k];
+                w.av_wq[k] = w.av_q[k];
+            }
+            #pragma unroll 1
+            for (int k = 0; k < w.n_cdom; ++k) {
+                int d = w.cdom[k];
+                w.p_new[d] = pos(d);
+                w.o_new[d] = ore[d];
+            }
+            phase = PH_LKR2;
+            return CMD_SNAP(2) | CMD_MORE;
+        }
+        // CTCBLinkerRegrowthMCMovetype::internal_attempt_move (:859)
+        #pragma unroll 1
+        for (int k = 1; k < w.n_lk1; ++k) lk_save_unassign(w.lk[k]);
+        #pragma unroll 1
+        for (int k = 1; k < w.n_lk2; ++k) lk_save_unassign(w.lk[w.n_lk1 + k]);
+        unsigned long long left = w.regrow;
+        #pragma unroll 1
+        while (left) {
+            int best = -1;
+            #pragma unroll 1
+            for (unsigned long long m = left; m; m &= m - 1ull) {
+                int cs = __ffsll((long long)m) - 1;
+                if (best < 0 || chain_c[cs] < chain_c[best]) best = cs;
+            }
+            left &= ~(1ull << best);
+            int len = chain_len(best);
+            #pragma unroll 1
+            for (int q = 0; q < len; ++q) lk_save_unassign(slot_of(best, q));
+        }
+        #pragma unroll 1
+        for (int k = 0; k < w.n_cdom; ++k) lk_save_unassign(w.cdom[k]);
+        phase = PH_LK2;
+        return CMD_SNAP(1) | CMD_MORE;
+    }
+    __device__ __noinline__ int lk_cb_new() {
+        LdoCtWork<C>& w = *ct;
+        regrow_old = false;
+        w_bias *= lk_transform(w.p_old, w.o_old, false);
+        if (rejected || bad()) return finish_move(false, 0);
+        ct_grow_list(2, 0, w.n_lk1);
+        if (rejected || bad()) return finish_move(false, 0);
+        ct_grow_list(2, w.n_lk1, w.n_lk2);
+        if (rejected || bad()) return finish_move(false, 0);
+        update_move_params();   // add_external_bias (:52)
+        w_bias *= dexp(-calc_move());
+        // setup_for_regrow_old (:215); the transformations of the old pass
+        // start from the central domains' new configuration
+        regrow_old = true;
+        w_new_bias = w_bias;
+        new_modifier = modifier;
+        w_bias = 1;
+        #pragma unroll 1
+        for (int k = 0; k < w.n_cdom; ++k) {
+            int d = w.cdom[k];
+            w.p_new[d] = pos(d);
+            w.o_new[d] = ore[d];
+        }
+        phase = PH_LK3;
+        return CMD_SNAP(2) | CMD_REST(1) | CMD_MORE;
+    }
+    __device__ __noinline__ int lk_cb_old() {
+        LdoCtWork<C>& w = *ct;
+        ct_reset_endpoints();
+        w_bias *= lk_transform(w.p_new, w.o_new, true);
+        if (bad()) return finish_move(false, 0);
+        // both linkers grow in the old configuration whatever the first did
+        ct_grow_list(2, 0, w.n_lk1);
+        ct_grow_list(2, w.n_lk1, w.n_lk2);
+        if (bad()) return finish_move(false, 0);
+        modifier = 1;
+        double ratio = w_new_bias / w_bias;   // test_cb_acceptance (:182)
+        bool acc = test_acceptance(ratio);
+        return finish_move(acc, acc ? 2 : 0);
+    }
+    // CTRGLinkerRegrowthMCMovetype, from the weights of the new configuration
+    // to the acceptance test (:1181-1211)
+    __device__ __noinline__ int lk_rg_weigh() {
+        LdoCtWork<C>& w = *ct;
+        #pragma unroll 1
+        for (int k = 1; k < w.n_rd; ++k) unassign_domain(w.rd[k]);   // unassign_and_save_domains
+        w.n_eq = 0;
+        ct_reset_endpoints();
+        rg_calc_weights(w.p_new, w.o_new);
+        if (bad()) return finish_move(false, 0);
+        #pragma unroll 1
+        for (int k = 1; k < w.n_rd; ++k) unassign_domain(w.rd[k]);   // unassign_domains
+        w.n_eq = 0;
+        #pragma unroll 1
+        for (int k = 0; k < w.n_cdom; ++k) unassign_domain(w.cdom[k]);
+        w.weight /= lk_transform(w.p_new, w.o_new, true);
+        if (bad()) return finish_move(false, 0);
+        ct_reset_endpoints();
+        rg_calc_old_c_opens();
+        if (bad()) return finish_move(false, 0);
+        // setup_for_calc_old_weights (:146)
+        w.weight_new = w.weight;
+        w.weight = 1;
+        #pragma unroll 1
+        for (int k = 0; k < w.n_rd; ++k) {
+            w.catt_wq[k] = w.catt_q[k];
+            w.av_wq[k] = w.av_q[k];
+        }
+        #pragma unroll 1
+        for (int k = 1; k < w.n_rd; ++k) unassign_domain(w.rd[k]);   // unassign_and_save_domains
+        w.n_eq = 0;
+        ct_reset_endpoints();
+        rg_calc_weights(w.p_old, w.o_old);
+        if (bad()) return finish_move(false, 0);
+        double ratio = w.weight_new / w.weight * dexp(-w.delta_e);   // test_rg_acceptance (:515)
+        bool acc = test_acceptance(ratio);
+        return finish_move(acc, acc ? 2 : 0);
+    }
+
     // GCMCSimulation::simulate, one step (src/simulation.cpp:575-619), as a
     // state machine: step_begin runs the move until it needs the warp to copy
     // snapshots, step_resume continues it, and each returns the next CMD_*
@@ -3941,6 +4569,13 @@ struct Rep : public LdoState<C> {
             }
             fail(LDO_RS_INVARIANT);
             return 0;
+        }
+        if constexpr (CT) {   // scaffold transforms with linker regrowth
+            if (kind >= LDO_MV_CTCB_LINKER && kind <= LDO_MV_CTRG_LINKER) {
+                if (ct) return lk_begin(kind);
+                fail(LDO_RS_INVARIANT);
+                return 0;
+            }
         }
         bool acc = false;
         switch (kind) {
@@ -4005,6 +4640,9 @@ struct Rep : public LdoState<C> {
             if (phase == PH_RG5) return rg_weigh_old();
             if (phase == PH_CT2) return ctcb_new();
             if (phase == PH_CT3) return ctcb_old();
+            if (phase == PH_LK2) return lk_cb_new();
+            if (phase == PH_LK3) return lk_cb_old();
+            if (phase == PH_LKR2) return lk_rg_weigh();
         }
         phase = 0;
         if (recalc) {

@@ -74,9 +74,13 @@ int move_kind(const string& t) {
     if (t == "CTRGJumpScaffoldRegrowth") return LDO_MV_CTRG_JUMP;
     if (t == "CTCBScaffoldRegrowth") return LDO_MV_CTCB;
     if (t == "CTCBJumpScaffoldRegrowth") return LDO_MV_CTCB_JUMP;
-    if (t == "CTCBLinkerRegrowth" || t == "CTCBClusteredLinkerRegrowth" || t == "CTRGLinkerRegrowth" ||
-        t == "CTRGClusteredLinkerRegrowth")
-        throw LdoError(LDO_EINVAL, t + ": linker (scaffold transform) movetypes are not implemented by this engine");
+    if (t == "CTCBLinkerRegrowth") return LDO_MV_CTCB_LINKER;
+    if (t == "CTCBClusteredLinkerRegrowth") return LDO_MV_CTCB_CLINKER;
+    if (t == "CTRGLinkerRegrowth") return LDO_MV_CTRG_LINKER;
+    // accepted by the reference's type check but never constructed there
+    // (GCMCSimulation::setup_scaffold_transform_movetype, src/simulation.cpp:445)
+    if (t == "CTRGClusteredLinkerRegrowth")
+        throw LdoError(LDO_EINVAL, t + ": the reference builds no such movetype");
     throw LdoError(LDO_EINVAL, t + ": no such movetype");
 }
 
@@ -178,7 +182,29 @@ HostSystem load_system(const string& inp, const string& overrides) {
         d.move_opt[m][LDO_MO_MAX_SEG_REGROWTH] = ms.max_seg_regrowth;
         d.move_opt[m][LDO_MO_MAX_RECOILS] = ms.max_num_recoils;
         d.move_opt[m][LDO_MO_MAX_C_ATTEMPTS] = ms.max_c_attempts;
+        d.move_opt[m][LDO_MO_MAX_DISP] = ms.max_disp;
+        d.move_opt[m][LDO_MO_MAX_TURNS] = ms.max_turns;
+        d.move_opt[m][LDO_MO_MAX_LINKER] = ms.max_linker_length;
+        d.move_opt[m][LDO_MO_NUM_TRANSFORMS] = ms.num_transforms;
         int k = d.move_kind[m];
+        if (k >= LDO_MV_CTCB_LINKER && k <= LDO_MV_CTRG_LINKER) {
+            d.has_ct = 1;
+            // uniform_int(2, max_linker_length + 1) for the linker lengths,
+            // uniform_int(1, min(ns, max_regrowth)) for the central segment
+            // (src/transform_movetypes.cpp:156, src/movetypes.cpp:469), and
+            // the clustered kernel domain uniform_int(1, ns - 2) (:670)
+            if (ms.num_transforms < 1 || ms.num_transforms > LDO_CT_MAX_TRANSFORMS)
+                throw LdoError(LDO_EINVAL, ms.type + ": num_transforms must be 1.." +
+                                               std::to_string(LDO_CT_MAX_TRANSFORMS));
+            if (ms.max_disp < 0 || ms.max_turns < 0 || ms.max_linker_length < 1)
+                throw LdoError(LDO_EINVAL, ms.type + ": max_disp and max_turns must not be negative and "
+                                                     "max_linker_length must be positive");
+            if (d.ns < 3) throw LdoError(LDO_EINVAL, ms.type + ": the scaffold needs at least 3 domains");
+            if (k != LDO_MV_CTCB_CLINKER && ms.max_regrowth < 1)
+                throw LdoError(LDO_EINVAL, ms.type + ": max_regrowth must be at least 1");
+            if (k == LDO_MV_CTRG_LINKER && (ms.max_c_attempts < 1 || ms.max_c_attempts > 36 || ms.max_num_recoils < 0))
+                throw LdoError(LDO_EINVAL, ms.type + ": max_c_attempts must be 1..36 and max_num_recoils >= 0");
+        }
         if (k >= LDO_MV_CTRG && k <= LDO_MV_CTCB_JUMP) {
             d.has_ct = 1;
             // the reference draws uniform_int(2, max_regrowth) and keeps at

@@ -600,6 +600,10 @@ struct MoveSpec {
     int max_seg_regrowth {0};
     int max_num_recoils {0};
     int max_c_attempts {0};
+    int max_disp {0};
+    int max_turns {0};
+    int max_linker_length {0};
+    int num_transforms {0};
 };
 
 // utility::Fraction (src/utility.cpp:266): "a/b" or a plain real number.
@@ -627,6 +631,10 @@ inline vector<MoveSpec> movetypes_from_json(const JVal& root) {
         ms.max_seg_regrowth = m["max_seg_regrowth"].as_int();
         ms.max_num_recoils = m["max_num_recoils"].as_int();
         ms.max_c_attempts = m["max_c_attempts"].as_int();
+        ms.max_disp = m["max_disp"].as_int();
+        ms.max_turns = m["max_turns"].as_int();
+        ms.max_linker_length = m["max_linker_length"].as_int();
+        ms.num_transforms = m["num_transforms"].as_int();
         out.push_back(ms);
     }
     return out;

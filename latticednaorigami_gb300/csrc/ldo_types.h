@@ -34,9 +34,25 @@ enum LdoMove {
     LDO_MV_CTRG_JUMP = 6,         // CTRGJumpScaffoldRegrowth
     LDO_MV_CTCB = 7,              // CTCBScaffoldRegrowth
     LDO_MV_CTCB_JUMP = 8,         // CTCBJumpScaffoldRegrowth
-    LDO_MV_LEARNED_REGROWTH = 9   // engine extension: Met regrowth with learned directions
+    LDO_MV_LEARNED_REGROWTH = 9,  // engine extension: Met regrowth with learned directions
+    // scaffold transforms with linker regrowth (src/transform_movetypes.cpp)
+    LDO_MV_CTCB_LINKER = 10,      // CTCBLinkerRegrowth
+    LDO_MV_CTCB_CLINKER = 11,     // CTCBClusteredLinkerRegrowth
+    LDO_MV_CTRG_LINKER = 12       // CTRGLinkerRegrowth
 };
-enum LdoMoveOpt { LDO_MO_MAX_REGROWTH = 0, LDO_MO_MAX_SEG_REGROWTH, LDO_MO_MAX_RECOILS, LDO_MO_MAX_C_ATTEMPTS };
+enum LdoMoveOpt {
+    LDO_MO_MAX_REGROWTH = 0,
+    LDO_MO_MAX_SEG_REGROWTH,
+    LDO_MO_MAX_RECOILS,
+    LDO_MO_MAX_C_ATTEMPTS,
+    LDO_MO_MAX_DISP,          // linker movetypes: translation range per axis
+    LDO_MO_MAX_TURNS,         // linker movetypes: quarter turns of the rotation
+    LDO_MO_MAX_LINKER,        // linker movetypes: max_linker_length
+    LDO_MO_NUM_TRANSFORMS,    // linker movetypes: trial transformations per configuration
+    LDO_N_MOVE_OPTS
+};
+// trial transformations of a linker move kept for the Rosenbluth choice
+#define LDO_CT_MAX_TRANSFORMS 32
 
 enum LdoOp {
     LDO_OP_NUMSTAPLES = 0,
@@ -76,7 +92,7 @@ struct LdoSys {
     int n_moves;
     int move_kind[LDO_MAX_MOVES];
     double move_cum[LDO_MAX_MOVES];
-    int move_opt[LDO_MAX_MOVES][4];   // scaffold regrowth options (LdoMoveOpt)
+    int move_opt[LDO_MAX_MOVES][LDO_N_MOVE_OPTS];   // scaffold regrowth options (LdoMoveOpt)
     int has_ct;                       // some movetype regrows the scaffold
     int adaptive_exchange, allow_nonsensical;
     double exchange_mults[LDO_MAX_TYPES];

@@ -36,6 +36,9 @@ int move_kind(const std::string& t) {
     if (t == "CTRGJumpScaffoldRegrowth") return MV_CTRG_JUMP;
     if (t == "CTCBScaffoldRegrowth") return MV_CTCB_SCAFFOLD;
     if (t == "CTCBJumpScaffoldRegrowth") return MV_CTCB_JUMP;
+    if (t == "CTCBLinkerRegrowth") return MV_CTCB_LINKER;
+    if (t == "CTCBClusteredLinkerRegrowth") return MV_CTCB_CLINKER;
+    if (t == "CTRGLinkerRegrowth") return MV_CTRG_LINKER;
     throw std::runtime_error(t + ": movetype not supported by the oracle");
 }
 
@@ -98,7 +101,8 @@ Replica* build(const char* inp_path, const char* overrides, uint32_t seed, uint3
         size_t S = c.identities.size() - 1;
         for (auto& mv : moves) {
             c.move_kinds.push_back(move_kind(mv.type));
-            c.move_opts.push_back({mv.max_regrowth, mv.max_seg_regrowth, mv.max_num_recoils, mv.max_c_attempts});
+            c.move_opts.push_back({mv.max_regrowth, mv.max_seg_regrowth, mv.max_num_recoils, mv.max_c_attempts,
+                                   mv.max_disp, mv.max_turns, mv.max_linker_length, mv.num_transforms});
             cum += mv.freq;
             c.move_cum.push_back(cum);
             if (mv.type == "MetStapleExchange" || mv.type == "LearnedStapleExchange") {

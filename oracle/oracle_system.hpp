@@ -43,6 +43,8 @@ struct V3 {
 
 // Order matters: random index -> direction (include/.../utility.hpp:156-162).
 static const V3 kUnit[6] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+// utility::basis_vectors (include/.../utility.hpp)
+static const V3 kBasis[3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
 
 // VectorThree::rotate_half (src/utility.cpp:68)
 inline V3 rotate_half(V3 v, V3 axis) {
@@ -193,7 +195,7 @@ struct BiasRec {
 
 enum MoveKind { MV_ORIENTATION = 0, MV_MET_EXCHANGE = 1, MV_MET_REGROWTH = 2, MV_CB_REGROWTH = 3, MV_LEARNED_EXCHANGE = 4,
                 MV_CTRG_SCAFFOLD = 5, MV_CTRG_JUMP = 6, MV_CTCB_SCAFFOLD = 7, MV_CTCB_JUMP = 8,
-                MV_LEARNED_REGROWTH = 9 };
+                MV_LEARNED_REGROWTH = 9, MV_CTCB_LINKER = 10, MV_CTCB_CLINKER = 11, MV_CTRG_LINKER = 12 };
 
 // Options of a scaffold regrowth movetype (src/simulation.cpp:400-560).
 struct ScaffoldMoveOpts {
@@ -201,6 +203,11 @@ struct ScaffoldMoveOpts {
     int max_seg_regrowth {0};
     int max_num_recoils {0};
     int max_c_attempts {0};
+    // linker movetypes (src/simulation.cpp:445)
+    int max_disp {0};
+    int max_turns {0};
+    int max_linker_length {0};
+    int num_transforms {0};
 };
 
 // IdealRandomWalks::num_walks (src/ideal_random_walk.cpp:14): the number of
@@ -3074,6 +3081,418 @@ class System {
         return ctcb_test_acceptance();
     }
 
+
+    // ================================= scaffold transforms with linkers ===
+    // LinkerRegrowthMCMovetype, ClusteredLinkerRegrowthMCMovetype and the
+    // CTCB / CTRG linker movetypes (src/transform_movetypes.cpp).
+    std::vector<int> lk1, lk2, lk_cen, lk_cdom;
+    int lk_end[2] {-1, -1};   // m_linker_endpoints
+
+    // scan_for_external_scaffold_domain (:262)
+    bool lk_scan_external(int dom, std::set<int>& part) {
+        bool ext = false;
+        int c_i = doms[dom].c;
+        part.insert(c_i);
+        for (int cur : get_chain(c_i)) {
+            if (cur == dom) continue;
+            int b = doms[cur].bound;
+            if (b < 0) continue;
+            if (doms[b].c == doms[dom].c) continue;
+            if (doms[b].c == scaffold_c()) {
+                if (!has(lk_cen, b)) {
+                    ext = true;
+                    break;
+                }
+                continue;
+            }
+            if (part.count(doms[b].c)) continue;
+            ext = lk_scan_external(b, part);
+            if (ext) break;
+        }
+        return ext;
+    }
+    bool lk_bound_externally() {   // domains_bound_externally (:238)
+        for (int d : lk_cen) {
+            if (doms[d].state == UNBOUND) continue;
+            int b = doms[d].bound;
+            if (doms[b].c == scaffold_c()) continue;
+            std::set<int> part {doms[d].c};
+            if (lk_scan_external(b, part)) return true;
+        }
+        return false;
+    }
+    // LinkerRegrowthMCMovetype::select_and_setup_segments (:156)
+    bool lk_select(const ScaffoldMoveOpts& mo) {
+        bool ext = true;
+        int attempts = 0;
+        while (ext && attempts != 10) {
+            lk1.clear();
+            lk2.clear();
+            lk_cen = select_indices(1, 0, mo.max_regrowth);
+            int len1 = rng.uniform_int(2, mo.max_linker_length + 1);
+            int d = lk_cen.front();
+            int stop = next(lk_cen.back(), 2 * ct_dir);
+            while ((int)lk1.size() != len1 && d >= 0 && d != stop) {
+                lk1.push_back(d);
+                d = next(d, -ct_dir);
+            }
+            if (cfg.cyclic && lk1.size() == 1) return false;
+            int len2 = rng.uniform_int(2, mo.max_linker_length + 1);
+            d = lk_cen.back();
+            stop = next(lk1.back(), -ct_dir);
+            while ((int)lk2.size() != len2 && d >= 0 && d != stop) {
+                lk2.push_back(d);
+                d = next(d, ct_dir);
+            }
+            ext = lk_bound_externally();
+            attempts++;
+        }
+        return !ext;
+    }
+    // ClusteredLinkerRegrowthMCMovetype::linear_select_central_segment (:670)
+    std::vector<int> lk_linear_central() {
+        ct_dir = 1;
+        std::vector<int> cen;
+        const std::vector<int>& sc = chains[0];
+        int kernel = rng.uniform_int(1, (int)sc.size() - 2);
+        bool started = false;
+        int kd = sc[kernel];
+        if (doms[kd].state == BOUND) {
+            started = true;
+            cen.push_back(kd);
+            int p = next(kd, -1);
+            while (p >= 0 && doms[p].state == BOUND && cen.size() != sc.size() - 1) {
+                cen.push_back(p);
+                p = next(p, -1);
+            }
+        }
+        if (cen.size() == sc.size() - 1) return {};
+        std::reverse(cen.begin(), cen.end());
+        int n = next(kd, 1);
+        bool ended = false;
+        while (!ended && n >= 0) {
+            if (doms[n].state == BOUND) {
+                started = true;
+                cen.push_back(n);
+            }
+            else if (started) {
+                ended = true;
+            }
+            n = next(n, 1);
+        }
+        n = next(kd, -1);
+        if (!started) {
+            while (!ended && n >= 0) {
+                if (doms[n].state == BOUND) {
+                    started = true;
+                    cen.push_back(n);
+                }
+                else if (started) {
+                    ended = true;
+                }
+                n = next(n, -1);
+            }
+            std::reverse(cen.begin(), cen.end());
+        }
+        return cen;
+    }
+    // ClusteredLinkerRegrowthMCMovetype::cyclic_select_central_segment (:734)
+    std::vector<int> lk_cyclic_central() {
+        ct_dir = 1;
+        std::vector<int> cen;
+        const std::vector<int>& sc = chains[0];
+        int kernel = rng.uniform_int(1, (int)sc.size() - 2);
+        bool started = false;
+        int kd = sc[kernel];
+        if (doms[kd].state == BOUND) {
+            started = true;
+            cen.push_back(kd);
+            int p = next(kd, -1);
+            while (doms[p].state == BOUND && cen.size() != sc.size() - 1) {
+                cen.push_back(p);
+                p = next(p, -1);
+            }
+        }
+        if (cen.size() == sc.size() - 1) return {};
+        std::reverse(cen.begin(), cen.end());
+        int n = next(kd, 1);
+        bool ended = false;
+        while (!ended && n != kd) {
+            if (doms[n].state == BOUND) {
+                started = true;
+                cen.push_back(n);
+            }
+            else if (started) {
+                ended = true;
+            }
+            n = next(n, 1);
+        }
+        return cen;
+    }
+    // ClusteredLinkerRegrowthMCMovetype::select_and_setup_segments (:607)
+    bool lk_select_clustered(const ScaffoldMoveOpts& mo) {
+        bool ext = true;
+        int attempts = 0;
+        while (ext && attempts != 10) {
+            lk_cen = cfg.cyclic ? lk_cyclic_central() : lk_linear_central();
+            if (lk_cen.empty()) return false;
+            ext = lk_bound_externally();
+            attempts++;
+        }
+        if (ext) return false;
+        lk1.clear();
+        lk2.clear();
+        int maxl = mo.max_linker_length;
+        lk1.push_back(lk_cen[0]);
+        int p = next(lk_cen[0], -1);
+        if (p != lk_cen.back() && p != next(lk_cen.back(), 1)) {
+            while (p >= 0 && doms[p].state != BOUND && (int)lk1.size() != maxl && p != next(lk_cen.back(), 2)) {
+                lk1.push_back(p);
+                p = next(p, -1);
+            }
+        }
+        if (lk1.size() == 1) return false;
+        lk2.push_back(lk_cen.back());
+        int n = next(lk_cen.back(), 1);
+        if (n != lk1.back()) {
+            while (n >= 0 && doms[n].state != BOUND && (int)lk2.size() != maxl && n != next(lk1.back(), -1)) {
+                lk2.push_back(n);
+                n = next(n, 1);
+            }
+        }
+        return true;
+    }
+    // setup_fixed_end_biases (:210)
+    void lk_setup_fixed_ends() {
+        lk_end[0] = next(lk1.back(), -ct_dir);
+        lk_end[1] = next(lk2.back(), ct_dir);
+        for (int seg = 0; seg < 2; ++seg)
+            if (lk_end[seg] >= 0) add_active_endpoint_seg(lk_end[seg], doms[lk_end[seg]].pos, seg);
+        std::vector<std::vector<int>> segs {{lk1.begin() + 1, lk1.end()}, {lk2.begin() + 1, lk2.end()}};
+        calculate_constraintpoints(segs, {-ct_dir, ct_dir});
+    }
+    // the central segment and the staples bound within it (find_staples, src/movetypes.cpp:179)
+    void lk_central_domains() {
+        std::set<int> staples;
+        for (int d : lk_cen) {
+            int b = doms[d].bound;
+            if (b >= 0 && doms[b].c != 0) scan_for_scaffold(b, staples);
+        }
+        lk_cdom = lk_cen;
+        for (int c : staples)
+            for (int id : get_chain(c)) lk_cdom.push_back(id);
+    }
+    void lk_reset_segment(size_t n) {   // reset_segment (:145)
+        for (size_t k = 0; k < n; ++k) {
+            unassign_domain(lk_cdom[k]);
+            assigned.pop_back();
+        }
+    }
+    bool lk_steps_less() {   // steps_less_than_distance (:524)
+        int d1 = lk_end[0] >= 0 ? (doms[lk1[0]].pos - doms[lk_end[0]].pos).abssum() : 0;
+        int d2 = lk_end[1] >= 0 ? (doms[lk2[0]].pos - doms[lk_end[1]].pos).abssum() : 0;
+        return !(d1 <= (int)lk1.size() && d2 <= (int)lk2.size());
+    }
+    static V3 lk_rot(V3 v, V3 origin, V3 axis, int turns) {   // VectorThree::rotate(origin, axis, turns)
+        if (turns == 0) return v;
+        return rotate_quarter(v - origin, axis, turns) + origin;
+    }
+    // apply_transformation (:401) from the positions in ct_prev_pos
+    double lk_apply(V3 disp, V3 center, V3 axis, int turns) {
+        double bf = 1, de = 0;
+        for (size_t di = 0; di < lk_cdom.size(); ++di) {
+            int d = lk_cdom[di];
+            V3 p = lk_rot(ct_prev_pos.at(d), center, axis, turns) + disp;
+            V3 o = lk_rot(ct_prev_ore.at(d), V3(0, 0, 0), axis, turns);
+            int occ = occupancy(p);
+            if (occ == BOUND || occ == MISBOUND) {
+                lk_reset_segment(di);
+                bf = 0;
+                break;
+            }
+            if (occ == UNBOUND) {
+                int ud = unbound_at(p);
+                bool scaf_mis = doms[d].c == scaffold_c() && doms[ud].c == scaffold_c();
+                bool new_pair = !has(lk_cdom, ud);
+                if (!scaf_mis && new_pair) {
+                    lk_reset_segment(di);
+                    bf = 0;
+                    break;
+                }
+                if (scaf_mis && new_pair) {
+                    check_domain_constraints(d, p, o);
+                    if (violated) {
+                        bf = 0;
+                        violated = false;
+                        lk_reset_segment(di);
+                        break;
+                    }
+                }
+            }
+            de += set_checked(d, p, o);
+            assigned.push_back(key_of(d));
+        }
+        if (bf != 0) bf = xexp(-de);
+        return bf;
+    }
+    // transform_segment (:316); with rev, revert_transformation (:467)
+    double lk_transform(const ScaffoldMoveOpts& mo, bool rev) {
+        std::vector<V3> centers, axes, disps;
+        std::vector<int> turnss;
+        std::vector<double> bfs;
+        double bias = 0;
+        int K = mo.num_transforms - (rev ? 1 : 0);
+        for (int k = 0; k < K; ++k) {
+            int ci = rng.uniform_int(0, (int)lk_cen.size() - 1);
+            V3 center = ct_prev_pos.at(lk_cen[ci]);
+            V3 axis = kBasis[rng.uniform_int(0, 2)];
+            int turns = rng.uniform_int(0, mo.max_turns);
+            V3 disp;
+            disp.x = rng.uniform_int(-mo.max_disp, mo.max_disp);
+            disp.y = rng.uniform_int(-mo.max_disp, mo.max_disp);
+            disp.z = rng.uniform_int(-mo.max_disp, mo.max_disp);
+            double bf = lk_apply(disp, center, axis, turns);
+            if (bf != 0) {
+                if (!lk_steps_less()) {
+                    if (rev) {
+                        bias += bf;
+                    }
+                    else {
+                        centers.push_back(center);
+                        axes.push_back(axis);
+                        turnss.push_back(turns);
+                        disps.push_back(disp);
+                        bfs.push_back(bf);
+                    }
+                }
+                lk_reset_segment(lk_cdom.size());
+            }
+        }
+        if (rev) {
+            for (int d : lk_cdom) {
+                double de = set_checked(d, cb_old_pos.at(d), cb_old_ore.at(d));
+                bias += xexp(-de);
+                assigned.push_back(key_of(d));
+            }
+            return bias;
+        }
+        for (double b : bfs) bias += b;
+        if (bias == 0) {
+            rejected = true;
+            return bias;
+        }
+        double r = bias * rng.uniform_real();
+        double cum = 0;
+        size_t t = 0;
+        for (; t + 1 < bfs.size(); ++t) {
+            cum += bfs[t];
+            if (r < cum) break;
+        }
+        lk_apply(disps[t], centers[t], axes[t], turnss[t]);
+        return bias;
+    }
+    // CTCBLinkerRegrowthMCMovetype::internal_attempt_move (:859), also the
+    // clustered variant (its selection differs)
+    bool ctcb_linker(const ScaffoldMoveOpts& mo, bool clustered) {
+        ctcb_reset();
+        lk_end[0] = lk_end[1] = -1;
+        bool ok = clustered ? lk_select_clustered(mo) : lk_select(mo);
+        if (!ok) return false;
+        lk_setup_fixed_ends();
+        std::set<int> staples = cp.regrowth_staples;
+        lk_central_domains();
+        std::vector<int> u1(lk1.begin() + 1, lk1.end()), u2(lk2.begin() + 1, lk2.end());
+        ctcb_unassign(u1);
+        ctcb_unassign(u2);
+        for (int c : staples) ctcb_unassign(get_chain(c));
+        ctcb_unassign(lk_cdom);
+        w_bias.mul(lk_transform(mo, false));
+        if (rejected) {
+            ct_sync_prev();
+            return false;
+        }
+        ctcb_grow_chain(lk1);
+        if (rejected) {
+            ct_sync_prev();
+            return false;
+        }
+        ctcb_grow_chain(lk2);
+        if (rejected) {
+            ct_sync_prev();
+            return false;
+        }
+        update_move_params();   // add_external_bias (:52)
+        w_bias.mul(xexp(-calc_move()));
+        ctcb_setup_regrow_old();
+        cp.active = cp.initial_active;
+        ctcb_unassign(u1);
+        ctcb_unassign(u2);
+        for (int c : staples) ctcb_unassign(get_chain(c));
+        ctcb_unassign(lk_cdom);
+        w_bias.mul(lk_transform(mo, true));
+        ctcb_grow_chain(lk1);
+        ctcb_grow_chain(lk2);
+        modifier = 1;
+        return ctcb_test_acceptance();
+    }
+    // CTRGLinkerRegrowthMCMovetype::internal_attempt_move (:1148)
+    bool ctrg_linker(const ScaffoldMoveOpts& mo) {
+        rg_reset();
+        lk_end[0] = lk_end[1] = -1;
+        rg_max_recoils = mo.max_num_recoils;
+        rg_max_c_attempts = mo.max_c_attempts;
+        if (!lk_select(mo)) return false;
+        lk_setup_fixed_ends();
+        lk_central_domains();
+        rg_ds = cp.d_stack;
+        rg_ds.insert(rg_ds.begin(), lk1.front());
+        if (rg_ds.size() < 2) throw std::runtime_error("linker regrowth with nothing to regrow");
+        rg_delta_e += rg_unassign_and_save();
+        for (int d : lk_cdom) ct_save_unassign(d, nullptr);
+        rg_weight *= lk_transform(mo, false);
+        if (rejected) {
+            ct_sync_prev();
+            return false;
+        }
+        rg_delta_e += recoil_regrow();
+        if (rejected) {
+            ct_sync_prev();
+            return false;
+        }
+        update_move_params();   // add_external_bias
+        rg_delta_e += calc_move();
+        // setup_for_calc_new_weights (:137)
+        catt_wq = catt_q;
+        avail_wq = avail_q;
+        rg_old_pos = ct_prev_pos;
+        rg_old_ore = ct_prev_ore;
+        cb_old_pos = ct_prev_pos;   // the old configuration revert_transformation places
+        cb_old_ore = ct_prev_ore;
+        modified.clear();
+        rg_unassign_and_save();
+        cp.active = cp.initial_active;
+        rg_calc_weights();
+        // old weights
+        rg_unassign_domains();
+        for (int d : lk_cdom) ct_save_unassign(d, nullptr);
+        rg_weight /= lk_transform(mo, true);
+        cp.active = cp.initial_active;
+        rg_calc_old_c_opens();
+        // setup_for_calc_old_weights (:146)
+        rg_weight_new = rg_weight;
+        rg_weight = 1;
+        catt_wq = catt_q;
+        avail_wq = avail_q;
+        rg_new_pos = ct_prev_pos;
+        rg_new_ore = ct_prev_ore;
+        modified.clear();
+        rg_unassign_and_save();
+        for (int d : lk_cdom) modified.push_back(key_of(d));
+        cp.active = cp.initial_active;
+        rg_calc_weights();
+        return rg_test_acceptance();
+    }
+
     // OrientationRotationMCMovetype::internal_attempt_move (src/orientation_movetype.cpp:30)
     bool orientation_rotation() {
         int dom = select_random_domain();
@@ -3124,6 +3543,9 @@ class System {
         case MV_CTRG_JUMP: acc = ctrg_jump(cfg.move_opts[m]); break;
         case MV_CTCB_SCAFFOLD: acc = ctcb_scaffold(cfg.move_opts[m]); break;
         case MV_CTCB_JUMP: acc = ctcb_jump(cfg.move_opts[m]); break;
+        case MV_CTCB_LINKER: acc = ctcb_linker(cfg.move_opts[m], false); break;
+        case MV_CTCB_CLINKER: acc = ctcb_linker(cfg.move_opts[m], true); break;
+        case MV_CTRG_LINKER: acc = ctrg_linker(cfg.move_opts[m]); break;
         }
         attempts[m]++;
         if (acc) accepts[m]++;

@@ -97,6 +97,16 @@ class TraceSim : public simulation::GCMCSimulation {
     long m_every;
     std::ostream& m_out;
     vector<string> m_dumps;
+    // attempts and accepts of every movetype, in the movetype file's order
+    string move_stats() {
+        std::ostringstream s;
+        s << "[";
+        for (size_t i = 0; i < m_movetypes.size(); ++i)
+            s << (i ? "," : "") << "[" << m_movetypes[i]->get_attempts() << "," << m_movetypes[i]->get_accepts()
+              << "]";
+        s << "]";
+        return s.str();
+    }
 };
 
 // The reference's own annealing loop (AnnealingGCMCSimulation::run,
@@ -221,7 +231,7 @@ int main(int argc, char** argv) {
             // trace_quiet=1: no per-step records (for timing the move loop)
             sim.m_quiet = kv.count("trace_quiet") && kv["trace_quiet"] == "1";
             sim.simulate(steps, 0, false);
-            std::cout << "], \"dumps\": [";
+            std::cout << "], \"move_stats\": " << sim.move_stats() << ", \"dumps\": [";
             for (size_t i = 0; i < sim.m_dumps.size(); ++i) std::cout << (i ? "," : "") << sim.m_dumps[i];
         }
         double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -49,7 +49,9 @@ RUNS = [("c1", 1, 20000), ("c1", 2, 20000), ("g24a", 3, 20000), ("g24b", 4, 2000
         # a run with a weight ratio within a rounding of 1 at step 19885 (long double vs FP64)
         ("s24a", 11, 20000),
         # Dist / AdjacentSite order parameters with biases, on a moving scaffold
-        ("d24", 12, 20000)]
+        ("d24", 12, 20000),
+        # scaffold transforms with linker regrowth (CTCB, clustered CTCB, CTRG)
+        ("l24a", 13, 20000), ("l24b", 14, 20000), ("l24c", 18, 20000), ("l24r", 16, 20000)]
 
 
 def ref_trace(inp, seed, steps, replica=0):

@@ -155,6 +155,29 @@ MOVES = {
               ("Contiguous CTCB scaffold regrowth", "CTCBScaffoldRegrowth", "1/8", dict(max_regrowth=5)),
               ("Non-contiguous CTCB scaffold regrowth", "CTCBJumpScaffoldRegrowth", "1/8",
                dict(max_regrowth=5, max_seg_regrowth=2))],
+    # scaffold transforms with linker regrowth (src/transform_movetypes.cpp)
+    "lkcb": [("Orientation rotation", "OrientationRotation", "2/6"),
+             ("Met staple exchange", "MetStapleExchange", "1/6"),
+             ("CB staple regrowth", "CBStapleRegrowth", "1/6"),
+             ("CTCB linker regrowth", "CTCBLinkerRegrowth", "1/6",
+              dict(max_disp=1, max_turns=3, max_regrowth=4, max_linker_length=3, num_transforms=4)),
+             ("CTCB clustered linker regrowth", "CTCBClusteredLinkerRegrowth", "1/6",
+              dict(max_disp=1, max_turns=3, max_linker_length=3, num_transforms=4))],
+    "lkrg": [("Orientation rotation", "OrientationRotation", "2/5"),
+             ("Met staple exchange", "MetStapleExchange", "1/5"),
+             ("CB staple regrowth", "CBStapleRegrowth", "1/5"),
+             ("CTRG linker regrowth", "CTRGLinkerRegrowth", "1/5",
+              dict(max_disp=1, max_turns=4, max_regrowth=5, max_linker_length=3, num_transforms=5,
+                   max_num_recoils=1, max_c_attempts=36))],
+    "lkall": [("Orientation rotation", "OrientationRotation", "2/6"),
+              ("Met staple exchange", "MetStapleExchange", "1/6"),
+              ("CTCB linker regrowth", "CTCBLinkerRegrowth", "1/6",
+               dict(max_disp=2, max_turns=2, max_regrowth=6, max_linker_length=4, num_transforms=6)),
+              ("CTCB clustered linker regrowth", "CTCBClusteredLinkerRegrowth", "1/6",
+               dict(max_disp=1, max_turns=1, max_linker_length=4, num_transforms=3)),
+              ("CTRG linker regrowth", "CTRGLinkerRegrowth", "1/6",
+               dict(max_disp=1, max_turns=3, max_regrowth=4, max_linker_length=3, num_transforms=4,
+                    max_num_recoils=2, max_c_attempts=12))],
     # conserved-topology configurational-bias scaffold regrowth
     "ctcb": [("Orientation rotation", "OrientationRotation", "2/6"),
              ("Met staple exchange", "MetStapleExchange", "1/6"),
@@ -245,6 +268,18 @@ CASES = {
     "s24c": ("grid24", "ctcb", dict(stacking_ene=-1000, staple_M=1e-3, temp=335, max_total_staples=24,
                                     max_type_staples=4, bias_functions_file="biases.json",
                                     bias_functions_mult=0.7)),
+    # scaffold transforms with linker regrowth: CTCB and clustered CTCB,
+    # CTRG, every linker movetype on the ThreeQuarterTurn grid with biases,
+    # and on the cyclic scaffold
+    "l24a": ("grid24", "lkcb", dict(stacking_ene=-1000, staple_M=1e-3, temp=335, max_total_staples=24,
+                                    max_type_staples=4)),
+    "l24b": ("grid24", "lkrg", dict(stacking_ene=-1000, staple_M=1e-3, temp=335, max_total_staples=24,
+                                    max_type_staples=4)),
+    "l24c": ("grid24", "lkall", dict(domain_type="ThreeQuarterTurn", stacking_ene=-1500, staple_M=1e-3,
+                                     temp=325, max_total_staples=24, max_type_staples=4,
+                                     bias_functions_file="biases.json", bias_functions_mult=0.7)),
+    "l24r": ("ring24", "lkall", dict(stacking_ene=-1000, staple_M=1e-3, temp=330, max_total_staples=24,
+                                     max_type_staples=4)),
     # cyclic scaffold (a closed ring), every scaffold movetype
     # Dist / AdjacentSite order parameters with biases on a scaffold that moves
     "d24": ("grid24", "ctrg", dict(stacking_ene=-1000, staple_M=1e-3, temp=335, max_total_staples=24,
