@@ -16,6 +16,7 @@ from oracle_lib import OracleReplica
 pytestmark = pytest.mark.gpu
 
 CASES = ["c1", "g24a", "g24b", "g24c", "g24d", "g24e", "c3"]
+LINKER_ENERGY_RTOL = 2e-11
 EXACT = [0, 2, 3, 4, 5, 7]   # step, staples, fully bound, bound, stacked, draws
 
 
@@ -61,7 +62,15 @@ def test_engine_matches_reference_golden(path):
     tr = eng.trace()[0]
     ref = np.array(fx["trace"], dtype=np.float64)
     np.testing.assert_array_equal(tr[:, EXACT], ref[:, EXACT])
-    np.testing.assert_allclose(tr[:, 1], ref[:, 1], rtol=1e-12, atol=1e-12)
+    # The reference's energy is a running total of every placement and
+    # removal a move makes, undone or not; the engine restores rejected and
+    # intermediate states from snapshots.  Under the linker movetypes (many
+    # trial transformations per move) the reference's total drifts from its
+    # configuration's energy by up to 7.5e-12 relative over these runs
+    # (tests/test_oracle_golden.py::test_reference_energy_drift_under_linker_moves),
+    # the others by less than 2e-13.
+    rtol = LINKER_ENERGY_RTOL if fx["case"].startswith("l24") else 1e-12
+    np.testing.assert_allclose(tr[:, 1], ref[:, 1], rtol=rtol, atol=1e-12)
     assert eng.config(0) == fx["final_config"]
 
 

@@ -105,3 +105,29 @@ def test_ideal_random_walk_counts():
                 for n in range(0, 10):
                     l1 = abs(dx) + abs(dy) + abs(dz)
                     assert (nw((dx, dy, dz), n) == 0) == (l1 > n or (n - l1) % 2 == 1)
+
+
+def test_reference_energy_drift_under_linker_moves():
+    """The reference keeps its energy as a running total of every placement
+    and removal; the oracle, bit for bit the reference on these fixtures,
+    shows how far that total drifts from the energy recomputed from the final
+    configuration: by more than 1e-12 relative under the linker movetypes
+    (many trial transformations per move), by less than 2e-13 under the
+    other moves.  The engine restores snapshots instead and compares with
+    the reference's traces at the drift's size (tests/test_gpu_parity.py)."""
+    import re
+    drift = {}
+    for name in ["l24a_s13", "l24r_s16", "s24a_s3", "g24a_s3"]:
+        fx = load(os.path.join(GOLDEN, name + ".json.gz"))
+        o = OracleReplica(inp(fx["case"]), seed=fx["seed"], replica=0)
+        o.set_reference_arithmetic(True)
+        run_golden(o, fx)
+        e_run = o.observables()["energy"]
+        assert e_run == fx["trace"][-1][1]
+        temp = float(re.search(r"temp\s*=\s*([0-9.]+)", open(inp(fx["case"])).read()).group(1))
+        o.update_temp(temp)
+        e_rec = o.observables()["energy"]
+        drift[name] = abs(e_run - e_rec) / abs(e_rec)
+    assert drift["l24a_s13"] > 1e-12 and drift["l24r_s16"] > 1e-12, drift
+    assert drift["s24a_s3"] < 2e-13 and drift["g24a_s3"] < 2e-13, drift
+    assert max(drift.values()) < 2e-11, drift
