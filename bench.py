@@ -592,6 +592,11 @@ C3_ROUNDS_PER_STEP = 25
 C3_BURN_ROUNDS = 200
 C3_RELAX_ROUNDS = 800
 C3_CPU_REPS = 128
+# The network's training set: C3_TRAIN_CONFIGS configurations sampled by
+# plain PT at the 64 temperatures after the burn-in (one collection of all
+# 2048 replicas every C3_TRAIN_EVERY steps, exchanges at the same interval).
+C3_TRAIN_CONFIGS = 10_000_000
+C3_TRAIN_EVERY = 100
 
 
 def write_c3(d):
@@ -671,22 +676,24 @@ def run_c3(args, impl):
         k = min(100, C3_BURN_ROUNDS - done)
         burn.pt_run(C3_RUNGS, k, C3_INTERVAL, 3)
         done += k
+    # the training set: plain PT configurations at the 64 temperatures
+    t_collect0 = time.perf_counter()
+    n_collect = -(-C3_TRAIN_CONFIGS // n)
+    for _ in range(n_collect):
+        burn.pt_run(C3_RUNGS, 1, C3_TRAIN_EVERY, 3)
+        burn.learn_collect()
+    collect_s = time.perf_counter() - t_collect0
     t_train0 = time.perf_counter()
-
-    def collect_train(e):
-        for _ in range(10):
-            e.pt_run(C3_RUNGS, 2, C3_INTERVAL, 3)
-            e.learn_collect()
-        return e.learn_train(LEARN_ITERS, lr=LEARN_LR, seed=0)
-
-    collect_train(burn)
-    table0 = burn.learn_table()
+    loss0, loss1 = burn.learn_train(LEARN_ITERS, lr=LEARN_LR, seed=0)
+    table = burn.learn_table()
     train_s = time.perf_counter() - t_train0
     perm = burn.pt_permutation()
     mid = [burn.config(int(perm[s])) for s in range(n)]   # by slot
     burn.close()
+    # the learned moveset relaxes the low-temperature rungs the plain burn-in
+    # leaves unassembled; both timed arms start from its configurations
     relax = Engine(inp, n_replicas=n, seed=901, overrides=learned_over)
-    relax.learn_set_table(table0)
+    relax.learn_set_table(table)
     relax.set_configs(mid)
     relax.autotune(probe_sweeps=2)
     done = 0
@@ -694,10 +701,6 @@ def run_c3(args, impl):
         k = min(100, C3_RELAX_ROUNDS - done)
         relax.pt_run(C3_RUNGS, k, C3_INTERVAL, 3)
         done += k
-    t_train1 = time.perf_counter()
-    loss0, loss1 = collect_train(relax)
-    table = relax.learn_table()
-    train_s += time.perf_counter() - t_train1
     perm = relax.pt_permutation()
     start = [relax.config(int(perm[s])) for s in range(n)]   # by slot
     relax.close()
@@ -869,8 +872,8 @@ def run_c3(args, impl):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": workload, "rounds_per_step": C3_ROUNDS_PER_STEP, "replicas": n,
                        "start": "both arms from the same configurations: %d rounds of plain PT from the empty "
-                                "scaffold, then %d rounds of PT with the learned moveset, imported by temperature "
-                                "slot" % (C3_BURN_ROUNDS, C3_RELAX_ROUNDS),
+                                "scaffold, the training collection, then %d rounds of PT with the learned moveset, "
+                                "imported by temperature slot" % (C3_BURN_ROUNDS, C3_RELAX_ROUNDS),
                        "l2": "state resident in shared memory; no L2 flush needed"},
             "ci95": learned["ci95"], "learned": learned, "plain": plain,
             "learned_over_plain": value / plain["value"],
@@ -885,7 +888,10 @@ def run_c3(args, impl):
                              "top_rung_370K_learned": learned["mean_fully_bound_by_temperature"][-1],
                              "constant_T_370K_from_empty": ref_empty,
                              "constant_T_370K_from_assembled": ref_assembled},
-            "network": {"train_iters": LEARN_ITERS, "loss_first": loss0, "loss_last": loss1, "train_s": train_s},
+            "network": {"train_iters": LEARN_ITERS, "loss_first": loss0, "loss_last": loss1, "train_s": train_s,
+                        "training_configurations": n_collect * n, "collect_s": collect_s,
+                        "training_set": "plain PT at the 64 temperatures, all 2048 replicas every %d steps after "
+                                        "the burn-in" % C3_TRAIN_EVERY},
             "burn_in_s": burn_s, "roofline": learned["roofline"], "e2e": e2e,
             # counted by the engine: per step C3_ROUNDS_PER_STEP rounds of the MC
             # kernel and the exchange kernel (graph replays), and the status fold
@@ -919,6 +925,7 @@ def c3_cpu(inp, rounds):
 
 def main():
     global C4_SWEEPS_PER_STEP, SWEEPS_PER_STEP
+    global C3_BURN_ROUNDS, C3_ROUNDS_PER_STEP, C3_RELAX_ROUNDS, C3_TRAIN_CONFIGS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -933,6 +940,8 @@ def main():
     ap.add_argument("--c3-relax-rounds", type=int, default=0,
                     help="c3 only: PT rounds of the learned relaxation after the burn-in")
     ap.add_argument("--c3-rounds-per-step", type=int, default=0, help="c3 only: PT rounds per timed step")
+    ap.add_argument("--c3-train-configs", type=int, default=0,
+                    help="c3 only: plain-PT configurations the network is trained on (default %d)" % C3_TRAIN_CONFIGS)
     ap.add_argument("--sweeps-per-step", type=int, default=0,
                     help="sweeps per launch (default c2 %d, c4 %d); small values make short profiler captures"
                          % (SWEEPS_PER_STEP, C4_SWEEPS_PER_STEP))
@@ -941,7 +950,8 @@ def main():
         C4_SWEEPS_PER_STEP = args.sweeps_per_step
         SWEEPS_PER_STEP = args.sweeps_per_step
     rank = int(os.environ.get("RANK", "0"))
-    global C3_BURN_ROUNDS, C3_ROUNDS_PER_STEP, C3_RELAX_ROUNDS
+    if args.c3_train_configs > 0:
+        C3_TRAIN_CONFIGS = args.c3_train_configs
     if args.c3_burn_rounds > 0:
         C3_BURN_ROUNDS = args.c3_burn_rounds
     if args.c3_relax_rounds > 0:

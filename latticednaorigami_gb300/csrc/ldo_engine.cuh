@@ -1812,8 +1812,9 @@ struct Rep : public LdoState<C> {
         return __ldg(learn_w + ldo_learn_index(learn_tb, ts, combo));
     }
     // Training data for the network: every bound (label 1) or unbound
-    // (label 0) domain, counted at its network input.
-    __device__ __noinline__ void learn_collect(float* cnt_b, float* cnt_t) const {
+    // (label 0) domain, counted at its network input (FP64 counters: exact
+    // integers past the 2^24 where single-precision increments stop).
+    __device__ __noinline__ void learn_collect(double* cnt_b, double* cnt_t) const {
         int nc = hdr.n_chains;
         #pragma unroll 1
         for (int c = 0; c < nc; ++c) {
@@ -1831,8 +1832,8 @@ struct Rep : public LdoState<C> {
                             (learn_code(n2, -1) << 6);
                 int ts = cs == 0 ? (int)sys->learn_tslot[d] : 0;
                 int k = ldo_learn_index(learn_tb, ts, combo);
-                atomicAdd(cnt_t + k, 1.f);
-                if (s == BOUND) atomicAdd(cnt_b + k, 1.f);
+                atomicAdd(cnt_t + k, 1.0);
+                if (s == BOUND) atomicAdd(cnt_b + k, 1.0);
             }
         }
         // regrowth directions: for every placed staple domain next to a
@@ -1862,8 +1863,8 @@ struct Rep : public LdoState<C> {
                             f = lr_site_class(i, add(pos(prev), unit(v)), nullptr);
                         }
                         int k = ldo_learn_dir_index(learn_tb, f);
-                        atomicAdd(cnt_t + k, 1.f);
-                        if (v == vstar) atomicAdd(cnt_b + k, 1.f);
+                        atomicAdd(cnt_t + k, 1.0);
+                        if (v == vstar) atomicAdd(cnt_b + k, 1.0);
                     }
                 }
             }

@@ -649,7 +649,7 @@ struct ldo_engine {
     size_t ct_stride {0};
     // learned insertion proposal: weight table, training counts, network
     DevBuf<double> d_learn_w;
-    DevBuf<float> d_cnt_b, d_cnt_t;
+    DevBuf<double> d_cnt_b, d_cnt_t;
     LdoMlp mlp;
     bool mlp_init {false};
     DevBuf<int> d_status;
@@ -1158,8 +1158,8 @@ struct ldo_engine {
             CU(copy(d_learn_w.p, ones.data(), ones.size() * sizeof(double), cudaMemcpyHostToDevice));
             d_cnt_b.alloc(LDO_LEARN_TABLE);
             d_cnt_t.alloc(LDO_LEARN_TABLE);
-            CU(cudaMemsetAsync(d_cnt_b.p, 0, LDO_LEARN_TABLE * sizeof(float), stream));
-            CU(cudaMemsetAsync(d_cnt_t.p, 0, LDO_LEARN_TABLE * sizeof(float), stream));
+            CU(cudaMemsetAsync(d_cnt_b.p, 0, LDO_LEARN_TABLE * sizeof(double), stream));
+            CU(cudaMemsetAsync(d_cnt_t.p, 0, LDO_LEARN_TABLE * sizeof(double), stream));
         }
         LdoLaunch L = launch_params(LDO_MODE_INIT, 0);
         CU(launch_mc(L));
@@ -1640,18 +1640,18 @@ struct ldo_engine {
     // Adam on the weighted logistic loss over the collected counts (full
     // batch), then the weight table.
     void learn_train(int iters, double lr, uint32_t seed, double* loss0, double* loss1) {
-        vector<float> cb(LDO_LEARN_TABLE), ct(LDO_LEARN_TABLE);
-        CU(copy(cb.data(), d_cnt_b.p, cb.size() * sizeof(float), cudaMemcpyDeviceToHost));
-        CU(copy(ct.data(), d_cnt_t.p, ct.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        vector<double> cb(LDO_LEARN_TABLE), ct(LDO_LEARN_TABLE);
+        CU(copy(cb.data(), d_cnt_b.p, cb.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        CU(copy(ct.data(), d_cnt_t.p, ct.size() * sizeof(double), cudaMemcpyDeviceToHost));
         vector<int32_t> idx;
         vector<float> bb, tt;
         double norm = 0;
         for (int k = 0; k < LDO_LEARN_TABLE; ++k)
             if (ct[k] > 0) {
                 idx.push_back(k);
-                bb.push_back(cb[k]);
-                tt.push_back(ct[k]);
-                norm += ct[k];
+                bb.push_back((float)cb[k]);
+                tt.push_back((float)ct[k]);
+                norm += (float)ct[k];
             }
         if (idx.empty()) throw LdoError(LDO_EINVAL, "no training data collected");
         if ((int)idx.size() > kMlpCap) throw LdoError(LDO_EINVAL, "too many distinct network inputs");
@@ -2968,16 +2968,21 @@ ldo_status ldo_learn_collect(ldo_engine* e) {
 ldo_status ldo_learn_reset_counts(ldo_engine* e) {
     if (!e) return LDO_EINVAL;
     return guard(e, [&]() {
-        CU(cudaMemsetAsync(e->d_cnt_b.p, 0, LDO_LEARN_TABLE * sizeof(float), e->stream));
-        CU(cudaMemsetAsync(e->d_cnt_t.p, 0, LDO_LEARN_TABLE * sizeof(float), e->stream));
+        CU(cudaMemsetAsync(e->d_cnt_b.p, 0, LDO_LEARN_TABLE * sizeof(double), e->stream));
+        CU(cudaMemsetAsync(e->d_cnt_t.p, 0, LDO_LEARN_TABLE * sizeof(double), e->stream));
     });
 }
 
 ldo_status ldo_learn_get_counts(ldo_engine* e, float* cnt_bound, float* cnt_total, int n) {
     if (!e || !cnt_bound || !cnt_total || n != LDO_LEARN_TABLE) return LDO_EINVAL;
     return guard(e, [&]() {
-        CU(e->copy(cnt_bound, e->d_cnt_b.p, n * sizeof(float), cudaMemcpyDeviceToHost));
-        CU(e->copy(cnt_total, e->d_cnt_t.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+        vector<double> b(n), t(n);
+        CU(e->copy(b.data(), e->d_cnt_b.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+        CU(e->copy(t.data(), e->d_cnt_t.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+        for (int k = 0; k < n; ++k) {
+            cnt_bound[k] = (float)b[k];
+            cnt_total[k] = (float)t[k];
+        }
     });
 }
 

@@ -40,8 +40,8 @@ struct LdoLaunch {
     // Learned insertion proposal: weight exp(logit) of every network input
     // (LDO_LEARN_TABLE entries), read by LearnedStapleExchange.
     const double* learn_w;
-    float* learn_cnt_b;          // collect mode: bound / total counts per network input
-    float* learn_cnt_t;
+    double* learn_cnt_b;         // collect mode: bound / total counts per network input
+    double* learn_cnt_t;
     // Scaffold regrowth working memory, ct_stride bytes per replica (null
     // when no system regrows its scaffold).
     unsigned char* ct_ws;
