@@ -279,6 +279,17 @@ ldo_status ldo_enumerate(ldo_engine* e, int32_t min_total, int32_t max_total, in
                          const char* op2_tag, int32_t n1, int32_t n2, double* weights, double* num_configs,
                          int32_t* n_units, double* device_ms);
 
+/* enumerate_main without enumerate_staples_only (src/enumerate.cpp:19-81,
+ * ConformationalEnumerator::enumerate, :218): the scaffold is unassigned and
+ * enumerated too, from its first domain at the origin, as the reference's
+ * full enumeration does, with the same staple sets, growth-point sets and
+ * overcount corrections.  Each unit is split into 6^split_levels parts (0..4)
+ * by the branch its recursion takes at its first split_levels choices
+ * (sites and orientations), which run in parallel. */
+ldo_status ldo_enumerate_full(ldo_engine* e, int32_t min_total, int32_t max_total, int32_t max_type,
+                              const char* op1_tag, const char* op2_tag, int32_t n1, int32_t n2, int32_t split_levels,
+                              double* weights, double* num_configs, int32_t* n_units, double* device_ms);
+
 /* The last ldo_enumerate's work units (the reference's growth-point sets, in
  * its enumeration order): out[2u] the unit's partition-function sum before
  * normalisation, out[2u+1] its number of configurations (NULL out: count

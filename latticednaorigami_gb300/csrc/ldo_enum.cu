@@ -13,12 +13,17 @@ namespace {
 template <class C>
 __host__ __device__ constexpr int enum_smem_bytes() { return (int)((sizeof(ldo::Rep<C>) + 15) / 16 * 16); }
 
-// One block per enumeration unit; its first lane runs the recursion on the
-// replica state in shared memory (the other lanes only copy it in).
+// One block per part of an enumeration unit (a unit is split into 6^split
+// parts by the branch taken at each of its first `split` choice levels);
+// its first lane runs the recursion on the replica state in shared memory
+// (the other lanes only copy it in).
 template <class C>
 __global__ void __launch_bounds__(32) ldo_enum_kernel(LdoEnumLaunch E) {
     extern __shared__ __align__(16) unsigned char smem[];
-    int u = blockIdx.x;
+    int parts = 1;
+    for (int k = 0; k < E.split; ++k) parts *= 6;
+    int b = blockIdx.x;
+    int u = b / parts;
     int lane = threadIdx.x;
     if (u >= E.n_units) return;
     warp_copy16(smem, E.state, (int)sizeof(LdoState<C>), lane);
@@ -26,7 +31,7 @@ __global__ void __launch_bounds__(32) ldo_enum_kernel(LdoEnumLaunch E) {
     if (lane != 0) return;
     ldo::Rep<C>* R = reinterpret_cast<ldo::Rep<C>*>(smem);
     bind_rep<C>(*R, E.L, 0);
-    auto* W = reinterpret_cast<ldo::EnumWork<C>*>(E.work + (size_t)u * E.work_stride);
+    auto* W = reinterpret_cast<ldo::EnumWork<C>*>(E.work + (size_t)b * E.work_stride);
     const LdoEnumUnit& U = E.units[u];
     for (int d = 0; d < C::DCAP; ++d) {
         W->gp_of[d] = -1;
@@ -41,7 +46,7 @@ __global__ void __launch_bounds__(32) ldo_enum_kernel(LdoEnumLaunch E) {
     W->part = 0;
     W->nconf = 0;
     W->sumE = 0;
-    W->row = E.hist + (size_t)u * E.n1 * E.n2;
+    W->row = E.hist + (size_t)b * E.n1 * E.n2;
     for (int k = 0; k < E.n1 * E.n2; ++k) W->row[k] = 0;
     W->op1 = E.op1;
     W->op2 = E.op2;
@@ -49,6 +54,15 @@ __global__ void __launch_bounds__(32) ldo_enum_kernel(LdoEnumLaunch E) {
     W->n2 = E.n2;
     W->overcount = E.overcount;
     W->bad = 0;
+    W->full = E.full;
+    W->depth = 0;
+    W->npre = E.split;
+    for (int k = 0, r = b % parts; k < E.split; ++k, r /= 6) W->pre[k] = (int8_t)(r % 6);
+    // m_identities_to_num_unassigned: 1 for each scaffold identity
+    // (ConformationalEnumerator's constructor, :203), then +1 per staple
+    // domain (add_staple, :260)
+    for (int k = 0; k < 2 * LDO_ENUM_MAX_IDENT + 1; ++k) W->cnt[k] = 0;
+    for (int d = 0; d < R->ns; ++d) W->cnt[R->did[d] + LDO_ENUM_MAX_IDENT] = 1;
     // ConformationalEnumerator::add_staple (src/enumerate.cpp:260)
     int cs[LDO_ENUM_MAX_STAPLES];
     for (int k = 0; k < U.n_chains; ++k) {
@@ -57,6 +71,8 @@ __global__ void __launch_bounds__(32) ldo_enum_kernel(LdoEnumLaunch E) {
         if (R->mean_field) W->E += R->log6;
         W->E += R->t_init_e;
         int len = R->sys->type_len[U.ident[k]];
+        if (!R->bad())
+            for (int q = 0; q < len; ++q) W->cnt[R->did[R->slot_of(cs[k], q)] + LDO_ENUM_MAX_IDENT] += 1;
         double six = 1;
         for (int q = 0; q < 2 * len - 1; ++q) six *= 6.0;
         W->prefix /= six;
@@ -68,9 +84,10 @@ __global__ void __launch_bounds__(32) ldo_enum_kernel(LdoEnumLaunch E) {
             W->gp_of[old] = (int16_t)R->slot_of(cs[U.gp_new_chain[g]], U.gp_new_dom[g]);
         }
         ldo::Enumerator<C> en {*R, *W};
-        en.run();
+        if (E.full) en.run_full();
+        else en.run();
     }
-    double* st = E.stats + 4 * (size_t)u;
+    double* st = E.stats + 4 * (size_t)b;
     st[0] = W->part;
     st[1] = W->nconf;
     st[2] = W->sumE;
@@ -84,7 +101,11 @@ static cudaError_t launch_enum_class(const LdoEnumLaunch& E, cudaStream_t stream
     size_t smem = (size_t)enum_smem_bytes<C>();
     cudaError_t err = cudaFuncSetAttribute(ldo_enum_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    if (E.n_units > 0) ldo_enum_kernel<C><<<E.n_units, 32, smem, stream>>>(E);
+    long long parts = 1;
+    for (int k = 0; k < E.split; ++k) parts *= 6;
+    long long blocks = (long long)E.n_units * parts;
+    if (E.split < 0 || E.split > LDO_ENUM_MAX_SPLIT || blocks > 0x7fffffffll) return cudaErrorInvalidValue;
+    if (blocks > 0) ldo_enum_kernel<C><<<(unsigned)blocks, 32, smem, stream>>>(E);
     return cudaGetLastError();
 }
 

@@ -41,6 +41,10 @@ struct EnumWork {
     int op1, op2, n1, n2;         // key order parameters and histogram shape
     int overcount;                // 0 MaxTwoDomain, 1 MisbindingOnly
     int bad;                      // a key outside the histogram
+    int full;                     // ConformationalEnumerator::enumerate: the scaffold enumerated too
+    int depth, npre;              // choice loops around the current call; levels fixed by the prefix
+    int8_t pre[LDO_ENUM_MAX_SPLIT];   // the branch taken at each fixed level
+    int16_t cnt[2 * LDO_ENUM_MAX_IDENT + 1];   // m_identities_to_num_unassigned
 };
 
 template <class C>
@@ -56,6 +60,9 @@ struct Enumerator {
         return R.set_domain_config(d, p, o);
     }
     __device__ double unset(int d) { return R.unassign_domain(d); }
+    __device__ int16_t& count(int ident) { return W.cnt[ident + LDO_ENUM_MAX_IDENT]; }
+    // a unit split by a prefix follows only its branch at the first levels
+    __device__ bool skip(int level, int k) const { return level < W.npre && k != W.pre[level]; }
 
     // ConformationalEnumerator::calc_and_save_weights (:639)
     __device__ __noinline__ void save() {
@@ -151,10 +158,40 @@ struct Enumerator {
         else enumerate_domain(nd, p);
     }
 
-    // StapleConformationalEnumerator::grow_next_domain (:729)
+    // StapleConformationalEnumerator::grow_next_domain (:729), or the base
+    // ConformationalEnumerator::grow_next_domain (:550) when the scaffold is
+    // enumerated too
     __device__ __noinline__ void grow_next(int d, V3 p) {
+        if (W.full) {
+            grow_next_full(d, p);
+            return;
+        }
         if (W.sp != 0) next_from(pop(), p);
         else save();
+        W.E += unset(d);
+    }
+    __device__ __noinline__ void grow_next_full(int d, V3 p) {
+        if (W.sp != 0) {
+            int nd = pop();
+            bool terminal = R.scs[d] != R.scs[nd];
+            V3 np = p;
+            if (terminal) {
+                if (W.npgp == 0) {   // no growth point to return to: not a stack the reference builds
+                    R.fail(LDO_RS_INVARIANT);
+                    return;
+                }
+                np = W.pgp[--W.npgp];
+            }
+            enumerate_domain(nd, np);
+            if (terminal) W.pgp[W.npgp++] = np;
+        }
+        else if (R.cyclic) {   // a closed scaffold must close
+            V3 e = sub(R.pos(0), R.pos(R.ns - 1));
+            if (abs(vx(e)) + abs(vy(e)) + abs(vz(e)) == 1) save();
+        }
+        else {
+            save();
+        }
         W.E += unset(d);
     }
 
@@ -185,6 +222,37 @@ struct Enumerator {
         W.mult /= 6.0;
     }
 
+    // ConformationalEnumerator::set_unbound_domain (:523): every orientation
+    // while a complementary domain is still unassigned, else the (0, 0, 0)
+    // stand-in counted six times
+    __device__ __noinline__ void set_unbound_full(int d, V3 p) {
+        int id = R.did[d];
+        if (count(-id) == 0) {
+            count(id) -= 1;
+            W.E += set(d, p, 0);
+            W.zero_ore[d] = 1;
+            W.mult *= 6.0;
+            grow_next_full(d, p);
+            count(id) += 1;
+            W.mult /= 6.0;
+            return;
+        }
+        int level = W.depth++;
+        #pragma unroll 1
+        for (int o = 0; o < 6; ++o) {
+            if (skip(level, o)) continue;
+            W.E += set(d, p, o);
+            if (R.hdr.violated) {
+                R.hdr.violated = 0;
+                continue;
+            }
+            count(id) -= 1;
+            grow_next_full(d, p);
+            count(id) += 1;
+        }
+        W.depth--;
+    }
+
     // ConformationalEnumerator::set_bound_domain (:499)
     __device__ __noinline__ void set_bound(int d, V3 p) {
         int occ = R.unbound_at(p);
@@ -197,14 +265,18 @@ struct Enumerator {
         }
         double m = overcount(d, occ);
         W.mult *= m;
+        count(R.did[d]) -= 1;
         grow_next(d, p);
+        count(R.did[d]) += 1;
         W.mult /= m;
     }
 
     // ConformationalEnumerator::set_comp_growthpoint_domains (:451)
     __device__ __noinline__ void set_comp_gp(int d, int bd, V3 p) {
+        int level = W.depth++;
         #pragma unroll 1
         for (int o = 0; o < 6; ++o) {
+            if (skip(level, o)) continue;
             W.E += set(d, p, o);
             W.E += set(bd, p, o ^ 1);
             if (R.hdr.violated) {
@@ -212,9 +284,14 @@ struct Enumerator {
                 W.E += unset(d);
                 continue;
             }
+            count(R.did[d]) -= 1;
+            count(R.did[bd]) -= 1;
             grow_next(bd, p);
+            count(R.did[d]) += 1;
+            count(R.did[bd]) += 1;
             W.E += unset(d);
         }
+        W.depth--;
     }
 
     // ConformationalEnumerator::set_mis_growthpoint_domains (:477)
@@ -222,7 +299,11 @@ struct Enumerator {
         W.E += set(d, p, 0);
         W.E += set(bd, p, 1);
         W.mult *= 6.0;
+        count(R.did[d]) -= 1;
+        count(R.did[bd]) -= 1;
         grow_next(bd, p);
+        count(R.did[d]) += 1;
+        count(R.did[bd]) += 1;
         W.E += unset(d);
         W.mult /= 6.0;
     }
@@ -247,8 +328,10 @@ struct Enumerator {
 
     // ConformationalEnumerator::enumerate_domain (:378)
     __device__ __noinline__ void enumerate_domain(int d, V3 p_prev) {
+        int level = W.depth++;
         #pragma unroll 1
         for (int k = 0; k < 6 && !R.bad(); ++k) {
+            if (skip(level, k)) continue;
             V3 p = add(p_prev, unit(k));
             bool is_gp = W.gp_of[d] >= 0;
             int occ = R.occupancy(p);
@@ -257,9 +340,62 @@ struct Enumerator {
             if ((is_gp && occupied) || bound) continue;
             if (is_gp) set_gp(d, p);
             else if (occupied) set_bound(d, p);
+            else if (W.full) set_unbound_full(d, p);
             else set_unbound(d, p);
         }
+        W.depth--;
         push(d);
+    }
+
+    // ConformationalEnumerator::create_domains_stack (:578): scaffold domains
+    // in order, each growth point followed by its staple's stack; reversed
+    __device__ void domains_stack_full() {
+        W.sp = 0;
+        #pragma unroll 1
+        for (int d = 0; d < R.ns; ++d) {
+            push(d);
+            if (W.gp_of[d] >= 0) {
+                W.inv_gp[W.gp_of[d]] = (int16_t)d;
+                staple_stack(W.gp_of[d]);
+            }
+        }
+        #pragma unroll 1
+        for (int a = 0, b = W.sp - 1; a < b; ++a, --b) {
+            int16_t t = W.stack[a];
+            W.stack[a] = W.stack[b];
+            W.stack[b] = t;
+        }
+    }
+    // ConformationalEnumerator::enumerate (:218), after the constructor's
+    // unassignment of the scaffold (:188): the first domain at the origin
+    // along +x, its staple first when it is a growth point
+    __device__ void run_full() {
+        #pragma unroll 1
+        for (int d = 0; d < R.ns; ++d) unset(d);
+        domains_stack_full();
+        if (W.sp < 2) return;
+        int start = pop();
+        V3 p = mk(0, 0, 0);
+        count(R.did[start]) -= 1;
+        set(start, p, 0);
+        int nd = pop();
+        if (W.gp_of[start] >= 0) {
+            W.pgp[W.npgp++] = p;
+            count(R.did[nd]) -= 1;
+            W.E += set(nd, p, 1);
+            if (W.sp > 0) {
+                int nn = pop();
+                enumerate_domain(nn, p);
+            }
+            count(R.did[nd]) += 1;
+            W.E += unset(nd);
+            W.npgp--;
+        }
+        else {
+            enumerate_domain(nd, p);
+        }
+        count(R.did[start]) += 1;
+        unset(start);
     }
 
     // StapleConformationalEnumerator::enumerate (:687)

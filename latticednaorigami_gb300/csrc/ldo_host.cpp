@@ -2253,8 +2253,13 @@ struct ldo_engine {
     // enumerate_staples_only, src/enumerate.cpp:19) of replica 0's system at
     // its temperature: normalised weights over (op1, op2) into w[n1 * n2].
     void enumerate(int min_total, int max_total, int max_type, int op1, int op2, int n1, int n2, double* w,
-                   double* num_configs, int* n_units, double* ms) {
+                   double* num_configs, int* n_units, double* ms, int full = 0, int split = 0) {
         const HostSystem& hs = systems[sys_of[0]];
+        if (split < 0 || split > LDO_ENUM_MAX_SPLIT) throw LdoError(LDO_EINVAL, "enumeration: split levels 0.." + std::to_string(LDO_ENUM_MAX_SPLIT));
+        for (auto& ids : hs.sf.identities)
+            for (int d : ids)
+                if (d > LDO_ENUM_MAX_IDENT || d < -LDO_ENUM_MAX_IDENT)
+                    throw LdoError(LDO_EINVAL, "enumeration: domain identities beyond +-64");
         if (hs.desc.n_biases != 0) throw LdoError(LDO_EINVAL, "enumeration: bias functions are not supported");
         if (hs.desc.has_ct) throw LdoError(LDO_EINVAL, "enumeration: the scaffold must stay fixed");
         if (op1 < 0 || op1 >= hs.desc.n_ops || op2 < 0 || op2 >= hs.desc.n_ops || n1 < 1 || n2 < 1)
@@ -2273,20 +2278,27 @@ struct ldo_engine {
         EnumBuilder b(hs.sf.identities, hs.p.misbinding_pot != "Disallowed", 1u << 22);
         b.run(min_total, max_total, max_type);
         int nu = (int)b.units.size();
+        int parts = 1;
+        for (int k = 0; k < split; ++k) parts *= 6;
+        size_t nb = (size_t)nu * parts;   // one block per part of a unit
+        size_t stride = ldo_enum_work_bytes(lay.cls);
+        if (nb * (stride + (size_t)n1 * n2 * sizeof(double)) > ((size_t)8 << 30))
+            throw LdoError(LDO_ECAPACITY, "enumeration: more than 8 GiB of per-part working memory");
         DevBuf<LdoEnumUnit> d_units;
         d_units.alloc(nu);
         CU(copy(d_units.p, b.units.data(), nu * sizeof(LdoEnumUnit), cudaMemcpyHostToDevice));
-        size_t stride = ldo_enum_work_bytes(lay.cls);
         DevBuf<unsigned char> d_work;
-        d_work.alloc((size_t)nu * stride);
+        d_work.alloc(nb * stride);
         DevBuf<double> d_hist, d_stats;
-        d_hist.alloc((size_t)nu * n1 * n2);
-        d_stats.alloc((size_t)nu * 4);
+        d_hist.alloc(nb * n1 * n2);
+        d_stats.alloc(nb * 4);
         LdoEnumLaunch E {};
         E.L = launch_params(LDO_MODE_RUN, 0);
         E.state = d_arena.p;
         E.units = d_units.p;
         E.n_units = nu;
+        E.full = full;
+        E.split = split;
         E.work = d_work.p;
         E.work_stride = stride;
         E.hist = d_hist.p;
@@ -2312,22 +2324,20 @@ struct ldo_engine {
             CU(cudaEventElapsedTime(&f, ev0, ev1));
             *ms = f;
         }
-        vector<double> hist((size_t)nu * n1 * n2), stats((size_t)nu * 4);
+        vector<double> hist(nb * n1 * n2), stats(nb * 4);
         CU(copy(hist.data(), d_hist.p, hist.size() * sizeof(double), cudaMemcpyDeviceToHost));
         CU(copy(stats.data(), d_stats.p, stats.size() * sizeof(double), cudaMemcpyDeviceToHost));
         double part = 0, nconf = 0;
         for (int k = 0; k < n1 * n2; ++k) w[k] = 0;
-        for (int u = 0; u < nu; ++u) {
-            if (stats[4 * u + 3] < 0) throw LdoError(LDO_EINVAL, "enumeration: an order parameter value outside the histogram");
-            if (stats[4 * u + 3] > 0) throw LdoError((ldo_status)(int)stats[4 * u + 3], "enumeration: a unit failed");
-            part += stats[4 * u];
-            nconf += stats[4 * u + 1];
-            for (int k = 0; k < n1 * n2; ++k) w[k] += hist[(size_t)u * n1 * n2 + k];
-        }
         enum_units.assign(2 * (size_t)nu, 0.0);
-        for (int u = 0; u < nu; ++u) {
-            enum_units[2 * u] = stats[4 * u];
-            enum_units[2 * u + 1] = stats[4 * u + 1];
+        for (size_t q = 0; q < nb; ++q) {   // parts in unit order, each unit's parts in branch order
+            if (stats[4 * q + 3] < 0) throw LdoError(LDO_EINVAL, "enumeration: an order parameter value outside the histogram");
+            if (stats[4 * q + 3] > 0) throw LdoError((ldo_status)(int)stats[4 * q + 3], "enumeration: a unit failed");
+            part += stats[4 * q];
+            nconf += stats[4 * q + 1];
+            enum_units[2 * (q / parts)] += stats[4 * q];
+            enum_units[2 * (q / parts) + 1] += stats[4 * q + 1];
+            for (int k = 0; k < n1 * n2; ++k) w[k] += hist[q * n1 * n2 + k];
         }
         // ConformationalEnumerator::normalize_weights (:344)
         for (int k = 0; k < n1 * n2; ++k) w[k] /= part;
@@ -2415,9 +2425,10 @@ ldo_status ldo_run_sweeps(ldo_engine* e, int64_t n_sweeps, double* device_ms) {
 
 int ldo_state_bytes(const ldo_engine* e) { return e ? e->lay.bytes : 0; }
 
-ldo_status ldo_enumerate(ldo_engine* e, int32_t min_total, int32_t max_total, int32_t max_type, const char* op1_tag,
-                         const char* op2_tag, int32_t n1, int32_t n2, double* weights, double* num_configs,
-                         int32_t* n_units, double* device_ms) {
+namespace {
+ldo_status enumerate_call(ldo_engine* e, int32_t min_total, int32_t max_total, int32_t max_type, const char* op1_tag,
+                          const char* op2_tag, int32_t n1, int32_t n2, double* weights, double* num_configs,
+                          int32_t* n_units, double* device_ms, int full, int split) {
     if (!e || !op1_tag || !op2_tag || !weights || min_total < 0 || max_total < min_total || max_type < 1)
         return LDO_EINVAL;
     return guard(e, [&]() {
@@ -2429,9 +2440,24 @@ ldo_status ldo_enumerate(ldo_engine* e, int32_t min_total, int32_t max_total, in
         };
         int nu = 0;
         e->enumerate(min_total, max_total, max_type, find(op1_tag), find(op2_tag), n1, n2, weights, num_configs, &nu,
-                     device_ms);
+                     device_ms, full, split);
         if (n_units) *n_units = nu;
     });
+}
+} // namespace
+
+ldo_status ldo_enumerate(ldo_engine* e, int32_t min_total, int32_t max_total, int32_t max_type, const char* op1_tag,
+                         const char* op2_tag, int32_t n1, int32_t n2, double* weights, double* num_configs,
+                         int32_t* n_units, double* device_ms) {
+    return enumerate_call(e, min_total, max_total, max_type, op1_tag, op2_tag, n1, n2, weights, num_configs, n_units,
+                          device_ms, 0, 0);
+}
+
+ldo_status ldo_enumerate_full(ldo_engine* e, int32_t min_total, int32_t max_total, int32_t max_type,
+                              const char* op1_tag, const char* op2_tag, int32_t n1, int32_t n2, int32_t split_levels,
+                              double* weights, double* num_configs, int32_t* n_units, double* device_ms) {
+    return enumerate_call(e, min_total, max_total, max_type, op1_tag, op2_tag, n1, n2, weights, num_configs, n_units,
+                          device_ms, 1, split_levels);
 }
 
 ldo_status ldo_enumerate_units(ldo_engine* e, double* out, int32_t cap, int32_t* n_units) {

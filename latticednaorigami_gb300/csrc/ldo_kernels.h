@@ -126,6 +126,10 @@ cudaError_t ldo_status_noalloc(const unsigned char* arena, int bytes, int o_hdr,
 // domain reference is (chain, domain index) with chain -1 for the scaffold
 // and k for the k-th added staple.
 #define LDO_ENUM_MAX_STAPLES 8
+// domain identities |d_ident| <= LDO_ENUM_MAX_IDENT keep an unassigned count
+#define LDO_ENUM_MAX_IDENT 64
+// choice levels a unit can be split at (6 branches each)
+#define LDO_ENUM_MAX_SPLIT 4
 struct LdoEnumUnit {
     int n_chains;
     int ident[LDO_ENUM_MAX_STAPLES];
@@ -140,10 +144,12 @@ struct LdoEnumLaunch {
     const unsigned char* state;   // the replica's state with the scaffold placed and no staples
     const LdoEnumUnit* units;
     int n_units;
-    unsigned char* work;          // per unit: recursion state (ldo_enum_work_bytes)
+    int full;                     // 1: the scaffold is enumerated too (ConformationalEnumerator::enumerate)
+    int split;                    // each unit runs as 6^split parts, one per branch of its first choice levels
+    unsigned char* work;          // per part: recursion state (ldo_enum_work_bytes)
     size_t work_stride;
-    double* hist;                 // per unit: n1 x n2 weights over (op1, op2)
-    double* stats;                // per unit: partition sum, configurations, sum of E w, status
+    double* hist;                 // per part: n1 x n2 weights over (op1, op2)
+    double* stats;                // per part: partition sum, configurations, sum of E w, status
     int op1, op2, n1, n2;
     int overcount;                // 0 MaxTwoDomain, 1 MisbindingOnly
 };

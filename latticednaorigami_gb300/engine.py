@@ -25,7 +25,7 @@ EXPORTS = [
     "ldo_writer_open", "ldo_writer_write", "ldo_writer_close", "ldo_pt2d_run", "ldo_engine_exp",
     "ldo_set_bias_centre", "ldo_swap_writer_open", "ldo_set_config", "ldo_set_configs", "ldo_anneal_run", "ldo_read_trj_frame", "ldo_checkpoint_save",
     "ldo_checkpoint_load", "ldo_autotune", "ldo_autotune_candidates", "ldo_us_write_biases",
-    "ldo_us_read_biases", "ldo_us_reset", "ldo_read_biases", "ldo_enumerate", "ldo_enumerate_units",
+    "ldo_us_read_biases", "ldo_us_reset", "ldo_read_biases", "ldo_enumerate", "ldo_enumerate_full", "ldo_enumerate_units",
     "ldo_batch_create", "ldo_batch_destroy", "ldo_batch_last_error", "ldo_batch_num_groups", "ldo_batch_group",
     "ldo_batch_set_controls", "ldo_batch_run", "ldo_batch_run_sweeps", "ldo_batch_set_sampling",
     "ldo_batch_get_samples", "ldo_batch_get_counters", "ldo_batch_autotune",
@@ -91,6 +91,9 @@ def load_library(path=None):
                                   ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, dp, dp,
                                   ctypes.POINTER(ctypes.c_int32), dp]
     lib.ldo_enumerate_units.argtypes = [vp, dp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
+    lib.ldo_enumerate_full.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p,
+                                       ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, dp,
+                                       dp, ctypes.POINTER(ctypes.c_int32), dp]
     lib.ldo_autotune.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(TuneReport)]
     lib.ldo_autotune_candidates.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), dp, ctypes.c_int32]
     lib.ldo_get_observables.argtypes = [vp, ctypes.POINTER(Observables), ip]
@@ -219,16 +222,25 @@ class Engine:
     def state_bytes(self):
         return self.lib.ldo_state_bytes(self.h)
 
-    def enumerate(self, min_total, max_total, max_type, ops=("numstaples", "numfulldomains"), shape=(9, 49)):
-        """Exact staple-only enumeration on the GPU (ldo_enumerate): dict
-        "k1 k2" -> normalised weight, and a dict of counts and timing."""
+    def enumerate(self, min_total, max_total, max_type, ops=("numstaples", "numfulldomains"), shape=(9, 49),
+                  full=False, split_levels=0):
+        """Exact enumeration on the GPU: staple-only (ldo_enumerate) or, with
+        full, the scaffold enumerated too (ldo_enumerate_full, each unit split
+        into 6^split_levels parallel parts): dict "k1 k2" -> normalised
+        weight, and a dict of counts and timing."""
         w = np.zeros(shape[0] * shape[1])
         nconf = ctypes.c_double(0)
         nu = ctypes.c_int32(0)
         ms = ctypes.c_double(0)
-        self._check(self.lib.ldo_enumerate(self.h, int(min_total), int(max_total), int(max_type), ops[0].encode(),
-                                           ops[1].encode(), shape[0], shape[1], _dptr(w), ctypes.byref(nconf),
-                                           ctypes.byref(nu), ctypes.byref(ms)))
+        if full:
+            self._check(self.lib.ldo_enumerate_full(self.h, int(min_total), int(max_total), int(max_type),
+                                                    ops[0].encode(), ops[1].encode(), shape[0], shape[1],
+                                                    int(split_levels), _dptr(w), ctypes.byref(nconf),
+                                                    ctypes.byref(nu), ctypes.byref(ms)))
+        else:
+            self._check(self.lib.ldo_enumerate(self.h, int(min_total), int(max_total), int(max_type),
+                                               ops[0].encode(), ops[1].encode(), shape[0], shape[1], _dptr(w),
+                                               ctypes.byref(nconf), ctypes.byref(nu), ctypes.byref(ms)))
         w = w.reshape(shape)
         out = {"%d %d" % (a, b): float(w[a, b]) for a in range(shape[0]) for b in range(shape[1]) if w[a, b] != 0}
         return out, {"num_configs": nconf.value, "units": nu.value, "ms": ms.value}

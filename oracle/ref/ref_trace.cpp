@@ -56,6 +56,19 @@ class UnitStapleEnum : public enumerator::StapleConformationalEnumerator {
     vector<std::pair<double, double>> units;
 };
 
+// The same for the full conformational enumeration (the scaffold
+// enumerated too, ConformationalEnumerator::enumerate, src/enumerate.cpp:218).
+class UnitConfEnum : public enumerator::ConformationalEnumerator {
+  public:
+    using ConformationalEnumerator::ConformationalEnumerator;
+    void enumerate() override {
+        long double z0 = m_partition_f, n0 = m_num_configs;
+        ConformationalEnumerator::enumerate();
+        units.push_back({(double)(m_partition_f - z0), (double)(m_num_configs - n0)});
+    }
+    vector<std::pair<double, double>> units;
+};
+
 class TraceSim : public simulation::GCMCSimulation {
   public:
     TraceSim(origami::OrigamiSystem& o, orderParams::SystemOrderParams& ops,
@@ -165,8 +178,7 @@ int main(int argc, char** argv) {
             if (params.m_enumerate_staples_only)
                 ce = new UnitStapleEnum {*o, *oc, ops, biases, params.m_ops_to_output, params.m_apply_mean_field_cor};
             else
-                ce = new enumerator::ConformationalEnumerator {*o, *oc, ops, biases, params.m_ops_to_output,
-                                                               params.m_apply_mean_field_cor};
+                ce = new UnitConfEnum {*o, *oc, ops, biases, params.m_ops_to_output, params.m_apply_mean_field_cor};
             enumerator::GrowthpointEnumerator* ge;
             if (params.m_misbinding_pot == "Disallowed")
                 ge = new enumerator::NoMisbindingGrowthpointEnumerator {*ce, *o};
@@ -194,9 +206,10 @@ int main(int argc, char** argv) {
             js << b;
             // trace_units=1: the partition-function increment of every
             // growth-point set, in enumeration order
-            if (kv.count("trace_units") && kv["trace_units"] == "1" && params.m_enumerate_staples_only) {
+            if (kv.count("trace_units") && kv["trace_units"] == "1") {
                 js << ", \"units\": [";
-                auto& us = static_cast<UnitStapleEnum*>(ce)->units;
+                auto& us = params.m_enumerate_staples_only ? static_cast<UnitStapleEnum*>(ce)->units
+                                                           : static_cast<UnitConfEnum*>(ce)->units;
                 for (size_t i = 0; i < us.size(); ++i) {
                     std::snprintf(b, sizeof b, "%s[%.17g, %.17g]", i ? ", " : "", us[i].first, us[i].second);
                     js << b;

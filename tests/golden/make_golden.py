@@ -80,16 +80,21 @@ def flatten(chains):
 
 # exact enumerations: fixture name, case (the 4-domain system, whose staples
 # never bind both domains; the capped 8-domain system, where they do)
-ENUMERATIONS = [("c1_enumeration", "c1"), ("e8_enumeration", "e8"), ("e8s3_enumeration", "e8")]
+ENUMERATIONS = [("c1_enumeration", "c1"), ("e8_enumeration", "e8"), ("e8s3_enumeration", "e8"),
+                # the full conformational enumeration (scaffold enumerated too, src/enumerate.cpp:218)
+                ("c1full_enumeration", "c1"), ("c1full3_enumeration", "c1")]
 # extra .inp options of an enumeration (defaults: the case's own)
-ENUM_OPTS = {"e8s3_enumeration": {"max_total_staples": 3}}
+ENUM_OPTS = {"e8s3_enumeration": {"max_total_staples": 3},
+             "c1full_enumeration": {"enumerate_staples_only": "false", "max_total_staples": 2},
+             "c1full3_enumeration": {"enumerate_staples_only": "false", "max_total_staples": 3}}
 # enumerations recorded with the partition sum of every growth-point set
-ENUM_UNITS = {"e8_enumeration"}
+ENUM_UNITS = {"e8_enumeration", "c1full_enumeration"}
 
 
 def enumerate_case(tmp, name, case):
-    """Exact staple-only enumeration of a small system with the reference's
-    enumerator (src/enumerate.cpp:687), weights over (numstaples,
+    """Exact enumeration of a small system with the reference's enumerator
+    (staple-only, src/enumerate.cpp:687, or with the scaffold enumerated too,
+    :218, as enumerate_staples_only says), weights over (numstaples,
     numfulldomains) at full precision (oracle/ref/ref_trace.cpp's enumerate
     mode runs enumerate_main's sequence and prints the normalised weights)."""
     base = os.path.join(tmp, name)

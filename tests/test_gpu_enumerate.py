@@ -56,3 +56,36 @@ def test_enumeration_units_match_reference(data_dir):
     tol = 1e-10 * np.abs(ref[:, 0]) + np.maximum(ref[:, 1], 1.0) * ulp
     bad = np.abs(units[:, 0] - ref[:, 0]) > tol
     assert not bad.any(), (np.flatnonzero(bad)[:10], units[bad][:5], ref[bad][:5])
+
+
+@pytest.mark.parametrize("name,max_total,split", [("c1full_enumeration", 2, 0), ("c1full_enumeration", 2, 2),
+                                                  ("c1full3_enumeration", 3, 3)])
+def test_full_enumeration_matches_reference(name, max_total, split, data_dir):
+    """The full conformational enumeration (the scaffold enumerated too,
+    ConformationalEnumerator::enumerate) of the 4-domain system with up to
+    two and three staples, against the reference's own at full precision,
+    whole and split into 6^split parts per unit."""
+    import numpy as np
+    from latticednaorigami_gb300 import Engine
+    path = os.path.join(GOLDEN, name + ".json")
+    if not os.path.exists(path):
+        pytest.skip("fixture not generated")
+    with open(path) as f:
+        fx = json.load(f)
+    over = "\n".join("%s = %s" % kv for kv in sorted(fx["options"].items()))
+    eng = Engine(os.path.join(data_dir, "c1.inp"), n_replicas=1, seed=0, overrides=over)
+    w, info = eng.enumerate(0, max_total, 4, full=True, split_levels=split)
+    assert set(w) == set(fx["weights"]), (sorted(w), sorted(fx["weights"]))
+    for k, v in fx["weights"].items():
+        assert abs(w[k] - v) <= 1e-10 * v, (k, w[k], v)
+    assert abs(info["num_configs"] - fx["num_configs"]) <= 1e-9 * fx["num_configs"]
+    if "units" in fx:
+        units = eng.enumerate_units()
+        ref = np.array(fx["units"])
+        assert units.shape == ref.shape
+        np.testing.assert_allclose(units[:, 1], ref[:, 1], rtol=1e-12, atol=0)
+        total = ref[:, 0].sum()
+        ulp = 2.0 ** -63 * 2.0 ** np.ceil(np.log2(total))
+        tol = 1e-10 * np.abs(ref[:, 0]) + np.maximum(ref[:, 1], 1.0) * ulp
+        bad = np.abs(units[:, 0] - ref[:, 0]) > tol
+        assert not bad.any(), (np.flatnonzero(bad)[:10], units[bad][:5], ref[bad][:5])
