@@ -14,21 +14,6 @@ __device__ __forceinline__ void warp_copy16(void* dst, const void* src, int byte
     for (int k = lane; k < n; k += 32) d[k] = s[k];
 }
 
-// The same copy into a move snapshot in global memory, storing only the
-// 16-byte chunks that differ from what the snapshot already holds: a move
-// changes a few domains, so most of the snapshot stays clean in L2 instead
-// of being written back to DRAM.
-__device__ __forceinline__ void warp_store_changed16(void* dst, const void* src, int bytes, int lane) {
-    uint4* d = reinterpret_cast<uint4*>(dst);
-    const uint4* s = reinterpret_cast<const uint4*>(src);
-    int n = bytes >> 4;
-    for (int k = lane; k < n; k += 32) {
-        uint4 v = s[k];
-        uint4 o = d[k];
-        if (v.x != o.x || v.y != o.y || v.z != o.z || v.w != o.w) d[k] = v;
-    }
-}
-
 template <class C>
 __device__ void bind_rep(ldo::Rep<C>& r, const LdoLaunch& L, int rep) {
     r.ctl = L.ctl + rep;

@@ -41,6 +41,7 @@ __global__ void __launch_bounds__(32) ldo_enum_kernel(LdoEnumLaunch E) {
     W->sp = 0;
     W->npgp = 0;
     W->E = 0;
+    W->E_lo = 0;
     W->mult = 1;
     W->prefix = 1;
     W->part = 0;
@@ -68,7 +69,7 @@ __global__ void __launch_bounds__(32) ldo_enum_kernel(LdoEnumLaunch E) {
     for (int k = 0; k < U.n_chains; ++k) {
         W->prefix *= R->c_staple_M;
         cs[k] = R->add_chain(U.ident[k]);
-        if (R->mean_field) W->E += R->log6;
+        if (R->mean_field) W->E += R->log6;   // (at most eight terms: no drift to speak of)
         W->E += R->t_init_e;
         int len = R->sys->type_len[U.ident[k]];
         if (!R->bad())

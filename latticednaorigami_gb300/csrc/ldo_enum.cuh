@@ -35,7 +35,7 @@ struct EnumWork {
     int16_t gp_of[C::DCAP];       // m_growthpoints
     int16_t inv_gp[C::DCAP];      // m_inverse_growthpoints
     uint8_t zero_ore[C::DCAP];    // orientation (0, 0, 0) in the reference
-    double E, mult, prefix;
+    double E, E_lo, mult, prefix;     // E + E_lo: the running energy, summed without rounding drift
     double part, nconf, sumE;
     double* row;                  // this unit's histogram row
     int op1, op2, n1, n2;         // key order parameters and histogram shape
@@ -60,6 +60,16 @@ struct Enumerator {
         return R.set_domain_config(d, p, o);
     }
     __device__ double unset(int d) { return R.unassign_domain(d); }
+    // m_energy (long double in the reference) as a two-term sum: a traversal
+    // adds and removes millions of domain energies, whose FP64 roundings would
+    // otherwise drift (TwoSum, Knuth; the error term collects each rounding)
+    __device__ void addE(double x) {
+        double s = W.E + x;
+        double bp = s - W.E;
+        W.E_lo += (W.E - (s - bp)) + (x - bp);
+        W.E = s;
+    }
+    __device__ double energy() const { return W.E + W.E_lo; }
     __device__ int16_t& count(int ident) { return W.cnt[ident + LDO_ENUM_MAX_IDENT]; }
     // a unit split by a prefix follows only its branch at the first levels
     __device__ bool skip(int level, int k) const { return level < W.npre && k != W.pre[level]; }
@@ -68,9 +78,10 @@ struct Enumerator {
     __device__ __noinline__ void save() {
         W.nconf += W.mult;
         R.update_move_params();
-        double w = W.prefix * exp(-W.E) * W.mult;
+        double e = energy();
+        double w = W.prefix * exp(-e) * W.mult;
         W.part += w;
-        W.sumE += W.E * w;
+        W.sumE += e * w;
         int k1 = R.op[2 * W.op1], k2 = R.op[2 * W.op2];
         if (k1 < 0 || k1 >= W.n1 || k2 < 0 || k2 >= W.n2) {
             W.bad = 1;
@@ -168,7 +179,7 @@ struct Enumerator {
         }
         if (W.sp != 0) next_from(pop(), p);
         else save();
-        W.E += unset(d);
+        addE(unset(d));
     }
     __device__ __noinline__ void grow_next_full(int d, V3 p) {
         if (W.sp != 0) {
@@ -192,14 +203,14 @@ struct Enumerator {
         else {
             save();
         }
-        W.E += unset(d);
+        addE(unset(d));
     }
 
     // StapleConformationalEnumerator::grow_off_scaffold (:754)
     __device__ __noinline__ void grow_off_scaffold(int nd) {
         int g = W.inv_gp[nd];
         V3 p = R.pos(g);
-        W.E += set(nd, p, R.ore[g] ^ 1);
+        addE(set(nd, p, R.ore[g] ^ 1));
         if (R.hdr.violated) {
             R.hdr.violated = 0;
             push(nd);
@@ -209,17 +220,18 @@ struct Enumerator {
                 next_from(pop(), p);
                 push(nd);
             }
-            W.E += unset(nd);
+            addE(unset(nd));
         }
     }
 
     // StapleConformationalEnumerator::set_unbound_domain (:781)
     __device__ __noinline__ void set_unbound(int d, V3 p) {
-        W.E += set(d, p, 0);
+        addE(set(d, p, 0));
         W.zero_ore[d] = 1;
+        double mult0 = W.mult;   // restored, not divided back: no drift over a traversal
         W.mult *= 6.0;
         grow_next(d, p);
-        W.mult /= 6.0;
+        W.mult = mult0;
     }
 
     // ConformationalEnumerator::set_unbound_domain (:523): every orientation
@@ -229,19 +241,20 @@ struct Enumerator {
         int id = R.did[d];
         if (count(-id) == 0) {
             count(id) -= 1;
-            W.E += set(d, p, 0);
+            addE(set(d, p, 0));
             W.zero_ore[d] = 1;
+            double mult0 = W.mult;   // restored, not divided back: no drift over a traversal
             W.mult *= 6.0;
             grow_next_full(d, p);
             count(id) += 1;
-            W.mult /= 6.0;
+            W.mult = mult0;
             return;
         }
         int level = W.depth++;
         #pragma unroll 1
         for (int o = 0; o < 6; ++o) {
             if (skip(level, o)) continue;
-            W.E += set(d, p, o);
+            addE(set(d, p, o));
             if (R.hdr.violated) {
                 R.hdr.violated = 0;
                 continue;
@@ -257,18 +270,19 @@ struct Enumerator {
     __device__ __noinline__ void set_bound(int d, V3 p) {
         int occ = R.unbound_at(p);
         int zero = W.zero_ore[occ];
-        W.E += set(d, p, R.ore[occ] ^ 1);
+        addE(set(d, p, R.ore[occ] ^ 1));
         W.zero_ore[d] = (uint8_t)zero;
         if (R.hdr.violated) {
             R.hdr.violated = 0;
             return;
         }
         double m = overcount(d, occ);
+        double mult0 = W.mult;   // restored, not divided back: no drift over a traversal
         W.mult *= m;
         count(R.did[d]) -= 1;
         grow_next(d, p);
         count(R.did[d]) += 1;
-        W.mult /= m;
+        W.mult = mult0;
     }
 
     // ConformationalEnumerator::set_comp_growthpoint_domains (:451)
@@ -277,11 +291,11 @@ struct Enumerator {
         #pragma unroll 1
         for (int o = 0; o < 6; ++o) {
             if (skip(level, o)) continue;
-            W.E += set(d, p, o);
-            W.E += set(bd, p, o ^ 1);
+            addE(set(d, p, o));
+            addE(set(bd, p, o ^ 1));
             if (R.hdr.violated) {
                 R.hdr.violated = 0;
-                W.E += unset(d);
+                addE(unset(d));
                 continue;
             }
             count(R.did[d]) -= 1;
@@ -289,23 +303,24 @@ struct Enumerator {
             grow_next(bd, p);
             count(R.did[d]) += 1;
             count(R.did[bd]) += 1;
-            W.E += unset(d);
+            addE(unset(d));
         }
         W.depth--;
     }
 
     // ConformationalEnumerator::set_mis_growthpoint_domains (:477)
     __device__ __noinline__ void set_mis_gp(int d, int bd, V3 p) {
-        W.E += set(d, p, 0);
-        W.E += set(bd, p, 1);
+        addE(set(d, p, 0));
+        addE(set(bd, p, 1));
+        double mult0 = W.mult;   // restored, not divided back: no drift over a traversal
         W.mult *= 6.0;
         count(R.did[d]) -= 1;
         count(R.did[bd]) -= 1;
         grow_next(bd, p);
         count(R.did[d]) += 1;
         count(R.did[bd]) += 1;
-        W.E += unset(d);
-        W.mult /= 6.0;
+        addE(unset(d));
+        W.mult = mult0;
     }
 
     // ConformationalEnumerator::set_growthpoint_domains (:413)
@@ -382,13 +397,13 @@ struct Enumerator {
         if (W.gp_of[start] >= 0) {
             W.pgp[W.npgp++] = p;
             count(R.did[nd]) -= 1;
-            W.E += set(nd, p, 1);
+            addE(set(nd, p, 1));
             if (W.sp > 0) {
                 int nn = pop();
                 enumerate_domain(nn, p);
             }
             count(R.did[nd]) += 1;
-            W.E += unset(nd);
+            addE(unset(nd));
             W.npgp--;
         }
         else {
@@ -408,7 +423,7 @@ struct Enumerator {
         int start = pop();
         int g = W.inv_gp[start];
         V3 p = R.pos(g);
-        W.E += set(start, p, R.ore[g] ^ 1);
+        addE(set(start, p, R.ore[g] ^ 1));
         if (W.sp != 0) {
             int nd = pop();
             next_from(nd, p);
@@ -416,7 +431,7 @@ struct Enumerator {
         else {
             save();
         }
-        if (R.st[start] != UNASSIGNED) W.E += unset(start);
+        if (R.st[start] != UNASSIGNED) addE(unset(start));
     }
 };
 

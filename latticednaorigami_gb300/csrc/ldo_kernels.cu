@@ -49,11 +49,9 @@ __device__ __forceinline__ void snapshot_ops(int cmd, ldo::Rep<C>* R, unsigned c
         tab = h.tab;
     }
     __syncwarp();
-    if (sn >= 0 && !(cmd & ldo::CMD_REST_FIRST))
-        warp_store_changed16(snap + (size_t)sn * snap_stride<C>(), base, snap_bytes<C>(), lane);
+    if (sn >= 0 && !(cmd & ldo::CMD_REST_FIRST)) warp_copy16(snap + (size_t)sn * snap_stride<C>(), base, snap_bytes<C>(), lane);
     if (rs >= 0) warp_copy16(base, snap + (size_t)rs * snap_stride<C>(), snap_bytes<C>(), lane);
-    if (sn >= 0 && (cmd & ldo::CMD_REST_FIRST))
-        warp_store_changed16(snap + (size_t)sn * snap_stride<C>(), base, snap_bytes<C>(), lane);
+    if (sn >= 0 && (cmd & ldo::CMD_REST_FIRST)) warp_copy16(snap + (size_t)sn * snap_stride<C>(), base, snap_bytes<C>(), lane);
     __syncwarp();
     if (lane == 0 && rs >= 0) {
         h.steps_done = steps_done;
@@ -126,7 +124,7 @@ __global__ void __launch_bounds__(128, 7) ldo_mc_kernel(LdoLaunch L) {
     if (nsteps > 0) {
         unsigned char* snap = L.snap + (size_t)rep * ldo::N_SNAPSHOTS * snap_stride<C>();
         __syncwarp();
-        warp_store_changed16(snap, base, snap_bytes<C>(), lane);   // snapshot 0: state at the start of the move
+        warp_copy16(snap, base, snap_bytes<C>(), lane);   // snapshot 0: state at the start of the move
         for (long long k = 0; k < nsteps; ++k) {
             int cmd = 0;
             if (lane == 0) cmd = R->bad() ? ldo::CMD_STOP : R->template step_begin<CT>(h.steps_done + 1);
