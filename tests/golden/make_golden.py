@@ -88,7 +88,7 @@ ENUM_OPTS = {"e8s3_enumeration": {"max_total_staples": 3},
              "c1full_enumeration": {"enumerate_staples_only": "false", "max_total_staples": 2},
              "c1full3_enumeration": {"enumerate_staples_only": "false", "max_total_staples": 3}}
 # enumerations recorded with the partition sum of every growth-point set
-ENUM_UNITS = {"e8_enumeration", "c1full_enumeration"}
+ENUM_UNITS = {"e8_enumeration", "c1full_enumeration", "c1full3_enumeration"}
 
 
 def enumerate_case(tmp, name, case):
