@@ -290,6 +290,11 @@ ldo_status ldo_enumerate_full(ldo_engine* e, int32_t min_total, int32_t max_tota
                               const char* op1_tag, const char* op2_tag, int32_t n1, int32_t n2, int32_t split_levels,
                               double* weights, double* num_configs, int32_t* n_units, double* device_ms);
 
+/* The last enumeration's weights unit by unit: out[(u * n1 + k1) * n2 + k2]
+ * the unnormalised weight of (op1, op2) = (k1, k2) within unit u (cap: room
+ * for n_units * n1 * n2 doubles; NULL out: count only). */
+ldo_status ldo_enumerate_unit_weights(ldo_engine* e, double* out, int64_t cap, int32_t* n_units);
+
 /* The last ldo_enumerate's work units (the reference's growth-point sets, in
  * its enumeration order): out[2u] the unit's partition-function sum before
  * normalisation, out[2u+1] its number of configurations (NULL out: count

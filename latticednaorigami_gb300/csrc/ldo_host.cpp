@@ -2248,6 +2248,8 @@ struct ldo_engine {
     }
 
     vector<double> enum_units;   // last enumeration: (partition sum, configurations) per unit
+    vector<double> enum_unit_w;  // last enumeration: per unit, its (op1, op2) weights before normalisation
+    int enum_n1 {0}, enum_n2 {0};
 
     // Exact staple-only enumeration (enumerate_main with
     // enumerate_staples_only, src/enumerate.cpp:19) of replica 0's system at
@@ -2330,6 +2332,9 @@ struct ldo_engine {
         double part = 0, nconf = 0;
         for (int k = 0; k < n1 * n2; ++k) w[k] = 0;
         enum_units.assign(2 * (size_t)nu, 0.0);
+        enum_unit_w.assign((size_t)nu * n1 * n2, 0.0);
+        enum_n1 = n1;
+        enum_n2 = n2;
         for (size_t q = 0; q < nb; ++q) {   // parts in unit order, each unit's parts in branch order
             if (stats[4 * q + 3] < 0) throw LdoError(LDO_EINVAL, "enumeration: an order parameter value outside the histogram");
             if (stats[4 * q + 3] > 0) throw LdoError((ldo_status)(int)stats[4 * q + 3], "enumeration: a unit failed");
@@ -2337,7 +2342,10 @@ struct ldo_engine {
             nconf += stats[4 * q + 1];
             enum_units[2 * (q / parts)] += stats[4 * q];
             enum_units[2 * (q / parts) + 1] += stats[4 * q + 1];
-            for (int k = 0; k < n1 * n2; ++k) w[k] += hist[q * n1 * n2 + k];
+            for (int k = 0; k < n1 * n2; ++k) {
+                w[k] += hist[q * n1 * n2 + k];
+                enum_unit_w[(q / parts) * n1 * n2 + k] += hist[q * n1 * n2 + k];
+            }
         }
         // ConformationalEnumerator::normalize_weights (:344)
         for (int k = 0; k < n1 * n2; ++k) w[k] /= part;
@@ -2458,6 +2466,16 @@ ldo_status ldo_enumerate_full(ldo_engine* e, int32_t min_total, int32_t max_tota
                               double* weights, double* num_configs, int32_t* n_units, double* device_ms) {
     return enumerate_call(e, min_total, max_total, max_type, op1_tag, op2_tag, n1, n2, weights, num_configs, n_units,
                           device_ms, 1, split_levels);
+}
+
+ldo_status ldo_enumerate_unit_weights(ldo_engine* e, double* out, int64_t cap, int32_t* n_units) {
+    if (!e || !n_units) return LDO_EINVAL;
+    int nu = (int)(e->enum_units.size() / 2);
+    *n_units = nu;
+    if (!out) return LDO_OK;
+    if (cap < (int64_t)e->enum_unit_w.size()) return LDO_EINVAL;
+    std::copy(e->enum_unit_w.begin(), e->enum_unit_w.end(), out);
+    return LDO_OK;
 }
 
 ldo_status ldo_enumerate_units(ldo_engine* e, double* out, int32_t cap, int32_t* n_units) {

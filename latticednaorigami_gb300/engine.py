@@ -26,6 +26,7 @@ EXPORTS = [
     "ldo_set_bias_centre", "ldo_swap_writer_open", "ldo_set_config", "ldo_set_configs", "ldo_anneal_run", "ldo_read_trj_frame", "ldo_checkpoint_save",
     "ldo_checkpoint_load", "ldo_autotune", "ldo_autotune_candidates", "ldo_us_write_biases",
     "ldo_us_read_biases", "ldo_us_reset", "ldo_read_biases", "ldo_enumerate", "ldo_enumerate_full", "ldo_enumerate_units",
+    "ldo_enumerate_unit_weights",
     "ldo_batch_create", "ldo_batch_destroy", "ldo_batch_last_error", "ldo_batch_num_groups", "ldo_batch_group",
     "ldo_batch_set_controls", "ldo_batch_run", "ldo_batch_run_sweeps", "ldo_batch_set_sampling",
     "ldo_batch_get_samples", "ldo_batch_get_counters", "ldo_batch_autotune",
@@ -91,6 +92,7 @@ def load_library(path=None):
                                   ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, dp, dp,
                                   ctypes.POINTER(ctypes.c_int32), dp]
     lib.ldo_enumerate_units.argtypes = [vp, dp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
+    lib.ldo_enumerate_unit_weights.argtypes = [vp, dp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32)]
     lib.ldo_enumerate_full.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p,
                                        ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, dp,
                                        dp, ctypes.POINTER(ctypes.c_int32), dp]
@@ -253,6 +255,15 @@ class Engine:
         out = np.zeros(2 * n.value)
         self._check(self.lib.ldo_enumerate_units(self.h, _dptr(out), n.value, ctypes.byref(n)))
         return out.reshape(-1, 2)
+
+    def enumerate_unit_weights(self, shape=(9, 49)):
+        """Unnormalised (op1, op2) weights of every unit of the last
+        enumeration (shape: the histogram shape it was called with)."""
+        n = ctypes.c_int32(0)
+        self._check(self.lib.ldo_enumerate_unit_weights(self.h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value * shape[0] * shape[1])
+        self._check(self.lib.ldo_enumerate_unit_weights(self.h, _dptr(out), out.size, ctypes.byref(n)))
+        return out.reshape(n.value, shape[0], shape[1])
 
     def autotune(self, probe_sweeps=4, use_cache=True):
         """The engine's autotuner (ldo_autotune): the fastest launch shape for

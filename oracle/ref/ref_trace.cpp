@@ -57,16 +57,29 @@ class UnitStapleEnum : public enumerator::StapleConformationalEnumerator {
 };
 
 // The same for the full conformational enumeration (the scaffold
-// enumerated too, ConformationalEnumerator::enumerate, src/enumerate.cpp:218).
+// enumerated too, ConformationalEnumerator::enumerate, src/enumerate.cpp:218),
+// with the change of the running energy m_energy over the unit, which every
+// set and unassign leaves balanced in exact arithmetic (its rounding drift).
 class UnitConfEnum : public enumerator::ConformationalEnumerator {
   public:
     using ConformationalEnumerator::ConformationalEnumerator;
     void enumerate() override {
-        long double z0 = m_partition_f, n0 = m_num_configs;
+        long double z0 = m_partition_f, n0 = m_num_configs, e0 = m_energy;
+        std::map<vector<int>, double> w0(m_state_weights.begin(), m_state_weights.end());
         ConformationalEnumerator::enumerate();
         units.push_back({(double)(m_partition_f - z0), (double)(m_num_configs - n0)});
+        drift.push_back((double)(m_energy - e0));
+        // each bin's increment over the unit (its double running sum's)
+        std::map<vector<int>, double> inc;
+        for (auto& kv : m_state_weights) {
+            double before = w0.count(kv.first) ? w0[kv.first] : 0.0;
+            if (kv.second != before) inc[kv.first] = kv.second - before;
+        }
+        bins.push_back(inc);
     }
     vector<std::pair<double, double>> units;
+    vector<double> drift;
+    vector<std::map<vector<int>, double>> bins;
 };
 
 class TraceSim : public simulation::GCMCSimulation {
@@ -215,6 +228,31 @@ int main(int argc, char** argv) {
                     js << b;
                 }
                 js << "]";
+                if (!params.m_enumerate_staples_only && kv.count("trace_unit_bins") && kv["trace_unit_bins"] == "1") {
+                    js << ", \"unit_bins\": [";
+                    auto& bs = static_cast<UnitConfEnum*>(ce)->bins;
+                    for (size_t i = 0; i < bs.size(); ++i) {
+                        js << (i ? ", {" : "{");
+                        bool f = true;
+                        for (auto& e : bs[i]) {
+                            std::snprintf(b, sizeof b, "%s\"%d %d\": %.17g", f ? "" : ", ", e.first[0], e.first[1],
+                                          e.second);
+                            js << b;
+                            f = false;
+                        }
+                        js << "}";
+                    }
+                    js << "]";
+                }
+                if (!params.m_enumerate_staples_only) {
+                    js << ", \"unit_energy_drift\": [";
+                    auto& dr = static_cast<UnitConfEnum*>(ce)->drift;
+                    for (size_t i = 0; i < dr.size(); ++i) {
+                        std::snprintf(b, sizeof b, "%s%.17g", i ? ", " : "", dr[i]);
+                        js << b;
+                    }
+                    js << "]";
+                }
             }
             js << "}";
             std::cout << "\n" << js.str() << "\n";

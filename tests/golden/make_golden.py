@@ -112,7 +112,9 @@ def enumerate_case(tmp, name, case):
     with open(path, "w") as f:
         json.dump({"case": case, "ops": ["numstaples", "numfulldomains"], "options": ENUM_OPTS.get(name, {}),
                    "weights": d["weights"], "num_configs": d["num_configs"],
-                   **({"units": d["units"]} if "units" in d else {})}, f, sort_keys=True)
+                   **({"units": d["units"]} if "units" in d else {}),
+                   **({"unit_energy_drift": d["unit_energy_drift"]} if "unit_energy_drift" in d else {})},
+                  f, sort_keys=True)
     print(path, d["weights"], "%.1f s" % d["seconds"])
 
 

@@ -64,7 +64,15 @@ def test_full_enumeration_matches_reference(name, max_total, split, data_dir):
     """The full conformational enumeration (the scaffold enumerated too,
     ConformationalEnumerator::enumerate) of the 4-domain system with up to
     two and three staples, against the reference's own at full precision,
-    whole and split into 6^split parts per unit."""
+    whole and split into 6^split parts per unit.
+
+    The reference carries one running energy (long double) through the whole
+    enumeration, some 1e12 balanced sets and unassignments; the rounding of
+    each leaves a drift, recorded per unit by the trace driver
+    (unit_energy_drift).  A configuration's weight exp(-E) then carries the
+    drift accumulated before it as a relative error, so the weights are
+    compared at 1e-10 plus twice the largest accumulated drift.  The engine
+    restarts the energy at every unit and sums it without drift."""
     import numpy as np
     from latticednaorigami_gb300 import Engine
     path = os.path.join(GOLDEN, name + ".json")
@@ -75,9 +83,13 @@ def test_full_enumeration_matches_reference(name, max_total, split, data_dir):
     over = "\n".join("%s = %s" % kv for kv in sorted(fx["options"].items()))
     eng = Engine(os.path.join(data_dir, "c1.inp"), n_replicas=1, seed=0, overrides=over)
     w, info = eng.enumerate(0, max_total, 4, full=True, split_levels=split)
+    drift = np.array(fx.get("unit_energy_drift", [0.0]))
+    offset = np.concatenate([[0.0], np.cumsum(drift)])
+    bound = float(np.max(np.abs(offset[:-1]) + np.abs(drift)))
+    rtol = 1e-10 + 2 * bound
     assert set(w) == set(fx["weights"]), (sorted(w), sorted(fx["weights"]))
     for k, v in fx["weights"].items():
-        assert abs(w[k] - v) <= 1e-10 * v, (k, w[k], v)
+        assert abs(w[k] - v) <= rtol * v, (k, w[k], v, rtol)
     assert abs(info["num_configs"] - fx["num_configs"]) <= 1e-9 * fx["num_configs"]
     if "units" in fx:
         units = eng.enumerate_units()
