@@ -47,8 +47,10 @@ __global__ void __launch_bounds__(32) ldo_enum_kernel(LdoEnumLaunch E) {
     W->part = 0;
     W->nconf = 0;
     W->sumE = 0;
-    W->row = E.hist + (size_t)b * E.n1 * E.n2;
-    for (int k = 0; k < E.n1 * E.n2; ++k) W->row[k] = 0;
+    W->part_c = 0;
+    W->sumE_c = 0;
+    W->row = E.hist + (size_t)b * 2 * E.n1 * E.n2;
+    for (int k = 0; k < 2 * E.n1 * E.n2; ++k) W->row[k] = 0;
     W->op1 = E.op1;
     W->op2 = E.op2;
     W->n1 = E.n1;
@@ -88,10 +90,12 @@ __global__ void __launch_bounds__(32) ldo_enum_kernel(LdoEnumLaunch E) {
         if (E.full) en.run_full();
         else en.run();
     }
+    // the compensated sums, folded
+    for (int k = 0; k < E.n1 * E.n2; ++k) W->row[k] += W->row[E.n1 * E.n2 + k];
     double* st = E.stats + 4 * (size_t)b;
-    st[0] = W->part;
+    st[0] = W->part + W->part_c;
     st[1] = W->nconf;
-    st[2] = W->sumE;
+    st[2] = W->sumE + W->sumE_c;
     st[3] = R->bad() ? (double)R->hdr.status : (W->bad ? -1.0 : 0.0);
 }
 

@@ -37,7 +37,8 @@ struct EnumWork {
     uint8_t zero_ore[C::DCAP];    // orientation (0, 0, 0) in the reference
     double E, E_lo, mult, prefix;     // E + E_lo: the running energy, summed without rounding drift
     double part, nconf, sumE;
-    double* row;                  // this unit's histogram row
+    double part_c, sumE_c;        // compensations of part and sumE
+    double* row;                  // this part's histogram row, then its compensations
     int op1, op2, n1, n2;         // key order parameters and histogram shape
     int overcount;                // 0 MaxTwoDomain, 1 MisbindingOnly
     int bad;                      // a key outside the histogram
@@ -70,6 +71,13 @@ struct Enumerator {
         W.E = s;
     }
     __device__ double energy() const { return W.E + W.E_lo; }
+    // Neumaier's compensated summation: s + c is the sum of the added terms
+    // without the drift a running double sum picks up over millions of terms
+    __device__ static void acc(double& s, double& c, double x) {
+        double t = s + x;
+        c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
+        s = t;
+    }
     __device__ int16_t& count(int ident) { return W.cnt[ident + LDO_ENUM_MAX_IDENT]; }
     // a unit split by a prefix follows only its branch at the first levels
     __device__ bool skip(int level, int k) const { return level < W.npre && k != W.pre[level]; }
@@ -80,14 +88,15 @@ struct Enumerator {
         R.update_move_params();
         double e = energy();
         double w = W.prefix * exp(-e) * W.mult;
-        W.part += w;
-        W.sumE += e * w;
+        acc(W.part, W.part_c, w);
+        acc(W.sumE, W.sumE_c, e * w);
         int k1 = R.op[2 * W.op1], k2 = R.op[2 * W.op2];
         if (k1 < 0 || k1 >= W.n1 || k2 < 0 || k2 >= W.n2) {
             W.bad = 1;
             return;
         }
-        W.row[k1 * W.n2 + k2] += w;
+        int k = k1 * W.n2 + k2;
+        acc(W.row[k], W.row[W.n1 * W.n2 + k], w);
     }
 
     // MaxTwoDomainOvercountCalculator::count_involved_staples (:131)

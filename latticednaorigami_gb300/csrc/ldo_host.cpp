@@ -421,6 +421,18 @@ vector<float> ldo_learn_init_params(uint32_t seed) {
     return p;
 }
 
+// Neumaier's compensated summation (value() is the sum without the drift a
+// running double sum accumulates)
+struct CompSum {
+    double s = 0, c = 0;
+    void add(double x) {
+        double t = s + x;
+        c += std::fabs(s) >= std::fabs(x) ? (s - t) + x : (x - t) + s;
+        s = t;
+    }
+    double value() const { return s + c; }
+};
+
 // Work units of the exact staple-only enumeration, in the order the reference
 // walks them: StapleEnumerator::enumerate / recurse (src/enumerate.cpp:1082,
 // :1103) over staple sets, and for each set GrowthpointEnumerator::enumerate
@@ -2284,7 +2296,7 @@ struct ldo_engine {
         for (int k = 0; k < split; ++k) parts *= 6;
         size_t nb = (size_t)nu * parts;   // one block per part of a unit
         size_t stride = ldo_enum_work_bytes(lay.cls);
-        if (nb * (stride + (size_t)n1 * n2 * sizeof(double)) > ((size_t)8 << 30))
+        if (nb * (stride + 2 * (size_t)n1 * n2 * sizeof(double)) > ((size_t)8 << 30))
             throw LdoError(LDO_ECAPACITY, "enumeration: more than 8 GiB of per-part working memory");
         DevBuf<LdoEnumUnit> d_units;
         d_units.alloc(nu);
@@ -2292,7 +2304,7 @@ struct ldo_engine {
         DevBuf<unsigned char> d_work;
         d_work.alloc(nb * stride);
         DevBuf<double> d_hist, d_stats;
-        d_hist.alloc(nb * n1 * n2);
+        d_hist.alloc(nb * 2 * n1 * n2);
         d_stats.alloc(nb * 4);
         LdoEnumLaunch E {};
         E.L = launch_params(LDO_MODE_RUN, 0);
@@ -2326,30 +2338,42 @@ struct ldo_engine {
             CU(cudaEventElapsedTime(&f, ev0, ev1));
             *ms = f;
         }
-        vector<double> hist(nb * n1 * n2), stats(nb * 4);
+        const size_t nk = (size_t)n1 * n2;
+        vector<double> hist(nb * 2 * nk), stats(nb * 4);
         CU(copy(hist.data(), d_hist.p, hist.size() * sizeof(double), cudaMemcpyDeviceToHost));
         CU(copy(stats.data(), d_stats.p, stats.size() * sizeof(double), cudaMemcpyDeviceToHost));
-        double part = 0, nconf = 0;
-        for (int k = 0; k < n1 * n2; ++k) w[k] = 0;
+        // every sum over parts compensated, as the parts' own sums are
+        CompSum part, nconf;
+        vector<CompSum> wt(nk), uw(nk);
         enum_units.assign(2 * (size_t)nu, 0.0);
-        enum_unit_w.assign((size_t)nu * n1 * n2, 0.0);
+        enum_unit_w.assign((size_t)nu * nk, 0.0);
         enum_n1 = n1;
         enum_n2 = n2;
+        CompSum upart, uconf;
         for (size_t q = 0; q < nb; ++q) {   // parts in unit order, each unit's parts in branch order
             if (stats[4 * q + 3] < 0) throw LdoError(LDO_EINVAL, "enumeration: an order parameter value outside the histogram");
             if (stats[4 * q + 3] > 0) throw LdoError((ldo_status)(int)stats[4 * q + 3], "enumeration: a unit failed");
-            part += stats[4 * q];
-            nconf += stats[4 * q + 1];
-            enum_units[2 * (q / parts)] += stats[4 * q];
-            enum_units[2 * (q / parts) + 1] += stats[4 * q + 1];
-            for (int k = 0; k < n1 * n2; ++k) {
-                w[k] += hist[q * n1 * n2 + k];
-                enum_unit_w[(q / parts) * n1 * n2 + k] += hist[q * n1 * n2 + k];
+            part.add(stats[4 * q]);
+            nconf.add(stats[4 * q + 1]);
+            upart.add(stats[4 * q]);
+            uconf.add(stats[4 * q + 1]);
+            const double* h = hist.data() + q * 2 * nk;   // the folded sums; the scratch half follows
+            for (size_t k = 0; k < nk; ++k) {
+                wt[k].add(h[k]);
+                uw[k].add(h[k]);
+            }
+            if ((q + 1) % parts == 0) {   // the unit's last part
+                size_t u = q / parts;
+                enum_units[2 * u] = upart.value();
+                enum_units[2 * u + 1] = uconf.value();
+                for (size_t k = 0; k < nk; ++k) enum_unit_w[u * nk + k] = uw[k].value();
+                upart = uconf = CompSum {};
+                for (auto& c : uw) c = CompSum {};
             }
         }
         // ConformationalEnumerator::normalize_weights (:344)
-        for (int k = 0; k < n1 * n2; ++k) w[k] /= part;
-        if (num_configs) *num_configs = nconf;
+        for (size_t k = 0; k < nk; ++k) w[k] = wt[k].value() / part.value();
+        if (num_configs) *num_configs = nconf.value();
         if (n_units) *n_units = nu;
     }
 

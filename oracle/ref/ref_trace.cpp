@@ -11,6 +11,7 @@
 //             trace_mode (simulate | enumerate | anneal: the reference's
 //             annealing loop over max_temp .. min_temp)
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -77,6 +78,58 @@ class UnitConfEnum : public enumerator::ConformationalEnumerator {
         }
         bins.push_back(inc);
     }
+
+    // With exact_bins set, the weight of every configuration, as
+    // calc_and_save_weights (src/enumerate.cpp:639) computes and adds it, is
+    // also summed into a compensated long-double sum per bin.  The reference
+    // keeps each bin of m_state_weights as a running double sum, whose
+    // roundings accumulate over the millions of configurations of a bin; the
+    // compensated sums are the same weights summed without that error.  The
+    // weight is read off m_partition_f (zeroed before the configuration is
+    // saved, so that it holds exactly the added weight) and m_partition_f is
+    // then given the value the reference's own addition gives.
+    void grow_next_domain(domainContainer::Domain* domain, utility::VectorThree p_new) override {
+        if (!exact_bins || !m_domains.empty()) {
+            ConformationalEnumerator::grow_next_domain(domain, p_new);
+            return;
+        }
+        m_ops.update_move_params();   // recomputes from the system: the key calc_and_save_weights reads
+        vector<int> key;
+        for (auto op : m_ops_to_output) key.push_back(op.get().get_param());
+        long double z = m_partition_f, n = m_num_configs;
+        m_partition_f = 0;
+        ConformationalEnumerator::grow_next_domain(domain, p_new);
+        long double w = m_partition_f;
+        m_partition_f = z + w;
+        if (m_num_configs != n) {
+            ++exact_calls;
+            if (key.size() == 2 && key[0] >= 0 && key[0] < 64 && key[1] >= 0 && key[1] < 64) flat[key[0] * 64 + key[1]].add(w);
+            else other[key].add(w);
+        }
+    }
+    // Neumaier's compensated summation in long double
+    struct Acc {
+        long double s = 0, c = 0;
+        long long n = 0;
+        void add(long double x) {
+            long double t = s + x;
+            c += (fabsl(s) >= fabsl(x)) ? (s - t) + x : (x - t) + s;
+            s = t;
+            ++n;
+        }
+        long double value() const { return s + c; }
+    };
+    std::map<vector<int>, Acc> exact() const {
+        std::map<vector<int>, Acc> out(other.begin(), other.end());
+        for (int k = 0; k < 64 * 64; ++k)
+            if (flat[k].n) out[{k / 64, k % 64}] = flat[k];
+        return out;
+    }
+    bool exact_bins = false;
+    long long exact_calls = 0;
+    vector<Acc> flat = vector<Acc>(64 * 64);
+    std::map<vector<int>, Acc> other;
+
     vector<std::pair<double, double>> units;
     vector<double> drift;
     vector<std::map<vector<int>, double>> bins;
@@ -190,8 +243,11 @@ int main(int argc, char** argv) {
             enumerator::ConformationalEnumerator* ce;
             if (params.m_enumerate_staples_only)
                 ce = new UnitStapleEnum {*o, *oc, ops, biases, params.m_ops_to_output, params.m_apply_mean_field_cor};
-            else
-                ce = new UnitConfEnum {*o, *oc, ops, biases, params.m_ops_to_output, params.m_apply_mean_field_cor};
+            else {
+                auto* uc = new UnitConfEnum {*o, *oc, ops, biases, params.m_ops_to_output, params.m_apply_mean_field_cor};
+                uc->exact_bins = kv.count("trace_exact_bins") && kv["trace_exact_bins"] == "1";
+                ce = uc;
+            }
             enumerator::GrowthpointEnumerator* ge;
             if (params.m_misbinding_pot == "Disallowed")
                 ge = new enumerator::NoMisbindingGrowthpointEnumerator {*ce, *o};
@@ -217,6 +273,34 @@ int main(int argc, char** argv) {
             char b[128];
             std::snprintf(b, sizeof b, "}, \"num_configs\": %.17Lg, \"seconds\": %.6f", ce->num_configs(), secs);
             js << b;
+            // trace_exact_bins=1: every bin summed without rounding drift
+            // (compensated), normalised by the compensated partition function,
+            // with the number of configurations saved into the bin
+            if (!params.m_enumerate_staples_only && static_cast<UnitConfEnum*>(ce)->exact_bins) {
+                auto* uc = static_cast<UnitConfEnum*>(ce);
+                auto ex = uc->exact();
+                UnitConfEnum::Acc z;
+                for (auto& e : ex) z.add(e.second.value());
+                js << ", \"weights_exact\": {";
+                bool f = true;
+                for (auto& e : ex) {
+                    js << (f ? "\"" : ", \"");
+                    for (size_t i = 0; i < e.first.size(); ++i) js << (i ? " " : "") << e.first[i];
+                    std::snprintf(b, sizeof b, "\": %.17g", (double)(e.second.value() / z.value()));
+                    js << b;
+                    f = false;
+                }
+                js << "}, \"bin_configs\": {";
+                f = true;
+                for (auto& e : ex) {
+                    js << (f ? "\"" : ", \"");
+                    for (size_t i = 0; i < e.first.size(); ++i) js << (i ? " " : "") << e.first[i];
+                    js << "\": " << e.second.n;
+                    f = false;
+                }
+                std::snprintf(b, sizeof b, "}, \"saved_configs\": %lld", uc->exact_calls);
+                js << b;
+            }
             // trace_units=1: the partition-function increment of every
             // growth-point set, in enumeration order
             if (kv.count("trace_units") && kv["trace_units"] == "1") {

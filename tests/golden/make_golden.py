@@ -89,6 +89,9 @@ ENUM_OPTS = {"e8s3_enumeration": {"max_total_staples": 3},
              "c1full3_enumeration": {"enumerate_staples_only": "false", "max_total_staples": 3}}
 # enumerations recorded with the partition sum of every growth-point set
 ENUM_UNITS = {"e8_enumeration", "c1full_enumeration", "c1full3_enumeration"}
+# full enumerations recorded also with every bin summed without rounding drift
+# (the reference's weights, compensated sums; ref_trace.cpp's exact_bins)
+ENUM_EXACT = {"c1full_enumeration", "c1full3_enumeration"}
 
 
 def enumerate_case(tmp, name, case):
@@ -106,6 +109,8 @@ def enumerate_case(tmp, name, case):
         f.write("trace_mode=enumerate\n")
         if name in ENUM_UNITS:
             f.write("trace_units=1\n")
+        if name in ENUM_EXACT:
+            f.write("trace_exact_bins=1\n")
     out = subprocess.run([REF, inp], capture_output=True, text=True, cwd=tmp, check=True).stdout
     d = json.loads([x for x in out.splitlines() if x.startswith("@@")][-1][2:])
     path = os.path.join(HERE, name + ".json")
@@ -113,7 +118,8 @@ def enumerate_case(tmp, name, case):
         json.dump({"case": case, "ops": ["numstaples", "numfulldomains"], "options": ENUM_OPTS.get(name, {}),
                    "weights": d["weights"], "num_configs": d["num_configs"],
                    **({"units": d["units"]} if "units" in d else {}),
-                   **({"unit_energy_drift": d["unit_energy_drift"]} if "unit_energy_drift" in d else {})},
+                   **({"unit_energy_drift": d["unit_energy_drift"]} if "unit_energy_drift" in d else {}),
+                   **({k: d[k] for k in ("weights_exact", "bin_configs", "saved_configs") if k in d})},
                   f, sort_keys=True)
     print(path, d["weights"], "%.1f s" % d["seconds"])
 

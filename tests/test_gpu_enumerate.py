@@ -63,16 +63,21 @@ def test_enumeration_units_match_reference(data_dir):
 def test_full_enumeration_matches_reference(name, max_total, split, data_dir):
     """The full conformational enumeration (the scaffold enumerated too,
     ConformationalEnumerator::enumerate) of the 4-domain system with up to
-    two and three staples, against the reference's own at full precision,
-    whole and split into 6^split parts per unit.
+    two and three staples, against the reference's own, whole and split into
+    6^split parts per unit.
 
-    The reference carries one running energy (long double) through the whole
-    enumeration, some 1e12 balanced sets and unassignments; the rounding of
-    each leaves a drift, recorded per unit by the trace driver
-    (unit_energy_drift).  A configuration's weight exp(-E) then carries the
-    drift accumulated before it as a relative error, so the weights are
-    compared at 1e-10 plus twice the largest accumulated drift.  The engine
-    restarts the energy at every unit and sums it without drift."""
+    The reference adds every configuration's weight to its bin of
+    m_state_weights, a running double sum (src/enumerate.cpp:658), over up to
+    1e8 configurations per bin; those roundings move a bin by up to (n - 1) u
+    relative (n configurations, u = 2^-53; recursive summation's bound,
+    Higham, Accuracy and Stability of Numerical Algorithms, 2nd ed., eq.
+    4.4), 3e-9 on the ≤3-staple system's smallest bins.  The trace driver
+    therefore also sums the reference's own weights, configuration by
+    configuration, without that drift (weights_exact: compensated sums,
+    oracle/ref/ref_trace.cpp).  The engine's bins (compensated sums of its
+    weights) match those at 1e-12, and the reference's printed weights lie
+    within the running-sum bound of them.  The reference's running energy
+    m_energy (long double) has no drift over a unit (unit_energy_drift)."""
     import numpy as np
     from latticednaorigami_gb300 import Engine
     path = os.path.join(GOLDEN, name + ".json")
@@ -86,11 +91,18 @@ def test_full_enumeration_matches_reference(name, max_total, split, data_dir):
     drift = np.array(fx.get("unit_energy_drift", [0.0]))
     offset = np.concatenate([[0.0], np.cumsum(drift)])
     bound = float(np.max(np.abs(offset[:-1]) + np.abs(drift)))
-    rtol = 1e-10 + 2 * bound
-    assert set(w) == set(fx["weights"]), (sorted(w), sorted(fx["weights"]))
-    for k, v in fx["weights"].items():
+    rtol = 1e-12 + 2 * bound
+    exact = fx["weights_exact"]
+    assert set(w) == set(fx["weights"]) == set(exact), (sorted(w), sorted(fx["weights"]))
+    u = 2.0 ** -53
+    for k, v in exact.items():
         assert abs(w[k] - v) <= rtol * v, (k, w[k], v, rtol)
-    assert abs(info["num_configs"] - fx["num_configs"]) <= 1e-9 * fx["num_configs"]
+        n = fx["bin_configs"][k]
+        # the bin's own running sum, the partition function's (long double,
+        # over every configuration), the roundings of the output
+        tol = max(n - 1, 1) * u + fx["saved_configs"] * 2.0 ** -64 + 4 * u
+        assert abs(fx["weights"][k] - v) <= tol * v, (k, fx["weights"][k], v, n)
+    assert abs(info["num_configs"] - fx["num_configs"]) <= 1e-12 * fx["num_configs"]
     if "units" in fx:
         units = eng.enumerate_units()
         ref = np.array(fx["units"])

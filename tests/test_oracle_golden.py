@@ -131,3 +131,32 @@ def test_reference_energy_drift_under_linker_moves():
     assert drift["l24a_s13"] > 1e-12 and drift["l24r_s16"] > 1e-12, drift
     assert drift["s24a_s3"] < 2e-13 and drift["g24a_s3"] < 2e-13, drift
     assert max(drift.values()) < 2e-11, drift
+
+
+@pytest.mark.parametrize("name", ["c1full_enumeration", "c1full3_enumeration"])
+def test_reference_enumeration_bins_carry_running_sum_rounding(name):
+    """The reference sums each bin of its full enumeration as a running double
+    (m_state_weights, src/enumerate.cpp:658), each partition-function term as
+    a running long double (:651).  The fixtures hold, besides the weights it
+    prints, the same weights summed by the trace driver without rounding drift
+    (weights_exact, compensated sums) and the configurations saved into each
+    bin.  The printed weights lie within recursive summation's error bound of
+    the drift-free ones ((n - 1) u for n terms, Higham, Accuracy and Stability
+    of Numerical Algorithms, 2nd ed., eq. 4.4), and do differ from them: the
+    differences the engine's compensated bins show against the printed
+    weights are the reference's summation, not its weights."""
+    path = os.path.join(GOLDEN, name + ".json")
+    with open(path) as f:
+        fx = json.load(f)
+    u = 2.0 ** -53
+    ex, pr, n = fx["weights_exact"], fx["weights"], fx["bin_configs"]
+    assert set(ex) == set(pr) == set(n)
+    assert sum(n.values()) == fx["saved_configs"]
+    assert abs(sum(ex.values()) - 1.0) < 1e-15
+    worst = 0.0
+    for k, v in ex.items():
+        tol = max(n[k] - 1, 1) * u + fx["saved_configs"] * 2.0 ** -64 + 4 * u
+        rel = abs(pr[k] - v) / v
+        assert rel <= tol, (k, pr[k], v, n[k])
+        worst = max(worst, rel)
+    assert worst > 1e-11   # the running sums' roundings are visible
