@@ -10,6 +10,7 @@
 #include <functional>
 #include <map>
 #include <memory>
+#include <set>
 #include <sstream>
 #include <string>
 #include <iterator>
@@ -454,7 +455,12 @@ struct EnumBuilder {
     vector<vector<DRef>> usd_nm;                       // no misbinding: per staple identity
     std::map<DRef, DRef> gmap;                         // m_growthpoints
     vector<GP> gp;                                     // m_growthpoints of the growth-point enumerator
-    vector<vector<GP>> enumerated;
+    // m_enumerated_growthpoints, each set sorted.  The reference tests a new
+    // set against every enumerated one of its size for containment; the
+    // growth points of one set are distinct (each old domain is taken out of
+    // the candidates while it is in use), so containment at equal size is
+    // set equality, looked up here in logarithmic time
+    std::set<vector<GP>> enumerated;
 
     EnumBuilder(const vector<vector<int>>& identities, bool mis, size_t cap)
         : ids(identities), S((int)identities.size() - 1), misbinding(mis), max_units(cap) {
@@ -486,19 +492,12 @@ struct EnumBuilder {
         units.push_back(u);
     }
 
-    bool repeated() const {   // growthpoints_repeated (:944, :1046)
-        for (auto& e : enumerated) {
-            if (e.size() != gp.size()) continue;
-            bool all = true;
-            for (auto& g : e)
-                if (std::find(gp.begin(), gp.end(), g) == gp.end()) {
-                    all = false;
-                    break;
-                }
-            if (all) return true;
-        }
-        return false;
+    vector<GP> sorted_gp() const {
+        vector<GP> key(gp);
+        std::sort(key.begin(), key.end());
+        return key;
     }
+    bool repeated() const { return enumerated.count(sorted_gp()) != 0; }   // growthpoints_repeated (:944, :1046)
 
     void recurse_or_enumerate(int ident, int d_i, DRef old) {
         int L = (int)ids[ident].size();
@@ -518,7 +517,7 @@ struct EnumBuilder {
         }
         else if (!repeated()) {
             emit();
-            enumerated.push_back(gp);
+            enumerated.insert(sorted_gp());
         }
         // remove_growthpoint (:336)
         DRef nw = gmap[old];

@@ -81,10 +81,12 @@ def flatten(chains):
 # exact enumerations: fixture name, case (the 4-domain system, whose staples
 # never bind both domains; the capped 8-domain system, where they do)
 ENUMERATIONS = [("c1_enumeration", "c1"), ("e8_enumeration", "e8"), ("e8s3_enumeration", "e8"),
+                # every staple set of the 8-domain system (38 min on one core)
+                ("e8s4_enumeration", "e8"),
                 # the full conformational enumeration (scaffold enumerated too, src/enumerate.cpp:218)
                 ("c1full_enumeration", "c1"), ("c1full3_enumeration", "c1")]
 # extra .inp options of an enumeration (defaults: the case's own)
-ENUM_OPTS = {"e8s3_enumeration": {"max_total_staples": 3},
+ENUM_OPTS = {"e8s3_enumeration": {"max_total_staples": 3}, "e8s4_enumeration": {"max_total_staples": 4},
              "c1full_enumeration": {"enumerate_staples_only": "false", "max_total_staples": 2},
              "c1full3_enumeration": {"enumerate_staples_only": "false", "max_total_staples": 3}}
 # enumerations recorded with the partition sum of every growth-point set

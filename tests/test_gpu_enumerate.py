@@ -1,10 +1,11 @@
 """Exact staple-only enumeration on the GPU (ldo_enumerate, csrc/ldo_enum.cuh)
 against the reference's own enumerator (src/enumerate.cpp, golden weights at
 full precision from tests/golden/make_golden.py): the 4-domain system with up
-to four staples and the 8-domain system with up to two and up to three
-(max_total_staples raised to 3 as in the fixture), where staples bind both
-of their domains.  The reference sums its weights in long double, the
-engine in FP64: weights agree to 1e-10 relative."""
+to four staples and the 8-domain system with up to two, three and four
+staples (max_total_staples raised as in the fixtures; four is every staple
+set, 38 min for the reference on one core, 0.6 s of GPU time), where staples
+bind both of their domains.  The reference sums its weights in long double,
+the engine in FP64 with compensated sums: weights agree to 1e-10 relative."""
 import json
 import os
 
@@ -17,7 +18,8 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("name,case,max_total,max_type", [("c1_enumeration", "c1", 4, 4),
                                                           ("e8_enumeration", "e8", 2, 1),
-                                                          ("e8s3_enumeration", "e8", 3, 1)])
+                                                          ("e8s3_enumeration", "e8", 3, 1),
+                                                          ("e8s4_enumeration", "e8", 4, 1)])
 def test_enumeration_matches_reference(name, case, max_total, max_type, data_dir):
     from latticednaorigami_gb300 import Engine
     with open(os.path.join(GOLDEN, name + ".json")) as f:
@@ -113,3 +115,56 @@ def test_full_enumeration_matches_reference(name, max_total, split, data_dir):
         tol = 1e-10 * np.abs(ref[:, 0]) + np.maximum(ref[:, 1], 1.0) * ulp
         bad = np.abs(units[:, 0] - ref[:, 0]) > tol
         assert not bad.any(), (np.flatnonzero(bad)[:10], units[bad][:5], ref[bad][:5])
+
+
+def _chi2_against(weights, samples):
+    """Chi-square p-value of (numstaples, numfulldomains) samples against
+    normalised weights, with the bins of fewer than 5 expected samples merged."""
+    from test_gpu_pt_and_stats import chi2_sf
+    counts = {}
+    for s in samples:
+        counts[s] = counts.get(s, 0) + 1
+    total = len(samples)
+    assert all(k in weights for k in counts), sorted(set(counts) - set(weights))
+    keys = sorted(weights, key=lambda k: -weights[k])
+    bins = [k for k in keys if weights[k] * total >= 5]
+    tail = [k for k in keys if k not in bins]
+    obs = [counts.get(k, 0) for k in bins] + [sum(counts.get(k, 0) for k in tail)]
+    exp = [weights[k] * total for k in bins] + [sum(weights[k] for k in tail) * total]
+    if exp[-1] < 5:
+        obs[-2] += obs[-1]
+        exp[-2] += exp[-1]
+        obs, exp = obs[:-1], exp[:-1]
+    chi2 = sum((o - e) ** 2 / e for o, e in zip(obs, exp))
+    return chi2_sf(chi2, len(obs) - 1), obs, exp
+
+
+@pytest.mark.parametrize("moves", ["plain", "learned"])
+def test_mc_samples_enumeration_of_every_staple_set(moves, data_dir):
+    """The 8-domain system with every staple set (up to four staples, one per
+    type; the reference's enumeration of it, 38 min on one core, is the
+    fixture): the engine's MC with the plain moveset, and with the learned
+    exchange and regrowth driven by a strongly non-uniform random weight
+    table, samples its distribution (chi-square p > 0.01)."""
+    import tempfile
+
+    import numpy as np
+    from latticednaorigami_gb300 import Engine
+    from test_learned_oracle import learn_ref, learned_moves
+
+    with open(os.path.join(GOLDEN, "e8s4_enumeration.json")) as f:
+        w4 = json.load(f)["weights"]
+    over = "max_total_staples = 4"
+    if moves == "learned":
+        over += "\nmovetype_file = %s" % learned_moves(tempfile.mkdtemp(), regrowth=True)
+    n_rep, burn, gap, snaps = 2048, 40000, 20000, 4
+    mc = Engine(os.path.join(data_dir, "e8.inp"), n_replicas=n_rep, seed=4242, overrides=over)
+    if moves == "learned":
+        mc.learn_set_table(np.exp(np.random.default_rng(21).normal(0.0, 2.0, learn_ref.TABLE)))
+    mc.run(burn)
+    samples = []
+    for _ in range(snaps):
+        mc.run(gap)
+        samples += ["%d %d" % (o["num_staples"], o["num_fully_bound"]) for o in mc.observables()]
+    p, obs, exp = _chi2_against(w4, samples)
+    assert p > 0.01, (obs, exp, p)
