@@ -49,6 +49,8 @@ __global__ void __launch_bounds__(32) ldo_enum_kernel(LdoEnumLaunch E) {
     W->sumE = 0;
     W->part_c = 0;
     W->sumE_c = 0;
+    // E.hist holds 2 x n1 x n2 doubles per part: the part's weights, then
+    // the compensations of their sums, folded into the weights at the end
     W->row = E.hist + (size_t)b * 2 * E.n1 * E.n2;
     for (int k = 0; k < 2 * E.n1 * E.n2; ++k) W->row[k] = 0;
     W->op1 = E.op1;

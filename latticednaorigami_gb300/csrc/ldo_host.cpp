@@ -2303,7 +2303,7 @@ struct ldo_engine {
         DevBuf<unsigned char> d_work;
         d_work.alloc(nb * stride);
         DevBuf<double> d_hist, d_stats;
-        d_hist.alloc(nb * 2 * n1 * n2);
+        d_hist.alloc(nb * 2 * n1 * n2);   // per part: weights, then the compensations of their sums
         d_stats.alloc(nb * 4);
         LdoEnumLaunch E {};
         E.L = launch_params(LDO_MODE_RUN, 0);

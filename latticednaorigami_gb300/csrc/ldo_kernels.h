@@ -148,8 +148,7 @@ struct LdoEnumLaunch {
     int split;                    // each unit runs as 6^split parts, one per branch of its first choice levels
     unsigned char* work;          // per part: recursion state (ldo_enum_work_bytes)
     size_t work_stride;
-    double* hist;                 // per part: n1 x n2 weights over (op1, op2), then n1 x n2 scratch
-                                  // (the compensations of the sums, folded in when the part ends)
+    double* hist;                 // per part: n1 x n2 weights over (op1, op2)
     double* stats;                // per part: partition sum, configurations, sum of E w, status
     int op1, op2, n1, n2;
     int overcount;                // 0 MaxTwoDomain, 1 MisbindingOnly

@@ -51,7 +51,9 @@ RUNS = [("c1", 1, 20000), ("c1", 2, 20000), ("g24a", 3, 20000), ("g24b", 4, 2000
         # Dist / AdjacentSite order parameters with biases, on a moving scaffold
         ("d24", 12, 20000),
         # scaffold transforms with linker regrowth (CTCB, clustered CTCB, CTRG)
-        ("l24a", 13, 20000), ("l24b", 14, 20000), ("l24c", 18, 20000), ("l24r", 16, 20000)]
+        ("l24a", 13, 20000), ("l24b", 14, 20000), ("l24c", 18, 20000), ("l24r", 16, 20000),
+        # three-domain staples with misbinding disallowed
+        ("m8", 19, 20000)]
 
 
 def ref_trace(inp, seed, steps, replica=0):
@@ -83,6 +85,9 @@ def flatten(chains):
 ENUMERATIONS = [("c1_enumeration", "c1"), ("e8_enumeration", "e8"), ("e8s3_enumeration", "e8"),
                 # every staple set of the 8-domain system (38 min on one core)
                 ("e8s4_enumeration", "e8"),
+                # three-domain staples, misbinding disallowed: the no-misbinding
+                # growth-point enumerator and the misbinding-only overcount
+                ("m8_enumeration", "m8"),
                 # the full conformational enumeration (scaffold enumerated too, src/enumerate.cpp:218)
                 ("c1full_enumeration", "c1"), ("c1full3_enumeration", "c1")]
 # extra .inp options of an enumeration (defaults: the case's own)
@@ -90,7 +95,7 @@ ENUM_OPTS = {"e8s3_enumeration": {"max_total_staples": 3}, "e8s4_enumeration": {
              "c1full_enumeration": {"enumerate_staples_only": "false", "max_total_staples": 2},
              "c1full3_enumeration": {"enumerate_staples_only": "false", "max_total_staples": 3}}
 # enumerations recorded with the partition sum of every growth-point set
-ENUM_UNITS = {"e8_enumeration", "c1full_enumeration", "c1full3_enumeration"}
+ENUM_UNITS = {"e8_enumeration", "m8_enumeration", "c1full_enumeration", "c1full3_enumeration"}
 # full enumerations recorded also with every bin summed without rounding drift
 # (the reference's weights, compensated sums; ref_trace.cpp's exact_bins)
 ENUM_EXACT = {"c1full_enumeration", "c1full3_enumeration"}

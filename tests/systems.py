@@ -95,7 +95,7 @@ def ring(n):
     return pos
 
 
-def make_system(n, pairs, seed, positions, seq_len=16, cyclic=False):
+def make_system(n, pairs, seed, positions, seq_len=16, cyclic=False, orientations=None):
     rng = random.Random(seed)
     scaf_seq = ["".join(rng.choice("ACGT") for _ in range(seq_len)) for _ in range(n)]
     idents = [[i + 1 for i in range(n)]]
@@ -110,7 +110,7 @@ def make_system(n, pairs, seed, positions, seq_len=16, cyclic=False):
         "configurations": [{"step": 0, "chains": [{
             "index": 0, "identity": 0,
             "positions": positions,
-            "orientations": [[0, 0, 1]] * n}]}]}}
+            "orientations": orientations or [[0, 0, 1]] * n}]}]}}
 
 
 MOVES = {
@@ -296,6 +296,11 @@ CASES = {
     # states with one fully and one partly bound staple (or one staple)
     "e8": ("grid8", "met3", dict(stacking_ene=-1000, staple_M=1e-4, temp=355, max_total_staples=2,
                                  max_type_staples=1)),
+    # three-domain staples with misbinding disallowed: the other growth-point
+    # enumerator (no misbinding) and overcount calculator (misbinding only)
+    # of the reference's exact enumeration
+    "m8": ("mixed8", "met3", dict(misbinding_pot="Disallowed", max_staple_size=3, stacking_ene=-1000,
+                                  staple_M=1e-4, temp=345, max_total_staples=3, max_type_staples=1)),
     # the 48-domain system's shape with the reference's standard moveset
     "s48": ("grid48", "ctrg", dict(stacking_ene=-1000, staple_M=1e-4, temp=335, max_total_staples=48,
                                    max_type_staples=2)),
@@ -309,6 +314,12 @@ def system_for(name):
     if name.startswith("ring"):
         n = int(name[4:])
         return make_system(n, linear_pairs(n), seed=n + 1, positions=ring(n), cyclic=True)
+    if name == "mixed8":
+        # two rows of four: two three-domain staple types (a crossover and a
+        # helix neighbour each) and a two-domain helix type, 8 bp domains,
+        # scaffold orientations turning by a half turn per domain
+        return make_system(8, staple_groups_mixed(8, 1), seed=808, positions=serpentine(8, 4), seq_len=8,
+                           orientations=[[0, 0, 1 - 2 * (i % 2)] for i in range(8)])
     if name == "mixed96":
         # the 96-domain design: 16 three-domain and 24 two-domain staple types, 8 bp domains
         return make_system(96, staple_groups_mixed(96, 8), seed=96, positions=serpentine(96, 4), seq_len=8)

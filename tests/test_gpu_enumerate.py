@@ -19,7 +19,8 @@ pytestmark = pytest.mark.gpu
 @pytest.mark.parametrize("name,case,max_total,max_type", [("c1_enumeration", "c1", 4, 4),
                                                           ("e8_enumeration", "e8", 2, 1),
                                                           ("e8s3_enumeration", "e8", 3, 1),
-                                                          ("e8s4_enumeration", "e8", 4, 1)])
+                                                          ("e8s4_enumeration", "e8", 4, 1),
+                                                          ("m8_enumeration", "m8", 3, 1)])
 def test_enumeration_matches_reference(name, case, max_total, max_type, data_dir):
     from latticednaorigami_gb300 import Engine
     with open(os.path.join(GOLDEN, name + ".json")) as f:
@@ -33,7 +34,8 @@ def test_enumeration_matches_reference(name, case, max_total, max_type, data_dir
     assert abs(info["num_configs"] - fx["num_configs"]) <= 1e-9 * fx["num_configs"]
 
 
-def test_enumeration_units_match_reference(data_dir):
+@pytest.mark.parametrize("name,case,max_total", [("e8_enumeration", "e8", 2), ("m8_enumeration", "m8", 3)])
+def test_enumeration_units_match_reference(name, case, max_total, data_dir):
     """Unit by unit: the growth-point sets in the reference's order, each
     with its partition-function sum and number of configurations.
 
@@ -45,10 +47,10 @@ def test_enumeration_units_match_reference(data_dir):
     per configuration); the engine sums each unit from zero in FP64."""
     import numpy as np
     from latticednaorigami_gb300 import Engine
-    with open(os.path.join(GOLDEN, "e8_enumeration.json")) as f:
+    with open(os.path.join(GOLDEN, name + ".json")) as f:
         fx = json.load(f)
-    eng = Engine(os.path.join(data_dir, "e8.inp"), n_replicas=1, seed=0)
-    eng.enumerate(0, 2, 1)
+    eng = Engine(os.path.join(data_dir, case + ".inp"), n_replicas=1, seed=0)
+    eng.enumerate(0, max_total, 1)
     units = eng.enumerate_units()
     ref = np.array(fx["units"])
     assert units.shape == ref.shape
@@ -139,26 +141,29 @@ def _chi2_against(weights, samples):
     return chi2_sf(chi2, len(obs) - 1), obs, exp
 
 
-@pytest.mark.parametrize("moves", ["plain", "learned"])
-def test_mc_samples_enumeration_of_every_staple_set(moves, data_dir):
-    """The 8-domain system with every staple set (up to four staples, one per
-    type; the reference's enumeration of it, 38 min on one core, is the
-    fixture): the engine's MC with the plain moveset, and with the learned
-    exchange and regrowth driven by a strongly non-uniform random weight
-    table, samples its distribution (chi-square p > 0.01)."""
+def _mc_samples(inp, over, moves, seed, cb=True):
+    """(numstaples, numfulldomains) of 2048 replicas at 4 snapshots 20000
+    steps apart after 40000 steps: the plain moveset (Met exchange, Met
+    regrowth) or the learned exchange and regrowth with a strongly
+    non-uniform random weight table, each with CB staple regrowth if cb."""
     import tempfile
 
     import numpy as np
     from latticednaorigami_gb300 import Engine
-    from test_learned_oracle import learn_ref, learned_moves
-
-    with open(os.path.join(GOLDEN, "e8s4_enumeration.json")) as f:
-        w4 = json.load(f)["weights"]
-    over = "max_total_staples = 4"
-    if moves == "learned":
-        over += "\nmovetype_file = %s" % learned_moves(tempfile.mkdtemp(), regrowth=True)
+    from test_learned_oracle import learn_ref
+    kinds = {"plain": [("Met staple exchange", "MetStapleExchange"), ("Met staple regrowth", "MetStapleRegrowth")],
+             "learned": [("Learned staple exchange", "LearnedStapleExchange"),
+                         ("Learned staple regrowth", "LearnedStapleRegrowth")]}[moves]
+    if cb:
+        kinds = kinds + [("CB staple regrowth", "CBStapleRegrowth")]
+    mv = {"origami": {"movetypes": [{"label": l, "type": t, "freq": "1/%d" % len(kinds), "adaptive_exchange": False}
+                                    for l, t in kinds]}}
+    path = os.path.join(tempfile.mkdtemp(), "moves.json")
+    with open(path, "w") as f:
+        json.dump(mv, f)
+    over = "\n".join(x for x in (over, "movetype_file = %s" % path) if x)
     n_rep, burn, gap, snaps = 2048, 40000, 20000, 4
-    mc = Engine(os.path.join(data_dir, "e8.inp"), n_replicas=n_rep, seed=4242, overrides=over)
+    mc = Engine(inp, n_replicas=n_rep, seed=seed, overrides=over)
     if moves == "learned":
         mc.learn_set_table(np.exp(np.random.default_rng(21).normal(0.0, 2.0, learn_ref.TABLE)))
     mc.run(burn)
@@ -166,5 +171,54 @@ def test_mc_samples_enumeration_of_every_staple_set(moves, data_dir):
     for _ in range(snaps):
         mc.run(gap)
         samples += ["%d %d" % (o["num_staples"], o["num_fully_bound"]) for o in mc.observables()]
+    return samples
+
+
+@pytest.mark.parametrize("moves", ["plain", "learned"])
+def test_mc_samples_enumeration_of_every_staple_set(moves, data_dir):
+    """Every staple set of the 8-domain system (up to four staples, one per
+    type; the reference's enumeration of it, 38 min on one core, is the
+    fixture): the engine's MC with the plain moveset, and with the learned
+    exchange and regrowth driven by a strongly non-uniform random weight
+    table, samples its distribution (chi-square p > 0.01)."""
+    with open(os.path.join(GOLDEN, "e8s4_enumeration.json")) as f:
+        w4 = json.load(f)["weights"]
+    samples = _mc_samples(os.path.join(data_dir, "e8.inp"), "max_total_staples = 4", moves, 4242)
     p, obs, exp = _chi2_against(w4, samples)
     assert p > 0.01, (obs, exp, p)
+
+
+def test_learned_and_met_moves_agree_with_three_domain_staples(data_dir):
+    """Three-domain staples with misbinding disallowed (m8): the learned
+    exchange and regrowth sample the distribution of the reference's Met
+    exchange and regrowth (two-sample chi-square p > 0.01).  Without CB
+    staple regrowth: on this system the reference's CBStapleRegrowth moves
+    the distribution away from the one its Met moves sample (all three
+    staples bound 0.113 of the samples with it, 0.081 without; CPU
+    restatement, which follows the reference's trace m8_s19 step for step),
+    and the reference's staple-only enumeration (misbinding-only overcount)
+    gives a third (0.133), which the engine's enumerator reproduces
+    (test_enumeration_matches_reference)."""
+    from test_gpu_pt_and_stats import chi2_sf
+    inp = os.path.join(data_dir, "m8.inp")
+    a = _mc_samples(inp, "", "plain", 4242, cb=False)
+    b = _mc_samples(inp, "", "learned", 4343, cb=False)
+    keys = sorted(set(a) | set(b))
+    ca = [a.count(k) for k in keys]
+    cb = [b.count(k) for k in keys]
+    # merge bins with fewer than 10 samples in all into one
+    small = [i for i in range(len(keys)) if ca[i] + cb[i] < 10]
+    big = [i for i in range(len(keys)) if i not in small]
+    ca = [ca[i] for i in big] + ([sum(ca[i] for i in small)] if small else [])
+    cb = [cb[i] for i in big] + ([sum(cb[i] for i in small)] if small else [])
+    if small and ca[-1] + cb[-1] < 10:
+        ca[-2] += ca.pop()
+        cb[-2] += cb.pop()
+    na, nb = len(a), len(b)
+    chi2 = 0.0
+    for x, y in zip(ca, cb):
+        t = x + y
+        ex, ey = t * na / (na + nb), t * nb / (na + nb)
+        chi2 += (x - ex) ** 2 / ex + (y - ey) ** 2 / ey
+    p = chi2_sf(chi2, len(ca) - 1)
+    assert p > 0.01, (keys, ca, cb, p)

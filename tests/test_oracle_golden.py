@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN, golden_overrides, inp
-from oracle_lib import OracleReplica, run_golden
+from oracle_lib import OracleReplica, run_batch_states, run_golden
 
 FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "*.json.gz")))
 
@@ -160,3 +160,28 @@ def test_reference_enumeration_bins_carry_running_sum_rounding(name):
         assert rel <= tol, (k, pr[k], v, n[k])
         worst = max(worst, rel)
     assert worst > 1e-11   # the running sums' roundings are visible
+
+
+def test_reference_cb_regrowth_shifts_three_domain_staple_distribution(tmp_path):
+    """On m8 (two three-domain staple types and one two-domain type,
+    misbinding disallowed) the reference's moves do not all sample one
+    distribution: Met exchange with Met regrowth puts about 0.08 of the
+    samples in the state with all three staples bound, Met exchange with CB
+    staple regrowth about 0.11.  The CPU restatement that shows it follows
+    the reference's own trace of this system step for step (m8_s19), so this
+    is the reference's behaviour, which the engine keeps; its learned moves
+    are checked against the Met moves (tests/test_gpu_enumerate.py).  The
+    runs are seeded: the fractions are the same on every run."""
+    moves = {"mr": [("Met staple exchange", "MetStapleExchange"), ("Met staple regrowth", "MetStapleRegrowth")],
+             "cb": [("Met staple exchange", "MetStapleExchange"), ("CB staple regrowth", "CBStapleRegrowth")]}
+    frac = {}
+    for k, mv in moves.items():
+        path = tmp_path / ("moves_%s.json" % k)
+        path.write_text(json.dumps({"origami": {"movetypes": [
+            {"label": l, "type": t, "freq": "1/2", "adaptive_exchange": False} for l, t in mv]}}))
+        st = run_batch_states(inp("m8"), 31, 512, 30000, 15000, 4, os.cpu_count() or 1,
+                              overrides="movetype_file = %s" % path)
+        flat = st.reshape(-1, 2)
+        frac[k] = float(np.mean((flat[:, 0] == 3) & (flat[:, 1] == 6)))
+    assert 0.06 < frac["mr"] < 0.10, frac
+    assert frac["cb"] - frac["mr"] > 0.015, frac
