@@ -171,7 +171,10 @@ def test_reference_cb_regrowth_shifts_three_domain_staple_distribution(tmp_path)
     the reference's own trace of this system step for step (m8_s19), so this
     is the reference's behaviour, which the engine keeps; its learned moves
     are checked against the Met moves (tests/test_gpu_enumerate.py).  The
-    runs are seeded: the fractions are the same on every run."""
+    cause: the reference weighs the old configuration by regrowing it from a
+    growth point drawn again among its bound domains (src/cb_movetypes.cpp:
+    331-336) instead of the one the new configuration grew from.  The runs
+    are seeded: the fractions are the same on every run."""
     moves = {"mr": [("Met staple exchange", "MetStapleExchange"), ("Met staple regrowth", "MetStapleRegrowth")],
              "cb": [("Met staple exchange", "MetStapleExchange"), ("CB staple regrowth", "CBStapleRegrowth")]}
     frac = {}
