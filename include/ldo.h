@@ -301,6 +301,16 @@ ldo_status ldo_enumerate_unit_weights(ldo_engine* e, double* out, int64_t cap, i
  * only). */
 ldo_status ldo_enumerate_units(ldo_engine* e, double* out, int32_t cap, int32_t* n_units);
 
+/* The work units an enumeration of the system in inp_path (with overrides,
+ * as ldo_create takes them) would run, listed on the host without a GPU:
+ * StapleEnumerator::enumerate (src/enumerate.cpp:1082) over the staple sets
+ * and GrowthpointEnumerator::enumerate (:819) over the growth-point sets
+ * without repeats, in the reference's order.  out[2u] the number of staples
+ * of unit u, out[2u+1] its number of growth points (cap: room for 2 *
+ * n_units; NULL out: count only).  Error text via ldo_last_error(NULL). */
+ldo_status ldo_enumeration_plan(const char* inp_path, const char* overrides, int32_t min_total, int32_t max_total,
+                                int32_t max_type, int32_t* out, int32_t cap, int32_t* n_units);
+
 /* No counterpart in the reference: the engine's autotuner of the MC kernel's
  * launch shape (the reference runs one replica per MPI process and has no
  * launch shape).  Times probe_sweeps sweeps of this engine's own batch for

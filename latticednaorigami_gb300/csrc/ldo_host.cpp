@@ -2995,6 +2995,25 @@ ldo_status ldo_nn_duplex_thermo(const char* seq, double temp, double cation_M, d
     });
 }
 
+ldo_status ldo_enumeration_plan(const char* inp_path, const char* overrides, int32_t min_total, int32_t max_total,
+                                int32_t max_type, int32_t* out, int32_t cap, int32_t* n_units) {
+    if (!inp_path || !n_units || min_total < 0 || max_total < min_total || max_type < 1) return LDO_EINVAL;
+    return guard(nullptr, [&]() {
+        HostSystem hs = load_system(inp_path, overrides ? overrides : "");
+        if (hs.p.max_staple_size != 2 && hs.p.misbinding_pot != "Disallowed")
+            throw LdoError(LDO_EINVAL, "No enumerator available for system");
+        EnumBuilder b(hs.sf.identities, hs.p.misbinding_pot != "Disallowed", 1u << 22);
+        b.run(min_total, max_total, max_type);
+        *n_units = (int32_t)b.units.size();
+        if (!out) return;
+        if ((size_t)cap < 2 * b.units.size()) throw LdoError(LDO_EINVAL, "unit buffer too small");
+        for (size_t u = 0; u < b.units.size(); ++u) {
+            out[2 * u] = b.units[u].n_chains;
+            out[2 * u + 1] = b.units[u].n_gp;
+        }
+    });
+}
+
 ldo_status ldo_energy_tables(const char* inp_path, double temp, double stacking_mult, int* imax, double* hyb_e,
                              double* hyb_h, double* hyb_s, double* stack, double* init, int cap) {
     if (!inp_path || !imax) return LDO_EINVAL;

@@ -26,7 +26,7 @@ EXPORTS = [
     "ldo_set_bias_centre", "ldo_swap_writer_open", "ldo_set_config", "ldo_set_configs", "ldo_anneal_run", "ldo_read_trj_frame", "ldo_checkpoint_save",
     "ldo_checkpoint_load", "ldo_autotune", "ldo_autotune_candidates", "ldo_us_write_biases",
     "ldo_us_read_biases", "ldo_us_reset", "ldo_read_biases", "ldo_enumerate", "ldo_enumerate_full", "ldo_enumerate_units",
-    "ldo_enumerate_unit_weights",
+    "ldo_enumerate_unit_weights", "ldo_enumeration_plan",
     "ldo_batch_create", "ldo_batch_destroy", "ldo_batch_last_error", "ldo_batch_num_groups", "ldo_batch_group",
     "ldo_batch_set_controls", "ldo_batch_run", "ldo_batch_run_sweeps", "ldo_batch_set_sampling",
     "ldo_batch_get_samples", "ldo_batch_get_counters", "ldo_batch_autotune",
@@ -160,6 +160,8 @@ def load_library(path=None):
     lib.ldo_nn_duplex_thermo.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, dp, dp]
     lib.ldo_energy_tables.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
                                       dp, dp, dp, dp, dp, ip]
+    lib.ldo_enumeration_plan.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32,
+                                         ctypes.c_int32, i32p, ctypes.c_int32, i32p]
     if path is None:
         _lib = lib
     return lib
@@ -584,6 +586,24 @@ def energy_tables(inp, temp, stacking_mult=1.0):
     if rc != 0:
         raise LdoError(rc, lib.ldo_last_error(None).decode())
     return imax.value, [a.reshape(d, d) for a in arrs], init
+
+
+def enumeration_plan(inp, min_total, max_total, max_type, overrides=""):
+    """(staples, growth points) of every work unit an exact enumeration of
+    the .inp system runs, in the reference's order (ldo_enumeration_plan;
+    host only, no GPU)."""
+    lib = load_library()
+    n = ctypes.c_int32(0)
+    rc = lib.ldo_enumeration_plan(os.fsencode(inp), overrides.encode(), min_total, max_total, max_type, None, 0,
+                                  ctypes.byref(n))
+    if rc != 0:
+        raise LdoError(rc, lib.ldo_last_error(None).decode())
+    out = np.zeros(2 * n.value, np.int32)
+    rc = lib.ldo_enumeration_plan(os.fsencode(inp), overrides.encode(), min_total, max_total, max_type,
+                                  out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), out.size, ctypes.byref(n))
+    if rc != 0:
+        raise LdoError(rc, lib.ldo_last_error(None).decode())
+    return out.reshape(-1, 2)
 
 
 class Batch:
