@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(128) gemm_tn_kernel(const uint16_t* __restrict
         bool done = mbar_wait(bar, parity);
         parity ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        // one verdict for the whole CTA: a wait that ran out anywhere stops it
+        // one outcome for the whole CTA: a wait that ran out anywhere stops it
         ok = __syncthreads_and(done) != 0;
         if (!ok && threadIdx.x == 0) atomicExch(err, 1);
     }
