@@ -96,6 +96,8 @@ ENUM_OPTS = {"e8s3_enumeration": {"max_total_staples": 3}, "e8s4_enumeration": {
              "c1full3_enumeration": {"enumerate_staples_only": "false", "max_total_staples": 3}}
 # enumerations recorded with the partition sum of every growth-point set
 ENUM_UNITS = {"e8_enumeration", "m8_enumeration", "c1full_enumeration", "c1full3_enumeration"}
+# enumerations recorded with their number of growth-point sets only
+ENUM_UNIT_COUNT = {"c1_enumeration", "e8s3_enumeration", "e8s4_enumeration"}
 # full enumerations recorded also with every bin summed without rounding drift
 # (the reference's weights, compensated sums; ref_trace.cpp's exact_bins)
 ENUM_EXACT = {"c1full_enumeration", "c1full3_enumeration"}
@@ -114,7 +116,7 @@ def enumerate_case(tmp, name, case):
     inp = systems.write_case(tmp, case, extra=opts)
     with open(inp, "a") as f:
         f.write("trace_mode=enumerate\n")
-        if name in ENUM_UNITS:
+        if name in ENUM_UNITS or name in ENUM_UNIT_COUNT:
             f.write("trace_units=1\n")
         if name in ENUM_EXACT:
             f.write("trace_exact_bins=1\n")
@@ -124,7 +126,8 @@ def enumerate_case(tmp, name, case):
     with open(path, "w") as f:
         json.dump({"case": case, "ops": ["numstaples", "numfulldomains"], "options": ENUM_OPTS.get(name, {}),
                    "weights": d["weights"], "num_configs": d["num_configs"],
-                   **({"units": d["units"]} if "units" in d else {}),
+                   **({"units": d["units"]} if "units" in d and name in ENUM_UNITS else {}),
+                   **({"n_units": len(d["units"])} if "units" in d and name in ENUM_UNIT_COUNT else {}),
                    **({"unit_energy_drift": d["unit_energy_drift"]} if "unit_energy_drift" in d else {}),
                    **({k: d[k] for k in ("weights_exact", "bin_configs", "saved_configs") if k in d})},
                   f, sort_keys=True)

@@ -32,6 +32,23 @@ def test_units_match_the_reference_count(name, case, max_total, max_type):
     assert (plan[1:, 0] >= plan[:-1, 0]).all()
 
 
+@pytest.mark.parametrize("name,case,max_total,max_type", [("c1_enumeration", "c1", 4, 4),
+                                                          ("e8s3_enumeration", "e8", 3, 1),
+                                                          ("e8s4_enumeration", "e8", 4, 1)])
+def test_unit_count_matches_the_reference(name, case, max_total, max_type):
+    """The larger staple-only enumerations (the reference's unit count only):
+    up to 151 553 growth-point sets, each checked against those enumerated
+    before it."""
+    from latticednaorigami_gb300.engine import enumeration_plan
+    with open(os.path.join(GOLDEN, name + ".json")) as f:
+        fx = json.load(f)
+    if "n_units" not in fx:
+        pytest.skip("fixture without a unit count")
+    over = "\n".join("%s = %s" % kv for kv in sorted(fx["options"].items()))
+    plan = enumeration_plan(inp(case), 0, max_total, max_type, overrides=over)
+    assert len(plan) == fx["n_units"]
+
+
 def test_plan_refuses_a_system_without_an_enumerator(tmp_path):
     from latticednaorigami_gb300.engine import LdoError, enumeration_plan
     with pytest.raises(LdoError, match="No enumerator"):
