@@ -33,7 +33,8 @@ def engine(*a, **k):
     return Engine(*a, **k)
 
 
-@pytest.mark.parametrize("case,regrowth", [("c1", False), ("g24a", False), ("c1", True), ("g24a", True)])
+@pytest.mark.parametrize("case,regrowth", [("c1", False), ("g24a", False), ("c1", True), ("g24a", True),
+                                            ("m8", False), ("m8", True)])
 def test_learned_moves_match_oracle_per_step(case, regrowth):
     d = tempfile.mkdtemp()
     over = "movetype_file = %s" % learned_moves(d, regrowth)
